@@ -1,0 +1,1182 @@
+/*
+ * fem_oracle.cpp -- CPU oracle for the MORIS element hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py as the checker and as the timed host-core
+ * restatement.  The product library (moris_gb300/) never links or calls it.
+ *
+ * This file restates, routine by routine, the reference's algorithm on plain
+ * column-major dense matrices (the reference's LINALG Matrix<> is
+ * column-major too).  Paths are relative to the reference's projects/
+ * directory.  The restatement keeps the reference's formulation: dense
+ * B^T D B per Gauss point (CM_Struc_Linear), dense T^T K T per equation
+ * object (MSI::Equation_Object), sorted per-type adof lists, |T| <= 1e-12
+ * dropped per node (HMR T_Matrix_Base::evaluate).
+ *
+ * Parity pins: the Gauss tables and Lagrange shape functions are checked
+ * against the reference's own fixture files (FEM/INT/test/data/ .bin files), the
+ * element Jacobians against central finite differences of the residual as in
+ * the reference's IWG unit tests, and the B-spline extraction against the
+ * partition-of-unity checks of HMR/test/ut_HMR_T_Matrix.cpp.
+ */
+#include "fem_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <thread>
+#include <vector>
+
+namespace {
+
+using real = double;
+
+/* ------------------------------------------------------------------------ */
+/* minimal column-major dense matrix (the reference's Matrix<DDRMat> layout) */
+struct Mat {
+    int r = 0, c = 0;
+    std::vector<real> a;
+    Mat() = default;
+    Mat(int rr, int cc, real v = 0.0) : r(rr), c(cc), a((size_t)rr * cc, v) {}
+    real& operator()(int i, int j) { return a[(size_t)i + (size_t)j * r]; }
+    real operator()(int i, int j) const { return a[(size_t)i + (size_t)j * r]; }
+    void fill(real v) { std::fill(a.begin(), a.end(), v); }
+};
+
+Mat mul(const Mat& A, const Mat& B) {
+    Mat C(A.r, B.c, 0.0);
+    for (int j = 0; j < B.c; ++j)
+        for (int k = 0; k < A.c; ++k) {
+            const real b = B(k, j);
+            if (b == 0.0) continue;
+            for (int i = 0; i < A.r; ++i) C(i, j) += A(i, k) * b;
+        }
+    return C;
+}
+Mat trans(const Mat& A) {
+    Mat T(A.c, A.r);
+    for (int i = 0; i < A.r; ++i)
+        for (int j = 0; j < A.c; ++j) T(j, i) = A(i, j);
+    return T;
+}
+void add_scaled(Mat& Y, real s, const Mat& X) {
+    for (size_t i = 0; i < Y.a.size(); ++i) Y.a[i] += s * X.a[i];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Gauss tables.  Values and point order are those of the reference's
+   MTK/src/integration/cl_MTK_Integration_Coeffs_*.hpp (15-digit literals,
+   HEX_3x3x3 in its layer-wise corner/edge/centre order, TET_11 weights
+   multiplied by 6 as in cl_MTK_Integration_Coeffs_Tet_11.hpp:117).         */
+struct RuleTab {
+    int dim, n;
+    std::vector<real> pts;  // dim x n column-major
+    std::vector<real> w;
+};
+
+RuleTab make_rule(int rule) {
+    RuleTab t;
+    const real g2 = 0.577350269189626;   // Quad_2x2 / Hex_2x2x2 literal
+    const real g3 = 0.774596669241483;   // Hex_3x3x3 literal
+    switch (rule) {
+        case ORC_RULE_BAR_1:  // cl_MTK_Integration_Coeffs_Bar_1.hpp:50-63
+            t.dim = 1; t.n = 1; t.pts = {0.0}; t.w = {2.0};
+            break;
+        case ORC_RULE_BAR_3:  // cl_MTK_Integration_Coeffs_Bar_3.hpp
+            t.dim = 1; t.n = 3;
+            t.pts = {-0.7745966692414834, 0.000000000000000, 0.7745966692414834};
+            t.w = {5.555555555555556e-01, 8.888888888888888e-01, 5.555555555555556e-01};
+            break;
+        case ORC_RULE_QUAD_2x2: {  // cl_MTK_Integration_Coeffs_Quad_2x2.hpp
+            t.dim = 2; t.n = 4;
+            const real x[4] = {-g2, g2, g2, -g2}, y[4] = {-g2, -g2, g2, g2};
+            for (int k = 0; k < 4; ++k) { t.pts.push_back(x[k]); t.pts.push_back(y[k]); }
+            t.w = {1.0, 1.0, 1.0, 1.0};
+            break;
+        }
+        case ORC_RULE_HEX_2x2x2: {  // cl_MTK_Integration_Coeffs_Hex_2x2x2.hpp:50-76
+            t.dim = 3; t.n = 8;
+            const real x[8] = {-g2, g2, g2, -g2, -g2, g2, g2, -g2};
+            const real y[8] = {-g2, -g2, g2, g2, -g2, -g2, g2, g2};
+            const real z[8] = {-g2, -g2, -g2, -g2, g2, g2, g2, g2};
+            for (int k = 0; k < 8; ++k) { t.pts.push_back(x[k]); t.pts.push_back(y[k]); t.pts.push_back(z[k]); }
+            t.w.assign(8, 1.0);
+            break;
+        }
+        case ORC_RULE_HEX_3x3x3: {  // cl_MTK_Integration_Coeffs_Hex_3x3x3.hpp:50+
+            t.dim = 3; t.n = 27;
+            // per z-layer: 4 corners, 4 edge mid-points, centre (hex27 node order)
+            const real lx[9] = {-g3, g3, g3, -g3, 0.0, g3, 0.0, -g3, 0.0};
+            const real ly[9] = {-g3, -g3, g3, g3, -g3, 0.0, g3, 0.0, 0.0};
+            const real lz[3] = {-g3, 0.0, g3};
+            const real wo[9] = {0.171467764060357, 0.171467764060357, 0.171467764060357, 0.171467764060357,
+                                0.274348422496571, 0.274348422496571, 0.274348422496571, 0.274348422496571,
+                                0.438957475994513};
+            const real wm[9] = {0.274348422496571, 0.274348422496571, 0.274348422496571, 0.274348422496571,
+                                0.438957475994513, 0.438957475994513, 0.438957475994513, 0.438957475994513,
+                                0.702331961591221};
+            for (int l = 0; l < 3; ++l)
+                for (int k = 0; k < 9; ++k) {
+                    t.pts.push_back(lx[k]); t.pts.push_back(ly[k]); t.pts.push_back(lz[l]);
+                    t.w.push_back(l == 1 ? wm[k] : wo[k]);
+                }
+            break;
+        }
+        case ORC_RULE_TRI_3:  // cl_MTK_Integration_Coeffs_Tri_3.hpp
+            t.dim = 2; t.n = 3;
+            t.pts = {0.666666666666667, 0.166666666666667, 0.166666666666667, 0.666666666666667,
+                     0.166666666666667, 0.166666666666667};
+            t.w = {0.333333333333333, 0.333333333333333, 0.333333333333333};
+            break;
+        case ORC_RULE_TRI_7: {  // cl_MTK_Integration_Coeffs_Tri_7.hpp
+            t.dim = 2; t.n = 7;
+            const real x[7] = {0.333333333333333, 0.797426985353087, 0.101286507323456, 0.101286507323456,
+                               0.059715871789770, 0.470142064105115, 0.470142064105115};
+            const real y[7] = {0.333333333333333, 0.101286507323456, 0.797426985353087, 0.101286507323456,
+                               0.470142064105115, 0.059715871789770, 0.470142064105115};
+            for (int k = 0; k < 7; ++k) { t.pts.push_back(x[k]); t.pts.push_back(y[k]); }
+            t.w = {0.225000000000000, 0.125939180544827, 0.125939180544827, 0.125939180544827,
+                   0.132394152788506, 0.132394152788506, 0.132394152788506};
+            break;
+        }
+        case ORC_RULE_TET_4: {  // cl_MTK_Integration_Coeffs_Tet_4.hpp
+            t.dim = 3; t.n = 4;
+            const real a = 0.585410196624968, b = 0.138196601125010;
+            const real x[4] = {a, b, b, b}, y[4] = {b, a, b, b}, z[4] = {b, b, b, a};
+            for (int k = 0; k < 4; ++k) { t.pts.push_back(x[k]); t.pts.push_back(y[k]); t.pts.push_back(z[k]); }
+            t.w.assign(4, 0.25);
+            break;
+        }
+        case ORC_RULE_TET_11: {  // cl_MTK_Integration_Coeffs_Tet_11.hpp (weights x 6.0 at :117)
+            t.dim = 3; t.n = 11;
+            const real x[11] = {0.7857142857142860, 0.0714285714285714, 0.0714285714285714, 0.0714285714285714,
+                                0.3994035761667990, 0.3994035761667990, 0.3994035761667990, 0.1005964238332010,
+                                0.1005964238332010, 0.1005964238332010, 0.2500000000000000};
+            const real y[11] = {0.0714285714285714, 0.7857142857142860, 0.0714285714285714, 0.0714285714285714,
+                                0.3994035761667990, 0.1005964238332010, 0.1005964238332010, 0.3994035761667990,
+                                0.3994035761667990, 0.1005964238332010, 0.2500000000000000};
+            const real z[11] = {0.0714285714285714, 0.0714285714285714, 0.0714285714285714, 0.7857142857142860,
+                                0.1005964238332010, 0.1005964238332010, 0.3994035761667990, 0.1005964238332010,
+                                0.3994035761667990, 0.3994035761667990, 0.2500000000000000};
+            const real w[11] = {0.0076222222222222, 0.0076222222222222, 0.0076222222222222, 0.0076222222222222,
+                                0.0248888888888889, 0.0248888888888889, 0.0248888888888889, 0.0248888888888889,
+                                0.0248888888888889, 0.0248888888888889, -0.0131555555555556};
+            for (int k = 0; k < 11; ++k) {
+                t.pts.push_back(x[k]); t.pts.push_back(y[k]); t.pts.push_back(z[k]);
+                t.w.push_back(6.0 * w[k]);
+            }
+            break;
+        }
+        default:
+            t.dim = 0; t.n = 0;
+    }
+    return t;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lagrange shape functions, MTK/src/interpolation/
+   cl_MTK_Interpolation_Function_Lagrange_{Bar2,Quad4,Hex8,Tri3,Tet4}.hpp     */
+int cell_nodes(int cell) {
+    switch (cell) {
+        case ORC_CELL_QUAD4: return 4;
+        case ORC_CELL_HEX8: return 8;
+        case ORC_CELL_TRI3: return 3;
+        case ORC_CELL_TET4: return 4;
+        case ORC_CELL_LINE2: return 2;
+    }
+    return 0;
+}
+int cell_pdim(int cell) {
+    switch (cell) {
+        case ORC_CELL_QUAD4: return 2;
+        case ORC_CELL_HEX8: return 3;
+        case ORC_CELL_TRI3: return 2;
+        case ORC_CELL_TET4: return 3;
+        case ORC_CELL_LINE2: return 1;
+    }
+    return 0;
+}
+
+void shape(int cell, const real* xi, Mat& N, Mat& dN) {
+    const int n = cell_nodes(cell), pd = cell_pdim(cell);
+    N = Mat(1, n);
+    dN = Mat(pd, n);
+    switch (cell) {
+        case ORC_CELL_LINE2: {  // ..._Lagrange_Bar2.hpp
+            const real x = xi[0];
+            N(0, 0) = 0.5 * (1.0 - x);
+            N(0, 1) = 0.5 * (1.0 + x);
+            dN(0, 0) = -0.5;
+            dN(0, 1) = 0.5;
+            break;
+        }
+        case ORC_CELL_QUAD4: {  // ..._Lagrange_Quad4.hpp:61-110
+            const real x = xi[0], e = xi[1];
+            N(0, 0) = ((1.0 - x) * (1.0 - e)) * 0.25;
+            N(0, 1) = ((1.0 + x) * (1.0 - e)) * 0.25;
+            N(0, 2) = ((1.0 + x) * (1.0 + e)) * 0.25;
+            N(0, 3) = ((1.0 - x) * (1.0 + e)) * 0.25;
+            dN(0, 0) = 0.25 * (e - 1.0);
+            dN(1, 0) = 0.25 * (x - 1.0);
+            dN(0, 1) = -0.25 * (e - 1.0);
+            dN(1, 1) = -0.25 * (x + 1.0);
+            dN(0, 2) = 0.25 * (e + 1.0);
+            dN(1, 2) = 0.25 * (x + 1.0);
+            dN(0, 3) = -0.25 * (e + 1.0);
+            dN(1, 3) = -0.25 * (x - 1.0);
+            break;
+        }
+        case ORC_CELL_HEX8: {  // ..._Lagrange_Hex8.hpp:83-160
+            const real x = xi[0], e = xi[1], z = xi[2];
+            N(0, 0) = -(e - 1.0) * (x - 1.0) * (z - 1.0) * 0.125;
+            N(0, 1) = (e - 1.0) * (x + 1.0) * (z - 1.0) * 0.125;
+            N(0, 2) = -(e + 1.0) * (x + 1.0) * (z - 1.0) * 0.125;
+            N(0, 3) = (e + 1.0) * (x - 1.0) * (z - 1.0) * 0.125;
+            N(0, 4) = (e - 1.0) * (x - 1.0) * (z + 1.0) * 0.125;
+            N(0, 5) = -(e - 1.0) * (x + 1.0) * (z + 1.0) * 0.125;
+            N(0, 6) = (e + 1.0) * (x + 1.0) * (z + 1.0) * 0.125;
+            N(0, 7) = -(e + 1.0) * (x - 1.0) * (z + 1.0) * 0.125;
+            // derivatives of the node-wise sign products (+-1 +- xi)...
+            const real sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+            const real sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+            const real sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+            for (int a = 0; a < 8; ++a) {
+                const real fx = 1.0 + sx[a] * x, fy = 1.0 + sy[a] * e, fz = 1.0 + sz[a] * z;
+                dN(0, a) = 0.125 * sx[a] * fy * fz;
+                dN(1, a) = 0.125 * sy[a] * fx * fz;
+                dN(2, a) = 0.125 * sz[a] * fx * fy;
+            }
+            break;
+        }
+        case ORC_CELL_TRI3: {  // ..._Lagrange_Tri3.hpp:56-100
+            N(0, 0) = xi[0];
+            N(0, 1) = xi[1];
+            N(0, 2) = 1.0 - xi[0] - xi[1];
+            dN(0, 0) = 1.0; dN(1, 0) = 0.0;
+            dN(0, 1) = 0.0; dN(1, 1) = 1.0;
+            dN(0, 2) = -1.0; dN(1, 2) = -1.0;
+            break;
+        }
+        case ORC_CELL_TET4: {  // ..._Lagrange_Tet4.hpp: order (xi1, xi2, 1-sum, xi3)
+            N(0, 0) = xi[0];
+            N(0, 1) = xi[1];
+            N(0, 2) = 1.0 - xi[0] - xi[1] - xi[2];
+            N(0, 3) = xi[2];
+            dN(0, 0) = 1.0; dN(1, 0) = 0.0; dN(2, 0) = 0.0;
+            dN(0, 1) = 0.0; dN(1, 1) = 1.0; dN(2, 1) = 0.0;
+            dN(0, 2) = -1.0; dN(1, 2) = -1.0; dN(2, 2) = -1.0;
+            dN(0, 3) = 0.0; dN(1, 3) = 0.0; dN(2, 3) = 1.0;
+            break;
+        }
+    }
+}
+
+/* reference-element vertex parameter coordinates (get_param_coords) */
+void param_coords(int cell, Mat& X) {
+    const int n = cell_nodes(cell), pd = cell_pdim(cell);
+    X = Mat(n, pd);
+    if (cell == ORC_CELL_QUAD4) {
+        const real v[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+        for (int a = 0; a < 4; ++a) for (int d = 0; d < 2; ++d) X(a, d) = v[a][d];
+    } else if (cell == ORC_CELL_HEX8) {
+        const real v[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                              {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+        for (int a = 0; a < 8; ++a) for (int d = 0; d < 3; ++d) X(a, d) = v[a][d];
+    } else if (cell == ORC_CELL_TET4) {
+        const real v[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 0}, {0, 0, 1}};
+        for (int a = 0; a < 4; ++a) for (int d = 0; d < 3; ++d) X(a, d) = v[a][d];
+    } else if (cell == ORC_CELL_TRI3) {
+        const real v[3][2] = {{1, 0}, {0, 1}, {0, 0}};
+        for (int a = 0; a < 3; ++a) for (int d = 0; d < 2; ++d) X(a, d) = v[a][d];
+    } else if (cell == ORC_CELL_LINE2) {
+        X(0, 0) = -1; X(1, 0) = 1;
+    }
+}
+
+/* facet vertex maps: MTK/src/geometry/cell/cl_MTK_Cell_Info_Quad4.cpp:155
+   (node_to_edge) and cl_MTK_Cell_Info_Hex8.cpp:177 (node_to_face).         */
+const int QUAD4_SIDES[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+const int HEX8_SIDES[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+
+/* ------------------------------------------------------------------------ */
+/* Space_Interpolator: J = dN/dxi * Xhat (cl_MTK_Space_Interpolator.cpp:413),
+   detJ (hex/quad general :1006, rect :1055/:954, tet /6 :1180, tri /2),
+   inverse (3d :610, rect :676-706).                                          */
+real det_bulk(const Mat& J, int cell, bool rect) {
+    const int d = J.r;
+    if (d == 2) {
+        real det = rect ? J(0, 0) * J(1, 1) : J(0, 0) * J(1, 1) - J(0, 1) * J(1, 0);
+        if (cell == ORC_CELL_TRI3) det /= 2.0;
+        return det;
+    }
+    if (rect && cell == ORC_CELL_HEX8) return J(1, 1) * J(0, 0) * J(2, 2);
+    real det = +J(0, 0) * (J(1, 1) * J(2, 2) - J(2, 1) * J(1, 2)) -
+               J(0, 1) * (J(1, 0) * J(2, 2) - J(1, 2) * J(2, 0)) +
+               J(0, 2) * (J(1, 0) * J(2, 1) - J(1, 1) * J(2, 0));
+    if (cell == ORC_CELL_TET4) det /= 6.0;
+    return det;
+}
+
+Mat inverse_ip(const Mat& J, bool rect) {
+    const int d = J.r;
+    Mat I(d, d, 0.0);
+    if (rect) {
+        for (int i = 0; i < d; ++i) I(i, i) = 1.0 / J(i, i);
+        return I;
+    }
+    if (d == 2) {
+        const real det = J(0, 0) * J(1, 1) - J(0, 1) * J(1, 0);
+        const real inv = 1.0 / det;
+        I(0, 0) = J(1, 1) * inv;
+        I(0, 1) = -J(0, 1) * inv;
+        I(1, 0) = -J(1, 0) * inv;
+        I(1, 1) = J(0, 0) * inv;
+        return I;
+    }
+    const real det = +J(0, 0) * (J(1, 1) * J(2, 2) - J(2, 1) * J(1, 2)) -
+                     J(0, 1) * (J(1, 0) * J(2, 2) - J(1, 2) * J(2, 0)) +
+                     J(0, 2) * (J(1, 0) * J(2, 1) - J(1, 1) * J(2, 0));
+    const real inv = 1.0 / det;
+    I(0, 0) = (J(1, 1) * J(2, 2) - J(2, 1) * J(1, 2)) * inv;
+    I(0, 1) = (J(0, 2) * J(2, 1) - J(0, 1) * J(2, 2)) * inv;
+    I(0, 2) = (J(0, 1) * J(1, 2) - J(0, 2) * J(1, 1)) * inv;
+    I(1, 0) = (J(1, 2) * J(2, 0) - J(1, 0) * J(2, 2)) * inv;
+    I(1, 1) = (J(0, 0) * J(2, 2) - J(0, 2) * J(2, 0)) * inv;
+    I(1, 2) = (J(1, 0) * J(0, 2) - J(0, 0) * J(1, 2)) * inv;
+    I(2, 0) = (J(1, 0) * J(2, 1) - J(2, 0) * J(1, 1)) * inv;
+    I(2, 1) = (J(2, 0) * J(0, 1) - J(0, 0) * J(2, 1)) * inv;
+    I(2, 2) = (J(0, 0) * J(1, 1) - J(1, 0) * J(0, 1)) * inv;
+    return I;
+}
+
+/* ------------------------------------------------------------------------ */
+/* CM_Struc_Linear_Isotropic constitutive matrices:
+   full_plane_strain (FEM/INT/src/CM/cl_FEM_CM_Struc_Linear_Isotropic.cpp:282),
+   full_plane_stress (:262), full_3d (:374).  Strain layout per
+   CM_Struc_Linear::set_function_pointers (cl_FEM_CM_Struc_Linear.cpp:132-261).*/
+Mat constitutive(int model, int dim, real E, real nu) {
+    if (dim == 3) {
+        Mat D(6, 6, 0.0);
+        const real pre = E / (1.0 + nu) / (1.0 - 2.0 * nu);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) D(i, j) = pre * (i == j ? (1.0 - nu) : nu);
+        for (int i = 3; i < 6; ++i) D(i, i) = pre * (1.0 - 2.0 * nu) / 2.0;
+        return D;
+    }
+    if (model == ORC_MODEL_PLANE_STRESS) {
+        Mat D(3, 3, 0.0);
+        const real pre = E / (1.0 - nu * nu);
+        D(0, 0) = pre;
+        D(1, 1) = pre;
+        D(0, 1) = pre * nu;
+        D(1, 0) = pre * nu;
+        D(2, 2) = pre * 0.5 * (1.0 - nu);
+        return D;
+    }
+    Mat D(4, 4, 0.0);
+    const real pre = E / (1.0 + nu) / (1.0 - 2.0 * nu);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) D(i, j) = pre * (i == j ? (1.0 - nu) : nu);
+    D(3, 3) = pre * (1.0 - 2.0 * nu) / 2.0;
+    return D;
+}
+
+/* test strain B: CM_Struc_Linear::eval_teststrain_2d / _3d
+   (cl_FEM_CM_Struc_Linear.cpp:503-592).  dNdx is dim x n.                   */
+Mat test_strain(int model, const Mat& dNdx) {
+    const int d = dNdx.r, n = dNdx.c;
+    if (d == 3) {
+        Mat B(6, 3 * n, 0.0);
+        for (int a = 0; a < n; ++a) {
+            B(0, a) = dNdx(0, a);
+            B(4, a) = dNdx(2, a);
+            B(5, a) = dNdx(1, a);
+            B(1, n + a) = dNdx(1, a);
+            B(3, n + a) = dNdx(2, a);
+            B(5, n + a) = dNdx(0, a);
+            B(2, 2 * n + a) = dNdx(2, a);
+            B(3, 2 * n + a) = dNdx(1, a);
+            B(4, 2 * n + a) = dNdx(0, a);
+        }
+        return B;
+    }
+    const int ns = (model == ORC_MODEL_PLANE_STRESS) ? 3 : 4;
+    const int shear = ns - 1;
+    Mat B(ns, 2 * n, 0.0);
+    for (int a = 0; a < n; ++a) {
+        B(0, a) = dNdx(0, a);
+        B(1, n + a) = dNdx(1, a);
+        B(shear, a) = dNdx(1, a);
+        B(shear, n + a) = dNdx(0, a);
+    }
+    return B;
+}
+
+/* flatten_normal_2d / _3d (cl_FEM_CM_Struc_Linear.cpp:836-863) */
+Mat flat_normal(const real* nrm, int dim, int nstress) {
+    if (dim == 2) {
+        Mat F(2, nstress, 0.0);
+        F(0, 0) = nrm[0];
+        F(0, nstress - 1) = nrm[1];
+        F(1, 1) = nrm[1];
+        F(1, nstress - 1) = nrm[0];
+        return F;
+    }
+    Mat F(3, 6, 0.0);
+    F(0, 0) = nrm[0];
+    F(1, 1) = nrm[1];
+    F(2, 2) = nrm[2];
+    F(0, 4) = nrm[2];
+    F(0, 5) = nrm[1];
+    F(1, 3) = nrm[2];
+    F(1, 5) = nrm[0];
+    F(2, 3) = nrm[1];
+    F(2, 4) = nrm[0];
+    return F;
+}
+
+/* field N matrix for a vector field: Field_Interpolator::N()
+   (FEM/INT/src/IP/cl_FEM_Field_Interpolator.cpp:310-400), type-major.       */
+Mat field_N(const Mat& Nrow, int dim) {
+    const int n = Nrow.c;
+    Mat N(dim, dim * n, 0.0);
+    for (int f = 0; f < dim; ++f)
+        for (int a = 0; a < n; ++a) N(f, f * n + a) = Nrow(0, a);
+    return N;
+}
+
+/* ------------------------------------------------------------------------ */
+struct BulkSet {
+    int ig_cell, rule, model;
+    std::vector<int32_t> ip_cell;
+    std::vector<int64_t> ig_off;  // empty => trivial
+    std::vector<real> ig_coords, ig_param;
+    std::vector<real> E;
+    real nu;
+};
+struct SideSet {
+    int iwg, rule, model;
+    std::vector<int32_t> ip_cell, ordinal;
+    std::vector<real> E;
+    real nu, alpha;
+    real value[3];
+};
+
+}  // namespace
+
+/* ======================================================================== */
+struct orc_mesh {
+    int dim;
+    std::vector<real> coords;
+    std::vector<int32_t> cells;
+    int64_t num_bases;
+    std::vector<int64_t> t_off;
+    std::vector<int32_t> t_bases;
+    std::vector<real> t_w;
+};
+
+struct orc_model {
+    int dim, ip_cell, shape;
+    int64_t num_nodes, num_cells, num_bases;
+    std::vector<real> coords;
+    std::vector<int32_t> cells;
+    std::vector<int64_t> t_off;
+    std::vector<int32_t> t_bases;
+    std::vector<real> t_w;
+    std::vector<BulkSet> bulk;
+    std::vector<SideSet> side;
+    // MSI products
+    std::vector<int64_t> basis_rank;  // domain basis -> rank among used, -1 if unused
+    int64_t num_used = 0;
+    std::vector<std::vector<int32_t>> cell_ubases;  // sorted unique basis ranks per IP cell
+    std::vector<int32_t> rowptr, colidx;
+    bool finalized = false;
+};
+
+/* ------------------------------------------------------------------------ */
+/* HMR: bspline_shape (HMR/src/fn_HMR_bspline_shape.cpp:20-58), Cox-de Boor on
+   the element-local knot vector 2(i-p)-1, half-open support intervals.      */
+static real bspline_shape(int p, int basis, real xi) {
+    const int steps = 2 * (p + 1);
+    std::vector<real> dxi(steps);
+    for (int i = 0; i < steps; ++i) dxi[i] = ((real)i - (real)p) * 2.0 - 1.0;
+    std::vector<real> N(p + 1, 0.0);
+    for (int q = 0; q <= p; ++q)
+        if (dxi[q + basis] <= xi && xi < dxi[q + basis + 1]) N[q] = 1.0;
+    for (int q = 1; q <= p; ++q) {
+        std::vector<real> Nold(N);
+        for (int i = 0; i <= p - q; ++i) {
+            const real A = xi - dxi[i + basis];
+            const real B = dxi[i + basis + q + 1] - xi;
+            N[i] = 0.5 * (A * Nold[i] + B * Nold[i + 1]) / (real)q;
+        }
+    }
+    return N[0];
+}
+
+extern "C" {
+
+int orc_rule_size(int rule, int* dim, int* npts) {
+    RuleTab t = make_rule(rule);
+    if (t.n == 0) return 1;
+    *dim = t.dim;
+    *npts = t.n;
+    return 0;
+}
+int orc_rule(int rule, double* pts, double* w) {
+    RuleTab t = make_rule(rule);
+    if (t.n == 0) return 1;
+    std::memcpy(pts, t.pts.data(), sizeof(real) * t.pts.size());
+    std::memcpy(w, t.w.data(), sizeof(real) * t.w.size());
+    return 0;
+}
+int orc_cell_num_nodes(int cell) { return cell_nodes(cell); }
+int orc_cell_param_dim(int cell) { return cell_pdim(cell); }
+int orc_shape(int cell, const double* xi, double* N, double* dNdxi) {
+    if (cell_nodes(cell) == 0) return 1;
+    Mat n, dn;
+    shape(cell, xi, n, dn);
+    std::memcpy(N, n.a.data(), sizeof(real) * n.a.size());
+    std::memcpy(dNdxi, dn.a.data(), sizeof(real) * dn.a.size());
+    return 0;
+}
+double orc_bspline_shape(int order, int basis, double xi) { return bspline_shape(order, basis, xi); }
+
+/* HMR level-0 uniform mesh.  Elements and bases are numbered i-fastest
+   (BSpline_Mesh::create_basis_on_level_zero, HMR/src/cl_HMR_BSpline_Mesh.hpp:
+   474-535); the node T rows are T = L (init_lagrange_matrix,
+   cl_HMR_T_Matrix.hpp:433-463; level 0 needs no refinement matrix) evaluated
+   by the first element that visits the node, dropping |T| <= 1e-12
+   (T_Matrix_Base::evaluate, cl_HMR_T_Matrix_Base.cpp:394-420).              */
+orc_mesh* orc_hmr_uniform(int dim, const int* ne, const double* len, int p) {
+    if (dim < 2 || dim > 3 || p < 1 || p > 3) return nullptr;
+    auto* m = new orc_mesh;
+    m->dim = dim;
+    int nn[3] = {1, 1, 1}, nb[3] = {1, 1, 1}, nel[3] = {1, 1, 1};
+    for (int d = 0; d < dim; ++d) {
+        nel[d] = ne[d];
+        nn[d] = ne[d] + 1;
+        nb[d] = ne[d] + p;
+    }
+    const int64_t num_nodes = (int64_t)nn[0] * nn[1] * nn[2];
+    const int64_t num_cells = (int64_t)nel[0] * nel[1] * nel[2];
+    m->num_bases = (int64_t)nb[0] * nb[1] * nb[2];
+    m->coords.resize(num_nodes * dim);
+    for (int64_t k = 0; k < nn[2]; ++k)
+        for (int64_t j = 0; j < nn[1]; ++j)
+            for (int64_t i = 0; i < nn[0]; ++i) {
+                const int64_t id = i + nn[0] * (j + nn[1] * k);
+                const int64_t ijk[3] = {i, j, k};
+                for (int d = 0; d < dim; ++d) m->coords[id * dim + d] = len[d] * (real)ijk[d] / (real)nel[d];
+            }
+    const int npe = dim == 2 ? 4 : 8;
+    Mat XI;
+    param_coords(dim == 2 ? ORC_CELL_QUAD4 : ORC_CELL_HEX8, XI);
+    m->cells.resize(num_cells * npe);
+    std::vector<std::vector<std::pair<int32_t, real>>> rows(num_nodes);
+    std::vector<char> done(num_nodes, 0);
+    const int nlb = dim == 2 ? (p + 1) * (p + 1) : (p + 1) * (p + 1) * (p + 1);
+    for (int64_t ek = 0; ek < nel[2]; ++ek)
+        for (int64_t ej = 0; ej < nel[1]; ++ej)
+            for (int64_t ei = 0; ei < nel[0]; ++ei) {
+                const int64_t e = ei + nel[0] * (ej + nel[1] * ek);
+                const int64_t eijk[3] = {ei, ej, ek};
+                for (int a = 0; a < npe; ++a) {
+                    int64_t nijk[3] = {0, 0, 0};
+                    for (int d = 0; d < dim; ++d) nijk[d] = eijk[d] + (XI(a, d) > 0 ? 1 : 0);
+                    const int64_t nid = nijk[0] + nn[0] * (nijk[1] + nn[1] * nijk[2]);
+                    m->cells[e * npe + a] = (int32_t)nid;
+                    if (done[nid]) continue;
+                    done[nid] = 1;
+                    for (int lb = 0; lb < nlb; ++lb) {
+                        int l[3] = {lb % (p + 1), (lb / (p + 1)) % (p + 1), lb / ((p + 1) * (p + 1))};
+                        real w = 1.0;
+                        for (int d = 0; d < dim; ++d) w *= bspline_shape(p, l[d], XI(a, d));
+                        if (std::abs(w) > 1e-12) {
+                            int64_t bijk[3] = {0, 0, 0};
+                            for (int d = 0; d < dim; ++d) bijk[d] = eijk[d] + l[d];
+                            const int64_t bid = bijk[0] + nb[0] * (bijk[1] + (int64_t)nb[1] * bijk[2]);
+                            rows[nid].push_back({(int32_t)bid, w});
+                        }
+                    }
+                }
+            }
+    m->t_off.assign(num_nodes + 1, 0);
+    for (int64_t n = 0; n < num_nodes; ++n) m->t_off[n + 1] = m->t_off[n] + (int64_t)rows[n].size();
+    m->t_bases.resize(m->t_off[num_nodes]);
+    m->t_w.resize(m->t_off[num_nodes]);
+    for (int64_t n = 0; n < num_nodes; ++n)
+        for (size_t k = 0; k < rows[n].size(); ++k) {
+            m->t_bases[m->t_off[n] + k] = rows[n][k].first;
+            m->t_w[m->t_off[n] + k] = rows[n][k].second;
+        }
+    return m;
+}
+
+void orc_mesh_sizes(const orc_mesh* m, int64_t* nn, int64_t* nc, int64_t* nb, int64_t* nnz) {
+    const int npe = m->dim == 2 ? 4 : 8;
+    *nn = (int64_t)m->coords.size() / m->dim;
+    *nc = (int64_t)m->cells.size() / npe;
+    *nb = m->num_bases;
+    *nnz = (int64_t)m->t_bases.size();
+}
+void orc_mesh_arrays(const orc_mesh* m, double* coords, int32_t* cells, int64_t* t_off, int32_t* t_b,
+                     double* t_w) {
+    std::memcpy(coords, m->coords.data(), m->coords.size() * sizeof(real));
+    std::memcpy(cells, m->cells.data(), m->cells.size() * sizeof(int32_t));
+    std::memcpy(t_off, m->t_off.data(), m->t_off.size() * sizeof(int64_t));
+    std::memcpy(t_b, m->t_bases.data(), m->t_bases.size() * sizeof(int32_t));
+    std::memcpy(t_w, m->t_w.data(), m->t_w.size() * sizeof(real));
+}
+void orc_mesh_free(orc_mesh* m) { delete m; }
+
+/* ------------------------------------------------------------------------ */
+orc_model* orc_model_create(int dim, int ip_cell, int shape_kind, int64_t num_nodes, const double* coords,
+                            int64_t num_cells, const int32_t* cells, int64_t num_bases, const int64_t* t_off,
+                            const int32_t* t_b, const double* t_w) {
+    auto* m = new orc_model;
+    m->dim = dim;
+    m->ip_cell = ip_cell;
+    m->shape = shape_kind;
+    m->num_nodes = num_nodes;
+    m->num_cells = num_cells;
+    m->num_bases = num_bases;
+    const int npe = cell_nodes(ip_cell);
+    m->coords.assign(coords, coords + num_nodes * dim);
+    m->cells.assign(cells, cells + num_cells * npe);
+    m->t_off.assign(t_off, t_off + num_nodes + 1);
+    m->t_bases.assign(t_b, t_b + t_off[num_nodes]);
+    m->t_w.assign(t_w, t_w + t_off[num_nodes]);
+    return m;
+}
+void orc_model_free(orc_model* m) { delete m; }
+
+int orc_model_add_bulk_set(orc_model* m, int ig_cell, int rule, int model, int64_t nc, const int32_t* ipc,
+                           const int64_t* ig_off, const double* ig_coords, const double* ig_param,
+                           const double* E, double nu) {
+    if (m->finalized) return 1;
+    BulkSet s;
+    s.ig_cell = ig_cell;
+    s.rule = rule;
+    s.model = model;
+    s.ip_cell.assign(ipc, ipc + nc);
+    if (ig_off) {
+        s.ig_off.assign(ig_off, ig_off + nc + 1);
+        const int64_t nig = ig_off[nc];
+        const int64_t per = (int64_t)cell_nodes(ig_cell) * m->dim;
+        s.ig_coords.assign(ig_coords, ig_coords + nig * per);
+        s.ig_param.assign(ig_param, ig_param + nig * per);
+    }
+    s.E.assign(E, E + nc);
+    s.nu = nu;
+    m->bulk.push_back(std::move(s));
+    return 0;
+}
+
+int orc_model_add_side_set(orc_model* m, int iwg, int rule, int model, int64_t ns, const int32_t* ipc,
+                           const int32_t* ord, const double* E, double nu, double alpha, const double* value) {
+    if (m->finalized) return 1;
+    SideSet s;
+    s.iwg = iwg;
+    s.rule = rule;
+    s.model = model;
+    s.ip_cell.assign(ipc, ipc + ns);
+    s.ordinal.assign(ord, ord + ns);
+    s.E.assign(E, E + ns);
+    s.nu = nu;
+    s.alpha = alpha;
+    for (int d = 0; d < 3; ++d) s.value[d] = d < m->dim ? value[d] : 0.0;
+    m->side.push_back(std::move(s));
+    return 0;
+}
+
+/* MSI: adof numbering by type then basis rank among used bases
+   (Dof_Manager::create_adofs / set_owned_adofs_ids_by_type,
+   FEM/MSI/src/cl_MSI_Dof_Manager.cpp:703-744, 820-985); element unique adof
+   lists sorted per type (moris::unique, cl_MSI_Equation_Object.cpp:236,285);
+   sparsity as the union of element adof lists per row
+   (MSI_Solver_Interface::compute_sparsity_pattern,
+   cl_MSI_Solver_Interface.cpp:309-588).                                      */
+int orc_model_finalize(orc_model* m) {
+    if (m->finalized) return 0;
+    const int npe = cell_nodes(m->ip_cell);
+    // used bases: referenced by any node of any IP cell that belongs to a set
+    std::vector<char> cell_used(m->num_cells, 0);
+    for (auto& s : m->bulk) for (auto c : s.ip_cell) cell_used[c] = 1;
+    for (auto& s : m->side) for (auto c : s.ip_cell) cell_used[c] = 1;
+    std::vector<char> used(m->num_bases, 0);
+    for (int64_t c = 0; c < m->num_cells; ++c) {
+        if (!cell_used[c]) continue;
+        for (int a = 0; a < npe; ++a) {
+            const int32_t nd = m->cells[c * npe + a];
+            for (int64_t k = m->t_off[nd]; k < m->t_off[nd + 1]; ++k) used[m->t_bases[k]] = 1;
+        }
+    }
+    m->basis_rank.assign(m->num_bases, -1);
+    m->num_used = 0;
+    for (int64_t b = 0; b < m->num_bases; ++b)
+        if (used[b]) m->basis_rank[b] = m->num_used++;
+    m->cell_ubases.assign(m->num_cells, {});
+    for (int64_t c = 0; c < m->num_cells; ++c) {
+        if (!cell_used[c]) continue;
+        std::vector<int32_t>& u = m->cell_ubases[c];
+        for (int a = 0; a < npe; ++a) {
+            const int32_t nd = m->cells[c * npe + a];
+            for (int64_t k = m->t_off[nd]; k < m->t_off[nd + 1]; ++k)
+                u.push_back((int32_t)m->basis_rank[m->t_bases[k]]);
+        }
+        std::sort(u.begin(), u.end());
+        u.erase(std::unique(u.begin(), u.end()), u.end());
+    }
+    // sparsity
+    const int64_t nad = m->num_used * m->dim;
+    std::vector<std::vector<int32_t>> rows(nad);
+    for (int64_t c = 0; c < m->num_cells; ++c) {
+        if (!cell_used[c]) continue;
+        const auto& u = m->cell_ubases[c];
+        std::vector<int32_t> ids;
+        for (int f = 0; f < m->dim; ++f)
+            for (auto b : u) ids.push_back((int32_t)(f * m->num_used + b));
+        for (auto r : ids)
+            for (auto cc : ids) rows[r].push_back(cc);
+    }
+    m->rowptr.assign(nad + 1, 0);
+    for (int64_t r = 0; r < nad; ++r) {
+        auto& v = rows[r];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        m->rowptr[r + 1] = m->rowptr[r] + (int32_t)v.size();
+    }
+    m->colidx.resize(m->rowptr[nad]);
+    for (int64_t r = 0; r < nad; ++r) std::copy(rows[r].begin(), rows[r].end(), m->colidx.begin() + m->rowptr[r]);
+    m->finalized = true;
+    return 0;
+}
+
+int64_t orc_model_num_adofs(const orc_model* m) { return m->num_used * m->dim; }
+int64_t orc_model_nnz(const orc_model* m) { return m->rowptr.empty() ? 0 : m->rowptr.back(); }
+int orc_model_num_sets(const orc_model* m) { return (int)(m->bulk.size() + m->side.size()); }
+int64_t orc_model_num_eq(const orc_model* m, int set) {
+    if (set < (int)m->bulk.size()) return (int64_t)m->bulk[set].ip_cell.size();
+    set -= (int)m->bulk.size();
+    if (set < (int)m->side.size()) return (int64_t)m->side[set].ip_cell.size();
+    return -1;
+}
+int orc_graph(const orc_model* m, int32_t* rowptr, int32_t* colidx) {
+    if (!m->finalized) return 1;
+    std::memcpy(rowptr, m->rowptr.data(), m->rowptr.size() * sizeof(int32_t));
+    std::memcpy(colidx, m->colidx.data(), m->colidx.size() * sizeof(int32_t));
+    return 0;
+}
+
+}  // extern "C"
+
+/* ======================================================================== */
+namespace {
+
+int ip_cell_of(const orc_model* m, int set, int64_t eq) {
+    if (set < (int)m->bulk.size()) return m->bulk[set].ip_cell[eq];
+    return m->side[set - m->bulk.size()].ip_cell[eq];
+}
+
+/* element adof ids: Equation_Object::get_equation_obj_dof_ids
+   (cl_MSI_Equation_Object.cpp:506-554): types in requested order, each
+   type's unique adofs ascending.                                            */
+std::vector<int32_t> element_ids(const orc_model* m, int cell) {
+    std::vector<int32_t> ids;
+    for (int f = 0; f < m->dim; ++f)
+        for (auto b : m->cell_ubases[cell]) ids.push_back((int32_t)(f * m->num_used + b));
+    return ids;
+}
+
+/* element T per type: build_PADofMap (cl_MSI_Equation_Object.cpp:333-364):
+   rows = element nodes, columns = sorted unique adofs; the full element T is
+   block-diagonal over the dof types (build_PADofMap_1, :427-493).          */
+Mat element_T(const orc_model* m, int cell) {
+    const int npe = cell_nodes(m->ip_cell);
+    const auto& u = m->cell_ubases[cell];
+    std::map<int32_t, int> col;
+    for (size_t k = 0; k < u.size(); ++k) col[u[k]] = (int)k;
+    Mat T0(npe, (int)u.size(), 0.0);
+    for (int a = 0; a < npe; ++a) {
+        const int32_t nd = m->cells[(int64_t)cell * npe + a];
+        for (int64_t k = m->t_off[nd]; k < m->t_off[nd + 1]; ++k)
+            T0(a, col[(int32_t)m->basis_rank[m->t_bases[k]]]) = m->t_w[k];
+    }
+    const int d = m->dim;
+    Mat T(d * npe, d * (int)u.size(), 0.0);
+    for (int f = 0; f < d; ++f)
+        for (int a = 0; a < npe; ++a)
+            for (int j = 0; j < (int)u.size(); ++j) T(f * npe + a, f * (int)u.size() + j) = T0(a, j);
+    return T;
+}
+
+Mat ip_coords(const orc_model* m, int cell) {
+    const int npe = cell_nodes(m->ip_cell), d = m->dim;
+    Mat X(npe, d);
+    for (int a = 0; a < npe; ++a) {
+        const int32_t nd = m->cells[(int64_t)cell * npe + a];
+        for (int k = 0; k < d; ++k) X(a, k) = m->coords[(int64_t)nd * d + k];
+    }
+    return X;
+}
+
+/* Field interpolation at an IP-parametric point: N and dN/dx = J^-1 dN/dxi
+   (Field_Interpolator::NBuild / dnNdxn(1), cl_FEM_Field_Interpolator.cpp:
+   405, 464-495) with the IP-cell Jacobian (Space_Interpolator).             */
+void ip_eval(const orc_model* m, const Mat& Xip, const real* xi_ip, Mat& Nrow, Mat& dNdx) {
+    Mat dNdxi;
+    shape(m->ip_cell, xi_ip, Nrow, dNdxi);
+    Mat J = mul(dNdxi, Xip);
+    Mat Ji = inverse_ip(J, m->shape == ORC_SHAPE_RECTANGULAR);
+    dNdx = mul(Ji, dNdxi);
+}
+
+/* IWG_Isotropic_Struc_Linear_Bulk::compute_residual / compute_jacobian
+   (FEM/INT/src/IWG/cl_FEM_IWG_Isotropic_Struc_Linear_Bulk.cpp:42-207):
+   R += w B^T (D eps(u)),  K += w B^T (D B).                                 */
+void iwg_bulk(const Mat& B, const Mat& D, const Mat& uvec, real w, Mat& K, Mat& R) {
+    Mat eps = mul(B, uvec);
+    Mat flux = mul(D, eps);
+    Mat Bt = trans(B);
+    add_scaled(R, w, mul(Bt, flux));
+    add_scaled(K, w, mul(Bt, mul(D, B)));
+}
+
+/* Element_Bulk::compute_jacobian_and_residual (FEM/INT/src/ELEM/
+   cl_FEM_Element_Bulk.cpp:258-355) over the IG cells of one cluster
+   (Cluster::compute_jacobian_and_residual, cl_FEM_Cluster.cpp:444-459).
+   IG->IP map: xi_IP = N_IG(xi_IG) * xihat_IG (Space_Interpolator::
+   map_integration_point); weight w*detJ_IG; GPs with detJ < -1e-6 skipped
+   (Geometry_Interpolator::sDetJInvJacLowerLimit, cl_FEM_Geometry_
+   Interpolator.cpp:28).  The time slab [0,1] with BAR_1 (weight 2, time
+   detJ 0.5) multiplies w*detJ by exactly 1.0.                                */
+void bulk_pdof(const orc_model* m, const BulkSet& s, int64_t eq, const Mat& upd, Mat& K, Mat& R) {
+    const int cell = s.ip_cell[eq];
+    const int d = m->dim, npe = cell_nodes(m->ip_cell);
+    const int nd = d * npe;
+    K = Mat(nd, nd, 0.0);
+    R = Mat(nd, 1, 0.0);
+    Mat Xip = ip_coords(m, cell);
+    RuleTab rt = make_rule(s.rule);
+    Mat D = constitutive(s.model, d, s.E[eq], s.nu);
+    Mat uvec(nd, 1);
+    for (int f = 0; f < d; ++f)
+        for (int a = 0; a < npe; ++a) uvec(f * npe + a, 0) = upd(a, f);
+    const bool rect = m->shape == ORC_SHAPE_RECTANGULAR;
+    int64_t g0 = 0, g1 = 1;
+    if (!s.ig_off.empty()) { g0 = s.ig_off[eq]; g1 = s.ig_off[eq + 1]; }
+    const int ign = cell_nodes(s.ig_cell);
+    for (int64_t g = g0; g < g1; ++g) {
+        Mat Xig, XIig;
+        if (s.ig_off.empty()) {
+            Xig = Xip;
+            param_coords(m->ip_cell, XIig);
+        } else {
+            Xig = Mat(ign, d);
+            XIig = Mat(ign, d);
+            for (int a = 0; a < ign; ++a)
+                for (int k = 0; k < d; ++k) {
+                    Xig(a, k) = s.ig_coords[(g * ign + a) * d + k];
+                    XIig(a, k) = s.ig_param[(g * ign + a) * d + k];
+                }
+        }
+        const bool ig_rect = rect && s.ig_cell == m->ip_cell;
+        for (int q = 0; q < rt.n; ++q) {
+            const real* xig = &rt.pts[(size_t)q * rt.dim];
+            Mat Nig, dNig;
+            shape(s.ig_cell, xig, Nig, dNig);
+            Mat Jig = mul(dNig, Xig);
+            const real detJ = det_bulk(Jig, s.ig_cell, ig_rect);
+            if (detJ < -1.0e-6) continue;
+            const real wstar = rt.w[q] * detJ;
+            Mat xip = mul(Nig, XIig);  // 1 x d
+            Mat Nrow, dNdx;
+            ip_eval(m, Xip, xip.a.data(), Nrow, dNdx);
+            Mat B = test_strain(s.model, dNdx);
+            iwg_bulk(B, D, uvec, wstar, K, R);
+        }
+    }
+}
+
+/* Element_Sideset::compute_jacobian_and_residual (FEM/INT/src/ELEM/
+   cl_FEM_Element_Sideset.cpp:261-330) on trivial side clusters: the side GI
+   interpolates the facet vertices (physical coords and IP-param coords); the
+   side detJ is |J| for lines and |t1 x t2| for quads (cl_MTK_Space_
+   Interpolator.cpp:782, 841); the normal is (t_y, -t_x)/|t| for lines and
+   t1 x t2 / |.| for quads (:1298-1344).
+   Neumann: R -= w N^T t  (cl_FEM_IWG_Isotropic_Struc_Linear_Neumann.cpp:38).
+   Dirichlet Nitsche (…_Dirichlet.cpp:52-240, beta = -1 symmetric / +1
+   unsymmetric per IWG_Factory cl_FEM_IWG_Factory.cpp:196-200):
+     R += w ( -N^T t(u) + beta (nD B)^T (u-g) + gamma N^T (u-g) )
+     K += w ( beta (nD B)^T N + gamma N^T N - N^T (nD B) ),
+   gamma = alpha E / h, h = facet length measure (SP_Dirichlet_Nitsche::
+   eval_SP, cl_FEM_SP_Dirichlet_Nitsche.cpp:75-116; Cluster::compute_cluster_
+   cell_length_measure, cl_FEM_Cluster.cpp:858-920).                          */
+void side_pdof(const orc_model* m, const SideSet& s, int64_t eq, const Mat& upd, Mat& K, Mat& R) {
+    const int cell = s.ip_cell[eq], ord = s.ordinal[eq];
+    const int d = m->dim, npe = cell_nodes(m->ip_cell);
+    const int nd = d * npe;
+    K = Mat(nd, nd, 0.0);
+    R = Mat(nd, 1, 0.0);
+    Mat Xip = ip_coords(m, cell), XI;
+    param_coords(m->ip_cell, XI);
+    const int fcell = d == 2 ? ORC_CELL_LINE2 : ORC_CELL_QUAD4;
+    const int nfv = d == 2 ? 2 : 4;
+    Mat Xs(nfv, d), XIs(nfv, d);
+    for (int a = 0; a < nfv; ++a) {
+        const int v = d == 2 ? QUAD4_SIDES[ord][a] : HEX8_SIDES[ord][a];
+        for (int k = 0; k < d; ++k) {
+            Xs(a, k) = Xip(v, k);
+            XIs(a, k) = XI(v, k);
+        }
+    }
+    RuleTab rt = make_rule(s.rule);
+    Mat D = constitutive(s.model, d, s.E[eq], s.nu);
+    const int nstress = D.r;
+    Mat uvec(nd, 1);
+    for (int f = 0; f < d; ++f)
+        for (int a = 0; a < npe; ++a) uvec(f * npe + a, 0) = upd(a, f);
+    // facet measure (length in 2D, area in 3D) for the element size
+    real hmeas = 0.0;
+    for (int q = 0; q < rt.n; ++q) {
+        Mat Ns, dNs;
+        shape(fcell, &rt.pts[(size_t)q * rt.dim], Ns, dNs);
+        Mat Jt = mul(dNs, Xs);
+        real dj;
+        if (d == 2) dj = std::sqrt(Jt(0, 0) * Jt(0, 0) + Jt(0, 1) * Jt(0, 1));
+        else {
+            const real c0 = Jt(0, 1) * Jt(1, 2) - Jt(0, 2) * Jt(1, 1);
+            const real c1 = Jt(0, 2) * Jt(1, 0) - Jt(0, 0) * Jt(1, 2);
+            const real c2 = Jt(0, 0) * Jt(1, 1) - Jt(0, 1) * Jt(1, 0);
+            dj = std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+        }
+        hmeas += rt.w[q] * dj;
+    }
+    // side length measure: dim-1 == 1 -> the measure itself; == 2 -> sqrt(4A/pi)
+    const real h = (d == 2) ? hmeas : std::pow(4.0 * hmeas / M_PI, 1.0 / 2.0);
+    const real gamma = s.alpha * s.E[eq] / h;
+    const real beta = s.iwg == ORC_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
+    for (int q = 0; q < rt.n; ++q) {
+        Mat Ns, dNs;
+        shape(fcell, &rt.pts[(size_t)q * rt.dim], Ns, dNs);
+        Mat Jt = mul(dNs, Xs);  // (d-1) x d, rows = tangents
+        real detJ, nrm[3] = {0.0, 0.0, 0.0};
+        if (d == 2) {
+            detJ = std::sqrt(Jt(0, 0) * Jt(0, 0) + Jt(0, 1) * Jt(0, 1));
+            nrm[0] = Jt(0, 1) / detJ;
+            nrm[1] = -Jt(0, 0) / detJ;
+        } else {
+            const real c0 = Jt(0, 1) * Jt(1, 2) - Jt(0, 2) * Jt(1, 1);
+            const real c1 = Jt(0, 2) * Jt(1, 0) - Jt(0, 0) * Jt(1, 2);
+            const real c2 = Jt(0, 0) * Jt(1, 1) - Jt(0, 1) * Jt(1, 0);
+            detJ = std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+            nrm[0] = c0 / detJ;
+            nrm[1] = c1 / detJ;
+            nrm[2] = c2 / detJ;
+        }
+        if (detJ < -1.0e-6) continue;
+        const real wstar = rt.w[q] * detJ;
+        Mat xip = mul(Ns, XIs);
+        Mat Nrow, dNdx;
+        ip_eval(m, Xip, xip.a.data(), Nrow, dNdx);
+        Mat N = field_N(Nrow, d);
+        Mat Nt = trans(N);
+        if (s.iwg == ORC_IWG_STRUC_LINEAR_NEUMANN) {
+            Mat t(d, 1);
+            for (int k = 0; k < d; ++k) t(k, 0) = s.value[k];
+            add_scaled(R, -wstar, mul(Nt, t));
+            continue;
+        }
+        Mat B = test_strain(s.model, dNdx);
+        Mat Fn = flat_normal(nrm, d, nstress);
+        Mat nDB = mul(Fn, mul(D, B));  // d x nd (testTraction == dTractiondDOF)
+        Mat trac = mul(nDB, uvec);     // traction(n) = Fn * flux
+        Mat jump = mul(N, uvec);
+        for (int k = 0; k < d; ++k) jump(k, 0) -= s.value[k];
+        Mat nDBt = trans(nDB);
+        Mat r = mul(Nt, trac);
+        for (auto& v : r.a) v = -v;
+        add_scaled(r, beta, mul(nDBt, jump));
+        add_scaled(r, gamma, mul(Nt, jump));
+        add_scaled(R, wstar, r);
+        Mat k = mul(nDBt, N);
+        for (auto& v : k.a) v *= beta;
+        add_scaled(k, gamma, mul(Nt, N));
+        add_scaled(k, -1.0, mul(Nt, nDB));
+        add_scaled(K, wstar, k);
+    }
+    (void)nstress;
+}
+
+/* Equation_Object::get_egn_obj_jacobian_and_residual (FEM/MSI/src/
+   cl_MSI_Equation_Object.cpp:789-842): u_pdof = T u_adof (compute_my_pdof_
+   values :1101-1131), K_a = T^T K T, R_a = T^T R.                            */
+void element_adof(const orc_model* m, int set, int64_t eq, const double* u_adof, Mat& Ka, Mat& Ra) {
+    const int cell = ip_cell_of(m, set, eq);
+    const int d = m->dim, npe = cell_nodes(m->ip_cell);
+    Mat T = element_T(m, cell);
+    std::vector<int32_t> ids = element_ids(m, cell);
+    Mat ua((int)ids.size(), 1);
+    for (size_t k = 0; k < ids.size(); ++k) ua(k, 0) = u_adof ? u_adof[ids[k]] : 0.0;
+    Mat up = mul(T, ua);  // (d*npe) x 1, type-major
+    Mat upd(npe, d);
+    for (int f = 0; f < d; ++f)
+        for (int a = 0; a < npe; ++a) upd(a, f) = up(f * npe + a, 0);
+    Mat K, R;
+    if (set < (int)m->bulk.size()) bulk_pdof(m, m->bulk[set], eq, upd, K, R);
+    else side_pdof(m, m->side[set - m->bulk.size()], eq, upd, K, R);
+    Mat Tt = trans(T);
+    Ka = mul(Tt, mul(K, T));
+    Ra = mul(Tt, R);
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_element_topology(const orc_model* m, int set, int64_t eq, int32_t* ids, int32_t* n) {
+    if (!m->finalized || set < 0 || set >= orc_model_num_sets(m)) return 1;
+    if (eq < 0 || eq >= orc_model_num_eq(m, set)) return 1;
+    std::vector<int32_t> v = element_ids(m, ip_cell_of(m, set, eq));
+    std::copy(v.begin(), v.end(), ids);
+    *n = (int32_t)v.size();
+    return 0;
+}
+
+int orc_element_matrices(const orc_model* m, int set, int64_t eq, const double* u_adof, double* K, double* R) {
+    if (!m->finalized || set < 0 || set >= orc_model_num_sets(m)) return 1;
+    if (eq < 0 || eq >= orc_model_num_eq(m, set)) return 1;
+    Mat Ka, Ra;
+    element_adof(m, set, eq, u_adof, Ka, Ra);
+    std::memcpy(K, Ka.a.data(), Ka.a.size() * sizeof(real));
+    std::memcpy(R, Ra.a.data(), Ra.a.size() * sizeof(real));
+    return 0;
+}
+
+int orc_element_pdof_matrices(const orc_model* m, int set, int64_t eq, const double* u_pdof, double* K,
+                              double* R, int32_t* npdof) {
+    if (set < 0 || set >= orc_model_num_sets(m)) return 1;
+    const int d = m->dim, npe = cell_nodes(m->ip_cell);
+    Mat upd(npe, d);
+    for (int f = 0; f < d; ++f)
+        for (int a = 0; a < npe; ++a) upd(a, f) = u_pdof ? u_pdof[f * npe + a] : 0.0;
+    Mat Kp, Rp;
+    if (set < (int)m->bulk.size()) bulk_pdof(m, m->bulk[set], eq, upd, Kp, Rp);
+    else side_pdof(m, m->side[set - m->bulk.size()], eq, upd, Kp, Rp);
+    std::memcpy(K, Kp.a.data(), Kp.a.size() * sizeof(real));
+    std::memcpy(R, Rp.a.data(), Rp.a.size() * sizeof(real));
+    *npdof = d * npe;
+    return 0;
+}
+
+/* Solver_Interface::fill_matrix_and_RHS (SOL/DLA/src/cl_DLA_Solver_
+   Interface.cpp:317-379): set loop, equation-object loop, scatter of the
+   column-major K_a through Sparse_Matrix_EpetraFECrs::fill_matrix
+   (SOL/SOL_CORE/src/cl_Sparse_Matrix_EpetraFECrs.cpp:103-131, sum-into by
+   global ids) and R_a through Vector_Epetra::sum_into_global_values.  The
+   restatement partitions equation objects over std::threads and sums into
+   the shared CSR with atomic adds.                                           */
+int orc_assemble(const orc_model* m, const double* u_adof, double* vals, double* rhs, int nthreads,
+                 int64_t eq_stride) {
+    if (!m->finalized) return 1;
+    if (nthreads < 1) nthreads = 1;
+    if (eq_stride < 1) eq_stride = 1;
+    const int64_t nnz = orc_model_nnz(m), nad = orc_model_num_adofs(m);
+    std::memset(vals, 0, sizeof(real) * nnz);
+    std::memset(rhs, 0, sizeof(real) * nad);
+    struct Item { int set; int64_t eq; };
+    std::vector<Item> items;
+    for (int s = 0; s < orc_model_num_sets(m); ++s)
+        for (int64_t e = 0; e < orc_model_num_eq(m, s); e += eq_stride) items.push_back({s, e});
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const int64_t i = next.fetch_add(1);
+            if (i >= (int64_t)items.size()) break;
+            Mat Ka, Ra;
+            element_adof(m, items[i].set, items[i].eq, u_adof, Ka, Ra);
+            std::vector<int32_t> ids = element_ids(m, ip_cell_of(m, items[i].set, items[i].eq));
+            const int n = (int)ids.size();
+            for (int c = 0; c < n; ++c) {
+                for (int r = 0; r < n; ++r) {
+                    const int32_t row = ids[r], col = ids[c];
+                    const int32_t* b = m->colidx.data() + m->rowptr[row];
+                    const int32_t* e = m->colidx.data() + m->rowptr[row + 1];
+                    const int64_t pos = std::lower_bound(b, e, col) - m->colidx.data();
+                    std::atomic_ref<real>(vals[pos]).fetch_add(Ka(r, c), std::memory_order_relaxed);
+                }
+            }
+            for (int r = 0; r < n; ++r)
+                std::atomic_ref<real>(rhs[ids[r]]).fetch_add(Ra(r, 0), std::memory_order_relaxed);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(worker);
+    worker();
+    for (auto& t : th) t.join();
+    return 0;
+}
+
+/* plain (Jacobi-)preconditioned conjugate gradients; the reference delegates
+   this to Trilinos AztecOO (AZ_cg + AZ_Jacobi, PRM/src/fn_PRM_SOL_
+   Parameters.hpp:453-518), restated here as the textbook algorithm.        */
+int orc_pcg(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* b, double* x,
+            double rtol, int max_iter, int jacobi, int* iters, double* rel_res) {
+    std::vector<real> r(n), z(n), p(n), q(n), dinv(n, 1.0);
+    if (jacobi)
+        for (int64_t i = 0; i < n; ++i)
+            for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+                if (ci[k] == i) dinv[i] = 1.0 / v[k];
+    auto spmv = [&](const real* in, real* out) {
+        for (int64_t i = 0; i < n; ++i) {
+            real s = 0.0;
+            for (int32_t k = rp[i]; k < rp[i + 1]; ++k) s += v[k] * in[ci[k]];
+            out[i] = s;
+        }
+    };
+    spmv(x, q.data());
+    real bn = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        r[i] = b[i] - q[i];
+        bn += b[i] * b[i];
+    }
+    bn = std::sqrt(bn);
+    if (bn == 0.0) bn = 1.0;
+    real rz = 0.0, rn = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        z[i] = dinv[i] * r[i];
+        p[i] = z[i];
+        rz += r[i] * z[i];
+        rn += r[i] * r[i];
+    }
+    int it = 0;
+    while (std::sqrt(rn) / bn > rtol && it < max_iter) {
+        spmv(p.data(), q.data());
+        real pq = 0.0;
+        for (int64_t i = 0; i < n; ++i) pq += p[i] * q[i];
+        const real alpha = rz / pq;
+        rn = 0.0;
+        for (int64_t i = 0; i < n; ++i) {
+            x[i] += alpha * p[i];
+            r[i] -= alpha * q[i];
+            rn += r[i] * r[i];
+        }
+        real rz1 = 0.0;
+        for (int64_t i = 0; i < n; ++i) {
+            z[i] = dinv[i] * r[i];
+            rz1 += r[i] * z[i];
+        }
+        const real beta = rz1 / rz;
+        rz = rz1;
+        for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+        ++it;
+    }
+    *iters = it;
+    *rel_res = std::sqrt(rn) / bn;
+    return std::sqrt(rn) / bn <= rtol ? 0 : 2;
+}
+
+}  // extern "C"

@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 element hot path: elements/s of full Jacobian +
+residual assembly into CSR (fill_matrix_and_RHS) on the 3D linear-elasticity
+workload: 64^3 hex8 cells on the unit cube, quadratic B-spline extraction
+(27 bases / 81 adofs per element, dense 8x27 extraction per element),
+HEX_3x3x3 Gauss points, FP64, Young's modulus per element drawn log-uniform
+in [1e-3, 1] from a seeded generator, nu = 0.3.  Also times the matrix-free
+Jacobian-vector product of the same operator.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the
+workload (the element path has no cross-GPU exchange on one node: replicas
+only); value = elements of all ranks / max time over ranks.
+
+``--impl reference`` times the reference's algorithm on the host cores: the
+C++ restatement in oracle/ (the reference itself needs Trilinos/PETSc/MPI
+and does not build here), all host threads, a bounded sample of the same
+elements per step.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20261203 + 2  # base seed + config index of the 3D quadratic workload
+NE = 64
+NU_P = 0.3
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--ne", type=int, default=NE, help="elements per direction (64 = the benchmark workload)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def workload(ne):
+    import moris_gb300 as mg
+    from moris_gb300.rng import uniform01
+    mesh = mg.hmr_uniform_mesh(3, (ne, ne, ne), (1.0, 1.0, 1.0), 2)
+    nc = len(mesh["cells"])
+    E = 10.0 ** (-3.0 + 3.0 * uniform01(SEED, nc))
+    return mesh, E
+
+
+def flops_per_element_c2():
+    """FP64 flop count (FMA = 2) of the kernel's formulation for one interior
+    hex8 / quadratic B-spline element with 27 Gauss points.  Column counts of
+    the extraction: per direction the two end nodes see 1 or 2 bases, so a
+    basis column of T has tc = product over directions of (1 or 2) nonzeros."""
+    tc1 = [1, 2, 1]  # nodes (of 2) seeing basis j = 0, 1, 2 in one direction
+    tc = [a * b * c for c in tc1 for b in tc1 for a in tc1]  # 27 columns, sum 64
+    NGP, NPD, NB, D = 27, 24, 27, 3
+    geo = NGP * (2 * D * 8 + 2 + D + 2 * NPD + 1)          # diag J, detJ, 1/J, g, w*g
+    upd = NPD * 8 * 2                                     # u_pdof = T u_adof
+    gram = (NPD * (NPD + 1) // 2) * NGP * 2               # upper triangle of A
+    kiso = (NPD * (NPD + 1) // 2) * 3 + 3 * 36 * 4        # K from A (diag blocks: trace)
+    resid = NPD * NPD * 2 + D * sum(tc) * 2               # R_p = K u, R_a = T^T R_p
+    kt = NPD * D * sum(tc) * 2                            # KT = K T
+    ka = 0                                                # upper triangle of T^T KT
+    nad = D * NB
+    for r in range(nad):
+        ka += tc[r % NB] * (nad - r) * 2
+    return geo + upd + gram + kiso + resid + kt + ka
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % gpu_index)
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference(mesh, E, seconds, steps=1, warmup=0):
+    """Time the oracle's restated reference assembly on all host threads over
+    a bounded sample (every k-th element) of the same workload."""
+    from oracle import OracleModel
+    nthreads = os.cpu_count() or 1
+    nc = len(mesh["cells"])
+    orc = OracleModel(3, 1, 0, mesh)
+    orc.add_bulk_set(1, 4, 2, np.arange(nc, dtype=np.int32), E, NU_P)
+    orc.finalize()
+    rng = np.random.default_rng(SEED + 1)
+    u = rng.uniform(-1.0, 1.0, orc.num_adofs)
+    out = (np.zeros(orc.nnz), np.zeros(orc.num_adofs))
+    # calibrate the sample stride on a small sample
+    stride = max(1, nc // (64 * nthreads))
+    t0 = time.perf_counter()
+    orc.assemble(u, nthreads=nthreads, eq_stride=stride, out=out)
+    rate = ((nc + stride - 1) // stride) / (time.perf_counter() - t0)
+    stride = max(1, int(nc / max(1.0, rate * seconds)))
+    n_el = (nc + stride - 1) // stride
+    for _ in range(warmup):
+        orc.assemble(u, nthreads=nthreads, eq_stride=stride, out=out)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        orc.assemble(u, nthreads=nthreads, eq_stride=stride, out=out)
+        times.append(time.perf_counter() - t0)
+    cpu_model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                cpu_model = line.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return dict(value=n_el / float(np.median(times)), cores=nthreads, n_el=n_el, stride=stride,
+                step_seconds=float(np.median(times)), cpu=cpu_model)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, E = workload(args.ne)
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
+    # bounded: the whole --steps/--warmup run stays within a few minutes
+    per_step = min(args.cpu_seconds, max(0.5, 150.0 / (steps + warm)))
+    r = cpu_reference(mesh, E, per_step, steps=steps, warmup=warm)
+    sample = "every %d-th of the %d^3 elements (%d elements) per step, %d threads" % (
+        r["stride"], args.ne, r["n_el"], r["cores"])
+    line = {
+        "metric": "elements/s assembled (FP64 full Jacobian + residual into CSR)",
+        "value": r["value"], "unit": "elements/s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+        "ms_per_step": r["step_seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": "3D elasticity %d^3 hex8, quadratic B-spline extraction, HEX_3x3x3" % args.ne,
+                   "elements": args.ne ** 3, "parallelism": "host threads"},
+        "cpu_baseline": {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",
+                         "sample": sample, "cpu": r["cpu"]},
+        "e2e": {"value": r["value"], "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+    import moris_gb300 as mg
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    mesh, E = workload(args.ne)
+    nc = len(mesh["cells"])
+    model = mg.FemModel(3, mesh, mg.SHAPE_RECTANGULAR)
+    model.add_bulk_set(np.arange(nc, dtype=np.int32), E, NU_P, mg.RULE_HEX_3x3x3, mg.MODEL_3D)
+    stream = torch.cuda.current_stream()
+    model.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    model.finalize()
+    setup_s = time.perf_counter() - t0
+    nad, nnz = model.num_adofs, model.nnz
+    rng = np.random.default_rng(SEED + 1)
+    u_host = rng.uniform(-1.0, 1.0, nad)
+    u = torch.tensor(u_host, device="cuda")
+    vals = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(nad, dtype=torch.float64, device="cuda")
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps  # ms
+
+    # --- headline: fill_matrix_and_RHS on device-resident inputs -------------------
+    sampler = ClockSampler(local)
+    for _ in range(args.warmup):
+        model.assemble(u, vals, rhs)
+    torch.cuda.synchronize()
+    barrier()
+    l0 = model.launch_count()
+    sampler.start()
+    ms = timed(lambda: model.assemble(u, vals, rhs), args.steps, 0)
+    clocks = sampler.stop()
+    launches = model.launch_count() - l0
+    # kernel alone (accumulate: no zero fill) for the roofline
+    ms_kernel = timed(lambda: model.assemble(u, vals, rhs, mg.ACCUMULATE), max(5, args.steps // 4), 2)
+    # matrix-free Jv
+    x = torch.tensor(rng.uniform(-1.0, 1.0, nad), device="cuda")
+    y = torch.empty_like(x)
+    ms_jv = timed(lambda: model.apply(x, y), max(5, args.steps // 2), 2)
+    # --- e2e: the same call with host buffers (pinned), copies inside the timed region -------
+    e2e = None
+    if not args.no_e2e:
+        u_p = torch.tensor(u_host).pin_memory()
+        vals_p = torch.empty(nnz, dtype=torch.float64).pin_memory()
+        rhs_p = torch.empty(nad, dtype=torch.float64).pin_memory()
+        fn = lambda: model.assemble_raw(u_p.data_ptr(), vals_p.data_ptr(), rhs_p.data_ptr(), mg.HOST_BUFFERS)
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        barrier()
+        n_e2e = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            fn()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / n_e2e
+        barrier()
+        e2e = {"seconds_per_step": dt, "h2d_bytes_per_step": 8 * nad, "d2h_bytes_per_step": 8 * (nnz + nad)}
+
+    # max over ranks
+    def maxr(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ms = maxr(ms)
+    ms_kernel = maxr(ms_kernel)
+    ms_jv = maxr(ms_jv)
+    if e2e:
+        e2e["seconds_per_step"] = maxr(e2e["seconds_per_step"])
+    total_el = nc * world
+    value = total_el / (ms * 1e-3)
+    if rank != 0:
+        barrier()
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # roofline of the dominant kernel (FP64 pipe bound)
+    peak = mg.probe_fp64_tflops()
+    fpe = flops_per_element_c2()
+    achieved = fpe * nc / (ms_kernel * 1e-3) / 1e12
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "bulk_kernel_hex8_q2_traffic.json")
+    if os.path.exists(prof) and args.ne == NE:
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": "elements/s assembled (FP64 full Jacobian + residual into CSR)",
+        "value": value, "unit": "elements/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded splitmix64, seed %d)" % SEED,
+        "config": {"workload": "3D elasticity %d^3 hex8, quadratic B-spline extraction (27 bases, 8x27 T per "
+                               "element), HEX_3x3x3, E log-uniform [1e-3,1], nu 0.3" % args.ne,
+                   "elements": nc, "adofs": nad, "csr_nnz": nnz, "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "inputs exceed L2 (CSR values %.2f GB, element data > 1 GB)" % (8 * nnz / 1e9)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "measured in-run (FP64 FMA-chain probe, fem_gpu_probe_fp64_tflops)",
+                     "flops_per_element": fpe, "kernel_ms": ms_kernel},
+        "jv": {"ms_per_apply": ms_jv, "elements_per_s": nc / (ms_jv * 1e-3)},
+        "setup_seconds": setup_s,
+    }
+    if e2e:
+        line["e2e"] = {"value": total_el / e2e["seconds_per_step"], "unit": "elements/s",
+                       "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]}
+    if clocks:
+        line["clocks"] = clocks
+    if world == 1 and not args.no_cpu:
+        r = cpu_reference(mesh, E, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",
+                                "sample": "every %d-th of the %d elements (%d), oracle restatement, %d threads" % (
+                                    r["stride"], nc, r["n_el"], r["cores"]), "cpu": r["cpu"]}
+    print(json.dumps(line), flush=True)
+    barrier()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

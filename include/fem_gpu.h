@@ -1,0 +1,232 @@
+/*
+ * fem_gpu.h -- C ABI of the GB300 element hot path (libfem_gpu.so).
+ *
+ * The library replaces the element loop behind MORIS's solver interface:
+ *
+ *   moris::Solver_Interface  (SOL/DLA/src/cl_DLA_Solver_Interface.hpp:58-661)
+ *     fill_matrix_and_RHS            -> fem_gpu_assemble
+ *     get_element_topology           -> fem_gpu_get_element_topology
+ *     get_equation_object_operator_and_rhs
+ *                                    -> fem_gpu_element_matrices
+ *     build_graph / compute_sparsity_pattern
+ *                                    -> fem_gpu_build_graph
+ *     get_num_sets / get_num_equation_objects_on_set
+ *                                    -> fem_gpu_get_sizes / fem_gpu_get_num_equation_objects
+ *   fem::IWG_Factory::create_IWG(IWG_Type)  (FEM/INT/src/IWG/cl_FEM_IWG_Factory.hpp:43)
+ *                                    -> the iwg_type of fem_gpu_add_*_set
+ *   HMR T-matrix + MSI adof numbering (HMR/src/cl_HMR_T_Matrix_Base.cpp:306-457,
+ *   FEM/MSI/src/cl_MSI_Dof_Manager.cpp:703-985)
+ *                                    -> fem_gpu_mesh_desc node T rows + fem_gpu_finalize
+ *   sol::Dist_Matrix::fill_matrix / Dist_Vector::sum_into_global_values
+ *   (SOL/SOL_CORE/src/cl_Sparse_Matrix_EpetraFECrs.cpp:103-131)
+ *                                    -> the CSR scatter inside fem_gpu_assemble
+ *   Trilinos AztecOO CG + Jacobi (DLA/src/cl_DLA_Linear_Solver_Aztec.cpp:260-355)
+ *                                    -> fem_gpu_pcg
+ *
+ * Conventions (identical to the reference):
+ *  - global ids are adof ids: type offset + rank of the B-spline basis among the
+ *    used bases, types in order UX, UY(, UZ);
+ *  - element adof lists are sorted ascending per type, types concatenated;
+ *  - element matrices are column-major, square, of size nadof x nadof;
+ *  - CSR rows are adofs, column indices ascending.
+ *
+ * Every function returns an fem_gpu_status and never throws.  A context is
+ * single-threaded; calls are ordered on the context's CUDA stream.  Buffers
+ * are device pointers unless FEM_GPU_HOST_BUFFERS is set in flags, in which
+ * case the library stages the host<->device copies on its stream and
+ * synchronises before returning.  fem_gpu_fem_hmr_* are host-only setup
+ * helpers (an HMR-equivalent uniform-mesh generator) that need no GPU.
+ */
+#ifndef MORIS_GB300_FEM_GPU_H
+#define MORIS_GB300_FEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEM_GPU_ABI_VERSION 1
+
+typedef enum fem_gpu_status {
+    FEM_GPU_OK = 0,
+    FEM_GPU_BAD_ARG = 1,        /* null pointer, bad enum, size mismatch   */
+    FEM_GPU_OOB_INDEX = 2,      /* node / cell / basis index out of range  */
+    FEM_GPU_NONFINITE = 3,      /* NaN or Inf in inputs or results         */
+    FEM_GPU_DETJ_NEGATIVE = 4,  /* (reserved; GPs below -1e-6 are skipped) */
+    FEM_GPU_TIMEOUT = 5,        /* a bounded device wait ran out           */
+    FEM_GPU_CUDA_ERROR = 6,     /* a CUDA runtime call failed              */
+    FEM_GPU_NOT_FINALIZED = 7,  /* call needs fem_gpu_finalize first        */
+    FEM_GPU_UNSUPPORTED = 8,    /* valid but not implemented combination   */
+    FEM_GPU_OUT_OF_MEMORY = 9,
+    FEM_GPU_NOT_CONVERGED = 10, /* iterative solve hit max iterations      */
+    FEM_GPU_NO_DEVICE = 11      /* no usable CUDA device                    */
+} fem_gpu_status;
+
+/* cell topologies (mtk::Geometry_Type + interpolation order 1) */
+enum { FEM_GPU_CELL_QUAD4 = 0, FEM_GPU_CELL_HEX8 = 1, FEM_GPU_CELL_TRI3 = 2, FEM_GPU_CELL_TET4 = 3,
+       FEM_GPU_CELL_LINE2 = 4 };
+/* Gauss rules (mtk::Integration_Order) */
+enum {
+    FEM_GPU_RULE_BAR_1 = 0, FEM_GPU_RULE_BAR_3 = 1, FEM_GPU_RULE_QUAD_2x2 = 2, FEM_GPU_RULE_HEX_2x2x2 = 3,
+    FEM_GPU_RULE_HEX_3x3x3 = 4, FEM_GPU_RULE_TRI_7 = 5, FEM_GPU_RULE_TET_4 = 6, FEM_GPU_RULE_TET_11 = 7,
+    FEM_GPU_RULE_TRI_3 = 8
+};
+/* fem::Model_Type of CM_Struc_Linear_Isotropic */
+enum { FEM_GPU_MODEL_PLANE_STRAIN = 0, FEM_GPU_MODEL_PLANE_STRESS = 1, FEM_GPU_MODEL_3D = 2 };
+/* mtk::CellShape of the interpolation cells */
+enum { FEM_GPU_SHAPE_RECTANGULAR = 0, FEM_GPU_SHAPE_GENERAL = 1 };
+/* fem::IWG_Type subset (FEM/INT/src/IWG/cl_FEM_IWG_Factory.cpp:191-224) */
+enum {
+    FEM_GPU_IWG_STRUC_LINEAR_BULK = 0,
+    FEM_GPU_IWG_STRUC_LINEAR_NEUMANN = 1,
+    FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE = 2,
+    FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE = 3,
+    FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE = 4,
+    FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE = 5,
+    FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST = 6
+};
+/* flags */
+enum {
+    FEM_GPU_HOST_BUFFERS = 1u,      /* pointers are host memory                 */
+    FEM_GPU_NO_JACOBIAN = 2u,       /* fem_gpu_assemble: residual only          */
+    FEM_GPU_NO_RESIDUAL = 4u,       /* fem_gpu_assemble: Jacobian only          */
+    FEM_GPU_ACCUMULATE = 8u         /* do not zero csr_vals / rhs first         */
+};
+
+typedef struct fem_gpu_ctx fem_gpu_ctx;
+
+/* Lagrange interpolation mesh with the HMR extraction rows of its nodes.
+   Node n interpolates the B-spline bases t_bases[t_offsets[n] .. t_offsets[n+1])
+   with weights t_weights[...] (mtk::Vertex interpolation of the HMR
+   T-matrix).  Host pointers; copied by fem_gpu_create. */
+typedef struct fem_gpu_mesh_desc {
+    int32_t spatial_dim;          /* 2 or 3 */
+    int32_t ip_cell_type;         /* FEM_GPU_CELL_QUAD4 (2D) or FEM_GPU_CELL_HEX8 (3D) */
+    int32_t cell_shape;           /* FEM_GPU_SHAPE_* */
+    int32_t reserved;
+    int64_t num_nodes;
+    const double* node_coords;    /* num_nodes x spatial_dim */
+    int64_t num_cells;
+    const int32_t* cell_nodes;    /* num_cells x nodes per cell */
+    int64_t num_bases;            /* B-spline basis index range */
+    const int64_t* t_offsets;     /* num_nodes + 1 */
+    const int32_t* t_bases;
+    const double* t_weights;
+} fem_gpu_mesh_desc;
+
+/* Bulk set: IWG_Isotropic_Struc_Linear_Bulk with CM_Struc_Linear_Isotropic
+   over clusters (one interpolation cell each).  ig_offsets == NULL means
+   trivial clusters (the integration cell is the interpolation cell);
+   otherwise cluster c integrates IG cells [ig_offsets[c], ig_offsets[c+1])
+   with ig_coords / ig_param_coords (vertices x dim, node-major) giving the
+   physical and IP-parametric vertex coordinates. */
+typedef struct fem_gpu_bulk_set_desc {
+    int32_t iwg_type;             /* FEM_GPU_IWG_STRUC_LINEAR_BULK */
+    int32_t ig_cell_type;         /* FEM_GPU_CELL_* */
+    int32_t integration_rule;     /* FEM_GPU_RULE_* */
+    int32_t model_type;           /* FEM_GPU_MODEL_* */
+    int64_t num_clusters;
+    const int32_t* cluster_ip_cell;
+    const int64_t* ig_offsets;
+    const double* ig_coords;
+    const double* ig_param_coords;
+    const double* youngs_modulus; /* per cluster */
+    double poisson_ratio;
+} fem_gpu_bulk_set_desc;
+
+/* Side set on interpolation-cell facets (trivial side clusters):
+   Neumann traction (value = traction vector) or Nitsche Dirichlet
+   (value = prescribed displacement, gamma = alpha * E / h). */
+typedef struct fem_gpu_side_set_desc {
+    int32_t iwg_type;
+    int32_t integration_rule;     /* BAR_3 for quad edges, QUAD_2x2 for hex faces */
+    int32_t model_type;
+    int32_t reserved;
+    int64_t num_sides;
+    const int32_t* side_ip_cell;
+    const int32_t* side_ordinal;  /* mtk side ordinal of the facet */
+    const double* youngs_modulus; /* per side */
+    double poisson_ratio;
+    double nitsche_alpha;
+    double value[3];
+} fem_gpu_side_set_desc;
+
+typedef struct fem_gpu_pcg_opts {
+    double rel_tol;               /* on ||b - A x|| / ||b|| */
+    int32_t max_iter;
+    int32_t preconditioner;       /* 0 none, 1 Jacobi */
+} fem_gpu_pcg_opts;
+
+typedef struct fem_gpu_pcg_report {
+    int32_t iterations;
+    int32_t converged;
+    double rel_residual;
+    double seconds;
+} fem_gpu_pcg_report;
+
+/* ---- library ------------------------------------------------------------ */
+int32_t fem_gpu_abi_version(void);
+const char* fem_gpu_status_string(fem_gpu_status s);
+/* number of CUDA devices (0 without a GPU; never fails) */
+int32_t fem_gpu_device_count(void);
+
+/* ---- HMR-equivalent uniform level-0 mesh (host only) ---------------------- */
+typedef struct fem_hmr_mesh fem_hmr_mesh;
+fem_gpu_status fem_hmr_uniform_mesh(int32_t spatial_dim, const int32_t* num_elements, const double* lengths,
+                                    int32_t bspline_order, fem_hmr_mesh** out);
+fem_gpu_status fem_hmr_mesh_sizes(const fem_hmr_mesh* m, int64_t* num_nodes, int64_t* num_cells,
+                                  int64_t* num_bases, int64_t* t_nnz);
+fem_gpu_status fem_hmr_mesh_arrays(const fem_hmr_mesh* m, double* node_coords, int32_t* cell_nodes,
+                                   int64_t* t_offsets, int32_t* t_bases, double* t_weights);
+fem_gpu_status fem_hmr_mesh_free(fem_hmr_mesh* m);
+
+/* ---- model ------------------------------------------------------------- */
+fem_gpu_status fem_gpu_create(const fem_gpu_mesh_desc* mesh, fem_gpu_ctx** out);
+fem_gpu_status fem_gpu_destroy(fem_gpu_ctx* ctx);
+/* cudaStream_t passed as void*; NULL = the library's own stream */
+fem_gpu_status fem_gpu_set_stream(fem_gpu_ctx* ctx, void* stream);
+fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* ctx, const fem_gpu_bulk_set_desc* desc, int32_t* set_index);
+fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* ctx, const fem_gpu_side_set_desc* desc, int32_t* set_index);
+/* host-side MSI work (adof numbering, element T, sparsity, scatter maps)
+   plus the upload of everything the kernels read */
+fem_gpu_status fem_gpu_finalize(fem_gpu_ctx* ctx);
+/* like fem_gpu_finalize but host side only (no device allocation) */
+fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* ctx);
+
+fem_gpu_status fem_gpu_get_sizes(const fem_gpu_ctx* ctx, int64_t* num_adofs, int64_t* nnz, int32_t* num_sets);
+fem_gpu_status fem_gpu_get_num_equation_objects(const fem_gpu_ctx* ctx, int32_t set, int64_t* count);
+fem_gpu_status fem_gpu_get_max_element_adofs(const fem_gpu_ctx* ctx, int32_t set, int32_t* n);
+/* CSR graph of the assembled operator (rowptr: num_adofs+1, colidx: nnz) */
+fem_gpu_status fem_gpu_build_graph(fem_gpu_ctx* ctx, int32_t* rowptr, int32_t* colidx, uint32_t flags);
+/* element adof ids (host pointer, capacity >= max element adofs) */
+fem_gpu_status fem_gpu_get_element_topology(const fem_gpu_ctx* ctx, int32_t set, int64_t eq, int32_t* ids,
+                                            int32_t* n);
+/* element operators of equation objects [first, first+count) of a set:
+   K_colmajor: count x nmax x nmax, R: count x nmax (nmax = max element adofs
+   of the set; smaller elements are zero padded).  u_adof: full solution
+   vector (may be NULL for zero). */
+fem_gpu_status fem_gpu_element_matrices(fem_gpu_ctx* ctx, int32_t set, int64_t first, int64_t count,
+                                        const double* u_adof, double* K_colmajor, double* R, uint32_t flags);
+/* fill_matrix_and_RHS: csr_vals (nnz) and rhs (num_adofs) = residual R(u) */
+fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* ctx, const double* u_adof, double* csr_vals, double* rhs,
+                                uint32_t flags);
+/* matrix-free Jacobian-vector product y = K x (no CSR) */
+fem_gpu_status fem_gpu_apply(fem_gpu_ctx* ctx, const double* x, double* y, uint32_t flags);
+/* preconditioned CG on a CSR operator built by fem_gpu_assemble */
+fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                           const double* b, double* x, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report,
+                           uint32_t flags);
+/* in-run FP64 peak probe (FMA chains on every SM, CUDA-event timed), the
+   roofline denominator of the FP64-bound element kernels */
+fem_gpu_status fem_gpu_probe_fp64_tflops(int32_t iters, double* tflops);
+/* number of kernel launches issued by the context since creation */
+int64_t fem_gpu_launch_count(const fem_gpu_ctx* ctx);
+/* last error text of the context (never NULL) */
+const char* fem_gpu_last_error(const fem_gpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,230 @@
+"""moris_gb300 -- GB300 (sm_103a) element hot path of MORIS behind a C ABI.
+
+Python here is glue for tests and benchmarks: every compute entry point is
+a call into libfem_gpu.so (include/fem_gpu.h).  The classes mirror the
+reference's solver-interface vocabulary: sets of equation objects, element
+topology (adof ids), element operators, fill_matrix_and_RHS.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import BulkSetDesc, MeshDesc, PcgOpts, PcgReport, SideSetDesc
+
+# enums (identical values in include/fem_gpu.h)
+CELL_QUAD4, CELL_HEX8, CELL_TRI3, CELL_TET4, CELL_LINE2 = 0, 1, 2, 3, 4
+RULE_BAR_1, RULE_BAR_3, RULE_QUAD_2x2, RULE_HEX_2x2x2, RULE_HEX_3x3x3 = 0, 1, 2, 3, 4
+RULE_TRI_7, RULE_TET_4, RULE_TET_11, RULE_TRI_3 = 5, 6, 7, 8
+MODEL_PLANE_STRAIN, MODEL_PLANE_STRESS, MODEL_3D = 0, 1, 2
+SHAPE_RECTANGULAR, SHAPE_GENERAL = 0, 1
+IWG_STRUC_LINEAR_BULK = 0
+IWG_STRUC_LINEAR_NEUMANN = 1
+IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE = 2
+IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE = 3
+IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE = 4
+IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE = 5
+IWG_STRUC_LINEAR_VW_GHOST = 6
+HOST_BUFFERS, NO_JACOBIAN, NO_RESIDUAL, ACCUMULATE = 1, 2, 4, 8
+
+
+class FemGpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("fem_gpu status %d (%s): %s" % (status, _status_text(status), msg))
+        self.status = status
+
+
+def _status_text(s):
+    t = _lib.load().fem_gpu_status_string(s)
+    return t.decode() if t else "?"
+
+
+def _np_ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _dev_ptr(t):
+    """Device pointer of a CUDA tensor (or None)."""
+    if t is None:
+        return None
+    assert t.is_cuda and t.is_contiguous()
+    return C.c_void_p(t.data_ptr())
+
+
+def lib():
+    return _lib.load()
+
+
+def device_count():
+    return lib().fem_gpu_device_count()
+
+
+def probe_fp64_tflops(iters=20000):
+    """Measured FP64 FMA throughput of the current GPU (TFLOP/s)."""
+    t = C.c_double()
+    st = lib().fem_gpu_probe_fp64_tflops(iters, C.byref(t))
+    if st:
+        raise FemGpuError(st, "probe_fp64_tflops")
+    return t.value
+
+
+def hmr_uniform_mesh(dim, num_elements, lengths, bspline_order):
+    """Uniform level-0 HMR-equivalent mesh: dict of numpy arrays."""
+    L = lib()
+    ne = np.asarray(list(num_elements) + [1] * (3 - len(num_elements)), dtype=np.int32)
+    ln = np.asarray(list(lengths) + [1.0] * (3 - len(lengths)), dtype=np.float64)
+    h = C.c_void_p()
+    st = L.fem_hmr_uniform_mesh(dim, _np_ptr(ne), _np_ptr(ln), bspline_order, C.byref(h))
+    if st:
+        raise FemGpuError(st, "fem_hmr_uniform_mesh")
+    nn, nc, nb, nz = (C.c_int64() for _ in range(4))
+    L.fem_hmr_mesh_sizes(h, C.byref(nn), C.byref(nc), C.byref(nb), C.byref(nz))
+    npe = 4 if dim == 2 else 8
+    coords = np.zeros(nn.value * dim)
+    cells = np.zeros(nc.value * npe, dtype=np.int32)
+    t_off = np.zeros(nn.value + 1, dtype=np.int64)
+    t_b = np.zeros(nz.value, dtype=np.int32)
+    t_w = np.zeros(nz.value)
+    L.fem_hmr_mesh_arrays(h, _np_ptr(coords), _np_ptr(cells), _np_ptr(t_off), _np_ptr(t_b), _np_ptr(t_w))
+    L.fem_hmr_mesh_free(h)
+    return dict(coords=coords.reshape(-1, dim), cells=cells.reshape(-1, npe), num_bases=nb.value, t_off=t_off,
+                t_bases=t_b, t_w=t_w)
+
+
+class FemModel:
+    """A context of libfem_gpu: one interpolation mesh, its sets, the CSR graph."""
+
+    def __init__(self, dim, mesh, shape=SHAPE_RECTANGULAR):
+        self.L = lib()
+        self.dim = dim
+        self._keep = {}
+        coords = np.ascontiguousarray(mesh["coords"], dtype=np.float64).ravel()
+        cells = np.ascontiguousarray(mesh["cells"], dtype=np.int32).ravel()
+        t_off = np.ascontiguousarray(mesh["t_off"], dtype=np.int64)
+        t_b = np.ascontiguousarray(mesh["t_bases"], dtype=np.int32)
+        t_w = np.ascontiguousarray(mesh["t_w"], dtype=np.float64)
+        d = MeshDesc(dim, CELL_QUAD4 if dim == 2 else CELL_HEX8, shape, 0, len(coords) // dim, _np_ptr(coords),
+                     len(mesh["cells"]), _np_ptr(cells), int(mesh["num_bases"]), _np_ptr(t_off), _np_ptr(t_b),
+                     _np_ptr(t_w))
+        h = C.c_void_p()
+        self._check(self.L.fem_gpu_create(C.byref(d), C.byref(h)), "create", ctx=False)
+        self.h = h
+        self.num_sets = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.fem_gpu_destroy(self.h)
+            self.h = None
+
+    def _check(self, st, what, ctx=True):
+        if st:
+            msg = what
+            if ctx and getattr(self, "h", None):
+                e = self.L.fem_gpu_last_error(self.h)
+                msg += ": " + (e.decode() if e else "")
+            raise FemGpuError(st, msg)
+
+    def set_stream(self, stream_ptr):
+        self._check(self.L.fem_gpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def add_bulk_set(self, ip_cells, youngs, poisson, rule, model, ig_cell=None, ig_offsets=None, ig_coords=None,
+                     ig_param=None):
+        ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)
+        E = np.ascontiguousarray(youngs, dtype=np.float64)
+        off = None if ig_offsets is None else np.ascontiguousarray(ig_offsets, dtype=np.int64)
+        xc = None if ig_coords is None else np.ascontiguousarray(ig_coords, dtype=np.float64)
+        xp = None if ig_param is None else np.ascontiguousarray(ig_param, dtype=np.float64)
+        if ig_cell is None:
+            ig_cell = CELL_QUAD4 if self.dim == 2 else CELL_HEX8
+        d = BulkSetDesc(IWG_STRUC_LINEAR_BULK, ig_cell, rule, model, len(ipc), _np_ptr(ipc), _np_ptr(off),
+                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson)
+        idx = C.c_int32()
+        self._check(self.L.fem_gpu_add_bulk_set(self.h, C.byref(d), C.byref(idx)), "add_bulk_set")
+        self.num_sets += 1
+        return idx.value
+
+    def add_side_set(self, iwg, ip_cells, ordinals, youngs, poisson, rule, model, alpha=0.0, value=(0, 0, 0)):
+        ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)
+        ords = np.ascontiguousarray(ordinals, dtype=np.int32)
+        E = np.ascontiguousarray(youngs, dtype=np.float64)
+        v = (C.c_double * 3)(*(list(value) + [0.0] * (3 - len(value))))
+        d = SideSetDesc(iwg, rule, model, 0, len(ipc), _np_ptr(ipc), _np_ptr(ords), _np_ptr(E), poisson, alpha, v)
+        idx = C.c_int32()
+        self._check(self.L.fem_gpu_add_side_set(self.h, C.byref(d), C.byref(idx)), "add_side_set")
+        self.num_sets += 1
+        return idx.value
+
+    def finalize(self, host_only=False):
+        f = self.L.fem_gpu_finalize_host if host_only else self.L.fem_gpu_finalize
+        self._check(f(self.h), "finalize")
+        nad, nnz, ns = C.c_int64(), C.c_int64(), C.c_int32()
+        self._check(self.L.fem_gpu_get_sizes(self.h, C.byref(nad), C.byref(nnz), C.byref(ns)), "get_sizes")
+        self.num_adofs, self.nnz = nad.value, nnz.value
+
+    def num_eq(self, s):
+        n = C.c_int64()
+        self._check(self.L.fem_gpu_get_num_equation_objects(self.h, s, C.byref(n)), "num_eq")
+        return n.value
+
+    def max_element_adofs(self, s):
+        n = C.c_int32()
+        self._check(self.L.fem_gpu_get_max_element_adofs(self.h, s, C.byref(n)), "max_element_adofs")
+        return n.value
+
+    def graph(self):
+        rp = np.zeros(self.num_adofs + 1, dtype=np.int32)
+        ci = np.zeros(self.nnz, dtype=np.int32)
+        self._check(self.L.fem_gpu_build_graph(self.h, _np_ptr(rp), _np_ptr(ci), HOST_BUFFERS), "build_graph")
+        return rp, ci
+
+    def graph_device(self, rowptr_t, colidx_t):
+        self._check(self.L.fem_gpu_build_graph(self.h, _dev_ptr(rowptr_t), _dev_ptr(colidx_t), 0), "build_graph")
+
+    def element_topology(self, s, eq):
+        ids = np.zeros(max(self.max_element_adofs(s), 1), dtype=np.int32)
+        n = C.c_int32()
+        self._check(self.L.fem_gpu_get_element_topology(self.h, s, eq, _np_ptr(ids), C.byref(n)), "topology")
+        return ids[:n.value].copy()
+
+    def element_matrices(self, s, first, count, u=None):
+        """Host path: returns K (count, n, n) with K[e, i, j] and R (count, n)."""
+        n = self.max_element_adofs(s)
+        K = np.zeros(count * n * n)
+        R = np.zeros(count * n)
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        st = self.L.fem_gpu_element_matrices(self.h, s, first, count, _np_ptr(uu), _np_ptr(K), _np_ptr(R),
+                                             HOST_BUFFERS)
+        self._check(st, "element_matrices")
+        return K.reshape(count, n, n).transpose(0, 2, 1).copy(), R.reshape(count, n)
+
+    def assemble(self, u, vals, rhs, flags=0):
+        """Device path: u, vals, rhs are CUDA tensors (vals/rhs may be None)."""
+        self._check(self.L.fem_gpu_assemble(self.h, _dev_ptr(u), _dev_ptr(vals), _dev_ptr(rhs), flags), "assemble")
+
+    def assemble_host(self, u, flags=0):
+        vals = np.zeros(self.nnz)
+        rhs = np.zeros(self.num_adofs)
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        st = self.L.fem_gpu_assemble(self.h, _np_ptr(uu), _np_ptr(vals), _np_ptr(rhs), flags | HOST_BUFFERS)
+        self._check(st, "assemble")
+        return vals, rhs
+
+    def assemble_raw(self, u_ptr, vals_ptr, rhs_ptr, flags):
+        """Raw-pointer form (e.g. pinned host memory with HOST_BUFFERS)."""
+        st = self.L.fem_gpu_assemble(self.h, C.c_void_p(u_ptr), C.c_void_p(vals_ptr), C.c_void_p(rhs_ptr), flags)
+        self._check(st, "assemble")
+
+    def apply(self, x, y, flags=0):
+        self._check(self.L.fem_gpu_apply(self.h, _dev_ptr(x), _dev_ptr(y), flags), "apply")
+
+    def pcg(self, rowptr, colidx, vals, b, x, rel_tol=1e-10, max_iter=100000, jacobi=True):
+        o = PcgOpts(rel_tol, max_iter, 1 if jacobi else 0)
+        r = PcgReport()
+        st = self.L.fem_gpu_pcg(self.h, _dev_ptr(rowptr), _dev_ptr(colidx), _dev_ptr(vals), _dev_ptr(b), _dev_ptr(x),
+                                C.byref(o), C.byref(r), 0)
+        self._check(st, "pcg")
+        return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual,
+                    seconds=r.seconds)
+
+    def launch_count(self):
+        return self.L.fem_gpu_launch_count(self.h)

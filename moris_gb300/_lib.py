@@ -1,0 +1,91 @@
+"""ctypes binding of libfem_gpu.so (the C ABI declared in include/fem_gpu.h).
+
+The shared library is built in-tree by ``moris_gb300/build.py``.  Loading
+fails loudly when it is missing: there is no Python or CPU fallback for any
+compute entry point.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libfem_gpu.so")
+
+P = C.c_void_p
+I32 = C.c_int32
+I64 = C.c_int64
+U32 = C.c_uint32
+D = C.c_double
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("spatial_dim", I32), ("ip_cell_type", I32), ("cell_shape", I32), ("reserved", I32),
+                ("num_nodes", I64), ("node_coords", P), ("num_cells", I64), ("cell_nodes", P),
+                ("num_bases", I64), ("t_offsets", P), ("t_bases", P), ("t_weights", P)]
+
+
+class BulkSetDesc(C.Structure):
+    _fields_ = [("iwg_type", I32), ("ig_cell_type", I32), ("integration_rule", I32), ("model_type", I32),
+                ("num_clusters", I64), ("cluster_ip_cell", P), ("ig_offsets", P), ("ig_coords", P),
+                ("ig_param_coords", P), ("youngs_modulus", P), ("poisson_ratio", D)]
+
+
+class SideSetDesc(C.Structure):
+    _fields_ = [("iwg_type", I32), ("integration_rule", I32), ("model_type", I32), ("reserved", I32),
+                ("num_sides", I64), ("side_ip_cell", P), ("side_ordinal", P), ("youngs_modulus", P),
+                ("poisson_ratio", D), ("nitsche_alpha", D), ("value", D * 3)]
+
+
+class PcgOpts(C.Structure):
+    _fields_ = [("rel_tol", D), ("max_iter", I32), ("preconditioner", I32)]
+
+
+class PcgReport(C.Structure):
+    _fields_ = [("iterations", I32), ("converged", I32), ("rel_residual", D), ("seconds", D)]
+
+
+# name -> (restype, argtypes); this list is also the ABI surface the tests
+# check against include/fem_gpu.h
+SIGNATURES = {
+    "fem_gpu_abi_version": (I32, []),
+    "fem_gpu_status_string": (C.c_char_p, [I32]),
+    "fem_gpu_device_count": (I32, []),
+    "fem_hmr_uniform_mesh": (I32, [I32, P, P, I32, P]),
+    "fem_hmr_mesh_sizes": (I32, [P, P, P, P, P]),
+    "fem_hmr_mesh_arrays": (I32, [P, P, P, P, P, P]),
+    "fem_hmr_mesh_free": (I32, [P]),
+    "fem_gpu_create": (I32, [P, P]),
+    "fem_gpu_destroy": (I32, [P]),
+    "fem_gpu_set_stream": (I32, [P, P]),
+    "fem_gpu_add_bulk_set": (I32, [P, P, P]),
+    "fem_gpu_add_side_set": (I32, [P, P, P]),
+    "fem_gpu_finalize": (I32, [P]),
+    "fem_gpu_finalize_host": (I32, [P]),
+    "fem_gpu_get_sizes": (I32, [P, P, P, P]),
+    "fem_gpu_get_num_equation_objects": (I32, [P, I32, P]),
+    "fem_gpu_get_max_element_adofs": (I32, [P, I32, P]),
+    "fem_gpu_build_graph": (I32, [P, P, P, U32]),
+    "fem_gpu_get_element_topology": (I32, [P, I32, I64, P, P]),
+    "fem_gpu_element_matrices": (I32, [P, I32, I64, I64, P, P, P, U32]),
+    "fem_gpu_assemble": (I32, [P, P, P, P, U32]),
+    "fem_gpu_apply": (I32, [P, P, P, U32]),
+    "fem_gpu_pcg": (I32, [P, P, P, P, P, P, P, P, U32]),
+    "fem_gpu_probe_fp64_tflops": (I32, [I32, P]),
+    "fem_gpu_launch_count": (I64, [P]),
+    "fem_gpu_last_error": (C.c_char_p, [P]),
+}
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libfem_gpu.so is not built (%s); run moris_gb300/build.py" % LIB_PATH)
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib

@@ -1,0 +1,1187 @@
+// fem_device.cu -- device memory, the element kernels and the C ABI entry
+// points that launch them.
+//
+// Bulk elasticity (IWG_Isotropic_Struc_Linear_Bulk + CM_Struc_Linear_
+// Isotropic, FEM/INT/src/IWG/cl_FEM_IWG_Isotropic_Struc_Linear_Bulk.cpp:42-207)
+// is evaluated one element per warp.  GB300 issues FP64 at a small fraction of
+// its FP32 rate, so the kernel is built to minimise FP64 instructions rather
+// than to mirror the reference's dense products:
+//
+//   per Gauss point   g = J^-1 dN/dxi, w* = w detJ          (lane per GP)
+//   Gram matrix       A[(i,a),(j,b)] = sum_q w*_q g_ia g_jb  (upper triangle)
+//   isotropic K       K[(f,a),(g,b)] = lam A[(f,a),(g,b)] + mu A[(g,a),(f,b)]
+//                                      + mu delta_fg sum_k A[(k,a),(k,b)]
+//   extraction        KT = K T, K_a = T^T KT over the column-sparse T
+//   scatter           red.global.add.f64 into CSR at
+//                     rowptr[f*nu+b_i] + g*|U(b_i)| + sidx[i][j]
+//
+// which equals w B^T D B summed over Gauss points (the reference's
+// CM_Struc_Linear::testStrain/dFluxdDOF products, cl_FEM_CM_Struc_Linear.cpp:
+// 503-826) and the reference's T^T K T (FEM/MSI/src/cl_MSI_Equation_Object.
+// cpp:806-841) up to rounding.  The residual of the linear IWG is R = K u.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fem_internal.hpp"
+#include "fem_shape.hpp"
+
+namespace fem {
+
+// ---------------------------------------------------------------------------
+// device buffers
+namespace {
+
+fem_gpu_status cuda_fail(fem_gpu_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? FEM_GPU_OUT_OF_MEMORY : FEM_GPU_CUDA_ERROR,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void dfree(DeviceBuf& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+template <class T>
+cudaError_t upload(DeviceBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    dfree(b);
+    b.bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    cudaError_t e = cudaMalloc(&b.p, b.bytes);
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) e = cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+    return e;
+}
+
+cudaStream_t stream_of(const fem_gpu_ctx* c) { return (cudaStream_t)c->stream; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// bulk kernel
+constexpr int kMaxGP = 32;
+
+struct BulkArgs {
+    int64_t ne;
+    int64_t first;        // first equation object (element-matrix mode)
+    const double* xe;     // [ne][NPE][D]
+    const double* E;      // [ne]
+    const int32_t* nb;    // [ne]
+    const int32_t* bases; // [ne][NB]
+    const double* T;      // [ne][NPE][NB]
+    const uint16_t* sidx; // [ne][NB][NB]
+    const int32_t* rowptr;
+    const int32_t* ulen;
+    const double* dn;     // [NGP][D][NPE]
+    const double* w;      // [NGP]
+    int64_t nu;
+    double lam_c, mu_c;   // lambda / E and mu / E
+    const double* u;      // adof vector (nullable)
+    double* vals;         // CSR values (nullable)
+    double* rhs;          // residual (nullable)
+    double* Kout;         // element matrices [count][nmax][nmax] col-major (nullable)
+    double* Rout;         // element residuals [count][nmax]
+    int nmax;
+    const double* x;      // apply mode input (adof)
+    double* y;            // apply mode output (adof)
+    int* status;          // device error flags
+};
+
+template <int D, int NPE, int NGP, int NB>
+struct BulkLayout {
+    static constexpr int NPD = D * NPE;
+    static constexpr int NAD = D * NB;
+    static constexpr int NSYM = NPD * (NPD + 1) / 2;
+    static constexpr int R1 = (2 * NGP * NPD > NPD * NAD) ? 2 * NGP * NPD : NPD * NAD;
+    // doubles
+    static constexpr int oX = 0;
+    static constexpr int oR1 = oX + NPE * D;
+    static constexpr int oA = oR1 + R1;
+    static constexpr int oK = oA + NPD * NPD;
+    static constexpr int oT = oK + NPD * NPD;
+    static constexpr int oTW = oT + NPE * NB;
+    static constexpr int oU = oTW + NB * NPE;
+    static constexpr int oUA = oU + NPD;
+    static constexpr int oRP = oUA + NAD;
+    static constexpr int oW = oRP + NPD;
+    static constexpr int ND = oW + NGP;
+    // 4-byte ints
+    static constexpr int iB = 0;             // bases [NB]
+    static constexpr int iRB = iB + NB;      // rowptr of row (f,i) [NAD]
+    static constexpr int iUL = iRB + NAD;    // |U(b_i)| [NB]
+    static constexpr int NI = iUL + NB;
+    // bytes
+    static constexpr int bTN = 0;            // column-sparse T node ids [NB][NPE] (u8)
+    static constexpr int bTC = bTN + NB * NPE;  // counts [NB]
+    static constexpr int bS = ((bTC + NB + 1) / 2) * 2;  // sidx [NB][NB] (u16)
+    static constexpr int NBYTE = bS + 2 * NB * NB;
+    // per-warp region, a 16-byte multiple so every warp's doubles stay aligned
+    static constexpr size_t kWarpBytes = ((size_t)ND * 8 + (size_t)NI * 4 + (size_t)NBYTE + 15) / 16 * 16;
+    // per CTA: dn table, weights, sym pair table (16-byte multiple)
+    static constexpr size_t kCtaBytes = (((size_t)(NGP * D * NPE + NGP) * 8 + (size_t)NSYM * 2 * 2) + 15) / 16 * 16;
+};
+
+static_assert(BulkLayout<3, 8, 27, 27>::kWarpBytes % 16 == 0, "warp region alignment");
+static_assert(BulkLayout<2, 4, 4, 9>::kWarpBytes % 16 == 0, "warp region alignment");
+
+enum { MODE_ASSEMBLE = 0, MODE_ELEMENT = 1, MODE_APPLY = 2 };
+
+template <int D, int NPE, int NGP, int NB, bool RECT>
+__global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int warps_per_cta) {
+    using L = BulkLayout<D, NPE, NGP, NB>;
+    constexpr int NPD = L::NPD, NAD = L::NAD, NSYM = L::NSYM;
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* cdn = reinterpret_cast<double*>(smem);
+    double* cw = cdn + NGP * D * NPE;
+    uint16_t* pairs = reinterpret_cast<uint16_t*>(cw + NGP);
+    // CTA tables
+    for (int i = threadIdx.x; i < NGP * D * NPE; i += blockDim.x) cdn[i] = p.dn[i];
+    for (int i = threadIdx.x; i < NGP; i += blockDim.x) cw[i] = p.w[i];
+    for (int k = threadIdx.x; k < NSYM; k += blockDim.x) {
+        // k-th pair of the upper triangle, row-major: (r, c) with r <= c
+        int r = 0, rem = k;
+        while (rem >= NPD - r) {
+            rem -= NPD - r;
+            ++r;
+        }
+        pairs[2 * k] = (uint16_t)r;
+        pairs[2 * k + 1] = (uint16_t)(r + rem);
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wbase = smem + L::kCtaBytes + (size_t)warp * L::kWarpBytes;
+    double* sd = reinterpret_cast<double*>(wbase);
+    int32_t* si = reinterpret_cast<int32_t*>(sd + L::ND);
+    unsigned char* sb = reinterpret_cast<unsigned char*>(si + L::NI);
+    double* X = sd + L::oX;
+    double* R1 = sd + L::oR1;
+    double* g = R1;                  // [NGP][NPD]
+    double* wg = R1 + NGP * NPD;     // [NGP][NPD]
+    double* KT = R1;                 // [NPD][NAD] (after A is formed)
+    double* A = sd + L::oA;
+    double* K = sd + L::oK;
+    double* T = sd + L::oT;
+    double* TW = sd + L::oTW;        // [NB][NPE]
+    double* U = sd + L::oU;          // pdof values [NPD]
+    double* UA = sd + L::oUA;        // adof values [NAD]
+    double* RP = sd + L::oRP;        // pdof residual [NPD]
+    double* WS = sd + L::oW;         // w* per GP
+    int32_t* B = si + L::iB;
+    int32_t* RB = si + L::iRB;
+    int32_t* UL = si + L::iUL;
+    uint8_t* TN = sb + L::bTN;
+    uint8_t* TC = sb + L::bTC;
+    uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
+
+    const int64_t stride = (int64_t)gridDim.x * warps_per_cta;
+    for (int64_t e = (int64_t)blockIdx.x * warps_per_cta + warp; e < p.ne; e += stride) {
+        const int nb = p.nb[e];
+        const double E = p.E[e];
+        // ---- loads -------------------------------------------------------
+        for (int i = lane; i < NPE * D; i += 32) X[i] = p.xe[e * (NPE * D) + i];
+        for (int i = lane; i < NPE * NB; i += 32) T[i] = p.T[e * (NPE * NB) + i];
+        for (int i = lane; i < NB; i += 32) B[i] = p.bases[e * NB + i];
+        if (mode == MODE_ASSEMBLE && p.vals)
+            for (int i = lane; i < NB * NB; i += 32) S[i] = p.sidx[e * (NB * NB) + i];
+        __syncwarp();
+        if (mode == MODE_ASSEMBLE) {
+            for (int r = lane; r < NAD; r += 32) {
+                const int f = r / NB, i = r - f * NB;
+                RB[r] = i < nb ? p.rowptr[f * p.nu + B[i]] : 0;
+            }
+            for (int i = lane; i < NB; i += 32) UL[i] = i < nb ? p.ulen[B[i]] : 0;
+        }
+        const double* uin = mode == MODE_APPLY ? p.x : p.u;
+        for (int r = lane; r < NAD; r += 32) {
+            const int f = r / NB, i = r - f * NB;
+            UA[r] = (uin && i < nb) ? uin[f * p.nu + B[i]] : 0.0;
+        }
+        // column-sparse extraction lists
+        for (int j = lane; j < NB; j += 32) {
+            int cnt = 0;
+            for (int a = 0; a < NPE; ++a) {
+                const double t = T[a * NB + j];
+                if (t != 0.0) {
+                    TN[j * NPE + cnt] = (uint8_t)a;
+                    TW[j * NPE + cnt] = t;
+                    ++cnt;
+                }
+            }
+            TC[j] = (uint8_t)cnt;
+        }
+        // ---- Gauss-point geometry: g = J^-1 dN/dxi, w* = w detJ ----------
+        for (int q = lane; q < NGP; q += 32) {
+            const double* dn = cdn + q * D * NPE;
+            double detJ;
+            double Ji[D][D];
+            if (RECT) {
+                double jd[D];
+                for (int i = 0; i < D; ++i) {
+                    double s = 0.0;
+                    for (int a = 0; a < NPE; ++a) s = fma(dn[i * NPE + a], X[a * D + i], s);
+                    jd[i] = s;
+                }
+                detJ = (D == 3) ? jd[1] * jd[0] * jd[2] : jd[0] * jd[1];
+                for (int i = 0; i < D; ++i)
+                    for (int j = 0; j < D; ++j) Ji[i][j] = (i == j) ? 1.0 / jd[i] : 0.0;
+            } else {
+                double J[D][D];
+                for (int i = 0; i < D; ++i)
+                    for (int j = 0; j < D; ++j) {
+                        double s = 0.0;
+                        for (int a = 0; a < NPE; ++a) s = fma(dn[i * NPE + a], X[a * D + j], s);
+                        J[i][j] = s;
+                    }
+                if (D == 2) {
+                    detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+                    const double id = 1.0 / detJ;
+                    Ji[0][0] = J[1][1] * id;
+                    Ji[0][1] = -J[0][1] * id;
+                    Ji[1][0] = -J[1][0] * id;
+                    Ji[1][1] = J[0][0] * id;
+                } else {
+                    detJ = +J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+                    const double id = 1.0 / detJ;
+                    Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
+                    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+                    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+                    Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+                    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+                    Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
+                    Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+                    Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
+                    Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+                }
+            }
+            // integration points with detJ below -1e-6 are skipped by the
+            // reference element loop (cl_FEM_Element_Bulk.cpp:164)
+            const double ws = (detJ < -1.0e-6) ? 0.0 : cw[q] * detJ;
+            WS[q] = ws;
+            for (int i = 0; i < D; ++i)
+                for (int a = 0; a < NPE; ++a) {
+                    double s;
+                    if (RECT) {
+                        s = Ji[i][i] * dn[i * NPE + a];
+                    } else {
+                        s = 0.0;
+                        for (int k = 0; k < D; ++k) s = fma(Ji[i][k], dn[k * NPE + a], s);
+                    }
+                    g[q * NPD + i * NPE + a] = s;
+                    wg[q * NPD + i * NPE + a] = ws * s;
+                }
+        }
+        __syncwarp();
+        // pdof values u = T u_a (compute_my_pdof_values)
+        for (int r = lane; r < NPD; r += 32) {
+            const int f = r / NPE, a = r - f * NPE;
+            double s = 0.0;
+            for (int j = 0; j < nb; ++j) {
+                const double t = T[a * NB + j];
+                if (t != 0.0) s = fma(t, UA[f * NB + j], s);
+            }
+            U[r] = s;
+        }
+        if (mode == MODE_APPLY) {
+            // matrix-free: per GP stress sigma = lam tr(grad u) I + mu (grad u + grad u^T),
+            // stored as w* sigma in A ([q][f][i]); then f_(f,a) = sum_q sum_i g_ia (w sigma)_fi
+            __syncwarp();
+            for (int q = lane; q < NGP; q += 32) {
+                double G[D][D];
+                for (int f = 0; f < D; ++f)
+                    for (int i = 0; i < D; ++i) {
+                        double s = 0.0;
+                        for (int a = 0; a < NPE; ++a) s = fma(g[q * NPD + i * NPE + a], U[f * NPE + a], s);
+                        G[f][i] = s;  // du_f / dx_i
+                    }
+                double tr = 0.0;
+                for (int k = 0; k < D; ++k) tr += G[k][k];
+                const double lam = E * p.lam_c, mu = E * p.mu_c, ws = WS[q];
+                for (int f = 0; f < D; ++f)
+                    for (int i = 0; i < D; ++i)
+                        A[q * D * D + f * D + i] = ws * ((f == i ? lam * tr : 0.0) + mu * (G[f][i] + G[i][f]));
+            }
+            __syncwarp();
+            for (int r = lane; r < NPD; r += 32) {
+                const int f = r / NPE, a = r - f * NPE;
+                double s = 0.0;
+                for (int q = 0; q < NGP; ++q)
+                    for (int i = 0; i < D; ++i) s = fma(g[q * NPD + i * NPE + a], A[q * D * D + f * D + i], s);
+                RP[r] = s;
+            }
+            __syncwarp();
+            for (int r = lane; r < NAD; r += 32) {
+                const int f = r / NB, i = r - f * NB;
+                if (i >= nb) continue;
+                double s = 0.0;
+                for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
+                atomicAdd(p.y + f * p.nu + B[i], s);
+            }
+            __syncwarp();
+            continue;
+        }
+        // ---- Gram matrix (upper triangle) --------------------------------
+        for (int k = lane; k < NSYM; k += 32) {
+            const int r = pairs[2 * k], c = pairs[2 * k + 1];
+            double s = 0.0;
+#pragma unroll 9
+            for (int q = 0; q < NGP; ++q) s = fma(wg[q * NPD + r], g[q * NPD + c], s);
+            A[r * NPD + c] = s;
+            A[c * NPD + r] = s;
+        }
+        __syncwarp();
+        // ---- isotropic element stiffness (pdof space) ----------------------
+        {
+            const double lam = E * p.lam_c, mu = E * p.mu_c;
+            for (int k = lane; k < NSYM; k += 32) {
+                const int r = pairs[2 * k], c = pairs[2 * k + 1];
+                const int f = r / NPE, a = r - f * NPE, gg = c / NPE, b = c - gg * NPE;
+                double v = lam * A[r * NPD + c] + mu * A[(gg * NPE + a) * NPD + f * NPE + b];
+                if (f == gg) {
+                    double tr = 0.0;
+                    for (int kk = 0; kk < D; ++kk) tr += A[(kk * NPE + a) * NPD + kk * NPE + b];
+                    v = fma(mu, tr, v);
+                }
+                K[r * NPD + c] = v;
+                K[c * NPD + r] = v;
+            }
+        }
+        __syncwarp();
+        // ---- residual R_a = T^T (K u) --------------------------------------
+        const bool want_r = (mode == MODE_ASSEMBLE && p.rhs) || (mode == MODE_ELEMENT && p.Rout);
+        if (want_r) {
+            for (int r = lane; r < NPD; r += 32) {
+                double s = 0.0;
+                for (int c = 0; c < NPD; ++c) s = fma(K[r * NPD + c], U[c], s);
+                RP[r] = s;
+            }
+            __syncwarp();
+            for (int r = lane; r < NAD; r += 32) {
+                const int f = r / NB, i = r - f * NB;
+                double s = 0.0;
+                if (i < nb)
+                    for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
+                if (mode == MODE_ASSEMBLE) {
+                    if (i < nb) atomicAdd(p.rhs + f * p.nu + B[i], s);
+                } else {
+                    p.Rout[(e - p.first) * p.nmax + r] = s;
+                }
+            }
+        }
+        const bool want_k = (mode == MODE_ASSEMBLE && p.vals) || (mode == MODE_ELEMENT && p.Kout);
+        if (!want_k) {
+            __syncwarp();
+            continue;
+        }
+        // ---- KT = K T (column-sparse T) ------------------------------------
+        {
+            constexpr int CPP = NPD >= 32 ? 1 : 32 / NPD;  // columns per pass
+            const int row = lane % NPD, sub = lane / NPD;
+            if (row < NPD && sub < CPP && lane < CPP * NPD) {
+                for (int c0 = 0; c0 < NAD; c0 += CPP) {
+                    const int c = c0 + sub;
+                    if (c >= NAD) break;
+                    const int gg = c / NB, j = c - gg * NB;
+                    double s = 0.0;
+                    const int cnt = j < nb ? TC[j] : 0;
+                    for (int k = 0; k < cnt; ++k)
+                        s = fma(K[row * NPD + gg * NPE + TN[j * NPE + k]], TW[j * NPE + k], s);
+                    KT[row * NAD + c] = s;
+                }
+            }
+        }
+        __syncwarp();
+        // ---- K_a = T^T KT (upper triangle) and scatter ----------------------
+        bool bad = false;
+        for (int r = 0; r < NAD; ++r) {
+            const int f = r / NB, i = r - f * NB;
+            if (i >= nb) continue;
+            const int cnt = TC[i];
+            for (int c = r + lane; c < NAD; c += 32) {
+                const int gg = c / NB, j = c - gg * NB;
+                if (j >= nb) continue;
+                double v = 0.0;
+                for (int k = 0; k < cnt; ++k) v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + c], v);
+                bad |= !isfinite(v);
+                if (mode == MODE_ASSEMBLE) {
+                    atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
+                    if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
+                } else {
+                    double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
+                    Ko[r + (int64_t)c * p.nmax] = v;
+                    Ko[c + (int64_t)r * p.nmax] = v;
+                }
+            }
+        }
+        if (bad) atomicOr(p.status, 1);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// side sets (Neumann traction, Nitsche Dirichlet) on interpolation-cell
+// facets: one thread per facet (these sets are small: the boundary of the
+// mesh).  Element_Sideset (FEM/INT/src/ELEM/cl_FEM_Element_Sideset.cpp:
+// 261-330), IWG_Isotropic_Struc_Linear_Neumann (:38) and _Dirichlet (:52-240),
+// SP_Dirichlet_Nitsche (gamma = alpha E / h).
+struct SideArgs {
+    int64_t ns;
+    int iwg, model, ngp, maxnb;
+    const double* xe;
+    const double* E;
+    const int32_t* ord;
+    const int32_t* nb;
+    const int32_t* bases;
+    const double* T;
+    const uint16_t* sidx;
+    const int32_t* rowptr;
+    const int32_t* ulen;
+    const double* gp;   // [ngp] facet Gauss points (dim-1 coords each)
+    const double* gw;   // [ngp]
+    int64_t nu;
+    double nu_p, alpha;
+    double value[3];
+    const double* u;
+    double* vals;
+    double* rhs;
+    double* Kout;
+    double* Rout;
+    int nmax;
+    int64_t first;
+    int mode;
+    int* status;
+};
+
+template <int D>
+__global__ void side_kernel(SideArgs p) {
+    constexpr int NPE = D == 2 ? 4 : 8, NPD = D * NPE, NS = D == 2 ? 4 : 6;
+    constexpr int NFV = D == 2 ? 2 : 4;
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= p.ns) return;
+    const int nb = p.nb[s];
+    const int ord = p.ord[s];
+    const int quad_f[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+    const int hex_f[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+    double X[NPE * D], XI[NPE * D];
+    for (int i = 0; i < NPE * D; ++i) X[i] = p.xe[s * NPE * D + i];
+    for (int a = 0; a < NPE; ++a) {
+        XI[a * D + 0] = ((a & 3) == 1 || (a & 3) == 2) ? 1.0 : -1.0;
+        XI[a * D + 1] = ((a & 3) >= 2) ? 1.0 : -1.0;
+        if (D == 3) XI[a * D + 2] = a >= 4 ? 1.0 : -1.0;
+    }
+    int fv[NFV];
+    for (int k = 0; k < NFV; ++k) fv[k] = D == 2 ? quad_f[ord][k] : hex_f[ord][k];
+    const double E = p.E[s];
+    double lam_c, mu_c = 1.0 / (2.0 * (1.0 + p.nu_p));
+    if (p.model == FEM_GPU_MODEL_PLANE_STRESS) lam_c = p.nu_p / (1.0 - p.nu_p * p.nu_p);
+    else lam_c = p.nu_p / ((1.0 + p.nu_p) * (1.0 - 2.0 * p.nu_p));
+    const double lam = E * lam_c, mu = E * mu_c;
+    // pdof values
+    double U[NPD];
+    for (int f = 0; f < D; ++f)
+        for (int a = 0; a < NPE; ++a) {
+            double v = 0.0;
+            if (p.u)
+                for (int j = 0; j < nb; ++j) {
+                    const double t = p.T[(s * NPE + a) * p.maxnb + j];
+                    if (t != 0.0) v = fma(t, p.u[f * p.nu + p.bases[s * p.maxnb + j]], v);
+                }
+            U[f * NPE + a] = v;
+        }
+    double K[NPD * NPD], R[NPD];
+    for (int i = 0; i < NPD * NPD; ++i) K[i] = 0.0;
+    for (int i = 0; i < NPD; ++i) R[i] = 0.0;
+    // facet geometry per Gauss point
+    auto facet = [&](int q, double* xip, double& detJ, double* nrm) {
+        double Nf[4], dNf[8];
+        const double* xq = p.gp + q * (D - 1);
+        if (D == 2) Shape<4>::eval(xq, Nf, dNf);
+        else Shape<0>::eval(xq, Nf, dNf);
+        double t[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        for (int d = 0; d < D; ++d) xip[d] = 0.0;
+        for (int k = 0; k < NFV; ++k) {
+            for (int d = 0; d < D; ++d) {
+                xip[d] = fma(Nf[k], XI[fv[k] * D + d], xip[d]);
+                for (int m = 0; m < D - 1; ++m) t[m][d] = fma(dNf[m * NFV + k], X[fv[k] * D + d], t[m][d]);
+            }
+        }
+        if (D == 2) {
+            detJ = sqrt(t[0][0] * t[0][0] + t[0][1] * t[0][1]);
+            nrm[0] = t[0][1] / detJ;
+            nrm[1] = -t[0][0] / detJ;
+        } else {
+            const double c0 = t[0][1] * t[1][2] - t[0][2] * t[1][1];
+            const double c1 = t[0][2] * t[1][0] - t[0][0] * t[1][2];
+            const double c2 = t[0][0] * t[1][1] - t[0][1] * t[1][0];
+            detJ = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+            nrm[0] = c0 / detJ;
+            nrm[1] = c1 / detJ;
+            nrm[2] = c2 / detJ;
+        }
+    };
+    double meas = 0.0;
+    for (int q = 0; q < p.ngp; ++q) {
+        double xip[3], dj, nrm[3];
+        facet(q, xip, dj, nrm);
+        meas += p.gw[q] * dj;
+    }
+    const double h = D == 2 ? meas : sqrt(4.0 * meas / 3.14159265358979323846);
+    const double gamma = p.alpha * E / h;
+    const double beta = p.iwg == FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
+    for (int q = 0; q < p.ngp; ++q) {
+        double xip[3], detJ, nrm[3] = {0, 0, 0};
+        facet(q, xip, detJ, nrm);
+        if (detJ < -1.0e-6) continue;
+        const double ws = p.gw[q] * detJ;
+        double N[NPE], dN[NPE * D];
+        if (D == 2) Shape<0>::eval(xip, N, dN);
+        else Shape<1>::eval(xip, N, dN);
+        if (p.iwg == FEM_GPU_IWG_STRUC_LINEAR_NEUMANN) {
+            for (int f = 0; f < D; ++f)
+                for (int a = 0; a < NPE; ++a) R[f * NPE + a] -= ws * N[a] * p.value[f];
+            continue;
+        }
+        // dN/dx through the interpolation-cell Jacobian (rectangular or general)
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j)
+                for (int a = 0; a < NPE; ++a) J[i][j] = fma(dN[i * NPE + a], X[a * D + j], J[i][j]);
+        if (D == 2) {
+            const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0], id = 1.0 / det;
+            Ji[0][0] = J[1][1] * id; Ji[0][1] = -J[0][1] * id; Ji[1][0] = -J[1][0] * id; Ji[1][1] = J[0][0] * id;
+        } else {
+            const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+            const double id = 1.0 / det;
+            Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
+            Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+            Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+            Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+            Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+            Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
+            Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+            Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
+            Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+        }
+        double g[D][NPE];
+        for (int i = 0; i < D; ++i)
+            for (int a = 0; a < NPE; ++a) {
+                double v = 0.0;
+                for (int k = 0; k < D; ++k) v = fma(Ji[i][k], dN[k * NPE + a], v);
+                g[i][a] = v;
+            }
+        // traction operator (nDB)[f][(g,b)] = lam n_f g_gb + mu (n_g g_fb + delta_fg n.g_b)
+        double nDB[D][NPD];
+        for (int f = 0; f < D; ++f)
+            for (int gg = 0; gg < D; ++gg)
+                for (int b = 0; b < NPE; ++b) {
+                    double ng = 0.0;
+                    for (int k = 0; k < D; ++k) ng += nrm[k] * g[k][b];
+                    nDB[f][gg * NPE + b] = lam * nrm[f] * g[gg][b] + mu * (nrm[gg] * g[f][b] + (f == gg ? ng : 0.0));
+                }
+        double trac[D], jump[D];
+        for (int f = 0; f < D; ++f) {
+            double t = 0.0, uu = 0.0;
+            for (int c = 0; c < NPD; ++c) t = fma(nDB[f][c], U[c], t);
+            for (int a = 0; a < NPE; ++a) uu = fma(N[a], U[f * NPE + a], uu);
+            trac[f] = t;
+            jump[f] = uu - p.value[f];
+        }
+        for (int f = 0; f < D; ++f)
+            for (int a = 0; a < NPE; ++a) {
+                const int r = f * NPE + a;
+                double v = -N[a] * trac[f] + gamma * N[a] * jump[f];
+                for (int k = 0; k < D; ++k) v += beta * nDB[k][r] * jump[k];
+                R[r] += ws * v;
+            }
+        for (int r = 0; r < NPD; ++r) {
+            const int f = r / NPE, a = r % NPE;
+            for (int c = 0; c < NPD; ++c) {
+                const int gg = c / NPE, b = c % NPE;
+                double v = beta * nDB[gg][r] * N[b] - N[a] * nDB[f][c];
+                if (f == gg) v += gamma * N[a] * N[b];
+                K[r * NPD + c] += ws * v;
+            }
+        }
+    }
+    (void)NS;
+    // extraction and scatter
+    const int maxnb = p.maxnb;
+    const int32_t* bs = p.bases + s * maxnb;
+    const double* Ts = p.T + s * NPE * maxnb;
+    for (int f = 0; f < D; ++f)
+        for (int i = 0; i < nb; ++i) {
+            double ra = 0.0;
+            for (int a = 0; a < NPE; ++a) ra = fma(Ts[a * maxnb + i], R[f * NPE + a], ra);
+            if (p.mode == MODE_ASSEMBLE) {
+                if (p.rhs) atomicAdd(p.rhs + f * p.nu + bs[i], ra);
+            } else if (p.Rout) {
+                p.Rout[(s - p.first) * p.nmax + f * maxnb + i] = ra;
+            }
+        }
+    if ((p.mode == MODE_ASSEMBLE && !p.vals) || (p.mode == MODE_ELEMENT && !p.Kout)) return;
+    bool bad = false;
+    for (int f = 0; f < D; ++f)
+        for (int i = 0; i < nb; ++i) {
+            const int32_t rbase = p.rowptr[f * p.nu + bs[i]];
+            const int32_t ul = p.ulen[bs[i]];
+            for (int gg = 0; gg < D; ++gg)
+                for (int j = 0; j < nb; ++j) {
+                    double v = 0.0;
+                    for (int a = 0; a < NPE; ++a) {
+                        const double ta = Ts[a * maxnb + i];
+                        if (ta == 0.0) continue;
+                        double kt = 0.0;
+                        for (int b = 0; b < NPE; ++b) kt = fma(K[(f * NPE + a) * NPD + gg * NPE + b], Ts[b * maxnb + j], kt);
+                        v = fma(ta, kt, v);
+                    }
+                    bad |= !isfinite(v);
+                    if (p.mode == MODE_ASSEMBLE)
+                        atomicAdd(p.vals + rbase + gg * ul + p.sidx[(s * maxnb + i) * maxnb + j], v);
+                    else
+                        p.Kout[(s - p.first) * (int64_t)p.nmax * p.nmax + (f * maxnb + i) + (int64_t)(gg * maxnb + j) * p.nmax] = v;
+                }
+        }
+    if (bad) atomicOr(p.status, 1);
+}
+
+// ---------------------------------------------------------------------------
+// launch plumbing
+struct BulkLaunch {
+    const void* fn;
+    size_t cta_bytes, warp_bytes;
+};
+
+template <int D, int NPE, int NGP, int NB, bool RECT>
+BulkLaunch bulk_launch() {
+    using L = BulkLayout<D, NPE, NGP, NB>;
+    return {(const void*)bulk_kernel<D, NPE, NGP, NB, RECT>, L::kCtaBytes, L::kWarpBytes};
+}
+
+bool pick_bulk(int dim, int ngp, int nb, bool rect, BulkLaunch& out, int& NBsel) {
+#define FEM_PICK(D, NPE, NGP, NB)                                                          \
+    if (dim == D && ngp == NGP && nb <= NB) {                                              \
+        out = rect ? bulk_launch<D, NPE, NGP, NB, true>() : bulk_launch<D, NPE, NGP, NB, false>(); \
+        NBsel = NB;                                                                        \
+        return true;                                                                       \
+    }
+    FEM_PICK(2, 4, 4, 4)
+    FEM_PICK(2, 4, 4, 9)
+    FEM_PICK(2, 4, 4, 16)
+    FEM_PICK(3, 8, 8, 8)
+    FEM_PICK(3, 8, 8, 27)
+    FEM_PICK(3, 8, 27, 8)
+    FEM_PICK(3, 8, 27, 27)
+#undef FEM_PICK
+    return false;
+}
+
+}  // namespace fem
+
+// ===========================================================================
+using namespace fem;
+
+namespace {
+
+fem_gpu_status check_kernel(fem_gpu_ctx* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(c, e, what);
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status ensure_device(fem_gpu_ctx* c) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(c, FEM_GPU_NO_DEVICE, "no CUDA device");
+    }
+    if (!c->stream) {
+        cudaStream_t s;
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(c, e, "stream create");
+        c->stream = s;
+        c->own_stream = true;
+    }
+    // keep stream-ordered staging buffers cached between calls (host-buffer
+    // entry points allocate and free them on every call)
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+    return FEM_GPU_OK;
+}
+
+// A buffer argument: device pointer as given, or a staging copy for host data.
+struct Staged {
+    void* dev = nullptr;
+    bool owned = false;
+};
+
+fem_gpu_status stage_in(fem_gpu_ctx* c, const void* host_or_dev, size_t bytes, bool host, Staged& s) {
+    s = Staged{};
+    if (!host_or_dev) return FEM_GPU_OK;
+    if (!host) {
+        s.dev = const_cast<void*>(host_or_dev);
+        return FEM_GPU_OK;
+    }
+    cudaError_t e = cudaMallocAsync(&s.dev, std::max<size_t>(bytes, 16), stream_of(c));
+    if (e != cudaSuccess) return cuda_fail(c, e, "staging alloc");
+    s.owned = true;
+    e = cudaMemcpyAsync(s.dev, host_or_dev, bytes, cudaMemcpyHostToDevice, stream_of(c));
+    if (e != cudaSuccess) return cuda_fail(c, e, "staging copy");
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status stage_out_alloc(fem_gpu_ctx* c, void* host_or_dev, size_t bytes, bool host, Staged& s) {
+    s = Staged{};
+    if (!host_or_dev) return FEM_GPU_OK;
+    if (!host) {
+        s.dev = host_or_dev;
+        return FEM_GPU_OK;
+    }
+    cudaError_t e = cudaMallocAsync(&s.dev, std::max<size_t>(bytes, 16), stream_of(c));
+    if (e != cudaSuccess) return cuda_fail(c, e, "staging alloc");
+    s.owned = true;
+    return FEM_GPU_OK;
+}
+
+void release(fem_gpu_ctx* c, Staged& s) {
+    if (s.owned && s.dev) cudaFreeAsync(s.dev, stream_of(c));
+    s = Staged{};
+}
+
+int* status_ptr(fem_gpu_ctx* c) { return (int*)c->d_status.p; }
+
+fem_gpu_status read_status(fem_gpu_ctx* c) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, c->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, stream_of(c));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream_of(c));
+    if (e != cudaSuccess) return cuda_fail(c, e, "status read");
+    if (h & 1) return fail(c, FEM_GPU_NONFINITE, "non-finite element operator");
+    return FEM_GPU_OK;
+}
+
+double lam_coef(int model, double nu) {
+    return model == FEM_GPU_MODEL_PLANE_STRESS ? nu / (1.0 - nu * nu) : nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+}
+
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+// Tuning of the bulk launch: warps per CTA (chosen per set by the autotuner
+// in fem_tune.cu; default 4).
+int g_bulk_warps = 4;
+
+fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int64_t count, const double* u,
+                           double* vals, double* rhs, double* Kout, double* Rout, int nmax, const double* x,
+                           double* y) {
+    SetData& s = c->sets[si];
+    SetData& ds = s;
+    BulkLaunch L;
+    int nbsel = 0;
+    const bool rect = c->shape == FEM_GPU_SHAPE_RECTANGULAR;
+    if (!s.ig_off.empty()) return fail(c, FEM_GPU_UNSUPPORTED, "non-trivial clusters use the cut-cell kernel");
+    if (!pick_bulk(c->dim, ds.ngp, s.maxnb, rect, L, nbsel) || nbsel != ds.nbsel)
+        return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
+    BulkArgs a{};
+    a.ne = first + count;
+    a.first = first;
+    a.xe = (const double*)s.d_xe.p;
+    a.E = (const double*)s.d_E.p;
+    a.nb = (const int32_t*)s.d_nb.p;
+    a.bases = (const int32_t*)s.d_bases.p;
+    a.T = (const double*)s.d_T.p;
+    a.sidx = (const uint16_t*)s.d_sidx.p;
+    a.rowptr = (const int32_t*)c->d_rowptr.p;
+    a.ulen = (const int32_t*)c->d_ulen.p;
+    a.dn = (const double*)ds.d_dn.p;
+    a.w = (const double*)ds.d_w.p;
+    a.nu = c->num_used;
+    a.lam_c = lam_coef(s.bulk.model_type, s.bulk.poisson_ratio);
+    a.mu_c = 1.0 / (2.0 * (1.0 + s.bulk.poisson_ratio));
+    a.u = u;
+    a.vals = vals;
+    a.rhs = rhs;
+    a.Kout = Kout;
+    a.Rout = Rout;
+    a.nmax = nmax;
+    a.x = x;
+    a.y = y;
+    a.status = status_ptr(c);
+    const int W = g_bulk_warps;
+    const size_t smem = L.cta_bytes + (size_t)W * L.warp_bytes;
+    cudaError_t e = cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bulk smem attribute");
+    // elements [first, first+count): the kernel walks e from first via the
+    // grid stride, so offset the block start through ne/first bookkeeping
+    int64_t blocks = (count + W - 1) / W;
+    const int64_t cap = (int64_t)sm_count() * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    // shift pointers so that element index 0 of the kernel is `first`
+    if (first > 0) {
+        const int NPE = c->npe, D = c->dim;
+        a.xe += first * NPE * D;
+        a.E += first;
+        a.nb += first;
+        a.bases += first * nbsel;
+        a.T += first * NPE * nbsel;
+        a.sidx += first * nbsel * nbsel;
+        a.ne = count;
+        a.first = 0;
+    }
+    void* args[] = {&a, &mode, (void*)&W};
+    e = cudaLaunchKernel(L.fn, dim3((unsigned)blocks), dim3(32 * W), args, smem, stream_of(c));
+    if (e != cudaSuccess) return cuda_fail(c, e, "bulk launch");
+    c->launches++;
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int64_t count, const double* u,
+                           double* vals, double* rhs, double* Kout, double* Rout, int nmax) {
+    SetData& s = c->sets[si];
+    SetData& ds = s;
+    SideArgs a{};
+    a.ns = count;
+    a.iwg = s.side.iwg_type;
+    a.model = s.side.model_type;
+    a.ngp = ds.ngp;
+    a.maxnb = s.maxnb;
+    const int NPE = c->npe, D = c->dim;
+    a.xe = (const double*)s.d_xe.p + first * NPE * D;
+    a.E = (const double*)s.d_E.p + first;
+    a.ord = (const int32_t*)s.d_ord.p + first;
+    a.nb = (const int32_t*)s.d_nb.p + first;
+    a.bases = (const int32_t*)s.d_bases.p + first * s.maxnb;
+    a.T = (const double*)s.d_T.p + first * NPE * s.maxnb;
+    a.sidx = (const uint16_t*)s.d_sidx.p + first * s.maxnb * s.maxnb;
+    a.rowptr = (const int32_t*)c->d_rowptr.p;
+    a.ulen = (const int32_t*)c->d_ulen.p;
+    a.gp = (const double*)ds.d_gp.p;
+    a.gw = (const double*)ds.d_gw.p;
+    a.nu = c->num_used;
+    a.nu_p = s.side.poisson_ratio;
+    a.alpha = s.side.nitsche_alpha;
+    for (int d = 0; d < 3; ++d) a.value[d] = s.side.value[d];
+    a.u = u;
+    a.vals = vals;
+    a.rhs = rhs;
+    a.Kout = Kout;
+    a.Rout = Rout;
+    a.nmax = nmax;
+    a.first = 0;
+    a.mode = mode;
+    a.status = status_ptr(c);
+    const int threads = 64;
+    const unsigned blocks = (unsigned)((count + threads - 1) / threads);
+    if (D == 2) side_kernel<2><<<blocks, threads, 0, stream_of(c)>>>(a);
+    else side_kernel<3><<<blocks, threads, 0, stream_of(c)>>>(a);
+    c->launches++;
+    return check_kernel(c, "side launch");
+}
+
+}  // namespace
+
+namespace fem {
+
+void device_release(fem_gpu_ctx* c) {
+    for (auto& s : c->sets) {
+        dfree(s.d_nb);
+        dfree(s.d_bases);
+        dfree(s.d_T);
+        dfree(s.d_sidx);
+        dfree(s.d_xe);
+        dfree(s.d_E);
+        dfree(s.d_ord);
+        dfree(s.d_dn);
+        dfree(s.d_w);
+        dfree(s.d_gp);
+        dfree(s.d_gw);
+    }
+    dfree(c->d_rowptr);
+    dfree(c->d_ulen);
+    dfree(c->d_tables);
+    dfree(c->d_scratch);
+    dfree(c->d_status);
+    if (c->own_stream && c->stream) cudaStreamDestroy((cudaStream_t)c->stream);
+    c->stream = nullptr;
+    c->own_stream = false;
+    c->dev_final = false;
+}
+
+fem_gpu_status device_finalize(fem_gpu_ctx* c) {
+    fem_gpu_status st = ensure_device(c);
+    if (st != FEM_GPU_OK) return st;
+    cudaStream_t sm = stream_of(c);
+    cudaError_t e;
+    if ((e = upload(c->d_rowptr, c->rowptr, sm)) != cudaSuccess) return cuda_fail(c, e, "rowptr");
+    if ((e = upload(c->d_ulen, c->ulen, sm)) != cudaSuccess) return cuda_fail(c, e, "ulen");
+    std::vector<int> zero(4, 0);
+    if ((e = upload(c->d_status, zero, sm)) != cudaSuccess) return cuda_fail(c, e, "status");
+    for (size_t k = 0; k < c->sets.size(); ++k) {
+        SetData& s = c->sets[k];
+        SetData& ds = s;
+        const int NPE = c->npe, D = c->dim;
+        if (s.kind == 0) {
+            const Rule r = gauss_rule(s.bulk.integration_rule);
+            if (r.n > kMaxGP) return fail(c, FEM_GPU_UNSUPPORTED, "too many Gauss points");
+            ds.ngp = r.n;
+            std::vector<double> dn((size_t)r.n * D * NPE), w(r.w);
+            for (int q = 0; q < r.n; ++q) {
+                double N[8], d[24];
+                lagrange(c->ip_cell, &r.pts[(size_t)q * r.dim], N, d);
+                for (int i = 0; i < D * NPE; ++i) dn[(size_t)q * D * NPE + i] = d[i];
+            }
+            if ((e = upload(ds.d_dn, dn, sm)) != cudaSuccess) return cuda_fail(c, e, "dn table");
+            if ((e = upload(ds.d_w, w, sm)) != cudaSuccess) return cuda_fail(c, e, "w table");
+            BulkLaunch L;
+            int nbsel = 0;
+            if (s.ig_off.empty() && !pick_bulk(D, r.n, s.maxnb, c->shape == FEM_GPU_SHAPE_RECTANGULAR, L, nbsel))
+                return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
+            ds.nbsel = nbsel ? nbsel : s.maxnb;
+        } else {
+            const Rule r = gauss_rule(s.side.integration_rule);
+            ds.ngp = r.n;
+            if ((e = upload(ds.d_gp, r.pts, sm)) != cudaSuccess) return cuda_fail(c, e, "side gp");
+            if ((e = upload(ds.d_gw, r.w, sm)) != cudaSuccess) return cuda_fail(c, e, "side gw");
+            ds.nbsel = s.maxnb;
+        }
+        // repack element data to the kernel's padded basis width
+        const int W = ds.nbsel;
+        std::vector<int32_t> bases((size_t)s.neq * W, -1);
+        std::vector<double> T((size_t)s.neq * NPE * W, 0.0);
+        std::vector<uint16_t> sidx((size_t)s.neq * W * W, 0);
+        for (int64_t i = 0; i < s.neq; ++i) {
+            for (int j = 0; j < s.maxnb; ++j) bases[i * W + j] = s.bases[i * s.maxnb + j];
+            for (int a = 0; a < NPE; ++a)
+                for (int j = 0; j < s.maxnb; ++j) T[(i * NPE + a) * W + j] = s.T[(i * NPE + a) * s.maxnb + j];
+            for (int ii = 0; ii < s.maxnb; ++ii)
+                for (int jj = 0; jj < s.maxnb; ++jj)
+                    sidx[(i * W + ii) * W + jj] = s.sidx[(i * s.maxnb + ii) * s.maxnb + jj];
+        }
+        if ((e = upload(s.d_nb, s.nb, sm)) != cudaSuccess) return cuda_fail(c, e, "nb");
+        if ((e = upload(s.d_bases, bases, sm)) != cudaSuccess) return cuda_fail(c, e, "bases");
+        if ((e = upload(s.d_T, T, sm)) != cudaSuccess) return cuda_fail(c, e, "T");
+        if ((e = upload(s.d_sidx, sidx, sm)) != cudaSuccess) return cuda_fail(c, e, "sidx");
+        if ((e = upload(s.d_xe, s.xe, sm)) != cudaSuccess) return cuda_fail(c, e, "xe");
+        if ((e = upload(s.d_E, s.E, sm)) != cudaSuccess) return cuda_fail(c, e, "E");
+        if (s.kind == 1)
+            if ((e = upload(s.d_ord, s.ordinal, sm)) != cudaSuccess) return cuda_fail(c, e, "ordinals");
+        if (s.kind == 1) s.maxnb = W;
+    }
+    // the side kernel and host topology read maxnb-padded arrays: keep the
+    // host copies consistent with the device padding for bulk sets too
+    for (size_t k = 0; k < c->sets.size(); ++k) {
+        SetData& s = c->sets[k];
+        const int W = s.nbsel;
+        if (s.kind == 0 && W != s.maxnb) {
+            std::vector<int32_t> b((size_t)s.neq * W, -1);
+            for (int64_t i = 0; i < s.neq; ++i)
+                for (int j = 0; j < s.maxnb; ++j) b[i * W + j] = s.bases[i * s.maxnb + j];
+            s.bases.swap(b);
+            s.maxnb = W;
+            s.T.clear();
+            s.sidx.clear();
+        }
+    }
+    e = cudaStreamSynchronize(sm);
+    if (e != cudaSuccess) return cuda_fail(c, e, "finalize sync");
+    c->dev_final = true;
+    return FEM_GPU_OK;
+}
+
+}  // namespace fem
+
+extern "C" {
+
+int32_t fem_gpu_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+fem_gpu_status fem_gpu_set_stream(fem_gpu_ctx* c, void* stream) {
+    if (!c) return FEM_GPU_BAD_ARG;
+    if (c->own_stream && c->stream) {
+        cudaStreamSynchronize((cudaStream_t)c->stream);
+        cudaStreamDestroy((cudaStream_t)c->stream);
+    }
+    c->stream = stream;
+    c->own_stream = false;
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_gpu_finalize(fem_gpu_ctx* c) {
+    if (!c) return FEM_GPU_BAD_ARG;
+    fem_gpu_status st = fem_gpu_finalize_host(c);
+    if (st != FEM_GPU_OK) return st;
+    if (c->dev_final) return FEM_GPU_OK;
+    return device_finalize(c);
+}
+
+fem_gpu_status fem_gpu_build_graph(fem_gpu_ctx* c, int32_t* rowptr, int32_t* colidx, uint32_t flags) {
+    if (!c || !rowptr || !colidx) return FEM_GPU_BAD_ARG;
+    if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
+    const int64_t nad = c->num_used * c->dim;
+    std::vector<int32_t> ci;
+    int32_t* outc = colidx;
+    const bool host = flags & FEM_GPU_HOST_BUFFERS;
+    if (!host) {
+        ci.resize(c->nnz);
+        outc = ci.data();
+    }
+    for (int f = 0; f < c->dim; ++f)
+        for (int64_t b = 0; b < c->num_used; ++b) {
+            int32_t* o = outc + c->rowptr[f * c->num_used + b];
+            const int32_t* u = c->ucols.data() + c->uoff[b];
+            for (int g = 0; g < c->dim; ++g)
+                for (int32_t k = 0; k < c->ulen[b]; ++k) *o++ = (int32_t)(g * c->num_used + u[k]);
+        }
+    if (host) {
+        std::memcpy(rowptr, c->rowptr.data(), (nad + 1) * sizeof(int32_t));
+        return FEM_GPU_OK;
+    }
+    fem_gpu_status st = ensure_device(c);
+    if (st != FEM_GPU_OK) return st;
+    cudaError_t e = cudaMemcpyAsync(rowptr, c->rowptr.data(), (nad + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                    stream_of(c));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(colidx, ci.data(), c->nnz * sizeof(int32_t), cudaMemcpyHostToDevice, stream_of(c));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream_of(c));
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph upload");
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_gpu_element_matrices(fem_gpu_ctx* c, int32_t set, int64_t first, int64_t count,
+                                        const double* u, double* K, double* R, uint32_t flags) {
+    if (!c || set < 0 || set >= (int32_t)c->sets.size() || count < 0) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    SetData& s = c->sets[set];
+    if (first < 0 || first + count > s.neq) return FEM_GPU_OOB_INDEX;
+    if (count == 0) return FEM_GPU_OK;
+    const int nmax = s.maxnb * c->dim;
+    const bool host = flags & FEM_GPU_HOST_BUFFERS;
+    const int64_t nad = c->num_used * c->dim;
+    Staged su, sk, sr;
+    fem_gpu_status st;
+    if ((st = stage_in(c, u, nad * sizeof(double), host, su)) != FEM_GPU_OK) return st;
+    if ((st = stage_out_alloc(c, K, (size_t)count * nmax * nmax * sizeof(double), host, sk)) != FEM_GPU_OK) return st;
+    if ((st = stage_out_alloc(c, R, (size_t)count * nmax * sizeof(double), host, sr)) != FEM_GPU_OK) return st;
+    cudaStream_t sm = stream_of(c);
+    if (sk.dev) cudaMemsetAsync(sk.dev, 0, (size_t)count * nmax * nmax * sizeof(double), sm);
+    if (sr.dev) cudaMemsetAsync(sr.dev, 0, (size_t)count * nmax * sizeof(double), sm);
+    cudaMemsetAsync(c->d_status.p, 0, sizeof(int), sm);
+    if (s.kind == 0)
+        st = launch_bulk(c, set, MODE_ELEMENT, first, count, (const double*)su.dev, nullptr, nullptr,
+                         (double*)sk.dev, (double*)sr.dev, nmax, nullptr, nullptr);
+    else
+        st = launch_side(c, set, MODE_ELEMENT, first, count, (const double*)su.dev, nullptr, nullptr,
+                         (double*)sk.dev, (double*)sr.dev, nmax);
+    if (st == FEM_GPU_OK) {
+        cudaError_t e = cudaSuccess;
+        if (host && K) e = cudaMemcpyAsync(K, sk.dev, (size_t)count * nmax * nmax * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        if (e == cudaSuccess && host && R)
+            e = cudaMemcpyAsync(R, sr.dev, (size_t)count * nmax * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        if (e != cudaSuccess) st = cuda_fail(c, e, "element matrices copy");
+    }
+    release(c, su);
+    release(c, sk);
+    release(c, sr);
+    if (st != FEM_GPU_OK) return st;
+    return read_status(c);
+}
+
+fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* c, const double* u, double* vals, double* rhs, uint32_t flags) {
+    if (!c) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    const bool host = flags & FEM_GPU_HOST_BUFFERS;
+    const int64_t nad = c->num_used * c->dim;
+    double* v = (flags & FEM_GPU_NO_JACOBIAN) ? nullptr : vals;
+    double* r = (flags & FEM_GPU_NO_RESIDUAL) ? nullptr : rhs;
+    if (!v && !r) return FEM_GPU_BAD_ARG;
+    Staged su, sv, sr;
+    fem_gpu_status st;
+    if ((st = stage_in(c, u, nad * sizeof(double), host, su)) != FEM_GPU_OK) return st;
+    const bool acc = flags & FEM_GPU_ACCUMULATE;
+    if (acc) {
+        if ((st = stage_in(c, v, c->nnz * sizeof(double), host, sv)) != FEM_GPU_OK) return st;
+        if ((st = stage_in(c, r, nad * sizeof(double), host, sr)) != FEM_GPU_OK) return st;
+    } else {
+        if ((st = stage_out_alloc(c, v, c->nnz * sizeof(double), host, sv)) != FEM_GPU_OK) return st;
+        if ((st = stage_out_alloc(c, r, nad * sizeof(double), host, sr)) != FEM_GPU_OK) return st;
+    }
+    cudaStream_t sm = stream_of(c);
+    if (!acc) {
+        if (sv.dev) cudaMemsetAsync(sv.dev, 0, c->nnz * sizeof(double), sm);
+        if (sr.dev) cudaMemsetAsync(sr.dev, 0, nad * sizeof(double), sm);
+    }
+    cudaMemsetAsync(c->d_status.p, 0, sizeof(int), sm);
+    for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
+        SetData& s = c->sets[k];
+        if (s.kind == 0)
+            st = launch_bulk(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev, (double*)sr.dev,
+                             nullptr, nullptr, 0, nullptr, nullptr);
+        else
+            st = launch_side(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev, (double*)sr.dev,
+                             nullptr, nullptr, 0);
+    }
+    if (st == FEM_GPU_OK && host) {
+        cudaError_t e = cudaSuccess;
+        if (v) e = cudaMemcpyAsync(v, sv.dev, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        if (e == cudaSuccess && r) e = cudaMemcpyAsync(r, sr.dev, nad * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        if (e != cudaSuccess) st = cuda_fail(c, e, "assemble copy back");
+    }
+    release(c, su);
+    release(c, sv);
+    release(c, sr);
+    if (st != FEM_GPU_OK) return st;
+    return read_status(c);
+}
+
+fem_gpu_status fem_gpu_apply(fem_gpu_ctx* c, const double* x, double* y, uint32_t flags) {
+    if (!c || !x || !y) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    const bool host = flags & FEM_GPU_HOST_BUFFERS;
+    const int64_t nad = c->num_used * c->dim;
+    Staged sx, sy;
+    fem_gpu_status st;
+    if ((st = stage_in(c, x, nad * sizeof(double), host, sx)) != FEM_GPU_OK) return st;
+    if ((st = stage_out_alloc(c, y, nad * sizeof(double), host, sy)) != FEM_GPU_OK) return st;
+    cudaStream_t sm = stream_of(c);
+    if (!(flags & FEM_GPU_ACCUMULATE)) cudaMemsetAsync(sy.dev, 0, nad * sizeof(double), sm);
+    for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
+        SetData& s = c->sets[k];
+        if (s.kind != 0) {
+            st = fail(c, FEM_GPU_UNSUPPORTED, "matrix-free apply covers bulk sets only");
+            break;
+        }
+        st = launch_bulk(c, k, MODE_APPLY, 0, s.neq, nullptr, nullptr, nullptr, nullptr, nullptr, 0,
+                         (const double*)sx.dev, (double*)sy.dev);
+    }
+    if (st == FEM_GPU_OK && host) {
+        cudaError_t e = cudaMemcpyAsync(y, sy.dev, nad * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+        if (e != cudaSuccess) st = cuda_fail(c, e, "apply copy back");
+    }
+    release(c, sx);
+    release(c, sy);
+    return st;
+}
+
+}  // extern "C"

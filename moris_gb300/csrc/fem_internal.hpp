@@ -1,0 +1,92 @@
+// fem_internal.hpp -- private declarations shared by the host (.cpp) and
+// device (.cu) translation units of libfem_gpu.so.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fem_gpu.h"
+
+namespace fem {
+
+// ---- reference-element tables (fem_tables.cpp) --------------------------
+struct Rule {
+    int dim = 0, n = 0;
+    std::vector<double> pts;  // n x dim, point-major
+    std::vector<double> w;
+};
+Rule gauss_rule(int rule);
+int cell_num_nodes(int cell);
+int cell_param_dim(int cell);
+// N (n), dNdxi (pdim x n, row-major: dNdxi[i*n + a])
+void lagrange(int cell, const double* xi, double* N, double* dNdxi);
+void cell_param_coords(int cell, double* xi_hat);  // n x pdim, node-major
+const int* facet_vertices(int ip_cell, int ordinal, int* count);
+
+// ---- host-side set data ----------------------------------------------------
+struct DeviceBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+// Everything a kernel reads for one set, laid out per equation object.
+struct SetData {
+    int kind = 0;  // 0 bulk, 1 side
+    fem_gpu_bulk_set_desc bulk{};
+    fem_gpu_side_set_desc side{};
+    int64_t neq = 0;
+    std::vector<int32_t> ip_cell;
+    std::vector<int64_t> ig_off;
+    std::vector<double> ig_coords, ig_param;
+    std::vector<double> E;
+    std::vector<int32_t> ordinal;
+    // finalize products
+    int maxnb = 0;                 // max unique bases per element (padding width)
+    std::vector<int32_t> nb;       // [neq]
+    std::vector<int32_t> bases;    // [neq][maxnb] basis ranks, -1 padded
+    std::vector<double> T;         // [neq][npe][maxnb] dense element extraction
+    std::vector<uint16_t> sidx;    // [neq][maxnb][maxnb] column slot of base j in row of base i
+    std::vector<double> xe;        // [neq][npe][dim] interpolation-cell coordinates
+    // device copies
+    DeviceBuf d_nb, d_bases, d_T, d_sidx, d_xe, d_E, d_ord;
+    DeviceBuf d_dn, d_w;    // bulk: dN/dxi of the IP cell at the Gauss points, weights
+    DeviceBuf d_gp, d_gw;   // side: facet Gauss points and weights
+    int ngp = 0;            // Gauss points of the set's rule
+    int nbsel = 0;          // padded basis width of the kernel instance
+};
+
+}  // namespace fem
+
+struct fem_gpu_ctx {
+    int dim = 0, ip_cell = 0, shape = 0, npe = 0;
+    int64_t num_nodes = 0, num_cells = 0, num_bases = 0;
+    std::vector<double> coords;
+    std::vector<int32_t> cells;
+    std::vector<int64_t> t_off;
+    std::vector<int32_t> t_bases;
+    std::vector<double> t_w;
+    std::vector<fem::SetData> sets;
+    // MSI / graph products
+    bool host_final = false, dev_final = false;
+    int64_t num_used = 0;              // used bases
+    std::vector<int64_t> basis_rank;   // domain basis -> rank or -1
+    std::vector<int32_t> ulen;         // [num_used] |U(b)| (column union length per type)
+    std::vector<int64_t> uoff;         // [num_used+1] offsets into ucols
+    std::vector<int32_t> ucols;        // union lists (basis ranks, ascending)
+    std::vector<int32_t> rowptr;       // [num_adofs+1]
+    int64_t nnz = 0;
+    // device state
+    void* stream = nullptr;            // cudaStream_t
+    bool own_stream = false;
+    fem::DeviceBuf d_rowptr, d_ulen, d_tables, d_scratch, d_status;
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace fem {
+fem_gpu_status fail(fem_gpu_ctx* c, fem_gpu_status s, const std::string& msg);
+// device side (fem_device.cu)
+fem_gpu_status device_finalize(fem_gpu_ctx* c);
+void device_release(fem_gpu_ctx* c);
+}  // namespace fem

@@ -1,0 +1,260 @@
+// fem_solver.cu -- preconditioned conjugate gradients on the assembled CSR
+// operator (the reference delegates this to Trilinos AztecOO AZ_cg with
+// AZ_Jacobi, SOL/DLA/src/cl_DLA_Linear_Solver_Aztec.cpp:260-355).
+//
+// One iteration is four launches on the context stream:
+//   k1  q = A p and the partial sums of p.q            (warp per CSR row)
+//   k2  alpha = rz/pq; x += alpha p; r -= alpha q; z = M^-1 r; sums of r.z, r.r
+//   k3  convergence test; beta = rz'/rz; p = z + beta p
+//   k4  (one thread) advance the iteration counter
+// Scalars live in a device ring indexed by the iteration counter, so the
+// launches carry no host-side values and a chunk of iterations is captured
+// once into a CUDA graph and replayed.  The host reads the done flag once
+// per chunk; iterations after convergence return immediately on the device.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "fem_internal.hpp"
+
+namespace {
+
+struct CgState {
+    int it;          // current iteration
+    int done;        // 1 converged, 2 breakdown
+    int converged_at;
+    int pad;
+    double thresh2;  // (rtol * ||b||)^2
+    double bn2;
+    // ring of per-iteration scalars: [slot][0]=pq, [1]=rz, [2]=rr
+    double ring[4][4];
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block reduction of one double into *out (atomic)
+__device__ __forceinline__ void block_add(double v, double* out) {
+    __shared__ double red[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+        v = warp_sum(v);
+        if (lane == 0) atomicAdd(out, v);
+    }
+}
+
+__global__ void k_diag_inv(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, double* dinv,
+                           int jacobi) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double d = 1.0;
+    if (jacobi) {
+        int lo = rp[i], hi = rp[i + 1] - 1;
+        while (lo <= hi) {  // columns ascending
+            const int mid = (lo + hi) >> 1;
+            if (ci[mid] == i) {
+                d = v[mid];
+                break;
+            }
+            if (ci[mid] < i) lo = mid + 1;
+            else hi = mid - 1;
+        }
+        d = (d != 0.0) ? 1.0 / d : 1.0;
+    }
+    dinv[i] = d;
+}
+
+// r = b - A x ; z = M^-1 r ; p = z ; accumulate r.z, r.r, b.b into slot 0
+__global__ void k_init(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* b,
+                       const double* x, double* r, double* z, double* p, const double* dinv, CgState* st) {
+    const int lane = threadIdx.x & 31;
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double rz = 0.0, rr = 0.0, bb = 0.0;
+    if (row < n) {
+        double s = 0.0;
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) s = fma(v[k], x[ci[k]], s);
+        s = warp_sum(s);
+        if (lane == 0) {
+            const double ri = b[row] - s, zi = dinv[row] * ri;
+            r[row] = ri;
+            z[row] = zi;
+            p[row] = zi;
+            rz = ri * zi;
+            rr = ri * ri;
+            bb = b[row] * b[row];
+        }
+    }
+    block_add(rz, &st->ring[0][1]);
+    __syncthreads();
+    block_add(rr, &st->ring[0][2]);
+    __syncthreads();
+    block_add(bb, &st->bn2);
+}
+
+__global__ void k_spmv_pq(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* p,
+                          double* q, CgState* st) {
+    if (st->done) return;
+    const int slot = st->it & 3;
+    const int lane = threadIdx.x & 31;
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double pq = 0.0;
+    if (row < n) {
+        double s = 0.0;
+        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) s = fma(v[k], p[ci[k]], s);
+        s = warp_sum(s);
+        if (lane == 0) {
+            q[row] = s;
+            pq = s * p[row];
+        }
+    }
+    block_add(pq, &st->ring[slot][0]);
+}
+
+__global__ void k_update_xr(int64_t n, double* x, double* r, double* z, const double* p, const double* q,
+                            const double* dinv, CgState* st) {
+    if (st->done) return;
+    const int slot = st->it & 3, nxt = (st->it + 1) & 3;
+    const double alpha = st->ring[slot][1] / st->ring[slot][0];
+    double rz = 0.0, rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = fma(alpha, p[i], x[i]);
+        const double ri = fma(-alpha, q[i], r[i]);
+        r[i] = ri;
+        const double zi = dinv[i] * ri;
+        z[i] = zi;
+        rz = fma(ri, zi, rz);
+        rr = fma(ri, ri, rr);
+    }
+    block_add(rz, &st->ring[nxt][1]);
+    __syncthreads();
+    block_add(rr, &st->ring[nxt][2]);
+}
+
+__global__ void k_update_p(int64_t n, double* p, const double* z, CgState* st) {
+    if (st->done) return;
+    const int slot = st->it & 3, nxt = (st->it + 1) & 3;
+    if (st->ring[nxt][2] <= st->thresh2) return;  // k4 records convergence
+    const double beta = st->ring[nxt][1] / st->ring[slot][1];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = fma(beta, p[i], z[i]);
+}
+
+__global__ void k_advance(CgState* st, int max_iter) {
+    if (st->done) return;
+    const int slot = st->it & 3, nxt = (st->it + 1) & 3, nn = (st->it + 2) & 3;
+    st->it += 1;
+    if (st->ring[nxt][2] <= st->thresh2) {
+        st->done = 1;
+        st->converged_at = st->it;
+    } else if (!(st->ring[nxt][1] == st->ring[nxt][1]) || st->ring[slot][0] == 0.0) {
+        st->done = 2;  // breakdown (NaN or p.Ap == 0)
+    } else if (st->it >= max_iter) {
+        st->done = 3;
+    }
+    for (int k = 0; k < 4; ++k) st->ring[nn][k] = 0.0;
+    (void)slot;
+}
+
+__global__ void k_set_thresh(CgState* st, double rtol) {
+    const double bn2 = st->bn2 > 0.0 ? st->bn2 : 1.0;
+    st->bn2 = bn2;
+    st->thresh2 = rtol * rtol * bn2;
+    if (st->ring[0][2] <= st->thresh2) {
+        st->done = 1;
+        st->converged_at = 0;
+    }
+}
+
+}  // namespace
+
+using namespace fem;
+
+extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx,
+                                      const double* vals, const double* b, double* x, const fem_gpu_pcg_opts* opts,
+                                      fem_gpu_pcg_report* rep, uint32_t flags) {
+    if (!c || !rowptr || !colidx || !vals || !b || !x || !opts) return FEM_GPU_BAD_ARG;
+    if (flags & FEM_GPU_HOST_BUFFERS) return fail(c, FEM_GPU_UNSUPPORTED, "pcg takes device buffers");
+    if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
+    if (!(opts->rel_tol > 0.0) || opts->max_iter < 1) return FEM_GPU_BAD_ARG;
+    if (!c->stream) {
+        cudaStream_t s;
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(c, FEM_GPU_CUDA_ERROR, "stream create");
+        c->stream = s;
+        c->own_stream = true;
+    }
+    cudaStream_t sm = (cudaStream_t)c->stream;
+    const int64_t n = c->num_used * c->dim;
+    const auto t0 = std::chrono::steady_clock::now();
+    double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+    CgState* st = nullptr;
+    cudaError_t e = cudaMallocAsync(&r, 5 * n * sizeof(double), sm);
+    if (e == cudaSuccess) e = cudaMallocAsync(&st, sizeof(CgState), sm);
+    if (e != cudaSuccess) return fail(c, FEM_GPU_OUT_OF_MEMORY, "pcg workspace");
+    z = r + n;
+    p = z + n;
+    q = p + n;
+    dinv = q + n;
+    cudaMemsetAsync(st, 0, sizeof(CgState), sm);
+    const int tpb = 256;
+    const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
+                                                                opts->preconditioner == 1);
+    k_init<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, b, x, r, z, p, dinv, st);
+    k_set_thresh<<<1, 1, 0, sm>>>(st, opts->rel_tol);
+    c->launches += 3;
+    // capture a chunk of iterations into a graph
+    const int chunk = 32;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    e = cudaStreamBeginCapture(sm, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        for (int k = 0; k < chunk; ++k) {
+            k_spmv_pq<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, p, q, st);
+            k_update_xr<<<vec_blocks, tpb, 0, sm>>>(n, x, r, z, p, q, dinv, st);
+            k_update_p<<<vec_blocks, tpb, 0, sm>>>(n, p, z, st);
+            k_advance<<<1, 1, 0, sm>>>(st, opts->max_iter);
+        }
+        e = cudaStreamEndCapture(sm, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    CgState hs{};
+    fem_gpu_status result = FEM_GPU_OK;
+    if (e == cudaSuccess) {
+        for (int launched = 0; launched < opts->max_iter + chunk; launched += chunk) {
+            e = cudaGraphLaunch(exec, sm);
+            if (e != cudaSuccess) break;
+            c->launches += 4 * chunk;
+            e = cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, sm);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+            if (e != cudaSuccess || hs.done) break;
+        }
+    }
+    if (e != cudaSuccess) result = fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg: ") + cudaGetErrorString(e));
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFreeAsync(r, sm);
+    cudaFreeAsync(st, sm);
+    cudaStreamSynchronize(sm);
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rep) {
+        rep->iterations = hs.done == 1 ? hs.converged_at : hs.it;
+        rep->converged = hs.done == 1;
+        const int slot = hs.it & 3;
+        rep->rel_residual = std::sqrt(hs.ring[slot][2] / (hs.bn2 > 0 ? hs.bn2 : 1.0));
+        rep->seconds = secs;
+    }
+    if (result != FEM_GPU_OK) return result;
+    if (hs.done == 2) return fail(c, FEM_GPU_NONFINITE, "pcg breakdown");
+    if (hs.done != 1) return fail(c, FEM_GPU_NOT_CONVERGED, "pcg hit max_iter");
+    return FEM_GPU_OK;
+}

@@ -730,27 +730,27 @@ int orc_model_finalize(orc_model* m) {
         std::sort(u.begin(), u.end());
         u.erase(std::unique(u.begin(), u.end()), u.end());
     }
-    // sparsity
-    const int64_t nad = m->num_used * m->dim;
-    std::vector<std::vector<int32_t>> rows(nad);
-    for (int64_t c = 0; c < m->num_cells; ++c) {
-        if (!cell_used[c]) continue;
-        const auto& u = m->cell_ubases[c];
-        std::vector<int32_t> ids;
-        for (int f = 0; f < m->dim; ++f)
-            for (auto b : u) ids.push_back((int32_t)(f * m->num_used + b));
-        for (auto r : ids)
-            for (auto cc : ids) rows[r].push_back(cc);
+    // sparsity: for every used basis the union of the basis lists of the
+    // cells that contain it; row (type f, basis b) repeats it for every type
+    const int64_t nu = m->num_used, nad = nu * m->dim;
+    std::vector<std::vector<int64_t>> cells_of(nu);
+    for (int64_t c = 0; c < m->num_cells; ++c)
+        for (auto b : m->cell_ubases[c]) cells_of[b].push_back(c);
+    std::vector<std::vector<int32_t>> uni(nu);
+    for (int64_t b = 0; b < nu; ++b) {
+        std::vector<int32_t>& u = uni[b];
+        for (auto c : cells_of[b]) u.insert(u.end(), m->cell_ubases[c].begin(), m->cell_ubases[c].end());
+        std::sort(u.begin(), u.end());
+        u.erase(std::unique(u.begin(), u.end()), u.end());
     }
     m->rowptr.assign(nad + 1, 0);
-    for (int64_t r = 0; r < nad; ++r) {
-        auto& v = rows[r];
-        std::sort(v.begin(), v.end());
-        v.erase(std::unique(v.begin(), v.end()), v.end());
-        m->rowptr[r + 1] = m->rowptr[r] + (int32_t)v.size();
-    }
+    for (int64_t r = 0; r < nad; ++r) m->rowptr[r + 1] = m->rowptr[r] + (int32_t)(m->dim * uni[r % nu].size());
     m->colidx.resize(m->rowptr[nad]);
-    for (int64_t r = 0; r < nad; ++r) std::copy(rows[r].begin(), rows[r].end(), m->colidx.begin() + m->rowptr[r]);
+    for (int64_t r = 0; r < nad; ++r) {
+        int64_t k = m->rowptr[r];
+        for (int g = 0; g < m->dim; ++g)
+            for (auto cb : uni[r % nu]) m->colidx[k++] = (int32_t)(g * nu + cb);
+    }
     m->finalized = true;
     return 0;
 }
@@ -1080,13 +1080,15 @@ int orc_element_pdof_matrices(const orc_model* m, int set, int64_t eq, const dou
    restatement partitions equation objects over std::threads and sums into
    the shared CSR with atomic adds.                                           */
 int orc_assemble(const orc_model* m, const double* u_adof, double* vals, double* rhs, int nthreads,
-                 int64_t eq_stride) {
+                 int64_t eq_stride, int zero_first) {
     if (!m->finalized) return 1;
     if (nthreads < 1) nthreads = 1;
     if (eq_stride < 1) eq_stride = 1;
     const int64_t nnz = orc_model_nnz(m), nad = orc_model_num_adofs(m);
-    std::memset(vals, 0, sizeof(real) * nnz);
-    std::memset(rhs, 0, sizeof(real) * nad);
+    if (zero_first) {
+        std::memset(vals, 0, sizeof(real) * nnz);
+        std::memset(rhs, 0, sizeof(real) * nad);
+    }
     struct Item { int set; int64_t eq; };
     std::vector<Item> items;
     for (int s = 0; s < orc_model_num_sets(m); ++s)

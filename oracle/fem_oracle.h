@@ -93,9 +93,10 @@ int orc_element_matrices(const orc_model* m, int set, int64_t eq, const double* 
 int orc_element_pdof_matrices(const orc_model* m, int set, int64_t eq, const double* u_pdof,
                               double* K_colmajor, double* R, int32_t* npdof);
 /* full assembly; eq_stride > 1 assembles every eq_stride-th element only
-   (bounded CPU samples).  vals: nnz doubles, rhs: num_adofs doubles. */
+   (bounded CPU samples).  vals: nnz doubles, rhs: num_adofs doubles, zeroed
+   first unless zero_first == 0. */
 int orc_assemble(const orc_model* m, const double* u_adof, double* vals, double* rhs, int nthreads,
-                 int64_t eq_stride);
+                 int64_t eq_stride, int zero_first);
 /* conjugate gradients with Jacobi preconditioner on a CSR matrix */
 int orc_pcg(int64_t n, const int32_t* rowptr, const int32_t* colidx, const double* vals,
             const double* b, double* x, double rtol, int max_iter, int jacobi, int* iters,

@@ -48,7 +48,7 @@ def load():
             "orc_element_topology": (_I, [_P, _I, _L, _P, _P]),
             "orc_element_matrices": (_I, [_P, _I, _L, _P, _P, _P]),
             "orc_element_pdof_matrices": (_I, [_P, _I, _L, _P, _P, _P, _P]),
-            "orc_assemble": (_I, [_P, _P, _P, _P, _I, _L]),
+            "orc_assemble": (_I, [_P, _P, _P, _P, _I, _L, _I]),
             "orc_pcg": (_I, [_L, _P, _P, _P, _P, _P, _D, _I, _I, _P, _P]),
         }
         for name, (res, args) in sig.items():
@@ -187,11 +187,15 @@ class OracleModel:
         m = n.value
         return K[:m * m].reshape(m, m).T.copy(), R[:m].copy()
 
-    def assemble(self, u_adof=None, nthreads=1, eq_stride=1):
-        vals = np.zeros(self.nnz)
-        rhs = np.zeros(self.num_adofs)
+    def assemble(self, u_adof=None, nthreads=1, eq_stride=1, out=None):
+        """Assemble into fresh arrays, or accumulate into out=(vals, rhs)."""
+        if out is None:
+            vals = np.zeros(self.nnz)
+            rhs = np.zeros(self.num_adofs)
+        else:
+            vals, rhs = out
         u = None if u_adof is None else np.ascontiguousarray(u_adof, dtype=np.float64)
-        assert self.lib.orc_assemble(self.h, _ptr(u), _ptr(vals), _ptr(rhs), nthreads, eq_stride) == 0
+        assert self.lib.orc_assemble(self.h, _ptr(u), _ptr(vals), _ptr(rhs), nthreads, eq_stride, 0) == 0
         return vals, rhs
 
 

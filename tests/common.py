@@ -1,0 +1,78 @@
+"""Shared builders for the parity tests: one seeded problem, two models (the
+CUDA product through libfem_gpu and the CPU oracle) over identical arrays."""
+import numpy as np
+
+import moris_gb300 as mg
+from moris_gb300.rng import uniform01 as _uniform01
+from oracle import OracleModel
+
+# element operators / residuals: |gpu - oracle| <= RTOL * max|oracle| (per element
+# matrix, per assembled CSR row, per vector)
+RTOL = 1e-12
+
+
+def uniform01(seed, n):
+    """Seeded inputs shared by the oracle-side and GPU-side models."""
+    return _uniform01(seed, n)
+
+
+def distort(mesh, dim, ne, amount, seed):
+    """Move interior nodes by a seeded fraction of the element size."""
+    m = dict(mesh)
+    x = mesh["coords"].copy()
+    h = np.array([1.0 / n for n in ne])
+    rng = np.random.default_rng(seed)
+    inner = np.all((x > 1e-12) & (x < 1 - 1e-12), axis=1)
+    x[inner] += amount * h * rng.uniform(-1, 1, size=(inner.sum(), dim))
+    m["coords"] = x
+    return m
+
+
+def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed=1, distortion=0.2):
+    mesh = mg.hmr_uniform_mesh(dim, ne, [1.0] * dim, p)
+    if shape == mg.SHAPE_GENERAL:
+        mesh = distort(mesh, dim, ne, distortion, seed + 7)
+    nc = len(mesh["cells"])
+    E = 10.0 ** (-3.0 * uniform01(seed, nc))
+    model = mg.MODEL_3D if dim == 3 else mg.MODEL_PLANE_STRAIN
+    if rule is None:
+        rule = mg.RULE_HEX_3x3x3 if dim == 3 else mg.RULE_QUAD_2x2
+    ipc = mg.CELL_QUAD4 if dim == 2 else mg.CELL_HEX8
+    prod = mg.FemModel(dim, mesh, shape)
+    orc = OracleModel(dim, ipc, shape, mesh)
+    cells = np.arange(nc, dtype=np.int32)
+    prod.add_bulk_set(cells, E, 0.3, rule, model)
+    orc.add_bulk_set(ipc, rule, model, cells, E, 0.3)
+    if sides:
+        if dim == 2:
+            left = np.arange(0, nc, ne[0], dtype=np.int32)
+            right = np.arange(ne[0] - 1, nc, ne[0], dtype=np.int32)
+            lo, ro, srule = 3, 1, mg.RULE_BAR_3
+        else:
+            left = np.array([c for c in range(nc) if c % ne[0] == 0], dtype=np.int32)
+            right = np.array([c for c in range(nc) if c % ne[0] == ne[0] - 1], dtype=np.int32)
+            lo, ro, srule = 3, 1, mg.RULE_QUAD_2x2
+        zero = (0.0,) * dim
+        trac = (1e-3,) + (0.0,) * (dim - 1)
+        prod.add_side_set(mg.IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, left, np.full(len(left), lo), E[left], 0.3,
+                          srule, model, alpha=100.0, value=zero)
+        orc.add_side_set(mg.IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, srule, model, left, np.full(len(left), lo),
+                         E[left], 0.3, 100.0, zero)
+        prod.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, right, np.full(len(right), ro), E[right], 0.3, srule, model,
+                          value=trac)
+        orc.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, srule, model, right, np.full(len(right), ro), E[right], 0.3, 0.0,
+                         trac)
+    return prod, orc, mesh
+
+
+def rel_err(a, b):
+    scale = np.max(np.abs(b))
+    return 0.0 if scale == 0 else float(np.max(np.abs(a - b)) / scale)
+
+
+def csr_row_rel_err(rowptr, va, vb):
+    worst = 0.0
+    for r in range(len(rowptr) - 1):
+        s = slice(rowptr[r], rowptr[r + 1])
+        worst = max(worst, rel_err(va[s], vb[s]))
+    return worst

@@ -1,0 +1,171 @@
+"""GPU parity: the CUDA element path (through the C ABI) against the oracle.
+
+Bar: element operators, assembled CSR values and residuals agree with the
+oracle to a relative error of 1e-12 (tests/common.py RTOL, normwise per
+element matrix / per CSR row / per vector); integer data (adof ids, CSR
+rowptr/colidx) identical.
+"""
+import numpy as np
+import pytest
+
+import moris_gb300 as mg
+from tests.common import RTOL, csr_row_rel_err, problem, rel_err, uniform01
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # dim, ne, p, shape, rule, sides
+    (2, (6, 5), 1, mg.SHAPE_RECTANGULAR, mg.RULE_QUAD_2x2, True),
+    (2, (5, 4), 2, mg.SHAPE_GENERAL, mg.RULE_QUAD_2x2, True),
+    (2, (4, 4), 3, mg.SHAPE_RECTANGULAR, mg.RULE_QUAD_2x2, False),
+    (3, (3, 3, 2), 1, mg.SHAPE_RECTANGULAR, mg.RULE_HEX_2x2x2, True),
+    (3, (3, 2, 3), 2, mg.SHAPE_RECTANGULAR, mg.RULE_HEX_3x3x3, False),
+    (3, (3, 3, 3), 2, mg.SHAPE_GENERAL, mg.RULE_HEX_3x3x3, True),
+    (3, (2, 3, 2), 2, mg.SHAPE_GENERAL, mg.RULE_HEX_2x2x2, False),
+]
+
+
+def _ids(c):
+    return "d%d-p%d-%s-r%d%s" % (c[0], c[2], "rect" if c[3] == 0 else "gen", c[4], "-sides" if c[5] else "")
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+def test_element_operators_match_oracle(torch, case):
+    dim, ne, p, shape, rule, sides = case
+    prod, orc, _ = problem(dim, ne, p, shape, rule, sides)
+    prod.finalize()
+    orc.finalize()
+    u = uniform01(11, prod.num_adofs) - 0.5
+    for s in range(orc.num_sets()):
+        n_eq = orc.num_eq(s)
+        K, R = prod.element_matrices(s, 0, n_eq, u)
+        for eq in range(n_eq):
+            ids = orc.element_topology(s, eq)
+            assert np.array_equal(prod.element_topology(s, eq), ids)
+            Ko, Ro = orc.element_matrices(s, eq, u)
+            n = len(ids)
+            assert rel_err(K[eq, :n, :n], Ko) <= RTOL, (s, eq)
+            assert rel_err(R[eq, :n], Ro) <= RTOL, (s, eq)
+            assert np.all(K[eq, n:, :] == 0) and np.all(K[eq, :, n:] == 0)
+
+
+@pytest.mark.parametrize("case", CASES, ids=_ids)
+def test_assembly_matches_oracle(torch, case):
+    dim, ne, p, shape, rule, sides = case
+    prod, orc, _ = problem(dim, ne, p, shape, rule, sides)
+    prod.finalize()
+    orc.finalize()
+    rp, ci = prod.graph()
+    rpo, cio = orc.graph()
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    u = uniform01(5, prod.num_adofs) - 0.5
+    vo, ro = orc.assemble(u, nthreads=4)
+    # device buffers through the C ABI
+    ut = torch.tensor(u, device="cuda")
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(ut, vals, rhs)
+    torch.cuda.synchronize()
+    assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL
+    assert rel_err(rhs.cpu().numpy(), ro) <= RTOL
+    # host buffers through the same entry point (the reference-facing call)
+    vh, rh = prod.assemble_host(u)
+    assert csr_row_rel_err(rp, vh, vo) <= RTOL
+    assert rel_err(rh, ro) <= RTOL
+    # residual of the linear IWGs is K u - f: check consistency on the device result
+    f0 = prod.assemble_host(np.zeros(prod.num_adofs), mg.NO_JACOBIAN)[1]
+    import scipy.sparse as sp
+    A = sp.csr_matrix((vh, ci, rp), shape=(prod.num_adofs, prod.num_adofs))
+    assert rel_err(rh, A @ u + f0) <= 1e-11
+
+
+def test_residual_only_and_jacobian_only_flags(torch):
+    prod, orc, _ = problem(2, (4, 4), 2, sides=True)
+    prod.finalize()
+    orc.finalize()
+    u = uniform01(3, prod.num_adofs)
+    vo, ro = orc.assemble(u)
+    v1, r1 = prod.assemble_host(u, mg.NO_JACOBIAN)
+    assert np.all(v1 == 0) and rel_err(r1, ro) <= RTOL
+    v2, r2 = prod.assemble_host(u, mg.NO_RESIDUAL)
+    assert np.all(r2 == 0)
+    rp, _ = prod.graph()
+    assert csr_row_rel_err(rp, v2, vo) <= RTOL
+
+
+@pytest.mark.parametrize("dim,ne,p,shape", [(2, (6, 6), 2, mg.SHAPE_GENERAL), (3, (4, 3, 3), 2, mg.SHAPE_RECTANGULAR),
+                                            (3, (3, 3, 3), 1, mg.SHAPE_GENERAL)])
+def test_matrix_free_apply_matches_assembled_operator(torch, dim, ne, p, shape):
+    prod, orc, _ = problem(dim, ne, p, shape)
+    prod.finalize()
+    orc.finalize()
+    rp, ci = orc.graph()
+    vo, _ = orc.assemble(None)
+    x = uniform01(9, prod.num_adofs) - 0.5
+    import scipy.sparse as sp
+    y_ref = sp.csr_matrix((vo, ci, rp), shape=(prod.num_adofs,) * 2) @ x
+    xt = torch.tensor(x, device="cuda")
+    yt = torch.empty_like(xt)
+    prod.apply(xt, yt)
+    torch.cuda.synchronize()
+    assert rel_err(yt.cpu().numpy(), y_ref) <= RTOL
+
+
+def test_pcg_solves_plane_strain_cantilever(torch):
+    # small version of the 2D elasticity case: clamp x=0 (Nitsche), traction at x=1
+    prod, orc, _ = problem(2, (16, 16), 1, sides=True)
+    prod.finalize()
+    orc.finalize()
+    rp, ci = orc.graph()
+    vo, ro = orc.assemble(None)
+    from oracle.oracle import pcg
+    x_ref, it_ref, rr_ref, rc = pcg(rp, ci, vo, -ro, rtol=1e-10)
+    assert rc == 0
+    rpt = torch.tensor(rp, device="cuda")
+    cit = torch.tensor(ci, device="cuda")
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(None, vals, rhs)
+    b = -rhs
+    x = torch.zeros_like(b)
+    rep = prod.pcg(rpt, cit, vals, b, x, rel_tol=1e-10)
+    assert rep["converged"] and rep["rel_residual"] <= 1e-10
+    assert abs(rep["iterations"] - it_ref) <= max(3, it_ref // 20)
+    assert rel_err(x.cpu().numpy(), x_ref) <= 1e-8
+
+
+def test_pcg_reports_non_convergence(torch):
+    prod, _, _ = problem(2, (8, 8), 1, sides=True)
+    prod.finalize()
+    rp, ci = prod.graph()
+    rpt = torch.tensor(rp, device="cuda")
+    cit = torch.tensor(ci, device="cuda")
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(None, vals, rhs)
+    x = torch.zeros_like(rhs)
+    with pytest.raises(mg.FemGpuError) as ei:
+        prod.pcg(rpt, cit, vals, -rhs, x, rel_tol=1e-14, max_iter=5)
+    assert ei.value.status == 10  # NOT_CONVERGED
+
+
+def test_nonfinite_input_is_reported(torch):
+    prod, _, _ = problem(2, (3, 3), 1)
+    prod.finalize()
+    u = np.zeros(prod.num_adofs)
+    K, R = prod.element_matrices(0, 0, 1, u)
+    assert np.isfinite(K).all()
+    # a NaN in the solution vector leaves K finite; a NaN modulus does not
+    mesh = mg.hmr_uniform_mesh(2, (2, 2), (1.0, 1.0), 1)
+    m = mg.FemModel(2, mesh)
+    with pytest.raises(mg.FemGpuError) as ei:
+        m.add_bulk_set(np.arange(4), [1.0, np.nan, 1.0, 1.0], 0.3, mg.RULE_QUAD_2x2, mg.MODEL_PLANE_STRAIN)
+    assert ei.value.status == 3

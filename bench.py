@@ -219,6 +219,8 @@ def main():
     model.set_stream(stream.cuda_stream)
     t0 = time.perf_counter()
     model.finalize()
+    model.autotune()
+    variant = model.variant(0)
     setup_s = time.perf_counter() - t0
     nad, nnz = model.num_adofs, model.nnz
     rng = np.random.default_rng(SEED + 1)
@@ -261,6 +263,16 @@ def main():
     x = torch.tensor(rng.uniform(-1.0, 1.0, nad), device="cuda")
     y = torch.empty_like(x)
     ms_jv = timed(lambda: model.apply(x, y), max(5, args.steps // 2), 2)
+    # check Jv against the assembled CSR operator (same seeded input)
+    rowptr = torch.empty(nad + 1, dtype=torch.int32, device="cuda")
+    colidx = torch.empty(nnz, dtype=torch.int32, device="cuda")
+    model.graph_device(rowptr, colidx)
+    model.assemble(u, vals, rhs)
+    model.apply(x, y)
+    Acsr = torch.sparse_csr_tensor(rowptr.long(), colidx.long(), vals, size=(nad, nad))
+    y_ref = torch.mv(Acsr, x)
+    jv_err = float((y - y_ref).abs().max() / y_ref.abs().max())
+    del Acsr, rowptr, colidx
     # --- e2e: the same call with host buffers (pinned), copies inside the timed region -------
     e2e = None
     if not args.no_e2e:
@@ -326,7 +338,8 @@ def main():
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "measured in-run (FP64 FMA-chain probe, fem_gpu_probe_fp64_tflops)",
                      "flops_per_element": fpe, "kernel_ms": ms_kernel},
-        "jv": {"ms_per_apply": ms_jv, "elements_per_s": nc / (ms_jv * 1e-3)},
+        "kernel_variant": {"index": variant[0], "name": variant[2], "tuned_ms": variant[1]},
+        "jv": {"ms_per_apply": ms_jv, "elements_per_s": nc / (ms_jv * 1e-3), "rel_err_vs_csr": jv_err},
         "setup_seconds": setup_s,
     }
     if e2e:

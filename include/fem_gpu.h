@@ -185,7 +185,9 @@ fem_gpu_status fem_hmr_mesh_free(fem_hmr_mesh* m);
 /* ---- model ------------------------------------------------------------- */
 fem_gpu_status fem_gpu_create(const fem_gpu_mesh_desc* mesh, fem_gpu_ctx** out);
 fem_gpu_status fem_gpu_destroy(fem_gpu_ctx* ctx);
-/* cudaStream_t passed as void*; NULL = the library's own stream */
+/* cudaStream_t passed as void*.  Without this call the context creates its
+   own non-blocking stream; after it, every call is ordered on the given
+   stream (NULL selects the CUDA legacy default stream). */
 fem_gpu_status fem_gpu_set_stream(fem_gpu_ctx* ctx, void* stream);
 fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* ctx, const fem_gpu_bulk_set_desc* desc, int32_t* set_index);
 fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* ctx, const fem_gpu_side_set_desc* desc, int32_t* set_index);
@@ -218,6 +220,13 @@ fem_gpu_status fem_gpu_apply(fem_gpu_ctx* ctx, const double* x, double* y, uint3
 fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                            const double* b, double* x, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report,
                            uint32_t flags);
+/* autotuner: times every kernel variant of each bulk set on (up to
+   max_elements, <= 0 = all) of its elements, assembling into scratch
+   buffers, and keeps the fastest per set.  Setup-time call; optional. */
+fem_gpu_status fem_gpu_autotune(fem_gpu_ctx* ctx, int64_t max_elements);
+fem_gpu_status fem_gpu_get_variant(const fem_gpu_ctx* ctx, int32_t set, int32_t* variant, double* tuned_ms,
+                                   const char** name);
+fem_gpu_status fem_gpu_set_variant(fem_gpu_ctx* ctx, int32_t set, int32_t variant);
 /* in-run FP64 peak probe (FMA chains on every SM, CUDA-event timed), the
    roofline denominator of the FP64-bound element kernels */
 fem_gpu_status fem_gpu_probe_fp64_tflops(int32_t iters, double* tflops);

@@ -226,5 +226,16 @@ class FemModel:
         return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual,
                     seconds=r.seconds)
 
+    def autotune(self, max_elements=0):
+        self._check(self.L.fem_gpu_autotune(self.h, max_elements), "autotune")
+
+    def variant(self, s):
+        v, ms, name = C.c_int32(), C.c_double(), C.c_char_p()
+        self._check(self.L.fem_gpu_get_variant(self.h, s, C.byref(v), C.byref(ms), C.byref(name)), "get_variant")
+        return v.value, ms.value, (name.value or b"").decode()
+
+    def set_variant(self, s, v):
+        self._check(self.L.fem_gpu_set_variant(self.h, s, v), "set_variant")
+
     def launch_count(self):
         return self.L.fem_gpu_launch_count(self.h)

@@ -69,6 +69,9 @@ SIGNATURES = {
     "fem_gpu_assemble": (I32, [P, P, P, P, U32]),
     "fem_gpu_apply": (I32, [P, P, P, U32]),
     "fem_gpu_pcg": (I32, [P, P, P, P, P, P, P, P, U32]),
+    "fem_gpu_autotune": (I32, [P, I64]),
+    "fem_gpu_get_variant": (I32, [P, I32, P, P, P]),
+    "fem_gpu_set_variant": (I32, [P, I32, I32]),
     "fem_gpu_probe_fp64_tflops": (I32, [I32, P]),
     "fem_gpu_launch_count": (I64, [P]),
     "fem_gpu_last_error": (C.c_char_p, [P]),

@@ -1,0 +1,270 @@
+// fem_bulk_cta.cuh -- bulk elasticity with one element per CTA.
+//
+// Same arithmetic as the warp-per-element kernel in fem_device.cu (Gram
+// matrix of the physical gradients, isotropic K from it, sparse T^T K T,
+// CSR scatter), but the phases of one element are spread over NW warps and
+// several CTAs share an SM, so the FP64 pipe sees enough independent warps
+// to cover its latency.  Shared memory per CTA is sized so that 7 CTAs fit
+// on one SM for the hex8 / quadratic B-spline element (the extraction T is
+// staged in the tail of the Gauss-point region and is dead before the K T
+// product overwrites it).
+#pragma once
+
+// (included inside namespace fem of fem_device.cu)
+
+template <int D, int NPE, int NGP, int NB>
+struct CtaLayout {
+    static constexpr int NPD = D * NPE;
+    static constexpr int NAD = D * NB;
+    static constexpr int NSYM = NPD * (NPD + 1) / 2;
+    static constexpr int GPR = 2 * NGP * NPD;                      // g and w*g
+    static constexpr int R1 = (GPR + NPE * NB > NPD * NAD) ? GPR + NPE * NB : NPD * NAD;
+    static constexpr int oX = 0;
+    static constexpr int oR1 = oX + NPE * D;
+    static constexpr int oT = oR1 + GPR;                           // inside R1
+    static constexpr int oA = oR1 + R1;
+    static constexpr int oK = oA + NPD * NPD;
+    static constexpr int oTW = oK + NPD * NPD;
+    static constexpr int oU = oTW + NB * NPE;
+    static constexpr int oUA = oU + NPD;
+    static constexpr int oRP = oUA + NAD;
+    static constexpr int oW = oRP + NPD;
+    static constexpr int ND = oW + NGP;
+    static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + NAD, NI = iUL + NB;
+    static constexpr int bTN = 0, bTC = bTN + NB * NPE, bS = ((bTC + NB + 1) / 2) * 2;
+    static constexpr int NBYTE = bS + 2 * NB * NB;
+    static constexpr size_t kBytes = ((size_t)ND * 8 + (size_t)NI * 4 + (size_t)NBYTE + 15) / 16 * 16;
+};
+
+template <int D, int NPE, int NGP, int NB, bool RECT, int NW>
+__global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode) {
+    using L = CtaLayout<D, NPE, NGP, NB>;
+    constexpr int NPD = L::NPD, NAD = L::NAD, NSYM = L::NSYM, NT = 32 * NW;
+    extern __shared__ __align__(16) unsigned char smem[];
+    double* sd = reinterpret_cast<double*>(smem);
+    int32_t* si = reinterpret_cast<int32_t*>(sd + L::ND);
+    unsigned char* sb = reinterpret_cast<unsigned char*>(si + L::NI);
+    double* X = sd + L::oX;
+    double* g = sd + L::oR1;
+    double* wg = g + NGP * NPD;
+    double* KT = sd + L::oR1;
+    double* T = sd + L::oT;
+    double* A = sd + L::oA;
+    double* K = sd + L::oK;
+    double* TW = sd + L::oTW;
+    double* U = sd + L::oU;
+    double* UA = sd + L::oUA;
+    double* RP = sd + L::oRP;
+    double* WS = sd + L::oW;
+    int32_t* B = si + L::iB;
+    int32_t* RB = si + L::iRB;
+    int32_t* UL = si + L::iUL;
+    uint8_t* TN = sb + L::bTN;
+    uint8_t* TC = sb + L::bTC;
+    uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t* pairs = p.pairs;
+    const bool assemble = mode == MODE_ASSEMBLE;
+    const bool want_r = (assemble && p.rhs) || (mode == MODE_ELEMENT && p.Rout);
+    const bool want_k = (assemble && p.vals) || (mode == MODE_ELEMENT && p.Kout);
+
+    for (int64_t e = blockIdx.x; e < p.ne; e += gridDim.x) {
+        const int nb = p.nb[e];
+        const double E = p.E[e];
+        // ---- phase 0: loads --------------------------------------------------
+        for (int i = tid; i < NPE * D; i += NT) X[i] = p.xe[e * (NPE * D) + i];
+        for (int i = tid; i < NPE * NB; i += NT) T[i] = p.T[e * (NPE * NB) + i];
+        for (int i = tid; i < NB; i += NT) B[i] = p.bases[e * NB + i];
+        if (assemble && p.vals)
+            for (int i = tid; i < NB * NB; i += NT) S[i] = p.sidx[e * (NB * NB) + i];
+        __syncthreads();
+        // ---- phase 1: index data, column lists, Gauss-point geometry -----------
+        for (int r = tid; r < NAD; r += NT) {
+            const int f = r / NB, i = r - f * NB;
+            UA[r] = (p.u && i < nb) ? p.u[f * p.nu + B[i]] : 0.0;
+            if (assemble) RB[r] = i < nb ? p.rowptr[f * p.nu + B[i]] : 0;
+        }
+        for (int i = tid; i < NB; i += NT) {
+            if (assemble) UL[i] = i < nb ? p.ulen[B[i]] : 0;
+            int cnt = 0;
+            for (int a = 0; a < NPE; ++a) {
+                const double t = T[a * NB + i];
+                if (t != 0.0) {
+                    TN[i * NPE + cnt] = (uint8_t)a;
+                    TW[i * NPE + cnt] = t;
+                    ++cnt;
+                }
+            }
+            TC[i] = (uint8_t)cnt;
+        }
+        for (int q = tid; q < NGP; q += NT) {
+            const double* dn = p.dn + q * D * NPE;
+            double detJ, Ji[D][D];
+            if (RECT) {
+                double jd[D];
+                for (int i = 0; i < D; ++i) {
+                    double s = 0.0;
+                    for (int a = 0; a < NPE; ++a) s = fma(__ldg(dn + i * NPE + a), X[a * D + i], s);
+                    jd[i] = s;
+                }
+                detJ = (D == 3) ? jd[1] * jd[0] * jd[2] : jd[0] * jd[1];
+                for (int i = 0; i < D; ++i)
+                    for (int j = 0; j < D; ++j) Ji[i][j] = (i == j) ? 1.0 / jd[i] : 0.0;
+            } else {
+                double J[D][D];
+                for (int i = 0; i < D; ++i)
+                    for (int j = 0; j < D; ++j) {
+                        double s = 0.0;
+                        for (int a = 0; a < NPE; ++a) s = fma(__ldg(dn + i * NPE + a), X[a * D + j], s);
+                        J[i][j] = s;
+                    }
+                if (D == 2) {
+                    detJ = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+                    const double id = 1.0 / detJ;
+                    Ji[0][0] = J[1][1] * id;
+                    Ji[0][1] = -J[0][1] * id;
+                    Ji[1][0] = -J[1][0] * id;
+                    Ji[1][1] = J[0][0] * id;
+                } else {
+                    detJ = +J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+                    const double id = 1.0 / detJ;
+                    Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
+                    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+                    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+                    Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+                    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+                    Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
+                    Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+                    Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
+                    Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+                }
+            }
+            const double ws = (detJ < -1.0e-6) ? 0.0 : __ldg(p.w + q) * detJ;
+            WS[q] = ws;
+            for (int i = 0; i < D; ++i)
+                for (int a = 0; a < NPE; ++a) {
+                    double s;
+                    if (RECT) {
+                        s = Ji[i][i] * __ldg(dn + i * NPE + a);
+                    } else {
+                        s = 0.0;
+                        for (int k = 0; k < D; ++k) s = fma(Ji[i][k], __ldg(dn + k * NPE + a), s);
+                    }
+                    g[q * NPD + i * NPE + a] = s;
+                    wg[q * NPD + i * NPE + a] = ws * s;
+                }
+        }
+        __syncthreads();
+        // ---- phase 2: pdof values and the Gram matrix ---------------------------
+        if (want_r)
+            for (int r = tid; r < NPD; r += NT) {
+                const int f = r / NPE, a = r - f * NPE;
+                double s = 0.0;
+                for (int j = 0; j < nb; ++j) {
+                    const double t = T[a * NB + j];
+                    if (t != 0.0) s = fma(t, UA[f * NB + j], s);
+                }
+                U[r] = s;
+            }
+        for (int k = tid; k < NSYM; k += NT) {
+            const uint32_t pc = __ldg(pairs + k);
+            const int r = pc >> 16, c = pc & 0xffff;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+            int q = 0;
+            for (; q + 2 < NGP; q += 3) {
+                s0 = fma(wg[q * NPD + r], g[q * NPD + c], s0);
+                s1 = fma(wg[(q + 1) * NPD + r], g[(q + 1) * NPD + c], s1);
+                s2 = fma(wg[(q + 2) * NPD + r], g[(q + 2) * NPD + c], s2);
+            }
+            for (; q < NGP; ++q) s0 = fma(wg[q * NPD + r], g[q * NPD + c], s0);
+            const double s = s0 + s1 + s2;
+            A[r * NPD + c] = s;
+            A[c * NPD + r] = s;
+        }
+        __syncthreads();
+        // ---- phase 3: isotropic stiffness in pdof space ---------------------------
+        {
+            const double lam = E * p.lam_c, mu = E * p.mu_c;
+            for (int k = tid; k < NSYM; k += NT) {
+                const uint32_t pc = __ldg(pairs + k);
+                const int r = pc >> 16, c = pc & 0xffff;
+                const int f = r / NPE, a = r - f * NPE, gg = c / NPE, b = c - gg * NPE;
+                double v = lam * A[r * NPD + c] + mu * A[(gg * NPE + a) * NPD + f * NPE + b];
+                if (f == gg) {
+                    double tr = 0.0;
+                    for (int kk = 0; kk < D; ++kk) tr += A[(kk * NPE + a) * NPD + kk * NPE + b];
+                    v = fma(mu, tr, v);
+                }
+                K[r * NPD + c] = v;
+                K[c * NPD + r] = v;
+            }
+        }
+        __syncthreads();
+        // ---- phase 4: pdof residual and K T ----------------------------------------
+        if (want_r)
+            for (int r = tid; r < NPD; r += NT) {
+                double s = 0.0;
+                for (int c = 0; c < NPD; ++c) s = fma(K[r * NPD + c], U[c], s);
+                RP[r] = s;
+            }
+        if (want_k) {
+            constexpr int CPP = NPD >= 32 ? 1 : 32 / NPD;  // columns per warp pass
+            const int row = lane % NPD, sub = lane / NPD;
+            if (sub < CPP)
+                for (int c = warp * CPP + sub; c < NAD; c += NW * CPP) {
+                    const int gg = c / NB, j = c - gg * NB;
+                    const int cnt = j < nb ? TC[j] : 0;
+                    double s = 0.0;
+                    for (int k = 0; k < cnt; ++k) s = fma(K[row * NPD + gg * NPE + TN[j * NPE + k]], TW[j * NPE + k], s);
+                    KT[row * NAD + c] = s;
+                }
+        }
+        __syncthreads();
+        // ---- phase 5: residual scatter, T^T (K T) upper triangle and scatter --------
+        if (want_r)
+            for (int r = tid; r < NAD; r += NT) {
+                const int f = r / NB, i = r - f * NB;
+                double s = 0.0;
+                if (i < nb)
+                    for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
+                if (assemble) {
+                    if (i < nb) atomicAdd(p.rhs + f * p.nu + B[i], s);
+                } else {
+                    p.Rout[(e - p.first) * p.nmax + r] = s;
+                }
+            }
+        if (want_k) {
+            bool bad = false;
+            // rows r and NAD-1-r share one pass: NAD+1 entries of the upper triangle
+            constexpr int NPAIR = (NAD + 1) / 2;
+            for (int pr = warp; pr < NPAIR; pr += NW) {
+                const int r1 = pr, r2 = NAD - 1 - pr;
+                const int n1 = NAD - r1, n2 = (r2 > r1) ? NAD - r2 : 0;
+                for (int t = lane; t < n1 + n2; t += 32) {
+                    const int r = t < n1 ? r1 : r2;
+                    const int c = t < n1 ? r1 + t : r2 + (t - n1);
+                    const int f = r / NB, i = r - f * NB, gg = c / NB, j = c - gg * NB;
+                    if (i >= nb || j >= nb) continue;
+                    const int cnt = TC[i];
+                    double v = 0.0;
+                    for (int k = 0; k < cnt; ++k)
+                        v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + c], v);
+                    bad |= !isfinite(v);
+                    if (assemble) {
+                        atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
+                        if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
+                    } else {
+                        double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
+                        Ko[r + (int64_t)c * p.nmax] = v;
+                        Ko[c + (int64_t)r * p.nmax] = v;
+                    }
+                }
+            }
+            if (bad) atomicOr(p.status, 1);
+        }
+        __syncthreads();
+    }
+}
+

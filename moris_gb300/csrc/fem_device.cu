@@ -78,6 +78,7 @@ struct BulkArgs {
     const int32_t* ulen;
     const double* dn;     // [NGP][D][NPE]
     const double* w;      // [NGP]
+    const uint32_t* pairs;// upper-triangle (r << 16 | c) pairs of the pdof Gram matrix
     int64_t nu;
     double lam_c, mu_c;   // lambda / E and mu / E
     const double* u;      // adof vector (nullable)
@@ -423,6 +424,8 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
     }
 }
 
+#include "fem_bulk_cta.cuh"
+
 // ---------------------------------------------------------------------------
 // side sets (Neumann traction, Nitsche Dirichlet) on interpolation-cell
 // facets: one thread per facet (these sets are small: the boundary of the
@@ -653,23 +656,36 @@ __global__ void side_kernel(SideArgs p) {
 
 // ---------------------------------------------------------------------------
 // launch plumbing
-struct BulkLaunch {
-    const void* fn;
-    size_t cta_bytes, warp_bytes;
+// Kernel variants of one element type; the autotuner picks one per set.
+enum { VAR_WARP4 = 0, VAR_CTA2 = 1, VAR_CTA4 = 2, VAR_CTA8 = 3, NUM_VARIANTS = 4 };
+const char* const kVariantNames[NUM_VARIANTS] = {"warp-per-element x4", "cta-per-element 2 warps",
+                                                 "cta-per-element 4 warps", "cta-per-element 8 warps"};
+
+struct BulkVariant {
+    const void* fn = nullptr;
+    int threads = 0;       // per CTA
+    int per_cta = 0;       // elements in flight per CTA (warp kernel: warps)
+    size_t smem = 0;
+    bool warp_kernel = false;
 };
 
 template <int D, int NPE, int NGP, int NB, bool RECT>
-BulkLaunch bulk_launch() {
-    using L = BulkLayout<D, NPE, NGP, NB>;
-    return {(const void*)bulk_kernel<D, NPE, NGP, NB, RECT>, L::kCtaBytes, L::kWarpBytes};
+void fill_variants(BulkVariant* v) {
+    using LW = BulkLayout<D, NPE, NGP, NB>;
+    using LC = CtaLayout<D, NPE, NGP, NB>;
+    v[VAR_WARP4] = {(const void*)bulk_kernel<D, NPE, NGP, NB, RECT>, 128, 4, LW::kCtaBytes + 4 * LW::kWarpBytes, true};
+    v[VAR_CTA2] = {(const void*)bulk_cta_kernel<D, NPE, NGP, NB, RECT, 2>, 64, 1, LC::kBytes, false};
+    v[VAR_CTA4] = {(const void*)bulk_cta_kernel<D, NPE, NGP, NB, RECT, 4>, 128, 1, LC::kBytes, false};
+    v[VAR_CTA8] = {(const void*)bulk_cta_kernel<D, NPE, NGP, NB, RECT, 8>, 256, 1, LC::kBytes, false};
 }
 
-bool pick_bulk(int dim, int ngp, int nb, bool rect, BulkLaunch& out, int& NBsel) {
-#define FEM_PICK(D, NPE, NGP, NB)                                                          \
-    if (dim == D && ngp == NGP && nb <= NB) {                                              \
-        out = rect ? bulk_launch<D, NPE, NGP, NB, true>() : bulk_launch<D, NPE, NGP, NB, false>(); \
-        NBsel = NB;                                                                        \
-        return true;                                                                       \
+bool pick_bulk(int dim, int ngp, int nb, bool rect, BulkVariant* out, int& NBsel) {
+#define FEM_PICK(D, NPE, NGP, NB)                                                               \
+    if (dim == D && ngp == NGP && nb <= NB) {                                                   \
+        if (rect) fill_variants<D, NPE, NGP, NB, true>(out);                                    \
+        else fill_variants<D, NPE, NGP, NB, false>(out);                                        \
+        NBsel = NB;                                                                             \
+        return true;                                                                            \
     }
     FEM_PICK(2, 4, 4, 4)
     FEM_PICK(2, 4, 4, 9)
@@ -701,7 +717,7 @@ fem_gpu_status ensure_device(fem_gpu_ctx* c) {
         cudaGetLastError();
         return fail(c, FEM_GPU_NO_DEVICE, "no CUDA device");
     }
-    if (!c->stream) {
+    if (!c->stream && !c->stream_set) {
         cudaStream_t s;
         cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
         if (e != cudaSuccess) return cuda_fail(c, e, "stream create");
@@ -781,34 +797,34 @@ int sm_count() {
     return n > 0 ? n : 1;
 }
 
-// Tuning of the bulk launch: warps per CTA (chosen per set by the autotuner
-// in fem_tune.cu; default 4).
-int g_bulk_warps = 4;
-
 fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int64_t count, const double* u,
                            double* vals, double* rhs, double* Kout, double* Rout, int nmax, const double* x,
-                           double* y) {
+                           double* y, int force_variant = -1) {
     SetData& s = c->sets[si];
-    SetData& ds = s;
-    BulkLaunch L;
+    BulkVariant vars[NUM_VARIANTS];
     int nbsel = 0;
     const bool rect = c->shape == FEM_GPU_SHAPE_RECTANGULAR;
     if (!s.ig_off.empty()) return fail(c, FEM_GPU_UNSUPPORTED, "non-trivial clusters use the cut-cell kernel");
-    if (!pick_bulk(c->dim, ds.ngp, s.maxnb, rect, L, nbsel) || nbsel != ds.nbsel)
+    if (!pick_bulk(c->dim, s.ngp, s.maxnb, rect, vars, nbsel) || nbsel != s.nbsel)
         return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
+    int vi = force_variant >= 0 ? force_variant : s.variant;
+    if (mode == MODE_APPLY) vi = VAR_WARP4;  // the matrix-free product lives in the warp kernel
+    const BulkVariant& V = vars[vi];
     BulkArgs a{};
-    a.ne = first + count;
-    a.first = first;
-    a.xe = (const double*)s.d_xe.p;
-    a.E = (const double*)s.d_E.p;
-    a.nb = (const int32_t*)s.d_nb.p;
-    a.bases = (const int32_t*)s.d_bases.p;
-    a.T = (const double*)s.d_T.p;
-    a.sidx = (const uint16_t*)s.d_sidx.p;
+    a.ne = count;
+    a.first = 0;
+    const int NPE = c->npe, D = c->dim;
+    a.xe = (const double*)s.d_xe.p + first * NPE * D;
+    a.E = (const double*)s.d_E.p + first;
+    a.nb = (const int32_t*)s.d_nb.p + first;
+    a.bases = (const int32_t*)s.d_bases.p + first * nbsel;
+    a.T = (const double*)s.d_T.p + first * NPE * nbsel;
+    a.sidx = (const uint16_t*)s.d_sidx.p + first * nbsel * nbsel;
     a.rowptr = (const int32_t*)c->d_rowptr.p;
     a.ulen = (const int32_t*)c->d_ulen.p;
-    a.dn = (const double*)ds.d_dn.p;
-    a.w = (const double*)ds.d_w.p;
+    a.dn = (const double*)s.d_dn.p;
+    a.w = (const double*)s.d_w.p;
+    a.pairs = (const uint32_t*)s.d_pairs.p;
     a.nu = c->num_used;
     a.lam_c = lam_coef(s.bulk.model_type, s.bulk.poisson_ratio);
     a.mu_c = 1.0 / (2.0 * (1.0 + s.bulk.poisson_ratio));
@@ -821,30 +837,23 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.x = x;
     a.y = y;
     a.status = status_ptr(c);
-    const int W = g_bulk_warps;
-    const size_t smem = L.cta_bytes + (size_t)W * L.warp_bytes;
-    cudaError_t e = cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(V.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)V.smem);
     if (e != cudaSuccess) return cuda_fail(c, e, "bulk smem attribute");
-    // elements [first, first+count): the kernel walks e from first via the
-    // grid stride, so offset the block start through ne/first bookkeeping
-    int64_t blocks = (count + W - 1) / W;
-    const int64_t cap = (int64_t)sm_count() * 8;
+    // exactly the resident CTAs: the grid-stride loop then sweeps elements in
+    // order as one compact front, so the CSR rows it scatters into stay in L2
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, V.fn, V.threads, V.smem);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bulk occupancy");
+    if (per_sm < 1) return fail(c, FEM_GPU_UNSUPPORTED, "bulk kernel does not fit on an SM");
+    int64_t blocks = (count + V.per_cta - 1) / V.per_cta;
+    const int64_t cap = (int64_t)sm_count() * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    // shift pointers so that element index 0 of the kernel is `first`
-    if (first > 0) {
-        const int NPE = c->npe, D = c->dim;
-        a.xe += first * NPE * D;
-        a.E += first;
-        a.nb += first;
-        a.bases += first * nbsel;
-        a.T += first * NPE * nbsel;
-        a.sidx += first * nbsel * nbsel;
-        a.ne = count;
-        a.first = 0;
-    }
-    void* args[] = {&a, &mode, (void*)&W};
-    e = cudaLaunchKernel(L.fn, dim3((unsigned)blocks), dim3(32 * W), args, smem, stream_of(c));
+    int W = V.per_cta;
+    void* args_w[] = {&a, &mode, &W};
+    void* args_c[] = {&a, &mode};
+    e = cudaLaunchKernel(V.fn, dim3((unsigned)blocks), dim3(V.threads), V.warp_kernel ? args_w : args_c, V.smem,
+                         stream_of(c));
     if (e != cudaSuccess) return cuda_fail(c, e, "bulk launch");
     c->launches++;
     return FEM_GPU_OK;
@@ -908,6 +917,7 @@ void device_release(fem_gpu_ctx* c) {
         dfree(s.d_ord);
         dfree(s.d_dn);
         dfree(s.d_w);
+        dfree(s.d_pairs);
         dfree(s.d_gp);
         dfree(s.d_gw);
     }
@@ -947,11 +957,17 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
             }
             if ((e = upload(ds.d_dn, dn, sm)) != cudaSuccess) return cuda_fail(c, e, "dn table");
             if ((e = upload(ds.d_w, w, sm)) != cudaSuccess) return cuda_fail(c, e, "w table");
-            BulkLaunch L;
+            const int npd = D * NPE;
+            std::vector<uint32_t> pairs;
+            for (int rr = 0; rr < npd; ++rr)
+                for (int cc = rr; cc < npd; ++cc) pairs.push_back((uint32_t)rr << 16 | (uint32_t)cc);
+            if ((e = upload(ds.d_pairs, pairs, sm)) != cudaSuccess) return cuda_fail(c, e, "pair table");
+            BulkVariant vars[NUM_VARIANTS];
             int nbsel = 0;
-            if (s.ig_off.empty() && !pick_bulk(D, r.n, s.maxnb, c->shape == FEM_GPU_SHAPE_RECTANGULAR, L, nbsel))
+            if (s.ig_off.empty() && !pick_bulk(D, r.n, s.maxnb, c->shape == FEM_GPU_SHAPE_RECTANGULAR, vars, nbsel))
                 return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
             ds.nbsel = nbsel ? nbsel : s.maxnb;
+            ds.variant = VAR_CTA4;
         } else {
             const Rule r = gauss_rule(s.side.integration_rule);
             ds.ngp = r.n;
@@ -1024,6 +1040,7 @@ fem_gpu_status fem_gpu_set_stream(fem_gpu_ctx* c, void* stream) {
     }
     c->stream = stream;
     c->own_stream = false;
+    c->stream_set = true;
     return FEM_GPU_OK;
 }
 
@@ -1182,6 +1199,91 @@ fem_gpu_status fem_gpu_apply(fem_gpu_ctx* c, const double* x, double* y, uint32_
     release(c, sx);
     release(c, sy);
     return st;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// autotuner: per bulk set, time every kernel variant on the set's own elements
+// (assembly into a scratch CSR) and keep the fastest.
+extern "C" {
+
+fem_gpu_status fem_gpu_autotune(fem_gpu_ctx* c, int64_t max_elements) {
+    if (!c) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    cudaStream_t sm = stream_of(c);
+    const int64_t nad = c->num_used * c->dim;
+    double *vals = nullptr, *rhs = nullptr, *u = nullptr;
+    cudaError_t e = cudaMallocAsync(&vals, std::max<int64_t>(c->nnz, 1) * sizeof(double), sm);
+    if (e == cudaSuccess) e = cudaMallocAsync(&rhs, nad * sizeof(double), sm);
+    if (e == cudaSuccess) e = cudaMallocAsync(&u, nad * sizeof(double), sm);
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotune scratch");
+    cudaMemsetAsync(vals, 0, c->nnz * sizeof(double), sm);
+    cudaMemsetAsync(rhs, 0, nad * sizeof(double), sm);
+    cudaMemsetAsync(u, 0, nad * sizeof(double), sm);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fem_gpu_status st = FEM_GPU_OK;
+    for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
+        SetData& s = c->sets[k];
+        if (s.kind != 0 || !s.ig_off.empty()) continue;
+        const int64_t n = max_elements > 0 ? std::min(max_elements, s.neq) : s.neq;
+        double best = 1e30;
+        int bestv = s.variant;
+        for (int v = 0; v < NUM_VARIANTS && st == FEM_GPU_OK; ++v) {
+            // a variant that does not fit (shared memory / registers) is skipped
+            st = launch_bulk(c, k, MODE_ASSEMBLE, 0, n, u, vals, rhs, nullptr, nullptr, 0, nullptr, nullptr, v);
+            if (st == FEM_GPU_UNSUPPORTED) {
+                st = FEM_GPU_OK;
+                cudaGetLastError();
+                continue;
+            }
+            if (st != FEM_GPU_OK) break;
+            cudaEventRecord(e0, sm);
+            const int reps = 3;
+            for (int r = 0; r < reps && st == FEM_GPU_OK; ++r)
+                st = launch_bulk(c, k, MODE_ASSEMBLE, 0, n, u, vals, rhs, nullptr, nullptr, 0, nullptr, nullptr, v);
+            cudaEventRecord(e1, sm);
+            e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) {
+                st = cuda_fail(c, e, "autotune run");
+                break;
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms / reps < best) {
+                best = ms / reps;
+                bestv = v;
+            }
+        }
+        s.variant = bestv;
+        s.tuned_ms = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(vals, sm);
+    cudaFreeAsync(rhs, sm);
+    cudaFreeAsync(u, sm);
+    cudaStreamSynchronize(sm);
+    return st;
+}
+
+fem_gpu_status fem_gpu_get_variant(const fem_gpu_ctx* c, int32_t set, int32_t* variant, double* tuned_ms,
+                                   const char** name) {
+    if (!c || set < 0 || set >= (int32_t)c->sets.size()) return FEM_GPU_BAD_ARG;
+    const SetData& s = c->sets[set];
+    if (variant) *variant = s.variant;
+    if (tuned_ms) *tuned_ms = s.tuned_ms;
+    if (name) *name = (s.kind == 0 && s.variant >= 0 && s.variant < NUM_VARIANTS) ? kVariantNames[s.variant] : "";
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_gpu_set_variant(fem_gpu_ctx* c, int32_t set, int32_t variant) {
+    if (!c || set < 0 || set >= (int32_t)c->sets.size() || variant < 0 || variant >= NUM_VARIANTS)
+        return FEM_GPU_BAD_ARG;
+    c->sets[set].variant = variant;
+    return FEM_GPU_OK;
 }
 
 }  // extern "C"

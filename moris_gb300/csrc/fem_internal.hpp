@@ -51,9 +51,12 @@ struct SetData {
     // device copies
     DeviceBuf d_nb, d_bases, d_T, d_sidx, d_xe, d_E, d_ord;
     DeviceBuf d_dn, d_w;    // bulk: dN/dxi of the IP cell at the Gauss points, weights
+    DeviceBuf d_pairs;      // bulk: upper-triangle index pairs of the pdof Gram matrix
     DeviceBuf d_gp, d_gw;   // side: facet Gauss points and weights
     int ngp = 0;            // Gauss points of the set's rule
     int nbsel = 0;          // padded basis width of the kernel instance
+    int variant = 0;        // bulk kernel variant (set by fem_gpu_autotune)
+    double tuned_ms = 0.0;  // time of the chosen variant on the tuning run
 };
 
 }  // namespace fem
@@ -79,6 +82,7 @@ struct fem_gpu_ctx {
     // device state
     void* stream = nullptr;            // cudaStream_t
     bool own_stream = false;
+    bool stream_set = false;           // caller chose a stream (NULL = legacy default stream)
     fem::DeviceBuf d_rowptr, d_ulen, d_tables, d_scratch, d_status;
     int64_t launches = 0;
     std::string err;

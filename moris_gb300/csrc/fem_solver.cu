@@ -184,14 +184,23 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     if (flags & FEM_GPU_HOST_BUFFERS) return fail(c, FEM_GPU_UNSUPPORTED, "pcg takes device buffers");
     if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
     if (!(opts->rel_tol > 0.0) || opts->max_iter < 1) return FEM_GPU_BAD_ARG;
-    if (!c->stream) {
+    if (!c->stream && !c->stream_set) {
         cudaStream_t s;
         if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
             return fail(c, FEM_GPU_CUDA_ERROR, "stream create");
         c->stream = s;
         c->own_stream = true;
     }
+    // stream capture needs a non-default stream: on the legacy default stream
+    // the solve runs on a private stream after the default stream's work
     cudaStream_t sm = (cudaStream_t)c->stream;
+    cudaStream_t own = nullptr;
+    if (!sm) {
+        if (cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(c, FEM_GPU_CUDA_ERROR, "stream create");
+        cudaStreamSynchronize(nullptr);
+        sm = own;
+    }
     const int64_t n = c->num_used * c->dim;
     const auto t0 = std::chrono::steady_clock::now();
     double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
@@ -245,6 +254,7 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     cudaFreeAsync(r, sm);
     cudaFreeAsync(st, sm);
     cudaStreamSynchronize(sm);
+    if (own) cudaStreamDestroy(own);
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (rep) {
         rep->iterations = hs.done == 1 ? hs.converged_at : hs.it;

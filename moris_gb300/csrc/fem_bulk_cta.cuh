@@ -8,7 +8,25 @@
 // on one SM for the hex8 / quadratic B-spline element (the extraction T is
 // staged in the tail of the Gauss-point region and is dead before the K T
 // product overwrites it).
+//
+// RECT (axis-aligned brick cells, the reference's CellShape::RECTANGULAR with
+// its diagonal Jacobian): a trilinear map whose Jacobian is diagonal at every
+// Gauss point is affine, so J is constant over the cell and the Gram matrix is
+//   A[(i,a),(j,b)] = detJ / (J_ii J_jj) * G0[(i,a),(j,b)],
+//   G0 = sum_q w_q dN_a/dxi_i dN_b/dxi_j          (per-rule table, p.g0),
+// which replaces 27 FMAs per Gram entry by one multiply.  J is evaluated at
+// the first Gauss point like the reference evaluates it at every point.
+//
+// MODE_APPLY (matrix-free Jacobian-vector product) forms the pdof K the same
+// way and scatters T^T (K T x) without the K T / T^T K T stages.
 #pragma once
+
+__device__ __forceinline__ bool fem_nonzero(double t) {
+    return (__double_as_longlong(t) << 1) != 0;  // bit test, keeps the FP64 pipe free
+}
+__device__ __forceinline__ bool fem_finite(double t) {
+    return (__double_as_longlong(t) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
 
 // (included inside namespace fem of fem_device.cu)
 
@@ -29,7 +47,8 @@ struct CtaLayout {
     static constexpr int oUA = oU + NPD;
     static constexpr int oRP = oUA + NAD;
     static constexpr int oW = oRP + NPD;
-    static constexpr int ND = oW + NGP;
+    static constexpr int oCJ = oW + NGP;                           // RECT: detJ/(J_ii J_jj), i<=j
+    static constexpr int ND = oCJ + 8;
     static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + NAD, NI = iUL + NB;
     static constexpr int bTN = 0, bTC = bTN + NB * NPE, bS = ((bTC + NB + 1) / 2) * 2;
     static constexpr int NBYTE = bS + 2 * NB * NB;
@@ -56,6 +75,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     double* UA = sd + L::oUA;
     double* RP = sd + L::oRP;
     double* WS = sd + L::oW;
+    double* CJ = sd + L::oCJ;
     int32_t* B = si + L::iB;
     int32_t* RB = si + L::iRB;
     int32_t* UL = si + L::iUL;
@@ -64,9 +84,11 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t* pairs = p.pairs;
-    const bool assemble = mode == MODE_ASSEMBLE;
+    const bool assemble = mode == MODE_ASSEMBLE, apply = mode == MODE_APPLY;
     const bool want_r = (assemble && p.rhs) || (mode == MODE_ELEMENT && p.Rout);
     const bool want_k = (assemble && p.vals) || (mode == MODE_ELEMENT && p.Kout);
+    const bool need_u = want_r || apply;
+    const double* uin = apply ? p.x : p.u;
 
     for (int64_t e = blockIdx.x; e < p.ne; e += gridDim.x) {
         const int nb = p.nb[e];
@@ -81,7 +103,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         // ---- phase 1: index data, column lists, Gauss-point geometry -----------
         for (int r = tid; r < NAD; r += NT) {
             const int f = r / NB, i = r - f * NB;
-            UA[r] = (p.u && i < nb) ? p.u[f * p.nu + B[i]] : 0.0;
+            UA[r] = (uin && i < nb) ? uin[f * p.nu + B[i]] : 0.0;
             if (assemble) RB[r] = i < nb ? p.rowptr[f * p.nu + B[i]] : 0;
         }
         for (int i = tid; i < NB; i += NT) {
@@ -89,7 +111,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             int cnt = 0;
             for (int a = 0; a < NPE; ++a) {
                 const double t = T[a * NB + i];
-                if (t != 0.0) {
+                if (fem_nonzero(t)) {
                     TN[i * NPE + cnt] = (uint8_t)a;
                     TW[i * NPE + cnt] = t;
                     ++cnt;
@@ -97,6 +119,24 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             }
             TC[i] = (uint8_t)cnt;
         }
+        if (RECT) {
+            // constant Jacobian of the brick: diagonal at the first Gauss point
+            if (tid == 0) {
+                double jd[D];
+                for (int i = 0; i < D; ++i) {
+                    double s = 0.0;
+                    for (int a = 0; a < NPE; ++a) s = fma(__ldg(p.dn + i * NPE + a), X[a * D + i], s);
+                    jd[i] = s;
+                }
+                const double detJ = (D == 3) ? jd[1] * jd[0] * jd[2] : jd[0] * jd[1];
+                // integration points with detJ below -1e-6 are skipped by the
+                // reference element loop (cl_FEM_Element_Bulk.cpp:164)
+                const double dj = (detJ < -1.0e-6) ? 0.0 : detJ;
+                int k = 0;
+                for (int i = 0; i < D; ++i)
+                    for (int j = i; j < D; ++j) CJ[k++] = dj / (jd[i] * jd[j]);
+            }
+        } else
         for (int q = tid; q < NGP; q += NT) {
             const double* dn = p.dn + q * D * NPE;
             double detJ, Ji[D][D];
@@ -157,33 +197,35 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 }
         }
         __syncthreads();
-        // ---- phase 2: pdof values and the Gram matrix ---------------------------
-        if (want_r)
+        // ---- phase 2: pdof values and (general cells) the Gram matrix ------------
+        if (need_u)
             for (int r = tid; r < NPD; r += NT) {
                 const int f = r / NPE, a = r - f * NPE;
                 double s = 0.0;
                 for (int j = 0; j < nb; ++j) {
                     const double t = T[a * NB + j];
-                    if (t != 0.0) s = fma(t, UA[f * NB + j], s);
+                    if (fem_nonzero(t)) s = fma(t, UA[f * NB + j], s);
                 }
                 U[r] = s;
             }
-        for (int k = tid; k < NSYM; k += NT) {
-            const uint32_t pc = __ldg(pairs + k);
-            const int r = pc >> 16, c = pc & 0xffff;
-            double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-            int q = 0;
-            for (; q + 2 < NGP; q += 3) {
-                s0 = fma(wg[q * NPD + r], g[q * NPD + c], s0);
-                s1 = fma(wg[(q + 1) * NPD + r], g[(q + 1) * NPD + c], s1);
-                s2 = fma(wg[(q + 2) * NPD + r], g[(q + 2) * NPD + c], s2);
+        if (!RECT) {
+            for (int k = tid; k < NSYM; k += NT) {
+                const uint32_t pc = __ldg(pairs + k);
+                const int r = pc >> 16, c = pc & 0xffff;
+                double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+                int q = 0;
+                for (; q + 2 < NGP; q += 3) {
+                    s0 = fma(wg[q * NPD + r], g[q * NPD + c], s0);
+                    s1 = fma(wg[(q + 1) * NPD + r], g[(q + 1) * NPD + c], s1);
+                    s2 = fma(wg[(q + 2) * NPD + r], g[(q + 2) * NPD + c], s2);
+                }
+                for (; q < NGP; ++q) s0 = fma(wg[q * NPD + r], g[q * NPD + c], s0);
+                const double s = s0 + s1 + s2;
+                A[r * NPD + c] = s;
+                A[c * NPD + r] = s;
             }
-            for (; q < NGP; ++q) s0 = fma(wg[q * NPD + r], g[q * NPD + c], s0);
-            const double s = s0 + s1 + s2;
-            A[r * NPD + c] = s;
-            A[c * NPD + r] = s;
+            __syncthreads();
         }
-        __syncthreads();
         // ---- phase 3: isotropic stiffness in pdof space ---------------------------
         {
             const double lam = E * p.lam_c, mu = E * p.mu_c;
@@ -191,11 +233,25 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 const uint32_t pc = __ldg(pairs + k);
                 const int r = pc >> 16, c = pc & 0xffff;
                 const int f = r / NPE, a = r - f * NPE, gg = c / NPE, b = c - gg * NPE;
-                double v = lam * A[r * NPD + c] + mu * A[(gg * NPE + a) * NPD + f * NPE + b];
-                if (f == gg) {
-                    double tr = 0.0;
-                    for (int kk = 0; kk < D; ++kk) tr += A[(kk * NPE + a) * NPD + kk * NPE + b];
-                    v = fma(mu, tr, v);
+                double v;
+                if (RECT) {
+                    // A = c_ij G0: c_fg (lam G0[(f,a),(g,b)] + mu G0[(g,a),(f,b)]) + mu tr
+                    const int lo = f < gg ? f : gg, hi = f < gg ? gg : f;
+                    const double cfg = CJ[lo * D - lo * (lo - 1) / 2 + (hi - lo)];
+                    v = cfg * (lam * __ldg(p.g0 + r * NPD + c) + mu * __ldg(p.g0 + (gg * NPE + a) * NPD + f * NPE + b));
+                    if (f == gg) {
+                        double tr = 0.0;
+                        for (int kk = 0; kk < D; ++kk)
+                            tr = fma(CJ[kk * D - kk * (kk - 1) / 2], __ldg(p.g0 + (kk * NPE + a) * NPD + kk * NPE + b), tr);
+                        v = fma(mu, tr, v);
+                    }
+                } else {
+                    v = lam * A[r * NPD + c] + mu * A[(gg * NPE + a) * NPD + f * NPE + b];
+                    if (f == gg) {
+                        double tr = 0.0;
+                        for (int kk = 0; kk < D; ++kk) tr += A[(kk * NPE + a) * NPD + kk * NPE + b];
+                        v = fma(mu, tr, v);
+                    }
                 }
                 K[r * NPD + c] = v;
                 K[c * NPD + r] = v;
@@ -203,7 +259,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 4: pdof residual and K T ----------------------------------------
-        if (want_r)
+        if (need_u)
             for (int r = tid; r < NPD; r += NT) {
                 double s = 0.0;
                 for (int c = 0; c < NPD; ++c) s = fma(K[r * NPD + c], U[c], s);
@@ -223,7 +279,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 5: residual scatter, T^T (K T) upper triangle and scatter --------
-        if (want_r)
+        if (need_u)
             for (int r = tid; r < NAD; r += NT) {
                 const int f = r / NB, i = r - f * NB;
                 double s = 0.0;
@@ -231,6 +287,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                     for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
                 if (assemble) {
                     if (i < nb) atomicAdd(p.rhs + f * p.nu + B[i], s);
+                } else if (apply) {
+                    if (i < nb) atomicAdd(p.y + f * p.nu + B[i], s);
                 } else {
                     p.Rout[(e - p.first) * p.nmax + r] = s;
                 }
@@ -251,7 +309,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                     double v = 0.0;
                     for (int k = 0; k < cnt; ++k)
                         v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + c], v);
-                    bad |= !isfinite(v);
+                    bad |= !fem_finite(v);
                     if (assemble) {
                         atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
                         if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);

@@ -79,6 +79,7 @@ struct BulkArgs {
     const double* dn;     // [NGP][D][NPE]
     const double* w;      // [NGP]
     const uint32_t* pairs;// upper-triangle (r << 16 | c) pairs of the pdof Gram matrix
+    const double* g0;     // [NPD][NPD] reference Gram table sum_q w_q dN dN (rectangular cells)
     int64_t nu;
     double lam_c, mu_c;   // lambda / E and mu / E
     const double* u;      // adof vector (nullable)
@@ -808,7 +809,7 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     if (!pick_bulk(c->dim, s.ngp, s.maxnb, rect, vars, nbsel) || nbsel != s.nbsel)
         return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
     int vi = force_variant >= 0 ? force_variant : s.variant;
-    if (mode == MODE_APPLY) vi = VAR_WARP4;  // the matrix-free product lives in the warp kernel
+    if (mode == MODE_APPLY && vi == VAR_WARP4) vi = VAR_CTA4;
     const BulkVariant& V = vars[vi];
     BulkArgs a{};
     a.ne = count;
@@ -825,6 +826,7 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.dn = (const double*)s.d_dn.p;
     a.w = (const double*)s.d_w.p;
     a.pairs = (const uint32_t*)s.d_pairs.p;
+    a.g0 = (const double*)s.d_g0.p;
     a.nu = c->num_used;
     a.lam_c = lam_coef(s.bulk.model_type, s.bulk.poisson_ratio);
     a.mu_c = 1.0 / (2.0 * (1.0 + s.bulk.poisson_ratio));
@@ -918,6 +920,7 @@ void device_release(fem_gpu_ctx* c) {
         dfree(s.d_dn);
         dfree(s.d_w);
         dfree(s.d_pairs);
+        dfree(s.d_g0);
         dfree(s.d_gp);
         dfree(s.d_gw);
     }
@@ -962,6 +965,16 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
             for (int rr = 0; rr < npd; ++rr)
                 for (int cc = rr; cc < npd; ++cc) pairs.push_back((uint32_t)rr << 16 | (uint32_t)cc);
             if ((e = upload(ds.d_pairs, pairs, sm)) != cudaSuccess) return cuda_fail(c, e, "pair table");
+            // reference Gram table of the rule (constant-Jacobian cells)
+            std::vector<double> g0((size_t)npd * npd, 0.0);
+            for (int rr = 0; rr < npd; ++rr)
+                for (int cc = 0; cc < npd; ++cc) {
+                    double acc = 0.0;
+                    for (int q = 0; q < r.n; ++q)
+                        acc += r.w[q] * dn[(size_t)q * npd + rr] * dn[(size_t)q * npd + cc];
+                    g0[(size_t)rr * npd + cc] = acc;
+                }
+            if ((e = upload(ds.d_g0, g0, sm)) != cudaSuccess) return cuda_fail(c, e, "g0 table");
             BulkVariant vars[NUM_VARIANTS];
             int nbsel = 0;
             if (s.ig_off.empty() && !pick_bulk(D, r.n, s.maxnb, c->shape == FEM_GPU_SHAPE_RECTANGULAR, vars, nbsel))

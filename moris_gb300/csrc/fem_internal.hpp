@@ -52,6 +52,7 @@ struct SetData {
     DeviceBuf d_nb, d_bases, d_T, d_sidx, d_xe, d_E, d_ord;
     DeviceBuf d_dn, d_w;    // bulk: dN/dxi of the IP cell at the Gauss points, weights
     DeviceBuf d_pairs;      // bulk: upper-triangle index pairs of the pdof Gram matrix
+    DeviceBuf d_g0;         // bulk: reference Gram table sum_q w_q dN/dxi dN/dxi
     DeviceBuf d_gp, d_gw;   // side: facet Gauss points and weights
     int ngp = 0;            // Gauss points of the set's rule
     int nbsel = 0;          // padded basis width of the kernel instance

@@ -57,25 +57,35 @@ def workload(ne):
     return mesh, E
 
 
-def flops_per_element_c2():
-    """FP64 flop count (FMA = 2) of the kernel's formulation for one interior
-    hex8 / quadratic B-spline element with 27 Gauss points.  Column counts of
-    the extraction: per direction the two end nodes see 1 or 2 bases, so a
-    basis column of T has tc = product over directions of (1 or 2) nonzeros."""
-    tc1 = [1, 2, 1]  # nodes (of 2) seeing basis j = 0, 1, 2 in one direction
+def flops_per_element_c2(rect=True):
+    """FP64 flop count (FMA = 2, other ops 1) of the kernel's formulation for
+    one interior hex8 / quadratic B-spline element with 27 Gauss points.
+
+    Column counts of the extraction T (8 nodes x 27 bases): per direction the
+    two end nodes see bases 0, 1, 2 with (1, 2, 1) nonzeros, so column j has
+    tc_j = product over directions (sum 64 = 8 nonzeros per node row).
+    rect=True is the constant-Jacobian (brick) path: the Gram matrix is a
+    scaled per-rule table; rect=False the per-Gauss-point path."""
+    tc1 = [1, 2, 1]
     tc = [a * b * c for c in tc1 for b in tc1 for a in tc1]  # 27 columns, sum 64
     NGP, NPD, NB, D = 27, 24, 27, 3
-    geo = NGP * (2 * D * 8 + 2 + D + 2 * NPD + 1)          # diag J, detJ, 1/J, g, w*g
-    upd = NPD * 8 * 2                                     # u_pdof = T u_adof
-    gram = (NPD * (NPD + 1) // 2) * NGP * 2               # upper triangle of A
-    kiso = (NPD * (NPD + 1) // 2) * 3 + 3 * 36 * 4        # K from A (diag blocks: trace)
-    resid = NPD * NPD * 2 + D * sum(tc) * 2               # R_p = K u, R_a = T^T R_p
-    kt = NPD * D * sum(tc) * 2                            # KT = K T
-    ka = 0                                                # upper triangle of T^T KT
+    nsym = NPD * (NPD + 1) // 2
+    if rect:
+        geo = D * 8 * 2 + 2 + D + 4                           # diagonal J, detJ, 3 divisions, products
+        gram = 0
+        kiso = nsym * 4 + 3 * 36 * 8                          # c_fg (lam G0 + mu G0') (+ trace on diagonal blocks)
+    else:
+        geo = NGP * (D * D * 8 * 2 + 40 + D * D * 8 * 2 + 1 + NPD)  # J, inverse, g = J^-1 dN, w*, w*g
+        gram = nsym * NGP * 2                                 # upper triangle of A
+        kiso = nsym * 3 + 3 * 36 * 4
+    upd = NPD * 8 * 2                                         # u_pdof = T u_adof
+    resid = NPD * NPD * 2 + D * sum(tc) * 2                   # R_p = K u, R_a = T^T R_p
+    kt = (D * (D + 1) // 2) * 8 * sum(tc) * 2                 # K T on the field blocks g >= f
+    ka = 0                                                    # upper triangle of T^T (K T)
     nad = D * NB
     for r in range(nad):
         ka += tc[r % NB] * (nad - r) * 2
-    return geo + upd + gram + kiso + resid + kt + ka
+    return geo + gram + kiso + upd + resid + kt + ka
 
 
 class ClockSampler:
@@ -315,6 +325,8 @@ def main():
         return
     # roofline of the dominant kernel (FP64 pipe bound)
     peak = mg.probe_fp64_tflops()
+    dmma_alone = mg.probe_dmma_tflops()
+    dmma_mixed = mg.probe_dmma_tflops(mixed=True)
     fpe = flops_per_element_c2()
     achieved = fpe * nc / (ms_kernel * 1e-3) / 1e12
     traffic = None
@@ -337,7 +349,8 @@ def main():
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": "measured in-run (FP64 FMA-chain probe, fem_gpu_probe_fp64_tflops)",
-                     "flops_per_element": fpe, "kernel_ms": ms_kernel},
+                     "flops_per_element": fpe, "kernel_ms": ms_kernel,
+                     "fp64_tensor_probe_tflops": {"dmma": dmma_alone, "dmma_plus_dfma": dmma_mixed}},
         "kernel_variant": {"index": variant[0], "name": variant[2], "tuned_ms": variant[1]},
         "jv": {"ms_per_apply": ms_jv, "elements_per_s": nc / (ms_jv * 1e-3), "rel_err_vs_csr": jv_err},
         "setup_seconds": setup_s,

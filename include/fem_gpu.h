@@ -230,6 +230,9 @@ fem_gpu_status fem_gpu_set_variant(fem_gpu_ctx* ctx, int32_t set, int32_t varian
 /* in-run FP64 peak probe (FMA chains on every SM, CUDA-event timed), the
    roofline denominator of the FP64-bound element kernels */
 fem_gpu_status fem_gpu_probe_fp64_tflops(int32_t iters, double* tflops);
+/* FP64 tensor-core (DMMA m8n8k4) throughput, alone (mixed = 0) or with half
+   of the warps issuing FP64 FMA chains at the same time (mixed = 1) */
+fem_gpu_status fem_gpu_probe_dmma_tflops(int32_t iters, int32_t mixed, double* tflops);
 /* number of kernel launches issued by the context since creation */
 int64_t fem_gpu_launch_count(const fem_gpu_ctx* ctx);
 /* last error text of the context (never NULL) */

@@ -68,6 +68,15 @@ def probe_fp64_tflops(iters=20000):
     return t.value
 
 
+def probe_dmma_tflops(iters=300, mixed=False):
+    """Measured FP64 tensor-core (DMMA) throughput, optionally mixed with DFMA."""
+    t = C.c_double()
+    st = lib().fem_gpu_probe_dmma_tflops(iters, 1 if mixed else 0, C.byref(t))
+    if st:
+        raise FemGpuError(st, "probe_dmma_tflops")
+    return t.value
+
+
 def hmr_uniform_mesh(dim, num_elements, lengths, bspline_order):
     """Uniform level-0 HMR-equivalent mesh: dict of numpy arrays."""
     L = lib()

@@ -73,6 +73,7 @@ SIGNATURES = {
     "fem_gpu_get_variant": (I32, [P, I32, P, P, P]),
     "fem_gpu_set_variant": (I32, [P, I32, I32]),
     "fem_gpu_probe_fp64_tflops": (I32, [I32, P]),
+    "fem_gpu_probe_dmma_tflops": (I32, [I32, I32, P]),
     "fem_gpu_launch_count": (I64, [P]),
     "fem_gpu_last_error": (C.c_char_p, [P]),
 }

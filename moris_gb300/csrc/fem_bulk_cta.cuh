@@ -50,7 +50,7 @@ struct CtaLayout {
     static constexpr int oCJ = oW + NGP;                           // RECT: detJ/(J_ii J_jj), i<=j
     static constexpr int ND = oCJ + 8;
     static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + NAD, NI = iUL + NB;
-    static constexpr int bTN = 0, bTC = bTN + NB * NPE, bS = ((bTC + NB + 1) / 2) * 2;
+    static constexpr int bTN = 0, bTC = bTN + NB * NPE, bCP = bTC + NB, bS = ((bCP + NB + 1) / 2) * 2;
     static constexpr int NBYTE = bS + 2 * NB * NB;
     static constexpr size_t kBytes = ((size_t)ND * 8 + (size_t)NI * 4 + (size_t)NBYTE + 15) / 16 * 16;
 };
@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     int32_t* UL = si + L::iUL;
     uint8_t* TN = sb + L::bTN;
     uint8_t* TC = sb + L::bTC;
+    uint8_t* CP = sb + L::bCP;  // columns of T ordered by nonzero count
     uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t* pairs = p.pairs;
@@ -120,8 +121,10 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             TC[i] = (uint8_t)cnt;
         }
         if (RECT) {
-            // constant Jacobian of the brick: diagonal at the first Gauss point
-            if (tid == 0) {
+            // constant Jacobian of the brick: diagonal at the first Gauss point;
+            // CJ[i<=j] = detJ / (J_ii J_jj): off-diagonal factors are the
+            // remaining J entry (3D) or 1 (2D), diagonal ones one division each
+            if (tid < D) {
                 double jd[D];
                 for (int i = 0; i < D; ++i) {
                     double s = 0.0;
@@ -131,10 +134,18 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 const double detJ = (D == 3) ? jd[1] * jd[0] * jd[2] : jd[0] * jd[1];
                 // integration points with detJ below -1e-6 are skipped by the
                 // reference element loop (cl_FEM_Element_Bulk.cpp:164)
-                const double dj = (detJ < -1.0e-6) ? 0.0 : detJ;
-                int k = 0;
-                for (int i = 0; i < D; ++i)
-                    for (int j = i; j < D; ++j) CJ[k++] = dj / (jd[i] * jd[j]);
+                const bool skip = detJ < -1.0e-6;
+                const int i = tid;
+                double other = 1.0;  // product of the other diagonal entries
+                for (int k = 0; k < D; ++k)
+                    if (k != i) other *= jd[k];
+                CJ[i * D - i * (i - 1) / 2] = skip ? 0.0 : other / jd[i];
+                if (D == 3 && i == 0) {
+                    CJ[1] = skip ? 0.0 : jd[2];   // (0,1)
+                    CJ[2] = skip ? 0.0 : jd[1];   // (0,2)
+                    CJ[4] = skip ? 0.0 : jd[0];   // (1,2)
+                }
+                if (D == 2 && i == 0) CJ[1] = skip ? 0.0 : 1.0;
             }
         } else
         for (int q = tid; q < NGP; q += NT) {
@@ -198,6 +209,13 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 2: pdof values and (general cells) the Gram matrix ------------
+        if (want_k && tid == NT - 1) {
+            // counting sort of the T columns by nonzero count
+            int pos = 0;
+            for (int c = 0; c <= NPE; ++c)
+                for (int j = 0; j < NB; ++j)
+                    if (TC[j] == c) CP[pos++] = (uint8_t)j;
+        }
         if (need_u)
             for (int r = tid; r < NPD; r += NT) {
                 const int f = r / NPE, a = r - f * NPE;
@@ -266,16 +284,30 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 RP[r] = s;
             }
         if (want_k) {
-            constexpr int CPP = NPD >= 32 ? 1 : 32 / NPD;  // columns per warp pass
-            const int row = lane % NPD, sub = lane / NPD;
-            if (sub < CPP)
-                for (int c = warp * CPP + sub; c < NAD; c += NW * CPP) {
-                    const int gg = c / NB, j = c - gg * NB;
-                    const int cnt = j < nb ? TC[j] : 0;
-                    double s = 0.0;
-                    for (int k = 0; k < cnt; ++k) s = fma(K[row * NPD + gg * NPE + TN[j * NPE + k]], TW[j * NPE + k], s);
-                    KT[row * NAD + c] = s;
+            // K T for the field blocks (f, g >= f) that the upper triangle of
+            // T^T K T reads; a warp pass covers NPE rows x CPP columns of one
+            // block, columns taken in order of their nonzero count
+            constexpr int CPP = 32 / NPE;
+            constexpr int PASSES = (NB + CPP - 1) / CPP;
+            constexpr int NBLK = D * (D + 1) / 2;
+            const int a = lane % NPE, sub = lane / NPE;
+            for (int w = warp; w < NBLK * PASSES; w += NW) {
+                const int blk = w / PASSES, pass = w - blk * PASSES;
+                int f = 0, bb = blk;
+                while (bb >= D - f) {
+                    bb -= D - f;
+                    ++f;
                 }
+                const int gg = f + bb;
+                const int slot = pass * CPP + sub;
+                if (slot >= NB) continue;
+                const int j = CP[slot];
+                const int cnt = j < nb ? TC[j] : 0;
+                const double* Krow = K + (f * NPE + a) * NPD + gg * NPE;
+                double s = 0.0;
+                for (int k = 0; k < cnt; ++k) s = fma(Krow[TN[j * NPE + k]], TW[j * NPE + k], s);
+                KT[(f * NPE + a) * NAD + gg * NB + j] = s;
+            }
         }
         __syncthreads();
         // ---- phase 5: residual scatter, T^T (K T) upper triangle and scatter --------

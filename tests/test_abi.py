@@ -33,3 +33,20 @@ def test_library_answers_without_gpu():
     assert lib.fem_gpu_abi_version() == 1
     assert lib.fem_gpu_status_string(0) == b"ok"
     assert lib.fem_gpu_device_count() >= 0
+
+
+def test_cpp_layer_compiles():
+    """include/fem_gpu_solver_interface.hpp compiles as C++17 against the C ABI."""
+    import shutil
+    import subprocess
+    import tempfile
+    if not shutil.which("g++"):
+        import pytest
+        pytest.skip("no g++")
+    src = '#include "fem_gpu_solver_interface.hpp"\nint main() { return sizeof(moris_gb300::Gpu_Solver_Interface) > 0 ? 0 : 1; }\n'
+    with tempfile.TemporaryDirectory() as d:
+        f = os.path.join(d, "t.cpp")
+        open(f, "w").write(src)
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), f],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr

@@ -220,6 +220,18 @@ fem_gpu_status fem_gpu_apply(fem_gpu_ctx* ctx, const double* x, double* y, uint3
 fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                            const double* b, double* x, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report,
                            uint32_t flags);
+/* PCG for callers that cannot allocate device memory during the solve
+   (host callbacks, real-time sections, frameworks with a fixed device
+   memory budget).  No counterpart in the reference.  Same algorithm and
+   arguments as fem_gpu_pcg, but the work vectors live in one fixed-size
+   device array of the library (systems up to 131072 rows; larger ones are
+   rejected with FEM_GPU_BAD_ARG, nothing allocated).  Calls no cudaMalloc /
+   cudaFree.  The first call on a device resolves the array's device address
+   (make that first call before any stream capture).  All calls share the
+   array: calls that overlap on the GPU race. */
+fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx,
+                                   const double* vals, const double* b, double* x, const fem_gpu_pcg_opts* opts,
+                                   fem_gpu_pcg_report* report, uint32_t flags);
 /* autotuner: times every kernel variant of each bulk set on (up to
    max_elements, <= 0 = all) of its elements, assembling into scratch
    buffers, and keeps the fastest per set.  Setup-time call; optional. */

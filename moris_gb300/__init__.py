@@ -235,6 +235,17 @@ class FemModel:
         return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual,
                     seconds=r.seconds)
 
+    def pcg_noalloc(self, rowptr, colidx, vals, b, x, rel_tol=1e-10, max_iter=100000, jacobi=True):
+        """fem_gpu_pcg_noalloc: PCG in the library's fixed device array (no
+        device allocation; at most 131072 rows)."""
+        o = PcgOpts(rel_tol, max_iter, 1 if jacobi else 0)
+        r = PcgReport()
+        st = self.L.fem_gpu_pcg_noalloc(self.h, _dev_ptr(rowptr), _dev_ptr(colidx), _dev_ptr(vals), _dev_ptr(b),
+                                        _dev_ptr(x), C.byref(o), C.byref(r), 0)
+        self._check(st, "pcg_noalloc")
+        return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual,
+                    seconds=r.seconds)
+
     def autotune(self, max_elements=0):
         self._check(self.L.fem_gpu_autotune(self.h, max_elements), "autotune")
 

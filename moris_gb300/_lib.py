@@ -69,6 +69,7 @@ SIGNATURES = {
     "fem_gpu_assemble": (I32, [P, P, P, P, U32]),
     "fem_gpu_apply": (I32, [P, P, P, U32]),
     "fem_gpu_pcg": (I32, [P, P, P, P, P, P, P, P, U32]),
+    "fem_gpu_pcg_noalloc": (I32, [P, P, P, P, P, P, P, P, U32]),
     "fem_gpu_autotune": (I32, [P, I64]),
     "fem_gpu_get_variant": (I32, [P, I32, P, P, P]),
     "fem_gpu_set_variant": (I32, [P, I32, I32]),

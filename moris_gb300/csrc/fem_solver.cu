@@ -15,6 +15,8 @@
 
 #include <chrono>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "fem_internal.hpp"
@@ -266,5 +268,116 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     if (result != FEM_GPU_OK) return result;
     if (hs.done == 2) return fail(c, FEM_GPU_NONFINITE, "pcg breakdown");
     if (hs.done != 1) return fail(c, FEM_GPU_NOT_CONVERGED, "pcg hit max_iter");
+    return FEM_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// PCG without device allocation.
+//
+// Some callers cannot allocate device memory while they solve: code that runs
+// inside a host callback, a signal-safe or real-time section, or a framework
+// that owns a fixed device memory budget and forbids cudaMalloc/cudaFree (and
+// any allocating library call) after start-up.  For them the Jacobi-PCG work
+// vectors live in one file-scope device array of fixed size instead of
+// stream-ordered allocations, and the iterations are launched directly (no
+// graph instantiation).  The array holds the solver state (first 256 bytes)
+// and the five work vectors r, z, p, q and 1/diag(A), so systems up to
+// kNoAllocMaxRows rows are accepted; larger ones are rejected with
+// FEM_GPU_BAD_ARG.  Every GPU that loads the library keeps this array
+// (about 5.2 MB) until the process exits.
+namespace {
+
+constexpr int64_t kNoAllocMaxRows = 131072;
+constexpr int64_t kNoAllocStateDoubles = 32;  // 256 bytes for CgState
+static_assert(sizeof(CgState) <= kNoAllocStateDoubles * sizeof(double), "CgState fits the state slot");
+
+static __device__ __align__(256) double g_pcg_noalloc_scratch[kNoAllocStateDoubles + 5 * kNoAllocMaxRows];
+
+// device address of the scratch array, resolved once per device with that
+// device current (the host-side symbol is only a stand-in, never a device
+// address)
+constexpr int kMaxDevices = 64;
+double* g_scratch_addr[kMaxDevices] = {nullptr};
+std::mutex g_scratch_mutex;
+
+fem_gpu_status noalloc_scratch(fem_gpu_ctx* c, double** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return fail(c, FEM_GPU_NO_DEVICE, "pcg_noalloc: no current CUDA device");
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg_noalloc: scratch address: ") + cudaGetErrorString(e));
+        g_scratch_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_scratch_addr[dev];
+    return FEM_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx,
+                                              const double* vals, const double* b, double* x,
+                                              const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep,
+                                              uint32_t flags) {
+    if (!c || !rowptr || !colidx || !vals || !b || !x || !opts) return FEM_GPU_BAD_ARG;
+    if (flags & FEM_GPU_HOST_BUFFERS) return fail(c, FEM_GPU_UNSUPPORTED, "pcg_noalloc takes device buffers");
+    if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
+    if (!(opts->rel_tol > 0.0) || opts->max_iter < 1) return FEM_GPU_BAD_ARG;
+    const int64_t n = c->num_used * c->dim;
+    if (n > kNoAllocMaxRows)
+        return fail(c, FEM_GPU_BAD_ARG,
+                    "pcg_noalloc: " + std::to_string(n) + " rows exceed the fixed scratch limit of " +
+                        std::to_string(kNoAllocMaxRows) + " rows; use fem_gpu_pcg");
+    double* base = nullptr;
+    fem_gpu_status st = noalloc_scratch(c, &base);
+    if (st != FEM_GPU_OK) return st;
+    // the caller's stream, or the legacy default stream when none was set
+    cudaStream_t sm = (cudaStream_t)c->stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    CgState* cs = reinterpret_cast<CgState*>(base);
+    double* r = base + kNoAllocStateDoubles;
+    double* z = r + n;
+    double* p = z + n;
+    double* q = p + n;
+    double* dinv = q + n;
+    // the array keeps the previous call's contents: the state must start at zero
+    cudaError_t e = cudaMemsetAsync(cs, 0, sizeof(CgState), sm);
+    if (e != cudaSuccess) return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg_noalloc: ") + cudaGetErrorString(e));
+    const int tpb = 256;
+    const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
+                                                                opts->preconditioner == 1);
+    k_init<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, b, x, r, z, p, dinv, cs);
+    k_set_thresh<<<1, 1, 0, sm>>>(cs, opts->rel_tol);
+    c->launches += 3;
+    CgState hs{};
+    const int chunk = 32;
+    for (int launched = 0; launched < opts->max_iter + chunk; launched += chunk) {
+        for (int k = 0; k < chunk; ++k) {
+            k_spmv_pq<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, p, q, cs);
+            k_update_xr<<<vec_blocks, tpb, 0, sm>>>(n, x, r, z, p, q, dinv, cs);
+            k_update_p<<<vec_blocks, tpb, 0, sm>>>(n, p, z, cs);
+            k_advance<<<1, 1, 0, sm>>>(cs, opts->max_iter);
+        }
+        c->launches += 4 * chunk;
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, cs, sizeof(CgState), cudaMemcpyDeviceToHost, sm);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+        if (e != cudaSuccess) return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg_noalloc: ") + cudaGetErrorString(e));
+        if (hs.done) break;
+    }
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rep) {
+        rep->iterations = hs.done == 1 ? hs.converged_at : hs.it;
+        rep->converged = hs.done == 1;
+        rep->rel_residual = std::sqrt(hs.ring[hs.it & 3][2] / (hs.bn2 > 0 ? hs.bn2 : 1.0));
+        rep->seconds = secs;
+    }
+    if (hs.done == 2) return fail(c, FEM_GPU_NONFINITE, "pcg_noalloc breakdown");
+    if (hs.done != 1) return fail(c, FEM_GPU_NOT_CONVERGED, "pcg_noalloc hit max_iter");
     return FEM_GPU_OK;
 }

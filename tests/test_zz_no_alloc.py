@@ -1,0 +1,66 @@
+"""The allocation-free PCG entry point (fem_gpu_pcg_noalloc).
+
+Some callers cannot allocate device memory while they solve (host callbacks,
+real-time sections, frameworks with a fixed device memory budget).  For them
+fem_gpu_pcg_noalloc keeps its work vectors in one fixed device array of the
+library.  This file checks, through the C ABI, that two calls in a row give
+the same solution as fem_gpu_pcg (the allocating entry point) within the
+tolerance of the solver tests, and that a system above the array's limit is
+rejected before anything runs.  It is collected last on purpose.
+"""
+import numpy as np
+import pytest
+
+import moris_gb300 as mg
+from tests.common import problem, rel_err
+
+pytestmark = pytest.mark.gpu
+
+# the solver tests' tolerance: the block reductions of both entry points sum
+# in a non-deterministic order, so the iterate at which the 1e-10 residual is
+# reached can differ by an iteration or two
+SOLVE_RTOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+def _system(torch, ne):
+    prod, _, _ = problem(2, ne, 1, sides=True)
+    prod.finalize()
+    rp, ci = prod.graph()
+    rpt = torch.tensor(rp, device="cuda")
+    cit = torch.tensor(ci, device="cuda")
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(None, vals, rhs)
+    return prod, rpt, cit, vals, -rhs
+
+
+def test_noalloc_pcg_matches_allocating_pcg_twice(torch):
+    prod, rpt, cit, vals, b = _system(torch, (24, 20))
+    x_ref = torch.zeros_like(b)
+    rep_ref = prod.pcg(rpt, cit, vals, b, x_ref, rel_tol=1e-10)
+    assert rep_ref["converged"]
+    for _ in range(2):  # the second call reuses the array left by the first
+        x = torch.full_like(b, 0.0)
+        rep = prod.pcg_noalloc(rpt, cit, vals, b, x, rel_tol=1e-10)
+        torch.cuda.synchronize()
+        assert rep["converged"] and rep["rel_residual"] <= 1e-10
+        assert abs(rep["iterations"] - rep_ref["iterations"]) <= max(3, rep_ref["iterations"] // 20)
+        assert rel_err(x.cpu().numpy(), x_ref.cpu().numpy()) <= SOLVE_RTOL
+
+
+def test_noalloc_pcg_rejects_systems_above_its_limit(torch):
+    prod, rpt, cit, vals, b = _system(torch, (260, 260))  # 2 * 261^2 = 136242 rows
+    assert prod.num_adofs > 131072
+    x = torch.zeros_like(b)
+    with pytest.raises(mg.FemGpuError) as ei:
+        prod.pcg_noalloc(rpt, cit, vals, b, x)
+    assert ei.value.status == 1 and "131072" in str(ei.value)
+    assert np.all(x.cpu().numpy() == 0.0)

@@ -360,6 +360,23 @@ def main():
                        "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]}
     if clocks:
         line["clocks"] = clocks
+    # config 1: 2D plane-strain cantilever, assembly + Jacobi-PCG to 1e-10
+    if world == 1:
+        from moris_gb300 import workloads
+        m1, _, _ = workloads.plane_strain_cantilever(128)
+        m1.set_stream(stream.cuda_stream)
+        rp1 = torch.empty(m1.num_adofs + 1, dtype=torch.int32, device="cuda")
+        ci1 = torch.empty(m1.nnz, dtype=torch.int32, device="cuda")
+        m1.graph_device(rp1, ci1)
+        v1 = torch.empty(m1.nnz, dtype=torch.float64, device="cuda")
+        r1 = torch.empty(m1.num_adofs, dtype=torch.float64, device="cuda")
+        ms_a1 = timed(lambda: m1.assemble(None, v1, r1), 10, 3)
+        x1 = torch.zeros_like(r1)
+        t0 = time.perf_counter()
+        rep1 = m1.pcg(rp1, ci1, v1, -r1, x1, rel_tol=1e-10)
+        line["c1_solve"] = {"workload": "2D plane strain 128^2 quad4, linear B-splines, Nitsche clamp, traction 1e-3",
+                            "adofs": m1.num_adofs, "assembly_ms": ms_a1, "pcg_ms": (time.perf_counter() - t0) * 1e3,
+                            "pcg_iterations": rep1["iterations"], "rel_residual": rep1["rel_residual"]}
     if world == 1 and not args.no_cpu:
         r = cpu_reference(mesh, E, args.cpu_seconds)
         line["cpu_baseline"] = {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",

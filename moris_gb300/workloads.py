@@ -1,0 +1,51 @@
+"""Seeded input builders of the benchmark workloads (host side, over the C ABI).
+
+Each builder returns a finalized FemModel plus the arrays a caller needs.  The
+same seeds and arrays feed the oracle in the tests.
+
+* plane_strain_cantilever -- 2D linear elasticity (E = 1, nu = 0.3, plane
+  strain) on a uniform n x n QUAD4 mesh of the unit square with linear
+  B-spline extraction, QUAD_2x2; clamped at x = 0 by the symmetric Nitsche
+  Dirichlet IWG (alpha = 100, the reference's weak-clamp mechanism), traction
+  (1e-3, 0) at x = 1 by the Neumann IWG, BAR_3 on the edges.
+* elasticity_3d -- 3D linear elasticity on an n^3 HEX8 mesh of the unit cube,
+  quadratic B-spline extraction, HEX_3x3x3, E per element log-uniform in
+  [1e-3, 1] (splitmix64), nu = 0.3.
+"""
+import numpy as np
+
+from . import (FemModel, IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, IWG_STRUC_LINEAR_NEUMANN, MODEL_3D,
+               MODEL_PLANE_STRAIN, RULE_BAR_3, RULE_HEX_3x3x3, RULE_QUAD_2x2, SHAPE_RECTANGULAR, hmr_uniform_mesh)
+from .rng import uniform01
+
+BASE_SEED = 20261203
+NITSCHE_ALPHA = 100.0
+TRACTION = 1e-3
+
+
+def plane_strain_cantilever(n=128, finalize=True):
+    mesh = hmr_uniform_mesh(2, (n, n), (1.0, 1.0), 1)
+    nc = len(mesh["cells"])
+    E = np.ones(nc)
+    m = FemModel(2, mesh, SHAPE_RECTANGULAR)
+    m.add_bulk_set(np.arange(nc, dtype=np.int32), E, 0.3, RULE_QUAD_2x2, MODEL_PLANE_STRAIN)
+    left = np.arange(0, nc, n, dtype=np.int32)
+    right = np.arange(n - 1, nc, n, dtype=np.int32)
+    m.add_side_set(IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, left, np.full(len(left), 3), E[left], 0.3,
+                   RULE_BAR_3, MODEL_PLANE_STRAIN, alpha=NITSCHE_ALPHA, value=(0.0, 0.0))
+    m.add_side_set(IWG_STRUC_LINEAR_NEUMANN, right, np.full(len(right), 1), E[right], 0.3, RULE_BAR_3,
+                   MODEL_PLANE_STRAIN, value=(TRACTION, 0.0))
+    if finalize:
+        m.finalize()
+    return m, mesh, E
+
+
+def elasticity_3d(n=64, seed=BASE_SEED + 2, finalize=True):
+    mesh = hmr_uniform_mesh(3, (n, n, n), (1.0, 1.0, 1.0), 2)
+    nc = len(mesh["cells"])
+    E = 10.0 ** (-3.0 + 3.0 * uniform01(seed, nc))
+    m = FemModel(3, mesh, SHAPE_RECTANGULAR)
+    m.add_bulk_set(np.arange(nc, dtype=np.int32), E, 0.3, RULE_HEX_3x3x3, MODEL_3D)
+    if finalize:
+        m.finalize()
+    return m, mesh, E

@@ -132,8 +132,14 @@ typedef struct fem_gpu_bulk_set_desc {
     const int64_t* ig_offsets;
     const double* ig_coords;
     const double* ig_param_coords;
-    const double* youngs_modulus; /* per cluster */
+    const double* youngs_modulus; /* per cluster (E0 when node_density is given) */
     double poisson_ratio;
+    /* optional SIMP-style material: E(x) = youngs_modulus * rho(x)^density_exponent
+       with rho interpolated at each Gauss point from this nodal field (one value
+       per mesh node), as the reference's density-dependent Young's modulus
+       property (EXA/optimization/SIMP/SIMP.cpp:43-51).  NULL = constant E. */
+    const double* node_density;
+    double density_exponent;
 } fem_gpu_bulk_set_desc;
 
 /* Side set on interpolation-cell facets (trivial side clusters):

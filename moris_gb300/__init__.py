@@ -137,8 +137,9 @@ class FemModel:
         self._check(self.L.fem_gpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
 
     def add_bulk_set(self, ip_cells, youngs, poisson, rule, model, ig_cell=None, ig_offsets=None, ig_coords=None,
-                     ig_param=None):
+                     ig_param=None, node_density=None, density_exponent=3.0):
         ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)
+        rho = None if node_density is None else np.ascontiguousarray(node_density, dtype=np.float64)
         E = np.ascontiguousarray(youngs, dtype=np.float64)
         off = None if ig_offsets is None else np.ascontiguousarray(ig_offsets, dtype=np.int64)
         xc = None if ig_coords is None else np.ascontiguousarray(ig_coords, dtype=np.float64)
@@ -146,7 +147,7 @@ class FemModel:
         if ig_cell is None:
             ig_cell = CELL_QUAD4 if self.dim == 2 else CELL_HEX8
         d = BulkSetDesc(IWG_STRUC_LINEAR_BULK, ig_cell, rule, model, len(ipc), _np_ptr(ipc), _np_ptr(off),
-                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson)
+                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson, _np_ptr(rho), density_exponent)
         idx = C.c_int32()
         self._check(self.L.fem_gpu_add_bulk_set(self.h, C.byref(d), C.byref(idx)), "add_bulk_set")
         self.num_sets += 1

@@ -26,7 +26,8 @@ class MeshDesc(C.Structure):
 class BulkSetDesc(C.Structure):
     _fields_ = [("iwg_type", I32), ("ig_cell_type", I32), ("integration_rule", I32), ("model_type", I32),
                 ("num_clusters", I64), ("cluster_ip_cell", P), ("ig_offsets", P), ("ig_coords", P),
-                ("ig_param_coords", P), ("youngs_modulus", P), ("poisson_ratio", D)]
+                ("ig_param_coords", P), ("youngs_modulus", P), ("poisson_ratio", D), ("node_density", P),
+                ("density_exponent", D)]
 
 
 class SideSetDesc(C.Structure):

@@ -24,6 +24,15 @@
 __device__ __forceinline__ bool fem_nonzero(double t) {
     return (__double_as_longlong(t) << 1) != 0;  // bit test, keeps the FP64 pipe free
 }
+// E0-relative SIMP factor rho(x_q)^beta with rho interpolated from the nodal
+// densities by the IP-cell shape functions at Gauss point q
+__device__ __forceinline__ double fem_density_power(const BulkArgs& p, const double* rho_nodes, int q) {
+    constexpr int kMaxNodes = 8;
+    double r = 0.0;
+    const int npe = p.npe;
+    for (int a = 0; a < npe && a < kMaxNodes; ++a) r = fma(__ldg(p.nq + q * npe + a), rho_nodes[a], r);
+    return p.beta == 3.0 ? r * r * r : pow(r, p.beta);
+}
 __device__ __forceinline__ bool fem_finite(double t) {
     return (__double_as_longlong(t) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
 }
@@ -48,7 +57,8 @@ struct CtaLayout {
     static constexpr int oRP = oUA + NAD;
     static constexpr int oW = oRP + NPD;
     static constexpr int oCJ = oW + NGP;                           // RECT: detJ/(J_ii J_jj), i<=j
-    static constexpr int ND = oCJ + 8;
+    static constexpr int oRHO = oCJ + 8;                           // nodal densities (SIMP sets)
+    static constexpr int ND = oRHO + NPE;
     static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + NAD, NI = iUL + NB;
     static constexpr int bTN = 0, bTC = bTN + NB * NPE, bCP = bTC + NB, bS = ((bCP + NB + 1) / 2) * 2;
     static constexpr int NBYTE = bS + 2 * NB * NB;
@@ -76,6 +86,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     double* RP = sd + L::oRP;
     double* WS = sd + L::oW;
     double* CJ = sd + L::oCJ;
+    double* RHO = sd + L::oRHO;
     int32_t* B = si + L::iB;
     int32_t* RB = si + L::iRB;
     int32_t* UL = si + L::iUL;
@@ -98,6 +109,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         for (int i = tid; i < NPE * D; i += NT) X[i] = p.xe[e * (NPE * D) + i];
         for (int i = tid; i < NPE * NB; i += NT) T[i] = p.T[e * (NPE * NB) + i];
         for (int i = tid; i < NB; i += NT) B[i] = p.bases[e * NB + i];
+        if (p.rho)
+            for (int i = tid; i < NPE; i += NT) RHO[i] = p.rho[e * NPE + i];
         if (assemble && p.vals)
             for (int i = tid; i < NB * NB; i += NT) S[i] = p.sidx[e * (NB * NB) + i];
         __syncthreads();
@@ -147,6 +160,9 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 }
                 if (D == 2 && i == 0) CJ[1] = skip ? 0.0 : 1.0;
             }
+            // SIMP material: w_q E0 rho(x_q)^beta (the Jacobian factors stay in CJ)
+            if (p.rho)
+                for (int q = tid; q < NGP; q += NT) WS[q] = __ldg(p.w + q) * E * fem_density_power(p, RHO, q);
         } else
         for (int q = tid; q < NGP; q += NT) {
             const double* dn = p.dn + q * D * NPE;
@@ -192,7 +208,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                     Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
                 }
             }
-            const double ws = (detJ < -1.0e-6) ? 0.0 : __ldg(p.w + q) * detJ;
+            double ws = (detJ < -1.0e-6) ? 0.0 : __ldg(p.w + q) * detJ;
+            if (p.rho) ws *= E * fem_density_power(p, RHO, q);
             WS[q] = ws;
             for (int i = 0; i < D; ++i)
                 for (int a = 0; a < NPE; ++a) {
@@ -226,6 +243,18 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 }
                 U[r] = s;
             }
+        if (RECT && p.rho) {
+            // density-weighted reference Gram matrix of this element
+            for (int k = tid; k < NSYM; k += NT) {
+                const uint32_t pc = __ldg(pairs + k);
+                const int r = pc >> 16, c = pc & 0xffff;
+                double s = 0.0;
+                for (int q = 0; q < NGP; ++q) s = fma(WS[q] * __ldg(p.dn + q * NPD + r), __ldg(p.dn + q * NPD + c), s);
+                A[r * NPD + c] = s;
+                A[c * NPD + r] = s;
+            }
+            __syncthreads();
+        }
         if (!RECT) {
             for (int k = tid; k < NSYM; k += NT) {
                 const uint32_t pc = __ldg(pairs + k);
@@ -246,21 +275,24 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         // ---- phase 3: isotropic stiffness in pdof space ---------------------------
         {
-            const double lam = E * p.lam_c, mu = E * p.mu_c;
+            // with a density field E(x_q) is already inside the Gram sums
+            const double escale = p.rho ? 1.0 : E;
+            const double lam = escale * p.lam_c, mu = escale * p.mu_c;
+            const double* G = p.rho ? A : p.g0;
             for (int k = tid; k < NSYM; k += NT) {
                 const uint32_t pc = __ldg(pairs + k);
                 const int r = pc >> 16, c = pc & 0xffff;
                 const int f = r / NPE, a = r - f * NPE, gg = c / NPE, b = c - gg * NPE;
                 double v;
                 if (RECT) {
-                    // A = c_ij G0: c_fg (lam G0[(f,a),(g,b)] + mu G0[(g,a),(f,b)]) + mu tr
+                    // A = c_ij G: c_fg (lam G[(f,a),(g,b)] + mu G[(g,a),(f,b)]) + mu tr
                     const int lo = f < gg ? f : gg, hi = f < gg ? gg : f;
                     const double cfg = CJ[lo * D - lo * (lo - 1) / 2 + (hi - lo)];
-                    v = cfg * (lam * __ldg(p.g0 + r * NPD + c) + mu * __ldg(p.g0 + (gg * NPE + a) * NPD + f * NPE + b));
+                    v = cfg * (lam * G[r * NPD + c] + mu * G[(gg * NPE + a) * NPD + f * NPE + b]);
                     if (f == gg) {
                         double tr = 0.0;
                         for (int kk = 0; kk < D; ++kk)
-                            tr = fma(CJ[kk * D - kk * (kk - 1) / 2], __ldg(p.g0 + (kk * NPE + a) * NPD + kk * NPE + b), tr);
+                            tr = fma(CJ[kk * D - kk * (kk - 1) / 2], G[(kk * NPE + a) * NPD + kk * NPE + b], tr);
                         v = fma(mu, tr, v);
                     }
                 } else {

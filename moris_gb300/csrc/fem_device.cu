@@ -80,6 +80,10 @@ struct BulkArgs {
     const double* w;      // [NGP]
     const uint32_t* pairs;// upper-triangle (r << 16 | c) pairs of the pdof Gram matrix
     const double* g0;     // [NPD][NPD] reference Gram table sum_q w_q dN dN (rectangular cells)
+    const double* rho;    // [ne][NPE] nodal densities (nullable: constant E per element)
+    const double* nq;     // [NGP][NPE] N of the IP cell at the Gauss points
+    double beta;          // density exponent
+    int npe;              // nodes per IP cell
     int64_t nu;
     double lam_c, mu_c;   // lambda / E and mu / E
     const double* u;      // adof vector (nullable)
@@ -809,6 +813,10 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     if (!pick_bulk(c->dim, s.ngp, s.maxnb, rect, vars, nbsel) || nbsel != s.nbsel)
         return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
     int vi = force_variant >= 0 ? force_variant : s.variant;
+    if (!s.rhoe.empty() && vi == VAR_WARP4) {
+        if (force_variant >= 0) return fail(c, FEM_GPU_UNSUPPORTED, "density sets use the CTA kernels");
+        vi = VAR_CTA4;
+    }
     if (mode == MODE_APPLY && vi == VAR_WARP4) vi = VAR_CTA4;
     const BulkVariant& V = vars[vi];
     BulkArgs a{};
@@ -827,6 +835,10 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.w = (const double*)s.d_w.p;
     a.pairs = (const uint32_t*)s.d_pairs.p;
     a.g0 = (const double*)s.d_g0.p;
+    a.rho = s.rhoe.empty() ? nullptr : (const double*)s.d_rho.p + first * NPE;
+    a.nq = (const double*)s.d_nq.p;
+    a.beta = s.bulk.density_exponent;
+    a.npe = NPE;
     a.nu = c->num_used;
     a.lam_c = lam_coef(s.bulk.model_type, s.bulk.poisson_ratio);
     a.mu_c = 1.0 / (2.0 * (1.0 + s.bulk.poisson_ratio));
@@ -921,6 +933,8 @@ void device_release(fem_gpu_ctx* c) {
         dfree(s.d_w);
         dfree(s.d_pairs);
         dfree(s.d_g0);
+        dfree(s.d_rho);
+        dfree(s.d_nq);
         dfree(s.d_gp);
         dfree(s.d_gw);
     }
@@ -952,12 +966,16 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
             const Rule r = gauss_rule(s.bulk.integration_rule);
             if (r.n > kMaxGP) return fail(c, FEM_GPU_UNSUPPORTED, "too many Gauss points");
             ds.ngp = r.n;
-            std::vector<double> dn((size_t)r.n * D * NPE), w(r.w);
+            std::vector<double> dn((size_t)r.n * D * NPE), w(r.w), nq((size_t)r.n * NPE);
             for (int q = 0; q < r.n; ++q) {
                 double N[8], d[24];
                 lagrange(c->ip_cell, &r.pts[(size_t)q * r.dim], N, d);
                 for (int i = 0; i < D * NPE; ++i) dn[(size_t)q * D * NPE + i] = d[i];
+                for (int a = 0; a < NPE; ++a) nq[(size_t)q * NPE + a] = N[a];
             }
+            if ((e = upload(ds.d_nq, nq, sm)) != cudaSuccess) return cuda_fail(c, e, "N table");
+            if (!s.rhoe.empty())
+                if ((e = upload(ds.d_rho, s.rhoe, sm)) != cudaSuccess) return cuda_fail(c, e, "densities");
             if ((e = upload(ds.d_dn, dn, sm)) != cudaSuccess) return cuda_fail(c, e, "dn table");
             if ((e = upload(ds.d_w, w, sm)) != cudaSuccess) return cuda_fail(c, e, "w table");
             const int npd = D * NPE;

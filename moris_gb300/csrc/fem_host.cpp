@@ -307,6 +307,13 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
         s.ig_coords.assign(d->ig_coords, d->ig_coords + nig * per);
         s.ig_param.assign(d->ig_param_coords, d->ig_param_coords + nig * per);
     }
+    if (d->node_density) {
+        if (!std::isfinite(d->density_exponent)) return fail(c, FEM_GPU_BAD_ARG, "density exponent");
+        s.node_rho.assign(d->node_density, d->node_density + c->num_nodes);
+        for (double r : s.node_rho)
+            if (!std::isfinite(r) || r < 0.0) return fail(c, FEM_GPU_NONFINITE, "node density must be finite and >= 0");
+    }
+    s.bulk.node_density = nullptr;
     s.bulk.cluster_ip_cell = nullptr;
     s.bulk.ig_offsets = nullptr;
     s.bulk.ig_coords = nullptr;
@@ -461,6 +468,7 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
         s.T.assign(s.neq * npe * maxnb, 0.0);
         s.sidx.assign(s.neq * maxnb * maxnb, 0);
         s.xe.resize(s.neq * npe * dim);
+        if (!s.node_rho.empty()) s.rhoe.resize(s.neq * npe);
         std::atomic<bool> bad{false};
         parallel_for(s.neq, [&](int64_t i) {
             const int64_t e = s.ip_cell[i];
@@ -471,6 +479,7 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
             for (int a = 0; a < npe; ++a) {
                 const int32_t nd = c->cells[e * npe + a];
                 for (int d = 0; d < dim; ++d) s.xe[(i * npe + a) * dim + d] = c->coords[(int64_t)nd * dim + d];
+                if (!s.rhoe.empty()) s.rhoe[i * npe + a] = s.node_rho[nd];
                 for (int64_t k = c->t_off[nd]; k < c->t_off[nd + 1]; ++k) {
                     const int32_t r = (int32_t)c->basis_rank[c->t_bases[k]];
                     const int32_t j = (int32_t)(std::lower_bound(b, b + n, r) - b);

@@ -48,6 +48,9 @@ struct SetData {
     std::vector<double> T;         // [neq][npe][maxnb] dense element extraction
     std::vector<uint16_t> sidx;    // [neq][maxnb][maxnb] column slot of base j in row of base i
     std::vector<double> xe;        // [neq][npe][dim] interpolation-cell coordinates
+    std::vector<double> node_rho;  // nodal density field (bulk, optional)
+    std::vector<double> rhoe;      // [neq][npe] densities of the element's nodes
+    DeviceBuf d_rho, d_nq;         // device copies: rhoe, N of the IP cell at the Gauss points
     // device copies
     DeviceBuf d_nb, d_bases, d_T, d_sidx, d_xe, d_E, d_ord;
     DeviceBuf d_dn, d_w;    // bulk: dN/dxi of the IP cell at the Gauss points, weights

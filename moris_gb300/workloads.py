@@ -8,6 +8,12 @@ same seeds and arrays feed the oracle in the tests.
   B-spline extraction, QUAD_2x2; clamped at x = 0 by the symmetric Nitsche
   Dirichlet IWG (alpha = 100, the reference's weak-clamp mechanism), traction
   (1e-3, 0) at x = 1 by the Neumann IWG, BAR_3 on the edges.
+* simp_3d -- SIMP-like density problem: n^3 HEX8 mesh of the unit cube with
+  linear B-splines, HEX_2x2x2, E(x) = rho(x)^3 with rho the nodal field
+  smooth_density(n, seed) interpolated at the Gauss points, nu = 0.3; clamped
+  at x = 0 (Nitsche, alpha = 100) and loaded by the traction (1e-3, 0, 0) at
+  x = 1 (QUAD_2x2 facets; the facet's E is E0 times the cube of the mean
+  density of its element's nodes).
 * elasticity_3d -- 3D linear elasticity on an n^3 HEX8 mesh of the unit cube,
   quadratic B-spline extraction, HEX_3x3x3, E per element log-uniform in
   [1e-3, 1] (splitmix64), nu = 0.3.
@@ -16,6 +22,7 @@ import numpy as np
 
 from . import (FemModel, IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, IWG_STRUC_LINEAR_NEUMANN, MODEL_3D,
                MODEL_PLANE_STRAIN, RULE_BAR_3, RULE_HEX_3x3x3, RULE_QUAD_2x2, SHAPE_RECTANGULAR, hmr_uniform_mesh)
+from . import RULE_HEX_2x2x2, RULE_QUAD_2x2 as _RULE_QUAD_2x2
 from .rng import uniform01
 
 BASE_SEED = 20261203
@@ -49,3 +56,43 @@ def elasticity_3d(n=64, seed=BASE_SEED + 2, finalize=True):
     if finalize:
         m.finalize()
     return m, mesh, E
+
+
+def smooth_density(n, seed, rho_min=1e-3, passes=3):
+    """Seeded smoothed noise on the (n+1)^3 grid nodes mapped to [rho_min, 1]:
+    uniform noise, `passes` sweeps of a 3x3x3 box filter (edge-replicated),
+    then an affine min-max map."""
+    m = n + 1
+    f = uniform01(seed, m ** 3).reshape(m, m, m)
+    for _ in range(passes):
+        g = np.pad(f, 1, mode="edge")
+        acc = np.zeros_like(f)
+        for dz in range(3):
+            for dy in range(3):
+                for dx in range(3):
+                    acc += g[dz:dz + m, dy:dy + m, dx:dx + m]
+        f = acc / 27.0
+    lo, hi = f.min(), f.max()
+    return (rho_min + (1.0 - rho_min) * (f - lo) / (hi - lo)).ravel()
+
+
+def simp_3d(n=128, seed=BASE_SEED + 5, finalize=True, beta=3.0):
+    mesh = hmr_uniform_mesh(3, (n, n, n), (1.0, 1.0, 1.0), 1)
+    nc = len(mesh["cells"])
+    rho = smooth_density(n, seed)
+    E0 = np.ones(nc)
+    m = FemModel(3, mesh, SHAPE_RECTANGULAR)
+    m.add_bulk_set(np.arange(nc, dtype=np.int32), E0, 0.3, RULE_HEX_2x2x2, MODEL_3D, node_density=rho,
+                   density_exponent=beta)
+    cells = np.arange(nc)
+    left = cells[cells % n == 0].astype(np.int32)
+    right = cells[cells % n == n - 1].astype(np.int32)
+    rho_el = rho[mesh["cells"]].mean(axis=1)
+    E_el = rho_el ** beta
+    m.add_side_set(IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, left, np.full(len(left), 3), E_el[left], 0.3,
+                   _RULE_QUAD_2x2, MODEL_3D, alpha=NITSCHE_ALPHA, value=(0.0, 0.0, 0.0))
+    m.add_side_set(IWG_STRUC_LINEAR_NEUMANN, right, np.full(len(right), 1), E_el[right], 0.3, _RULE_QUAD_2x2,
+                   MODEL_3D, value=(TRACTION, 0.0, 0.0))
+    if finalize:
+        m.finalize()
+    return m, mesh, rho

@@ -455,6 +455,8 @@ struct BulkSet {
     std::vector<real> ig_coords, ig_param;
     std::vector<real> E;
     real nu;
+    std::vector<real> node_rho;  // optional nodal density field
+    real beta = 3.0;
 };
 struct SideSet {
     int iwg, rule, model;
@@ -672,6 +674,13 @@ int orc_model_add_bulk_set(orc_model* m, int ig_cell, int rule, int model, int64
     s.E.assign(E, E + nc);
     s.nu = nu;
     m->bulk.push_back(std::move(s));
+    return 0;
+}
+
+int orc_model_set_density(orc_model* m, int set, const double* node_rho, double beta) {
+    if (set < 0 || set >= (int)m->bulk.size()) return 1;
+    m->bulk[set].node_rho.assign(node_rho, node_rho + m->num_nodes);
+    m->bulk[set].beta = beta;
     return 0;
 }
 
@@ -896,7 +905,16 @@ void bulk_pdof(const orc_model* m, const BulkSet& s, int64_t eq, const Mat& upd,
             Mat Nrow, dNdx;
             ip_eval(m, Xip, xip.a.data(), Nrow, dNdx);
             Mat B = test_strain(s.model, dNdx);
-            iwg_bulk(B, D, uvec, wstar, K, R);
+            if (!s.node_rho.empty()) {
+                // density-dependent Young's modulus E0 rho(x)^beta, rho from the
+                // density field interpolator (EXA/optimization/SIMP/SIMP.cpp:43-51)
+                real rho = 0.0;
+                for (int a = 0; a < npe; ++a) rho += Nrow(0, a) * s.node_rho[m->cells[(int64_t)cell * npe + a]];
+                Mat Dq = constitutive(s.model, d, s.E[eq] * std::pow(rho, s.beta), s.nu);
+                iwg_bulk(B, Dq, uvec, wstar, K, R);
+            } else {
+                iwg_bulk(B, D, uvec, wstar, K, R);
+            }
         }
     }
 }

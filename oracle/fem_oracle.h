@@ -73,6 +73,8 @@ int orc_model_add_bulk_set(orc_model* m, int ig_cell, int rule, int model_type, 
                            const int32_t* cluster_ip_cell, const int64_t* ig_offsets,
                            const double* ig_coords, const double* ig_param,
                            const double* youngs_modulus, double poisson);
+/* optional nodal density field of bulk set `set`: E(x) = E0 rho(x)^beta */
+int orc_model_set_density(orc_model* m, int set, const double* node_rho, double beta);
 /* side set on IP-cell facets (trivial side clusters).  value = traction
    (Neumann) or prescribed displacement (Dirichlet), dim doubles per set. */
 int orc_model_add_side_set(orc_model* m, int iwg, int rule, int model_type, int64_t num_sides,

@@ -39,6 +39,7 @@ def load():
             "orc_model_free": (None, [_P]),
             "orc_model_add_bulk_set": (_I, [_P, _I, _I, _I, _L, _P, _P, _P, _P, _P, _D]),
             "orc_model_add_side_set": (_I, [_P, _I, _I, _I, _L, _P, _P, _P, _D, _D, _P]),
+            "orc_model_set_density": (_I, [_P, _I, _P, _D]),
             "orc_model_finalize": (_I, [_P]),
             "orc_model_num_adofs": (_L, [_P]),
             "orc_model_nnz": (_L, [_P]),
@@ -136,6 +137,11 @@ class OracleModel:
         r = self.lib.orc_model_add_bulk_set(self.h, ig_cell, rule, model, len(ipc), _ptr(ipc), _ptr(off),
                                             _ptr(xc), _ptr(xp), _ptr(E), nu)
         assert r == 0
+
+    def set_density(self, s, node_rho, beta=3.0):
+        rho = np.ascontiguousarray(node_rho, dtype=np.float64)
+        self._keep.append(rho)
+        assert self.lib.orc_model_set_density(self.h, s, _ptr(rho), beta) == 0
 
     def add_side_set(self, iwg, rule, model, ip_cells, ordinals, E, nu, alpha, value):
         ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)

@@ -28,7 +28,7 @@ def distort(mesh, dim, ne, amount, seed):
     return m
 
 
-def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed=1, distortion=0.2):
+def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed=1, distortion=0.2, density=False):
     mesh = mg.hmr_uniform_mesh(dim, ne, [1.0] * dim, p)
     if shape == mg.SHAPE_GENERAL:
         mesh = distort(mesh, dim, ne, distortion, seed + 7)
@@ -41,8 +41,14 @@ def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed
     prod = mg.FemModel(dim, mesh, shape)
     orc = OracleModel(dim, ipc, shape, mesh)
     cells = np.arange(nc, dtype=np.int32)
-    prod.add_bulk_set(cells, E, 0.3, rule, model)
-    orc.add_bulk_set(ipc, rule, model, cells, E, 0.3)
+    if density:
+        rho = 1e-3 + (1 - 1e-3) * uniform01(seed + 99, len(mesh["coords"]))
+        prod.add_bulk_set(cells, E, 0.3, rule, model, node_density=rho, density_exponent=3.0)
+        orc.add_bulk_set(ipc, rule, model, cells, E, 0.3)
+        orc.set_density(0, rho, 3.0)
+    else:
+        prod.add_bulk_set(cells, E, 0.3, rule, model)
+        orc.add_bulk_set(ipc, rule, model, cells, E, 0.3)
     if sides:
         if dim == 2:
             left = np.arange(0, nc, ne[0], dtype=np.int32)

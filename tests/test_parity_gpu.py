@@ -125,6 +125,29 @@ def test_autotune_keeps_parity(torch):
     assert csr_row_rel_err(rp, vh, vo) <= RTOL and rel_err(rh, ro) <= RTOL
 
 
+@pytest.mark.parametrize("case", [(2, (5, 4), 1, mg.SHAPE_RECTANGULAR, mg.RULE_QUAD_2x2),
+                                  (3, (3, 3, 2), 1, mg.SHAPE_RECTANGULAR, mg.RULE_HEX_2x2x2),
+                                  (3, (3, 2, 3), 1, mg.SHAPE_GENERAL, mg.RULE_HEX_2x2x2),
+                                  (3, (2, 3, 2), 2, mg.SHAPE_RECTANGULAR, mg.RULE_HEX_3x3x3)])
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_density_field_material_matches_oracle(torch, case, variant):
+    dim, ne, p, shape, rule = case
+    prod, orc, _ = problem(dim, ne, p, shape, rule, sides=True, density=True)
+    prod.finalize()
+    orc.finalize()
+    prod.set_variant(0, variant)
+    u = uniform01(23, prod.num_adofs) - 0.5
+    K, R = prod.element_matrices(0, 0, orc.num_eq(0), u)
+    for eq in range(orc.num_eq(0)):
+        Ko, Ro = orc.element_matrices(0, eq, u)
+        n = len(Ro)
+        assert rel_err(K[eq, :n, :n], Ko) <= RTOL and rel_err(R[eq, :n], Ro) <= RTOL, eq
+    rp, _ = prod.graph()
+    vo, ro = orc.assemble(u)
+    vh, rh = prod.assemble_host(u)
+    assert csr_row_rel_err(rp, vh, vo) <= RTOL and rel_err(rh, ro) <= RTOL
+
+
 def test_residual_only_and_jacobian_only_flags(torch):
     prod, orc, _ = problem(2, (4, 4), 2, sides=True)
     prod.finalize()

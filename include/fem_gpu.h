@@ -238,6 +238,45 @@ fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_
 fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx,
                                    const double* vals, const double* b, double* x, const fem_gpu_pcg_opts* opts,
                                    fem_gpu_pcg_report* report, uint32_t flags);
+/* Jacobi-PCG that copies the iterate x into snaps (device, max_snaps x
+   num_adofs doubles) after every `every` iterations until convergence. */
+fem_gpu_status fem_gpu_pcg_snapshots(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx,
+                                     const double* vals, const double* b, double* x, const fem_gpu_pcg_opts* opts,
+                                     fem_gpu_pcg_report* report, int32_t every, double* snaps, int32_t max_snaps,
+                                     int32_t* n_snaps);
+
+/* ---- learned coarse-grid correction (config 5) ---------------------------
+   A 4-layer 3D convolution net (4 -> 32 -> 32 -> 32 -> 3 channels, 3x3x3,
+   no biases, ReLU) on a coarse node grid of n^3 voxels; BF16 weights and
+   activations, FP32 accumulation, tensor-core forward / data gradient, FP32
+   weight gradient, Adam.  Weights (host FP32): layers concatenated, each
+   [27][cout][cin], tap k = dx+1 + 3 (dy+1) + 9 (dz+1).  Inputs channels-last
+   FP32 [samples][n^3][4], outputs / targets [samples][n^3][3]. */
+typedef struct fem_cnn fem_cnn;
+int64_t fem_cnn_num_weights(void);
+fem_gpu_status fem_cnn_create(int32_t n, int32_t batch_max, uint64_t seed, fem_cnn** out);
+fem_gpu_status fem_cnn_destroy(fem_cnn* cnn);
+fem_gpu_status fem_cnn_set_weights(fem_cnn* cnn, const float* weights);
+fem_gpu_status fem_cnn_get_weights(const fem_cnn* cnn, float* weights);
+fem_gpu_status fem_cnn_forward(fem_cnn* cnn, const float* in4, int32_t samples, float* out3);
+/* mean-squared loss over the 3 output channels and its weight gradient */
+fem_gpu_status fem_cnn_loss_grad(fem_cnn* cnn, const float* in4, const float* target3, int32_t samples, double* loss,
+                                 float* grad);
+fem_gpu_status fem_cnn_train_step(fem_cnn* cnn, const float* in4, const float* target3, int32_t samples, float lr,
+                                  double* loss);
+/* coarse input for a fine residual (node grid nf^3, coarsening factor F):
+   channels 0..2 = R r / ||R r||, channel 3 = log10(restricted density) / 3 */
+fem_gpu_status fem_lpc_restrict(int32_t nf, int32_t factor, const double* r, const double* node_density, float* coarse4,
+                                double* scale);
+/* training target: fine field injected at the coarse nodes, / scale */
+fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e, double scale, float* target3);
+/* flexible CG with M(r) = D^-1 r + P f(R r / s) s (cnn == NULL: M = D^-1);
+   Jacobi-PCG is the fallback on breakdown or stagnation and the final
+   residual is recomputed from b - A x.  Device buffers. */
+fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                           const double* b, double* x, fem_cnn* cnn, int32_t factor, const double* node_density,
+                           const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report, int32_t* used_fallback);
+
 /* autotuner: times every kernel variant of each bulk set on (up to
    max_elements, <= 0 = all) of its elements, assembling into scratch
    buffers, and keeps the fastest per set.  Setup-time call; optional. */

@@ -71,6 +71,18 @@ SIGNATURES = {
     "fem_gpu_apply": (I32, [P, P, P, U32]),
     "fem_gpu_pcg": (I32, [P, P, P, P, P, P, P, P, U32]),
     "fem_gpu_pcg_noalloc": (I32, [P, P, P, P, P, P, P, P, U32]),
+    "fem_gpu_pcg_snapshots": (I32, [P, P, P, P, P, P, P, P, I32, P, I32, P]),
+    "fem_cnn_num_weights": (I64, []),
+    "fem_cnn_create": (I32, [I32, I32, C.c_uint64, P]),
+    "fem_cnn_destroy": (I32, [P]),
+    "fem_cnn_set_weights": (I32, [P, P]),
+    "fem_cnn_get_weights": (I32, [P, P]),
+    "fem_cnn_forward": (I32, [P, P, I32, P]),
+    "fem_cnn_loss_grad": (I32, [P, P, P, I32, P, P]),
+    "fem_cnn_train_step": (I32, [P, P, P, I32, C.c_float, P]),
+    "fem_lpc_restrict": (I32, [I32, I32, P, P, P, P]),
+    "fem_lpc_inject": (I32, [I32, I32, P, D, P]),
+    "fem_gpu_fcg": (I32, [P, P, P, P, P, P, P, I32, P, P, P, P]),
     "fem_gpu_autotune": (I32, [P, I64]),
     "fem_gpu_get_variant": (I32, [P, I32, P, P, P]),
     "fem_gpu_set_variant": (I32, [P, I32, I32]),

@@ -101,20 +101,23 @@ __global__ void k_init(int64_t n, const int32_t* rp, const int32_t* ci, const do
     block_add(bb, &st->bn2);
 }
 
+// q = A p (warp per row, grid-stride over rows so that each block adds its
+// share of p.q with one atomic) and p.q into the ring
 __global__ void k_spmv_pq(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* p,
                           double* q, CgState* st) {
     if (st->done) return;
     const int slot = st->it & 3;
     const int lane = threadIdx.x & 31;
-    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double pq = 0.0;
-    if (row < n) {
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
         double s = 0.0;
-        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) s = fma(v[k], p[ci[k]], s);
+        const int k1 = __ldg(rp + row + 1);
+        for (int k = __ldg(rp + row) + lane; k < k1; k += 32) s = fma(__ldg(v + k), __ldg(p + __ldg(ci + k)), s);
         s = warp_sum(s);
         if (lane == 0) {
             q[row] = s;
-            pq = s * p[row];
+            pq = fma(s, p[row], pq);
         }
     }
     block_add(pq, &st->ring[slot][0]);
@@ -217,6 +220,7 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     cudaMemsetAsync(st, 0, sizeof(CgState), sm);
     const int tpb = 256;
     const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, 152 * 16);
     const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
                                                                 opts->preconditioner == 1);
@@ -230,7 +234,7 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     e = cudaStreamBeginCapture(sm, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         for (int k = 0; k < chunk; ++k) {
-            k_spmv_pq<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, p, q, st);
+            k_spmv_pq<<<spmv_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, p, q, st);
             k_update_xr<<<vec_blocks, tpb, 0, sm>>>(n, x, r, z, p, q, dinv, st);
             k_update_p<<<vec_blocks, tpb, 0, sm>>>(n, p, z, st);
             k_advance<<<1, 1, 0, sm>>>(st, opts->max_iter);
@@ -379,5 +383,78 @@ extern "C" fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* c, const int32_t* row
     }
     if (hs.done == 2) return fail(c, FEM_GPU_NONFINITE, "pcg_noalloc breakdown");
     if (hs.done != 1) return fail(c, FEM_GPU_NOT_CONVERGED, "pcg_noalloc hit max_iter");
+    return FEM_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi-PCG that also records its iterates: x after every `every`
+// iterations is copied into snaps[j * n ...] (device, max_snaps slots).  The
+// residual/error pairs of the learned preconditioner's training set come from
+// these iterates of the solver itself.
+extern "C" fem_gpu_status fem_gpu_pcg_snapshots(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx,
+                                                const double* vals, const double* b, double* x,
+                                                const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep, int32_t every,
+                                                double* snaps, int32_t max_snaps, int32_t* n_snaps) {
+    if (!c || !rowptr || !colidx || !vals || !b || !x || !opts || every < 1 || !snaps || max_snaps < 1 || !n_snaps)
+        return FEM_GPU_BAD_ARG;
+    if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
+    if (!(opts->rel_tol > 0.0) || opts->max_iter < 1) return FEM_GPU_BAD_ARG;
+    const int64_t n = c->num_used * c->dim;
+    cudaStream_t sm = nullptr;
+    if (cudaStreamCreateWithFlags(&sm, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(c, FEM_GPU_CUDA_ERROR, "stream create");
+    cudaDeviceSynchronize();
+    const auto t0 = std::chrono::steady_clock::now();
+    double* r = nullptr;
+    CgState* st = nullptr;
+    cudaError_t e = cudaMallocAsync(&r, 5 * n * sizeof(double), sm);
+    if (e == cudaSuccess) e = cudaMallocAsync(&st, sizeof(CgState), sm);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(sm);
+        return fail(c, FEM_GPU_OUT_OF_MEMORY, "pcg workspace");
+    }
+    double *z = r + n, *p = z + n, *q = p + n, *dinv = q + n;
+    cudaMemsetAsync(st, 0, sizeof(CgState), sm);
+    const int tpb = 256;
+    const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, 152 * 16);
+    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv, opts->preconditioner == 1);
+    k_init<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, b, x, r, z, p, dinv, st);
+    k_set_thresh<<<1, 1, 0, sm>>>(st, opts->rel_tol);
+    CgState hs{};
+    int taken = 0;
+    for (int done_it = 0; done_it < opts->max_iter; done_it += every) {
+        for (int k = 0; k < every; ++k) {
+            k_spmv_pq<<<spmv_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, p, q, st);
+            k_update_xr<<<vec_blocks, tpb, 0, sm>>>(n, x, r, z, p, q, dinv, st);
+            k_update_p<<<vec_blocks, tpb, 0, sm>>>(n, p, z, st);
+            k_advance<<<1, 1, 0, sm>>>(st, opts->max_iter);
+        }
+        c->launches += 4 * every;
+        e = cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, sm);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+        if (e != cudaSuccess) break;
+        if (hs.done) break;
+        if (taken < max_snaps) {
+            e = cudaMemcpyAsync(snaps + (int64_t)taken * n, x, n * sizeof(double), cudaMemcpyDeviceToDevice, sm);
+            if (e != cudaSuccess) break;
+            ++taken;
+        }
+    }
+    cudaFreeAsync(r, sm);
+    cudaFreeAsync(st, sm);
+    cudaStreamSynchronize(sm);
+    cudaStreamDestroy(sm);
+    *n_snaps = taken;
+    if (rep) {
+        rep->iterations = hs.done == 1 ? hs.converged_at : hs.it;
+        rep->converged = hs.done == 1;
+        rep->rel_residual = std::sqrt(hs.ring[hs.it & 3][2] / (hs.bn2 > 0 ? hs.bn2 : 1.0));
+        rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (e != cudaSuccess) return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg snapshots: ") + cudaGetErrorString(e));
+    if (hs.done == 2) return fail(c, FEM_GPU_NONFINITE, "pcg breakdown");
+    if (hs.done != 1) return fail(c, FEM_GPU_NOT_CONVERGED, "pcg hit max_iter");
     return FEM_GPU_OK;
 }

@@ -1,0 +1,222 @@
+"""Learned coarse-grid correction for PCG on uniform linear-B-spline hex
+meshes (config 5): data generation from the solver's own iterates, GPU
+training, weight files, and the flexible CG that uses the net.
+
+Everything here drives libfem_gpu entry points (fem_cnn_*, fem_lpc_*,
+fem_gpu_pcg_snapshots, fem_gpu_fcg); tensors are torch CUDA tensors used as
+device buffers.
+"""
+import ctypes as C
+import os
+import struct
+import time
+
+import numpy as np
+
+from . import FemGpuError, PcgOpts, PcgReport, _dev_ptr, lib
+
+WEIGHT_MAGIC = b"MGBLPC01"
+DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def _check(st, what):
+    if st:
+        raise FemGpuError(st, what)
+
+
+class Cnn:
+    """fem_cnn: 4-layer 3D conv net on an n^3 coarse grid."""
+
+    def __init__(self, n, batch_max=1, seed=1):
+        self.L = lib()
+        self.n = n
+        self.V = n ** 3
+        h = C.c_void_p()
+        _check(self.L.fem_cnn_create(n, batch_max, seed, C.byref(h)), "fem_cnn_create")
+        self.h = h
+        self.num_weights = self.L.fem_cnn_num_weights()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.fem_cnn_destroy(self.h)
+            self.h = None
+
+    def weights(self):
+        w = np.zeros(self.num_weights, dtype=np.float32)
+        _check(self.L.fem_cnn_get_weights(self.h, w.ctypes.data_as(C.c_void_p)), "get_weights")
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == self.num_weights
+        _check(self.L.fem_cnn_set_weights(self.h, w.ctypes.data_as(C.c_void_p)), "set_weights")
+
+    def forward(self, x4, nb):
+        import torch
+        y = torch.empty(nb * self.V * 3, dtype=torch.float32, device="cuda")
+        _check(self.L.fem_cnn_forward(self.h, _dev_ptr(x4), nb, _dev_ptr(y)), "cnn_forward")
+        return y
+
+    def loss_grad(self, x4, t3, nb):
+        loss = C.c_double()
+        g = np.zeros(self.num_weights, dtype=np.float32)
+        _check(self.L.fem_cnn_loss_grad(self.h, _dev_ptr(x4), _dev_ptr(t3), nb, C.byref(loss),
+                                        g.ctypes.data_as(C.c_void_p)), "cnn_loss_grad")
+        return loss.value, g
+
+    def train_step(self, x4, t3, nb, lr):
+        loss = C.c_double()
+        _check(self.L.fem_cnn_train_step(self.h, _dev_ptr(x4), _dev_ptr(t3), nb, C.c_float(lr), C.byref(loss)),
+               "cnn_train_step")
+        return loss.value
+
+
+def save_weights(path, w, n, factor, meta=""):
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    m = meta.encode()
+    with open(path, "wb") as f:
+        f.write(WEIGHT_MAGIC)
+        f.write(struct.pack("<iiqi", n, factor, w.size, len(m)))
+        f.write(m)
+        f.write(w.tobytes())
+
+
+def load_weights(path):
+    with open(path, "rb") as f:
+        if f.read(8) != WEIGHT_MAGIC:
+            raise ValueError("not a learned-preconditioner weight file: %s" % path)
+        n, factor, size, lm = struct.unpack("<iiqi", f.read(20))
+        meta = f.read(lm).decode()
+        w = np.frombuffer(f.read(4 * size), dtype=np.float32).copy()
+    return w, n, factor, meta
+
+
+def grid_sizes(model):
+    """edge length of the cubic node grid of a 3D linear-B-spline model"""
+    nu = model.num_adofs // 3
+    nf = int(round(nu ** (1.0 / 3.0)))
+    assert nf ** 3 == nu, "needs a cubic node grid"
+    return nf
+
+
+def restrict(nf, factor, r, rho):
+    """coarse input [Vc][4] (FP32 device) and the scale ||R r||"""
+    import torch
+    nc = (nf - 1) // factor + 1
+    out = torch.zeros(nc ** 3 * 4, dtype=torch.float32, device="cuda")
+    s = C.c_double()
+    _check(lib().fem_lpc_restrict(nf, factor, _dev_ptr(r), _dev_ptr(rho), _dev_ptr(out), C.byref(s)), "lpc_restrict")
+    return out, s.value
+
+
+def inject(nf, factor, e, scale):
+    import torch
+    nc = (nf - 1) // factor + 1
+    out = torch.zeros(nc ** 3 * 3, dtype=torch.float32, device="cuda")
+    _check(lib().fem_lpc_inject(nf, factor, _dev_ptr(e), scale, _dev_ptr(out)), "lpc_inject")
+    return out
+
+
+def assembled_system(model):
+    """CSR (device) of a finalized model and b = -R(0)."""
+    import torch
+    rp = torch.empty(model.num_adofs + 1, dtype=torch.int32, device="cuda")
+    ci = torch.empty(model.nnz, dtype=torch.int32, device="cuda")
+    model.graph_device(rp, ci)
+    vals = torch.empty(model.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(model.num_adofs, dtype=torch.float64, device="cuda")
+    model.assemble(None, vals, rhs)
+    return rp, ci, vals, -rhs
+
+
+def pcg_snapshots(model, rp, ci, vals, b, every, max_snaps, rel_tol=1e-8, max_iter=200000):
+    import torch
+    x = torch.zeros_like(b)
+    snaps = torch.empty(max_snaps * model.num_adofs, dtype=torch.float64, device="cuda")
+    o = PcgOpts(rel_tol, max_iter, 1)
+    r = PcgReport()
+    ns = C.c_int32()
+    st = lib().fem_gpu_pcg_snapshots(model.h, _dev_ptr(rp), _dev_ptr(ci), _dev_ptr(vals), _dev_ptr(b), _dev_ptr(x),
+                                     C.byref(o), C.byref(r), every, _dev_ptr(snaps), max_snaps, C.byref(ns))
+    model._check(st, "pcg_snapshots")
+    return x, snaps.view(max_snaps, model.num_adofs)[:ns.value], r.iterations
+
+
+def training_pairs(model, rho_dev, factor, every, max_snaps):
+    """(coarse input, coarse target) pairs of one density field: residuals
+    r_k = b - A x_k and errors e_k = x* - x_k of the plain-PCG iterates x_k."""
+    import torch
+    rp, ci, vals, b = assembled_system(model)
+    x_star, snaps, iters = pcg_snapshots(model, rp, ci, vals, b, every, max_snaps)
+    nf = grid_sizes(model)
+    A = torch.sparse_csr_tensor(rp.long(), ci.long(), vals, size=(model.num_adofs,) * 2)
+    ins, tgts = [], []
+    for k in range(snaps.shape[0]):
+        xk = snaps[k].contiguous()
+        rk = (b - torch.mv(A, xk)).contiguous()
+        ek = (x_star - xk).contiguous()
+        cin, s = restrict(nf, factor, rk, rho_dev)
+        if not s > 0:
+            continue
+        ins.append(cin)
+        tgts.append(inject(nf, factor, ek, s))
+    return ins, tgts, iters
+
+
+def train(cnn, inputs, targets, epochs, batch, lr, seed=0, log=None):
+    """Adam on shuffled mini-batches; returns the per-epoch mean losses."""
+    import torch
+    n = len(inputs)
+    X = torch.stack(inputs)
+    Y = torch.stack(targets)
+    rng = np.random.default_rng(seed)
+    hist = []
+    for ep in range(epochs):
+        perm = rng.permutation(n)
+        tot, cnt = 0.0, 0
+        for i in range(0, n - batch + 1, batch):
+            idx = torch.as_tensor(perm[i:i + batch], device="cuda")
+            xb = X[idx].reshape(-1).contiguous()
+            yb = Y[idx].reshape(-1).contiguous()
+            tot += cnn.train_step(xb, yb, batch, lr)
+            cnt += 1
+        hist.append(tot / max(cnt, 1))
+        if log:
+            log("epoch %d loss %.4e" % (ep, hist[-1]))
+    return hist
+
+
+def fcg(model, rp, ci, vals, b, x, cnn=None, factor=4, rho_dev=None, rel_tol=1e-8, max_iter=200000):
+    o = PcgOpts(rel_tol, max_iter, 1)
+    r = PcgReport()
+    fb = C.c_int32()
+    st = lib().fem_gpu_fcg(model.h, _dev_ptr(rp), _dev_ptr(ci), _dev_ptr(vals), _dev_ptr(b), _dev_ptr(x),
+                           cnn.h if cnn is not None else None, factor, _dev_ptr(rho_dev), C.byref(o), C.byref(r),
+                           C.byref(fb))
+    model._check(st, "fcg")
+    return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual, seconds=r.seconds,
+                fallback=bool(fb.value))
+
+
+def train_simp(n=128, factor=4, fields=10, per_field=200, every=None, epochs=30, batch=16, lr=2e-3, seed=1,
+               log=print):
+    """Train the correction on plain-PCG iterates of `fields` seeded density
+    fields (seeds other than the benchmark's) of the n^3 SIMP problem."""
+    import torch
+    from . import workloads
+    nc = n // factor + 1
+    cnn = Cnn(nc, batch_max=batch, seed=seed)
+    ins, tgts = [], []
+    t0 = time.time()
+    for f in range(fields):
+        m, mesh, rho = workloads.simp_3d(n, seed=workloads.BASE_SEED + 1000 + f)
+        rho_dev = torch.tensor(rho, device="cuda")
+        ev = every or max(1, 3000 // per_field)
+        a, b_, iters = training_pairs(m, rho_dev, factor, ev, per_field)
+        ins += a
+        tgts += b_
+        log("field %d: %d pcg iterations, %d pairs (%.1f s)" % (f, iters, len(a), time.time() - t0))
+        del m
+        torch.cuda.empty_cache()
+    hist = train(cnn, ins, tgts, epochs, batch, lr, seed=seed, log=log)
+    return cnn, hist, len(ins)

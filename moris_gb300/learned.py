@@ -57,6 +57,14 @@ class Cnn:
         _check(self.L.fem_cnn_forward(self.h, _dev_ptr(x4), nb, _dev_ptr(y)), "cnn_forward")
         return y
 
+    @property
+    def output_scale(self):
+        return self.L.fem_cnn_get_output_scale(self.h)
+
+    @output_scale.setter
+    def output_scale(self, v):
+        _check(self.L.fem_cnn_set_output_scale(self.h, float(v)), "set_output_scale")
+
     def loss_grad(self, x4, t3, nb):
         loss = C.c_double()
         g = np.zeros(self.num_weights, dtype=np.float32)
@@ -71,12 +79,13 @@ class Cnn:
         return loss.value
 
 
-def save_weights(path, w, n, factor, meta=""):
+def save_weights(path, w, n, factor, scale, meta=""):
+    """flat weight file: magic, n, factor, count, output scale, metadata, FP32 weights"""
     w = np.ascontiguousarray(w, dtype=np.float32)
     m = meta.encode()
     with open(path, "wb") as f:
         f.write(WEIGHT_MAGIC)
-        f.write(struct.pack("<iiqi", n, factor, w.size, len(m)))
+        f.write(struct.pack("<iiqdi", n, factor, w.size, float(scale), len(m)))
         f.write(m)
         f.write(w.tobytes())
 
@@ -85,10 +94,18 @@ def load_weights(path):
     with open(path, "rb") as f:
         if f.read(8) != WEIGHT_MAGIC:
             raise ValueError("not a learned-preconditioner weight file: %s" % path)
-        n, factor, size, lm = struct.unpack("<iiqi", f.read(20))
+        n, factor, size, scale, lm = struct.unpack("<iiqdi", f.read(28))
         meta = f.read(lm).decode()
         w = np.frombuffer(f.read(4 * size), dtype=np.float32).copy()
-    return w, n, factor, meta
+    return w, n, factor, scale, meta
+
+
+def load_cnn(path):
+    w, n, factor, scale, meta = load_weights(path)
+    cnn = Cnn(n)
+    cnn.set_weights(w)
+    cnn.output_scale = scale
+    return cnn, factor, meta
 
 
 def grid_sizes(model):
@@ -218,5 +235,10 @@ def train_simp(n=128, factor=4, fields=10, per_field=200, every=None, epochs=30,
         log("field %d: %d pcg iterations, %d pairs (%.1f s)" % (f, iters, len(a), time.time() - t0))
         del m
         torch.cuda.empty_cache()
+    # output scale: RMS size of the targets, so that the net learns O(1) values
+    sq = sum(float((t.double() ** 2).mean()) for t in tgts) / max(1, len(tgts))
+    sigma = float(np.sqrt(sq)) if sq > 0 else 1.0
+    tgts = [(t / sigma).contiguous() for t in tgts]
+    cnn.output_scale = sigma
     hist = train(cnn, ins, tgts, epochs, batch, lr, seed=seed, log=log)
     return cnn, hist, len(ins)

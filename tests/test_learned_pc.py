@@ -58,15 +58,37 @@ def test_gpu_network_matches_oracle(torch):
     y = cnn.forward(xd, nb).cpu().numpy().reshape(nb, n, n, n, 3)
     loss, g = cnn.loss_grad(xd, td, nb)
     loss_o, g_o, y_o = co.loss_grad(w, x, t, quantized=True)
-    # forward: bf16 operands, fp32 accumulation in a different order
-    assert np.abs(y - y_o).max() <= 2e-3 * np.abs(y_o).max()
-    assert abs(loss - loss_o) <= 1e-3 * loss_o
+    # forward: bf16 operands and activations, fp32 accumulation in another
+    # order; a hidden activation can round to the neighbouring bf16 value
+    # (relative 2^-8), so the bound is a bf16 ulp on the largest output and
+    # almost every entry agrees far more closely
+    err = np.abs(y - y_o)
+    assert err.max() <= 2e-2 * np.abs(y_o).max()
+    assert np.linalg.norm(y - y_o) <= 5e-3 * np.linalg.norm(y_o)
+    assert abs(loss - loss_o) <= 5e-3 * loss_o
     off = 0
     for cin, cout in co.LAYERS:
         m = 27 * cin * cout
         ga, gb = g[off:off + m], g_o[off:off + m]
         assert np.linalg.norm(ga - gb) <= 2e-2 * np.linalg.norm(gb), (cin, cout)
         off += m
+
+
+@pytest.mark.gpu
+def test_gpu_forward_is_exact_on_exactly_representable_data(torch):
+    """Weights in {-1, 0, 1}/8 and inputs in (1/16) Z keep every product and
+    partial sum exact in fp32, so the tensor-core forward must equal the
+    oracle; this pins the fragment layouts and the tap / channel order."""
+    from moris_gb300.learned import Cnn
+    nb, n = 2, 5
+    rng = np.random.default_rng(11)
+    x = (rng.integers(-8, 9, size=(nb, n, n, n, 4)) / 16.0).astype(np.float32)
+    w = (rng.integers(-1, 2, size=_weights(0).size) / 8.0).astype(np.float32)
+    cnn = Cnn(n, batch_max=nb)
+    cnn.set_weights(w)
+    y = cnn.forward(torch.tensor(x.ravel(), device="cuda"), nb).cpu().numpy().reshape(nb, n, n, n, 3)
+    y_o, _, _ = co.forward(w, x, quantized=True)
+    assert np.array_equal(y, y_o.astype(np.float32))
 
 
 @pytest.mark.gpu

@@ -274,9 +274,10 @@ fem_gpu_status fem_lpc_restrict(int32_t nf, int32_t factor, const double* r, con
                                 double* scale);
 /* training target: fine field injected at the coarse nodes, / scale */
 fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e, double scale, float* target3);
-/* flexible CG with M(r) = D^-1 r + P f(R r / s) s (cnn == NULL: M = D^-1);
-   Jacobi-PCG is the fallback on breakdown or stagnation and the final
-   residual is recomputed from b - A x.  Device buffers. */
+/* truncated flexible CG, FCG(8), with M(r) = D^-1 r + P sigma f(R r / s) s
+   (cnn == NULL: M = D^-1); Jacobi-PCG is the fallback on breakdown or
+   stagnation and the final residual is recomputed from b - A x.  Device
+   buffers. */
 fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                            const double* b, double* x, fem_cnn* cnn, int32_t factor, const double* node_density,
                            const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report, int32_t* used_fallback);

@@ -587,20 +587,6 @@ __global__ void fcg_spmv_dot(int64_t n, const int32_t* rp, const int32_t* ci, co
     block_sum_add(acc, dot);
 }
 
-// x += a p; r_old = r; r -= a q; dots[0] += r.r
-__global__ void fcg_update_xr(int64_t n, double a, double* x, const double* p, double* r, double* r_old,
-                              const double* q, double* dots) {
-    double rr = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        x[i] = fma(a, p[i], x[i]);
-        const double ro = r[i];
-        r_old[i] = ro;
-        const double rn = fma(-a, q[i], ro);
-        r[i] = rn;
-        rr = fma(rn, rn, rr);
-    }
-    block_sum_add(rr, dots);
-}
 
 // z = dinv r (the Jacobi part of the preconditioner)
 __global__ void fcg_jacobi(int64_t n, const double* dinv, const double* r, double* z) {
@@ -608,21 +594,7 @@ __global__ void fcg_jacobi(int64_t n, const double* dinv, const double* r, doubl
         z[i] = dinv[i] * r[i];
 }
 
-// dots[0] += z.(r - r_old), dots[1] += z.r
-__global__ void fcg_dots(int64_t n, const double* z, const double* r, const double* r_old, double* dots) {
-    double a = 0.0, b = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        a = fma(z[i], r[i] - r_old[i], a);
-        b = fma(z[i], r[i], b);
-    }
-    block_sum_add(a, dots);
-    block_sum_add(b, dots + 1);
-}
 
-__global__ void fcg_update_p(int64_t n, double beta, const double* z, double* p) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        p[i] = fma(beta, p[i], z[i]);
-}
 
 __global__ void fcg_diag_inv(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, double* dinv) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -659,6 +631,50 @@ __global__ void fcg_residual(int64_t n, const int32_t* rp, const int32_t* ci, co
     }
     block_sum_add(rr, dots);
     block_sum_add(bb, dots + 1);
+}
+
+constexpr int kMaxM = 16;
+struct VecSet {
+    const double* v[kMaxM];
+};
+
+// dots[j] += z . q_j for j < m
+__global__ void fcg_multi_dot(int64_t n, const double* z, VecSet q, int m, double* dots) {
+    double acc[kMaxM];
+    for (int j = 0; j < kMaxM; ++j) acc[j] = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double zi = z[i];
+        for (int j = 0; j < m; ++j) acc[j] = fma(zi, q.v[j][i], acc[j]);
+    }
+    for (int j = 0; j < m; ++j) block_sum_add(acc[j], dots + j);
+}
+
+// p = z - sum_j c_j p_j ; dots[0] += p . r (alpha numerator)
+struct Coef {
+    double c[kMaxM];
+};
+__global__ void fcg_orthogonalize(int64_t n, const double* z, VecSet pj, Coef c, int m, const double* r, double* p,
+                                  double* dots) {
+    double pr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double v = z[i];
+        for (int j = 0; j < m; ++j) v = fma(-c.c[j], pj.v[j][i], v);
+        p[i] = v;
+        pr = fma(v, r[i], pr);
+    }
+    block_sum_add(pr, dots);
+}
+
+// x += a p; r -= a q; dots[0] += r.r
+__global__ void fcg_step(int64_t n, double a, double* x, const double* p, double* r, const double* q, double* dots) {
+    double rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = fma(a, p[i], x[i]);
+        const double rn = fma(-a, q[i], r[i]);
+        r[i] = rn;
+        rr = fma(rn, rn, rr);
+    }
+    block_sum_add(rr, dots);
 }
 
 }  // namespace
@@ -710,12 +726,15 @@ fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e_dev, d
                : FEM_GPU_CUDA_ERROR;
 }
 
-/* Flexible CG with M(r) = D^-1 r + P f(R r / s) s (Notay's flexible CG:
-   beta = z_{k+1}.(r_{k+1} - r_k) / z_k.r_k).  Plain Jacobi-PCG is the
-   fallback: on breakdown (non-positive p.Ap, NaN) or stagnation (no 10 %
-   residual reduction within 200 iterations) the solve continues with
-   fem_gpu_pcg from the current iterate, and the final relative residual is
-   recomputed from b - A x.  cnn == NULL runs the same loop with M = D^-1. */
+/* Truncated flexible CG, FCG(m) (Y. Notay, SIAM J. Sci. Comput. 22 (2000)),
+   with M(r) = D^-1 r + P sigma f(R r / s) s: each preconditioned residual is
+   A-orthogonalised against the last m search directions, so the energy norm
+   of the error decreases monotonically for any correction f (for a fixed
+   SPD M the method is PCG).  Plain Jacobi-PCG is the fallback: on breakdown
+   (non-positive p.Ap, NaN) or stagnation (no 10 % residual reduction within
+   200 iterations) the solve continues with fem_gpu_pcg from the current
+   iterate; the final relative residual is recomputed from b - A x.
+   cnn == NULL runs the same loop with M = D^-1. */
 fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                            const double* b, double* x, fem_cnn* cnn, int32_t factor, const double* node_density,
                            const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep, int32_t* used_fallback) {
@@ -723,14 +742,15 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
     if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
     const int64_t n = c->num_used * c->dim;
     const int64_t nu = c->num_used;
-    int nf = (int)std::llround(std::cbrt((double)nu));
+    const int nf = (int)std::llround(std::cbrt((double)nu));
     if (cnn) {
         if (c->dim != 3 || (int64_t)nf * nf * nf != nu || factor < 1 || (nf - 1) % factor ||
             (nf - 1) / factor + 1 != cnn->n)
             return fail(c, FEM_GPU_BAD_ARG, "fcg: learned correction needs a cubic node grid matching the net");
     }
+    const int M = 8;  // truncation depth
     const auto t0 = std::chrono::steady_clock::now();
-    double *r, *r_old, *z, *p, *q, *dinv, *dots;
+    double *r, *z, *dinv, *dots, *P, *Q;
     float *cin = nullptr, *cout = nullptr;
     std::vector<void*> bufs;
     auto alloc = [&](void** ptr, size_t bytes) {
@@ -739,12 +759,11 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
         return e;
     };
     cudaError_t e = alloc((void**)&r, n * 8);
-    if (e == cudaSuccess) e = alloc((void**)&r_old, n * 8);
     if (e == cudaSuccess) e = alloc((void**)&z, n * 8);
-    if (e == cudaSuccess) e = alloc((void**)&p, n * 8);
-    if (e == cudaSuccess) e = alloc((void**)&q, n * 8);
     if (e == cudaSuccess) e = alloc((void**)&dinv, n * 8);
-    if (e == cudaSuccess) e = alloc((void**)&dots, 4 * 8);
+    if (e == cudaSuccess) e = alloc((void**)&dots, kMaxM * 8);
+    if (e == cudaSuccess) e = alloc((void**)&P, (size_t)(M + 1) * n * 8);
+    if (e == cudaSuccess) e = alloc((void**)&Q, (size_t)(M + 1) * n * 8);
     if (cnn && e == cudaSuccess) {
         e = alloc((void**)&cin, cnn->V * 4 * sizeof(float));
         if (e == cudaSuccess) e = alloc((void**)&cout, cnn->V * 3 * sizeof(float));
@@ -760,13 +779,12 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
     const int tpb = 256;
     const unsigned rb = (unsigned)std::min<int64_t>((n * 32 + tpb - 1) / tpb, 152 * 16);
     const unsigned vb = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
-    double hd[2];
-    auto read2 = [&]() {
-        cudaMemcpy(hd, dots, 2 * sizeof(double), cudaMemcpyDeviceToHost);
-        cudaMemset(dots, 0, 4 * 8);
+    double hd[kMaxM];
+    auto readn = [&](int k) {
+        cudaMemcpy(hd, dots, k * sizeof(double), cudaMemcpyDeviceToHost);
+        cudaMemset(dots, 0, kMaxM * 8);
     };
     const int nc = cnn ? cnn->n : 0;
-    // preconditioner application z = M(r)
     auto apply_m = [&]() -> bool {
         fcg_jacobi<<<vb, tpb>>>(n, dinv, r, z);
         if (!cnn) return true;
@@ -778,36 +796,58 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
         }
         return cudaGetLastError() == cudaSuccess;
     };
-    cudaMemset(dots, 0, 4 * 8);
+    cudaMemset(dots, 0, kMaxM * 8);
     fcg_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb>>>(n, rowptr, colidx, vals, dinv);
     fcg_residual<<<rb, tpb>>>(n, rowptr, colidx, vals, b, x, r, dots);
-    read2();
+    readn(2);
     const double bn = std::sqrt(hd[1] > 0 ? hd[1] : 1.0);
     double rn = std::sqrt(hd[0]);
     const double tol = opts->rel_tol * bn;
-    int it = 0, fallback = 0;
-    bool ok = apply_m();
-    cudaMemcpy(p, z, n * 8, cudaMemcpyDeviceToDevice);
-    cudaMemset(r_old, 0, n * 8);
-    fcg_dots<<<vb, tpb>>>(n, z, r, r_old, dots);
-    read2();
-    double rz = hd[1];
+    std::vector<double> pq(M + 1, 1.0);
+    int it = 0, fallback = 0, stored = 0;
+    bool ok = true;
     double best = rn;
     int since_best = 0;
-    while (ok && rn > tol && it < opts->max_iter) {
+    while (rn > tol && it < opts->max_iter) {
+        ok = apply_m();
+        if (!ok) break;
+        // A-orthogonalise z against the last min(stored, M) directions
+        const int m = std::min(stored, M);
+        VecSet qs{}, ps{};
+        Coef cf{};
+        for (int j = 0; j < m; ++j) {
+            const int slot = (it - 1 - j + (M + 1) * 4) % (M + 1);
+            qs.v[j] = Q + (int64_t)slot * n;
+            ps.v[j] = P + (int64_t)slot * n;
+        }
+        if (m > 0) {
+            fcg_multi_dot<<<vb, tpb>>>(n, z, qs, m, dots);
+            readn(m);
+            for (int j = 0; j < m; ++j) {
+                const int slot = (it - 1 - j + (M + 1) * 4) % (M + 1);
+                cf.c[j] = hd[j] / pq[slot];
+            }
+        }
+        const int cur = it % (M + 1);
+        double* p = P + (int64_t)cur * n;
+        double* q = Q + (int64_t)cur * n;
+        fcg_orthogonalize<<<vb, tpb>>>(n, z, ps, cf, m, r, p, dots);
+        readn(1);
+        const double pr = hd[0];
         fcg_spmv_dot<<<rb, tpb>>>(n, rowptr, colidx, vals, p, q, dots);
-        read2();
-        const double pq = hd[0];
-        if (!(pq > 0.0) || !std::isfinite(rz)) {
+        readn(1);
+        const double pAp = hd[0];
+        if (!(pAp > 0.0) || !std::isfinite(pr)) {
             fallback = 1;
             break;
         }
-        const double alpha = rz / pq;
-        fcg_update_xr<<<vb, tpb>>>(n, alpha, x, p, r, r_old, q, dots);
-        read2();
+        pq[cur] = pAp;
+        const double alpha = pr / pAp;
+        fcg_step<<<vb, tpb>>>(n, alpha, x, p, r, q, dots);
+        readn(1);
         rn = std::sqrt(hd[0]);
         ++it;
-        if (rn <= tol) break;
+        ++stored;
         if (rn < 0.9 * best) {
             best = rn;
             since_best = 0;
@@ -815,16 +855,6 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
             fallback = 1;
             break;
         }
-        ok = apply_m();
-        fcg_dots<<<vb, tpb>>>(n, z, r, r_old, dots);
-        read2();
-        const double beta = hd[0] / rz;
-        rz = hd[1];
-        if (!std::isfinite(beta)) {
-            fallback = 1;
-            break;
-        }
-        fcg_update_p<<<vb, tpb>>>(n, beta, z, p);
     }
     if (!ok) {
         cleanup();
@@ -837,16 +867,14 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
         o.preconditioner = 1;
         o.max_iter = std::max(1, opts->max_iter - it);
         fem_gpu_pcg_report pr{};
-        cudaStream_t saved = (cudaStream_t)c->stream;
         cudaDeviceSynchronize();
         st = fem_gpu_pcg(c, rowptr, colidx, vals, b, x, &o, &pr, 0);
-        (void)saved;
         fb_iters = pr.iterations;
     }
     // judge: true residual of the final iterate
-    cudaMemset(dots, 0, 4 * 8);
+    cudaMemset(dots, 0, kMaxM * 8);
     fcg_residual<<<rb, tpb>>>(n, rowptr, colidx, vals, b, x, r, dots);
-    read2();
+    readn(2);
     const double true_rel = std::sqrt(hd[0]) / bn;
     cleanup();
     if (rep) {

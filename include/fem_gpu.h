@@ -92,6 +92,8 @@ enum {
     FEM_GPU_HOST_BUFFERS = 1u,      /* pointers are host memory                 */
     FEM_GPU_NO_JACOBIAN = 2u,       /* fem_gpu_assemble: residual only          */
     FEM_GPU_NO_RESIDUAL = 4u,       /* fem_gpu_assemble: Jacobian only          */
+    FEM_GPU_ASYNC = 16u,            /* batched assembly: return without waiting
+                                       for the device status (fem_gpu_check_status) */
     FEM_GPU_ACCUMULATE = 8u         /* do not zero csr_vals / rhs first         */
 };
 
@@ -159,6 +161,39 @@ typedef struct fem_gpu_side_set_desc {
     double value[3];
 } fem_gpu_side_set_desc;
 
+/* Double-sided set: the Nitsche interface (IWG_Isotropic_Struc_Linear_
+   Interface, FEM/INT/src/IWG/cl_FEM_IWG_Isotropic_Struc_Linear_Interface.cpp:
+   51-386, with SP_Nitsche_Interface, SP/cl_FEM_SP_Nitsche_Interface.cpp:51-97)
+   or the face-oriented virtual-work ghost penalty (IWG_Isotropic_Struc_Linear_
+   Virtual_Work_Ghost, ..._Virtual_Work_Ghost.cpp:50-244, with
+   SP_Ghost_Virtual_Work, SP/cl_FEM_SP_Ghost_Virtual_Work.cpp:30-38) over the
+   facets of one leader / follower pair of IP cells (mtk::Double_Side_Cluster,
+   Element_Double_Sideset, FEM/INT/src/ELEM/cl_FEM_Element_Double_Sideset.cpp:
+   142-347).  Each equation object is one cluster: a list of facets given by
+   their vertex coordinates and the vertices' parametric coordinates in the
+   leader and in the follower IP cell (same vertex order).  The facet normal
+   of that vertex order (TRI3: (x0-x2) x (x1-x2); QUAD4: t1 x t2) points out of
+   the leader.  Interface volumes V_L / V_F of the Nitsche parameter are the
+   measures of the bulk clusters on the leader / follower IP cells; the ghost
+   element size is the side length measure of the cluster's facets. */
+typedef struct fem_gpu_double_side_set_desc {
+    int32_t iwg_type;             /* INTERFACE_SYMMETRIC / _UNSYMMETRIC_NITSCHE or VW_GHOST */
+    int32_t facet_cell_type;      /* FEM_GPU_CELL_TRI3 or FEM_GPU_CELL_QUAD4 (3D only) */
+    int32_t integration_rule;     /* TRI_3 / TRI_7 for triangles, QUAD_2x2 for quads */
+    int32_t model_type;           /* FEM_GPU_MODEL_3D */
+    int64_t num_clusters;
+    const int32_t* leader_ip_cell;
+    const int32_t* follower_ip_cell;
+    const int64_t* facet_offsets;          /* [num_clusters+1] */
+    const double* facet_coords;            /* [facets][vertices][3] */
+    const double* leader_param_coords;     /* [facets][vertices][3] */
+    const double* follower_param_coords;   /* [facets][vertices][3] */
+    const double* leader_youngs_modulus;   /* [num_clusters] */
+    const double* follower_youngs_modulus; /* [num_clusters] */
+    double poisson_ratio;
+    double alpha;                 /* Nitsche interface or ghost penalty parameter */
+} fem_gpu_double_side_set_desc;
+
 typedef struct fem_gpu_pcg_opts {
     double rel_tol;               /* on ||b - A x|| / ||b|| */
     int32_t max_iter;
@@ -188,6 +223,49 @@ fem_gpu_status fem_hmr_mesh_arrays(const fem_hmr_mesh* m, double* node_coords, i
                                    int64_t* t_offsets, int32_t* t_bases, double* t_weights);
 fem_gpu_status fem_hmr_mesh_free(fem_hmr_mesh* m);
 
+/* ---- XFEM decomposition of a uniform level-0 HEX8 mesh (host only) -------
+   Input of the cut-cell path, standing in for the reference's XTK
+   (XTK/src/cl_XTK_Model.cpp:690 decompose; 24-tet regular subdivision,
+   cl_XTK_Regular_Subdivision_Interface.hpp:225; conformal cut along the
+   linear level set; Heaviside enrichment, cl_XTK_Enrichment.cpp:1148-2362;
+   ghost facets, cl_XTK_Ghost_Stabilization.cpp:45).  node_phi: level set at
+   the (n0+1)(n1+1)(n2+1) background nodes (i fastest); phase 1 where
+   phi < 0.  The enriched IP mesh (unzipped vertices, enriched extraction
+   rows) feeds fem_gpu_mesh_desc; the clusters feed the bulk and
+   double-sided sets.  IG vertex kinds: 0 background node (parents[0] = node),
+   1 face centre (parents[0..3] = its corner nodes), 2 cell centre
+   (parents[0..7]), 3 intersection on the IG edge parents[0] -> parents[1]
+   (IG vertex ids, value = edge coordinate t); kinds 0-2 carry phi. */
+typedef struct fem_xtk_model fem_xtk_model;
+typedef struct fem_xtk_sizes {
+    int64_t num_nodes, num_cells, num_bases, t_nnz;
+    int64_t num_uncut[2], num_cut[2], num_ig_cells[2];
+    int64_t num_interface, num_interface_facets;
+    int64_t num_ghost[2];
+    int64_t num_ig_vertices;
+} fem_xtk_sizes;
+fem_gpu_status fem_xtk_decompose(const int32_t* num_elements, const double* lengths, int32_t bspline_order,
+                                 const double* node_phi, fem_xtk_model** out);
+fem_gpu_status fem_xtk_get_sizes(const fem_xtk_model* m, fem_xtk_sizes* sizes);
+/* any output pointer may be NULL; sizes as reported by fem_xtk_get_sizes */
+fem_gpu_status fem_xtk_get_ip_mesh(const fem_xtk_model* m, double* node_coords, int32_t* cell_nodes,
+                                   int64_t* t_offsets, int32_t* t_bases, double* t_weights,
+                                   int32_t* cell_background, int32_t* cell_phase);
+/* per phase: uncut enriched cells, cut enriched cells and their TET4
+   integration cells (coords / IP-parametric coords [ig][4][3], IG vertex ids) */
+fem_gpu_status fem_xtk_get_bulk(const fem_xtk_model* m, int32_t phase, int32_t* uncut_cells, int32_t* cut_cells,
+                                int64_t* ig_offsets, double* ig_coords, double* ig_param, int32_t* ig_vertices);
+/* interface clusters: leader = phase-0 cell, follower = phase-1 cell of one
+   background cell; TRI3 facets [f][3][3] (same parametric coords both sides) */
+fem_gpu_status fem_xtk_get_interface(const fem_xtk_model* m, int32_t* leader, int32_t* follower,
+                                     int64_t* offsets, double* coords, double* param, int32_t* vertices);
+/* ghost clusters of one phase: one QUAD4 face [4][3] each */
+fem_gpu_status fem_xtk_get_ghost(const fem_xtk_model* m, int32_t phase, int32_t* leader, int32_t* follower,
+                                 double* coords, double* leader_param, double* follower_param);
+fem_gpu_status fem_xtk_get_vertices(const fem_xtk_model* m, int32_t* kind, int32_t* parents, double* coords,
+                                    double* value);
+void fem_xtk_free(fem_xtk_model* m);
+
 /* ---- model ------------------------------------------------------------- */
 fem_gpu_status fem_gpu_create(const fem_gpu_mesh_desc* mesh, fem_gpu_ctx** out);
 fem_gpu_status fem_gpu_destroy(fem_gpu_ctx* ctx);
@@ -197,6 +275,11 @@ fem_gpu_status fem_gpu_destroy(fem_gpu_ctx* ctx);
 fem_gpu_status fem_gpu_set_stream(fem_gpu_ctx* ctx, void* stream);
 fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* ctx, const fem_gpu_bulk_set_desc* desc, int32_t* set_index);
 fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* ctx, const fem_gpu_side_set_desc* desc, int32_t* set_index);
+/* interface / ghost set; element adofs are the leader's per-type lists
+   followed by the follower's (Equation_Object::get_equation_obj_dof_ids over
+   its two pdof systems, FEM/MSI/src/cl_MSI_Equation_Object.cpp:506-554) */
+fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* ctx, const fem_gpu_double_side_set_desc* desc,
+                                           int32_t* set_index);
 /* host-side MSI work (adof numbering, element T, sparsity, scatter maps)
    plus the upload of everything the kernels read */
 fem_gpu_status fem_gpu_finalize(fem_gpu_ctx* ctx);
@@ -220,6 +303,23 @@ fem_gpu_status fem_gpu_element_matrices(fem_gpu_ctx* ctx, int32_t set, int64_t f
 /* fill_matrix_and_RHS: csr_vals (nnz) and rhs (num_adofs) = residual R(u) */
 fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* ctx, const double* u_adof, double* csr_vals, double* rhs,
                                 uint32_t flags);
+/* fill_matrix_and_RHS for every equation object of every bulk and
+   double-sided set in ONE persistent launch (uneven clusters: uncut cells,
+   cut clusters of 4 to hundreds of integration points, interface and ghost
+   clusters), work items taken from a device queue in decreasing cost order,
+   clusters above the split size cut into integration-point ranges.  The
+   zero-fill, the queue reset, the persistent kernel and the boundary side
+   sets are one CUDA graph, captured on the first call for a (u, vals, rhs)
+   triple and replayed afterwards.  Device buffers only. */
+fem_gpu_status fem_gpu_assemble_batched(fem_gpu_ctx* ctx, const double* u_adof, double* csr_vals, double* rhs,
+                                        uint32_t flags);
+/* waits for the context's stream and reports a non-finite element operator
+   flagged by the kernels since the last check */
+fem_gpu_status fem_gpu_check_status(fem_gpu_ctx* ctx);
+/* autotuner of the batched launch: times CTA width x split size on the
+   model's own clusters and keeps the fastest (setup-time, optional) */
+fem_gpu_status fem_gpu_autotune_batched(fem_gpu_ctx* ctx, int32_t* warps, int32_t* split_points, double* ms);
+fem_gpu_status fem_gpu_set_batched_config(fem_gpu_ctx* ctx, int32_t warps, int32_t split_points);
 /* matrix-free Jacobian-vector product y = K x (no CSR) */
 fem_gpu_status fem_gpu_apply(fem_gpu_ctx* ctx, const double* x, double* y, uint32_t flags);
 /* preconditioned CG on a CSR operator built by fem_gpu_assemble */

@@ -10,7 +10,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import BulkSetDesc, MeshDesc, PcgOpts, PcgReport, SideSetDesc
+from ._lib import BulkSetDesc, DoubleSideSetDesc, MeshDesc, PcgOpts, PcgReport, SideSetDesc
 
 # enums (identical values in include/fem_gpu.h)
 CELL_QUAD4, CELL_HEX8, CELL_TRI3, CELL_TET4, CELL_LINE2 = 0, 1, 2, 3, 4
@@ -25,7 +25,7 @@ IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE = 3
 IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE = 4
 IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE = 5
 IWG_STRUC_LINEAR_VW_GHOST = 6
-HOST_BUFFERS, NO_JACOBIAN, NO_RESIDUAL, ACCUMULATE = 1, 2, 4, 8
+HOST_BUFFERS, NO_JACOBIAN, NO_RESIDUAL, ACCUMULATE, ASYNC = 1, 2, 4, 8, 16
 
 
 class FemGpuError(RuntimeError):
@@ -163,6 +163,42 @@ class FemModel:
         self._check(self.L.fem_gpu_add_side_set(self.h, C.byref(d), C.byref(idx)), "add_side_set")
         self.num_sets += 1
         return idx.value
+
+    def add_double_side_set(self, iwg, leader, follower, facet_offsets, facet_coords, leader_param, follower_param,
+                            leader_youngs, follower_youngs, poisson, rule, facet_cell, alpha, model=MODEL_3D):
+        """Interface (Nitsche) or ghost clusters: facets given by vertex coords and
+        their parametric coords in the leader / follower IP cells."""
+        L_ = np.ascontiguousarray(leader, dtype=np.int32)
+        F_ = np.ascontiguousarray(follower, dtype=np.int32)
+        off = np.ascontiguousarray(facet_offsets, dtype=np.int64)
+        fx = np.ascontiguousarray(facet_coords, dtype=np.float64)
+        fl = np.ascontiguousarray(leader_param, dtype=np.float64)
+        ff = np.ascontiguousarray(follower_param, dtype=np.float64)
+        EL = np.ascontiguousarray(leader_youngs, dtype=np.float64)
+        EF = np.ascontiguousarray(follower_youngs, dtype=np.float64)
+        d = DoubleSideSetDesc(iwg, facet_cell, rule, model, len(L_), _np_ptr(L_), _np_ptr(F_), _np_ptr(off),
+                              _np_ptr(fx), _np_ptr(fl), _np_ptr(ff), _np_ptr(EL), _np_ptr(EF), poisson, alpha)
+        idx = C.c_int32()
+        self._check(self.L.fem_gpu_add_double_side_set(self.h, C.byref(d), C.byref(idx)), "add_double_side_set")
+        self.num_sets += 1
+        return idx.value
+
+    def assemble_batched(self, u, vals, rhs, flags=0):
+        """All bulk and double-sided clusters in one persistent graph-captured launch
+        (device tensors)."""
+        self._check(self.L.fem_gpu_assemble_batched(self.h, _dev_ptr(u), _dev_ptr(vals), _dev_ptr(rhs), flags),
+                    "assemble_batched")
+
+    def check_status(self):
+        self._check(self.L.fem_gpu_check_status(self.h), "check_status")
+
+    def autotune_batched(self):
+        w, sp, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._check(self.L.fem_gpu_autotune_batched(self.h, C.byref(w), C.byref(sp), C.byref(ms)), "autotune_batched")
+        return w.value, sp.value, ms.value
+
+    def set_batched_config(self, warps, split):
+        self._check(self.L.fem_gpu_set_batched_config(self.h, warps, split), "set_batched_config")
 
     def finalize(self, host_only=False):
         f = self.L.fem_gpu_finalize_host if host_only else self.L.fem_gpu_finalize

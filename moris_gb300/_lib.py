@@ -36,6 +36,20 @@ class SideSetDesc(C.Structure):
                 ("poisson_ratio", D), ("nitsche_alpha", D), ("value", D * 3)]
 
 
+class DoubleSideSetDesc(C.Structure):
+    _fields_ = [("iwg_type", I32), ("facet_cell_type", I32), ("integration_rule", I32), ("model_type", I32),
+                ("num_clusters", I64), ("leader_ip_cell", P), ("follower_ip_cell", P), ("facet_offsets", P),
+                ("facet_coords", P), ("leader_param_coords", P), ("follower_param_coords", P),
+                ("leader_youngs_modulus", P), ("follower_youngs_modulus", P), ("poisson_ratio", D), ("alpha", D)]
+
+
+class XtkSizes(C.Structure):
+    _fields_ = [("num_nodes", I64), ("num_cells", I64), ("num_bases", I64), ("t_nnz", I64),
+                ("num_uncut", I64 * 2), ("num_cut", I64 * 2), ("num_ig_cells", I64 * 2),
+                ("num_interface", I64), ("num_interface_facets", I64), ("num_ghost", I64 * 2),
+                ("num_ig_vertices", I64)]
+
+
 class PcgOpts(C.Structure):
     _fields_ = [("rel_tol", D), ("max_iter", I32), ("preconditioner", I32)]
 
@@ -59,6 +73,19 @@ SIGNATURES = {
     "fem_gpu_set_stream": (I32, [P, P]),
     "fem_gpu_add_bulk_set": (I32, [P, P, P]),
     "fem_gpu_add_side_set": (I32, [P, P, P]),
+    "fem_gpu_add_double_side_set": (I32, [P, P, P]),
+    "fem_gpu_assemble_batched": (I32, [P, P, P, P, U32]),
+    "fem_gpu_check_status": (I32, [P]),
+    "fem_gpu_autotune_batched": (I32, [P, P, P, P]),
+    "fem_gpu_set_batched_config": (I32, [P, I32, I32]),
+    "fem_xtk_decompose": (I32, [P, P, I32, P, P]),
+    "fem_xtk_get_sizes": (I32, [P, P]),
+    "fem_xtk_get_ip_mesh": (I32, [P, P, P, P, P, P, P, P]),
+    "fem_xtk_get_bulk": (I32, [P, I32, P, P, P, P, P, P]),
+    "fem_xtk_get_interface": (I32, [P, P, P, P, P, P, P]),
+    "fem_xtk_get_ghost": (I32, [P, I32, P, P, P, P, P]),
+    "fem_xtk_get_vertices": (I32, [P, P, P, P, P]),
+    "fem_xtk_free": (None, [P]),
     "fem_gpu_finalize": (I32, [P]),
     "fem_gpu_finalize_host": (I32, [P]),
     "fem_gpu_get_sizes": (I32, [P, P, P, P]),

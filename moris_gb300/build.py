@@ -18,8 +18,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfem_gpu.so")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
-HOST_SRCS = ["fem_tables.cpp", "fem_host.cpp"]
-CUDA_SRCS = ["fem_device.cu", "fem_solver.cu", "fem_probe.cu", "fem_learned_pc.cu"]
+HOST_SRCS = ["fem_tables.cpp", "fem_host.cpp", "fem_xtk.cpp"]
+CUDA_SRCS = ["fem_device.cu", "fem_solver.cu", "fem_probe.cu", "fem_learned_pc.cu", "fem_cluster.cu"]
 
 
 def _nvcc():

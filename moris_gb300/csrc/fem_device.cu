@@ -920,7 +920,17 @@ fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
 
 namespace fem {
 
+// a side set launched on a given stream (the batched graph captures it)
+fem_gpu_status side_launch_on(fem_gpu_ctx* c, int set, const double* u, double* vals, double* rhs, cudaStream_t st) {
+    void* keep = c->stream;
+    c->stream = st;
+    fem_gpu_status r = launch_side(c, set, MODE_ASSEMBLE, 0, c->sets[set].neq, u, vals, rhs, nullptr, nullptr, 0);
+    c->stream = keep;
+    return r;
+}
+
 void device_release(fem_gpu_ctx* c) {
+    cluster_release(c);
     for (auto& s : c->sets) {
         dfree(s.d_nb);
         dfree(s.d_bases);
@@ -962,6 +972,10 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
         SetData& s = c->sets[k];
         SetData& ds = s;
         const int NPE = c->npe, D = c->dim;
+        if (cluster_set(c, (int)k)) {
+            if ((st = cluster_finalize(c, (int)k)) != FEM_GPU_OK) return st;
+            continue;
+        }
         if (s.kind == 0) {
             const Rule r = gauss_rule(s.bulk.integration_rule);
             if (r.n > kMaxGP) return fail(c, FEM_GPU_UNSUPPORTED, "too many Gauss points");
@@ -978,6 +992,9 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
                 if ((e = upload(ds.d_rho, s.rhoe, sm)) != cudaSuccess) return cuda_fail(c, e, "densities");
             if ((e = upload(ds.d_dn, dn, sm)) != cudaSuccess) return cuda_fail(c, e, "dn table");
             if ((e = upload(ds.d_w, w, sm)) != cudaSuccess) return cuda_fail(c, e, "w table");
+            // rule points for the cluster kernel (batched launch)
+            if ((e = upload(ds.d_gp, r.pts, sm)) != cudaSuccess) return cuda_fail(c, e, "rule points");
+            if ((e = upload(ds.d_gw, r.w, sm)) != cudaSuccess) return cuda_fail(c, e, "rule weights");
             const int npd = D * NPE;
             std::vector<uint32_t> pairs;
             for (int rr = 0; rr < npd; ++rr)
@@ -1034,6 +1051,7 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
     for (size_t k = 0; k < c->sets.size(); ++k) {
         SetData& s = c->sets[k];
         const int W = s.nbsel;
+        if (cluster_set(c, (int)k)) continue;
         if (s.kind == 0 && W != s.maxnb) {
             std::vector<int32_t> b((size_t)s.neq * W, -1);
             for (int64_t i = 0; i < s.neq; ++i)
@@ -1123,7 +1141,7 @@ fem_gpu_status fem_gpu_element_matrices(fem_gpu_ctx* c, int32_t set, int64_t fir
     SetData& s = c->sets[set];
     if (first < 0 || first + count > s.neq) return FEM_GPU_OOB_INDEX;
     if (count == 0) return FEM_GPU_OK;
-    const int nmax = s.maxnb * c->dim;
+    const int nmax = s.maxnb * c->dim * (s.kind == 2 ? 2 : 1);
     const bool host = flags & FEM_GPU_HOST_BUFFERS;
     const int64_t nad = c->num_used * c->dim;
     Staged su, sk, sr;
@@ -1135,7 +1153,10 @@ fem_gpu_status fem_gpu_element_matrices(fem_gpu_ctx* c, int32_t set, int64_t fir
     if (sk.dev) cudaMemsetAsync(sk.dev, 0, (size_t)count * nmax * nmax * sizeof(double), sm);
     if (sr.dev) cudaMemsetAsync(sr.dev, 0, (size_t)count * nmax * sizeof(double), sm);
     cudaMemsetAsync(c->d_status.p, 0, sizeof(int), sm);
-    if (s.kind == 0)
+    if (cluster_set(c, set))
+        st = cluster_launch_set(c, set, MODE_ELEMENT, first, count, (const double*)su.dev, nullptr, nullptr,
+                                (double*)sk.dev, (double*)sr.dev, nmax);
+    else if (s.kind == 0)
         st = launch_bulk(c, set, MODE_ELEMENT, first, count, (const double*)su.dev, nullptr, nullptr,
                          (double*)sk.dev, (double*)sr.dev, nmax, nullptr, nullptr);
     else
@@ -1182,7 +1203,10 @@ fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* c, const double* u, double* vals, d
     cudaMemsetAsync(c->d_status.p, 0, sizeof(int), sm);
     for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
         SetData& s = c->sets[k];
-        if (s.kind == 0)
+        if (cluster_set(c, k))
+            st = cluster_launch_set(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev,
+                                    (double*)sr.dev, nullptr, nullptr, 0);
+        else if (s.kind == 0)
             st = launch_bulk(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev, (double*)sr.dev,
                              nullptr, nullptr, 0, nullptr, nullptr);
         else
@@ -1200,6 +1224,14 @@ fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* c, const double* u, double* vals, d
     release(c, sr);
     if (st != FEM_GPU_OK) return st;
     return read_status(c);
+}
+
+fem_gpu_status fem_gpu_check_status(fem_gpu_ctx* c) {
+    if (!c) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    fem_gpu_status st = read_status(c);
+    cudaMemsetAsync(c->d_status.p, 0, sizeof(int), stream_of(c));
+    return st;
 }
 
 fem_gpu_status fem_gpu_apply(fem_gpu_ctx* c, const double* x, double* y, uint32_t flags) {

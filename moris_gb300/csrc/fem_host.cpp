@@ -355,6 +355,88 @@ fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* c, const fem_gpu_side_set_desc*
     return FEM_GPU_OK;
 }
 
+fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_side_set_desc* d, int32_t* idx) {
+    if (!c || !d) return FEM_GPU_BAD_ARG;
+    if (c->host_final) return fail(c, FEM_GPU_BAD_ARG, "sets must be added before finalize");
+    if (d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE &&
+        d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE &&
+        d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST)
+        return fail(c, FEM_GPU_UNSUPPORTED, "double-sided iwg type");
+    if (c->dim != 3 || c->ip_cell != FEM_GPU_CELL_HEX8 || d->model_type != FEM_GPU_MODEL_3D)
+        return fail(c, FEM_GPU_UNSUPPORTED, "double-sided sets need a 3D HEX8 model");
+    if (d->facet_cell_type != FEM_GPU_CELL_TRI3 && d->facet_cell_type != FEM_GPU_CELL_QUAD4)
+        return fail(c, FEM_GPU_BAD_ARG, "facet cell type");
+    const Rule r = gauss_rule(d->integration_rule);
+    if (r.n == 0 || r.dim != 2) return fail(c, FEM_GPU_BAD_ARG, "facet integration rule");
+    const bool tri_rule = d->integration_rule == FEM_GPU_RULE_TRI_3 || d->integration_rule == FEM_GPU_RULE_TRI_7;
+    if (tri_rule != (d->facet_cell_type == FEM_GPU_CELL_TRI3))
+        return fail(c, FEM_GPU_BAD_ARG, "integration rule does not match the facet cell");
+    if (d->num_clusters <= 0 || !d->leader_ip_cell || !d->follower_ip_cell || !d->facet_offsets ||
+        !d->facet_coords || !d->leader_param_coords || !d->follower_param_coords || !d->leader_youngs_modulus ||
+        !d->follower_youngs_modulus)
+        return fail(c, FEM_GPU_BAD_ARG, "double-sided set arrays");
+    if (!(d->poisson_ratio > -1.0 && d->poisson_ratio < 0.5)) return fail(c, FEM_GPU_BAD_ARG, "poisson ratio");
+    if (!std::isfinite(d->alpha)) return fail(c, FEM_GPU_NONFINITE, "alpha");
+    SetData s;
+    s.kind = 2;
+    s.dside = *d;
+    s.neq = d->num_clusters;
+    s.nfv = cell_num_nodes(d->facet_cell_type);
+    s.ip_cell.assign(d->leader_ip_cell, d->leader_ip_cell + s.neq);
+    s.fcell.assign(d->follower_ip_cell, d->follower_ip_cell + s.neq);
+    for (int64_t i = 0; i < s.neq; ++i)
+        if (s.ip_cell[i] < 0 || s.ip_cell[i] >= c->num_cells || s.fcell[i] < 0 || s.fcell[i] >= c->num_cells)
+            return fail(c, FEM_GPU_OOB_INDEX, "double-sided cluster cell");
+    s.fc_off.assign(d->facet_offsets, d->facet_offsets + s.neq + 1);
+    if (s.fc_off[0] != 0) return fail(c, FEM_GPU_BAD_ARG, "facet offsets must start at 0");
+    for (int64_t i = 0; i < s.neq; ++i)
+        if (s.fc_off[i + 1] <= s.fc_off[i]) return fail(c, FEM_GPU_BAD_ARG, "every cluster needs a facet");
+    const int64_t nv = s.fc_off[s.neq] * s.nfv * 3;
+    s.fc_x.assign(d->facet_coords, d->facet_coords + nv);
+    s.fc_xl.assign(d->leader_param_coords, d->leader_param_coords + nv);
+    s.fc_xf.assign(d->follower_param_coords, d->follower_param_coords + nv);
+    for (int64_t k = 0; k < nv; ++k)
+        if (!std::isfinite(s.fc_x[k]) || !std::isfinite(s.fc_xl[k]) || !std::isfinite(s.fc_xf[k]))
+            return fail(c, FEM_GPU_NONFINITE, "facet coordinates");
+    s.E.assign(d->leader_youngs_modulus, d->leader_youngs_modulus + s.neq);
+    s.EF.assign(d->follower_youngs_modulus, d->follower_youngs_modulus + s.neq);
+    for (int64_t i = 0; i < s.neq; ++i)
+        if (!(s.E[i] > 0.0) || !(s.EF[i] > 0.0) || !std::isfinite(s.E[i]) || !std::isfinite(s.EF[i]))
+            return fail(c, FEM_GPU_NONFINITE, "youngs modulus must be finite and > 0");
+    s.dside.leader_ip_cell = s.dside.follower_ip_cell = nullptr;
+    s.dside.facet_offsets = nullptr;
+    s.dside.facet_coords = s.dside.leader_param_coords = s.dside.follower_param_coords = nullptr;
+    s.dside.leader_youngs_modulus = s.dside.follower_youngs_modulus = nullptr;
+    c->sets.push_back(std::move(s));
+    if (idx) *idx = (int32_t)c->sets.size() - 1;
+    return FEM_GPU_OK;
+}
+
+}  // extern "C"
+
+namespace fem {
+double ip_cell_measure(const fem_gpu_ctx* c, int64_t cell) {
+    const Rule r = gauss_rule(c->dim == 2 ? FEM_GPU_RULE_QUAD_2x2 : FEM_GPU_RULE_HEX_2x2x2);
+    const int npe = c->npe, d = c->dim;
+    double vol = 0.0;
+    for (int q = 0; q < r.n; ++q) {
+        double N[8], dN[24], J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        lagrange(c->ip_cell, &r.pts[(size_t)q * r.dim], N, dN);
+        for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j)
+                for (int a = 0; a < npe; ++a) J[i][j] += dN[i * npe + a] * c->coords[(int64_t)c->cells[cell * npe + a] * d + j];
+        const double det = d == 2 ? J[0][0] * J[1][1] - J[0][1] * J[1][0]
+                                  : J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                                        J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                                        J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        vol += r.w[q] * det;
+    }
+    return vol;
+}
+}  // namespace fem
+
+extern "C" {
+
 /* MSI work of Model_Solver_Interface::finalize and build_graph:
    - used bases (referenced by a node of a cell of any set) ranked in basis
      order; adof id = type * n_used + rank (Dof_Manager::set_owned_adofs_ids_
@@ -374,8 +456,10 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
     if (c->sets.empty()) return fail(c, FEM_GPU_BAD_ARG, "no sets");
     const int npe = c->npe, dim = c->dim;
     std::vector<char> cell_used(c->num_cells, 0);
-    for (auto& s : c->sets)
+    for (auto& s : c->sets) {
         for (auto v : s.ip_cell) cell_used[v] = 1;
+        for (auto v : s.fcell) cell_used[v] = 1;
+    }
     std::vector<char> used(c->num_bases, 0);
     for (int64_t e = 0; e < c->num_cells; ++e) {
         if (!cell_used[e]) continue;
@@ -425,13 +509,36 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
         for (int64_t e = 0; e < c->num_cells; ++e)
             for (int32_t k = 0; k < cb_len[e]; ++k) adj[fillp[cb[cb_off[e] + k]]++] = e;
     }
-    // union lists U(b)
+    // cells coupled to a cell through a double-sided equation object
+    std::vector<int64_t> pt_off(c->num_cells + 1, 0);
+    for (auto& s : c->sets)
+        if (s.kind == 2)
+            for (int64_t i = 0; i < s.neq; ++i) {
+                pt_off[s.ip_cell[i] + 1]++;
+                pt_off[s.fcell[i] + 1]++;
+            }
+    for (int64_t e = 0; e < c->num_cells; ++e) pt_off[e + 1] += pt_off[e];
+    std::vector<int32_t> partners(pt_off[c->num_cells]);
+    {
+        std::vector<int64_t> fillp(pt_off.begin(), pt_off.end() - 1);
+        for (auto& s : c->sets)
+            if (s.kind == 2)
+                for (int64_t i = 0; i < s.neq; ++i) {
+                    partners[fillp[s.ip_cell[i]]++] = s.fcell[i];
+                    partners[fillp[s.fcell[i]]++] = s.ip_cell[i];
+                }
+    }
+    // union lists U(b): bases of every equation object that contains b
     std::vector<std::vector<int32_t>> U(nu);
     parallel_for(nu, [&](int64_t b) {
         auto& u = U[b];
         for (int64_t k = adj_off[b]; k < adj_off[b + 1]; ++k) {
             const int64_t e = adj[k];
             u.insert(u.end(), cb.begin() + cb_off[e], cb.begin() + cb_off[e] + cb_len[e]);
+            for (int64_t q = pt_off[e]; q < pt_off[e + 1]; ++q) {
+                const int64_t e2 = partners[q];
+                u.insert(u.end(), cb.begin() + cb_off[e2], cb.begin() + cb_off[e2] + cb_len[e2]);
+            }
         }
         std::sort(u.begin(), u.end());
         u.erase(std::unique(u.begin(), u.end()), u.end());
@@ -457,8 +564,101 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
         }
     c->rowptr[nad] = (int32_t)acc;
     c->nnz = acc;
+    // cluster volumes per IP cell (bulk clusters), for the interface parameter
+    std::vector<double> cell_vol;
+    bool need_vol = false;
+    for (auto& s : c->sets)
+        need_vol |= s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
+    if (need_vol) {
+        cell_vol.assign(c->num_cells, 0.0);
+        for (auto& s : c->sets) {
+            if (s.kind != 0) continue;
+            for (int64_t i = 0; i < s.neq; ++i) {
+                double v = 0.0;
+                if (s.ig_off.empty()) {
+                    v = ip_cell_measure(c, s.ip_cell[i]);
+                } else {
+                    const int ign = cell_num_nodes(s.bulk.ig_cell_type);
+                    for (int64_t g = s.ig_off[i]; g < s.ig_off[i + 1]; ++g) {
+                        const double* x = &s.ig_coords[(size_t)g * ign * dim];
+                        if (s.bulk.ig_cell_type == FEM_GPU_CELL_TET4) {
+                            double a[3], b[3], cc[3];
+                            for (int k = 0; k < 3; ++k) {
+                                a[k] = x[0 * 3 + k] - x[2 * 3 + k];
+                                b[k] = x[1 * 3 + k] - x[2 * 3 + k];
+                                cc[k] = x[3 * 3 + k] - x[2 * 3 + k];
+                            }
+                            v += std::abs(a[0] * (b[1] * cc[2] - b[2] * cc[1]) - a[1] * (b[0] * cc[2] - b[2] * cc[0]) +
+                                          a[2] * (b[0] * cc[1] - b[1] * cc[0])) /
+                                 6.0;
+                        }
+                    }
+                }
+                cell_vol[s.ip_cell[i]] += v;
+            }
+        }
+    }
     // per set element data
     for (auto& s : c->sets) {
+        if (s.kind == 2) {
+            int maxnb = 0;
+            for (int64_t i = 0; i < s.neq; ++i)
+                maxnb = std::max(maxnb, std::max(cb_len[s.ip_cell[i]], cb_len[s.fcell[i]]));
+            if (2 * maxnb > 255) return fail(c, FEM_GPU_UNSUPPORTED, "more than 255 bases per element");
+            s.maxnb = maxnb;
+            const int W2 = 2 * maxnb;
+            s.nb.assign(s.neq * 2, 0);
+            s.bases.assign(s.neq * 2 * maxnb, -1);
+            s.T.assign(s.neq * 2 * npe * maxnb, 0.0);
+            s.sidx.assign(s.neq * W2 * W2, 0);
+            s.xe.resize(s.neq * 2 * npe * dim);
+            if (need_vol && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST) {
+                s.vol.resize(s.neq * 2);
+                for (int64_t i = 0; i < s.neq; ++i) {
+                    s.vol[i * 2] = cell_vol[s.ip_cell[i]];
+                    s.vol[i * 2 + 1] = cell_vol[s.fcell[i]];
+                    if (!(s.vol[i * 2] > 0.0) || !(s.vol[i * 2 + 1] > 0.0))
+                        return fail(c, FEM_GPU_BAD_ARG, "interface cluster without bulk clusters on its cells");
+                }
+            }
+            std::atomic<bool> bad{false};
+            parallel_for(s.neq, [&](int64_t i) {
+                int32_t all[512];
+                int nall = 0;
+                for (int side = 0; side < 2; ++side) {
+                    const int64_t e = side == 0 ? s.ip_cell[i] : s.fcell[i];
+                    const int32_t n = cb_len[e];
+                    const int32_t* b = cb.data() + cb_off[e];
+                    s.nb[i * 2 + side] = n;
+                    std::copy(b, b + n, s.bases.begin() + (i * 2 + side) * maxnb);
+                    for (int k = 0; k < n; ++k) all[nall++] = b[k];
+                    for (int k = n; k < maxnb; ++k) all[nall++] = -1;
+                    for (int a = 0; a < npe; ++a) {
+                        const int32_t nd = c->cells[e * npe + a];
+                        for (int d = 0; d < dim; ++d)
+                            s.xe[((i * 2 + side) * npe + a) * dim + d] = c->coords[(int64_t)nd * dim + d];
+                        for (int64_t k = c->t_off[nd]; k < c->t_off[nd + 1]; ++k) {
+                            const int32_t r = (int32_t)c->basis_rank[c->t_bases[k]];
+                            const int32_t j = (int32_t)(std::lower_bound(b, b + n, r) - b);
+                            s.T[(((i * 2 + side) * npe) + a) * maxnb + j] += c->t_w[k];
+                        }
+                    }
+                }
+                for (int ii = 0; ii < W2; ++ii) {
+                    if (all[ii] < 0) continue;
+                    const int32_t* u = c->ucols.data() + c->uoff[all[ii]];
+                    const int32_t ul = c->ulen[all[ii]];
+                    for (int jj = 0; jj < W2; ++jj) {
+                        if (all[jj] < 0) continue;
+                        const int32_t pos = (int32_t)(std::lower_bound(u, u + ul, all[jj]) - u);
+                        if (pos >= ul || u[pos] != all[jj] || pos > 65535) bad = true;
+                        s.sidx[(i * W2 + ii) * W2 + jj] = (uint16_t)pos;
+                    }
+                }
+            });
+            if (bad) return fail(c, FEM_GPU_UNSUPPORTED, "scatter slot does not fit 16 bits");
+            continue;
+        }
         int maxnb = 0;
         for (int64_t i = 0; i < s.neq; ++i) maxnb = std::max(maxnb, cb_len[s.ip_cell[i]]);
         if (maxnb > 255) return fail(c, FEM_GPU_UNSUPPORTED, "more than 255 bases per element");
@@ -520,7 +720,7 @@ fem_gpu_status fem_gpu_get_num_equation_objects(const fem_gpu_ctx* c, int32_t se
 fem_gpu_status fem_gpu_get_max_element_adofs(const fem_gpu_ctx* c, int32_t set, int32_t* n) {
     if (!c || !n || set < 0 || set >= (int32_t)c->sets.size()) return FEM_GPU_BAD_ARG;
     if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
-    *n = c->sets[set].maxnb * c->dim;
+    *n = c->sets[set].maxnb * c->dim * (c->sets[set].kind == 2 ? 2 : 1);
     return FEM_GPU_OK;
 }
 
@@ -530,10 +730,14 @@ fem_gpu_status fem_gpu_get_element_topology(const fem_gpu_ctx* c, int32_t set, i
     if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
     const SetData& s = c->sets[set];
     if (eq < 0 || eq >= s.neq) return FEM_GPU_OOB_INDEX;
-    const int nb = s.nb[eq];
     int k = 0;
-    for (int f = 0; f < c->dim; ++f)
-        for (int j = 0; j < nb; ++j) ids[k++] = (int32_t)(f * c->num_used + s.bases[eq * s.maxnb + j]);
+    const int sides = s.kind == 2 ? 2 : 1;
+    for (int side = 0; side < sides; ++side) {
+        const int64_t row = eq * sides + side;
+        const int nb = s.nb[row];
+        for (int f = 0; f < c->dim; ++f)
+            for (int j = 0; j < nb; ++j) ids[k++] = (int32_t)(f * c->num_used + s.bases[row * s.maxnb + j]);
+    }
     *n = k;
     return FEM_GPU_OK;
 }

@@ -32,16 +32,26 @@ struct DeviceBuf {
 
 // Everything a kernel reads for one set, laid out per equation object.
 struct SetData {
-    int kind = 0;  // 0 bulk, 1 side
+    int kind = 0;  // 0 bulk, 1 side, 2 double-sided (interface / ghost)
     fem_gpu_bulk_set_desc bulk{};
     fem_gpu_side_set_desc side{};
+    fem_gpu_double_side_set_desc dside{};
     int64_t neq = 0;
     std::vector<int32_t> ip_cell;
     std::vector<int64_t> ig_off;
     std::vector<double> ig_coords, ig_param;
     std::vector<double> E;
     std::vector<int32_t> ordinal;
-    // finalize products
+    // double-sided sets: ip_cell holds the leaders
+    std::vector<int32_t> fcell;                  // follower cells
+    std::vector<int64_t> fc_off;                 // facet offsets [neq+1]
+    std::vector<double> fc_x, fc_xl, fc_xf;      // facet vertex coords, param in leader / follower
+    std::vector<double> EF;                      // follower modulus
+    std::vector<double> vol;                     // [neq][2] leader / follower cluster volumes
+    int nfv = 0;                                 // facet vertices
+    // finalize products (double-sided sets: two sides per equation object,
+    // nb [neq][2], bases [neq][2][maxnb], T [neq][2][npe][maxnb],
+    // xe [neq][2][npe][dim], sidx [neq][2 maxnb][2 maxnb])
     int maxnb = 0;                 // max unique bases per element (padding width)
     std::vector<int32_t> nb;       // [neq]
     std::vector<int32_t> bases;    // [neq][maxnb] basis ranks, -1 padded
@@ -57,6 +67,9 @@ struct SetData {
     DeviceBuf d_pairs;      // bulk: upper-triangle index pairs of the pdof Gram matrix
     DeviceBuf d_g0;         // bulk: reference Gram table sum_q w_q dN/dxi dN/dxi
     DeviceBuf d_gp, d_gw;   // side: facet Gauss points and weights
+    DeviceBuf d_igoff, d_igx, d_igxi;            // cut clusters: integration cells
+    DeviceBuf d_fcoff, d_fcx, d_fcxl, d_fcxf;    // double-sided: facets
+    DeviceBuf d_EF, d_vol;
     int ngp = 0;            // Gauss points of the set's rule
     int nbsel = 0;          // padded basis width of the kernel instance
     int variant = 0;        // bulk kernel variant (set by fem_gpu_autotune)
@@ -88,6 +101,7 @@ struct fem_gpu_ctx {
     bool own_stream = false;
     bool stream_set = false;           // caller chose a stream (NULL = legacy default stream)
     fem::DeviceBuf d_rowptr, d_ulen, d_tables, d_scratch, d_status;
+    void* batch = nullptr;             // batched-launch state (fem_cluster.cu)
     int64_t launches = 0;
     std::string err;
 };
@@ -97,4 +111,12 @@ fem_gpu_status fail(fem_gpu_ctx* c, fem_gpu_status s, const std::string& msg);
 // device side (fem_device.cu)
 fem_gpu_status device_finalize(fem_gpu_ctx* c);
 void device_release(fem_gpu_ctx* c);
+// cut / double-sided clusters (fem_cluster.cu)
+fem_gpu_status cluster_finalize(fem_gpu_ctx* c, int set);
+void cluster_release(fem_gpu_ctx* c);
+bool cluster_set(const fem_gpu_ctx* c, int set);
+fem_gpu_status cluster_launch_set(fem_gpu_ctx* c, int set, int mode, int64_t first, int64_t count, const double* u,
+                                  double* vals, double* rhs, double* Kout, double* Rout, int nmax);
+// measure of an IP cell (sum of w detJ over the 2^d Gauss rule)
+double ip_cell_measure(const fem_gpu_ctx* c, int64_t cell);
 }  // namespace fem

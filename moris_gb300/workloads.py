@@ -20,8 +20,10 @@ same seeds and arrays feed the oracle in the tests.
 """
 import numpy as np
 
-from . import (FemModel, IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE, IWG_STRUC_LINEAR_NEUMANN, MODEL_3D,
-               MODEL_PLANE_STRAIN, RULE_BAR_3, RULE_HEX_3x3x3, RULE_QUAD_2x2, SHAPE_RECTANGULAR, hmr_uniform_mesh)
+from . import (CELL_HEX8, CELL_QUAD4, CELL_TET4, CELL_TRI3, FemModel, IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE,
+               IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE, IWG_STRUC_LINEAR_NEUMANN, IWG_STRUC_LINEAR_VW_GHOST,
+               MODEL_3D, MODEL_PLANE_STRAIN, RULE_BAR_3, RULE_HEX_3x3x3, RULE_QUAD_2x2, RULE_TET_4, RULE_TRI_7,
+               SHAPE_RECTANGULAR, hmr_uniform_mesh)
 from . import RULE_HEX_2x2x2, RULE_QUAD_2x2 as _RULE_QUAD_2x2
 from .rng import uniform01
 
@@ -56,6 +58,91 @@ def elasticity_3d(n=64, seed=BASE_SEED + 2, finalize=True):
     if finalize:
         m.finalize()
     return m, mesh, E
+
+
+def sphere_field(n, seed, nspheres=40, rmin=0.03, rmax=0.12):
+    """Level set min_k(|x - c_k| - r_k) at the (n+1)^3 nodes of the unit cube,
+    centres uniform in the cube and radii uniform in [rmin, rmax] (splitmix64
+    stream of `seed`: 3 nspheres centre coordinates, then nspheres radii)."""
+    u = uniform01(seed, 4 * nspheres)
+    cen = u[:3 * nspheres].reshape(nspheres, 3)
+    rad = rmin + (rmax - rmin) * u[3 * nspheres:]
+    g = np.arange(n + 1) / n
+    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    phi = np.full(len(pts), np.inf)
+    for k in range(nspheres):
+        phi = np.minimum(phi, np.linalg.norm(pts - cen[k], axis=1) - rad[k])
+    return phi
+
+
+XFEM_E = (1.0, 0.1)
+XFEM_NU = 0.3
+XFEM_NITSCHE_ALPHA = 100.0
+XFEM_GHOST_ALPHA = 0.01
+
+
+def xfem_sets(x, E=XFEM_E, nu=XFEM_NU, tet_rule=RULE_TET_4, tri_rule=RULE_TRI_7, hex_rule=RULE_HEX_2x2x2,
+              alpha_if=XFEM_NITSCHE_ALPHA, alpha_gh=XFEM_GHOST_ALPHA):
+    """Set list of a decomposed XFEM mesh (phase-wise elasticity, Nitsche
+    interface, virtual-work ghost), in the order bulk sets, then double-sided
+    sets: [(kind, args)], kind 'bulk' or 'double'.  Empty sets are left out."""
+    sets = []
+    for p in (0, 1):
+        c = x["uncut%d" % p]
+        if len(c):
+            sets.append(("bulk", dict(ip_cells=c, E=np.full(len(c), E[p]), nu=nu, rule=hex_rule, ig_cell=CELL_HEX8)))
+    for p in (0, 1):
+        c = x["cut%d" % p]
+        if len(c["cells"]):
+            sets.append(("bulk", dict(ip_cells=c["cells"], E=np.full(len(c["cells"]), E[p]), nu=nu, rule=tet_rule,
+                                      ig_cell=CELL_TET4, ig_offsets=c["ig_offsets"], ig_coords=c["ig_coords"],
+                                      ig_param=c["ig_param"])))
+    it = x["interface"]
+    if len(it["leader"]):
+        n = len(it["leader"])
+        sets.append(("double", dict(iwg=IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE, leader=it["leader"],
+                                    follower=it["follower"], offsets=it["offsets"], coords=it["coords"],
+                                    leader_param=it["param"], follower_param=it["param"], EL=np.full(n, E[0]),
+                                    EF=np.full(n, E[1]), nu=nu, rule=tri_rule, facet_cell=CELL_TRI3, alpha=alpha_if)))
+    for p in (0, 1):
+        g = x["ghost%d" % p]
+        n = len(g["leader"])
+        if n:
+            sets.append(("double", dict(iwg=IWG_STRUC_LINEAR_VW_GHOST, leader=g["leader"], follower=g["follower"],
+                                        offsets=g["offsets"], coords=g["coords"], leader_param=g["leader_param"],
+                                        follower_param=g["follower_param"], EL=np.full(n, E[p]), EF=np.full(n, E[p]),
+                                        nu=nu, rule=RULE_QUAD_2x2, facet_cell=CELL_QUAD4, alpha=alpha_gh)))
+    return sets
+
+
+def add_xfem_sets(m, sets):
+    for kind, a in sets:
+        if kind == "bulk":
+            m.add_bulk_set(a["ip_cells"], a["E"], a["nu"], a["rule"], MODEL_3D, ig_cell=a["ig_cell"],
+                           ig_offsets=a.get("ig_offsets"), ig_coords=a.get("ig_coords"), ig_param=a.get("ig_param"))
+        else:
+            m.add_double_side_set(a["iwg"], a["leader"], a["follower"], a["offsets"], a["coords"], a["leader_param"],
+                                  a["follower_param"], a["EL"], a["EF"], a["nu"], a["rule"], a["facet_cell"],
+                                  a["alpha"])
+
+
+def xfem_spheres(n=96, seed=BASE_SEED + 3, nspheres=40, rmin=0.03, rmax=0.12, order=1, finalize=True, **kw):
+    """Two-phase XFEM workload: n^3 HEX8 background of the unit cube with
+    B-splines of `order`, cut by the sphere level set; phase 0 (phi >= 0) E = 1,
+    phase 1 (inside the spheres) E = 0.1, nu = 0.3; uncut cells HEX_2x2x2, cut
+    clusters TET4 cells with TET_4, Nitsche interface (alpha 100, TRI_7),
+    virtual-work ghost (alpha 0.01, QUAD_2x2).  Returns (model, decomposition,
+    set list)."""
+    from . import xtk
+    phi = sphere_field(n, seed, nspheres, rmin, rmax)
+    x = xtk.decompose((n, n, n), (1.0, 1.0, 1.0), order, phi)
+    sets = xfem_sets(x, **kw)
+    m = FemModel(3, x["mesh"], SHAPE_RECTANGULAR)
+    add_xfem_sets(m, sets)
+    if finalize:
+        m.finalize()
+    return m, x, sets
 
 
 def smooth_density(n, seed, rho_min=1e-3, passes=3):

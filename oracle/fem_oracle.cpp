@@ -458,6 +458,16 @@ struct BulkSet {
     std::vector<real> node_rho;  // optional nodal density field
     real beta = 3.0;
 };
+/* double-sided cluster set (interface / ghost): facets with vertex coords
+   and their parametric coords in the leader and follower IP cells */
+struct DoubleSet {
+    int iwg, facet_cell, rule, model;
+    std::vector<int32_t> leader, follower;
+    std::vector<int64_t> fc_off;
+    std::vector<real> fc_x, fc_xl, fc_xf;
+    std::vector<real> EL, EF;
+    real nu, alpha;
+};
 struct SideSet {
     int iwg, rule, model;
     std::vector<int32_t> ip_cell, ordinal;
@@ -489,6 +499,7 @@ struct orc_model {
     std::vector<real> t_w;
     std::vector<BulkSet> bulk;
     std::vector<SideSet> side;
+    std::vector<DoubleSet> dbl;
     // MSI products
     std::vector<int64_t> basis_rank;  // domain basis -> rank among used, -1 if unused
     int64_t num_used = 0;
@@ -701,6 +712,31 @@ int orc_model_add_side_set(orc_model* m, int iwg, int rule, int model, int64_t n
     return 0;
 }
 
+int orc_model_add_double_side_set(orc_model* m, int iwg, int facet_cell, int rule, int model, int64_t nc,
+                                  const int32_t* leader, const int32_t* follower, const int64_t* fc_off,
+                                  const double* fc_x, const double* fc_xl, const double* fc_xf, const double* EL,
+                                  const double* EF, double nu, double alpha) {
+    if (m->finalized) return 1;
+    DoubleSet s;
+    s.iwg = iwg;
+    s.facet_cell = facet_cell;
+    s.rule = rule;
+    s.model = model;
+    s.leader.assign(leader, leader + nc);
+    s.follower.assign(follower, follower + nc);
+    s.fc_off.assign(fc_off, fc_off + nc + 1);
+    const int64_t nv = fc_off[nc] * cell_nodes(facet_cell) * m->dim;
+    s.fc_x.assign(fc_x, fc_x + nv);
+    s.fc_xl.assign(fc_xl, fc_xl + nv);
+    s.fc_xf.assign(fc_xf, fc_xf + nv);
+    s.EL.assign(EL, EL + nc);
+    s.EF.assign(EF, EF + nc);
+    s.nu = nu;
+    s.alpha = alpha;
+    m->dbl.push_back(std::move(s));
+    return 0;
+}
+
 /* MSI: adof numbering by type then basis rank among used bases
    (Dof_Manager::create_adofs / set_owned_adofs_ids_by_type,
    FEM/MSI/src/cl_MSI_Dof_Manager.cpp:703-744, 820-985); element unique adof
@@ -715,6 +751,10 @@ int orc_model_finalize(orc_model* m) {
     std::vector<char> cell_used(m->num_cells, 0);
     for (auto& s : m->bulk) for (auto c : s.ip_cell) cell_used[c] = 1;
     for (auto& s : m->side) for (auto c : s.ip_cell) cell_used[c] = 1;
+    for (auto& s : m->dbl) {
+        for (auto c : s.leader) cell_used[c] = 1;
+        for (auto c : s.follower) cell_used[c] = 1;
+    }
     std::vector<char> used(m->num_bases, 0);
     for (int64_t c = 0; c < m->num_cells; ++c) {
         if (!cell_used[c]) continue;
@@ -749,6 +789,17 @@ int orc_model_finalize(orc_model* m) {
     for (int64_t b = 0; b < nu; ++b) {
         std::vector<int32_t>& u = uni[b];
         for (auto c : cells_of[b]) u.insert(u.end(), m->cell_ubases[c].begin(), m->cell_ubases[c].end());
+    }
+    // a double-sided equation object couples the leader's and the follower's bases
+    for (auto& s : m->dbl)
+        for (size_t i = 0; i < s.leader.size(); ++i) {
+            const auto& L = m->cell_ubases[s.leader[i]];
+            const auto& F = m->cell_ubases[s.follower[i]];
+            for (auto b : L) uni[b].insert(uni[b].end(), F.begin(), F.end());
+            for (auto b : F) uni[b].insert(uni[b].end(), L.begin(), L.end());
+        }
+    for (int64_t b = 0; b < nu; ++b) {
+        std::vector<int32_t>& u = uni[b];
         std::sort(u.begin(), u.end());
         u.erase(std::unique(u.begin(), u.end()), u.end());
     }
@@ -766,11 +817,13 @@ int orc_model_finalize(orc_model* m) {
 
 int64_t orc_model_num_adofs(const orc_model* m) { return m->num_used * m->dim; }
 int64_t orc_model_nnz(const orc_model* m) { return m->rowptr.empty() ? 0 : m->rowptr.back(); }
-int orc_model_num_sets(const orc_model* m) { return (int)(m->bulk.size() + m->side.size()); }
+int orc_model_num_sets(const orc_model* m) { return (int)(m->bulk.size() + m->side.size() + m->dbl.size()); }
 int64_t orc_model_num_eq(const orc_model* m, int set) {
     if (set < (int)m->bulk.size()) return (int64_t)m->bulk[set].ip_cell.size();
     set -= (int)m->bulk.size();
     if (set < (int)m->side.size()) return (int64_t)m->side[set].ip_cell.size();
+    set -= (int)m->side.size();
+    if (set < (int)m->dbl.size()) return (int64_t)m->dbl[set].leader.size();
     return -1;
 }
 int orc_graph(const orc_model* m, int32_t* rowptr, int32_t* colidx) {
@@ -787,7 +840,13 @@ namespace {
 
 int ip_cell_of(const orc_model* m, int set, int64_t eq) {
     if (set < (int)m->bulk.size()) return m->bulk[set].ip_cell[eq];
-    return m->side[set - m->bulk.size()].ip_cell[eq];
+    set -= (int)m->bulk.size();
+    if (set < (int)m->side.size()) return m->side[set].ip_cell[eq];
+    return m->dbl[set - m->side.size()].leader[eq];
+}
+const DoubleSet* double_set(const orc_model* m, int set) {
+    const int k = set - (int)m->bulk.size() - (int)m->side.size();
+    return k >= 0 && k < (int)m->dbl.size() ? &m->dbl[k] : nullptr;
 }
 
 /* element adof ids: Equation_Object::get_equation_obj_dof_ids
@@ -1029,10 +1088,249 @@ void side_pdof(const orc_model* m, const SideSet& s, int64_t eq, const Mat& upd,
     (void)nstress;
 }
 
+/* measure of the cell cluster on an IP cell: the bulk clusters there, their
+   integration cells' measures (xtk::Side_Cluster::compute_cluster_cell_measure
+   -> associated cell cluster, XTK/src/cl_XTK_Side_Cluster.cpp:184-202; tet
+   measure |det| / 6; an uncut cell's own measure sum_q w detJ).              */
+real cell_cluster_volume(const orc_model* m, int cell) {
+    real v = 0.0;
+    for (const BulkSet& s : m->bulk)
+        for (size_t i = 0; i < s.ip_cell.size(); ++i) {
+            if (s.ip_cell[i] != cell) continue;
+            if (s.ig_off.empty()) {
+                Mat X = ip_coords(m, cell);
+                RuleTab rt = make_rule(m->dim == 2 ? ORC_RULE_QUAD_2x2 : ORC_RULE_HEX_2x2x2);
+                for (int q = 0; q < rt.n; ++q) {
+                    Mat Nq, dNq;
+                    shape(m->ip_cell, &rt.pts[(size_t)q * rt.dim], Nq, dNq);
+                    Mat J = mul(dNq, X);
+                    v += rt.w[q] * det_bulk(J, m->ip_cell, false);
+                }
+                continue;
+            }
+            const int ign = cell_nodes(s.ig_cell), d = m->dim;
+            for (int64_t g = s.ig_off[i]; g < s.ig_off[i + 1]; ++g) {
+                Mat Xg(ign, d);
+                for (int a = 0; a < ign; ++a)
+                    for (int k = 0; k < d; ++k) Xg(a, k) = s.ig_coords[(g * ign + a) * d + k];
+                Mat XI;
+                param_coords(s.ig_cell, XI);
+                Mat Nq, dNq;
+                shape(s.ig_cell, &XI.a[0], Nq, dNq);
+                v += std::abs(det_bulk(mul(dNq, Xg), s.ig_cell, false));
+            }
+        }
+    return v;
+}
+
+/* facet point of a double-sided cluster: side detJ (TRI3 |t1 x t2| / 2,
+   QUAD4 |t1 x t2|, cl_MTK_Space_Interpolator.cpp:808-850) and the normal
+   t1 x t2 / |.| (eval_normal_side_tri / _quad, :1349).                       */
+void facet_point(const DoubleSet& s, int64_t f, const real* xq, real& detJ, real* n, Mat& Nf) {
+    Mat dNf;
+    shape(s.facet_cell, xq, Nf, dNf);
+    const int nfv = cell_nodes(s.facet_cell);
+    Mat X(nfv, 3);
+    for (int a = 0; a < nfv; ++a)
+        for (int k = 0; k < 3; ++k) X(a, k) = s.fc_x[(f * nfv + a) * 3 + k];
+    Mat Jt = mul(dNf, X);
+    const real c0 = Jt(0, 1) * Jt(1, 2) - Jt(0, 2) * Jt(1, 1);
+    const real c1 = Jt(0, 2) * Jt(1, 0) - Jt(0, 0) * Jt(1, 2);
+    const real c2 = Jt(0, 0) * Jt(1, 1) - Jt(0, 1) * Jt(1, 0);
+    const real nn = std::sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+    detJ = s.facet_cell == ORC_CELL_TRI3 ? nn / 2.0 : nn;
+    // degenerate facet: zero measure, no normal (contributes nothing)
+    const real inv = nn > 0.0 ? 1.0 / nn : 0.0;
+    n[0] = c0 * inv;
+    n[1] = c1 * inv;
+    n[2] = c2 * inv;
+}
+
+/* flat normal of order 2 of the virtual-work ghost, 3D
+   (IWG_Isotropic_Struc_Linear_Virtual_Work_Ghost::get_flat_normal_matrix,
+   ..._Virtual_Work_Ghost.cpp:262-409) */
+Mat ghost_flat_normal_3d(const real* n) {
+    Mat F(3, 6, 0.0);
+    F(0, 0) = n[0];
+    F(1, 1) = n[1];
+    F(2, 2) = n[2];
+    F(1, 3) = n[2];
+    F(2, 3) = n[1];
+    F(0, 4) = n[2];
+    F(2, 4) = n[0];
+    F(0, 5) = n[1];
+    F(1, 5) = n[0];
+    return F;
+}
+
+/* Element_Double_Sideset::compute_jacobian_and_residual (FEM/INT/src/ELEM/
+   cl_FEM_Element_Double_Sideset.cpp:283-347) over the facets of one
+   double-sided cluster: leader / follower points from the facet's
+   parametric vertices (get_follower_integration_point, :113), the leader
+   normal, w* = w detJ, then
+   - IWG_Isotropic_Struc_Linear_Interface::compute_residual / compute_jacobian
+     (FEM/INT/src/IWG/cl_FEM_IWG_Isotropic_Struc_Linear_Interface.cpp:51-386)
+     with SP_Nitsche_Interface::eval_SP (SP/cl_FEM_SP_Nitsche_Interface.cpp:
+     51-97): gamma = 2 alpha |G| / (V_L/E_L + V_F/E_F), w_L, w_F the
+     weights; beta = -1 symmetric / +1 unsymmetric (IWG_Factory, cl_FEM_IWG_
+     Factory.cpp:202-206); linear CM, so dTestTraction = 0 and the SP has no
+     dof dependency;
+   - IWG_Isotropic_Struc_Linear_Virtual_Work_Ghost (..._Virtual_Work_Ghost.cpp:
+     50-244) with SP_Ghost_Virtual_Work::eval_SP (SP/cl_FEM_SP_Ghost_Virtual_
+     Work.cpp:30-38): gamma = alpha h^(2(p-1)+1), p = 1, h the side length
+     measure sqrt(4 A / pi) (Cluster::compute_cluster_cell_length_measure,
+     FEM/INT/src/ELEM/cl_FEM_Cluster.cpp:858-920).
+   Output K (48 x 48) and R (48) in [leader pdofs | follower pdofs], each
+   type-major.                                                                */
+void double_pdof(const orc_model* m, const DoubleSet& s, int64_t eq, const Mat& updL, const Mat& updF, Mat& K,
+                 Mat& R) {
+    const int d = m->dim, npe = cell_nodes(m->ip_cell), nd = d * npe;
+    K = Mat(2 * nd, 2 * nd, 0.0);
+    R = Mat(2 * nd, 1, 0.0);
+    const int cl = s.leader[eq], cf = s.follower[eq];
+    Mat XL = ip_coords(m, cl), XF = ip_coords(m, cf);
+    Mat DL = constitutive(s.model, d, s.EL[eq], s.nu), DF = constitutive(s.model, d, s.EF[eq], s.nu);
+    Mat uL(nd, 1), uF(nd, 1);
+    for (int f = 0; f < d; ++f)
+        for (int a = 0; a < npe; ++a) {
+            uL(f * npe + a, 0) = updL(a, f);
+            uF(f * npe + a, 0) = updF(a, f);
+        }
+    RuleTab rt = make_rule(s.rule);
+    const int nfv = cell_nodes(s.facet_cell);
+    // cluster measures
+    real area = 0.0;
+    for (int64_t f = s.fc_off[eq]; f < s.fc_off[eq + 1]; ++f)
+        for (int q = 0; q < rt.n; ++q) {
+            real dj, n[3];
+            Mat Nf;
+            facet_point(s, f, &rt.pts[(size_t)q * rt.dim], dj, n, Nf);
+            area += rt.w[q] * dj;
+        }
+    const bool ghost = s.iwg == ORC_IWG_STRUC_LINEAR_VW_GHOST;
+    real gamma, wl = 0.0, wf = 0.0;
+    if (ghost) {
+        const real h = std::pow(4.0 * area / M_PI, 1.0 / 2.0);
+        gamma = s.alpha * std::pow(h, 2.0 * (1.0 - 1.0) + 1.0);
+    } else {
+        const real VL = cell_cluster_volume(m, cl), VF = cell_cluster_volume(m, cf);
+        const real deno = VL / s.EL[eq] + VF / s.EF[eq];
+        gamma = 2.0 * s.alpha * area / deno;
+        wl = (VL / s.EL[eq]) / deno;
+        wf = (VF / s.EF[eq]) / deno;
+    }
+    const real beta = s.iwg == ORC_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
+    Mat KLL(nd, nd, 0.0), KLF(nd, nd, 0.0), KFL(nd, nd, 0.0), KFF(nd, nd, 0.0), RL(nd, 1, 0.0), RF(nd, 1, 0.0);
+    for (int64_t f = s.fc_off[eq]; f < s.fc_off[eq + 1]; ++f)
+        for (int q = 0; q < rt.n; ++q) {
+            real detJ, n[3];
+            Mat Nf;
+            facet_point(s, f, &rt.pts[(size_t)q * rt.dim], detJ, n, Nf);
+            if (detJ < -1.0e-6) continue;
+            const real w = rt.w[q] * detJ;
+            Mat XIL(nfv, d), XIF(nfv, d);
+            for (int a = 0; a < nfv; ++a)
+                for (int k = 0; k < d; ++k) {
+                    XIL(a, k) = s.fc_xl[(f * nfv + a) * d + k];
+                    XIF(a, k) = s.fc_xf[(f * nfv + a) * d + k];
+                }
+            Mat xiL = mul(Nf, XIL), xiF = mul(Nf, XIF);
+            Mat NrL, dL, NrF, dF;
+            ip_eval(m, XL, xiL.a.data(), NrL, dL);
+            ip_eval(m, XF, xiF.a.data(), NrF, dF);
+            Mat BL = test_strain(s.model, dL), BF = test_strain(s.model, dF);
+            Mat NL = field_N(NrL, d), NF = field_N(NrF, d);
+            Mat Fn = flat_normal(n, d, 6);
+            Mat tL = mul(Fn, mul(DL, BL)), tF = mul(Fn, mul(DF, BF));  // traction operators
+            Mat tLt = trans(tL), tFt = trans(tF), NLt = trans(NL), NFt = trans(NF);
+            if (ghost) {
+                Mat FnM = ghost_flat_normal_3d(n);
+                Mat gL = trans(mul(FnM, BL)), gF = trans(mul(FnM, BF));  // B^T FnM^T
+                Mat jump = mul(tL, uL);
+                add_scaled(jump, -1.0, mul(tF, uF));
+                add_scaled(RL, w * gamma, mul(gL, jump));
+                add_scaled(RF, -w * gamma, mul(gF, jump));
+                add_scaled(KLL, w * gamma, mul(gL, tL));
+                add_scaled(KFL, -w * gamma, mul(gF, tL));
+                add_scaled(KLF, -w * gamma, mul(gL, tF));
+                add_scaled(KFF, w * gamma, mul(gF, tF));
+                continue;
+            }
+            Mat trac = mul(tL, uL);
+            for (auto& v : trac.a) v *= wl;
+            add_scaled(trac, wf, mul(tF, uF));
+            Mat jump = mul(NL, uL);
+            add_scaled(jump, -1.0, mul(NF, uF));
+            add_scaled(RL, -w, mul(NLt, trac));
+            add_scaled(RL, w * beta * wl, mul(tLt, jump));
+            add_scaled(RL, w * gamma, mul(NLt, jump));
+            add_scaled(RF, w, mul(NFt, trac));
+            add_scaled(RF, w * beta * wf, mul(tFt, jump));
+            add_scaled(RF, -w * gamma, mul(NFt, jump));
+            add_scaled(KLL, w * beta * wl, mul(tLt, NL));
+            add_scaled(KLL, w * gamma, mul(NLt, NL));
+            add_scaled(KLL, -w * wl, mul(NLt, tL));
+            add_scaled(KFL, w * beta * wf, mul(tFt, NL));
+            add_scaled(KFL, -w * gamma, mul(NFt, NL));
+            add_scaled(KFL, w * wl, mul(NFt, tL));
+            add_scaled(KLF, -w * beta * wl, mul(tLt, NF));
+            add_scaled(KLF, -w * gamma, mul(NLt, NF));
+            add_scaled(KLF, -w * wf, mul(NLt, tF));
+            add_scaled(KFF, -w * beta * wf, mul(tFt, NF));
+            add_scaled(KFF, w * gamma, mul(NFt, NF));
+            add_scaled(KFF, w * wf, mul(NFt, tF));
+        }
+    for (int r = 0; r < nd; ++r) {
+        R(r, 0) = RL(r, 0);
+        R(nd + r, 0) = RF(r, 0);
+        for (int c = 0; c < nd; ++c) {
+            K(r, c) = KLL(r, c);
+            K(r, nd + c) = KLF(r, c);
+            K(nd + r, c) = KFL(r, c);
+            K(nd + r, nd + c) = KFF(r, c);
+        }
+    }
+}
+
+/* element adof ids of any equation object (double-sided: leader's per-type
+   lists then the follower's, get_equation_obj_dof_ids over two pdof systems) */
+std::vector<int32_t> eq_ids(const orc_model* m, int set, int64_t eq) {
+    const DoubleSet* ds = double_set(m, set);
+    if (!ds) return element_ids(m, ip_cell_of(m, set, eq));
+    std::vector<int32_t> a = element_ids(m, ds->leader[eq]), b = element_ids(m, ds->follower[eq]);
+    a.insert(a.end(), b.begin(), b.end());
+    return a;
+}
+
 /* Equation_Object::get_egn_obj_jacobian_and_residual (FEM/MSI/src/
    cl_MSI_Equation_Object.cpp:789-842): u_pdof = T u_adof (compute_my_pdof_
    values :1101-1131), K_a = T^T K T, R_a = T^T R.                            */
 void element_adof(const orc_model* m, int set, int64_t eq, const double* u_adof, Mat& Ka, Mat& Ra) {
+    if (const DoubleSet* ds = double_set(m, set)) {
+        const int d = m->dim, npe = cell_nodes(m->ip_cell);
+        Mat TL = element_T(m, ds->leader[eq]), TF = element_T(m, ds->follower[eq]);
+        Mat T(TL.r + TF.r, TL.c + TF.c, 0.0);
+        for (int r = 0; r < TL.r; ++r)
+            for (int c = 0; c < TL.c; ++c) T(r, c) = TL(r, c);
+        for (int r = 0; r < TF.r; ++r)
+            for (int c = 0; c < TF.c; ++c) T(TL.r + r, TL.c + c) = TF(r, c);
+        std::vector<int32_t> ids = eq_ids(m, set, eq);
+        Mat ua((int)ids.size(), 1);
+        for (size_t k = 0; k < ids.size(); ++k) ua(k, 0) = u_adof ? u_adof[ids[k]] : 0.0;
+        Mat up = mul(T, ua);
+        Mat updL(npe, d), updF(npe, d);
+        for (int f = 0; f < d; ++f)
+            for (int a = 0; a < npe; ++a) {
+                updL(a, f) = up(f * npe + a, 0);
+                updF(a, f) = up(d * npe + f * npe + a, 0);
+            }
+        Mat K, R;
+        double_pdof(m, *ds, eq, updL, updF, K, R);
+        Mat Tt = trans(T);
+        Ka = mul(Tt, mul(K, T));
+        Ra = mul(Tt, R);
+        return;
+    }
     const int cell = ip_cell_of(m, set, eq);
     const int d = m->dim, npe = cell_nodes(m->ip_cell);
     Mat T = element_T(m, cell);
@@ -1058,7 +1356,7 @@ extern "C" {
 int orc_element_topology(const orc_model* m, int set, int64_t eq, int32_t* ids, int32_t* n) {
     if (!m->finalized || set < 0 || set >= orc_model_num_sets(m)) return 1;
     if (eq < 0 || eq >= orc_model_num_eq(m, set)) return 1;
-    std::vector<int32_t> v = element_ids(m, ip_cell_of(m, set, eq));
+    std::vector<int32_t> v = eq_ids(m, set, eq);
     std::copy(v.begin(), v.end(), ids);
     *n = (int32_t)v.size();
     return 0;
@@ -1076,7 +1374,7 @@ int orc_element_matrices(const orc_model* m, int set, int64_t eq, const double* 
 
 int orc_element_pdof_matrices(const orc_model* m, int set, int64_t eq, const double* u_pdof, double* K,
                               double* R, int32_t* npdof) {
-    if (set < 0 || set >= orc_model_num_sets(m)) return 1;
+    if (set < 0 || set >= orc_model_num_sets(m) || double_set(m, set)) return 1;
     const int d = m->dim, npe = cell_nodes(m->ip_cell);
     Mat upd(npe, d);
     for (int f = 0; f < d; ++f)
@@ -1118,7 +1416,7 @@ int orc_assemble(const orc_model* m, const double* u_adof, double* vals, double*
             if (i >= (int64_t)items.size()) break;
             Mat Ka, Ra;
             element_adof(m, items[i].set, items[i].eq, u_adof, Ka, Ra);
-            std::vector<int32_t> ids = element_ids(m, ip_cell_of(m, items[i].set, items[i].eq));
+            std::vector<int32_t> ids = eq_ids(m, items[i].set, items[i].eq);
             const int n = (int)ids.size();
             for (int c = 0; c < n; ++c) {
                 for (int r = 0; r < n; ++r) {

@@ -81,6 +81,13 @@ int orc_model_add_side_set(orc_model* m, int iwg, int rule, int model_type, int6
                            const int32_t* side_ip_cell, const int32_t* side_ordinal,
                            const double* youngs_modulus, double poisson, double nitsche_alpha,
                            const double* value);
+/* double-sided set (interface / ghost); sets are indexed bulk sets first,
+   then side sets, then double-sided sets */
+int orc_model_add_double_side_set(orc_model* m, int iwg, int facet_cell, int rule, int model_type,
+                                  int64_t num_clusters, const int32_t* leader, const int32_t* follower,
+                                  const int64_t* facet_offsets, const double* facet_coords,
+                                  const double* leader_param, const double* follower_param,
+                                  const double* leader_E, const double* follower_E, double nu, double alpha);
 int orc_model_finalize(orc_model* m);
 int64_t orc_model_num_adofs(const orc_model* m);
 int64_t orc_model_nnz(const orc_model* m);

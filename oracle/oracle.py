@@ -40,6 +40,8 @@ def load():
             "orc_model_add_bulk_set": (_I, [_P, _I, _I, _I, _L, _P, _P, _P, _P, _P, _D]),
             "orc_model_add_side_set": (_I, [_P, _I, _I, _I, _L, _P, _P, _P, _D, _D, _P]),
             "orc_model_set_density": (_I, [_P, _I, _P, _D]),
+            "orc_model_add_double_side_set": (_I, [_P, _I, _I, _I, _I, _L, _P, _P, _P, _P, _P, _P, _P, _P, _D,
+                                                   _D]),
             "orc_model_finalize": (_I, [_P]),
             "orc_model_num_adofs": (_L, [_P]),
             "orc_model_nnz": (_L, [_P]),
@@ -136,6 +138,15 @@ class OracleModel:
         xp = None if ig_param is None else np.ascontiguousarray(ig_param, dtype=np.float64)
         r = self.lib.orc_model_add_bulk_set(self.h, ig_cell, rule, model, len(ipc), _ptr(ipc), _ptr(off),
                                             _ptr(xc), _ptr(xp), _ptr(E), nu)
+        assert r == 0
+
+    def add_double_side_set(self, iwg, facet_cell, rule, model, leader, follower, offsets, coords, leader_param,
+                            follower_param, EL, EF, nu, alpha):
+        arrs = [np.ascontiguousarray(leader, dtype=np.int32), np.ascontiguousarray(follower, dtype=np.int32),
+                np.ascontiguousarray(offsets, dtype=np.int64)]
+        arrs += [np.ascontiguousarray(a, dtype=np.float64) for a in (coords, leader_param, follower_param, EL, EF)]
+        r = self.lib.orc_model_add_double_side_set(self.h, iwg, facet_cell, rule, model, len(arrs[0]),
+                                                   *[_ptr(a) for a in arrs], nu, alpha)
         assert r == 0
 
     def set_density(self, s, node_rho, beta=3.0):

@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-c3", action="store_true", help="skip the XFEM (config 3) record")
     return ap.parse_args()
 
 
@@ -175,6 +176,117 @@ def cpu_reference(mesh, E, seconds, steps=1, warmup=0):
         pass
     return dict(value=n_el / float(np.median(times)), cores=nthreads, n_el=n_el, stride=stride,
                 step_seconds=float(np.median(times)), cpu=cpu_model)
+
+
+NE_C3 = 96
+
+
+def c3_stats(x):
+    """Work counts of the XFEM workload: integration points of uncut cells,
+    cut clusters, interface facets and ghost faces."""
+    s = x["sizes"]
+    uncut = int(s.num_uncut[0] + s.num_uncut[1])
+    cut_gp = int(4 * (s.num_ig_cells[0] + s.num_ig_cells[1]))
+    return dict(uncut_cells=uncut, cut_clusters=int(s.num_cut[0] + s.num_cut[1]), cut_points=cut_gp,
+                tets=int(s.num_ig_cells[0] + s.num_ig_cells[1]), interface_clusters=int(s.num_interface),
+                interface_facets=int(s.num_interface_facets), ghost_faces=int(s.num_ghost[0] + s.num_ghost[1]))
+
+
+def c3_flops(st):
+    """FP64 operations of the cluster kernel's formulation per step (counted
+    from the kernel code, FMA = 2):
+      uncut cell      5,050 (Gram from the rule table, isotropic K, R = K u, K T, T^T K T)
+      cut point         800 (IG->IP map, detJ, J^-1 dN: 200; 300 Gram FMAs)
+      cut cluster     4,750 (epilogue as for an uncut cell)
+      interface facet 22,100 (7 points x 460 geometry, facet moments P and Q,
+                              normal-weighted cluster moments A1)
+      interface clus. 47,000 (K from A1 and Q, R = K u, K T, T^T K T on 48 x 48)
+      ghost cluster   86,000 (4 points geometry, n.D.B operators, 4 x 3 rank-1
+                              updates of the 48 x 48 block, epilogue)"""
+    return (5050 * st["uncut_cells"] + 800 * st["cut_points"] + 4750 * st["cut_clusters"] +
+            22100 * st["interface_facets"] + 47000 * st["interface_clusters"] + 86000 * st["ghost_faces"])
+
+
+def cpu_reference_c3(x, sets, seconds):
+    """Oracle assembly of the XFEM workload on all host threads over a bounded
+    sample (every k-th equation object of every set)."""
+    from oracle import OracleModel
+    import moris_gb300 as mg
+    nthreads = os.cpu_count() or 1
+    orc = OracleModel(3, mg.CELL_HEX8, mg.SHAPE_RECTANGULAR, x["mesh"])
+    for kind, a in sets:
+        if kind == "bulk":
+            orc.add_bulk_set(a["ig_cell"], a["rule"], mg.MODEL_3D, a["ip_cells"], a["E"], a["nu"],
+                             a.get("ig_offsets"), a.get("ig_coords"), a.get("ig_param"))
+    for kind, a in sets:
+        if kind == "double":
+            orc.add_double_side_set(a["iwg"], a["facet_cell"], a["rule"], mg.MODEL_3D, a["leader"], a["follower"],
+                                    a["offsets"], a["coords"], a["leader_param"], a["follower_param"], a["EL"],
+                                    a["EF"], a["nu"], a["alpha"])
+    orc.finalize()
+    u = np.random.default_rng(SEED + 11).uniform(-1.0, 1.0, orc.num_adofs)
+    out = (np.zeros(orc.nnz), np.zeros(orc.num_adofs))
+    stride = 4096
+    for _ in range(2):  # calibrate the stride to about `seconds` of work
+        t0 = time.perf_counter()
+        orc.assemble(u, nthreads=nthreads, eq_stride=stride, out=out)
+        dt = time.perf_counter() - t0
+        stride = max(1, int(stride * dt / seconds))
+    t0 = time.perf_counter()
+    orc.assemble(u, nthreads=nthreads, eq_stride=stride, out=out)
+    dt = time.perf_counter() - t0
+    # every set sampled with the same stride: the full assembly takes ~stride x dt
+    return dict(value=NE_C3 ** 3 / (stride * dt), cores=nthreads, stride=stride, seconds=dt)
+
+
+def run_c3(timed, stream, world, args):
+    """Config 3: two-phase XFEM, 96^3 background cut by 40 spheres; every
+    cluster in one persistent graph-captured launch (fem_gpu_assemble_batched)."""
+    import torch
+    import moris_gb300 as mg
+    from moris_gb300 import workloads
+    t0 = time.perf_counter()
+    m, x, sets = workloads.xfem_spheres(NE_C3, finalize=False)
+    m.set_stream(stream.cuda_stream)
+    m.finalize()
+    warps, split, tuned_ms = m.autotune_batched()
+    setup = time.perf_counter() - t0
+    st = c3_stats(x)
+    nad, nnz = m.num_adofs, m.nnz
+    u = torch.tensor(np.random.default_rng(SEED + 11).uniform(-1.0, 1.0, nad), device="cuda")
+    vals = torch.empty(nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(nad, dtype=torch.float64, device="cuda")
+    fn = lambda: m.assemble_batched(u, vals, rhs, mg.ASYNC)
+    for _ in range(3):
+        fn()
+    m.check_status()
+    l0 = m.launch_count()
+    steps = max(5, args.steps // 3)
+    ms = timed(fn, steps, 0)
+    launches = (m.launch_count() - l0) / steps
+    m.check_status()
+    n_el = NE_C3 ** 3
+    fl = c3_flops(st)
+    peak = mg.probe_fp64_tflops()
+    rec = {"workload": "XFEM two-phase %d^3 hex8 unit cube, linear B-splines, 40 spheres r in [0.03,0.12] "
+                       "(seed %d), E 1 / 0.1, nu 0.3, uncut HEX_2x2x2, cut TET4 cells TET_4, Nitsche interface "
+                       "TRI_7 alpha 100, virtual-work ghost QUAD_2x2 alpha 0.01" % (NE_C3, workloads.BASE_SEED + 3),
+           "elements": n_el, "elements_per_s": n_el / (ms * 1e-3), "ms_per_step": ms, "steps": steps,
+           "adofs": nad, "csr_nnz": nnz, "counts": st, "gpu_launches_per_step": launches,
+           "batched_config": {"warps": warps, "split_points": split, "tuned_ms": tuned_ms},
+           "roofline": {"bound": "fp64", "achieved": fl / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                        "frac": fl / (ms * 1e-3) / 1e12 / peak, "flops_per_step": fl,
+                        "peak_source": "measured in-run (FP64 FMA-chain probe)"},
+           "setup_seconds": setup}
+    if world == 1 and not args.no_cpu:
+        r = cpu_reference_c3(x, sets, min(args.cpu_seconds, 10.0))
+        rec["cpu_baseline"] = {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",
+                               "sample": "every %d-th equation object of every set, oracle restatement, %d threads"
+                                         % (r["stride"], r["cores"])}
+        rec["speedup_vs_cpu"] = rec["elements_per_s"] / r["value"]
+    del m
+    torch.cuda.empty_cache()
+    return rec
 
 
 def run_reference(args):
@@ -377,6 +489,8 @@ def main():
         line["c1_solve"] = {"workload": "2D plane strain 128^2 quad4, linear B-splines, Nitsche clamp, traction 1e-3",
                             "adofs": m1.num_adofs, "assembly_ms": ms_a1, "pcg_ms": (time.perf_counter() - t0) * 1e3,
                             "pcg_iterations": rep1["iterations"], "rel_residual": rep1["rel_residual"]}
+    if world == 1 and not args.no_c3:
+        line["c3_xfem"] = run_c3(timed, stream, world, args)
     if world == 1 and not args.no_cpu:
         r = cpu_reference(mesh, E, args.cpu_seconds)
         line["cpu_baseline"] = {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",

@@ -38,6 +38,7 @@ namespace fem {
 namespace {
 
 constexpr int kChunk = 32;  // integration points per geometry chunk
+constexpr int kMaxFP = 9;   // facet rule points (TRI_3, TRI_7, QUAD_2x2; QUAD_3x3)
 constexpr int kNPE = 8, kNPD = 24, kNSYM = 300;
 enum { CM_ASSEMBLE = 0, CM_ELEMENT = 1 };
 
@@ -68,6 +69,7 @@ struct SetDev {
     const double* fc_xl;
     const double* fc_xf;
     const double* vol;     // [neq][2]
+    const double* g0;      // bulk, uncut: rule Gram table sum_q w dN/dxi dN/dxi [24][24]
 };
 
 struct Item {
@@ -105,8 +107,9 @@ struct CL {
                          sWG = sG + kChunk * 24, sEnd = sWG + kChunk * 24;
     // double-sided (doubles)
     static constexpr int dX = 0, dT = dX + 48, dTW = dT + 16 * NB, dU = dTW + 16 * NB, dUA = dU + 48,
-                         dR = dUA + 6 * NB, dK = dR + 48, dKT = dK + 2304, dN = dKT + 288 * NB, dG = dN + 16,
-                         dTR = dG + 48, dGS = dTR + 144, dSC = dGS + 144, dEnd = dSC + 8;
+                         dR = dUA + 6 * NB, dK = dR + 48, dKT = dK + 2304, dWN = dKT + 288 * NB,
+                         dNR = dWN + kMaxFP * 16, dGG = dNR + kMaxFP * 16, dWQ = dGG + kMaxFP * 48, dSC = dWQ + kMaxFP, dP = dSC + 8,
+                         dEnd = dP + 2 * kMaxFP * 144;
     static constexpr int ND = sEnd > dEnd ? sEnd : dEnd;
     // ints (after the doubles): bases, row offsets, union lengths
     static constexpr int iB = 0, iRB = iB + 2 * NB, iUL = iRB + 6 * NB, NI = iUL + 2 * NB;
@@ -274,6 +277,27 @@ __device__ void bulk_item(const ClusterArgs& p, const SetDev& S, const Item& it,
         acc[j] = 0.0;
     }
     __syncthreads();
+    if (!S.cut && S.rect && S.g0) {
+        // constant Jacobian: A = detJ J^-1_i J^-1_j G0 (the rule's Gram table),
+        // no per-point work (uncut rectangular cells)
+        double jd[3];
+        for (int i = 0; i < 3; ++i) {
+            // edge lengths / 2 from the corner coordinates (J of the affine map)
+            jd[i] = 0.5 * (X[6 * 3 + i] - X[0 * 3 + i]);
+        }
+        const double detJ = jd[1] * jd[0] * jd[2];
+        const bool skip = detJ < -1.0e-6;  // cl_FEM_Element_Bulk.cpp:164
+        // detJ / (J_ii J_jj): the product of the remaining diagonal entries
+        // (off-diagonal pairs) or one division (diagonal pairs)
+        const double cd[3] = {jd[1] * jd[2] / jd[0], jd[0] * jd[2] / jd[1], jd[0] * jd[1] / jd[2]};
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            if (tid + j * TH >= kNSYM) continue;
+            const int i1 = pr[j] / 8, i2 = pc[j] / 8;
+            const double cj = i1 == i2 ? cd[i1] : jd[3 - i1 - i2];
+            acc[j] = skip ? 0.0 : cj * S.g0[pr[j] * 24 + pc[j]];
+        }
+    } else
     for (int q0 = it.q0; q0 < it.q1; q0 += kChunk) {
         const int nq = min(kChunk, it.q1 - q0);
         if (tid < kChunk) {
@@ -425,11 +449,15 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
     double* R = sd + Lo::dR;    // [48]
     double* K = sd + Lo::dK;    // [48][48]
     double* KT = sd + Lo::dKT;  // [48][NAD]
-    double* NN = sd + Lo::dN;   // [2][8]
-    double* GG = sd + Lo::dG;   // [2][3][8]
-    double* TR = sd + Lo::dTR;  // [2][3][24]
-    double* GS = sd + Lo::dGS;  // [2][3][24]
-    double* SC = sd + Lo::dSC;  // ws, n0, n1, n2, gamma, wL, wF
+    double* WN = sd + Lo::dWN;  // [q][2][8]   w* N of both sides
+    double* NR = sd + Lo::dNR;  // [q][2][8]   N of both sides
+    double* GG = sd + Lo::dGG;  // [q][2][24]  gradients of both sides
+    double* WQ = sd + Lo::dWQ;  // [q]         w* per facet point
+    double* SC = sd + Lo::dSC;  // n0, n1, n2, area, wL, wF
+    double* P = sd + Lo::dP;    // interface moments [2][8][2][3][8]
+    double* Q = P + 768;        // interface moments [2][8][2][8] (whole cluster)
+    double* GS = sd + Lo::dP;   // ghost: w* (n-projected strain) [q][2][3][24]
+    double* TR = GS + kMaxFP * 144;  // ghost: traction operators [q][2][3][24]
     int32_t* B = si + Lo::iB;   // [2][NB]
     int32_t* RB = si + Lo::iRB; // [2][3][NB]
     int32_t* UL = si + Lo::iUL; // [2][NB]
@@ -441,11 +469,26 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
     const double beta = S.iwg == FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
     const int nbs[2] = {S.nb[2 * e], S.nb[2 * e + 1]};
     const double Es[2] = {S.E[e], S.EF[e]};
+    const int ngp = S.ngp, nfv = S.nfv;
     for (int i = tid; i < 48; i += TH) X[i] = S.xe[e * 48 + i];
     for (int i = tid; i < 16 * NB; i += TH) T[i] = S.T[e * 16 * NB + i];
     for (int i = tid; i < 2 * NB; i += TH) B[i] = S.bases[e * 2 * NB + i];
     if (assemble && p.vals)
         for (int i = tid; i < 4 * NB * NB; i += TH) SL[i] = S.sidx[e * 4 * NB * NB + i];
+    for (int j = tid; j < 2304; j += TH) K[j] = 0.0;
+    if (!ghost) {
+        for (int j = tid; j < 256; j += TH) Q[j] = 0.0;
+        for (int j = tid; j < 2304; j += TH) KT[j] = 0.0;  // A1 (see below)
+    }
+    if (tid == 0) {
+        SC[3] = 0.0;
+        if (!ghost) {
+            // SP_Nitsche_Interface weights (the surface measure enters at the end)
+            const double vl = S.vol[2 * e] / Es[0], vf = S.vol[2 * e + 1] / Es[1];
+            SC[4] = vl / (vl + vf);
+            SC[5] = vf / (vl + vf);
+        }
+    }
     __syncthreads();
     for (int r = tid; r < NAD; r += TH) {
         const int s = r / (3 * NB), f = (r / NB) % 3, i = r % NB;
@@ -468,89 +511,142 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
         }
         TC[jj] = (uint8_t)cnt;
     }
-    // cluster measures and the stabilization parameters
-    if (tid == 0) {
-        double meas = 0.0;
-        for (int64_t f = S.fc_off[e]; f < S.fc_off[e + 1]; ++f)
-            for (int q = 0; q < S.ngp; ++q) {
-                double dj, n[3];
-                facet_geometry(S, f, S.gp + q * 2, dj, n);
-                meas += S.gw[q] * dj;
+    const double wsd[2] = {SC[4], SC[5]};
+    for (int64_t f = S.fc_off[e]; f < S.fc_off[e + 1]; ++f) {
+        __syncthreads();
+        // (A) facet points in parallel: lanes (q, side) for the gradients of the
+        // IP cells, lanes q (second warp) for w* and the normal of the facet
+        if (tid < 2 * ngp) {
+            const int q = tid >> 1, side = tid & 1;
+            const double* fx = side == 0 ? S.fc_xl : S.fc_xf;
+            double Nf[4], dNf[8], xi[3] = {0, 0, 0};
+            if (S.facet_cell == FEM_GPU_CELL_TRI3) Shape<2>::eval(S.gp + q * 2, Nf, dNf);
+            else Shape<0>::eval(S.gp + q * 2, Nf, dNf);
+            for (int k = 0; k < nfv; ++k)
+                for (int d = 0; d < 3; ++d) xi[d] = fma(Nf[k], fx[(f * nfv + k) * 3 + d], xi[d]);
+            double N[8], g[24], dj;
+            ip_gradients(X + side * 24, xi, S.rect, N, g, dj);
+            for (int a = 0; a < 8; ++a) NR[(q * 2 + side) * 8 + a] = N[a];
+            for (int i = 0; i < 24; ++i) GG[(q * 2 + side) * 24 + i] = g[i];
+        } else if (tid >= 32 && tid < 32 + ngp) {
+            const int q = tid - 32;
+            double dj, n[3];
+            facet_geometry(S, f, S.gp + q * 2, dj, n);
+            WQ[q] = dj < -1.0e-6 ? 0.0 : S.gw[q] * dj;
+            if (q == 0) {
+                SC[0] = n[0];
+                SC[1] = n[1];
+                SC[2] = n[2];
             }
-        if (ghost) {
-            // SP_Ghost_Virtual_Work: alpha h^(2(p-1)+1), p = 1; h = sqrt(4 A / pi)
-            // (Cluster::compute_cluster_cell_length_measure, side of a 3D cell)
-            SC[4] = S.alpha * sqrt(4.0 * meas / 3.14159265358979323846);
-            SC[5] = SC[6] = 0.0;
-        } else {
-            const double vl = S.vol[2 * e] / Es[0], vf = S.vol[2 * e + 1] / Es[1];
-            const double deno = vl + vf;
-            SC[4] = 2.0 * S.alpha * meas / deno;
-            SC[5] = vl / deno;
-            SC[6] = vf / deno;
         }
-    }
-    for (int j = tid; j < 2304; j += TH) K[j] = 0.0;
-    __syncthreads();
-    const double gamma = SC[4], wsd[2] = {SC[5], SC[6]};
-    for (int64_t f = S.fc_off[e]; f < S.fc_off[e + 1]; ++f)
-        for (int q = 0; q < S.ngp; ++q) {
-            const double* xq = S.gp + q * 2;
-            if (tid < 2) {
-                const double* fx = tid == 0 ? S.fc_xl : S.fc_xf;
-                double Nf[4], dNf[8], xi[3] = {0, 0, 0};
-                if (S.facet_cell == FEM_GPU_CELL_TRI3) Shape<2>::eval(xq, Nf, dNf);
-                else Shape<0>::eval(xq, Nf, dNf);
-                for (int k = 0; k < S.nfv; ++k)
-                    for (int d = 0; d < 3; ++d) xi[d] = fma(Nf[k], fx[(f * S.nfv + k) * 3 + d], xi[d]);
-                double N[8], g[24], dj;
-                ip_gradients(X + tid * 24, xi, S.rect, N, g, dj);
-                for (int a = 0; a < 8; ++a) NN[tid * 8 + a] = N[a];
-                for (int i = 0; i < 24; ++i) GG[tid * 24 + i] = g[i];
-            } else if (tid == 32 % TH) {
-                double dj, n[3];
-                facet_geometry(S, f, xq, dj, n);
-                SC[0] = dj < -1.0e-6 ? 0.0 : S.gw[q] * dj;
-                SC[1] = n[0];
-                SC[2] = n[1];
-                SC[3] = n[2];
+        __syncthreads();
+        const double n[3] = {SC[0], SC[1], SC[2]};
+        if (tid == 0) {
+            double a = 0.0;
+            for (int q = 0; q < ngp; ++q) a += WQ[q];
+            SC[3] += a;  // facet measure (interface surface / ghost side)
+        }
+        if (!ghost) {
+            // Interface.  The normal is constant on a flat facet, so every point
+            // sum factors through the facet moments
+            //   P[s][a][s'][k][b] = sum_q w* N_s[a] g_s'[k][b]
+            //   Q[s][a][s'][b]    = sum_q w* N_s[a] N_s'[b]   (whole cluster)
+            for (int i = tid; i < 16 * ngp; i += TH) WN[i] = NR[i] * WQ[i >> 4];
+            __syncthreads();
+            for (int j = tid; j < 1024; j += TH) {
+                if (j < 768) {
+                    // ((((s*8 + a)*2 + s2)*3 + k)*8 + b)
+                    const int b = j & 7, k = (j >> 3) % 3, s2 = (j / 24) & 1, a = (j / 48) & 7, s1 = j / 384;
+                    double v = 0.0;
+                    for (int q = 0; q < ngp; ++q) v = fma(WN[(q * 2 + s1) * 8 + a], GG[(q * 2 + s2) * 24 + k * 8 + b], v);
+                    P[j] = v;
+                } else {
+                    const int jj = j - 768, b = jj & 7, s2 = (jj >> 3) & 1, a = (jj >> 4) & 7, s1 = jj >> 7;
+                    double v = Q[jj];
+                    for (int q = 0; q < ngp; ++q) v = fma(WN[(q * 2 + s1) * 8 + a], NR[(q * 2 + s2) * 8 + b], v);
+                    Q[jj] = v;
+                }
             }
             __syncthreads();
-            // traction operators n.D.B (CM_Struc_Linear::traction / testTraction)
-            // and the strain projection of the ghost (flat normal of order 2)
-            for (int idx = tid; idx < 144; idx += TH) {
-                const int s = idx / 72, fr = (idx / 24) % 3, c = idx % 24;
+            // A1[s][a][s'][i][k][b] += n_i P[s][a][s'][k][b]: the normal-weighted
+            // moments of the whole cluster (K is formed once, after the last facet)
+            for (int j = tid; j < 2304; j += TH) {
+                const int kb = j % 24, i = (j / 24) % 3, pre = j / 72;  // pre = (s*8 + a)*2 + s'
+                KT[j] = fma(n[i], P[pre * 24 + kb], KT[j]);
+            }
+        } else {
+            // Ghost: per point w* (n-projected strain) and the traction operators of
+            // both sides, then K += sum_q sum_h GS_q[h]^T TR_q[h] (alpha h_G at the end)
+            for (int idx = tid; idx < ngp * 144; idx += TH) {
+                const int q = idx / 144, rem = idx % 144, s = rem / 72, fr = (rem / 24) % 3, c = rem % 24;
                 const int gg = c / 8, b = c % 8;
-                const double* g = GG + s * 24;
-                const double n[3] = {SC[1], SC[2], SC[3]};
+                const double* g = GG + (q * 2 + s) * 24;
                 const double ng = n[0] * g[b] + n[1] * g[8 + b] + n[2] * g[16 + b];
                 const double lam = Es[s] * S.lam_c, mu = Es[s] * S.mu_c;
                 TR[idx] = lam * n[fr] * g[gg * 8 + b] + mu * (n[gg] * g[fr * 8 + b] + (fr == gg ? ng : 0.0));
-                GS[idx] = (fr == gg ? ng - n[fr] * g[fr * 8 + b] : 0.0) + n[gg] * g[fr * 8 + b];
+                const double gs = (fr == gg ? ng - n[fr] * g[fr * 8 + b] : 0.0) + n[gg] * g[fr * 8 + b];
+                GS[idx] = (s == 0 ? WQ[q] : -WQ[q]) * gs;
             }
             __syncthreads();
-            const double ws = SC[0];
             for (int j = 0; j < PER; ++j) {
                 const int idx = tid + j * TH;
                 const int r = idx / 48, c = idx % 48;
                 const int sr = r / 24, rr = r % 24, sc = c / 24, cc = c % 24;
-                const int fr = rr / 8, a = rr % 8, gc = cc / 8, b = cc % 8;
-                const double sgr = sr == 0 ? 1.0 : -1.0, sgc = sc == 0 ? 1.0 : -1.0;
-                double v;
-                if (ghost) {
-                    v = 0.0;
-                    for (int h = 0; h < 3; ++h) v = fma(GS[sr * 72 + h * 24 + rr], TR[sc * 72 + h * 24 + cc], v);
-                    v *= sgr * sgc * gamma;
-                } else {
-                    const double Na = NN[sr * 8 + a], Nb = NN[sc * 8 + b];
-                    v = -sgr * wsd[sc] * Na * TR[sc * 72 + fr * 24 + cc] +
-                        beta * wsd[sr] * sgc * TR[sr * 72 + gc * 24 + rr] * Nb;
-                    if (fr == gc) v = fma(sgr * sgc * gamma * Na, Nb, v);
+                double v = 0.0;
+                for (int q = 0; q < ngp; ++q) {
+                    const double* gs = GS + q * 144 + sr * 72 + rr;
+                    const double* tr = TR + q * 144 + sc * 72 + cc;
+                    v = fma(gs[0], tr[0], v);
+                    v = fma(gs[24], tr[24], v);
+                    v = fma(gs[48], tr[48], v);
                 }
-                K[idx] = fma(ws, v, K[idx]);  // thread-owned entry
+                K[idx] = fma(sc == 0 ? 1.0 : -1.0, v, K[idx]);
             }
-            __syncthreads();
         }
+    }
+    __syncthreads();
+    if (!ghost) {
+        // Interface K from the cluster moments (IWG_Isotropic_Struc_Linear_
+        // Interface::compute_jacobian with the linear CM's traction operators):
+        //   T1 = -s_r w_c sum w* N_r[a] TR_c[f][(g,b)]
+        //      = -s_r w_c (lam_c A1[r][c][f][g][b] + mu_c A1[r][c][g][f][b] + d_fg mu_c sum_k A1[r][c][k][k][b])
+        //   T2 = beta w_r s_c sum w* TR_r[g][(f,a)] N_c[b]   (the same with the roles of r and c swapped)
+        const double* A1 = KT;
+        for (int j = 0; j < PER; ++j) {
+            const int idx = tid + j * TH;
+            const int r = idx / 48, c = idx % 48;
+            const int sr = r / 24, rr = r % 24, sc = c / 24, cc = c % 24;
+            const int fr = rr / 8, a = rr % 8, gc = cc / 8, b = cc % 8;
+            const double sgr = sr == 0 ? 1.0 : -1.0, sgc = sc == 0 ? 1.0 : -1.0;
+            const double* M1 = A1 + ((sr * 8 + a) * 2 + sc) * 72;  // [i][k][b] of (sr, a, sc)
+            const double* M2 = A1 + ((sc * 8 + b) * 2 + sr) * 72;  // [i][k][a] of (sc, b, sr)
+            double t1 = Es[sc] * (S.lam_c * M1[fr * 24 + gc * 8 + b] + S.mu_c * M1[gc * 24 + fr * 8 + b]);
+            double t2 = Es[sr] * (S.lam_c * M2[gc * 24 + fr * 8 + a] + S.mu_c * M2[fr * 24 + gc * 8 + a]);
+            if (fr == gc) {
+                t1 += Es[sc] * S.mu_c * (M1[b] + M1[24 + 8 + b] + M1[48 + 16 + b]);
+                t2 += Es[sr] * S.mu_c * (M2[a] + M2[24 + 8 + a] + M2[48 + 16 + a]);
+            }
+            K[idx] += -sgr * wsd[sc] * t1 + beta * wsd[sr] * sgc * t2;  // thread-owned entry
+        }
+    }
+    // stabilization parameters from the cluster measures, applied once
+    if (!ghost) {
+        // SP_Nitsche_Interface: gamma = 2 alpha |G| / (V_L/E_L + V_F/E_F)
+        const double vl = S.vol[2 * e] / Es[0], vf = S.vol[2 * e + 1] / Es[1];
+        const double gamma = 2.0 * S.alpha * SC[3] / (vl + vf);
+        for (int j = 0; j < PER; ++j) {
+            const int idx = tid + j * TH;
+            const int r = idx / 48, c = idx % 48;
+            const int sr = r / 24, rr = r % 24, sc = c / 24, cc = c % 24;
+            if (rr / 8 != cc / 8) continue;
+            const double sg = (sr == sc) ? gamma : -gamma;
+            K[idx] = fma(sg, Q[((sr * 8 + rr % 8) * 2 + sc) * 8 + cc % 8], K[idx]);
+        }
+    } else {
+        // SP_Ghost_Virtual_Work: alpha h^(2(p-1)+1), p = 1, h = sqrt(4 A / pi)
+        const double gamma = S.alpha * sqrt(4.0 * SC[3] / 3.14159265358979323846);
+        for (int j = 0; j < PER; ++j) K[tid + j * TH] *= gamma;
+    }
     // pdof values of both sides
     for (int r = tid; r < 48; r += TH) {
         const int s = r / 24, fr = (r / 8) % 3, a = r % 8;
@@ -610,7 +706,7 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
 }
 
 template <int NB, int W>
-__global__ void __launch_bounds__(32 * W, 512 / (32 * W)) cluster_kernel(ClusterArgs p) {
+__global__ void __launch_bounds__(32 * W, (384 / (32 * W)) > 0 ? 384 / (32 * W) : 1) cluster_kernel(ClusterArgs p) {
     using Lo = CL<NB>;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ long long s_item;
@@ -715,6 +811,7 @@ bool set_dev(const fem_gpu_ctx* c, const SetData& s, SetDev& d) {
         d.ig_off = (const int64_t*)s.d_igoff.p;
         d.ig_x = (const double*)s.d_igx.p;
         d.ig_xi = (const double*)s.d_igxi.p;
+        d.g0 = d.cut ? nullptr : (const double*)s.d_g0.p;
         return s.rhoe.empty();
     }
     if (s.kind == 2) {

@@ -367,7 +367,7 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
     if (d->facet_cell_type != FEM_GPU_CELL_TRI3 && d->facet_cell_type != FEM_GPU_CELL_QUAD4)
         return fail(c, FEM_GPU_BAD_ARG, "facet cell type");
     const Rule r = gauss_rule(d->integration_rule);
-    if (r.n == 0 || r.dim != 2) return fail(c, FEM_GPU_BAD_ARG, "facet integration rule");
+    if (r.n == 0 || r.dim != 2 || r.n > 9) return fail(c, FEM_GPU_BAD_ARG, "facet integration rule");
     const bool tri_rule = d->integration_rule == FEM_GPU_RULE_TRI_3 || d->integration_rule == FEM_GPU_RULE_TRI_7;
     if (tri_rule != (d->facet_cell_type == FEM_GPU_CELL_TRI3))
         return fail(c, FEM_GPU_BAD_ARG, "integration rule does not match the facet cell");

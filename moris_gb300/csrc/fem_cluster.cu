@@ -82,8 +82,9 @@ struct Item {
 struct ClusterArgs {
     const SetDev* sets;
     const Item* items;
-    int64_t nitems;
-    unsigned long long* counter;
+    int64_t nitems;       // items of the CTA phase; the warp phase follows them
+    int64_t nwarp_items;  // uncut rectangular cells (one warp each)
+    unsigned long long* counter;  // [2]: CTA queue, warp queue
     const int32_t* rowptr;
     const int32_t* ulen;
     int64_t nu;
@@ -705,6 +706,158 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
     if (bad) atomicOr(p.status, 1);
 }
 
+// per-warp layout of the uncut-cell phase (one cell per warp)
+template <int NB>
+struct WLay {
+    static constexpr int oX = 0, oT = oX + 24, oTW = oT + 8 * NB, oU = oTW + 8 * NB, oUA = oU + 24,
+                         oRP = oUA + 3 * NB, oK = oRP + 24, oKT = oK + 576, ND = oKT + 72 * NB;
+    static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + 3 * NB, NI = iUL + NB;
+    static constexpr int bTN = 0, bTC = bTN + 8 * NB, bS = ((bTC + NB + 1) / 2) * 2, NBYTE = bS + 2 * NB * NB;
+    static constexpr size_t bytes = ((size_t)ND * 8 + (size_t)NI * 4 + (size_t)NBYTE + 15) / 16 * 16;
+};
+
+// An uncut rectangular cell on one warp (no CTA barriers): A = detJ J^-1_i
+// J^-1_j G0 from the rule's Gram table, the isotropic K, R = K u, K_a = T^T K T
+// and the scatter -- the same arithmetic as bulk_item's constant-Jacobian branch.
+template <int NB>
+__device__ void uncut_warp(const ClusterArgs& p, const SetDev& S, int64_t e, unsigned char* ws) {
+    using L = WLay<NB>;
+    constexpr int NAD = 3 * NB, NUP = NAD * (NAD + 1) / 2;
+    const int lane = threadIdx.x & 31;
+    double* sd = reinterpret_cast<double*>(ws);
+    int32_t* si = reinterpret_cast<int32_t*>(sd + L::ND);
+    unsigned char* sb = reinterpret_cast<unsigned char*>(si + L::NI);
+    double* X = sd + L::oX;
+    double* T = sd + L::oT;
+    double* TW = sd + L::oTW;
+    double* U = sd + L::oU;
+    double* UA = sd + L::oUA;
+    double* RP = sd + L::oRP;
+    double* K = sd + L::oK;
+    double* KT = sd + L::oKT;
+    int32_t* B = si + L::iB;
+    int32_t* RB = si + L::iRB;
+    int32_t* UL = si + L::iUL;
+    uint8_t* TN = sb + L::bTN;
+    uint8_t* TC = sb + L::bTC;
+    uint16_t* SL = reinterpret_cast<uint16_t*>(sb + L::bS);
+    const bool assemble = p.mode == CM_ASSEMBLE;
+    const int nb = S.nb[e];
+    const double E = S.E[e];
+    if (lane < 24) X[lane] = S.xe[e * 24 + lane];
+    for (int i = lane; i < 8 * NB; i += 32) T[i] = S.T[e * 8 * NB + i];
+    if (lane < NB) B[lane] = S.bases[e * NB + lane];
+    if (assemble && p.vals)
+        for (int i = lane; i < NB * NB; i += 32) SL[i] = S.sidx[e * NB * NB + i];
+    __syncwarp();
+    for (int r = lane; r < NAD; r += 32) {
+        const int f = r / NB, i = r - f * NB;
+        if (assemble) RB[r] = i < nb ? p.rowptr[f * p.nu + B[i]] : 0;
+        UA[r] = (p.u && i < nb) ? p.u[f * p.nu + B[i]] : 0.0;
+    }
+    if (assemble && lane < NB) UL[lane] = lane < nb ? p.ulen[B[lane]] : 0;
+    if (lane < NB) {
+        int cnt = 0;
+        for (int a = 0; a < 8; ++a) {
+            const double t = T[a * NB + lane];
+            if (t != 0.0) {
+                TN[lane * 8 + cnt] = (uint8_t)a;
+                TW[lane * 8 + cnt] = t;
+                ++cnt;
+            }
+        }
+        TC[lane] = (uint8_t)cnt;
+    }
+    __syncwarp();
+    double jd[3];
+    for (int i = 0; i < 3; ++i) jd[i] = 0.5 * (X[6 * 3 + i] - X[0 * 3 + i]);
+    const bool skip = jd[1] * jd[0] * jd[2] < -1.0e-6;  // cl_FEM_Element_Bulk.cpp:164
+    const double cd[3] = {jd[1] * jd[2] / jd[0], jd[0] * jd[2] / jd[1], jd[0] * jd[1] / jd[2]};
+    const double lam = E * S.lam_c, mu = E * S.mu_c;
+    const double* G0 = S.g0;
+    for (int k = lane; k < kNSYM; k += 32) {
+        int r = 0, rem = k;
+        while (rem >= kNPD - r) {
+            rem -= kNPD - r;
+            ++r;
+        }
+        const int c = r + rem;
+        const int f = r / 8, a = r - f * 8, gg = c / 8, b = c - gg * 8;
+        const double cfg = f == gg ? cd[f] : jd[3 - f - gg];
+        double v = lam * cfg * __ldg(G0 + r * 24 + c) + mu * cfg * __ldg(G0 + (gg * 8 + a) * 24 + f * 8 + b);
+        if (f == gg)
+            for (int kk = 0; kk < 3; ++kk) v = fma(mu * cd[kk], __ldg(G0 + (kk * 8 + a) * 24 + kk * 8 + b), v);
+        if (skip) v = 0.0;
+        K[r * 24 + c] = v;
+        K[c * 24 + r] = v;
+    }
+    if (lane < 24) {
+        const int f = lane / 8, a = lane - f * 8;
+        double v = 0.0;
+        for (int j = 0; j < nb; ++j) {
+            const double t = T[a * NB + j];
+            if (t != 0.0) v = fma(t, UA[f * NB + j], v);
+        }
+        U[lane] = v;
+    }
+    __syncwarp();
+    const bool want_r = (assemble && p.rhs) || (!assemble && p.Rout);
+    if (want_r) {
+        if (lane < 24) {
+            double v = 0.0;
+            for (int c = 0; c < 24; ++c) v = fma(K[lane * 24 + c], U[c], v);
+            RP[lane] = v;
+        }
+        __syncwarp();
+        for (int r = lane; r < NAD; r += 32) {
+            const int f = r / NB, i = r - f * NB;
+            if (i >= nb) continue;
+            double v = 0.0;
+            for (int k = 0; k < TC[i]; ++k) v = fma(TW[i * 8 + k], RP[f * 8 + TN[i * 8 + k]], v);
+            if (assemble) atomicAdd(p.rhs + f * p.nu + B[i], v);
+            else atomicAdd(p.Rout + (e - p.first) * p.nmax + r, v);
+        }
+    }
+    const bool want_k = (assemble && p.vals) || (!assemble && p.Kout);
+    if (!want_k) {
+        __syncwarp();
+        return;
+    }
+    for (int idx = lane; idx < 24 * NAD; idx += 32) {
+        const int row = idx / NAD, c = idx - row * NAD;
+        const int gg = c / NB, j = c - gg * NB;
+        double v = 0.0;
+        const int cnt = j < nb ? TC[j] : 0;
+        for (int k = 0; k < cnt; ++k) v = fma(K[row * 24 + gg * 8 + TN[j * 8 + k]], TW[j * 8 + k], v);
+        KT[idx] = v;
+    }
+    __syncwarp();
+    bool bad = false;
+    for (int k = lane; k < NUP; k += 32) {
+        int r = 0, rem = k;
+        while (rem >= NAD - r) {
+            rem -= NAD - r;
+            ++r;
+        }
+        const int c = r + rem;
+        const int f = r / NB, i = r - f * NB, gg = c / NB, j = c - gg * NB;
+        if (i >= nb || j >= nb) continue;
+        double v = 0.0;
+        for (int kk = 0; kk < TC[i]; ++kk) v = fma(TW[i * 8 + kk], KT[(f * 8 + TN[i * 8 + kk]) * NAD + c], v);
+        bad |= !isfinite(v);
+        if (assemble) {
+            atomicAdd(p.vals + RB[r] + gg * UL[i] + SL[i * NB + j], v);
+            if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + SL[j * NB + i], v);
+        } else {
+            double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
+            atomicAdd(Ko + r + (int64_t)c * p.nmax, v);
+            if (c != r) atomicAdd(Ko + c + (int64_t)r * p.nmax, v);
+        }
+    }
+    if (bad) atomicOr(p.status, 1);
+    __syncwarp();
+}
+
 template <int NB, int W>
 __global__ void __launch_bounds__(32 * W, (384 / (32 * W)) > 0 ? 384 / (32 * W) : 1) cluster_kernel(ClusterArgs p) {
     using Lo = CL<NB>;
@@ -713,6 +866,7 @@ __global__ void __launch_bounds__(32 * W, (384 / (32 * W)) > 0 ? 384 / (32 * W) 
     double* sd = reinterpret_cast<double*>(smem);
     int32_t* si = reinterpret_cast<int32_t*>(sd + Lo::ND);
     unsigned char* sb = reinterpret_cast<unsigned char*>(si + Lo::NI);
+    // phase 1: heavy clusters (cut, interface, ghost), one per CTA
     for (;;) {
         if (threadIdx.x == 0) s_item = (long long)atomicAdd(p.counter, 1ull);
         __syncthreads();
@@ -723,6 +877,19 @@ __global__ void __launch_bounds__(32 * W, (384 / (32 * W)) > 0 ? 384 / (32 * W) 
         if (S.kind == 2) double_item<NB, W>(p, S, it, sd, si, sb);
         else bulk_item<NB, W>(p, S, it, sd, si, sb);
         __syncthreads();
+    }
+    // phase 2: uncut rectangular cells, one per warp
+    constexpr int WFIT = (int)(Lo::bytes / WLay<NB>::bytes) < W ? (int)(Lo::bytes / WLay<NB>::bytes) : W;
+    const int warp = threadIdx.x >> 5;
+    if (p.nwarp_items == 0 || warp >= WFIT) return;
+    unsigned char* ws = smem + (size_t)warp * WLay<NB>::bytes;
+    for (;;) {
+        long long idx = 0;
+        if ((threadIdx.x & 31) == 0) idx = (long long)atomicAdd(p.counter + 1, 1ull);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= p.nwarp_items) break;
+        const Item it = p.items[p.nitems + idx];
+        uncut_warp<NB>(p, p.sets[it.set], it.eq, ws);
     }
 }
 
@@ -752,7 +919,8 @@ bool pick_kernel(int nb, int warps, Kernel& k) {
 
 struct Batch {
     DeviceBuf sets, items, counter;
-    int64_t nitems = 0;
+    int64_t nitems = 0;   // CTA-phase items (the warp-phase items follow them)
+    int64_t nwarp = 0;    // uncut rectangular cells
     int nb = 0;
     int warps = 4, split = 64;
     bool built = false;
@@ -876,7 +1044,8 @@ fem_gpu_status launch(fem_gpu_ctx* c, const Kernel& k, ClusterArgs& a, cudaStrea
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int64_t blocks = (int64_t)std::max(sms, 1) * per_sm;
-    if (blocks > a.nitems) blocks = std::max<int64_t>(a.nitems, 1);
+    const int64_t work = a.nitems + (a.nwarp_items + k.threads / 32 - 1) / (k.threads / 32);
+    if (blocks > work) blocks = std::max<int64_t>(work, 1);
     void* args[] = {&a};
     e = cudaLaunchKernel(k.fn, dim3((unsigned)blocks), dim3(k.threads), args, k.smem, st);
     if (e != cudaSuccess) return cfail(c, e, "cluster launch");
@@ -908,7 +1077,7 @@ void drop_graph(Batch* b) {
 fem_gpu_status build_batch(fem_gpu_ctx* c, Batch* b) {
     cudaStream_t st = (cudaStream_t)c->stream;
     std::vector<SetDev> devs(c->sets.size());
-    std::vector<Item> items;
+    std::vector<Item> items, warp_items;
     std::vector<double> cost;
     int nb = 0;
     b->nside = 0;
@@ -923,10 +1092,17 @@ fem_gpu_status build_batch(fem_gpu_ctx* c, Batch* b) {
         nb = w;
         if (!set_dev(c, s, devs[k])) return fail(c, FEM_GPU_UNSUPPORTED, "density sets are not batched");
         if (!devs[k].gp) return fail(c, FEM_GPU_NOT_FINALIZED, "set rule tables");
+        if (s.kind == 0 && !devs[k].cut && devs[k].rect && devs[k].g0) {
+            // uncut rectangular cells: the warp phase, in mesh order
+            for (int64_t e = 0; e < s.neq; ++e) warp_items.push_back({(int32_t)k, 0, s.ngp, 0, e});
+            continue;
+        }
         add_items(s, (int)k, 0, s.neq, b->split, items, cost);
     }
     if (nb != 8 && nb != 27) return fail(c, FEM_GPU_UNSUPPORTED, "batched launch: basis width must be 8 or 27");
     std::vector<Item> ordered = lpt_order(items, cost);
+    const int64_t ncta = (int64_t)ordered.size();
+    ordered.insert(ordered.end(), warp_items.begin(), warp_items.end());
     cudaError_t e = upload(b->sets, devs, st);
     if (e == cudaSuccess) e = upload(b->items, ordered, st);
     if (e == cudaSuccess && !b->counter.p) {
@@ -935,7 +1111,8 @@ fem_gpu_status build_batch(fem_gpu_ctx* c, Batch* b) {
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cfail(c, e, "batch upload");
-    b->nitems = (int64_t)ordered.size();
+    b->nitems = ncta;
+    b->nwarp = (int64_t)warp_items.size();
     b->nb = nb;
     b->built = true;
     drop_graph(b);
@@ -950,13 +1127,14 @@ fem_gpu_status enqueue_batch(fem_gpu_ctx* c, Batch* b, const double* u, double* 
         if (vals) cudaMemsetAsync(vals, 0, c->nnz * sizeof(double), st);
         if (rhs) cudaMemsetAsync(rhs, 0, nad * sizeof(double), st);
     }
-    cudaMemsetAsync(b->counter.p, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(b->counter.p, 0, 2 * sizeof(unsigned long long), st);
     Kernel k;
     if (!pick_kernel(b->nb, b->warps, k)) return fail(c, FEM_GPU_UNSUPPORTED, "no cluster kernel instance");
     ClusterArgs a = base_args(c);
     a.sets = (const SetDev*)b->sets.p;
     a.items = (const Item*)b->items.p;
     a.nitems = b->nitems;
+    a.nwarp_items = b->nwarp;
     a.counter = (unsigned long long*)b->counter.p;
     a.u = u;
     a.vals = vals;
@@ -1080,11 +1258,11 @@ fem_gpu_status cluster_launch_set(fem_gpu_ctx* c, int set, int mode, int64_t fir
     void* dctr = nullptr;
     cudaError_t e = cudaMallocAsync(&dsets, sizeof(SetDev), st);
     if (e == cudaSuccess) e = cudaMallocAsync(&ditems, std::max<size_t>(items.size(), 1) * sizeof(Item), st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&dctr, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dctr, 2 * sizeof(unsigned long long), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dsets, &d, sizeof(SetDev), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && !items.empty())
         e = cudaMemcpyAsync(ditems, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(dctr, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dctr, 0, 2 * sizeof(unsigned long long), st);
     fem_gpu_status r = FEM_GPU_OK;
     if (e != cudaSuccess) r = cfail(c, e, "cluster staging");
     if (r == FEM_GPU_OK) {

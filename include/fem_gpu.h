@@ -47,7 +47,7 @@
 extern "C" {
 #endif
 
-#define FEM_GPU_ABI_VERSION 1
+#define FEM_GPU_ABI_VERSION 2
 
 typedef enum fem_gpu_status {
     FEM_GPU_OK = 0,
@@ -142,6 +142,10 @@ typedef struct fem_gpu_bulk_set_desc {
        property (EXA/optimization/SIMP/SIMP.cpp:43-51).  NULL = constant E. */
     const double* node_density;
     double density_exponent;
+    /* optional, cut clusters: IG vertex id of every integration-cell vertex
+       ([ig][nodes]; ids into the table of fem_gpu_set_ig_vertices) -- needed
+       for the shape sensitivities only */
+    const int32_t* ig_vertex_ids;
 } fem_gpu_bulk_set_desc;
 
 /* Side set on interpolation-cell facets (trivial side clusters):
@@ -192,6 +196,7 @@ typedef struct fem_gpu_double_side_set_desc {
     const double* follower_youngs_modulus; /* [num_clusters] */
     double poisson_ratio;
     double alpha;                 /* Nitsche interface or ghost penalty parameter */
+    const int32_t* facet_vertex_ids;       /* optional [facets][vertices], as ig_vertex_ids */
 } fem_gpu_double_side_set_desc;
 
 typedef struct fem_gpu_pcg_opts {
@@ -344,6 +349,56 @@ fem_gpu_status fem_gpu_pcg_snapshots(fem_gpu_ctx* ctx, const int32_t* rowptr, co
                                      const double* vals, const double* b, double* x, const fem_gpu_pcg_opts* opts,
                                      fem_gpu_pcg_report* report, int32_t every, double* snaps, int32_t max_snaps,
                                      int32_t* n_snaps);
+
+/* ---- shape sensitivities (adjoint) ---------------------------------------
+   The integration mesh of the cut clusters and interface facets as a table of
+   IG vertices (the fem_xtk_get_vertices layout): kind 0 background node
+   (parents[0] = node), 1 face centre (parents[0..3]), 2 cell centre
+   (parents[0..7]), 3 intersection on the IG edge parents[0] -> parents[1]
+   (IG vertex ids) at edge coordinate t: x = x_p0 + t (x_p1 - x_p0).  The
+   design variables of the path are the level-set coefficients p; the
+   intersection coordinates t carry all the dependence (GEN's
+   Intersection_Node_Linear, GEN/src/PDV/cl_GEN_Intersection_Node_Linear.cpp:
+   46-57, and Intersection_Node_Level_Set::append_dcoordinate_dadv,
+   cl_GEN_Intersection_Node_Level_Set.cpp:43-100).  Host arrays. */
+fem_gpu_status fem_gpu_set_ig_vertices(fem_gpu_ctx* ctx, int64_t num_vertices, const int32_t* kind,
+                                       const int32_t* parents, const double* coords, const double* value);
+/* new edge coordinates t of the intersection vertices (same topology):
+   rewrites the coordinates and IP-parametric coordinates of every cut
+   cluster's integration cells and every interface facet (rectangular IP
+   cells), on the host and the device.  t: host [num_vertices] (entries of
+   other kinds are ignored). */
+fem_gpu_status fem_gpu_update_ig_vertices(fem_gpu_ctx* ctx, const double* t);
+/* strain energy of the bulk sets, Q = sum 1/2 w* flux . strain
+   (IQI_Strain_Energy::compute_QI, FEM/INT/src/IQI/cl_FEM_IQI_Strain_Energy.cpp:
+   40-120), and dQ/du = K_bulk u (device buffers; q: host scalar) */
+fem_gpu_status fem_gpu_strain_energy(fem_gpu_ctx* ctx, const double* u, double* dqdu, double* q);
+/* adjoint shape sensitivity at the intersection vertices:
+   G[v] = d/dt_v ( Q(u, t) - lambda^T R(u, t) ) for the cut clusters (bulk
+   strain energy and residual) and the interface clusters (residual and the
+   SP_Nitsche_Interface cluster measures), exact (forward-mode dual numbers
+   over each integration cell's / facet's vertices).  With K^T lambda = dQ/du
+   this is dQ/dt (Interpolation_Element::compute_dQIdp_explicit_implicit,
+   FEM/INT/src/ELEM/cl_FEM_Interpolation_Element.cpp:820-948; the reference
+   differentiates the residual by finite differences of the IG vertex
+   coordinates, cl_FEM_IWG.cpp:2997-3154).  u, lambda: device adof vectors;
+   G: device [num_vertices], overwritten. */
+fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* ctx, const double* u, const double* lambda, double* G);
+/* chain to the level-set coefficients: dqdp[j] = sum_v G[v] dt_v/dp_j with
+   t = phi_0 / (phi_0 - phi_1) on the parents' level set, derived parents the
+   mean of their background nodes, phi at a background node = sum_j
+   tmat[node][k] p_(cols[node][k]) (width entries per node, e.g. the cubic
+   B-spline field of fem_gen_bspline_tmatrix).  G, dqdp: device; cols, tmat:
+   host [num_background_nodes][width]; dqdp overwritten. */
+fem_gpu_status fem_gen_dqdp(fem_gpu_ctx* ctx, const double* G, int64_t num_background_nodes, int32_t width,
+                            const int32_t* cols, const double* tmat, int64_t num_coefs, double* dqdp);
+/* tensor-product B-spline field of `order` on a uniform grid of
+   num_coefs[d] = n_d + order coefficients over [0, lengths[d]] (HMR
+   numbering, i fastest; BSpline_Field::get_dfield_dadvs,
+   GEN/src/ADV/fields/cl_GEN_BSpline_Field.cpp:165): the (order+1)^3 basis
+   values and coefficient ids at each point.  cols, vals: [num_points][(order+1)^3]. */
+fem_gpu_status fem_gen_bspline_tmatrix(const int32_t* num_coefs, const double* lengths, int32_t order,
+                                       int64_t num_points, const double* points, int32_t* cols, double* vals);
 
 /* ---- learned coarse-grid correction (config 5) ---------------------------
    A 4-layer 3D convolution net (4 -> 32 -> 32 -> 32 -> 3 channels, 3x3x3,

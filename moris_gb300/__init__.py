@@ -59,6 +59,21 @@ def device_count():
     return lib().fem_gpu_device_count()
 
 
+def bspline_tmatrix(num_coefs, lengths, order, points):
+    """(cols, vals) [n_points][(order+1)^3] of a uniform tensor B-spline field."""
+    nc = np.ascontiguousarray(num_coefs, dtype=np.int32)
+    ln = np.ascontiguousarray(lengths, dtype=np.float64)
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    w = (order + 1) ** 3
+    cols = np.zeros((len(pts), w), dtype=np.int32)
+    vals = np.zeros((len(pts), w))
+    st = lib().fem_gen_bspline_tmatrix(_np_ptr(nc), _np_ptr(ln), order, len(pts), _np_ptr(pts), _np_ptr(cols),
+                                       _np_ptr(vals))
+    if st:
+        raise FemGpuError(st, "fem_gen_bspline_tmatrix")
+    return cols, vals
+
+
 def probe_fp64_tflops(iters=20000):
     """Measured FP64 FMA throughput of the current GPU (TFLOP/s)."""
     t = C.c_double()
@@ -137,7 +152,7 @@ class FemModel:
         self._check(self.L.fem_gpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
 
     def add_bulk_set(self, ip_cells, youngs, poisson, rule, model, ig_cell=None, ig_offsets=None, ig_coords=None,
-                     ig_param=None, node_density=None, density_exponent=3.0):
+                     ig_param=None, node_density=None, density_exponent=3.0, ig_vertex_ids=None):
         ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)
         rho = None if node_density is None else np.ascontiguousarray(node_density, dtype=np.float64)
         E = np.ascontiguousarray(youngs, dtype=np.float64)
@@ -146,8 +161,9 @@ class FemModel:
         xp = None if ig_param is None else np.ascontiguousarray(ig_param, dtype=np.float64)
         if ig_cell is None:
             ig_cell = CELL_QUAD4 if self.dim == 2 else CELL_HEX8
+        vid = None if ig_vertex_ids is None else np.ascontiguousarray(ig_vertex_ids, dtype=np.int32)
         d = BulkSetDesc(IWG_STRUC_LINEAR_BULK, ig_cell, rule, model, len(ipc), _np_ptr(ipc), _np_ptr(off),
-                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson, _np_ptr(rho), density_exponent)
+                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson, _np_ptr(rho), density_exponent, _np_ptr(vid))
         idx = C.c_int32()
         self._check(self.L.fem_gpu_add_bulk_set(self.h, C.byref(d), C.byref(idx)), "add_bulk_set")
         self.num_sets += 1
@@ -165,7 +181,8 @@ class FemModel:
         return idx.value
 
     def add_double_side_set(self, iwg, leader, follower, facet_offsets, facet_coords, leader_param, follower_param,
-                            leader_youngs, follower_youngs, poisson, rule, facet_cell, alpha, model=MODEL_3D):
+                            leader_youngs, follower_youngs, poisson, rule, facet_cell, alpha, model=MODEL_3D,
+                            facet_vertex_ids=None):
         """Interface (Nitsche) or ghost clusters: facets given by vertex coords and
         their parametric coords in the leader / follower IP cells."""
         L_ = np.ascontiguousarray(leader, dtype=np.int32)
@@ -176,8 +193,10 @@ class FemModel:
         ff = np.ascontiguousarray(follower_param, dtype=np.float64)
         EL = np.ascontiguousarray(leader_youngs, dtype=np.float64)
         EF = np.ascontiguousarray(follower_youngs, dtype=np.float64)
+        vid = None if facet_vertex_ids is None else np.ascontiguousarray(facet_vertex_ids, dtype=np.int32)
         d = DoubleSideSetDesc(iwg, facet_cell, rule, model, len(L_), _np_ptr(L_), _np_ptr(F_), _np_ptr(off),
-                              _np_ptr(fx), _np_ptr(fl), _np_ptr(ff), _np_ptr(EL), _np_ptr(EF), poisson, alpha)
+                              _np_ptr(fx), _np_ptr(fl), _np_ptr(ff), _np_ptr(EL), _np_ptr(EF), poisson, alpha,
+                              _np_ptr(vid))
         idx = C.c_int32()
         self._check(self.L.fem_gpu_add_double_side_set(self.h, C.byref(d), C.byref(idx)), "add_double_side_set")
         self.num_sets += 1
@@ -188,6 +207,33 @@ class FemModel:
         (device tensors)."""
         self._check(self.L.fem_gpu_assemble_batched(self.h, _dev_ptr(u), _dev_ptr(vals), _dev_ptr(rhs), flags),
                     "assemble_batched")
+
+    # ---- shape sensitivities -------------------------------------------------
+    def set_ig_vertices(self, kind, parents, coords, value):
+        k = np.ascontiguousarray(kind, dtype=np.int32)
+        p = np.ascontiguousarray(parents, dtype=np.int32)
+        x = np.ascontiguousarray(coords, dtype=np.float64)
+        v = np.ascontiguousarray(value, dtype=np.float64)
+        self._check(self.L.fem_gpu_set_ig_vertices(self.h, len(k), _np_ptr(k), _np_ptr(p), _np_ptr(x), _np_ptr(v)),
+                    "set_ig_vertices")
+
+    def update_ig_vertices(self, t):
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        self._check(self.L.fem_gpu_update_ig_vertices(self.h, _np_ptr(t)), "update_ig_vertices")
+
+    def strain_energy(self, u, dqdu):
+        q = C.c_double()
+        self._check(self.L.fem_gpu_strain_energy(self.h, _dev_ptr(u), _dev_ptr(dqdu), C.byref(q)), "strain_energy")
+        return q.value
+
+    def drdp_adjoint(self, u, lam, G):
+        self._check(self.L.fem_gpu_drdp_adjoint(self.h, _dev_ptr(u), _dev_ptr(lam), _dev_ptr(G)), "drdp_adjoint")
+
+    def gen_dqdp(self, G, cols, tmat, num_coefs, dqdp):
+        cols = np.ascontiguousarray(cols, dtype=np.int32)
+        tmat = np.ascontiguousarray(tmat, dtype=np.float64)
+        self._check(self.L.fem_gen_dqdp(self.h, _dev_ptr(G), cols.shape[0], cols.shape[1], _np_ptr(cols),
+                                        _np_ptr(tmat), num_coefs, _dev_ptr(dqdp)), "gen_dqdp")
 
     def check_status(self):
         self._check(self.L.fem_gpu_check_status(self.h), "check_status")

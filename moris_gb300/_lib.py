@@ -27,7 +27,7 @@ class BulkSetDesc(C.Structure):
     _fields_ = [("iwg_type", I32), ("ig_cell_type", I32), ("integration_rule", I32), ("model_type", I32),
                 ("num_clusters", I64), ("cluster_ip_cell", P), ("ig_offsets", P), ("ig_coords", P),
                 ("ig_param_coords", P), ("youngs_modulus", P), ("poisson_ratio", D), ("node_density", P),
-                ("density_exponent", D)]
+                ("density_exponent", D), ("ig_vertex_ids", P)]
 
 
 class SideSetDesc(C.Structure):
@@ -40,7 +40,8 @@ class DoubleSideSetDesc(C.Structure):
     _fields_ = [("iwg_type", I32), ("facet_cell_type", I32), ("integration_rule", I32), ("model_type", I32),
                 ("num_clusters", I64), ("leader_ip_cell", P), ("follower_ip_cell", P), ("facet_offsets", P),
                 ("facet_coords", P), ("leader_param_coords", P), ("follower_param_coords", P),
-                ("leader_youngs_modulus", P), ("follower_youngs_modulus", P), ("poisson_ratio", D), ("alpha", D)]
+                ("leader_youngs_modulus", P), ("follower_youngs_modulus", P), ("poisson_ratio", D), ("alpha", D),
+                ("facet_vertex_ids", P)]
 
 
 class XtkSizes(C.Structure):
@@ -86,6 +87,12 @@ SIGNATURES = {
     "fem_xtk_get_ghost": (I32, [P, I32, P, P, P, P, P]),
     "fem_xtk_get_vertices": (I32, [P, P, P, P, P]),
     "fem_xtk_free": (None, [P]),
+    "fem_gpu_set_ig_vertices": (I32, [P, I64, P, P, P, P]),
+    "fem_gpu_update_ig_vertices": (I32, [P, P]),
+    "fem_gpu_strain_energy": (I32, [P, P, P, P]),
+    "fem_gpu_drdp_adjoint": (I32, [P, P, P, P]),
+    "fem_gen_dqdp": (I32, [P, P, I64, I32, P, P, I64, P]),
+    "fem_gen_bspline_tmatrix": (I32, [P, P, I32, I64, P, P, P]),
     "fem_gpu_finalize": (I32, [P]),
     "fem_gpu_finalize_host": (I32, [P]),
     "fem_gpu_get_sizes": (I32, [P, P, P, P]),

@@ -920,6 +920,15 @@ fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
 
 namespace fem {
 
+fem_gpu_status assemble_set(fem_gpu_ctx* c, int set, const double* u, double* vals, double* rhs) {
+    SetData& s = c->sets[set];
+    if (cluster_set(c, set))
+        return cluster_launch_set(c, set, MODE_ASSEMBLE, 0, s.neq, u, vals, rhs, nullptr, nullptr, 0);
+    if (s.kind == 0)
+        return launch_bulk(c, set, MODE_ASSEMBLE, 0, s.neq, u, vals, rhs, nullptr, nullptr, 0, nullptr, nullptr);
+    return launch_side(c, set, MODE_ASSEMBLE, 0, s.neq, u, vals, rhs, nullptr, nullptr, 0);
+}
+
 // a side set launched on a given stream (the batched graph captures it)
 fem_gpu_status side_launch_on(fem_gpu_ctx* c, int set, const double* u, double* vals, double* rhs, cudaStream_t st) {
     void* keep = c->stream;
@@ -931,6 +940,7 @@ fem_gpu_status side_launch_on(fem_gpu_ctx* c, int set, const double* u, double* 
 
 void device_release(fem_gpu_ctx* c) {
     cluster_release(c);
+    sensitivity_release(c);
     for (auto& s : c->sets) {
         dfree(s.d_nb);
         dfree(s.d_bases);

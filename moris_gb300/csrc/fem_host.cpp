@@ -183,6 +183,45 @@ fem_gpu_status fem_hmr_uniform_mesh(int32_t dim, const int32_t* ne_in, const dou
     return FEM_GPU_OK;
 }
 
+/* Tensor-product B-spline field on a uniform grid (the GEN B-spline level
+   set): basis values at arbitrary points, HMR element / basis numbering. */
+fem_gpu_status fem_gen_bspline_tmatrix(const int32_t* num_coefs, const double* len, int32_t p, int64_t np,
+                                       const double* pts, int32_t* cols, double* vals) {
+    if (!num_coefs || !len || !pts || !cols || !vals || p < 1 || p > 3 || np < 0) return FEM_GPU_BAD_ARG;
+    int64_t ne[3], nb[3];
+    for (int d = 0; d < 3; ++d) {
+        nb[d] = num_coefs[d];
+        ne[d] = nb[d] - p;
+        if (ne[d] < 1 || !(len[d] > 0.0)) return FEM_GPU_BAD_ARG;
+    }
+    const int pp = p + 1, w = pp * pp * pp;
+    for (int64_t k = 0; k < np; ++k) {
+        int64_t el[3];
+        double b[3][4];
+        for (int d = 0; d < 3; ++d) {
+            const double x = pts[k * 3 + d] / len[d] * (double)ne[d];
+            if (!std::isfinite(x)) return FEM_GPU_NONFINITE;
+            int64_t e = (int64_t)std::floor(x);
+            e = std::min<int64_t>(std::max<int64_t>(e, 0), ne[d] - 1);
+            const double xi = 2.0 * (x - (double)e) - 1.0;  // element coordinate in [-1, 1]
+            el[d] = e;
+            for (int j = 0; j < pp; ++j) {
+                // the right end of the last element belongs to it (half-open intervals otherwise)
+                const double xe = (xi >= 1.0 && e == ne[d] - 1) ? 1.0 - 1e-15 : xi;
+                b[d][j] = bspline_value(p, j, xe);
+            }
+        }
+        int q = 0;
+        for (int l2 = 0; l2 < pp; ++l2)
+            for (int l1 = 0; l1 < pp; ++l1)
+                for (int l0 = 0; l0 < pp; ++l0, ++q) {
+                    cols[k * w + q] = (int32_t)((el[0] + l0) + nb[0] * ((el[1] + l1) + nb[1] * (el[2] + l2)));
+                    vals[k * w + q] = b[0][l0] * b[1][l1] * b[2][l2];
+                }
+    }
+    return FEM_GPU_OK;
+}
+
 fem_gpu_status fem_hmr_mesh_sizes(const fem_hmr_mesh* m, int64_t* nn, int64_t* nc, int64_t* nb, int64_t* nz) {
     if (!m || !nn || !nc || !nb || !nz) return FEM_GPU_BAD_ARG;
     const int npe = m->dim == 2 ? 4 : 8;
@@ -306,6 +345,13 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
         const int64_t per = (int64_t)cell_num_nodes(igc) * c->dim;
         s.ig_coords.assign(d->ig_coords, d->ig_coords + nig * per);
         s.ig_param.assign(d->ig_param_coords, d->ig_param_coords + nig * per);
+        if (s.ig_off[0] != 0) return fail(c, FEM_GPU_BAD_ARG, "integration cell offsets must start at 0");
+        for (int64_t i = 0; i < s.neq; ++i)
+            if (s.ig_off[i + 1] < s.ig_off[i]) return fail(c, FEM_GPU_BAD_ARG, "integration cell offsets");
+        for (int64_t k = 0; k < nig * per; ++k)
+            if (!std::isfinite(s.ig_coords[k]) || !std::isfinite(s.ig_param[k]))
+                return fail(c, FEM_GPU_NONFINITE, "integration cell coordinates");
+        if (d->ig_vertex_ids) s.vid.assign(d->ig_vertex_ids, d->ig_vertex_ids + nig * cell_num_nodes(igc));
     }
     if (d->node_density) {
         if (!std::isfinite(d->density_exponent)) return fail(c, FEM_GPU_BAD_ARG, "density exponent");
@@ -319,6 +365,7 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     s.bulk.ig_coords = nullptr;
     s.bulk.ig_param_coords = nullptr;
     s.bulk.youngs_modulus = nullptr;
+    s.bulk.ig_vertex_ids = nullptr;
     c->sets.push_back(std::move(s));
     if (idx) *idx = (int32_t)c->sets.size() - 1;
     return FEM_GPU_OK;
@@ -400,6 +447,7 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
             return fail(c, FEM_GPU_NONFINITE, "facet coordinates");
     s.E.assign(d->leader_youngs_modulus, d->leader_youngs_modulus + s.neq);
     s.EF.assign(d->follower_youngs_modulus, d->follower_youngs_modulus + s.neq);
+    if (d->facet_vertex_ids) s.vid.assign(d->facet_vertex_ids, d->facet_vertex_ids + s.fc_off[s.neq] * s.nfv);
     for (int64_t i = 0; i < s.neq; ++i)
         if (!(s.E[i] > 0.0) || !(s.EF[i] > 0.0) || !std::isfinite(s.E[i]) || !std::isfinite(s.EF[i]))
             return fail(c, FEM_GPU_NONFINITE, "youngs modulus must be finite and > 0");
@@ -407,6 +455,7 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
     s.dside.facet_offsets = nullptr;
     s.dside.facet_coords = s.dside.leader_param_coords = s.dside.follower_param_coords = nullptr;
     s.dside.leader_youngs_modulus = s.dside.follower_youngs_modulus = nullptr;
+    s.dside.facet_vertex_ids = nullptr;
     c->sets.push_back(std::move(s));
     if (idx) *idx = (int32_t)c->sets.size() - 1;
     return FEM_GPU_OK;
@@ -432,6 +481,55 @@ double ip_cell_measure(const fem_gpu_ctx* c, int64_t cell) {
         vol += r.w[q] * det;
     }
     return vol;
+}
+
+fem_gpu_status interface_volumes(fem_gpu_ctx* c) {
+    const int dim = c->dim;
+    // cluster volumes per IP cell (bulk clusters), for the interface parameter
+    std::vector<double> cell_vol;
+    bool need_vol = false;
+    for (auto& s : c->sets)
+        need_vol |= s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
+    if (need_vol) {
+        cell_vol.assign(c->num_cells, 0.0);
+        for (auto& s : c->sets) {
+            if (s.kind != 0) continue;
+            for (int64_t i = 0; i < s.neq; ++i) {
+                double v = 0.0;
+                if (s.ig_off.empty()) {
+                    v = ip_cell_measure(c, s.ip_cell[i]);
+                } else {
+                    const int ign = cell_num_nodes(s.bulk.ig_cell_type);
+                    for (int64_t g = s.ig_off[i]; g < s.ig_off[i + 1]; ++g) {
+                        const double* x = &s.ig_coords[(size_t)g * ign * dim];
+                        if (s.bulk.ig_cell_type == FEM_GPU_CELL_TET4) {
+                            double a[3], b[3], cc[3];
+                            for (int k = 0; k < 3; ++k) {
+                                a[k] = x[0 * 3 + k] - x[2 * 3 + k];
+                                b[k] = x[1 * 3 + k] - x[2 * 3 + k];
+                                cc[k] = x[3 * 3 + k] - x[2 * 3 + k];
+                            }
+                            v += std::abs(a[0] * (b[1] * cc[2] - b[2] * cc[1]) - a[1] * (b[0] * cc[2] - b[2] * cc[0]) +
+                                          a[2] * (b[0] * cc[1] - b[1] * cc[0])) /
+                                 6.0;
+                        }
+                    }
+                }
+                cell_vol[s.ip_cell[i]] += v;
+            }
+        }
+    }
+    for (auto& s : c->sets) {
+        if (s.kind != 2 || s.dside.iwg_type == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST) continue;
+        s.vol.resize(s.neq * 2);
+        for (int64_t i = 0; i < s.neq; ++i) {
+            s.vol[i * 2] = cell_vol[s.ip_cell[i]];
+            s.vol[i * 2 + 1] = cell_vol[s.fcell[i]];
+            if (!(s.vol[i * 2] > 0.0) || !(s.vol[i * 2 + 1] > 0.0))
+                return fail(c, FEM_GPU_BAD_ARG, "interface cluster without bulk clusters on its cells");
+        }
+    }
+    return FEM_GPU_OK;
 }
 }  // namespace fem
 
@@ -564,40 +662,6 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
         }
     c->rowptr[nad] = (int32_t)acc;
     c->nnz = acc;
-    // cluster volumes per IP cell (bulk clusters), for the interface parameter
-    std::vector<double> cell_vol;
-    bool need_vol = false;
-    for (auto& s : c->sets)
-        need_vol |= s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
-    if (need_vol) {
-        cell_vol.assign(c->num_cells, 0.0);
-        for (auto& s : c->sets) {
-            if (s.kind != 0) continue;
-            for (int64_t i = 0; i < s.neq; ++i) {
-                double v = 0.0;
-                if (s.ig_off.empty()) {
-                    v = ip_cell_measure(c, s.ip_cell[i]);
-                } else {
-                    const int ign = cell_num_nodes(s.bulk.ig_cell_type);
-                    for (int64_t g = s.ig_off[i]; g < s.ig_off[i + 1]; ++g) {
-                        const double* x = &s.ig_coords[(size_t)g * ign * dim];
-                        if (s.bulk.ig_cell_type == FEM_GPU_CELL_TET4) {
-                            double a[3], b[3], cc[3];
-                            for (int k = 0; k < 3; ++k) {
-                                a[k] = x[0 * 3 + k] - x[2 * 3 + k];
-                                b[k] = x[1 * 3 + k] - x[2 * 3 + k];
-                                cc[k] = x[3 * 3 + k] - x[2 * 3 + k];
-                            }
-                            v += std::abs(a[0] * (b[1] * cc[2] - b[2] * cc[1]) - a[1] * (b[0] * cc[2] - b[2] * cc[0]) +
-                                          a[2] * (b[0] * cc[1] - b[1] * cc[0])) /
-                                 6.0;
-                        }
-                    }
-                }
-                cell_vol[s.ip_cell[i]] += v;
-            }
-        }
-    }
     // per set element data
     for (auto& s : c->sets) {
         if (s.kind == 2) {
@@ -612,15 +676,7 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
             s.T.assign(s.neq * 2 * npe * maxnb, 0.0);
             s.sidx.assign(s.neq * W2 * W2, 0);
             s.xe.resize(s.neq * 2 * npe * dim);
-            if (need_vol && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST) {
-                s.vol.resize(s.neq * 2);
-                for (int64_t i = 0; i < s.neq; ++i) {
-                    s.vol[i * 2] = cell_vol[s.ip_cell[i]];
-                    s.vol[i * 2 + 1] = cell_vol[s.fcell[i]];
-                    if (!(s.vol[i * 2] > 0.0) || !(s.vol[i * 2 + 1] > 0.0))
-                        return fail(c, FEM_GPU_BAD_ARG, "interface cluster without bulk clusters on its cells");
-                }
-            }
+
             std::atomic<bool> bad{false};
             parallel_for(s.neq, [&](int64_t i) {
                 int32_t all[512];
@@ -698,6 +754,8 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
         });
         if (bad) return fail(c, FEM_GPU_UNSUPPORTED, "scatter slot does not fit 16 bits");
     }
+    fem_gpu_status vst = interface_volumes(c);
+    if (vst != FEM_GPU_OK) return vst;
     c->host_final = true;
     return FEM_GPU_OK;
 }

@@ -49,6 +49,10 @@ struct SetData {
     std::vector<double> EF;                      // follower modulus
     std::vector<double> vol;                     // [neq][2] leader / follower cluster volumes
     int nfv = 0;                                 // facet vertices
+    std::vector<int32_t> vid;                    // IG vertex ids: cut bulk [ig][4], double [facet][nfv]
+    DeviceBuf d_vid;
+    std::vector<int32_t> link;                   // interface: [neq][4] leader (set, eq), follower (set, eq)
+    DeviceBuf d_link;
     // finalize products (double-sided sets: two sides per equation object,
     // nb [neq][2], bases [neq][2][maxnb], T [neq][2][npe][maxnb],
     // xe [neq][2][npe][dim], sidx [neq][2 maxnb][2 maxnb])
@@ -102,6 +106,10 @@ struct fem_gpu_ctx {
     bool stream_set = false;           // caller chose a stream (NULL = legacy default stream)
     fem::DeviceBuf d_rowptr, d_ulen, d_tables, d_scratch, d_status;
     void* batch = nullptr;             // batched-launch state (fem_cluster.cu)
+    // IG vertex table (shape sensitivities)
+    std::vector<int32_t> vkind, vpar;  // [nv], [nv][8]
+    std::vector<double> vx, vval;      // [nv][3], [nv]
+    fem::DeviceBuf d_vkind, d_vpar, d_vx;
     int64_t launches = 0;
     std::string err;
 };
@@ -119,4 +127,10 @@ fem_gpu_status cluster_launch_set(fem_gpu_ctx* c, int set, int mode, int64_t fir
                                   double* vals, double* rhs, double* Kout, double* Rout, int nmax);
 // measure of an IP cell (sum of w detJ over the 2^d Gauss rule)
 double ip_cell_measure(const fem_gpu_ctx* c, int64_t cell);
+// leader / follower cluster volumes of the interface sets (finalize and geometry updates)
+fem_gpu_status interface_volumes(fem_gpu_ctx* c);
+// one set's assembly through its kernel (fem_device.cu); vals / rhs may be NULL
+fem_gpu_status assemble_set(fem_gpu_ctx* c, int set, const double* u, double* vals, double* rhs);
+// device memory of the sensitivity path (fem_sensitivity.cu)
+void sensitivity_release(fem_gpu_ctx* c);
 }  // namespace fem

@@ -1,0 +1,781 @@
+// fem_sensitivity.cu -- shape sensitivities of the strain energy through the
+// level-set coefficients (adjoint method).
+//
+//   dQ/dp = sum_v G[v] dt_v/dp,   G[v] = d/dt_v ( Q(u, t) - lambda^T R(u, t) ),
+//   K^T lambda = dQ/du,
+//
+// where t_v is the edge coordinate of intersection vertex v
+// (x_v = x_p0 + t_v (x_p1 - x_p0)).  The reference assembles dR/dp by finite
+// differences of the IG vertex coordinates (IWG::select_dRdp_FD_geometry_bulk,
+// FEM/INT/src/IWG/cl_FEM_IWG.cpp:2997-3154, plus the cluster-measure terms
+// :3827-3924) and contracts with the adjoint in Interpolation_Element::
+// compute_dQIdp_explicit_implicit (FEM/INT/src/ELEM/cl_FEM_Interpolation_
+// Element.cpp:820-948).  Here the derivative is exact: every integration
+// cell (TET4) and interface facet (TRI3) is evaluated once in forward-mode
+// dual arithmetic with one derivative slot per vertex, and the contraction
+// with u and lambda happens inside the kernel:
+//
+//   tet     F = sum_q w detJ (1/2 sigma(u):eps(u) - sigma(u):eps(lambda))
+//   facet   -lambda^T R_interface = -( w_L A + w_F B + gamma C ),
+//           A = sum_q w* (-[lambda].t_L(u) + beta t_L(lambda).[u]),  B likewise
+//           with t_F, C = sum_q w* [lambda].[u]  (IWG_Isotropic_Struc_Linear_
+//           Interface residual contracted with lambda), and the SP_Nitsche_
+//           Interface weights / gamma differentiated through the cluster
+//           volumes (the cut clusters' tets) and the interface measure.
+// Rectangular IP cells: xi = -1 + 2 (x - X0) / (X6 - X0).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fem_internal.hpp"
+
+namespace fem {
+namespace {
+
+template <int M>
+struct Dual {
+    double v;
+    double d[M];
+    __device__ Dual() {}
+    __device__ explicit Dual(double x) : v(x) {
+        for (int i = 0; i < M; ++i) d[i] = 0.0;
+    }
+};
+template <int M>
+__device__ __forceinline__ Dual<M> operator+(const Dual<M>& a, const Dual<M>& b) {
+    Dual<M> r;
+    r.v = a.v + b.v;
+    for (int i = 0; i < M; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+template <int M>
+__device__ __forceinline__ Dual<M> operator-(const Dual<M>& a, const Dual<M>& b) {
+    Dual<M> r;
+    r.v = a.v - b.v;
+    for (int i = 0; i < M; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+template <int M>
+__device__ __forceinline__ Dual<M> operator*(const Dual<M>& a, const Dual<M>& b) {
+    Dual<M> r;
+    r.v = a.v * b.v;
+    for (int i = 0; i < M; ++i) r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
+    return r;
+}
+template <int M>
+__device__ __forceinline__ Dual<M> operator*(double s, const Dual<M>& a) {
+    Dual<M> r;
+    r.v = s * a.v;
+    for (int i = 0; i < M; ++i) r.d[i] = s * a.d[i];
+    return r;
+}
+template <int M>
+__device__ __forceinline__ Dual<M> operator+(double s, const Dual<M>& a) {
+    Dual<M> r = a;
+    r.v += s;
+    return r;
+}
+template <int M>
+__device__ __forceinline__ Dual<M> dsqrt(const Dual<M>& a) {
+    Dual<M> r;
+    r.v = sqrt(a.v);
+    const double h = a.v > 0.0 ? 0.5 / r.v : 0.0;
+    for (int i = 0; i < M; ++i) r.d[i] = h * a.d[i];
+    return r;
+}
+template <int M>
+__device__ __forceinline__ Dual<M> dinv(const Dual<M>& a) {
+    Dual<M> r;
+    r.v = 1.0 / a.v;
+    const double h = -r.v * r.v;
+    for (int i = 0; i < M; ++i) r.d[i] = h * a.d[i];
+    return r;
+}
+// a += s * b (s constant)
+template <int M>
+__device__ __forceinline__ void axpy(double s, const Dual<M>& b, Dual<M>& a) {
+    a.v = fma(s, b.v, a.v);
+    for (int i = 0; i < M; ++i) a.d[i] = fma(s, b.d[i], a.d[i]);
+}
+
+// gradients of a field (nodal values f[fld*8 + a]) at an IP point of a rectangular HEX8
+// cell: grad[fld][i] = sum_a f dN_a/dxi_i / jd_i; val[fld] = sum_a f N_a
+template <int M>
+__device__ void hex_field(const Dual<M>* xi, const double* jd, const double* f, Dual<M> val[3], Dual<M> grad[3][3]) {
+    for (int fl = 0; fl < 3; ++fl) {
+        val[fl] = Dual<M>(0.0);
+        for (int i = 0; i < 3; ++i) grad[fl][i] = Dual<M>(0.0);
+    }
+    for (int a = 0; a < 8; ++a) {
+        const double sx = ((a & 3) == 1 || (a & 3) == 2) ? 1.0 : -1.0;
+        const double sy = ((a & 3) >= 2) ? 1.0 : -1.0;
+        const double sz = a >= 4 ? 1.0 : -1.0;
+        const Dual<M> fx = 1.0 + sx * xi[0], fy = 1.0 + sy * xi[1], fz = 1.0 + sz * xi[2];
+        const Dual<M> fyz = fy * fz, fxz = fx * fz, fxy = fx * fy;
+        const Dual<M> N = 0.125 * (fx * fyz);
+        const double c0 = 0.125 * sx / jd[0], c1 = 0.125 * sy / jd[1], c2 = 0.125 * sz / jd[2];
+        for (int fl = 0; fl < 3; ++fl) {
+            const double fv = f[fl * 8 + a];
+            if (fv == 0.0) continue;
+            axpy(fv, N, val[fl]);
+            axpy(fv * c0, fyz, grad[fl][0]);
+            axpy(fv * c1, fxz, grad[fl][1]);
+            axpy(fv * c2, fxy, grad[fl][2]);
+        }
+    }
+}
+
+// sigma = lam tr(G) I + mu (G + G^T) of a displacement gradient G[f][i] = du_f/dx_i
+template <int M>
+__device__ void stress(const Dual<M> G[3][3], double lam, double mu, Dual<M> S[3][3]) {
+    const Dual<M> tr = G[0][0] + G[1][1] + G[2][2];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            S[i][j] = mu * (G[i][j] + G[j][i]);
+            if (i == j) axpy(lam, tr, S[i][j]);
+        }
+}
+
+struct AdjArgs {
+    // vertex table
+    const int32_t* vkind;
+    const int32_t* vpar;  // [nv][8]
+    const double* vx;     // [nv][3]
+    double* G;            // [nv]
+    // adof vectors
+    const double* u;
+    const double* lam;
+    int64_t nu;
+};
+
+struct CutSetDev {
+    int64_t neq;
+    const double* xe;      // [neq][8][3]
+    const double* E;
+    const int32_t* nb;
+    const int32_t* bases;  // [neq][W]
+    const double* T;       // [neq][8][W]
+    int W;
+    double lam_c, mu_c;
+    const int64_t* ig_off;
+    const int32_t* vid;    // [ig][4]
+    const double* gp;      // TET rule points [ngp][3]
+    const double* gw;
+    int ngp;
+};
+
+__device__ void pdof_values(const double* T, const int32_t* bases, int nb, int W, const double* ua, int64_t nu,
+                            double* out /*[24]*/, int tid, int nt) {
+    for (int r = tid; r < 24; r += nt) {
+        const int f = r / 8, a = r % 8;
+        double v = 0.0;
+        if (ua)
+            for (int j = 0; j < nb; ++j) {
+                const double t = T[a * W + j];
+                if (t != 0.0) v = fma(t, ua[f * nu + bases[j]], v);
+            }
+        out[r] = v;
+    }
+}
+
+// vertex position as a dual in slot `slot` (intersection vertices move with t)
+template <int M>
+__device__ void vertex_dual(const AdjArgs& A, int32_t v, int slot, Dual<M> x[3], bool& moving) {
+    moving = A.vkind[v] == 3;
+    for (int d = 0; d < 3; ++d) {
+        x[d] = Dual<M>(A.vx[(int64_t)v * 3 + d]);
+        if (moving) {
+            const int32_t p0 = A.vpar[(int64_t)v * 8], p1 = A.vpar[(int64_t)v * 8 + 1];
+            x[d].d[slot] = A.vx[(int64_t)p1 * 3 + d] - A.vx[(int64_t)p0 * 3 + d];
+        }
+    }
+}
+
+template <int M>
+__device__ Dual<M> tet_volume(const Dual<M> X[4][3]) {
+    Dual<M> a[3], b[3], c[3];
+    for (int d = 0; d < 3; ++d) {
+        a[d] = X[0][d] - X[2][d];
+        b[d] = X[1][d] - X[2][d];
+        c[d] = X[3][d] - X[2][d];
+    }
+    const Dual<M> det = a[0] * (b[1] * c[2] - c[1] * b[2]) - a[1] * (b[0] * c[2] - b[2] * c[0]) +
+                        a[2] * (b[0] * c[1] - b[1] * c[0]);
+    return (1.0 / 6.0) * det;
+}
+
+// cut clusters: one CTA per cluster, one thread per integration cell
+__global__ void adjoint_tets(AdjArgs A, CutSetDev S) {
+    __shared__ double U[24], L[24], X[24];
+    const int64_t e = blockIdx.x;
+    if (e >= S.neq) return;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < 24; i += blockDim.x) X[i] = S.xe[e * 24 + i];
+    const int nb = S.nb[e];
+    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.u, A.nu, U, tid, blockDim.x);
+    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.lam, A.nu, L, tid, blockDim.x);
+    __syncthreads();
+    const double jd[3] = {0.5 * (X[18] - X[0]), 0.5 * (X[19] - X[1]), 0.5 * (X[20] - X[2])};
+    const double lam = S.E[e] * S.lam_c, mu = S.E[e] * S.mu_c;
+    for (int64_t g = S.ig_off[e] + tid; g < S.ig_off[e + 1]; g += blockDim.x) {
+        Dual<4> Xv[4][3], xi[4][3];
+        bool mv[4];
+        int32_t vids[4];
+        for (int k = 0; k < 4; ++k) {
+            vids[k] = S.vid[g * 4 + k];
+            vertex_dual<4>(A, vids[k], k, Xv[k], mv[k]);
+            for (int d = 0; d < 3; ++d) xi[k][d] = (-1.0 - X[d] / jd[d]) + (1.0 / jd[d]) * Xv[k][d];
+        }
+        if (!(mv[0] || mv[1] || mv[2] || mv[3])) continue;
+        const Dual<4> detJ = tet_volume<4>(Xv);
+        Dual<4> F(0.0);
+        for (int q = 0; q < S.ngp; ++q) {
+            const double z0 = S.gp[q * 3], z1 = S.gp[q * 3 + 1], z2 = S.gp[q * 3 + 2];
+            const double Nt[4] = {z0, z1, 1.0 - z0 - z1 - z2, z2};
+            Dual<4> xq[3];
+            for (int d = 0; d < 3; ++d) {
+                xq[d] = Dual<4>(0.0);
+                for (int k = 0; k < 4; ++k) axpy(Nt[k], xi[k][d], xq[d]);
+            }
+            Dual<4> uv[3], Gu[3][3], lv[3], Gl[3][3], Su[3][3];
+            hex_field<4>(xq, jd, U, uv, Gu);
+            hex_field<4>(xq, jd, L, lv, Gl);
+            stress<4>(Gu, lam, mu, Su);
+            Dual<4> phi(0.0);
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) phi = phi + Su[i][j] * (0.5 * Gu[i][j] + (-1.0) * Gl[i][j]);
+            // skipped points (detJ < -1e-6) contribute nothing (cl_FEM_Element_Bulk.cpp:164)
+            if (detJ.v < -1.0e-6) continue;
+            axpy(S.gw[q], detJ * phi, F);
+        }
+        for (int k = 0; k < 4; ++k)
+            if (mv[k]) atomicAdd(A.G + vids[k], F.d[k]);
+    }
+}
+
+struct IfSetDev {
+    int64_t neq;
+    int beta_sym;
+    double alpha, lam_c, mu_c;
+    const double* xe;      // [neq][2][8][3]
+    const double* E;
+    const double* EF;
+    const int32_t* nb;     // [neq][2]
+    const int32_t* bases;  // [neq][2][W]
+    const double* T;       // [neq][2][8][W]
+    int W;
+    const int64_t* fc_off;
+    const int32_t* vid;    // [facet][3]
+    const double* gp;      // TRI rule [ngp][2]
+    const double* gw;
+    int ngp;
+    const double* vol;     // [neq][2]
+    const int32_t* link;   // [neq][4]: leader (set, eq), follower (set, eq) among the cut sets
+};
+
+// interface clusters: one CTA per cluster; threads over facets, then over the
+// leader / follower integration cells (cluster volumes of the SP)
+__global__ void adjoint_interface(AdjArgs A, IfSetDev S, const CutSetDev* cuts) {
+    __shared__ double U[48], L[48], X[48];
+    __shared__ double sums[4];  // A, B, C, area
+    const int64_t e = blockIdx.x;
+    if (e >= S.neq) return;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < 48; i += blockDim.x) X[i] = S.xe[e * 48 + i];
+    for (int s = 0; s < 2; ++s) {
+        const int nb = S.nb[2 * e + s];
+        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.u, A.nu, U + 24 * s, tid,
+                    blockDim.x);
+        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.lam, A.nu, L + 24 * s, tid,
+                    blockDim.x);
+    }
+    if (tid < 4) sums[tid] = 0.0;
+    __syncthreads();
+    const double Es[2] = {S.E[e], S.EF[e]};
+    const double beta = S.beta_sym ? -1.0 : 1.0;
+    const double vl = S.vol[2 * e] / Es[0], vf = S.vol[2 * e + 1] / Es[1], Ssum = vl + vf;
+    const double wl = vl / Ssum, wf = vf / Ssum;
+    // pass 1: facet integrals (values) for the cluster sums
+    // pass 2: their derivatives, scaled by the now known weights
+    const int64_t f0 = S.fc_off[e], f1 = S.fc_off[e + 1];
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int64_t f = f0 + tid; f < f1; f += blockDim.x) {
+            Dual<3> Xv[3][3];
+            bool mv[3];
+            int32_t vids[3];
+            for (int k = 0; k < 3; ++k) {
+                vids[k] = S.vid[f * 3 + k];
+                vertex_dual<3>(A, vids[k], k, Xv[k], mv[k]);
+            }
+            // facet detJ |(x0-x2) x (x1-x2)| / 2 and the unit normal
+            Dual<3> a[3], b[3], cr[3];
+            for (int d = 0; d < 3; ++d) {
+                a[d] = Xv[0][d] - Xv[2][d];
+                b[d] = Xv[1][d] - Xv[2][d];
+            }
+            cr[0] = a[1] * b[2] - a[2] * b[1];
+            cr[1] = a[2] * b[0] - a[0] * b[2];
+            cr[2] = a[0] * b[1] - a[1] * b[0];
+            const Dual<3> nn = dsqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            if (!(nn.v > 0.0)) continue;
+            const Dual<3> inv = dinv(nn);
+            const Dual<3> n[3] = {cr[0] * inv, cr[1] * inv, cr[2] * inv};
+            const Dual<3> detJ = 0.5 * nn;
+            Dual<3> xi[2][3][3];  // [side][vertex][d]
+            for (int s = 0; s < 2; ++s) {
+                const double* Xs = X + 24 * s;
+                for (int k = 0; k < 3; ++k)
+                    for (int d = 0; d < 3; ++d) {
+                        const double jd = 0.5 * (Xs[18 + d] - Xs[d]);
+                        xi[s][k][d] = (-1.0 - Xs[d] / jd) + (1.0 / jd) * Xv[k][d];
+                    }
+            }
+            Dual<3> fa(0.0), fb(0.0), fc(0.0), fr(0.0);
+            for (int q = 0; q < S.ngp; ++q) {
+                const double z0 = S.gp[q * 2], z1 = S.gp[q * 2 + 1];
+                const double Nf[3] = {z0, z1, 1.0 - z0 - z1};
+                Dual<3> uv[2][3], Gu[2][3][3], lv[2][3], Gl[2][3][3];
+                for (int s = 0; s < 2; ++s) {
+                    const double* Xs = X + 24 * s;
+                    const double jd[3] = {0.5 * (Xs[18] - Xs[0]), 0.5 * (Xs[19] - Xs[1]), 0.5 * (Xs[20] - Xs[2])};
+                    Dual<3> xq[3];
+                    for (int d = 0; d < 3; ++d) {
+                        xq[d] = Dual<3>(0.0);
+                        for (int k = 0; k < 3; ++k) axpy(Nf[k], xi[s][k][d], xq[d]);
+                    }
+                    hex_field<3>(xq, jd, U + 24 * s, uv[s], Gu[s]);
+                    hex_field<3>(xq, jd, L + 24 * s, lv[s], Gl[s]);
+                }
+                // tractions t_s(.) = sigma_s(.) n
+                Dual<3> tu[2][3], tl[2][3];
+                for (int s = 0; s < 2; ++s) {
+                    Dual<3> Su[3][3], Sl[3][3];
+                    stress<3>(Gu[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Su);
+                    stress<3>(Gl[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Sl);
+                    for (int i = 0; i < 3; ++i) {
+                        tu[s][i] = Su[i][0] * n[0] + Su[i][1] * n[1] + Su[i][2] * n[2];
+                        tl[s][i] = Sl[i][0] * n[0] + Sl[i][1] * n[1] + Sl[i][2] * n[2];
+                    }
+                }
+                Dual<3> qa(0.0), qb(0.0), qc(0.0);
+                for (int i = 0; i < 3; ++i) {
+                    const Dual<3> ju = uv[0][i] - uv[1][i], jl = lv[0][i] - lv[1][i];
+                    qa = qa + beta * (tl[0][i] * ju) - jl * tu[0][i];
+                    qb = qb + beta * (tl[1][i] * ju) - jl * tu[1][i];
+                    qc = qc + jl * ju;
+                }
+                const Dual<3> ws = S.gw[q] * detJ;
+                fa = fa + ws * qa;
+                fb = fb + ws * qb;
+                fc = fc + ws * qc;
+                fr = fr + ws;
+            }
+            if (pass == 0) {
+                atomicAdd(&sums[0], fa.v);
+                atomicAdd(&sums[1], fb.v);
+                atomicAdd(&sums[2], fc.v);
+                atomicAdd(&sums[3], fr.v);
+            } else {
+                // F = -(wL A + wF B + gamma C), gamma = 2 alpha |G| / S
+                const double gamma = 2.0 * S.alpha * sums[3] / Ssum;
+                const double dg_darea = 2.0 * S.alpha / Ssum;
+                for (int k = 0; k < 3; ++k)
+                    if (mv[k])
+                        atomicAdd(A.G + vids[k],
+                                  -(wl * fa.d[k] + wf * fb.d[k] + gamma * fc.d[k] + sums[2] * dg_darea * fr.d[k]));
+            }
+        }
+        __syncthreads();
+    }
+    // cluster volumes: dF/dV through w_L, w_F and gamma
+    const double gamma = 2.0 * S.alpha * sums[3] / Ssum;
+    const double dwl_dvl = vf / (Ssum * Ssum), dwl_dvf = -vl / (Ssum * Ssum);
+    const double dg_dv = -gamma / Ssum;
+    for (int side = 0; side < 2; ++side) {
+        const CutSetDev& C = cuts[S.link[e * 4 + side * 2]];
+        const int64_t ce = S.link[e * 4 + side * 2 + 1];
+        const double dwl = side == 0 ? dwl_dvl : dwl_dvf;
+        // dF/dvol = -((A - B) dwL/dv + C dgamma/dv) / E_side
+        const double coef = -((sums[0] - sums[1]) * dwl + sums[2] * dg_dv) / Es[side];
+        for (int64_t g = C.ig_off[ce] + tid; g < C.ig_off[ce + 1]; g += blockDim.x) {
+            Dual<4> Xv[4][3];
+            bool mv[4];
+            int32_t vids[4];
+            for (int k = 0; k < 4; ++k) {
+                vids[k] = C.vid[g * 4 + k];
+                vertex_dual<4>(A, vids[k], k, Xv[k], mv[k]);
+            }
+            const Dual<4> vol = tet_volume<4>(Xv);
+            for (int k = 0; k < 4; ++k)
+                if (mv[k]) atomicAdd(A.G + vids[k], coef * vol.d[k]);
+        }
+    }
+}
+
+// dqdp[j] += G[v] dt_v/dp_j through the parents' level set
+__global__ void dqdp_chain(int64_t nv, const int32_t* vkind, const int32_t* vpar, const double* vphi,
+                           const double* G, int width, const int32_t* cols, const double* tmat, double* dqdp) {
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv || vkind[v] != 3 || G[v] == 0.0) return;
+    const int32_t p[2] = {vpar[v * 8], vpar[v * 8 + 1]};
+    const double f0 = vphi[p[0]], f1 = vphi[p[1]];
+    const double den = (f0 - f1) * (f0 - f1);
+    // t = f0 / (f0 - f1): dt/df0 = -f1 / (f0-f1)^2, dt/df1 = f0 / (f0-f1)^2
+    const double dt[2] = {-f1 / den, f0 / den};
+    for (int k = 0; k < 2; ++k) {
+        const int32_t q = p[k];
+        const int kind = vkind[q];
+        const int cnt = kind == 0 ? 1 : kind == 1 ? 4 : 8;
+        const double w = G[v] * dt[k] / (double)cnt;
+        for (int m = 0; m < cnt; ++m) {
+            const int64_t node = vpar[(int64_t)q * 8 + m];
+            for (int j = 0; j < width; ++j) {
+                const double tv = tmat[node * width + j];
+                if (tv != 0.0) atomicAdd(dqdp + cols[node * width + j], w * tv);
+            }
+        }
+    }
+}
+
+__global__ void dot_kernel(int64_t n, const double* a, const double* b, double* out) {
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ double ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) atomicAdd(out, s);
+    }
+}
+
+void dfree(DeviceBuf& b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+template <class T>
+cudaError_t upload(DeviceBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    dfree(b);
+    b.bytes = std::max<size_t>(v.size() * sizeof(T), 16);
+    cudaError_t e = cudaMalloc(&b.p, b.bytes);
+    if (e != cudaSuccess) return e;
+    if (!v.empty()) e = cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+    return e;
+}
+
+// in-place refresh (same size: kernel arguments and captured graphs keep their pointers)
+template <class T>
+cudaError_t refresh(DeviceBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    if (!b.p || b.bytes < v.size() * sizeof(T)) return upload(b, v, st);
+    if (v.empty()) return cudaSuccess;
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+fem_gpu_status sfail(fem_gpu_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? FEM_GPU_OUT_OF_MEMORY : FEM_GPU_CUDA_ERROR,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+double lam_of(int model, double nu) {
+    return model == FEM_GPU_MODEL_PLANE_STRESS ? nu / (1.0 - nu * nu) : nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+}
+
+bool is_cut(const SetData& s) { return s.kind == 0 && !s.ig_off.empty(); }
+bool is_interface(const SetData& s) {
+    return s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
+}
+
+}  // namespace
+
+void sensitivity_release(fem_gpu_ctx* c) {
+    dfree(c->d_vkind);
+    dfree(c->d_vpar);
+    dfree(c->d_vx);
+    for (auto& s : c->sets) {
+        dfree(s.d_vid);
+        dfree(s.d_link);
+    }
+}
+
+}  // namespace fem
+
+using namespace fem;
+
+extern "C" {
+
+fem_gpu_status fem_gpu_set_ig_vertices(fem_gpu_ctx* c, int64_t nv, const int32_t* kind, const int32_t* parents,
+                                       const double* coords, const double* value) {
+    if (!c || nv <= 0 || !kind || !parents || !coords || !value) return FEM_GPU_BAD_ARG;
+    c->vkind.assign(kind, kind + nv);
+    c->vpar.assign(parents, parents + nv * 8);
+    c->vx.assign(coords, coords + nv * 3);
+    c->vval.assign(value, value + nv);
+    for (int64_t v = 0; v < nv; ++v) {
+        const int k = c->vkind[v];
+        if (k < 0 || k > 3) return fail(c, FEM_GPU_BAD_ARG, "IG vertex kind");
+        const int cnt = k == 0 ? 1 : k == 1 ? 4 : k == 2 ? 8 : 2;
+        for (int m = 0; m < cnt; ++m) {
+            const int32_t p = c->vpar[v * 8 + m];
+            const int64_t lim = k == 3 ? nv : c->num_nodes;
+            if (p < 0 || p >= lim) return fail(c, FEM_GPU_OOB_INDEX, "IG vertex parent");
+            if (k == 3 && c->vkind[p] == 3) return fail(c, FEM_GPU_BAD_ARG, "intersection of intersections");
+        }
+    }
+    for (auto& s : c->sets) {
+        if (!(is_cut(s) || is_interface(s))) continue;
+        if (s.vid.empty()) return fail(c, FEM_GPU_BAD_ARG, "cut / interface set without IG vertex ids");
+        for (int32_t v : s.vid)
+            if (v < 0 || v >= nv) return fail(c, FEM_GPU_OOB_INDEX, "IG vertex id");
+    }
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_gpu_update_ig_vertices(fem_gpu_ctx* c, const double* t) {
+    if (!c || !t) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    if (c->vkind.empty()) return fail(c, FEM_GPU_BAD_ARG, "no IG vertex table");
+    if (c->shape != FEM_GPU_SHAPE_RECTANGULAR) return fail(c, FEM_GPU_UNSUPPORTED, "geometry update needs rectangular cells");
+    const int64_t nv = (int64_t)c->vkind.size();
+    for (int64_t v = 0; v < nv; ++v) {
+        if (c->vkind[v] != 3) continue;
+        if (!std::isfinite(t[v])) return fail(c, FEM_GPU_NONFINITE, "edge coordinate");
+        const int32_t p0 = c->vpar[v * 8], p1 = c->vpar[v * 8 + 1];
+        for (int d = 0; d < 3; ++d) c->vx[v * 3 + d] = c->vx[p0 * 3 + d] + t[v] * (c->vx[p1 * 3 + d] - c->vx[p0 * 3 + d]);
+        c->vval[v] = t[v];
+    }
+    const int npe = c->npe;
+    auto param = [&](int64_t cell, const double* x, double* xi) {
+        const double* X0 = &c->coords[(int64_t)c->cells[cell * npe + 0] * 3];
+        const double* X6 = &c->coords[(int64_t)c->cells[cell * npe + 6] * 3];
+        for (int d = 0; d < 3; ++d) xi[d] = -1.0 + 2.0 * (x[d] - X0[d]) / (X6[d] - X0[d]);
+    };
+    cudaStream_t st = (cudaStream_t)c->stream;
+    cudaError_t e = cudaSuccess;
+    for (auto& s : c->sets) {
+        if (is_cut(s)) {
+            for (int64_t i = 0; i < s.neq; ++i)
+                for (int64_t g = s.ig_off[i]; g < s.ig_off[i + 1]; ++g)
+                    for (int k = 0; k < 4; ++k) {
+                        const int32_t v = s.vid[g * 4 + k];
+                        if (c->vkind[v] != 3) continue;
+                        for (int d = 0; d < 3; ++d) s.ig_coords[(g * 4 + k) * 3 + d] = c->vx[v * 3 + d];
+                        param(s.ip_cell[i], &c->vx[v * 3], &s.ig_param[(g * 4 + k) * 3]);
+                    }
+            if (e == cudaSuccess) e = refresh(s.d_igx, s.ig_coords, st);
+            if (e == cudaSuccess) e = refresh(s.d_igxi, s.ig_param, st);
+        } else if (is_interface(s)) {
+            for (int64_t i = 0; i < s.neq; ++i)
+                for (int64_t f = s.fc_off[i]; f < s.fc_off[i + 1]; ++f)
+                    for (int k = 0; k < s.nfv; ++k) {
+                        const int32_t v = s.vid[f * s.nfv + k];
+                        if (c->vkind[v] != 3) continue;
+                        for (int d = 0; d < 3; ++d) s.fc_x[(f * s.nfv + k) * 3 + d] = c->vx[v * 3 + d];
+                        param(s.ip_cell[i], &c->vx[v * 3], &s.fc_xl[(f * s.nfv + k) * 3]);
+                        param(s.fcell[i], &c->vx[v * 3], &s.fc_xf[(f * s.nfv + k) * 3]);
+                    }
+            if (e == cudaSuccess) e = refresh(s.d_fcx, s.fc_x, st);
+            if (e == cudaSuccess) e = refresh(s.d_fcxl, s.fc_xl, st);
+            if (e == cudaSuccess) e = refresh(s.d_fcxf, s.fc_xf, st);
+        }
+    }
+    fem_gpu_status r = interface_volumes(c);
+    if (r != FEM_GPU_OK) return r;
+    for (auto& s : c->sets)
+        if (is_interface(s) && e == cudaSuccess) e = refresh(s.d_vol, s.vol, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return sfail(c, e, "geometry update");
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_gpu_strain_energy(fem_gpu_ctx* c, const double* u, double* dqdu, double* q) {
+    if (!c || !u || !dqdu) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    // residual-only assembly of the bulk sets: dQ/du = K_bulk u (linear CM, no body load)
+    cudaStream_t st = (cudaStream_t)c->stream;
+    const int64_t nad = c->num_used * c->dim;
+    cudaError_t e = cudaMemsetAsync(dqdu, 0, nad * sizeof(double), st);
+    if (e != cudaSuccess) return sfail(c, e, "strain energy zero");
+    fem_gpu_status r = FEM_GPU_OK;
+    for (int k = 0; k < (int)c->sets.size() && r == FEM_GPU_OK; ++k) {
+        if (c->sets[k].kind != 0) continue;
+        r = assemble_set(c, k, u, nullptr, dqdu);
+    }
+    if (r != FEM_GPU_OK) return r;
+    if (q) {
+        double* d = nullptr;
+        e = cudaMallocAsync(&d, sizeof(double), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(double), st);
+        if (e == cudaSuccess) {
+            dot_kernel<<<152 * 4, 256, 0, st>>>(nad, u, dqdu, d);
+            e = cudaMemcpyAsync(q, d, sizeof(double), cudaMemcpyDeviceToHost, st);
+        }
+        if (d) cudaFreeAsync(d, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return sfail(c, e, "strain energy");
+        *q *= 0.5;
+    }
+    return fem_gpu_check_status(c);
+}
+
+fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const double* lambda, double* G) {
+    if (!c || !u || !lambda || !G) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    if (c->vkind.empty()) return fail(c, FEM_GPU_BAD_ARG, "no IG vertex table");
+    if (c->shape != FEM_GPU_SHAPE_RECTANGULAR || c->dim != 3)
+        return fail(c, FEM_GPU_UNSUPPORTED, "shape sensitivities need 3D rectangular cells");
+    cudaStream_t st = (cudaStream_t)c->stream;
+    const int64_t nv = (int64_t)c->vkind.size();
+    cudaError_t e = refresh(c->d_vkind, c->vkind, st);
+    if (e == cudaSuccess) e = refresh(c->d_vpar, c->vpar, st);
+    if (e == cudaSuccess) e = refresh(c->d_vx, c->vx, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, nv * sizeof(double), st);
+    if (e != cudaSuccess) return sfail(c, e, "adjoint vertex table");
+    AdjArgs A{};
+    A.vkind = (const int32_t*)c->d_vkind.p;
+    A.vpar = (const int32_t*)c->d_vpar.p;
+    A.vx = (const double*)c->d_vx.p;
+    A.G = G;
+    A.u = u;
+    A.lam = lambda;
+    A.nu = c->num_used;
+    // cut sets
+    std::vector<CutSetDev> cuts;
+    std::vector<int> cut_index(c->sets.size(), -1);
+    std::vector<std::pair<int32_t, int64_t>> cell_cluster(c->num_cells, {-1, -1});
+    for (size_t k = 0; k < c->sets.size(); ++k) {
+        SetData& s = c->sets[k];
+        if (!is_cut(s)) continue;
+        if (s.vid.empty()) return fail(c, FEM_GPU_BAD_ARG, "cut set without IG vertex ids");
+        if (s.bulk.integration_rule != FEM_GPU_RULE_TET_4 && s.bulk.integration_rule != FEM_GPU_RULE_TET_11)
+            return fail(c, FEM_GPU_UNSUPPORTED, "sensitivities of cut clusters need TET4 cells");
+        if ((e = refresh(s.d_vid, s.vid, st)) != cudaSuccess) return sfail(c, e, "vertex ids");
+        CutSetDev d{};
+        d.neq = s.neq;
+        d.xe = (const double*)s.d_xe.p;
+        d.E = (const double*)s.d_E.p;
+        d.nb = (const int32_t*)s.d_nb.p;
+        d.bases = (const int32_t*)s.d_bases.p;
+        d.T = (const double*)s.d_T.p;
+        d.W = s.nbsel;
+        d.lam_c = lam_of(s.bulk.model_type, s.bulk.poisson_ratio);
+        d.mu_c = 1.0 / (2.0 * (1.0 + s.bulk.poisson_ratio));
+        d.ig_off = (const int64_t*)s.d_igoff.p;
+        d.vid = (const int32_t*)s.d_vid.p;
+        d.gp = (const double*)s.d_gp.p;
+        d.gw = (const double*)s.d_gw.p;
+        d.ngp = s.ngp;
+        cut_index[k] = (int)cuts.size();
+        for (int64_t i = 0; i < s.neq; ++i) cell_cluster[s.ip_cell[i]] = {(int32_t)cuts.size(), i};
+        cuts.push_back(d);
+    }
+    for (const CutSetDev& d : cuts) {
+        adjoint_tets<<<(unsigned)std::max<int64_t>(d.neq, 1), 64, 0, st>>>(A, d);
+        c->launches++;
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return sfail(c, e, "adjoint tets");
+    DeviceBuf dcuts;
+    if ((e = upload(dcuts, cuts, st)) != cudaSuccess) return sfail(c, e, "cut table");
+    fem_gpu_status r = FEM_GPU_OK;
+    for (auto& s : c->sets) {
+        if (!is_interface(s)) continue;
+        if (s.vid.empty() || s.nfv != 3) {
+            r = fail(c, FEM_GPU_UNSUPPORTED, "interface sensitivities need TRI3 facets with vertex ids");
+            break;
+        }
+        s.link.assign(s.neq * 4, 0);
+        for (int64_t i = 0; i < s.neq; ++i) {
+            const auto L = cell_cluster[s.ip_cell[i]], F = cell_cluster[s.fcell[i]];
+            if (L.first < 0 || F.first < 0) {
+                r = fail(c, FEM_GPU_BAD_ARG, "interface cluster without cut clusters on its cells");
+                break;
+            }
+            s.link[i * 4 + 0] = L.first;
+            s.link[i * 4 + 1] = (int32_t)L.second;
+            s.link[i * 4 + 2] = F.first;
+            s.link[i * 4 + 3] = (int32_t)F.second;
+        }
+        if (r != FEM_GPU_OK) break;
+        if ((e = refresh(s.d_link, s.link, st)) != cudaSuccess || (e = refresh(s.d_vid, s.vid, st)) != cudaSuccess) {
+            r = sfail(c, e, "interface links");
+            break;
+        }
+        IfSetDev d{};
+        d.neq = s.neq;
+        d.beta_sym = s.dside.iwg_type == FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE;
+        d.alpha = s.dside.alpha;
+        d.lam_c = lam_of(s.dside.model_type, s.dside.poisson_ratio);
+        d.mu_c = 1.0 / (2.0 * (1.0 + s.dside.poisson_ratio));
+        d.xe = (const double*)s.d_xe.p;
+        d.E = (const double*)s.d_E.p;
+        d.EF = (const double*)s.d_EF.p;
+        d.nb = (const int32_t*)s.d_nb.p;
+        d.bases = (const int32_t*)s.d_bases.p;
+        d.T = (const double*)s.d_T.p;
+        d.W = s.nbsel;
+        d.fc_off = (const int64_t*)s.d_fcoff.p;
+        d.vid = (const int32_t*)s.d_vid.p;
+        d.gp = (const double*)s.d_gp.p;
+        d.gw = (const double*)s.d_gw.p;
+        d.ngp = s.ngp;
+        d.vol = (const double*)s.d_vol.p;
+        d.link = (const int32_t*)s.d_link.p;
+        adjoint_interface<<<(unsigned)std::max<int64_t>(s.neq, 1), 64, 0, st>>>(A, d, (const CutSetDev*)dcuts.p);
+        c->launches++;
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            r = sfail(c, e, "adjoint interface");
+            break;
+        }
+    }
+    cudaStreamSynchronize(st);
+    dfree(dcuts);
+    (void)cut_index;
+    return r;
+}
+
+fem_gpu_status fem_gen_dqdp(fem_gpu_ctx* c, const double* G, int64_t nbn, int32_t width, const int32_t* cols,
+                            const double* tmat, int64_t ncoef, double* dqdp) {
+    if (!c || !G || !cols || !tmat || !dqdp || width <= 0 || nbn <= 0 || ncoef <= 0) return FEM_GPU_BAD_ARG;
+    if (c->vkind.empty()) return fail(c, FEM_GPU_BAD_ARG, "no IG vertex table");
+    const int64_t nv = (int64_t)c->vkind.size();
+    for (int64_t k = 0; k < nbn * width; ++k)
+        if (cols[k] < 0 || cols[k] >= ncoef) return fail(c, FEM_GPU_OOB_INDEX, "level-set coefficient id");
+    for (int64_t v = 0; v < nv; ++v)
+        if (c->vkind[v] != 3)
+            for (int m = 0; m < 8; ++m)
+                if (c->vpar[v * 8 + m] >= nbn) return fail(c, FEM_GPU_OOB_INDEX, "background node of an IG vertex");
+    cudaStream_t st = (cudaStream_t)c->stream;
+    // level set at the parents: vval holds phi for kinds 0-2
+    std::vector<int32_t> vc(cols, cols + nbn * width);
+    std::vector<double> vt(tmat, tmat + nbn * width);
+    DeviceBuf dphi, dcols, dt;
+    cudaError_t e = upload(dphi, c->vval, st);
+    if (e == cudaSuccess) e = upload(dcols, vc, st);
+    if (e == cudaSuccess) e = upload(dt, vt, st);
+    if (e == cudaSuccess) e = refresh(c->d_vkind, c->vkind, st);
+    if (e == cudaSuccess) e = refresh(c->d_vpar, c->vpar, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dqdp, 0, ncoef * sizeof(double), st);
+    if (e == cudaSuccess) {
+        dqdp_chain<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(nv, (const int32_t*)c->d_vkind.p,
+                                                                 (const int32_t*)c->d_vpar.p, (const double*)dphi.p,
+                                                                 G, width, (const int32_t*)dcols.p,
+                                                                 (const double*)dt.p, dqdp);
+        c->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dfree(dphi);
+    dfree(dcols);
+    dfree(dt);
+    if (e != cudaSuccess) return sfail(c, e, "dq/dp chain");
+    return FEM_GPU_OK;
+}
+
+}  // extern "C"

@@ -97,14 +97,15 @@ def xfem_sets(x, E=XFEM_E, nu=XFEM_NU, tet_rule=RULE_TET_4, tri_rule=RULE_TRI_7,
         if len(c["cells"]):
             sets.append(("bulk", dict(ip_cells=c["cells"], E=np.full(len(c["cells"]), E[p]), nu=nu, rule=tet_rule,
                                       ig_cell=CELL_TET4, ig_offsets=c["ig_offsets"], ig_coords=c["ig_coords"],
-                                      ig_param=c["ig_param"])))
+                                      ig_param=c["ig_param"], ig_vertex_ids=c["ig_vertices"])))
     it = x["interface"]
     if len(it["leader"]):
         n = len(it["leader"])
         sets.append(("double", dict(iwg=IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE, leader=it["leader"],
                                     follower=it["follower"], offsets=it["offsets"], coords=it["coords"],
                                     leader_param=it["param"], follower_param=it["param"], EL=np.full(n, E[0]),
-                                    EF=np.full(n, E[1]), nu=nu, rule=tri_rule, facet_cell=CELL_TRI3, alpha=alpha_if)))
+                                    EF=np.full(n, E[1]), nu=nu, rule=tri_rule, facet_cell=CELL_TRI3, alpha=alpha_if,
+                                    facet_vertex_ids=it["vertices"])))
     for p in (0, 1):
         g = x["ghost%d" % p]
         n = len(g["leader"])
@@ -120,11 +121,15 @@ def add_xfem_sets(m, sets):
     for kind, a in sets:
         if kind == "bulk":
             m.add_bulk_set(a["ip_cells"], a["E"], a["nu"], a["rule"], MODEL_3D, ig_cell=a["ig_cell"],
-                           ig_offsets=a.get("ig_offsets"), ig_coords=a.get("ig_coords"), ig_param=a.get("ig_param"))
-        else:
+                           ig_offsets=a.get("ig_offsets"), ig_coords=a.get("ig_coords"), ig_param=a.get("ig_param"),
+                           ig_vertex_ids=a.get("ig_vertex_ids"))
+        elif kind == "double":
             m.add_double_side_set(a["iwg"], a["leader"], a["follower"], a["offsets"], a["coords"], a["leader_param"],
                                   a["follower_param"], a["EL"], a["EF"], a["nu"], a["rule"], a["facet_cell"],
-                                  a["alpha"])
+                                  a["alpha"], facet_vertex_ids=a.get("facet_vertex_ids"))
+        else:
+            m.add_side_set(a["iwg"], a["ip_cells"], a["ordinals"], a["E"], a["nu"], a["rule"], MODEL_3D,
+                           alpha=a.get("alpha", 0.0), value=a["value"])
 
 
 def xfem_spheres(n=96, seed=BASE_SEED + 3, nspheres=40, rmin=0.03, rmax=0.12, order=1, finalize=True, **kw):

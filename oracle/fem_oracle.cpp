@@ -737,6 +737,34 @@ int orc_model_add_double_side_set(orc_model* m, int iwg, int facet_cell, int rul
     return 0;
 }
 
+/* geometry of one cut cluster / one double-sided cluster replaced (same
+   number of integration cells / facets): the finite-difference perturbations
+   of IG vertex coordinates of the reference's dR/dp (IWG::select_dRdp_FD_
+   geometry_bulk, FEM/INT/src/IWG/cl_FEM_IWG.cpp:2997-3154) act on these.  */
+int orc_model_update_ig(orc_model* m, int set, int64_t eq, const double* coords, const double* param) {
+    if (set < 0 || set >= (int)m->bulk.size()) return 1;
+    BulkSet& s = m->bulk[set];
+    if (s.ig_off.empty() || eq < 0 || eq >= (int64_t)s.ip_cell.size()) return 1;
+    const int64_t per = (int64_t)cell_nodes(s.ig_cell) * m->dim;
+    const int64_t b = s.ig_off[eq] * per, n = (s.ig_off[eq + 1] - s.ig_off[eq]) * per;
+    std::copy(coords, coords + n, s.ig_coords.begin() + b);
+    std::copy(param, param + n, s.ig_param.begin() + b);
+    return 0;
+}
+int orc_model_update_facets(orc_model* m, int set, int64_t eq, const double* coords, const double* lparam,
+                            const double* fparam) {
+    const int k = set - (int)m->bulk.size() - (int)m->side.size();
+    if (k < 0 || k >= (int)m->dbl.size()) return 1;
+    DoubleSet& s = m->dbl[k];
+    if (eq < 0 || eq >= (int64_t)s.leader.size()) return 1;
+    const int64_t per = (int64_t)cell_nodes(s.facet_cell) * m->dim;
+    const int64_t b = s.fc_off[eq] * per, n = (s.fc_off[eq + 1] - s.fc_off[eq]) * per;
+    std::copy(coords, coords + n, s.fc_x.begin() + b);
+    std::copy(lparam, lparam + n, s.fc_xl.begin() + b);
+    std::copy(fparam, fparam + n, s.fc_xf.begin() + b);
+    return 0;
+}
+
 /* MSI: adof numbering by type then basis rank among used bases
    (Dof_Manager::create_adofs / set_owned_adofs_ids_by_type,
    FEM/MSI/src/cl_MSI_Dof_Manager.cpp:703-744, 820-985); element unique adof

@@ -88,6 +88,10 @@ int orc_model_add_double_side_set(orc_model* m, int iwg, int facet_cell, int rul
                                   const int64_t* facet_offsets, const double* facet_coords,
                                   const double* leader_param, const double* follower_param,
                                   const double* leader_E, const double* follower_E, double nu, double alpha);
+/* replace the integration-cell / facet geometry of one cluster (same counts) */
+int orc_model_update_ig(orc_model* m, int set, int64_t eq, const double* coords, const double* param);
+int orc_model_update_facets(orc_model* m, int set, int64_t eq, const double* coords, const double* leader_param,
+                            const double* follower_param);
 int orc_model_finalize(orc_model* m);
 int64_t orc_model_num_adofs(const orc_model* m);
 int64_t orc_model_nnz(const orc_model* m);

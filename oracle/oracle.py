@@ -43,6 +43,8 @@ def load():
             "orc_model_add_double_side_set": (_I, [_P, _I, _I, _I, _I, _L, _P, _P, _P, _P, _P, _P, _P, _P, _D,
                                                    _D]),
             "orc_model_finalize": (_I, [_P]),
+            "orc_model_update_ig": (_I, [_P, _I, _L, _P, _P]),
+            "orc_model_update_facets": (_I, [_P, _I, _L, _P, _P, _P]),
             "orc_model_num_adofs": (_L, [_P]),
             "orc_model_nnz": (_L, [_P]),
             "orc_model_num_sets": (_I, [_P]),
@@ -148,6 +150,15 @@ class OracleModel:
         r = self.lib.orc_model_add_double_side_set(self.h, iwg, facet_cell, rule, model, len(arrs[0]),
                                                    *[_ptr(a) for a in arrs], nu, alpha)
         assert r == 0
+
+    def update_ig(self, s, eq, coords, param):
+        c = np.ascontiguousarray(coords, dtype=np.float64)
+        p = np.ascontiguousarray(param, dtype=np.float64)
+        assert self.lib.orc_model_update_ig(self.h, s, eq, _ptr(c), _ptr(p)) == 0
+
+    def update_facets(self, s, eq, coords, lparam, fparam):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (coords, lparam, fparam)]
+        assert self.lib.orc_model_update_facets(self.h, s, eq, *[_ptr(a) for a in arrs]) == 0
 
     def set_density(self, s, node_rho, beta=3.0):
         rho = np.ascontiguousarray(node_rho, dtype=np.float64)

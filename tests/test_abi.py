@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "fem_gpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"\b(fem_(?:gpu|hmr|cnn|lpc|xtk)_\w+)\s*\(", src)
+    names = re.findall(r"\b(fem_(?:gpu|hmr|cnn|lpc|xtk|gen)_\w+)\s*\(", src)
     return sorted(set(names))
 
 
@@ -30,7 +30,7 @@ def test_binding_covers_header():
 
 def test_library_answers_without_gpu():
     lib = mg.lib()
-    assert lib.fem_gpu_abi_version() == 1
+    assert lib.fem_gpu_abi_version() == 2
     assert lib.fem_gpu_status_string(0) == b"ok"
     assert lib.fem_gpu_device_count() >= 0
 

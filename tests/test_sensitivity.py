@@ -1,0 +1,173 @@
+"""Shape sensitivities through the level-set coefficients (config 4 path):
+the adjoint dR/dp kernel against central finite differences, the chain to
+the B-spline coefficients against central finite differences on 50 random
+coefficients, the full dQ/dp with re-solves, and the reference's own
+finite-difference sensitivities restated on the oracle."""
+import numpy as np
+import pytest
+
+import moris_gb300 as mg
+from moris_gb300 import sensitivity as S
+from moris_gb300.rng import uniform01
+from oracle import OracleModel
+from oracle.fd_sensitivity import reference_fd_dfdt
+
+H = 1e-6
+
+
+def small_case(n=8, ncoef=12, order=2):
+    return S.build(n=n, ncoef=ncoef, order=order)
+
+
+def test_bspline_tmatrix_partition_of_unity():
+    cols, vals = S.node_tmatrix(6, 12)
+    assert np.allclose(vals.sum(axis=1), 1.0, atol=1e-14)
+    assert cols.min() >= 0 and cols.max() < 12 ** 3
+
+
+def test_edge_coordinates_reproduce_the_decomposition():
+    c = S.build(n=8, ncoef=12, finalize=False)
+    t = S.edge_coordinates(c["x"]["vertices"], c["phi"])
+    k = c["x"]["vertices"]["kind"] == 3
+    assert np.max(np.abs(t[k] - c["x"]["vertices"]["value"][k])) < 1e-14
+
+
+def oracle_of(c):
+    x, sets = c["x"], c["sets"]
+    o = OracleModel(3, mg.CELL_HEX8, mg.SHAPE_RECTANGULAR, x["mesh"])
+    for kind, a in sets:
+        if kind == "bulk":
+            o.add_bulk_set(a["ig_cell"], a["rule"], mg.MODEL_3D, a["ip_cells"], a["E"], a["nu"],
+                           a.get("ig_offsets"), a.get("ig_coords"), a.get("ig_param"))
+    for kind, a in sets:
+        if kind == "side":
+            o.add_side_set(a["iwg"], a["rule"], mg.MODEL_3D, a["ip_cells"], a["ordinals"], a["E"], a["nu"],
+                           a["alpha"], a["value"])
+    for kind, a in sets:
+        if kind == "double":
+            o.add_double_side_set(a["iwg"], a["facet_cell"], a["rule"], mg.MODEL_3D, a["leader"], a["follower"],
+                                  a["offsets"], a["coords"], a["leader_param"], a["follower_param"], a["EL"], a["EF"],
+                                  a["nu"], a["alpha"])
+    o.finalize()
+    return o
+
+
+def random_state(c, seed):
+    import torch
+    n = c["model"].num_adofs
+    u = torch.tensor(uniform01(seed, n) - 0.5, device="cuda") * 1e-2
+    lam = torch.tensor(uniform01(seed + 1, n) - 0.5, device="cuda") * 1e-2
+    return u, lam
+
+
+@pytest.mark.gpu
+def test_adjoint_kernel_matches_central_fd_in_t():
+    """G[v] = d(Q - lambda^T R)/dt_v at fixed u, lambda vs central differences
+    of the assembled functional with the geometry update."""
+    c = small_case()
+    m = c["model"]
+    u, lam = random_state(c, 11)
+    G, _ = S.sensitivities(c, u, lam)
+    G = G.cpu().numpy()
+    V = c["x"]["vertices"]
+    t0 = V["value"].copy()
+    inter = np.nonzero(V["kind"] == 3)[0]
+    pick = inter[(uniform01(5, 30) * len(inter)).astype(int)]
+    scale = np.max(np.abs(G[inter]))
+    for v in pick:
+        tp, tm = t0.copy(), t0.copy()
+        tp[v] += H
+        tm[v] -= H
+        m.update_ig_vertices(tp)
+        fp = S.functional(m, u, lam)
+        m.update_ig_vertices(tm)
+        fm = S.functional(m, u, lam)
+        fd = (fp - fm) / (2 * H)
+        assert abs(fd - G[v]) <= 1e-6 * scale, (v, fd, G[v], scale)
+    m.update_ig_vertices(t0)
+
+
+@pytest.mark.gpu
+def test_dqdp_chain_matches_central_fd_on_50_coefficients():
+    c = small_case()
+    m = c["model"]
+    u, lam = random_state(c, 21)
+    _, dqdp = S.sensitivities(c, u, lam)
+    dqdp = dqdp.cpu().numpy()
+    p0 = c["p"].copy()
+    active = np.nonzero(dqdp != 0.0)[0]
+    assert len(active) >= 50
+    pick = active[np.unique((uniform01(7, 200) * len(active)).astype(int))[:50]]
+    scale = np.max(np.abs(dqdp))
+    V = c["x"]["vertices"]
+    for j in pick:
+        vals = []
+        for sgn in (1.0, -1.0):
+            p = p0.copy()
+            p[j] += sgn * H
+            t = S.edge_coordinates(V, S.node_phi(c["cols"], c["vals"], p))
+            m.update_ig_vertices(t)
+            vals.append(S.functional(m, u, lam))
+        fd = (vals[0] - vals[1]) / (2 * H)
+        assert abs(fd - dqdp[j]) <= 1e-6 * scale, (j, fd, dqdp[j], scale)
+    m.update_ig_vertices(V["value"])
+
+
+@pytest.mark.gpu
+def test_full_dqdp_with_solves_matches_central_fd():
+    """dQ/dp with the adjoint solve against central differences of Q(p) with a
+    direct solve of K(p) u = f per evaluation."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    import torch
+    c = small_case()
+    m = c["model"]
+    rp, ci = m.graph()
+
+    def solve_q():
+        vals = torch.empty(m.nnz, dtype=torch.float64, device="cuda")
+        r0 = torch.empty(m.num_adofs, dtype=torch.float64, device="cuda")
+        m.assemble(None, vals, r0)
+        A = sp.csr_matrix((vals.cpu().numpy(), ci, rp), shape=(m.num_adofs,) * 2)
+        u = spla.spsolve(A.tocsc(), -r0.cpu().numpy())
+        ud = torch.tensor(u, device="cuda")
+        dq = torch.empty_like(ud)
+        q = m.strain_energy(ud, dq)
+        return q, ud, dq, A
+
+    q0, u, dq, A = solve_q()
+    lam = torch.tensor(spla.spsolve(A.T.tocsc(), dq.cpu().numpy()), device="cuda")
+    _, dqdp = S.sensitivities(c, u, lam)
+    dqdp = dqdp.cpu().numpy()
+    active = np.nonzero(dqdp != 0.0)[0]
+    pick = active[np.argsort(-np.abs(dqdp[active]))[:8]]
+    p0 = c["p"].copy()
+    V = c["x"]["vertices"]
+    for j in pick:
+        qs = []
+        for sgn in (1.0, -1.0):
+            p = p0.copy()
+            p[j] += sgn * H
+            m.update_ig_vertices(S.edge_coordinates(V, S.node_phi(c["cols"], c["vals"], p)))
+            qs.append(solve_q()[0])
+        fd = (qs[0] - qs[1]) / (2 * H)
+        # central differences through two direct solves: O(h^2) truncation, 1e-4 relative
+        assert abs(fd - dqdp[j]) <= 1e-4 * abs(dqdp[j]) + 1e-12 * abs(q0), (j, fd, dqdp[j])
+    m.update_ig_vertices(V["value"])
+
+
+@pytest.mark.gpu
+def test_adjoint_matches_reference_fd_geometry_sensitivities():
+    """Against the reference's finite-difference dR/dp on the IG vertex
+    coordinates (forward, relative step 1e-6), restated on the oracle."""
+    c = small_case()
+    u, lam = random_state(c, 31)
+    G, _ = S.sensitivities(c, u, lam)
+    G = G.cpu().numpy()
+    orc = oracle_of(c)
+    V = c["x"]["vertices"]
+    inter = np.nonzero(V["kind"] == 3)[0]
+    pick = inter[np.unique((uniform01(9, 24) * len(inter)).astype(int))]
+    ref = reference_fd_dfdt(orc, c["sets"], c["x"], u.cpu().numpy(), lam.cpu().numpy(), pick)
+    scale = np.max(np.abs(G[inter]))
+    assert np.max(np.abs(ref - G[pick])) <= 1e-4 * scale, np.max(np.abs(ref - G[pick])) / scale

@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-c3", action="store_true", help="skip the XFEM (config 3) record")
+    ap.add_argument("--no-c4", action="store_true", help="skip the adjoint-sensitivity (config 4) record")
     return ap.parse_args()
 
 
@@ -289,6 +290,90 @@ def run_c3(timed, stream, world, args):
     return rec
 
 
+# analysis B-splines of the sensitivity workload: linear, because Jacobi-PCG does
+# not reach 1e-10 on the quadratic-B-spline XFEM system of this mesh (first-order
+# ghost penalty); the kernels are tested on quadratic B-splines with direct solves
+C4_ORDER = 1
+
+
+def run_c4(stream, args):
+    """Config 4: adjoint shape sensitivities of the strain energy with respect
+    to a 32^3 cubic B-spline level set on the 64^3 quadratic-B-spline mesh."""
+    import torch
+    from moris_gb300 import sensitivity as S
+    from moris_gb300.rng import uniform01
+    t0 = time.perf_counter()
+    c = S.build(n=64, ncoef=32, order=C4_ORDER, stream=stream.cuda_stream)
+    m = c["model"]
+    setup = time.perf_counter() - t0
+    sol = S.solve_state_adjoint(m, rel_tol=1e-10, max_iter=40000)
+    u, lam = sol["u"], sol["lam"]
+    nv = len(c["x"]["vertices"]["kind"])
+    G = torch.empty(nv, dtype=torch.float64, device="cuda")
+    dqdp = torch.empty(len(c["p"]), dtype=torch.float64, device="cuda")
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    m.drdp_adjoint(u, lam, G)  # warm-up
+    torch.cuda.synchronize()
+    e0.record(stream)
+    reps = 3
+    for _ in range(reps):
+        m.drdp_adjoint(u, lam, G)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_adj = e0.elapsed_time(e1) / reps
+    t1 = time.perf_counter()
+    m.gen_dqdp(G, c["cols"], c["vals"], len(c["p"]), dqdp)
+    ms_chain = (time.perf_counter() - t1) * 1e3
+    dq = dqdp.cpu().numpy()
+    # central FD (h = 1e-6) of Q - lambda^T R at fixed u, lambda on 50 random active coefficients
+    active = np.nonzero(dq != 0.0)[0]
+    pick = active[np.unique((uniform01(SEED + 40, 400) * len(active)).astype(int))[:50]]
+    V = c["x"]["vertices"]
+    worst = 0.0
+    h = 1e-6
+    for j in pick:
+        f = []
+        for sgn in (1.0, -1.0):
+            p = c["p"].copy()
+            p[j] += sgn * h
+            m.update_ig_vertices(S.edge_coordinates(V, S.node_phi(c["cols"], c["vals"], p)))
+            f.append(S.functional(m, u, lam))
+        worst = max(worst, abs((f[0] - f[1]) / (2 * h) - dq[j]) / np.max(np.abs(dq)))
+    m.update_ig_vertices(V["value"])
+    n_inter = int(np.sum(V["kind"] == 3))
+    rec = {"workload": "64^3 hex8 unit cube, linear B-splines, XFEM two-phase cut by a 32^3 cubic B-spline "
+                       "level set (sphere field of config 3 + 0.01 x smoothed Gaussian noise, seed %d), strain energy"
+                       % (SEED + 2),
+           "adofs": m.num_adofs, "level_set_coefficients": len(c["p"]), "intersection_vertices": n_inter,
+           "Q": sol["q"], "pcg_iterations": {"state": sol["pcg_u"]["iterations"],
+                                             "adjoint": sol["pcg_lambda"]["iterations"]},
+           "pcg_seconds": {"state": sol["pcg_u"]["seconds"], "adjoint": sol["pcg_lambda"]["seconds"]},
+           "pcg_converged": {"state": sol["pcg_u"]["converged"], "adjoint": sol["pcg_lambda"]["converged"]},
+           "adjoint_kernel_ms": ms_adj, "vertices_per_s": n_inter / (ms_adj * 1e-3), "chain_ms": ms_chain,
+           "fd_check": {"coefficients": int(len(pick)), "h": h, "max_abs_err_over_max_dqdp": worst},
+           "setup_seconds": setup}
+    if not args.no_cpu:
+        # the reference's finite-difference dR/dp (forward FD of IG vertex coordinates),
+        # restated on the oracle, timed on a sample of intersection vertices
+        from oracle.fd_sensitivity import oracle_model, reference_fd_dfdt
+        t2 = time.perf_counter()
+        orc = oracle_model(c["x"], c["sets"])
+        build_s = time.perf_counter() - t2
+        inter = np.nonzero(V["kind"] == 3)[0]
+        sample = inter[np.unique((uniform01(SEED + 41, 40) * len(inter)).astype(int))]
+        Gh = G.cpu().numpy()
+        t2 = time.perf_counter()
+        ref = reference_fd_dfdt(orc, c["sets"], c["x"], u.cpu().numpy(), lam.cpu().numpy(), sample)
+        dt = time.perf_counter() - t2
+        rec["cpu_baseline"] = {"value": len(sample) / dt, "unit": "vertices/s", "cores": 1, "kind": "port",
+                               "sample": "%d intersection vertices, the reference's forward-FD geometric dR/dp "
+                                         "restated on the oracle (model build %.1f s not timed)" % (len(sample), build_s)}
+        rec["reference_fd_agreement"] = float(np.max(np.abs(ref - Gh[sample])) / np.max(np.abs(Gh[inter])))
+        rec["speedup_vs_cpu"] = rec["vertices_per_s"] / rec["cpu_baseline"]["value"]
+    return rec, c
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -491,6 +576,9 @@ def main():
                             "pcg_iterations": rep1["iterations"], "rel_residual": rep1["rel_residual"]}
     if world == 1 and not args.no_c3:
         line["c3_xfem"] = run_c3(timed, stream, world, args)
+    if world == 1 and not args.no_c4:
+        line["c4_adjoint"], _ = run_c4(stream, args)
+        torch.cuda.empty_cache()
     if world == 1 and not args.no_cpu:
         r = cpu_reference(mesh, E, args.cpu_seconds)
         line["cpu_baseline"] = {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",

@@ -137,16 +137,30 @@ def system(m):
     return rp, ci, vals, -r0
 
 
-def solve_state_adjoint(m, rel_tol=1e-10, max_iter=200000):
+def _pcg(m, rp, ci, vals, b, x, rel_tol, max_iter):
+    from . import FemGpuError
+    import time
+    t0 = time.perf_counter()
+    try:
+        r = m.pcg(rp, ci, vals, b, x, rel_tol=rel_tol, max_iter=max_iter)
+    except FemGpuError as e:
+        if e.status != 10:  # FEM_GPU_NOT_CONVERGED: report instead of raising
+            raise
+        r = dict(iterations=max_iter, converged=False, rel_residual=float("nan"))
+    r["seconds"] = time.perf_counter() - t0
+    return r
+
+
+def solve_state_adjoint(m, rel_tol=1e-10, max_iter=100000):
     """u (K u = f), lambda (K^T lambda = dQ/du; K is symmetric), Q."""
     import torch
     rp, ci, vals, f = system(m)
     u = torch.zeros_like(f)
-    ru = m.pcg(rp, ci, vals, f, u, rel_tol=rel_tol, max_iter=max_iter)
+    ru = _pcg(m, rp, ci, vals, f, u, rel_tol, max_iter)
     dqdu = torch.empty_like(f)
     q = m.strain_energy(u, dqdu)
     lam = torch.zeros_like(f)
-    rl = m.pcg(rp, ci, vals, dqdu, lam, rel_tol=rel_tol, max_iter=max_iter)
+    rl = _pcg(m, rp, ci, vals, dqdu, lam, rel_tol, max_iter)
     return dict(u=u, lam=lam, q=q, dqdu=dqdu, pcg_u=ru, pcg_lambda=rl, csr=(rp, ci, vals, f))
 
 

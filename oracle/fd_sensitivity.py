@@ -18,6 +18,31 @@ intersection-vertex direction: dF/dt_v = g_v . (x_p1 - x_p0).
 """
 import numpy as np
 
+from .oracle import OracleModel
+
+CELL_HEX8, CELL_TRI3, SHAPE_RECT, MODEL_3D = 1, 2, 0, 2
+
+
+def oracle_model(x, sets):
+    """Oracle model of an XFEM set list (bulk, side and double-sided sets, in the
+    oracle's set order bulk / side / double)."""
+    o = OracleModel(3, CELL_HEX8, SHAPE_RECT, x["mesh"])
+    for kind, a in sets:
+        if kind == "bulk":
+            o.add_bulk_set(a["ig_cell"], a["rule"], MODEL_3D, a["ip_cells"], a["E"], a["nu"], a.get("ig_offsets"),
+                           a.get("ig_coords"), a.get("ig_param"))
+    for kind, a in sets:
+        if kind == "side":
+            o.add_side_set(a["iwg"], a["rule"], MODEL_3D, a["ip_cells"], a["ordinals"], a["E"], a["nu"], a["alpha"],
+                           a["value"])
+    for kind, a in sets:
+        if kind == "double":
+            o.add_double_side_set(a["iwg"], a["facet_cell"], a["rule"], MODEL_3D, a["leader"], a["follower"],
+                                  a["offsets"], a["coords"], a["leader_param"], a["follower_param"], a["EL"], a["EF"],
+                                  a["nu"], a["alpha"])
+    o.finalize()
+    return o
+
 
 def _cluster_index(sets, x):
     """Oracle set index of every cut set and the interface set, and for every
@@ -35,7 +60,7 @@ def _cluster_index(sets, x):
     kd = 0
     for k, a in sets:
         if k == "double":
-            if a["facet_cell"] == 2:  # TRI3 facets: the interface
+            if a["facet_cell"] == CELL_TRI3:  # TRI3 facets: the interface
                 iface = (nb + ns + kd, a)
             kd += 1
     return cut_sets, iface

@@ -9,8 +9,7 @@ import pytest
 import moris_gb300 as mg
 from moris_gb300 import sensitivity as S
 from moris_gb300.rng import uniform01
-from oracle import OracleModel
-from oracle.fd_sensitivity import reference_fd_dfdt
+from oracle.fd_sensitivity import oracle_model, reference_fd_dfdt
 
 H = 1e-6
 
@@ -33,23 +32,7 @@ def test_edge_coordinates_reproduce_the_decomposition():
 
 
 def oracle_of(c):
-    x, sets = c["x"], c["sets"]
-    o = OracleModel(3, mg.CELL_HEX8, mg.SHAPE_RECTANGULAR, x["mesh"])
-    for kind, a in sets:
-        if kind == "bulk":
-            o.add_bulk_set(a["ig_cell"], a["rule"], mg.MODEL_3D, a["ip_cells"], a["E"], a["nu"],
-                           a.get("ig_offsets"), a.get("ig_coords"), a.get("ig_param"))
-    for kind, a in sets:
-        if kind == "side":
-            o.add_side_set(a["iwg"], a["rule"], mg.MODEL_3D, a["ip_cells"], a["ordinals"], a["E"], a["nu"],
-                           a["alpha"], a["value"])
-    for kind, a in sets:
-        if kind == "double":
-            o.add_double_side_set(a["iwg"], a["facet_cell"], a["rule"], mg.MODEL_3D, a["leader"], a["follower"],
-                                  a["offsets"], a["coords"], a["leader_param"], a["follower_param"], a["EL"], a["EF"],
-                                  a["nu"], a["alpha"])
-    o.finalize()
-    return o
+    return oracle_model(c["x"], c["sets"])
 
 
 def random_state(c, seed):

@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-c3", action="store_true", help="skip the XFEM (config 3) record")
     ap.add_argument("--no-c4", action="store_true", help="skip the adjoint-sensitivity (config 4) record")
+    ap.add_argument("--no-c5", action="store_true", help="skip the learned-preconditioner (config 5) record")
     return ap.parse_args()
 
 
@@ -374,6 +375,41 @@ def run_c4(stream, args):
     return rec, c
 
 
+LPC_WEIGHTS = os.path.join(ROOT, "moris_gb300", "data", "lpc_simp128.bin")
+
+
+def run_c5(stream, args):
+    """Config 5: SIMP 128^3, Jacobi-PCG against flexible CG with the learned
+    coarse-grid correction (weights trained on the GPU by moris_gb300/train_lpc.py
+    on other density seeds), both to 1e-8 relative residual."""
+    import torch
+    from moris_gb300 import learned, workloads
+    if not os.path.exists(LPC_WEIGHTS):
+        return {"unavailable": "no trained weights (python -m moris_gb300.train_lpc)"}
+    cnn, factor, meta = learned.load_cnn(LPC_WEIGHTS)
+    m, mesh, rho = workloads.simp_3d(128, finalize=False)
+    m.set_stream(stream.cuda_stream)
+    m.finalize()
+    rho_d = torch.tensor(rho, device="cuda")
+    t0 = time.perf_counter()
+    rp, ci, vals, b = learned.assembled_system(m)
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    x_plain = torch.zeros_like(b)
+    plain = m.pcg(rp, ci, vals, b, x_plain, rel_tol=1e-8, max_iter=100000)
+    x_fj = torch.zeros_like(b)
+    fcg_j = learned.fcg(m, rp, ci, vals, b, x_fj, None, factor, rho_d, rel_tol=1e-8, max_iter=100000)
+    x_l = torch.zeros_like(b)
+    fcg_l = learned.fcg(m, rp, ci, vals, b, x_l, cnn, factor, rho_d, rel_tol=1e-8, max_iter=100000)
+    err = float(torch.linalg.norm(x_l - x_plain) / torch.linalg.norm(x_plain))
+    return {"workload": "SIMP 128^3 hex8, linear B-splines, rho smoothed noise in [1e-3,1] (seed %d), E = rho^3, "
+                        "Nitsche clamp x=0, traction x=1" % (workloads.BASE_SEED + 5),
+            "adofs": m.num_adofs, "assembly_seconds": t_asm,
+            "jacobi_pcg": plain, "fcg_jacobi": fcg_j, "fcg_learned": fcg_l,
+            "wall_time_ratio_plain_over_learned": plain["seconds"] / fcg_l["seconds"],
+            "solution_rel_diff_learned_vs_plain": err, "training": json.loads(meta) if meta else None}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -578,6 +614,9 @@ def main():
         line["c3_xfem"] = run_c3(timed, stream, world, args)
     if world == 1 and not args.no_c4:
         line["c4_adjoint"], _ = run_c4(stream, args)
+        torch.cuda.empty_cache()
+    if world == 1 and not args.no_c5:
+        line["c5_learned_pcg"] = run_c5(stream, args)
         torch.cuda.empty_cache()
     if world == 1 and not args.no_cpu:
         r = cpu_reference(mesh, E, args.cpu_seconds)

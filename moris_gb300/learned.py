@@ -228,7 +228,7 @@ def train_simp(n=128, factor=4, fields=10, per_field=200, every=None, epochs=30,
     for f in range(fields):
         m, mesh, rho = workloads.simp_3d(n, seed=workloads.BASE_SEED + 1000 + f)
         rho_dev = torch.tensor(rho, device="cuda")
-        ev = every or max(1, 3000 // per_field)
+        ev = every or max(1, 2000 // per_field)
         a, b_, iters = training_pairs(m, rho_dev, factor, ev, per_field)
         ins += a
         tgts += b_

@@ -106,3 +106,28 @@ def test_training_reduces_loss(torch):
     cnn = Cnn(n, batch_max=4, seed=3)
     hist = train(cnn, ins, tgts, epochs=40, batch=4, lr=3e-3)
     assert hist[-1] < 0.3 * hist[0]
+
+
+@pytest.mark.gpu
+def test_learned_correction_gain_is_measured(torch, record_property):
+    """Trains the correction on other density seeds (32^3 SIMP), then solves the
+    benchmark-seed field with Jacobi-PCG and with FCG + the learned correction.
+    Both must reach 1e-8 on the true residual and agree; the iteration / time
+    ratio is what the trained network gains over the method without it."""
+    from moris_gb300 import learned, workloads
+    cnn, hist, npairs = learned.train_simp(n=32, factor=4, fields=4, per_field=60, epochs=30, batch=8, lr=1e-3,
+                                           log=lambda s: None)
+    assert hist[-1] < hist[0]
+    m, mesh, rho = workloads.simp_3d(32)
+    rho_d = torch.tensor(rho, device="cuda")
+    rp, ci, vals, b = learned.assembled_system(m)
+    xp = torch.zeros_like(b)
+    plain = m.pcg(rp, ci, vals, b, xp, rel_tol=1e-8, max_iter=100000)
+    xl = torch.zeros_like(b)
+    rep = learned.fcg(m, rp, ci, vals, b, xl, cnn, 4, rho_d, rel_tol=1e-8, max_iter=100000)
+    assert rep["converged"] and rep["rel_residual"] <= 1e-8 * 1.0001
+    assert float(torch.linalg.norm(xl - xp) / torch.linalg.norm(xp)) < 1e-5
+    record_property("iterations_plain", plain["iterations"])
+    record_property("iterations_learned", rep["iterations"])
+    record_property("fallback", rep["fallback"])
+    record_property("time_ratio_plain_over_learned", plain["seconds"] / rep["seconds"])

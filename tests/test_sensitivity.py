@@ -134,8 +134,10 @@ def test_full_dqdp_with_solves_matches_central_fd():
             m.update_ig_vertices(S.edge_coordinates(V, S.node_phi(c["cols"], c["vals"], p)))
             qs.append(solve_q()[0])
         fd = (qs[0] - qs[1]) / (2 * H)
-        # central differences through two direct solves: O(h^2) truncation, 1e-4 relative
-        assert abs(fd - dqdp[j]) <= 1e-4 * abs(dqdp[j]) + 1e-12 * abs(q0), (j, fd, dqdp[j])
+        # central differences through two direct solves: O(h^2) truncation (1e-4 relative)
+        # plus the rounding of Q itself (atomic summation order, the solve), amplified by 1/H
+        noise = 1e-11 * abs(q0) / H
+        assert abs(fd - dqdp[j]) <= 1e-4 * abs(dqdp[j]) + noise, (j, fd, dqdp[j], noise)
     m.update_ig_vertices(V["value"])
 
 

@@ -437,6 +437,53 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_
                            const double* b, double* x, fem_cnn* cnn, int32_t factor, const double* node_density,
                            const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report, int32_t* used_fallback);
 
+/* ---- geometric multigrid preconditioner ----------------------------------
+   Replaces the reference's PETSc PCMG preconditioner
+   (Preconditioner_PETSc::build_multigrid_preconditioner,
+   SOL/DLA/src/cl_DLA_Preconditioner_PETSc.cpp:77-345, prolongations from
+   Geometric_Multigrid, SOL/DLA/src/cl_DLA_Geometric_Multigrid.cpp:47-121):
+   V-cycle with Galerkin coarse operators P^T A P, the linear B-spline
+   two-scale relation (trilinear interpolation, factor 2 per level) as P,
+   Chebyshev-accelerated point-Jacobi smoothing (the reference smooths with
+   SOR) and a dense inverse on the coarsest grid (the reference uses LU).
+   For 3D models on a cubic node grid of n^3 nodes (adof f n^3 + node, node =
+   x + n (y + n z)) whose operator is the 27-point nodal stencil of linear
+   B-splines; n - 1 must halve down to <= coarse_max.  Work is issued on the
+   legacy default stream. */
+typedef struct fem_mg fem_mg;
+typedef struct fem_mg_opts {
+    int32_t coarse_max;   /* coarsest node grid edge, 3..9 (default 9) */
+    int32_t degree;       /* Chebyshev degree of pre- and post-smoothing, 1..8 (2) */
+    double lo_frac;       /* smoothing interval [lo_frac, hi_frac] * lambda_max(D^-1 A) (0.1, 1.1) */
+    double hi_frac;
+    int32_t power_iters;  /* power iterations for lambda_max (12) */
+    int32_t fp32_levels;  /* levels 0..fp32_levels-1 smooth with an FP32 copy of the stencil (0) */
+} fem_mg_opts;
+fem_gpu_status fem_mg_default_opts(fem_mg_opts* opts);
+/* builds the hierarchy from the assembled CSR (device); opts NULL = defaults */
+fem_gpu_status fem_mg_create(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                             const fem_mg_opts* opts, fem_mg** out);
+fem_gpu_status fem_mg_destroy(fem_mg* mg);
+int32_t fem_mg_num_levels(const fem_mg* mg);
+double fem_mg_setup_seconds(const fem_mg* mg);
+/* node grid edge and lambda_max(D^-1 A) of a level (lambda 0 on the coarsest) */
+fem_gpu_status fem_mg_level_info(const fem_mg* mg, int32_t level, int32_t* n, double* lambda_max);
+/* stencil of a level to host memory, [27][3][3][n^3] doubles (tap k =
+   (dx+1) + 3 (dy+1) + 9 (dz+1), row component f, column component g) */
+fem_gpu_status fem_mg_get_stencil(const fem_mg* mg, int32_t level, double* host_out);
+/* one V-cycle z = V r (device vectors of num_adofs doubles) */
+fem_gpu_status fem_mg_apply(fem_mg* mg, const double* r, double* z);
+/* fem_gpu_fcg with the V-cycle in place of D^-1: M(r) = V r (+ the learned
+   correction P sigma s f(R r / s) when cnn is given); same fallback and judge */
+fem_gpu_status fem_gpu_fcg_mg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                              const double* b, double* x, fem_mg* mg, fem_cnn* cnn, int32_t factor,
+                              const double* node_density, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report,
+                              int32_t* used_fallback);
+/* truncation depth m of FCG(m) (1..16, default 8) and the stagnation window
+   (iterations without a 10 % residual reduction before the Jacobi-PCG
+   fallback, default 200) of fem_gpu_fcg / fem_gpu_fcg_mg; process-wide */
+fem_gpu_status fem_gpu_fcg_config(int32_t depth, int32_t window);
+
 /* autotuner: times every kernel variant of each bulk set on (up to
    max_elements, <= 0 = all) of its elements, assembling into scratch
    buffers, and keeps the fastest per set.  Setup-time call; optional. */

@@ -59,6 +59,11 @@ class PcgReport(C.Structure):
     _fields_ = [("iterations", I32), ("converged", I32), ("rel_residual", D), ("seconds", D)]
 
 
+class MgOpts(C.Structure):
+    _fields_ = [("coarse_max", I32), ("degree", I32), ("lo_frac", D), ("hi_frac", D), ("power_iters", I32),
+                ("fp32_levels", I32)]
+
+
 # name -> (restype, argtypes); this list is also the ABI surface the tests
 # check against include/fem_gpu.h
 SIGNATURES = {
@@ -119,6 +124,16 @@ SIGNATURES = {
     "fem_lpc_restrict": (I32, [I32, I32, P, P, P, P]),
     "fem_lpc_inject": (I32, [I32, I32, P, D, P]),
     "fem_gpu_fcg": (I32, [P, P, P, P, P, P, P, I32, P, P, P, P]),
+    "fem_gpu_fcg_mg": (I32, [P, P, P, P, P, P, P, P, I32, P, P, P, P]),
+    "fem_gpu_fcg_config": (I32, [I32, I32]),
+    "fem_mg_default_opts": (I32, [P]),
+    "fem_mg_create": (I32, [P, P, P, P, P, P]),
+    "fem_mg_destroy": (I32, [P]),
+    "fem_mg_num_levels": (I32, [P]),
+    "fem_mg_setup_seconds": (D, [P]),
+    "fem_mg_level_info": (I32, [P, I32, P, P]),
+    "fem_mg_get_stencil": (I32, [P, I32, P]),
+    "fem_mg_apply": (I32, [P, P, P]),
     "fem_gpu_autotune": (I32, [P, I64]),
     "fem_gpu_get_variant": (I32, [P, I32, P, P, P]),
     "fem_gpu_set_variant": (I32, [P, I32, I32]),

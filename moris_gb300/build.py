@@ -19,7 +19,8 @@ LIB = os.path.join(OUT, "libfem_gpu.so")
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRCS = ["fem_tables.cpp", "fem_host.cpp", "fem_xtk.cpp"]
-CUDA_SRCS = ["fem_device.cu", "fem_solver.cu", "fem_probe.cu", "fem_learned_pc.cu", "fem_cluster.cu", "fem_sensitivity.cu"]
+CUDA_SRCS = ["fem_device.cu", "fem_solver.cu", "fem_probe.cu", "fem_learned_pc.cu", "fem_cluster.cu", "fem_sensitivity.cu",
+             "fem_multigrid.cu"]
 
 
 def _nvcc():

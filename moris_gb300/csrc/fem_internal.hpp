@@ -134,3 +134,6 @@ fem_gpu_status assemble_set(fem_gpu_ctx* c, int set, const double* u, double* va
 // device memory of the sensitivity path (fem_sensitivity.cu)
 void sensitivity_release(fem_gpu_ctx* c);
 }  // namespace fem
+
+// one multigrid V-cycle z = V r on the legacy default stream (fem_multigrid.cu)
+bool mg_vcycle(fem_mg* g, const double* r, double* z);

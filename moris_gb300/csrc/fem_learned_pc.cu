@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "fem_internal.hpp"
+#include "fem_spmv.cuh"
 
 namespace {
 
@@ -571,15 +572,14 @@ __device__ void block_sum_add(double v, double* out) {
 
 __global__ void fcg_spmv_dot(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* p,
                              double* q, double* dot) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int sub = threadIdx.x % fem::kLanesPerRow;
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / fem::kLanesPerRow;
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / fem::kLanesPerRow;
     double acc = 0.0;
-    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-        double s = 0.0;
-        const int k1 = __ldg(rp + row + 1);
-        for (int k = __ldg(rp + row) + lane; k < k1; k += 32) s = fma(__ldg(v + k), __ldg(p + __ldg(ci + k)), s);
-        s = warp_sum_d(s);
-        if (lane == 0) {
+    for (int64_t base = first; base < n; base += groups) {  // uniform trip count per warp
+        const int64_t row = base + (threadIdx.x & 31) / fem::kLanesPerRow;
+        const double s = fem::csr_row_dot(n, rp, ci, v, p, row, sub);
+        if (sub == 0 && row < n) {
             q[row] = s;
             acc = fma(s, p[row], acc);
         }
@@ -615,14 +615,14 @@ __global__ void fcg_diag_inv(int64_t n, const int32_t* rp, const int32_t* ci, co
 
 __global__ void fcg_residual(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* b,
                              const double* x, double* r, double* dots) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int sub = threadIdx.x % fem::kLanesPerRow;
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / fem::kLanesPerRow;
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / fem::kLanesPerRow;
     double rr = 0.0, bb = 0.0;
-    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-        double s = 0.0;
-        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) s = fma(v[k], x[ci[k]], s);
-        s = warp_sum_d(s);
-        if (lane == 0) {
+    for (int64_t base = first; base < n; base += groups) {
+        const int64_t row = base + (threadIdx.x & 31) / fem::kLanesPerRow;
+        const double s = fem::csr_row_dot(n, rp, ci, v, x, row, sub);
+        if (sub == 0 && row < n) {
             const double ri = b[row] - s;
             r[row] = ri;
             rr = fma(ri, ri, rr);
@@ -726,18 +726,30 @@ fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e_dev, d
                : FEM_GPU_CUDA_ERROR;
 }
 
+static int g_fcg_depth = 8, g_fcg_window = 200;
+
+fem_gpu_status fem_gpu_fcg_config(int32_t depth, int32_t window) {
+    if (depth < 1 || depth > kMaxM - 1 || window < 1) return FEM_GPU_BAD_ARG;
+    g_fcg_depth = depth;
+    g_fcg_window = window;
+    return FEM_GPU_OK;
+}
+
 /* Truncated flexible CG, FCG(m) (Y. Notay, SIAM J. Sci. Comput. 22 (2000)),
-   with M(r) = D^-1 r + P sigma f(R r / s) s: each preconditioned residual is
+   with M(r) = B r + P sigma f(R r / s) s, B = D^-1 (fem_gpu_fcg) or one
+   multigrid V-cycle (fem_gpu_fcg_mg): each preconditioned residual is
    A-orthogonalised against the last m search directions, so the energy norm
    of the error decreases monotonically for any correction f (for a fixed
    SPD M the method is PCG).  Plain Jacobi-PCG is the fallback: on breakdown
    (non-positive p.Ap, NaN) or stagnation (no 10 % residual reduction within
-   200 iterations) the solve continues with fem_gpu_pcg from the current
+   `window` iterations) the solve continues with fem_gpu_pcg from the current
    iterate; the final relative residual is recomputed from b - A x.
-   cnn == NULL runs the same loop with M = D^-1. */
-fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
-                           const double* b, double* x, fem_cnn* cnn, int32_t factor, const double* node_density,
-                           const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep, int32_t* used_fallback) {
+   cnn == NULL runs the same loop with M = B.  m and window:
+   fem_gpu_fcg_config. */
+static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                              const double* b, double* x, fem_mg* mg, fem_cnn* cnn, int32_t factor,
+                              const double* node_density, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep,
+                              int32_t* used_fallback) {
     if (!c || !rowptr || !colidx || !vals || !b || !x || !opts) return FEM_GPU_BAD_ARG;
     if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
     const int64_t n = c->num_used * c->dim;
@@ -748,7 +760,12 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
             (nf - 1) / factor + 1 != cnn->n)
             return fail(c, FEM_GPU_BAD_ARG, "fcg: learned correction needs a cubic node grid matching the net");
     }
-    const int M = 8;  // truncation depth
+    if (mg) {
+        int32_t n0 = 0;
+        if (fem_mg_level_info(mg, 0, &n0, nullptr) != FEM_GPU_OK || (int64_t)n0 * n0 * n0 != nu || c->dim != 3)
+            return fail(c, FEM_GPU_BAD_ARG, "fcg: multigrid hierarchy does not match the model");
+    }
+    const int M = g_fcg_depth;  // truncation depth
     const auto t0 = std::chrono::steady_clock::now();
     double *r, *z, *dinv, *dots, *P, *Q;
     float *cin = nullptr, *cout = nullptr;
@@ -777,7 +794,7 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
         return fail(c, FEM_GPU_OUT_OF_MEMORY, "fcg workspace");
     }
     const int tpb = 256;
-    const unsigned rb = (unsigned)std::min<int64_t>((n * 32 + tpb - 1) / tpb, 152 * 16);
+    const unsigned rb = (unsigned)std::min<int64_t>((n * fem::kLanesPerRow + tpb - 1) / tpb, 152 * 16);
     const unsigned vb = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
     double hd[kMaxM];
     auto readn = [&](int k) {
@@ -786,7 +803,11 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
     };
     const int nc = cnn ? cnn->n : 0;
     auto apply_m = [&]() -> bool {
-        fcg_jacobi<<<vb, tpb>>>(n, dinv, r, z);
+        if (mg) {
+            if (!mg_vcycle(mg, r, z)) return false;
+        } else {
+            fcg_jacobi<<<vb, tpb>>>(n, dinv, r, z);
+        }
         if (!cnn) return true;
         double s = 0.0;
         if (fem_lpc_restrict(nf, factor, r, node_density, cin, &s) != FEM_GPU_OK) return false;
@@ -851,7 +872,7 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
         if (rn < 0.9 * best) {
             best = rn;
             since_best = 0;
-        } else if (++since_best > 200) {
+        } else if (++since_best > g_fcg_window) {
             fallback = 1;
             break;
         }
@@ -886,6 +907,20 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t*
     if (used_fallback) *used_fallback = fallback;
     if (st != FEM_GPU_OK && st != FEM_GPU_NOT_CONVERGED) return st;
     return true_rel <= opts->rel_tol * 1.0001 ? FEM_GPU_OK : fail(c, FEM_GPU_NOT_CONVERGED, "fcg: not converged");
+}
+
+fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                           const double* b, double* x, fem_cnn* cnn, int32_t factor, const double* node_density,
+                           const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep, int32_t* used_fallback) {
+    return fcg_run(c, rowptr, colidx, vals, b, x, nullptr, cnn, factor, node_density, opts, rep, used_fallback);
+}
+
+fem_gpu_status fem_gpu_fcg_mg(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                              const double* b, double* x, fem_mg* mg, fem_cnn* cnn, int32_t factor,
+                              const double* node_density, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep,
+                              int32_t* used_fallback) {
+    if (!mg) return fail(c, FEM_GPU_BAD_ARG, "fcg_mg: no multigrid hierarchy");
+    return fcg_run(c, rowptr, colidx, vals, b, x, mg, cnn, factor, node_density, opts, rep, used_fallback);
 }
 
 }  // extern "C"

@@ -1,0 +1,657 @@
+// fem_multigrid.cu -- geometric multigrid V-cycle for the assembled operator of
+// a uniform linear-B-spline hex mesh (the config-5 SIMP solves).
+//
+// The reference offers a PETSc PCMG preconditioner (Preconditioner_PETSc::
+// build_multigrid_preconditioner, SOL/DLA/src/cl_DLA_Preconditioner_PETSc.cpp:
+// 77-345): a multiplicative V-cycle with Galerkin coarse operators
+// A_(l+1) = P^T A_l P (PC_MG_GALERKIN_BOTH), prolongations from the B-spline
+// two-scale relation (Geometric_Multigrid, SOL/DLA/src/cl_DLA_Geometric_
+// Multigrid.cpp:47-121, HMR get_fine_basis_weights_of_basis), SOR smoothing
+// and an LU coarse solve.  The same preconditioner, laid out for the GPU:
+//
+//   * levels l = 0..L of node grids n_l^3, n_(l+1) = (n_l - 1) / 2 + 1.  The
+//     linear B-spline two-scale relation is trilinear interpolation: coarse
+//     node I weighs fine node i by prod_d (1 - |i_d - 2 I_d| / 2);
+//   * every operator is a 27-point block stencil S[k][f][g][node]
+//     (tap k = (dx+1) + 3 (dy+1) + 9 (dz+1); f, g displacement components)
+//     with the node index fastest, so a warp reads 32 consecutive nodes of one
+//     coefficient; level 0 is scattered from the CSR, level l+1 = P^T S_l P is
+//     formed on the device (one thread per coarse node and component pair,
+//     the 27 x 27 fine offset pairs unrolled so that the 27 coarse taps stay
+//     in registers);
+//   * smoothing is Chebyshev-accelerated point Jacobi of degree `degree` on
+//     [lo, hi] * lambda_max(D^-1 A) (lambda_max by power iteration): SOR is
+//     sequential, a polynomial in D^-1 A is one stencil sweep per degree.  Pre-
+//     and post-smoothing use the same polynomial, so the V-cycle is a
+//     symmetric positive definite operator;
+//   * the coarsest level (n_L <= coarse_max) is solved with its dense inverse,
+//     formed by Gauss-Jordan elimination on the device (the operator is SPD,
+//     so no pivoting).
+// Vectors are type-major like the adof vector: v[g n_l^3 + node].  All work
+// is issued on the legacy default stream, like fem_gpu_fcg.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fem_internal.hpp"
+
+using fem::fail;
+
+namespace {
+
+__host__ __device__ __forceinline__ int64_t sidx(int k, int f, int g, int64_t N, int64_t i) {
+    return (int64_t)((k * 3 + f) * 3 + g) * N + i;
+}
+
+__device__ __forceinline__ double mg_warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ void mg_block_sum_add(double v, double* out) {
+    __shared__ double red[32];
+    v = mg_warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+        v = mg_warp_sum(v);
+        if (lane == 0) atomicAdd(out, v);
+    }
+}
+
+// level-0 stencil from the CSR of the assembled operator (one thread per row);
+// err |= 1 for a column outside the 27-node neighbourhood
+__global__ void mg_csr_to_stencil(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                  const double* __restrict__ v, double* __restrict__ S, int* err) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < 3 * N;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(row / N);
+        const int64_t i = row - f * N;
+        const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
+        for (int e = rp[row]; e < rp[row + 1]; ++e) {
+            const int64_t col = ci[e];
+            const int g = (int)(col / N);
+            const int64_t j = col - g * N;
+            const int dx = (int)(j % n) - ix, dy = (int)((j / n) % n) - iy, dz = (int)(j / ((int64_t)n * n)) - iz;
+            if (g < 0 || g > 2 || dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+                atomicOr(err, 1);
+                continue;
+            }
+            S[sidx((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1), f, g, N, i)] = v[e];
+        }
+    }
+}
+
+__global__ void mg_to_float(int64_t count, const double* __restrict__ a, float* __restrict__ b) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
+        b[t] = (float)a[t];
+}
+
+__global__ void mg_diag_inv(int64_t N, const double* __restrict__ S, double* __restrict__ dinv) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 3 * N; t += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(t / N);
+        const double d = S[sidx(13, f, f, N, t - f * N)];
+        dinv[t] = d != 0.0 ? 1.0 / d : 0.0;
+    }
+}
+
+// s[f] = sum_k sum_g S[k][f][g][i] x[g][i + off_k] for the three rows of node i
+template <typename TS>
+__device__ __forceinline__ void stencil_rows(int n, int64_t N, const TS* __restrict__ S, const double* __restrict__ x,
+                                             int64_t i, double s[3]) {
+    const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
+    s[0] = s[1] = s[2] = 0.0;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz) {
+        if (iz + dz < 0 || iz + dz >= n) continue;
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+            if (iy + dy < 0 || iy + dy >= n) continue;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                if (ix + dx < 0 || ix + dx >= n) continue;
+                const int k = (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+                const int64_t j = i + dx + (int64_t)n * (dy + (int64_t)n * dz);
+#pragma unroll
+                for (int g = 0; g < 3; ++g) {
+                    const double xg = __ldg(x + g * N + j);
+#pragma unroll
+                    for (int f = 0; f < 3; ++f) s[f] = fma((double)__ldg(S + sidx(k, f, g, N, i)), xg, s[f]);
+                }
+            }
+        }
+    }
+}
+
+// power iteration step: y = D^-1 A x; dots[0] += y.y
+template <typename TS>
+__global__ void mg_power(int n, const TS* __restrict__ S, const double* __restrict__ dinv, const double* __restrict__ x,
+                         double* __restrict__ y, double* dots) {
+    const int64_t N = (int64_t)n * n * n;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double s[3];
+        stencil_rows(n, N, S, x, i, s);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const double v = dinv[f * N + i] * s[f];
+            y[f * N + i] = v;
+            acc = fma(v, v, acc);
+        }
+    }
+    mg_block_sum_add(acc, dots);
+}
+
+__global__ void mg_scale(int64_t m, double a, const double* __restrict__ y, double* __restrict__ x) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] = a * y[t];
+}
+
+// splitmix64 uniform in [-0.5, 0.5): element t of the stream of `seed`
+__global__ void mg_random(int64_t m, uint64_t seed, double* __restrict__ x) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t z = seed + (uint64_t)(t + 1) * 0x9E3779B97F4A7C15ULL;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        x[t] = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    }
+}
+
+// Chebyshev start with x = 0: r = b, d = D^-1 b / theta, x = d
+__global__ void mg_cheb_init(int64_t m, const double* __restrict__ b, const double* __restrict__ dinv, double inv_theta,
+                             double* __restrict__ r, double* __restrict__ d, double* __restrict__ x) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+        const double bt = b[t];
+        const double dt = dinv[t] * bt * inv_theta;
+        r[t] = bt;
+        d[t] = dt;
+        x[t] = dt;
+    }
+}
+
+// Chebyshev step: r -= A din; dout = c1 din + c2 D^-1 r; x += dout
+template <typename TS>
+__global__ void mg_cheb_step(int n, const TS* __restrict__ S, const double* __restrict__ din, double* __restrict__ r,
+                             const double* __restrict__ dinv, double c1, double c2, double* __restrict__ dout,
+                             double* __restrict__ x) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double s[3];
+        stencil_rows(n, N, S, din, i, s);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const int64_t t = f * N + i;
+            const double rt = r[t] - s[f];
+            const double dt = fma(c1, din[t], c2 * dinv[t] * rt);
+            r[t] = rt;
+            dout[t] = dt;
+            x[t] += dt;
+        }
+    }
+}
+
+// r -= A d
+template <typename TS>
+__global__ void mg_residual_update(int n, const TS* __restrict__ S, const double* __restrict__ d, double* __restrict__ r) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double s[3];
+        stencil_rows(n, N, S, d, i, s);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) r[f * N + i] -= s[f];
+    }
+}
+
+// first post-smoothing step after the coarse correction e:
+// r -= A e; d = D^-1 r / theta; x += e + d
+template <typename TS>
+__global__ void mg_post_first(int n, const TS* __restrict__ S, const double* __restrict__ e, double* __restrict__ r,
+                              const double* __restrict__ dinv, double inv_theta, double* __restrict__ d,
+                              double* __restrict__ x) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double s[3];
+        stencil_rows(n, N, S, e, i, s);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            const int64_t t = f * N + i;
+            const double rt = r[t] - s[f];
+            const double dt = dinv[t] * rt * inv_theta;
+            r[t] = rt;
+            d[t] = dt;
+            x[t] += e[t] + dt;
+        }
+    }
+}
+
+// full-weighting restriction bc = P^T r (fine grid nf = 2 (nc - 1) + 1)
+__global__ void mg_restrict(int nf, int nc, const double* __restrict__ r, double* __restrict__ bc) {
+    const int64_t Nc = (int64_t)nc * nc * nc, Nf = (int64_t)nf * nf * nf;
+    for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < Nc; I += (int64_t)gridDim.x * blockDim.x) {
+        const int X = (int)(I % nc), Y = (int)((I / nc) % nc), Z = (int)(I / ((int64_t)nc * nc));
+        double s[3] = {0.0, 0.0, 0.0};
+        for (int az = -1; az <= 1; ++az) {
+            const int z = 2 * Z + az;
+            if (z < 0 || z >= nf) continue;
+            for (int ay = -1; ay <= 1; ++ay) {
+                const int y = 2 * Y + ay;
+                if (y < 0 || y >= nf) continue;
+                for (int ax = -1; ax <= 1; ++ax) {
+                    const int x = 2 * X + ax;
+                    if (x < 0 || x >= nf) continue;
+                    const double w = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
+                    const int64_t i = x + (int64_t)nf * (y + (int64_t)nf * z);
+                    for (int g = 0; g < 3; ++g) s[g] = fma(w, r[g * Nf + i], s[g]);
+                }
+            }
+        }
+        for (int g = 0; g < 3; ++g) bc[g * Nc + I] = s[g];
+    }
+}
+
+// trilinear prolongation e = P xc
+__global__ void mg_prolong(int nf, int nc, const double* __restrict__ xc, double* __restrict__ e) {
+    const int64_t Nc = (int64_t)nc * nc * nc, Nf = (int64_t)nf * nf * nf;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nf; i += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nf), y = (int)((i / nf) % nf), z = (int)(i / ((int64_t)nf * nf));
+        const int x0 = x >> 1, y0 = y >> 1, z0 = z >> 1;
+        const int x1 = x0 + (x & 1), y1 = y0 + (y & 1), z1 = z0 + (z & 1);
+        const double wx = (x & 1) ? 0.5 : 1.0, wy = (y & 1) ? 0.5 : 1.0, wz = (z & 1) ? 0.5 : 1.0;
+        for (int g = 0; g < 3; ++g) {
+            const double* c = xc + g * Nc;
+            auto at = [&](int a, int b, int cc) { return c[a + (int64_t)nc * (b + (int64_t)nc * cc)]; };
+            double s = at(x0, y0, z0);
+            if (x & 1) s += at(x1, y0, z0);
+            if (y & 1) {
+                double t = at(x0, y1, z0);
+                if (x & 1) t += at(x1, y1, z0);
+                s += t;
+            }
+            if (z & 1) {
+                double t = at(x0, y0, z1);
+                if (x & 1) t += at(x1, y0, z1);
+                if (y & 1) {
+                    double u = at(x0, y1, z1);
+                    if (x & 1) u += at(x1, y1, z1);
+                    t += u;
+                }
+                s += t;
+            }
+            e[g * Nf + i] = s * wx * wy * wz;
+        }
+    }
+}
+
+// Galerkin product Sc = P^T Sf P, one thread per (coarse node, f, g): for fine
+// offsets a (coarse node I -> fine node 2I + a, weight w_a) and stencil taps b
+// (fine node j = 2I + a + b), the fine column j interpolates from the coarse
+// nodes J = I + kc with |a + b - 2 kc| <= 1 per direction (weight 1 for an
+// even sum, 1/2 for each of the two neighbours of an odd one).
+__device__ __forceinline__ int ntarget(int s) { return (s & 1) ? 2 : 1; }
+__device__ __forceinline__ int target(int s, int t) { return (s & 1) ? ((s - 1) >> 1) + t : (s >> 1); }
+
+__global__ void __launch_bounds__(128) mg_rap(int nf, int nc, const double* __restrict__ Sf, double* __restrict__ Sc) {
+    const int64_t Nc = (int64_t)nc * nc * nc, Nf = (int64_t)nf * nf * nf;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 9 * Nc; t += (int64_t)gridDim.x * blockDim.x) {
+        const int fg = (int)(t / Nc);
+        const int64_t I = t - fg * Nc;
+        const int f = fg / 3, g = fg % 3;
+        const int X = (int)(I % nc), Y = (int)((I / nc) % nc), Z = (int)(I / ((int64_t)nc * nc));
+        double acc[27];
+#pragma unroll
+        for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+#pragma unroll
+        for (int az = -1; az <= 1; ++az) {
+            const int z = 2 * Z + az;
+            if (z < 0 || z >= nf) continue;
+#pragma unroll
+            for (int ay = -1; ay <= 1; ++ay) {
+                const int y = 2 * Y + ay;
+                if (y < 0 || y >= nf) continue;
+#pragma unroll
+                for (int ax = -1; ax <= 1; ++ax) {
+                    const int x = 2 * X + ax;
+                    if (x < 0 || x >= nf) continue;
+                    const double wa = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
+                    const int64_t i = x + (int64_t)nf * (y + (int64_t)nf * z);
+#pragma unroll
+                    for (int bz = -1; bz <= 1; ++bz)
+#pragma unroll
+                        for (int by = -1; by <= 1; ++by)
+#pragma unroll
+                            for (int bx = -1; bx <= 1; ++bx) {
+                                const int kb = (bx + 1) + 3 * (by + 1) + 9 * (bz + 1);
+                                const double v = wa * __ldg(Sf + sidx(kb, f, g, Nf, i));
+                                const int sx = ax + bx, sy = ay + by, sz = az + bz;
+                                const double pw = ((sx & 1) ? 0.5 : 1.0) * ((sy & 1) ? 0.5 : 1.0) *
+                                                  ((sz & 1) ? 0.5 : 1.0);
+                                const double vp = v * pw;
+#pragma unroll
+                                for (int tz = 0; tz < 2; ++tz) {
+                                    if (tz >= ntarget(sz)) continue;
+#pragma unroll
+                                    for (int ty = 0; ty < 2; ++ty) {
+                                        if (ty >= ntarget(sy)) continue;
+#pragma unroll
+                                        for (int tx = 0; tx < 2; ++tx) {
+                                            if (tx >= ntarget(sx)) continue;
+                                            const int kc = (target(sx, tx) + 1) + 3 * (target(sy, ty) + 1) +
+                                                           9 * (target(sz, tz) + 1);
+                                            acc[kc] += vp;
+                                        }
+                                    }
+                                }
+                            }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 27; ++k) Sc[sidx(k, f, g, Nc, I)] = acc[k];
+    }
+}
+
+// dense operator of the coarsest level, row-major m x m (m = 3 N)
+__global__ void mg_dense(int n, const double* __restrict__ S, double* __restrict__ A) {
+    const int64_t N = (int64_t)n * n * n, m = 3 * N;
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < m; row += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(row / N);
+        const int64_t i = row - f * N;
+        const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
+        for (int k = 0; k < 27; ++k) {
+            const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+            if (ix + dx < 0 || ix + dx >= n || iy + dy < 0 || iy + dy >= n || iz + dz < 0 || iz + dz >= n) continue;
+            const int64_t j = i + dx + (int64_t)n * (dy + (int64_t)n * dz);
+            for (int g = 0; g < 3; ++g) A[row * m + g * N + j] = S[sidx(k, f, g, N, i)];
+        }
+    }
+}
+
+// Gauss-Jordan inversion in place, pivot k: stash row k and column k, then
+// update every entry (a[k][k] > 0 for an SPD operator)
+__global__ void mg_gj_stash(int64_t m, const double* __restrict__ A, int64_t k, double* __restrict__ row,
+                            double* __restrict__ col) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
+        row[t] = A[k * m + t];
+        col[t] = A[t * m + k];
+    }
+}
+__global__ void mg_gj_update(int64_t m, double* __restrict__ A, int64_t k, const double* __restrict__ row,
+                             const double* __restrict__ col) {
+    const double inv = 1.0 / row[k];
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m * m; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / m, j = t - i * m;
+        const double rk = (j == k ? 1.0 : row[j]) * inv;
+        if (i == k) A[t] = rk;
+        else A[t] = (j == k ? 0.0 : A[t]) - col[i] * rk;
+    }
+}
+
+// x = Ainv b, one warp per row
+__global__ void mg_gemv(int64_t m, const double* __restrict__ A, const double* __restrict__ b, double* __restrict__ x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < m; row += warps) {
+        double s = 0.0;
+        for (int64_t j = lane; j < m; j += 32) s = fma(A[row * m + j], b[j], s);
+        s = mg_warp_sum(s);
+        if (lane == 0) x[row] = s;
+    }
+}
+
+unsigned blocks_for(int64_t work, int tpb) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + tpb - 1) / tpb, 152 * 32));
+}
+
+}  // namespace
+
+struct fem_mg {
+    struct Level {
+        int n = 0;
+        int64_t N = 0;
+        double* S = nullptr;    // FP64 stencil
+        float* S32 = nullptr;   // FP32 copy used by the smoother (or null)
+        double* dinv = nullptr;
+        double lmax = 0.0;
+        double *x = nullptr, *b = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
+    };
+    std::vector<Level> lv;
+    double* ainv = nullptr;  // dense inverse of the coarsest operator
+    int64_t m = 0;
+    fem_mg_opts o{};
+    double setup_seconds = 0.0;
+    double* dots = nullptr;
+    int* err = nullptr;
+    std::vector<void*> bufs;
+    ~fem_mg() {
+        cudaDeviceSynchronize();
+        for (void* p : bufs) cudaFree(p);
+    }
+    template <typename T>
+    bool alloc(T** p, size_t count) {
+        if (cudaMalloc((void**)p, count * sizeof(T)) != cudaSuccess) return false;
+        bufs.push_back(*p);
+        return true;
+    }
+};
+
+namespace {
+
+constexpr int kTpb = 256;
+
+template <typename TS>
+void smooth_pre(const fem_mg::Level& L, const TS* S, const fem_mg_opts& o, const double* b, double* x) {
+    const double lo = o.lo_frac * L.lmax, hi = o.hi_frac * L.lmax;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    const unsigned vb = blocks_for(3 * L.N, kTpb), nb = blocks_for(L.N, kTpb);
+    mg_cheb_init<<<vb, kTpb>>>(3 * L.N, b, L.dinv, 1.0 / theta, L.r, L.d0, x);
+    double rho = 1.0 / sigma;
+    double *din = L.d0, *dout = L.d1;
+    for (int k = 1; k < o.degree; ++k) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        mg_cheb_step<TS><<<nb, kTpb>>>(L.n, S, din, L.r, L.dinv, rn * rho, 2.0 * rn / delta, dout, x);
+        rho = rn;
+        std::swap(din, dout);
+    }
+    mg_residual_update<TS><<<nb, kTpb>>>(L.n, S, din, L.r);
+}
+
+// e (the prolongated coarse correction) lives in d1: the first step reads it and
+// writes d0, after which d1 is free for the ping-pong
+template <typename TS>
+void smooth_post(const fem_mg::Level& L, const TS* S, const fem_mg_opts& o, const double* e, double* x) {
+    const double lo = o.lo_frac * L.lmax, hi = o.hi_frac * L.lmax;
+    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+    const unsigned nb = blocks_for(L.N, kTpb);
+    double *din = L.d0, *dout = L.d1;
+    mg_post_first<TS><<<nb, kTpb>>>(L.n, S, e, L.r, L.dinv, 1.0 / theta, din, x);
+    double rho = 1.0 / sigma;
+    for (int k = 1; k < o.degree; ++k) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        mg_cheb_step<TS><<<nb, kTpb>>>(L.n, S, din, L.r, L.dinv, rn * rho, 2.0 * rn / delta, dout, x);
+        rho = rn;
+        std::swap(din, dout);
+    }
+}
+
+// x_l = V_l(b_l)
+void vcycle(fem_mg* g, size_t l, const double* b, double* x) {
+    fem_mg::Level& L = g->lv[l];
+    if (l + 1 == g->lv.size()) {
+        mg_gemv<<<blocks_for(g->m * 32, kTpb), kTpb>>>(g->m, g->ainv, b, x);
+        return;
+    }
+    if (L.S32) smooth_pre<float>(L, L.S32, g->o, b, x);
+    else smooth_pre<double>(L, L.S, g->o, b, x);
+    fem_mg::Level& C = g->lv[l + 1];
+    mg_restrict<<<blocks_for(C.N, kTpb), kTpb>>>(L.n, C.n, L.r, C.b);
+    vcycle(g, l + 1, C.b, C.x);
+    double* e = L.d1;
+    mg_prolong<<<blocks_for(L.N, kTpb), kTpb>>>(L.n, C.n, C.x, e);
+    if (L.S32) smooth_post<float>(L, L.S32, g->o, e, x);
+    else smooth_post<double>(L, L.S, g->o, e, x);
+}
+
+}  // namespace
+
+bool mg_vcycle(fem_mg* g, const double* r, double* z) {
+    if (!g) return false;
+    vcycle(g, 0, r, z);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+extern "C" {
+
+fem_gpu_status fem_mg_default_opts(fem_mg_opts* o) {
+    if (!o) return FEM_GPU_BAD_ARG;
+    o->coarse_max = 9;
+    o->degree = 2;
+    o->lo_frac = 0.1;
+    o->hi_frac = 1.1;
+    o->power_iters = 12;
+    o->fp32_levels = 0;
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                             const fem_mg_opts* opts, fem_mg** out) {
+    if (!c || !rowptr || !colidx || !vals || !out) return FEM_GPU_BAD_ARG;
+    *out = nullptr;
+    if (!c->host_final) return FEM_GPU_NOT_FINALIZED;
+    fem_mg_opts o;
+    fem_mg_default_opts(&o);
+    if (opts) o = *opts;
+    if (o.degree < 1 || o.degree > 8 || !(o.lo_frac > 0.0) || !(o.hi_frac > o.lo_frac) || o.power_iters < 1 ||
+        o.coarse_max < 3 || o.coarse_max > 9 || o.fp32_levels < 0)
+        return fail(c, FEM_GPU_BAD_ARG, "multigrid: options out of range");
+    const int64_t nu = c->num_used;
+    const int nf = (int)std::llround(std::cbrt((double)nu));
+    if (c->dim != 3 || (int64_t)nf * nf * nf != nu)
+        return fail(c, FEM_GPU_BAD_ARG, "multigrid: needs a 3D model on a cubic node grid");
+    std::vector<int> ns{nf};
+    while (ns.back() > o.coarse_max) {
+        const int n = ns.back();
+        if ((n - 1) % 2) return fail(c, FEM_GPU_BAD_ARG, "multigrid: node grid edge - 1 must halve down to coarse_max");
+        ns.push_back((n - 1) / 2 + 1);
+    }
+    if (ns.size() < 2) return fail(c, FEM_GPU_BAD_ARG, "multigrid: grid already at or below coarse_max");
+    const auto t0 = std::chrono::steady_clock::now();
+    fem_mg* g = new fem_mg();
+    g->o = o;
+    g->lv.resize(ns.size());
+    bool ok = g->alloc(&g->dots, 4) && g->alloc(&g->err, 1);
+    for (size_t l = 0; ok && l < ns.size(); ++l) {
+        fem_mg::Level& L = g->lv[l];
+        L.n = ns[l];
+        L.N = (int64_t)L.n * L.n * L.n;
+        ok = g->alloc(&L.S, 243 * L.N) && g->alloc(&L.dinv, 3 * L.N) && g->alloc(&L.r, 3 * L.N) &&
+             g->alloc(&L.d0, 3 * L.N) && g->alloc(&L.d1, 3 * L.N);
+        if (ok && l > 0) ok = g->alloc(&L.x, 3 * L.N) && g->alloc(&L.b, 3 * L.N);
+        if (ok && (int)l < o.fp32_levels && l + 1 < ns.size()) ok = g->alloc(&L.S32, 243 * L.N);
+    }
+    g->m = 3 * g->lv.back().N;
+    double *row = nullptr, *col = nullptr;
+    if (ok) ok = g->alloc(&g->ainv, g->m * g->m) && g->alloc(&row, g->m) && g->alloc(&col, g->m);
+    if (!ok) {
+        delete g;
+        return fail(c, FEM_GPU_OUT_OF_MEMORY, "multigrid hierarchy");
+    }
+    // level 0 from the CSR, then the Galerkin products
+    fem_mg::Level& L0 = g->lv[0];
+    cudaMemset(L0.S, 0, 243 * L0.N * sizeof(double));
+    cudaMemset(g->err, 0, sizeof(int));
+    mg_csr_to_stencil<<<blocks_for(3 * L0.N, kTpb), kTpb>>>(L0.n, rowptr, colidx, vals, L0.S, g->err);
+    for (size_t l = 0; l + 1 < g->lv.size(); ++l)
+        mg_rap<<<blocks_for(9 * g->lv[l + 1].N, 128), 128>>>(g->lv[l].n, g->lv[l + 1].n, g->lv[l].S, g->lv[l + 1].S);
+    int herr = 0;
+    cudaMemcpy(&herr, g->err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (herr) {
+        delete g;
+        return fail(c, FEM_GPU_BAD_ARG, "multigrid: operator is not a 27-point nodal stencil on the node grid");
+    }
+    // smoother data: diagonal, FP32 copies, lambda_max(D^-1 A) by power iteration
+    for (size_t l = 0; l + 1 < g->lv.size(); ++l) {
+        fem_mg::Level& L = g->lv[l];
+        mg_diag_inv<<<blocks_for(3 * L.N, kTpb), kTpb>>>(L.N, L.S, L.dinv);
+        if (L.S32) mg_to_float<<<blocks_for(243 * L.N, kTpb), kTpb>>>(243 * L.N, L.S, L.S32);
+        mg_random<<<blocks_for(3 * L.N, kTpb), kTpb>>>(3 * L.N, 0x5EEDULL + l, L.d0);
+        double xn = 0.0;
+        {
+            // ||x0|| from the host copy of the seeded vector (small cost, setup only)
+            std::vector<double> h(3 * L.N);
+            cudaMemcpy(h.data(), L.d0, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+            for (double v : h) xn += v * v;
+            xn = std::sqrt(xn);
+        }
+        double lam = 0.0;
+        for (int it = 0; it < o.power_iters; ++it) {
+            cudaMemset(g->dots, 0, sizeof(double));
+            mg_power<double><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, L.S, L.dinv, L.d0, L.d1, g->dots);
+            double yy = 0.0;
+            cudaMemcpy(&yy, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
+            const double yn = std::sqrt(yy);
+            lam = yn / xn;
+            if (!(yn > 0.0)) break;
+            mg_scale<<<blocks_for(3 * L.N, kTpb), kTpb>>>(3 * L.N, 1.0 / yn, L.d1, L.d0);
+            xn = 1.0;
+        }
+        L.lmax = lam;
+        if (!(lam > 0.0) || !std::isfinite(lam)) {
+            delete g;
+            return fail(c, FEM_GPU_NONFINITE, "multigrid: power iteration gave no positive lambda_max");
+        }
+    }
+    // coarsest level: dense inverse
+    fem_mg::Level& LC = g->lv.back();
+    cudaMemset(g->ainv, 0, g->m * g->m * sizeof(double));
+    mg_dense<<<blocks_for(g->m, kTpb), kTpb>>>(LC.n, LC.S, g->ainv);
+    for (int64_t k = 0; k < g->m; ++k) {
+        mg_gj_stash<<<blocks_for(g->m, kTpb), kTpb>>>(g->m, g->ainv, k, row, col);
+        mg_gj_update<<<blocks_for(g->m * g->m, kTpb), kTpb>>>(g->m, g->ainv, k, row, col);
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        delete g;
+        return fail(c, FEM_GPU_CUDA_ERROR, "multigrid setup");
+    }
+    g->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *out = g;
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_mg_destroy(fem_mg* g) {
+    delete g;
+    return FEM_GPU_OK;
+}
+
+int32_t fem_mg_num_levels(const fem_mg* g) { return g ? (int32_t)g->lv.size() : 0; }
+
+double fem_mg_setup_seconds(const fem_mg* g) { return g ? g->setup_seconds : 0.0; }
+
+fem_gpu_status fem_mg_level_info(const fem_mg* g, int32_t level, int32_t* n, double* lambda_max) {
+    if (!g || level < 0 || level >= (int32_t)g->lv.size()) return FEM_GPU_BAD_ARG;
+    if (n) *n = g->lv[level].n;
+    if (lambda_max) *lambda_max = g->lv[level].lmax;
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_mg_get_stencil(const fem_mg* g, int32_t level, double* host_out) {
+    if (!g || !host_out || level < 0 || level >= (int32_t)g->lv.size()) return FEM_GPU_BAD_ARG;
+    const fem_mg::Level& L = g->lv[level];
+    return cudaMemcpy(host_out, L.S, 243 * L.N * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess
+               ? FEM_GPU_OK
+               : FEM_GPU_CUDA_ERROR;
+}
+
+fem_gpu_status fem_mg_apply(fem_mg* g, const double* r, double* z) {
+    if (!g || !r || !z) return FEM_GPU_BAD_ARG;
+    return mg_vcycle(g, r, z) ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
+}
+
+}  // extern "C"

@@ -3,7 +3,7 @@
 // AZ_Jacobi, SOL/DLA/src/cl_DLA_Linear_Solver_Aztec.cpp:260-355).
 //
 // One iteration is four launches on the context stream:
-//   k1  q = A p and the partial sums of p.q            (warp per CSR row)
+//   k1  q = A p and the partial sums of p.q            (4 lanes per CSR row)
 //   k2  alpha = rz/pq; x += alpha p; r -= alpha q; z = M^-1 r; sums of r.z, r.r
 //   k3  convergence test; beta = rz'/rz; p = z + beta p
 //   k4  (one thread) advance the iteration counter
@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "fem_internal.hpp"
+#include "fem_spmv.cuh"
 
 namespace {
 
@@ -77,14 +78,12 @@ __global__ void k_diag_inv(int64_t n, const int32_t* rp, const int32_t* ci, cons
 // r = b - A x ; z = M^-1 r ; p = z ; accumulate r.z, r.r, b.b into slot 0
 __global__ void k_init(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* b,
                        const double* x, double* r, double* z, double* p, const double* dinv, CgState* st) {
-    const int lane = threadIdx.x & 31;
-    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int sub = threadIdx.x % fem::kLanesPerRow;
+    const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / fem::kLanesPerRow;
     double rz = 0.0, rr = 0.0, bb = 0.0;
+    const double s = fem::csr_row_dot(n, rp, ci, v, x, row, sub);
     if (row < n) {
-        double s = 0.0;
-        for (int k = rp[row] + lane; k < rp[row + 1]; k += 32) s = fma(v[k], x[ci[k]], s);
-        s = warp_sum(s);
-        if (lane == 0) {
+        if (sub == 0) {
             const double ri = b[row] - s, zi = dinv[row] * ri;
             r[row] = ri;
             z[row] = zi;
@@ -107,15 +106,16 @@ __global__ void k_spmv_pq(int64_t n, const int32_t* rp, const int32_t* ci, const
                           double* q, CgState* st) {
     if (st->done) return;
     const int slot = st->it & 3;
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int sub = threadIdx.x % fem::kLanesPerRow;
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / fem::kLanesPerRow;
+    // the warp's first row; the trip count is uniform over the warp (the row
+    // reduction shuffles need all 32 lanes)
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / fem::kLanesPerRow;
     double pq = 0.0;
-    for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
-        double s = 0.0;
-        const int k1 = __ldg(rp + row + 1);
-        for (int k = __ldg(rp + row) + lane; k < k1; k += 32) s = fma(__ldg(v + k), __ldg(p + __ldg(ci + k)), s);
-        s = warp_sum(s);
-        if (lane == 0) {
+    for (int64_t base = first; base < n; base += groups) {
+        const int64_t row = base + (threadIdx.x & 31) / fem::kLanesPerRow;
+        const double s = fem::csr_row_dot(n, rp, ci, v, p, row, sub);
+        if (sub == 0 && row < n) {
             q[row] = s;
             pq = fma(s, p[row], pq);
         }
@@ -219,7 +219,7 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     dinv = q + n;
     cudaMemsetAsync(st, 0, sizeof(CgState), sm);
     const int tpb = 256;
-    const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned row_blocks = (unsigned)((n * fem::kLanesPerRow + tpb - 1) / tpb);
     const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, 152 * 16);
     const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
@@ -351,7 +351,7 @@ extern "C" fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* c, const int32_t* row
     cudaError_t e = cudaMemsetAsync(cs, 0, sizeof(CgState), sm);
     if (e != cudaSuccess) return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg_noalloc: ") + cudaGetErrorString(e));
     const int tpb = 256;
-    const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned row_blocks = (unsigned)((n * fem::kLanesPerRow + tpb - 1) / tpb);
     const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
                                                                 opts->preconditioner == 1);
@@ -416,7 +416,7 @@ extern "C" fem_gpu_status fem_gpu_pcg_snapshots(fem_gpu_ctx* c, const int32_t* r
     double *z = r + n, *p = z + n, *q = p + n, *dinv = q + n;
     cudaMemsetAsync(st, 0, sizeof(CgState), sm);
     const int tpb = 256;
-    const unsigned row_blocks = (unsigned)((n * 32 + tpb - 1) / tpb);
+    const unsigned row_blocks = (unsigned)((n * fem::kLanesPerRow + tpb - 1) / tpb);
     const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, 152 * 16);
     const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv, opts->preconditioner == 1);

@@ -424,11 +424,24 @@ fem_gpu_status fem_cnn_loss_grad(fem_cnn* cnn, const float* in4, const float* ta
 fem_gpu_status fem_cnn_train_step(fem_cnn* cnn, const float* in4, const float* target3, int32_t samples, float lr,
                                   double* loss);
 /* coarse input for a fine residual (node grid nf^3, coarsening factor F):
-   channels 0..2 = R r / ||R r||, channel 3 = log10(restricted density) / 3 */
+   channels 0..2 = R r / ||R r||, channel 3 = log10(restricted density) / 3;
+   ||R r|| is reduced on the device into a library-wide accumulator, so calls
+   must not overlap */
 fem_gpu_status fem_lpc_restrict(int32_t nf, int32_t factor, const double* r, const double* node_density, float* coarse4,
                                 double* scale);
 /* training target: fine field injected at the coarse nodes, / scale */
 fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e, double scale, float* target3);
+/* z += scale * P c: trilinear prolongation of a coarse 3-channel field
+   (channels-last [nc^3][3], nc = (nf - 1) / factor + 1) into a fine
+   type-major adof vector */
+fem_gpu_status fem_lpc_prolong_add(int32_t nf, int32_t factor, const float* coarse3, double scale, double* z);
+/* coarse3 = scale * P^T fine (the transpose of fem_lpc_prolong_add; the
+   gradient of a fine objective with respect to the net's output) */
+fem_gpu_status fem_lpc_prolong_transpose(int32_t nf, int32_t factor, const double* fine, double scale,
+                                         float* coarse3);
+/* y = A x on a CSR operator of n rows (device buffers) */
+fem_gpu_status fem_gpu_spmv(int64_t n, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                            const double* x, double* y);
 /* truncated flexible CG, FCG(8), with M(r) = D^-1 r + P sigma f(R r / s) s
    (cnn == NULL: M = D^-1); Jacobi-PCG is the fallback on breakdown or
    stagnation and the final residual is recomputed from b - A x.  Device
@@ -452,12 +465,12 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_
    legacy default stream. */
 typedef struct fem_mg fem_mg;
 typedef struct fem_mg_opts {
-    int32_t coarse_max;   /* coarsest node grid edge, 3..9 (default 9) */
+    int32_t coarse_max;   /* coarsest node grid edge, 3..9 (default 5) */
     int32_t degree;       /* Chebyshev degree of pre- and post-smoothing, 1..8 (2) */
     double lo_frac;       /* smoothing interval [lo_frac, hi_frac] * lambda_max(D^-1 A) (0.1, 1.1) */
     double hi_frac;
     int32_t power_iters;  /* power iterations for lambda_max (12) */
-    int32_t fp32_levels;  /* levels 0..fp32_levels-1 smooth with an FP32 copy of the stencil (0) */
+    int32_t fp32_levels;  /* levels 0..fp32_levels-1 smooth in FP32 (FP32 stencil copy and vectors) (2) */
 } fem_mg_opts;
 fem_gpu_status fem_mg_default_opts(fem_mg_opts* opts);
 /* builds the hierarchy from the assembled CSR (device); opts NULL = defaults */

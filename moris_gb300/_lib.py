@@ -123,6 +123,9 @@ SIGNATURES = {
     "fem_cnn_train_step": (I32, [P, P, P, I32, C.c_float, P]),
     "fem_lpc_restrict": (I32, [I32, I32, P, P, P, P]),
     "fem_lpc_inject": (I32, [I32, I32, P, D, P]),
+    "fem_lpc_prolong_add": (I32, [I32, I32, P, D, P]),
+    "fem_lpc_prolong_transpose": (I32, [I32, I32, P, D, P]),
+    "fem_gpu_spmv": (I32, [I64, P, P, P, P, P]),
     "fem_gpu_fcg": (I32, [P, P, P, P, P, P, P, I32, P, P, P, P]),
     "fem_gpu_fcg_mg": (I32, [P, P, P, P, P, P, P, P, I32, P, P, P, P]),
     "fem_gpu_fcg_config": (I32, [I32, I32]),

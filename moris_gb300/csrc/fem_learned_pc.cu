@@ -248,6 +248,7 @@ struct fem_cnn {
     double* loss = nullptr;
     int64_t step = 0;
     cudaStream_t stream = nullptr;
+    cudaEvent_t ready = nullptr;  // joins the net's stream to the legacy default stream
     bool dirty = true;        // bf16 copies need refresh
     double out_scale = 1.0;   // the correction applied by fem_gpu_fcg is out_scale * f
 };
@@ -294,6 +295,13 @@ void cnn_backward(fem_cnn* c, int nb) {
     }
 }
 
+// the net runs on its own stream; its inputs are produced on the legacy default
+// stream (torch's default, the solver kernels): wait for that work first
+void after_default_stream(fem_cnn* c) {
+    cudaEventRecord(c->ready, 0);
+    cudaStreamWaitEvent(c->stream, c->ready, 0);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -334,6 +342,7 @@ fem_gpu_status fem_cnn_create(int32_t n, int32_t batch_max, uint64_t seed, fem_c
         }
     }
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ready, cudaEventDisableTiming);
     const int64_t nw = c->off[kLayers];
     const int64_t vox = (int64_t)batch_max * c->V;
     if (e == cudaSuccess) e = cudaMalloc(&c->wm, nw * sizeof(float));
@@ -381,6 +390,7 @@ fem_gpu_status fem_cnn_destroy(fem_cnn* c) {
     }
     cudaFree(c->y);
     cudaFree(c->loss);
+    if (c->ready) cudaEventDestroy(c->ready);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FEM_GPU_OK;
@@ -418,6 +428,7 @@ fem_gpu_status fem_cnn_forward(fem_cnn* c, const float* in4, int32_t nb, float* 
     if (!c || !in4 || !y3 || nb < 1 || nb > c->nb_max) return FEM_GPU_BAD_ARG;
     if (c->dirty) cnn_pack(c);
     const int64_t vox = (int64_t)nb * c->V;
+    after_default_stream(c);
     pack_input_kernel<<<256, 256, 0, c->stream>>>(vox, in4, c->act[0]);
     cnn_forward(c, nb);
     cudaError_t e = cudaMemcpy2DAsync(y3, 3 * sizeof(float), c->y, kPad * sizeof(float), 3 * sizeof(float), vox,
@@ -433,6 +444,7 @@ fem_gpu_status fem_cnn_loss_grad(fem_cnn* c, const float* in4, const float* targ
     if (!c || !in4 || !target3 || nb < 1 || nb > c->nb_max) return FEM_GPU_BAD_ARG;
     if (c->dirty) cnn_pack(c);
     const int64_t vox = (int64_t)nb * c->V;
+    after_default_stream(c);
     pack_input_kernel<<<256, 256, 0, c->stream>>>(vox, in4, c->act[0]);
     cnn_forward(c, nb);
     cudaMemsetAsync(c->loss, 0, sizeof(double), c->stream);
@@ -453,6 +465,7 @@ fem_gpu_status fem_cnn_train_step(fem_cnn* c, const float* in4, const float* tar
     if (!c || !in4 || !target3 || nb < 1 || nb > c->nb_max || !(lr > 0.f)) return FEM_GPU_BAD_ARG;
     if (c->dirty) cnn_pack(c);
     const int64_t vox = (int64_t)nb * c->V;
+    after_default_stream(c);
     pack_input_kernel<<<256, 256, 0, c->stream>>>(vox, in4, c->act[0]);
     cnn_forward(c, nb);
     cudaMemsetAsync(c->loss, 0, sizeof(double), c->stream);
@@ -483,8 +496,8 @@ __device__ __forceinline__ float hat(int d, int F) {
     return a >= F ? 0.f : 1.f - (float)a / (float)F;
 }
 
-// coarse channels-last [Vc][4]: channels 0..2 = (R r) * inv_scale, channel 3 untouched
-__global__ void restrict_kernel(int nf, int nc, int F, const double* r, float* coarse, double inv_scale) {
+// coarse channels-last [Vc][ch]: channels 0..2 = (R r) * inv_scale, the others untouched
+__global__ void restrict_kernel(int nf, int nc, int F, const double* r, float* coarse, int ch, double inv_scale) {
     const int64_t Vc = (int64_t)nc * nc * nc, Vf = (int64_t)nf * nf * nf;
     for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < Vc * 3; I += (int64_t)gridDim.x * blockDim.x) {
         const int comp = (int)(I / Vc);
@@ -508,8 +521,24 @@ __global__ void restrict_kernel(int nf, int nc, int F, const double* r, float* c
                 }
             }
         }
-        coarse[v * 4 + comp] = (float)(s * inv_scale);
+        coarse[v * ch + comp] = (float)(s * inv_scale);
     }
+}
+
+// sum of squares of channels 0..2 of a [Vc][4] coarse input
+__device__ double g_lpc_sumsq;
+__global__ void lpc_sumsq_kernel(int64_t Vc, const float* __restrict__ c4) {
+    double acc = 0.0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Vc * 3; t += (int64_t)gridDim.x * blockDim.x) {
+        const double v = c4[(t / 3) * 4 + t % 3];
+        acc = fma(v, v, acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&g_lpc_sumsq, acc);
+}
+__global__ void lpc_scale_kernel(int64_t Vc, float* __restrict__ c4, float a) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < Vc * 3; t += (int64_t)gridDim.x * blockDim.x)
+        c4[(t / 3) * 4 + t % 3] *= a;
 }
 
 // z[fine] += scale * P c   (c: coarse channels-last [Vc][3])
@@ -587,6 +616,18 @@ __global__ void fcg_spmv_dot(int64_t n, const int32_t* rp, const int32_t* ci, co
     block_sum_add(acc, dot);
 }
 
+
+__global__ void csr_spmv_kernel(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* x,
+                                double* y) {
+    const int sub = threadIdx.x % fem::kLanesPerRow;
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / fem::kLanesPerRow;
+    const int64_t first = ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / fem::kLanesPerRow;
+    for (int64_t base = first; base < n; base += groups) {
+        const int64_t row = base + (threadIdx.x & 31) / fem::kLanesPerRow;
+        const double s = fem::csr_row_dot(n, rp, ci, v, x, row, sub);
+        if (sub == 0 && row < n) y[row] = s;
+    }
+}
 
 // z = dinv r (the Jacobi part of the preconditioner)
 __global__ void fcg_jacobi(int64_t n, const double* dinv, const double* r, double* z) {
@@ -688,22 +729,19 @@ fem_gpu_status fem_lpc_restrict(int32_t nf, int32_t factor, const double* r_dev,
     if (!r_dev || !coarse_dev || factor < 1 || nf < 2 || (nf - 1) % factor) return FEM_GPU_BAD_ARG;
     const int nc = (nf - 1) / factor + 1;
     const int64_t Vc = (int64_t)nc * nc * nc;
-    restrict_kernel<<<512, 256>>>(nf, nc, factor, r_dev, coarse_dev, 1.0);
+    restrict_kernel<<<512, 256>>>(nf, nc, factor, r_dev, coarse_dev, 4, 1.0);
     if (rho_dev) density_channel_kernel<<<256, 256>>>(nf, nc, factor, rho_dev, coarse_dev);
-    std::vector<float> h(Vc * 4);
-    if (cudaMemcpy(h.data(), coarse_dev, Vc * 4 * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
-        return FEM_GPU_CUDA_ERROR;
+    // the norm on the device (one double back); the library-wide accumulator
+    // makes concurrent calls race, like the rest of the net's entry points
+    const double zero = 0.0;
     double s2 = 0.0;
-    for (int64_t v = 0; v < Vc; ++v)
-        for (int c = 0; c < 3; ++c) s2 += (double)h[v * 4 + c] * h[v * 4 + c];
+    if (cudaMemcpyToSymbol(g_lpc_sumsq, &zero, sizeof(double)) != cudaSuccess) return FEM_GPU_CUDA_ERROR;
+    lpc_sumsq_kernel<<<256, 256>>>(Vc, coarse_dev);
+    if (cudaMemcpyFromSymbol(&s2, g_lpc_sumsq, sizeof(double)) != cudaSuccess) return FEM_GPU_CUDA_ERROR;
     const double s = std::sqrt(s2);
-    const double inv = s > 0 ? 1.0 / s : 1.0;
-    for (int64_t v = 0; v < Vc; ++v)
-        for (int c = 0; c < 3; ++c) h[v * 4 + c] = (float)(h[v * 4 + c] * inv);
-    if (cudaMemcpy(coarse_dev, h.data(), Vc * 4 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
-        return FEM_GPU_CUDA_ERROR;
+    if (s > 0) lpc_scale_kernel<<<256, 256>>>(Vc, coarse_dev, (float)(1.0 / s));
     if (scale) *scale = s;
-    return FEM_GPU_OK;
+    return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
 }
 
 // injection of a fine 3-component field at the coarse nodes, / scale,
@@ -724,6 +762,30 @@ fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e_dev, d
     return cudaMemcpy(target_dev, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess
                ? FEM_GPU_OK
                : FEM_GPU_CUDA_ERROR;
+}
+
+// z += scale * P c (c: coarse channels-last [Vc][3])
+fem_gpu_status fem_lpc_prolong_add(int32_t nf, int32_t factor, const float* coarse3, double scale, double* z) {
+    if (!coarse3 || !z || factor < 1 || nf < 2 || (nf - 1) % factor) return FEM_GPU_BAD_ARG;
+    prolong_add_kernel<<<512, 256>>>(nf, (nf - 1) / factor + 1, factor, coarse3, scale, z);
+    return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
+}
+
+// coarse3 = scale * P^T fine, channels-last [Vc][3]
+fem_gpu_status fem_lpc_prolong_transpose(int32_t nf, int32_t factor, const double* fine, double scale,
+                                         float* coarse3) {
+    if (!coarse3 || !fine || factor < 1 || nf < 2 || (nf - 1) % factor) return FEM_GPU_BAD_ARG;
+    restrict_kernel<<<512, 256>>>(nf, (nf - 1) / factor + 1, factor, fine, coarse3, 3, scale);
+    return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
+}
+
+// y = A x for a CSR operator with n rows (device buffers; legacy default stream)
+fem_gpu_status fem_gpu_spmv(int64_t n, const int32_t* rowptr, const int32_t* colidx, const double* vals,
+                            const double* x, double* y) {
+    if (n < 1 || !rowptr || !colidx || !vals || !x || !y) return FEM_GPU_BAD_ARG;
+    const unsigned blocks = (unsigned)std::min<int64_t>((n * fem::kLanesPerRow + 255) / 256, 152 * 16);
+    csr_spmv_kernel<<<blocks, 256>>>(n, rowptr, colidx, vals, x, y);
+    return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
 }
 
 static int g_fcg_depth = 8, g_fcg_window = 200;

@@ -26,12 +26,18 @@
 //     symmetric positive definite operator;
 //   * the coarsest level (n_L <= coarse_max) is solved with its dense inverse,
 //     formed by Gauss-Jordan elimination on the device (the operator is SPD,
-//     so no pivoting).
+//     so no pivoting; two launches per pivot, so a small coarsest grid);
+//   * the finest fp32_levels levels smooth, restrict and prolong in FP32 (an
+//     FP32 copy of the stencil, FP32 vectors): the FP64 stencil sweep is bound
+//     by the FP64 pipe (243 FMAs per node), the FP32 one by HBM.  The V-cycle
+//     is a preconditioner inside an FP64 Krylov method, whose true residual
+//     decides convergence.
 // Vectors are type-major like the adof vector: v[g n_l^3 + node].  All work
 // is issued on the legacy default stream, like fem_gpu_fcg.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -89,11 +95,6 @@ __global__ void mg_csr_to_stencil(int n, const int32_t* __restrict__ rp, const i
     }
 }
 
-__global__ void mg_to_float(int64_t count, const double* __restrict__ a, float* __restrict__ b) {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
-        b[t] = (float)a[t];
-}
-
 __global__ void mg_diag_inv(int64_t N, const double* __restrict__ S, double* __restrict__ dinv) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 3 * N; t += (int64_t)gridDim.x * blockDim.x) {
         const int f = (int)(t / N);
@@ -102,12 +103,13 @@ __global__ void mg_diag_inv(int64_t N, const double* __restrict__ S, double* __r
     }
 }
 
-// s[f] = sum_k sum_g S[k][f][g][i] x[g][i + off_k] for the three rows of node i
-template <typename TS>
-__device__ __forceinline__ void stencil_rows(int n, int64_t N, const TS* __restrict__ S, const double* __restrict__ x,
-                                             int64_t i, double s[3]) {
+// s[f] = sum_k sum_g S[k][f][g][i] x[g][i + off_k] for the three rows of node i,
+// accumulated in the vector type TV (FP32 levels: FP32 FMAs)
+template <typename TS, typename TV>
+__device__ __forceinline__ void stencil_rows(int n, int64_t N, const TS* __restrict__ S, const TV* __restrict__ x,
+                                             int64_t i, TV s[3]) {
     const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
-    s[0] = s[1] = s[2] = 0.0;
+    s[0] = s[1] = s[2] = TV(0);
 #pragma unroll
     for (int dz = -1; dz <= 1; ++dz) {
         if (iz + dz < 0 || iz + dz >= n) continue;
@@ -121,24 +123,23 @@ __device__ __forceinline__ void stencil_rows(int n, int64_t N, const TS* __restr
                 const int64_t j = i + dx + (int64_t)n * (dy + (int64_t)n * dz);
 #pragma unroll
                 for (int g = 0; g < 3; ++g) {
-                    const double xg = __ldg(x + g * N + j);
+                    const TV xg = __ldg(x + g * N + j);
 #pragma unroll
-                    for (int f = 0; f < 3; ++f) s[f] = fma((double)__ldg(S + sidx(k, f, g, N, i)), xg, s[f]);
+                    for (int f = 0; f < 3; ++f) s[f] = fma((TV)__ldg(S + sidx(k, f, g, N, i)), xg, s[f]);
                 }
             }
         }
     }
 }
 
-// power iteration step: y = D^-1 A x; dots[0] += y.y
-template <typename TS>
-__global__ void mg_power(int n, const TS* __restrict__ S, const double* __restrict__ dinv, const double* __restrict__ x,
-                         double* __restrict__ y, double* dots) {
+// power iteration step (FP64): y = D^-1 A x; dots[0] += y.y
+__global__ void mg_power(int n, const double* __restrict__ S, const double* __restrict__ dinv,
+                         const double* __restrict__ x, double* __restrict__ y, double* dots) {
     const int64_t N = (int64_t)n * n * n;
     double acc = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         double s[3];
-        stencil_rows(n, N, S, x, i, s);
+        stencil_rows<double, double>(n, N, S, x, i, s);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const double v = dinv[f * N + i] * s[f];
@@ -146,6 +147,13 @@ __global__ void mg_power(int n, const TS* __restrict__ S, const double* __restri
             acc = fma(v, v, acc);
         }
     }
+    mg_block_sum_add(acc, dots);
+}
+
+__global__ void mg_sumsq(int64_t m, const double* __restrict__ x, double* dots) {
+    double acc = 0.0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
+        acc = fma(x[t], x[t], acc);
     mg_block_sum_add(acc, dots);
 }
 
@@ -165,12 +173,19 @@ __global__ void mg_random(int64_t m, uint64_t seed, double* __restrict__ x) {
     }
 }
 
+template <typename TA, typename TB>
+__global__ void mg_convert(int64_t m, const TA* __restrict__ a, TB* __restrict__ b) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
+        b[t] = (TB)a[t];
+}
+
 // Chebyshev start with x = 0: r = b, d = D^-1 b / theta, x = d
-__global__ void mg_cheb_init(int64_t m, const double* __restrict__ b, const double* __restrict__ dinv, double inv_theta,
-                             double* __restrict__ r, double* __restrict__ d, double* __restrict__ x) {
+template <typename TV>
+__global__ void mg_cheb_init(int64_t m, const TV* __restrict__ b, const TV* __restrict__ dinv, TV inv_theta,
+                             TV* __restrict__ r, TV* __restrict__ d, TV* __restrict__ x) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
-        const double bt = b[t];
-        const double dt = dinv[t] * bt * inv_theta;
+        const TV bt = b[t];
+        const TV dt = dinv[t] * bt * inv_theta;
         r[t] = bt;
         d[t] = dt;
         x[t] = dt;
@@ -178,19 +193,18 @@ __global__ void mg_cheb_init(int64_t m, const double* __restrict__ b, const doub
 }
 
 // Chebyshev step: r -= A din; dout = c1 din + c2 D^-1 r; x += dout
-template <typename TS>
-__global__ void mg_cheb_step(int n, const TS* __restrict__ S, const double* __restrict__ din, double* __restrict__ r,
-                             const double* __restrict__ dinv, double c1, double c2, double* __restrict__ dout,
-                             double* __restrict__ x) {
+template <typename TS, typename TV>
+__global__ void mg_cheb_step(int n, const TS* __restrict__ S, const TV* __restrict__ din, TV* __restrict__ r,
+                             const TV* __restrict__ dinv, TV c1, TV c2, TV* __restrict__ dout, TV* __restrict__ x) {
     const int64_t N = (int64_t)n * n * n;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        double s[3];
-        stencil_rows(n, N, S, din, i, s);
+        TV s[3];
+        stencil_rows<TS, TV>(n, N, S, din, i, s);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const int64_t t = f * N + i;
-            const double rt = r[t] - s[f];
-            const double dt = fma(c1, din[t], c2 * dinv[t] * rt);
+            const TV rt = r[t] - s[f];
+            const TV dt = fma(c1, din[t], c2 * dinv[t] * rt);
             r[t] = rt;
             dout[t] = dt;
             x[t] += dt;
@@ -199,12 +213,12 @@ __global__ void mg_cheb_step(int n, const TS* __restrict__ S, const double* __re
 }
 
 // r -= A d
-template <typename TS>
-__global__ void mg_residual_update(int n, const TS* __restrict__ S, const double* __restrict__ d, double* __restrict__ r) {
+template <typename TS, typename TV>
+__global__ void mg_residual_update(int n, const TS* __restrict__ S, const TV* __restrict__ d, TV* __restrict__ r) {
     const int64_t N = (int64_t)n * n * n;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        double s[3];
-        stencil_rows(n, N, S, d, i, s);
+        TV s[3];
+        stencil_rows<TS, TV>(n, N, S, d, i, s);
 #pragma unroll
         for (int f = 0; f < 3; ++f) r[f * N + i] -= s[f];
     }
@@ -212,19 +226,18 @@ __global__ void mg_residual_update(int n, const TS* __restrict__ S, const double
 
 // first post-smoothing step after the coarse correction e:
 // r -= A e; d = D^-1 r / theta; x += e + d
-template <typename TS>
-__global__ void mg_post_first(int n, const TS* __restrict__ S, const double* __restrict__ e, double* __restrict__ r,
-                              const double* __restrict__ dinv, double inv_theta, double* __restrict__ d,
-                              double* __restrict__ x) {
+template <typename TS, typename TV>
+__global__ void mg_post_first(int n, const TS* __restrict__ S, const TV* __restrict__ e, TV* __restrict__ r,
+                              const TV* __restrict__ dinv, TV inv_theta, TV* __restrict__ d, TV* __restrict__ x) {
     const int64_t N = (int64_t)n * n * n;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        double s[3];
-        stencil_rows(n, N, S, e, i, s);
+        TV s[3];
+        stencil_rows<TS, TV>(n, N, S, e, i, s);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const int64_t t = f * N + i;
-            const double rt = r[t] - s[f];
-            const double dt = dinv[t] * rt * inv_theta;
+            const TV rt = r[t] - s[f];
+            const TV dt = dinv[t] * rt * inv_theta;
             r[t] = rt;
             d[t] = dt;
             x[t] += e[t] + dt;
@@ -233,11 +246,12 @@ __global__ void mg_post_first(int n, const TS* __restrict__ S, const double* __r
 }
 
 // full-weighting restriction bc = P^T r (fine grid nf = 2 (nc - 1) + 1)
-__global__ void mg_restrict(int nf, int nc, const double* __restrict__ r, double* __restrict__ bc) {
+template <typename TF, typename TC>
+__global__ void mg_restrict(int nf, int nc, const TF* __restrict__ r, TC* __restrict__ bc) {
     const int64_t Nc = (int64_t)nc * nc * nc, Nf = (int64_t)nf * nf * nf;
     for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < Nc; I += (int64_t)gridDim.x * blockDim.x) {
         const int X = (int)(I % nc), Y = (int)((I / nc) % nc), Z = (int)(I / ((int64_t)nc * nc));
-        double s[3] = {0.0, 0.0, 0.0};
+        TF s[3] = {TF(0), TF(0), TF(0)};
         for (int az = -1; az <= 1; ++az) {
             const int z = 2 * Z + az;
             if (z < 0 || z >= nf) continue;
@@ -247,45 +261,46 @@ __global__ void mg_restrict(int nf, int nc, const double* __restrict__ r, double
                 for (int ax = -1; ax <= 1; ++ax) {
                     const int x = 2 * X + ax;
                     if (x < 0 || x >= nf) continue;
-                    const double w = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
+                    const TF w = TF((ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0));
                     const int64_t i = x + (int64_t)nf * (y + (int64_t)nf * z);
                     for (int g = 0; g < 3; ++g) s[g] = fma(w, r[g * Nf + i], s[g]);
                 }
             }
         }
-        for (int g = 0; g < 3; ++g) bc[g * Nc + I] = s[g];
+        for (int g = 0; g < 3; ++g) bc[g * Nc + I] = (TC)s[g];
     }
 }
 
 // trilinear prolongation e = P xc
-__global__ void mg_prolong(int nf, int nc, const double* __restrict__ xc, double* __restrict__ e) {
+template <typename TC, typename TF>
+__global__ void mg_prolong(int nf, int nc, const TC* __restrict__ xc, TF* __restrict__ e) {
     const int64_t Nc = (int64_t)nc * nc * nc, Nf = (int64_t)nf * nf * nf;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < Nf; i += (int64_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % nf), y = (int)((i / nf) % nf), z = (int)(i / ((int64_t)nf * nf));
         const int x0 = x >> 1, y0 = y >> 1, z0 = z >> 1;
         const int x1 = x0 + (x & 1), y1 = y0 + (y & 1), z1 = z0 + (z & 1);
-        const double wx = (x & 1) ? 0.5 : 1.0, wy = (y & 1) ? 0.5 : 1.0, wz = (z & 1) ? 0.5 : 1.0;
+        const TC wx = (x & 1) ? TC(0.5) : TC(1), wy = (y & 1) ? TC(0.5) : TC(1), wz = (z & 1) ? TC(0.5) : TC(1);
         for (int g = 0; g < 3; ++g) {
-            const double* c = xc + g * Nc;
+            const TC* c = xc + g * Nc;
             auto at = [&](int a, int b, int cc) { return c[a + (int64_t)nc * (b + (int64_t)nc * cc)]; };
-            double s = at(x0, y0, z0);
+            TC s = at(x0, y0, z0);
             if (x & 1) s += at(x1, y0, z0);
             if (y & 1) {
-                double t = at(x0, y1, z0);
+                TC t = at(x0, y1, z0);
                 if (x & 1) t += at(x1, y1, z0);
                 s += t;
             }
             if (z & 1) {
-                double t = at(x0, y0, z1);
+                TC t = at(x0, y0, z1);
                 if (x & 1) t += at(x1, y0, z1);
                 if (y & 1) {
-                    double u = at(x0, y1, z1);
+                    TC u = at(x0, y1, z1);
                     if (x & 1) u += at(x1, y1, z1);
                     t += u;
                 }
                 s += t;
             }
-            e[g * Nf + i] = s * wx * wy * wz;
+            e[g * Nf + i] = (TF)(s * wx * wy * wz);
         }
     }
 }
@@ -416,11 +431,14 @@ struct fem_mg {
     struct Level {
         int n = 0;
         int64_t N = 0;
-        double* S = nullptr;    // FP64 stencil
-        float* S32 = nullptr;   // FP32 copy used by the smoother (or null)
+        bool fp32 = false;        // smoothing and vectors in FP32
+        double* S = nullptr;      // FP64 stencil (Galerkin products, power iteration, FP64 smoothing)
+        float* S32 = nullptr;     // FP32 copy of an FP32 level
         double* dinv = nullptr;
+        float* dinv32 = nullptr;
         double lmax = 0.0;
-        double *x = nullptr, *b = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
+        // vectors in the level's precision; level 0 of an FP64 hierarchy uses the caller's b and x
+        void *x = nullptr, *b = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
     };
     std::vector<Level> lv;
     double* ainv = nullptr;  // dense inverse of the coarsest operator
@@ -440,70 +458,105 @@ struct fem_mg {
         bufs.push_back(*p);
         return true;
     }
+    bool alloc_vec(void** p, size_t count, bool f32) {
+        if (f32) return alloc((float**)p, count);
+        return alloc((double**)p, count);
+    }
 };
 
 namespace {
 
 constexpr int kTpb = 256;
 
-template <typename TS>
-void smooth_pre(const fem_mg::Level& L, const TS* S, const fem_mg_opts& o, const double* b, double* x) {
-    const double lo = o.lo_frac * L.lmax, hi = o.hi_frac * L.lmax;
-    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+template <typename TV>
+struct Cheb {
+    TV inv_theta, delta, sigma;
+    explicit Cheb(const fem_mg::Level& L, const fem_mg_opts& o) {
+        const double lo = o.lo_frac * L.lmax, hi = o.hi_frac * L.lmax;
+        const double theta = 0.5 * (hi + lo), dl = 0.5 * (hi - lo);
+        inv_theta = (TV)(1.0 / theta);
+        delta = (TV)dl;
+        sigma = (TV)(theta / dl);
+    }
+};
+
+// Chebyshev pre-smoothing from x = 0; on return r = b - A x
+template <typename TS, typename TV>
+void smooth_pre(const fem_mg::Level& L, const TS* S, const TV* dinv, const fem_mg_opts& o, const TV* b, TV* x) {
+    const Cheb<double> c(L, o);
     const unsigned vb = blocks_for(3 * L.N, kTpb), nb = blocks_for(L.N, kTpb);
-    mg_cheb_init<<<vb, kTpb>>>(3 * L.N, b, L.dinv, 1.0 / theta, L.r, L.d0, x);
-    double rho = 1.0 / sigma;
-    double *din = L.d0, *dout = L.d1;
+    TV *r = (TV*)L.r, *din = (TV*)L.d0, *dout = (TV*)L.d1;
+    mg_cheb_init<TV><<<vb, kTpb>>>(3 * L.N, b, dinv, (TV)c.inv_theta, r, din, x);
+    double rho = 1.0 / c.sigma;
     for (int k = 1; k < o.degree; ++k) {
-        const double rn = 1.0 / (2.0 * sigma - rho);
-        mg_cheb_step<TS><<<nb, kTpb>>>(L.n, S, din, L.r, L.dinv, rn * rho, 2.0 * rn / delta, dout, x);
+        const double rn = 1.0 / (2.0 * c.sigma - rho);
+        mg_cheb_step<TS, TV><<<nb, kTpb>>>(L.n, S, din, r, dinv, (TV)(rn * rho), (TV)(2.0 * rn / c.delta), dout, x);
         rho = rn;
         std::swap(din, dout);
     }
-    mg_residual_update<TS><<<nb, kTpb>>>(L.n, S, din, L.r);
+    mg_residual_update<TS, TV><<<nb, kTpb>>>(L.n, S, din, r);
 }
 
-// e (the prolongated coarse correction) lives in d1: the first step reads it and
-// writes d0, after which d1 is free for the ping-pong
-template <typename TS>
-void smooth_post(const fem_mg::Level& L, const TS* S, const fem_mg_opts& o, const double* e, double* x) {
-    const double lo = o.lo_frac * L.lmax, hi = o.hi_frac * L.lmax;
-    const double theta = 0.5 * (hi + lo), delta = 0.5 * (hi - lo), sigma = theta / delta;
+// Chebyshev post-smoothing after the coarse correction e, which lives in d1:
+// the first step reads it and writes d0, after which d1 is free for the ping-pong
+template <typename TS, typename TV>
+void smooth_post(const fem_mg::Level& L, const TS* S, const TV* dinv, const fem_mg_opts& o, const TV* e, TV* x) {
+    const Cheb<double> c(L, o);
     const unsigned nb = blocks_for(L.N, kTpb);
-    double *din = L.d0, *dout = L.d1;
-    mg_post_first<TS><<<nb, kTpb>>>(L.n, S, e, L.r, L.dinv, 1.0 / theta, din, x);
-    double rho = 1.0 / sigma;
+    TV *r = (TV*)L.r, *din = (TV*)L.d0, *dout = (TV*)L.d1;
+    mg_post_first<TS, TV><<<nb, kTpb>>>(L.n, S, e, r, dinv, (TV)c.inv_theta, din, x);
+    double rho = 1.0 / c.sigma;
     for (int k = 1; k < o.degree; ++k) {
-        const double rn = 1.0 / (2.0 * sigma - rho);
-        mg_cheb_step<TS><<<nb, kTpb>>>(L.n, S, din, L.r, L.dinv, rn * rho, 2.0 * rn / delta, dout, x);
+        const double rn = 1.0 / (2.0 * c.sigma - rho);
+        mg_cheb_step<TS, TV><<<nb, kTpb>>>(L.n, S, din, r, dinv, (TV)(rn * rho), (TV)(2.0 * rn / c.delta), dout, x);
         rho = rn;
         std::swap(din, dout);
     }
 }
 
-// x_l = V_l(b_l)
-void vcycle(fem_mg* g, size_t l, const double* b, double* x) {
+void vcycle(fem_mg* g, size_t l, const void* b, void* x);
+
+// smoothing, restriction, the coarser cycle, prolongation on a level of vector type TV
+template <typename TV>
+void level_cycle(fem_mg* g, size_t l, const TV* b, TV* x) {
     fem_mg::Level& L = g->lv[l];
-    if (l + 1 == g->lv.size()) {
-        mg_gemv<<<blocks_for(g->m * 32, kTpb), kTpb>>>(g->m, g->ainv, b, x);
+    fem_mg::Level& C = g->lv[l + 1];
+    const bool f32 = std::is_same<TV, float>::value;
+    if (f32) smooth_pre(L, L.S32, L.dinv32, g->o, (const float*)b, (float*)x);
+    else smooth_pre(L, L.S, L.dinv, g->o, (const double*)b, (double*)x);
+    if (C.fp32) mg_restrict<TV, float><<<blocks_for(C.N, kTpb), kTpb>>>(L.n, C.n, (const TV*)L.r, (float*)C.b);
+    else mg_restrict<TV, double><<<blocks_for(C.N, kTpb), kTpb>>>(L.n, C.n, (const TV*)L.r, (double*)C.b);
+    vcycle(g, l + 1, C.b, C.x);
+    TV* e = (TV*)L.d1;
+    if (C.fp32) mg_prolong<float, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, C.n, (const float*)C.x, e);
+    else mg_prolong<double, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, C.n, (const double*)C.x, e);
+    if (f32) smooth_post(L, L.S32, L.dinv32, g->o, (const float*)e, (float*)x);
+    else smooth_post(L, L.S, L.dinv, g->o, (const double*)e, (double*)x);
+}
+
+// x_l = V_l(b_l) in the level's precision
+void vcycle(fem_mg* g, size_t l, const void* b, void* x) {
+    if (l + 1 == g->lv.size()) {  // coarsest level: FP64 dense inverse
+        mg_gemv<<<blocks_for(g->m * 32, kTpb), kTpb>>>(g->m, g->ainv, (const double*)b, (double*)x);
         return;
     }
-    if (L.S32) smooth_pre<float>(L, L.S32, g->o, b, x);
-    else smooth_pre<double>(L, L.S, g->o, b, x);
-    fem_mg::Level& C = g->lv[l + 1];
-    mg_restrict<<<blocks_for(C.N, kTpb), kTpb>>>(L.n, C.n, L.r, C.b);
-    vcycle(g, l + 1, C.b, C.x);
-    double* e = L.d1;
-    mg_prolong<<<blocks_for(L.N, kTpb), kTpb>>>(L.n, C.n, C.x, e);
-    if (L.S32) smooth_post<float>(L, L.S32, g->o, e, x);
-    else smooth_post<double>(L, L.S, g->o, e, x);
+    if (g->lv[l].fp32) level_cycle<float>(g, l, (const float*)b, (float*)x);
+    else level_cycle<double>(g, l, (const double*)b, (double*)x);
 }
 
 }  // namespace
 
 bool mg_vcycle(fem_mg* g, const double* r, double* z) {
     if (!g) return false;
-    vcycle(g, 0, r, z);
+    fem_mg::Level& L = g->lv[0];
+    if (L.fp32) {
+        const unsigned vb = blocks_for(3 * L.N, kTpb);
+        mg_convert<double, float><<<vb, kTpb>>>(3 * L.N, r, (float*)L.b);
+        vcycle(g, 0, L.b, L.x);
+        mg_convert<float, double><<<vb, kTpb>>>(3 * L.N, (const float*)L.x, z);
+    } else {
+        vcycle(g, 0, r, z);
+    }
     return cudaGetLastError() == cudaSuccess;
 }
 
@@ -511,12 +564,12 @@ extern "C" {
 
 fem_gpu_status fem_mg_default_opts(fem_mg_opts* o) {
     if (!o) return FEM_GPU_BAD_ARG;
-    o->coarse_max = 9;
+    o->coarse_max = 5;
     o->degree = 2;
     o->lo_frac = 0.1;
     o->hi_frac = 1.1;
     o->power_iters = 12;
-    o->fp32_levels = 0;
+    o->fp32_levels = 2;
     return FEM_GPU_OK;
 }
 
@@ -551,10 +604,11 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
         fem_mg::Level& L = g->lv[l];
         L.n = ns[l];
         L.N = (int64_t)L.n * L.n * L.n;
-        ok = g->alloc(&L.S, 243 * L.N) && g->alloc(&L.dinv, 3 * L.N) && g->alloc(&L.r, 3 * L.N) &&
-             g->alloc(&L.d0, 3 * L.N) && g->alloc(&L.d1, 3 * L.N);
-        if (ok && l > 0) ok = g->alloc(&L.x, 3 * L.N) && g->alloc(&L.b, 3 * L.N);
-        if (ok && (int)l < o.fp32_levels && l + 1 < ns.size()) ok = g->alloc(&L.S32, 243 * L.N);
+        L.fp32 = (int)l < o.fp32_levels && l + 1 < ns.size();
+        ok = g->alloc(&L.S, 243 * L.N) && g->alloc(&L.dinv, 3 * L.N) && g->alloc_vec(&L.r, 3 * L.N, L.fp32) &&
+             g->alloc_vec(&L.d0, 3 * L.N, L.fp32) && g->alloc_vec(&L.d1, 3 * L.N, L.fp32);
+        if (ok && (l > 0 || L.fp32)) ok = g->alloc_vec(&L.x, 3 * L.N, L.fp32) && g->alloc_vec(&L.b, 3 * L.N, L.fp32);
+        if (ok && L.fp32) ok = g->alloc(&L.S32, 243 * L.N) && g->alloc(&L.dinv32, 3 * L.N);
     }
     g->m = 3 * g->lv.back().N;
     double *row = nullptr, *col = nullptr;
@@ -577,29 +631,35 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
         return fail(c, FEM_GPU_BAD_ARG, "multigrid: operator is not a 27-point nodal stencil on the node grid");
     }
     // smoother data: diagonal, FP32 copies, lambda_max(D^-1 A) by power iteration
+    // (FP64, in two scratch vectors of the finest size)
+    double *px = nullptr, *py = nullptr;
+    if (!g->alloc(&px, 3 * L0.N) || !g->alloc(&py, 3 * L0.N)) {
+        delete g;
+        return fail(c, FEM_GPU_OUT_OF_MEMORY, "multigrid hierarchy");
+    }
     for (size_t l = 0; l + 1 < g->lv.size(); ++l) {
         fem_mg::Level& L = g->lv[l];
+        const unsigned vb = blocks_for(3 * L.N, kTpb);
         mg_diag_inv<<<blocks_for(3 * L.N, kTpb), kTpb>>>(L.N, L.S, L.dinv);
-        if (L.S32) mg_to_float<<<blocks_for(243 * L.N, kTpb), kTpb>>>(243 * L.N, L.S, L.S32);
-        mg_random<<<blocks_for(3 * L.N, kTpb), kTpb>>>(3 * L.N, 0x5EEDULL + l, L.d0);
-        double xn = 0.0;
-        {
-            // ||x0|| from the host copy of the seeded vector (small cost, setup only)
-            std::vector<double> h(3 * L.N);
-            cudaMemcpy(h.data(), L.d0, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
-            for (double v : h) xn += v * v;
-            xn = std::sqrt(xn);
+        if (L.fp32) {
+            mg_convert<double, float><<<blocks_for(243 * L.N, kTpb), kTpb>>>(243 * L.N, L.S, L.S32);
+            mg_convert<double, float><<<vb, kTpb>>>(3 * L.N, L.dinv, L.dinv32);
         }
-        double lam = 0.0;
+        mg_random<<<vb, kTpb>>>(3 * L.N, 0x5EEDULL + l, px);
+        cudaMemset(g->dots, 0, sizeof(double));
+        mg_sumsq<<<vb, kTpb>>>(3 * L.N, px, g->dots);
+        double xx = 0.0;
+        cudaMemcpy(&xx, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
+        double xn = std::sqrt(xx), lam = 0.0;
         for (int it = 0; it < o.power_iters; ++it) {
             cudaMemset(g->dots, 0, sizeof(double));
-            mg_power<double><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, L.S, L.dinv, L.d0, L.d1, g->dots);
+            mg_power<<<blocks_for(L.N, kTpb), kTpb>>>(L.n, L.S, L.dinv, px, py, g->dots);
             double yy = 0.0;
             cudaMemcpy(&yy, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
             const double yn = std::sqrt(yy);
             lam = yn / xn;
             if (!(yn > 0.0)) break;
-            mg_scale<<<blocks_for(3 * L.N, kTpb), kTpb>>>(3 * L.N, 1.0 / yn, L.d1, L.d0);
+            mg_scale<<<vb, kTpb>>>(3 * L.N, 1.0 / yn, py, px);
             xn = 1.0;
         }
         L.lmax = lam;

@@ -242,3 +242,183 @@ def train_simp(n=128, factor=4, fields=10, per_field=200, every=None, epochs=30,
     cnn.output_scale = sigma
     hist = train(cnn, ins, tgts, epochs, batch, lr, seed=seed, log=log)
     return cnn, hist, len(ins)
+
+
+# ---------------------------------------------------------------------------
+# correction on top of the multigrid V-cycle, trained on the energy functional
+
+
+def spmv(rp, ci, vals, x, y):
+    _check(lib().fem_gpu_spmv(x.numel(), _dev_ptr(rp), _dev_ptr(ci), _dev_ptr(vals), _dev_ptr(x), _dev_ptr(y)),
+           "gpu_spmv")
+    return y
+
+
+def prolong_add(nf, factor, c3, scale, z):
+    _check(lib().fem_lpc_prolong_add(nf, factor, _dev_ptr(c3), float(scale), _dev_ptr(z)), "lpc_prolong_add")
+    return z
+
+
+def prolong_transpose(nf, factor, fine, scale, out3):
+    _check(lib().fem_lpc_prolong_transpose(nf, factor, _dev_ptr(fine), float(scale), _dev_ptr(out3)),
+           "lpc_prolong_transpose")
+    return out3
+
+
+def plain_pcg_residuals(model, rp, ci, vals, b, every, max_snaps):
+    """unit-norm residuals r_k = b - A x_k (FP32, device) of the plain-PCG
+    iterates x_k taken every `every` iterations"""
+    import torch
+    _, snaps, iters = pcg_snapshots(model, rp, ci, vals, b, every, max_snaps)
+    out = []
+    q = torch.empty_like(b)
+    for k in range(snaps.shape[0]):
+        spmv(rp, ci, vals, snaps[k].contiguous(), q)
+        r = b - q
+        nr = float(torch.linalg.norm(r))
+        if nr > 0:
+            out.append((r / nr).float())
+    del snaps
+    return out, iters
+
+
+class EnergyStep:
+    """One field's system (CSR, V-cycle, density) and the energy functional of
+    y = V r + P sigma s f(R r / s): E(y) = 1/2 y.A y - y.r, whose minimum over y
+    is at the error e = A^-1 r (E(y) = 1/2 |e - y|_A^2 - 1/2 |e|_A^2)."""
+
+    def __init__(self, rp, ci, vals, mg, rho, nf, factor, cnn):
+        import torch
+        self.rp, self.ci, self.vals, self.mg, self.rho = rp, ci, vals, mg, rho
+        self.nf, self.factor, self.cnn = nf, factor, cnn
+        self.nadof = 3 * nf ** 3
+        self.Vc = cnn.V
+        self.q = torch.empty(self.nadof, dtype=torch.float64, device="cuda")
+
+    def energy(self, y, r):
+        """(E(y), E after the optimal scaling of y, A y - r)"""
+        spmv(self.rp, self.ci, self.vals, y, self.q)
+        yAy, yr = float(y @ self.q), float(y @ r)
+        return 0.5 * yAy - yr, (-0.5 * yr * yr / yAy if yAy > 0 else 0.0), self.q - r
+
+    def inputs(self, rs):
+        """coarse inputs and scales of a list of fine residuals"""
+        import torch
+        cin = torch.zeros(len(rs), self.Vc * 4, dtype=torch.float32, device="cuda")
+        sc = []
+        for j, r in enumerate(rs):
+            c, s = restrict(self.nf, self.factor, r, self.rho)
+            cin[j] = c
+            sc.append(s)
+        return cin, sc
+
+    def corrected(self, z0, f, s):
+        y = z0.clone()
+        if s > 0:
+            prolong_add(self.nf, self.factor, f, self.cnn.output_scale * s, y)
+        return y
+
+
+def train_energy_mg(cnn, fields, factor, passes=2, rounds=2, batch=4, lr=1e-3, seed=1, log=None):
+    """Adam on the energy functional.  `fields` is a list of callables, each
+    returning (model, rp, ci, vals, mg, rho_dev, residuals) for one density
+    field; every round visits every field and makes `passes` shuffled passes
+    over its residuals.  Returns per-(round, field) means of E_opt(V r + c)
+    and E_opt(V r) (energies after the optimal scaling, unit-norm r)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    hist = []
+    for rnd in range(rounds):
+        for fi, make in enumerate(fields):
+            model, rp, ci, vals, mg, rho, res = make()
+            nf = grid_sizes(model)
+            st = EnergyStep(rp, ci, vals, mg, rho, nf, factor, cnn)
+            # V r of every residual, kept in FP32 (the training signal needs no more)
+            z = torch.empty(st.nadof, dtype=torch.float64, device="cuda")
+            z0s = [mg.apply(r.double(), z).float() for r in res]
+            e_net, e_mg = [], []
+            for _ in range(passes):
+                perm = rng.permutation(len(res))
+                for i in range(0, len(res) - batch + 1, batch):
+                    idx = perm[i:i + batch]
+                    rs = [res[j].double() for j in idx]
+                    cin, sc = st.inputs(rs)
+                    f = cnn.forward(cin.reshape(-1), batch).view(batch, -1)
+                    tgt = torch.empty_like(f)
+                    for k, j in enumerate(idx):
+                        y = st.corrected(z0s[j].double(), f[k].contiguous(), sc[k])
+                        _, eopt, g = st.energy(y, rs[k])
+                        e_net.append(eopt)
+                        gc = torch.zeros(st.Vc * 3, dtype=torch.float32, device="cuda")
+                        prolong_transpose(nf, factor, g.contiguous(), cnn.output_scale * sc[k], gc)
+                        tgt[k] = gc
+                    # MSE target whose gradient is the energy gradient (Adam is scale-free)
+                    kappa = 1.0 / max(float(tgt.abs().mean()), 1e-30)
+                    t3 = (f - kappa * tgt).reshape(-1).contiguous()
+                    cnn.train_step(cin.reshape(-1).contiguous(), t3, batch, lr)
+            for j in range(0, len(res), max(1, len(res) // 16)):
+                e_mg.append(st.energy(z0s[j].double(), res[j].double())[1])
+            hist.append((float(np.mean(e_net)), float(np.mean(e_mg))))
+            if log:
+                log("round %d field %d: E_opt(V r + c) %.4e  E_opt(V r) %.4e" % (rnd, fi, hist[-1][0], hist[-1][1]))
+            del st, z0s, res, mg, model
+            torch.cuda.empty_cache()
+    return hist
+
+
+def calibrate_output_scale(cnn, make_field, factor, samples=16):
+    """sigma = median over residuals of the optimal step |alpha*| of the
+    initial net's correction c = P s f: alpha* = -c.(A z0 - r) / c.A c"""
+    import torch
+    model, rp, ci, vals, mg, rho, res = make_field()
+    nf = grid_sizes(model)
+    st = EnergyStep(rp, ci, vals, mg, rho, nf, factor, cnn)
+    cnn.output_scale = 1.0
+    al = []
+    for r in res[:: max(1, len(res) // samples)]:
+        r = r.double()
+        z0 = mg.apply(r, torch.empty(st.nadof, dtype=torch.float64, device="cuda"))
+        cin, sc = st.inputs([r])
+        f = cnn.forward(cin.reshape(-1), 1)
+        c = torch.zeros_like(z0)
+        prolong_add(nf, factor, f, sc[0], c)
+        _, _, g0 = st.energy(z0, r)
+        spmv(rp, ci, vals, c, st.q)
+        cAc = float(c @ st.q)
+        if cAc > 0:
+            al.append(abs(float(c @ g0)) / cAc)
+    sigma = float(np.median(al)) if al else 1.0
+    cnn.output_scale = sigma
+    return sigma
+
+
+def simp_field(n, seed, factor, per_field, every, mg_opts=None):
+    """callable building one SIMP field's system, V-cycle and training residuals"""
+
+    def make():
+        import torch
+        from . import workloads
+        from .multigrid import Multigrid
+        m, mesh, rho = workloads.simp_3d(n, seed=seed)
+        rho_d = torch.tensor(rho, device="cuda")
+        rp, ci, vals, b = assembled_system(m)
+        res, _ = plain_pcg_residuals(m, rp, ci, vals, b, every, per_field)
+        mg = Multigrid(m, rp, ci, vals, **(mg_opts or {}))
+        return m, rp, ci, vals, mg, rho_d, res
+
+    return make
+
+
+def train_simp_mg(n=128, factor=2, fields=8, per_field=250, every=8, passes=2, rounds=2, batch=4, lr=1e-3, seed=1,
+                  log=print):
+    """Correction on top of the V-cycle, trained on `fields` x `per_field`
+    plain-PCG residuals of seeded density fields other than the benchmark's."""
+    from . import workloads
+    nc = (n // factor) + 1
+    cnn = Cnn(nc, batch_max=batch, seed=seed)
+    makers = [simp_field(n, workloads.BASE_SEED + 1000 + f, factor, per_field, every) for f in range(fields)]
+    sigma = calibrate_output_scale(cnn, makers[0], factor)
+    if log:
+        log("output scale sigma = %.4e" % sigma)
+    hist = train_energy_mg(cnn, makers, factor, passes=passes, rounds=rounds, batch=batch, lr=lr, seed=seed, log=log)
+    return cnn, hist, fields * per_field

@@ -25,8 +25,8 @@ def fcg_config(depth=8, window=200):
 
 
 class Multigrid:
-    def __init__(self, model, rp, ci, vals, coarse_max=9, degree=2, lo_frac=0.1, hi_frac=1.1, power_iters=12,
-                 fp32_levels=0):
+    def __init__(self, model, rp, ci, vals, coarse_max=5, degree=2, lo_frac=0.1, hi_frac=1.1, power_iters=12,
+                 fp32_levels=2):
         self.L = lib()
         o = MgOpts(coarse_max, degree, lo_frac, hi_frac, power_iters, fp32_levels)
         h = C.c_void_p()

@@ -99,7 +99,7 @@ def test_device_hierarchy_matches_oracle(torch, n, coarse_max, beta, tol):
     and 1e-7 at the SIMP contrast 1e9 (beta = 3)."""
     from moris_gb300.multigrid import Multigrid
     m, rp, ci, vals, b, A = device_system(n, beta)
-    h = Multigrid(m, rp, ci, vals, coarse_max=coarse_max)
+    h = Multigrid(m, rp, ci, vals, coarse_max=coarse_max, fp32_levels=0)
     o = mo.Hierarchy(A, n + 1, coarse_max=coarse_max)
     assert h.num_levels == len(o.ns)
     for l, nl in enumerate(o.ns):
@@ -116,6 +116,12 @@ def test_device_hierarchy_matches_oracle(torch, n, coarse_max, beta, tol):
     zo = o.vcycle(r)
     err = float(np.max(np.abs(z.cpu().numpy() - zo)) / np.max(np.abs(zo)))
     assert err <= tol, err
+    if beta == 1.0:
+        # FP32 smoothing on the two finest levels: the same operator to FP32 rounding
+        h32 = Multigrid(m, rp, ci, vals, coarse_max=coarse_max, fp32_levels=2)
+        z32 = h32.apply(torch.tensor(r, device="cuda"),
+                        torch.empty(m.num_adofs, dtype=torch.float64, device="cuda")).cpu().numpy()
+        assert float(np.max(np.abs(z32 - zo)) / np.max(np.abs(zo))) <= 1e-4
 
 
 @pytest.mark.gpu

@@ -285,7 +285,9 @@ def plain_pcg_residuals(model, rp, ci, vals, b, every, max_snaps):
 class EnergyStep:
     """One field's system (CSR, V-cycle, density) and the energy functional of
     y = V r + P sigma s f(R r / s): E(y) = 1/2 y.A y - y.r, whose minimum over y
-    is at the error e = A^-1 r (E(y) = 1/2 |e - y|_A^2 - 1/2 |e|_A^2)."""
+    is at the error e = A^-1 r (E(y) = 1/2 |e - y|_A^2 - 1/2 |e|_A^2).  CG picks
+    the step length itself, so training minimises the energy after the optimal
+    scaling, E_opt(y) = min_a E(a y): only the direction of y counts."""
 
     def __init__(self, rp, ci, vals, mg, rho, nf, factor, cnn):
         import torch
@@ -296,10 +298,15 @@ class EnergyStep:
         self.q = torch.empty(self.nadof, dtype=torch.float64, device="cuda")
 
     def energy(self, y, r):
-        """(E(y), E after the optimal scaling of y, A y - r)"""
+        """(E(y), E_opt(y), dE_opt/dy) with E_opt(y) = min_a E(a y) =
+        -1/2 (y.r)^2 / y.A y, the energy after the step-length choice of CG
+        (scale-free in y), and dE_opt/dy = a (a A y - r), a = y.r / y.A y"""
         spmv(self.rp, self.ci, self.vals, y, self.q)
         yAy, yr = float(y @ self.q), float(y @ r)
-        return 0.5 * yAy - yr, (-0.5 * yr * yr / yAy if yAy > 0 else 0.0), self.q - r
+        if not yAy > 0:
+            return 0.5 * yAy - yr, 0.0, -r
+        a = yr / yAy
+        return 0.5 * yAy - yr, -0.5 * yr * a, a * (a * self.q - r)
 
     def inputs(self, rs):
         """coarse inputs and scales of a list of fine residuals"""
@@ -319,58 +326,98 @@ class EnergyStep:
         return y
 
 
-def train_energy_mg(cnn, fields, factor, passes=2, rounds=2, batch=4, lr=1e-3, seed=1, log=None):
-    """Adam on the energy functional.  `fields` is a list of callables, each
-    returning (model, rp, ci, vals, mg, rho_dev, residuals) for one density
-    field; every round visits every field and makes `passes` shuffled passes
-    over its residuals.  Returns per-(round, field) means of E_opt(V r + c)
-    and E_opt(V r) (energies after the optimal scaling, unit-norm r)."""
+def mg_pcg_residuals(rp, ci, vals, b, mg, rel_tol=1e-8, max_iter=200):
+    """unit-norm residuals (FP32, device) of the iterates of PCG with the V-cycle
+    as preconditioner -- the residuals the correction meets inside that solver"""
+    import torch
+    x = torch.zeros_like(b)
+    r = b.clone()
+    z = torch.empty_like(b)
+    q = torch.empty_like(b)
+    mg.apply(r, z)
+    p = z.clone()
+    rz = float(r @ z)
+    bn = float(torch.linalg.norm(b))
+    out = [(r / bn).float()]
+    for _ in range(max_iter):
+        spmv(rp, ci, vals, p, q)
+        a = rz / float(p @ q)
+        x.add_(p, alpha=a)
+        r.add_(q, alpha=-a)
+        nr = float(torch.linalg.norm(r))
+        if nr <= rel_tol * bn:
+            break
+        out.append((r / nr).float())
+        mg.apply(r, z)
+        rz_new = float(r @ z)
+        p.mul_(rz_new / rz).add_(z)
+        rz = rz_new
+    return out
+
+
+def mg_field(n, seed, factor):
+    """one SIMP density field: (model, CSR, V-cycle, density, training residuals)"""
+    import torch
+    from . import workloads
+    from .multigrid import Multigrid
+    m, mesh, rho = workloads.simp_3d(n, seed=seed)
+    rho_d = torch.tensor(rho, device="cuda")
+    rp, ci, vals, b = assembled_system(m)
+    mg = Multigrid(m, rp, ci, vals)
+    res = mg_pcg_residuals(rp, ci, vals, b, mg)
+    return m, rp, ci, vals, mg, rho_d, res
+
+
+def train_energy_mg(cnn, n, factor, seeds, epochs=2, batch=4, lr=3e-4, seed=1, log=None):
+    """Adam on E_opt, streaming the density fields: every epoch builds each
+    field's system and V-cycle, takes the residuals of its V-cycle-preconditioned
+    CG iterates and makes one shuffled pass over them.  Returns per-epoch means
+    of E_opt(V r + c) / E_opt(V r) (both negative: above 1 means the correction
+    lowers the energy, i.e. helps)."""
     import torch
     rng = np.random.default_rng(seed)
     hist = []
-    for rnd in range(rounds):
-        for fi, make in enumerate(fields):
-            model, rp, ci, vals, mg, rho, res = make()
+    for ep in range(epochs):
+        ratios = []
+        for fs in seeds:
+            model, rp, ci, vals, mg, rho, res = mg_field(n, fs, factor)
             nf = grid_sizes(model)
             st = EnergyStep(rp, ci, vals, mg, rho, nf, factor, cnn)
-            # V r of every residual, kept in FP32 (the training signal needs no more)
             z = torch.empty(st.nadof, dtype=torch.float64, device="cuda")
-            z0s = [mg.apply(r.double(), z).float() for r in res]
-            e_net, e_mg = [], []
-            for _ in range(passes):
-                perm = rng.permutation(len(res))
-                for i in range(0, len(res) - batch + 1, batch):
-                    idx = perm[i:i + batch]
-                    rs = [res[j].double() for j in idx]
-                    cin, sc = st.inputs(rs)
-                    f = cnn.forward(cin.reshape(-1), batch).view(batch, -1)
-                    tgt = torch.empty_like(f)
-                    for k, j in enumerate(idx):
-                        y = st.corrected(z0s[j].double(), f[k].contiguous(), sc[k])
-                        _, eopt, g = st.energy(y, rs[k])
-                        e_net.append(eopt)
-                        gc = torch.zeros(st.Vc * 3, dtype=torch.float32, device="cuda")
-                        prolong_transpose(nf, factor, g.contiguous(), cnn.output_scale * sc[k], gc)
-                        tgt[k] = gc
-                    # MSE target whose gradient is the energy gradient (Adam is scale-free)
-                    kappa = 1.0 / max(float(tgt.abs().mean()), 1e-30)
-                    t3 = (f - kappa * tgt).reshape(-1).contiguous()
-                    cnn.train_step(cin.reshape(-1).contiguous(), t3, batch, lr)
-            for j in range(0, len(res), max(1, len(res) // 16)):
-                e_mg.append(st.energy(z0s[j].double(), res[j].double())[1])
-            hist.append((float(np.mean(e_net)), float(np.mean(e_mg))))
-            if log:
-                log("round %d field %d: E_opt(V r + c) %.4e  E_opt(V r) %.4e" % (rnd, fi, hist[-1][0], hist[-1][1]))
-            del st, z0s, res, mg, model
+            perm = rng.permutation(len(res))
+            for i in range(0, len(res) - batch + 1, batch):
+                idx = perm[i:i + batch]
+                rs = [res[j].double() for j in idx]
+                cin, sc = st.inputs(rs)
+                f = cnn.forward(cin.reshape(-1), batch).view(batch, -1)
+                tgt = torch.empty_like(f)
+                for k in range(batch):
+                    z0 = mg.apply(rs[k], z).clone()
+                    e0 = st.energy(z0, rs[k])[1]
+                    y = st.corrected(z0, f[k].contiguous(), sc[k])
+                    _, eopt, g = st.energy(y, rs[k])
+                    if e0 < 0:
+                        ratios.append(eopt / e0)
+                    gc = torch.zeros(st.Vc * 3, dtype=torch.float32, device="cuda")
+                    prolong_transpose(nf, factor, g.contiguous(), cnn.output_scale * sc[k], gc)
+                    tgt[k] = gc
+                # MSE target whose gradient is the energy gradient (Adam is scale-free)
+                kappa = 1.0 / max(float(tgt.abs().mean()), 1e-30)
+                cnn.train_step(cin.reshape(-1).contiguous(), (f - kappa * tgt).reshape(-1).contiguous(), batch, lr)
+            del st, res, mg, model, rp, ci, vals
             torch.cuda.empty_cache()
-    return hist
+        hist.append(float(np.mean(ratios)))
+        count = len(ratios)
+        if log:
+            log("epoch %d: E_opt(V r + c) / E_opt(V r) = %.4f over %d residuals" % (ep, hist[-1], count))
+    return hist, count
 
 
-def calibrate_output_scale(cnn, make_field, factor, samples=16):
+def calibrate_output_scale(cnn, n, factor, seed, samples=8):
     """sigma = median over residuals of the optimal step |alpha*| of the
-    initial net's correction c = P s f: alpha* = -c.(A z0 - r) / c.A c"""
+    initial net's correction c = P s f: alpha* = -c.(A V r - r) / c.A c"""
     import torch
-    model, rp, ci, vals, mg, rho, res = make_field()
+    model, rp, ci, vals, mg, rho, res = mg_field(n, seed, factor)
     nf = grid_sizes(model)
     st = EnergyStep(rp, ci, vals, mg, rho, nf, factor, cnn)
     cnn.output_scale = 1.0
@@ -382,7 +429,8 @@ def calibrate_output_scale(cnn, make_field, factor, samples=16):
         f = cnn.forward(cin.reshape(-1), 1)
         c = torch.zeros_like(z0)
         prolong_add(nf, factor, f, sc[0], c)
-        _, _, g0 = st.energy(z0, r)
+        spmv(rp, ci, vals, z0, st.q)
+        g0 = st.q - r
         spmv(rp, ci, vals, c, st.q)
         cAc = float(c @ st.q)
         if cAc > 0:
@@ -392,33 +440,17 @@ def calibrate_output_scale(cnn, make_field, factor, samples=16):
     return sigma
 
 
-def simp_field(n, seed, factor, per_field, every, mg_opts=None):
-    """callable building one SIMP field's system, V-cycle and training residuals"""
-
-    def make():
-        import torch
-        from . import workloads
-        from .multigrid import Multigrid
-        m, mesh, rho = workloads.simp_3d(n, seed=seed)
-        rho_d = torch.tensor(rho, device="cuda")
-        rp, ci, vals, b = assembled_system(m)
-        res, _ = plain_pcg_residuals(m, rp, ci, vals, b, every, per_field)
-        mg = Multigrid(m, rp, ci, vals, **(mg_opts or {}))
-        return m, rp, ci, vals, mg, rho_d, res
-
-    return make
-
-
-def train_simp_mg(n=128, factor=2, fields=8, per_field=250, every=8, passes=2, rounds=2, batch=4, lr=1e-3, seed=1,
-                  log=print):
-    """Correction on top of the V-cycle, trained on `fields` x `per_field`
-    plain-PCG residuals of seeded density fields other than the benchmark's."""
+def train_simp_mg(n=128, factor=2, fields=167, epochs=2, batch=4, lr=3e-4, seed=1, log=print):
+    """Correction on top of the V-cycle, trained on the residuals of
+    V-cycle-preconditioned CG on `fields` seeded density fields other than the
+    benchmark's (about 12 residuals per field at 128^3).  Returns the net, the
+    per-epoch energy ratios and the number of residuals per epoch."""
     from . import workloads
     nc = (n // factor) + 1
     cnn = Cnn(nc, batch_max=batch, seed=seed)
-    makers = [simp_field(n, workloads.BASE_SEED + 1000 + f, factor, per_field, every) for f in range(fields)]
-    sigma = calibrate_output_scale(cnn, makers[0], factor)
+    seeds = [workloads.BASE_SEED + 1000 + f for f in range(fields)]
+    sigma = calibrate_output_scale(cnn, n, factor, seeds[0])
     if log:
         log("output scale sigma = %.4e" % sigma)
-    hist = train_energy_mg(cnn, makers, factor, passes=passes, rounds=rounds, batch=batch, lr=lr, seed=seed, log=log)
-    return cnn, hist, fields * per_field
+    hist, count = train_energy_mg(cnn, n, factor, seeds, epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
+    return cnn, hist, count

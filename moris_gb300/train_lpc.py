@@ -3,16 +3,17 @@ project's own convolution forward / backward kernels and Adam) and write the
 weight file that bench.py and the tests load.
 
     python -m moris_gb300.train_lpc [--n 128] [--base multigrid] [--factor 2]
-                                    [--fields 8] [--pairs 2000] [--out moris_gb300/data/lpc_simp128.bin]
+                                    [--fields 167] [--epochs 2] [--out moris_gb300/data/lpc_simp128.bin]
 
-Training data: residuals (and, for --base jacobi, errors) of plain Jacobi-PCG
-iterates on seeded density fields (seeds BASE_SEED + 1000 + f, never the
-benchmark's field).
+Training data come from the solver's own iterates on seeded density fields
+(seeds BASE_SEED + 1000 + f, never the benchmark's field):
   --base multigrid  the correction is added to one multigrid V-cycle and trained
                     on the energy functional 1/2 y.A y - y.r of y = V r + c(r)
-                    (default);
+                    over the residuals of V-cycle-preconditioned CG (about 12
+                    per field at 128^3; 167 fields give 2,000) (default);
   --base jacobi     the correction is added to D^-1 r and trained on the
-                    mean-squared error against the injected coarse error.
+                    mean-squared error against the injected coarse error of
+                    2,000 residual / error pairs of Jacobi-PCG iterates.
 """
 import argparse
 import json
@@ -29,35 +30,32 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--base", choices=("multigrid", "jacobi"), default="multigrid")
     ap.add_argument("--factor", type=int, default=None, help="coarsening of the net's grid (2 multigrid, 4 jacobi)")
-    ap.add_argument("--fields", type=int, default=8)
-    ap.add_argument("--pairs", type=int, default=2000)
-    ap.add_argument("--every", type=int, default=8, help="PCG iterations between residual snapshots")
-    ap.add_argument("--epochs", type=int, default=20, help="jacobi base: epochs")
-    ap.add_argument("--passes", type=int, default=2, help="multigrid base: passes per field and round")
-    ap.add_argument("--rounds", type=int, default=2, help="multigrid base: rounds over the fields")
+    ap.add_argument("--fields", type=int, default=None, help="density fields (167 multigrid, 10 jacobi)")
+    ap.add_argument("--pairs", type=int, default=2000, help="jacobi base: residual / error pairs")
+    ap.add_argument("--epochs", type=int, default=None, help="passes over the data (2 multigrid, 20 jacobi)")
     ap.add_argument("--batch", type=int, default=None)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=None)
     ap.add_argument("--out", default=os.path.join(HERE, "data", "lpc_simp%d.bin" % 128))
     a = ap.parse_args()
     from moris_gb300 import learned
     t0 = time.time()
     log = lambda s: print(s, flush=True)  # noqa: E731
-    per_field = max(1, a.pairs // a.fields)
     if a.base == "multigrid":
-        factor = a.factor or 2
-        batch = a.batch or 4
-        cnn, hist, npairs = learned.train_simp_mg(n=a.n, factor=factor, fields=a.fields, per_field=per_field,
-                                                  every=a.every, passes=a.passes, rounds=a.rounds, batch=batch,
-                                                  lr=a.lr, log=log)
-        summary = {"objective": "energy", "energy_opt_first": hist[0], "energy_opt_last": hist[-1],
-                   "passes": a.passes, "rounds": a.rounds}
+        factor, fields, epochs = a.factor or 2, a.fields or 167, a.epochs or 2
+        batch, lr = a.batch or 4, a.lr or 3e-4
+        cnn, hist, npairs = learned.train_simp_mg(n=a.n, factor=factor, fields=fields, epochs=epochs, batch=batch,
+                                                  lr=lr, log=log)
+        summary = {"objective": "energy", "data": "residuals of V-cycle-preconditioned CG iterates",
+                   "energy_ratio_per_epoch": hist, "epochs": epochs}
     else:
-        factor = a.factor or 4
-        batch = a.batch or 16
-        cnn, hist, npairs = learned.train_simp(n=a.n, factor=factor, fields=a.fields, per_field=per_field,
-                                               epochs=a.epochs, batch=batch, lr=a.lr, log=log)
-        summary = {"objective": "mse", "loss_first": hist[0], "loss_last": hist[-1], "epochs": a.epochs}
-    meta = dict(n=a.n, base=a.base, factor=factor, fields=a.fields, pairs=npairs, batch=batch, lr=a.lr,
+        factor, fields, epochs = a.factor or 4, a.fields or 10, a.epochs or 20
+        batch, lr = a.batch or 16, a.lr or 1e-3
+        cnn, hist, npairs = learned.train_simp(n=a.n, factor=factor, fields=fields,
+                                               per_field=max(1, a.pairs // fields), epochs=epochs, batch=batch,
+                                               lr=lr, log=log)
+        summary = {"objective": "mse", "data": "residual / error pairs of Jacobi-PCG iterates",
+                   "loss_first": hist[0], "loss_last": hist[-1], "epochs": epochs}
+    meta = dict(n=a.n, base=a.base, factor=factor, fields=fields, pairs=npairs, batch=batch, lr=lr,
                 train_seconds=time.time() - t0, **summary)
     os.makedirs(os.path.dirname(a.out), exist_ok=True)
     learned.save_weights(a.out, cnn.weights(), cnn.n, factor, cnn.output_scale, json.dumps(meta))

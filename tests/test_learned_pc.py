@@ -109,25 +109,84 @@ def test_training_reduces_loss(torch):
 
 
 @pytest.mark.gpu
+def test_prolongation_transpose_is_the_adjoint(torch):
+    """<P c, v> = <c, P^T v> for the net's grid transfer (factors 2 and 4)."""
+    from moris_gb300 import learned
+    nf = 17
+    rng = np.random.default_rng(21)
+    for factor in (2, 4):
+        nc = (nf - 1) // factor + 1
+        c = torch.tensor(rng.standard_normal(nc ** 3 * 3).astype(np.float32), device="cuda")
+        v = torch.tensor(rng.standard_normal(3 * nf ** 3), device="cuda")
+        pc = learned.prolong_add(nf, factor, c, 1.0, torch.zeros(3 * nf ** 3, dtype=torch.float64, device="cuda"))
+        ptv = learned.prolong_transpose(nf, factor, v, 1.0, torch.zeros(nc ** 3 * 3, dtype=torch.float32,
+                                                                          device="cuda"))
+        lhs, rhs = float(pc @ v), float(c.double() @ ptv.double())
+        assert abs(lhs - rhs) <= 1e-5 * (abs(lhs) + 1.0), (factor, lhs, rhs)
+
+
+@pytest.mark.gpu
+def test_energy_training_gradient_matches_finite_differences(torch):
+    """The training signal of the correction on top of the V-cycle: dE_opt/df =
+    sigma s P^T (a (a A y - r)), y = V r + P sigma s f, against central
+    differences of E_opt in single entries of the net's output f."""
+    from moris_gb300 import learned
+    from moris_gb300.learned import Cnn, EnergyStep
+    n, factor = 16, 2
+    model, rp, ci, vals, mg, rho, res = learned.mg_field(n, 7, factor)
+    nf = learned.grid_sizes(model)
+    cnn = Cnn((nf - 1) // factor + 1)
+    cnn.output_scale = 0.05
+    st = EnergyStep(rp, ci, vals, mg, rho, nf, factor, cnn)
+    r = res[1].double()
+    z0 = mg.apply(r, torch.empty_like(r)).clone()
+    cin, sc = st.inputs([r])
+    rng = np.random.default_rng(3)
+    f = torch.tensor(rng.standard_normal(cnn.V * 3).astype(np.float32) * 0.1, device="cuda")
+    _, e0, g = st.energy(st.corrected(z0, f, sc[0]), r)
+    gc = learned.prolong_transpose(nf, factor, g.contiguous(), cnn.output_scale * sc[0],
+                                   torch.zeros(cnn.V * 3, dtype=torch.float32, device="cuda")).double()
+    h = 1e-2
+    for j in rng.choice(cnn.V * 3, 6, replace=False):
+        fp, fm = f.clone(), f.clone()
+        fp[j] += h
+        fm[j] -= h
+        ep = st.energy(st.corrected(z0, fp, sc[0]), r)[1]
+        em = st.energy(st.corrected(z0, fm, sc[0]), r)[1]
+        fd = (ep - em) / (2 * h)
+        assert abs(fd - float(gc[j])) <= 1e-3 * float(gc.abs().max()) + 1e-6 * abs(e0), (j, fd, float(gc[j]))
+
+
+@pytest.mark.gpu
 def test_learned_correction_gain_is_measured(torch, record_property):
-    """Trains the correction on other density seeds (32^3 SIMP), then solves the
-    benchmark-seed field with Jacobi-PCG and with FCG + the learned correction.
-    Both must reach 1e-8 on the true residual and agree; the iteration / time
-    ratio is what the trained network gains over the method without it."""
+    """Trains the correction on top of the V-cycle (energy after the optimal step,
+    residuals of V-cycle-preconditioned CG on other density seeds, 32^3 SIMP),
+    then solves the benchmark-seed field with FCG and the V-cycle, with and
+    without the net.  Both must reach 1e-8 on the true residual and agree with
+    Jacobi-PCG; the iteration and time ratios are what the trained network
+    gains over the method without it (recorded, not asserted: measured at
+    32^3-128^3 the net does not pay off on top of the V-cycle)."""
     from moris_gb300 import learned, workloads
-    cnn, hist, npairs = learned.train_simp(n=32, factor=4, fields=4, per_field=60, epochs=30, batch=8, lr=1e-3,
-                                           log=lambda s: None)
-    assert hist[-1] < hist[0]
+    from moris_gb300.multigrid import Multigrid, fcg_config, fcg_mg
+    cnn, hist, _ = learned.train_simp_mg(n=32, factor=2, fields=12, epochs=2, batch=4, lr=3e-4, log=lambda s: None)
+    assert all(np.isfinite(hist))
     m, mesh, rho = workloads.simp_3d(32)
     rho_d = torch.tensor(rho, device="cuda")
     rp, ci, vals, b = learned.assembled_system(m)
     xp = torch.zeros_like(b)
     plain = m.pcg(rp, ci, vals, b, xp, rel_tol=1e-8, max_iter=100000)
-    xl = torch.zeros_like(b)
-    rep = learned.fcg(m, rp, ci, vals, b, xl, cnn, 4, rho_d, rel_tol=1e-8, max_iter=100000)
-    assert rep["converged"] and rep["rel_residual"] <= 1e-8 * 1.0001
-    assert float(torch.linalg.norm(xl - xp) / torch.linalg.norm(xp)) < 1e-5
-    record_property("iterations_plain", plain["iterations"])
-    record_property("iterations_learned", rep["iterations"])
-    record_property("fallback", rep["fallback"])
-    record_property("time_ratio_plain_over_learned", plain["seconds"] / rep["seconds"])
+    h = Multigrid(m, rp, ci, vals)
+    reps = {}
+    fcg_config(8, 200)
+    for name, net in (("multigrid", None), ("learned", cnn)):
+        x = torch.zeros_like(b)
+        rep = fcg_mg(m, rp, ci, vals, b, x, h, cnn=net, factor=2, rho_dev=rho_d, rel_tol=1e-8, max_iter=20000)
+        assert rep["converged"] and rep["rel_residual"] <= 1e-8 * 1.0001
+        assert float(torch.linalg.norm(x - xp) / torch.linalg.norm(xp)) < 1e-5
+        reps[name] = rep
+    record_property("energy_ratio_per_epoch", hist)
+    record_property("iterations_jacobi", plain["iterations"])
+    record_property("iterations_multigrid", reps["multigrid"]["iterations"])
+    record_property("iterations_learned", reps["learned"]["iterations"])
+    record_property("fallback", reps["learned"]["fallback"])
+    record_property("time_ratio_multigrid_over_learned", reps["multigrid"]["seconds"] / reps["learned"]["seconds"])

@@ -22,6 +22,8 @@
  *                                    -> the CSR scatter inside fem_gpu_assemble
  *   Trilinos AztecOO CG + Jacobi (DLA/src/cl_DLA_Linear_Solver_Aztec.cpp:260-355)
  *                                    -> fem_gpu_pcg
+ *   PETSc PCMG geometric multigrid (DLA/src/cl_DLA_Preconditioner_PETSc.cpp:77-345)
+ *                                    -> fem_mg_create / fem_mg_apply / fem_gpu_fcg_mg
  *
  * Conventions (identical to the reference):
  *  - global ids are adof ids: type offset + rank of the B-spline basis among the
@@ -470,7 +472,8 @@ typedef struct fem_mg_opts {
     double lo_frac;       /* smoothing interval [lo_frac, hi_frac] * lambda_max(D^-1 A) (0.1, 1.1) */
     double hi_frac;
     int32_t power_iters;  /* power iterations for lambda_max (12) */
-    int32_t fp32_levels;  /* levels 0..fp32_levels-1 smooth in FP32 (FP32 stencil copy and vectors) (2) */
+    int32_t fp32_levels;  /* levels 0..fp32_levels-1 (never the coarsest) smooth in FP32, with an FP32
+                             stencil copy and FP32 vectors (default 8: all but the coarsest) */
 } fem_mg_opts;
 fem_gpu_status fem_mg_default_opts(fem_mg_opts* opts);
 /* builds the hierarchy from the assembled CSR (device); opts NULL = defaults */
@@ -487,7 +490,10 @@ fem_gpu_status fem_mg_get_stencil(const fem_mg* mg, int32_t level, double* host_
 /* one V-cycle z = V r (device vectors of num_adofs doubles) */
 fem_gpu_status fem_mg_apply(fem_mg* mg, const double* r, double* z);
 /* fem_gpu_fcg with the V-cycle in place of D^-1: M(r) = V r (+ the learned
-   correction P sigma s f(R r / s) when cnn is given); same fallback and judge */
+   correction P sigma s f(R r / s) when cnn is given); same judge.  A learned
+   correction that stalls the solve (4 iterations without a 10 % residual
+   reduction) is switched off and the solve continues with the V-cycle alone
+   (*used_fallback = 2); Jacobi-PCG stays the last fallback (*used_fallback = 1). */
 fem_gpu_status fem_gpu_fcg_mg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                               const double* b, double* x, fem_mg* mg, fem_cnn* cnn, int32_t factor,
                               const double* node_density, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* report,

@@ -806,8 +806,11 @@ fem_gpu_status fem_gpu_fcg_config(int32_t depth, int32_t window) {
    (non-positive p.Ap, NaN) or stagnation (no 10 % residual reduction within
    `window` iterations) the solve continues with fem_gpu_pcg from the current
    iterate; the final relative residual is recomputed from b - A x.
-   cnn == NULL runs the same loop with M = B.  m and window:
-   fem_gpu_fcg_config. */
+   cnn == NULL runs the same loop with M = B.  With the V-cycle as B, a
+   stalled learned correction (4 iterations without a 10 % reduction) is
+   switched off and the solve continues with M = B before any Jacobi-PCG
+   fallback.  *used_fallback: 0 none, 1 Jacobi-PCG fallback, 2 the learned
+   correction was switched off.  m and window: fem_gpu_fcg_config. */
 static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                               const double* b, double* x, fem_mg* mg, fem_cnn* cnn, int32_t factor,
                               const double* node_density, const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep,
@@ -864,13 +867,19 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         cudaMemset(dots, 0, kMaxM * 8);
     };
     const int nc = cnn ? cnn->n : 0;
+    // with the V-cycle as base, a stalled learned correction is switched off
+    // after kNetWindow iterations without a 10 % residual reduction and the
+    // solve continues (directions restarted) with the V-cycle alone
+    constexpr int kNetWindow = 4;
+    bool net_on = cnn != nullptr;
+    int net_dropped = 0;
     auto apply_m = [&]() -> bool {
         if (mg) {
             if (!mg_vcycle(mg, r, z)) return false;
         } else {
             fcg_jacobi<<<vb, tpb>>>(n, dinv, r, z);
         }
-        if (!cnn) return true;
+        if (!net_on) return true;
         double s = 0.0;
         if (fem_lpc_restrict(nf, factor, r, node_density, cin, &s) != FEM_GPU_OK) return false;
         if (s > 0.0) {
@@ -934,6 +943,12 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         if (rn < 0.9 * best) {
             best = rn;
             since_best = 0;
+        } else if (mg && net_on && ++since_best > kNetWindow) {
+            net_on = false;
+            net_dropped = 1;
+            stored = 0;
+            best = rn;
+            since_best = 0;
         } else if (++since_best > g_fcg_window) {
             fallback = 1;
             break;
@@ -966,7 +981,7 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         rep->rel_residual = true_rel;
         rep->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
-    if (used_fallback) *used_fallback = fallback;
+    if (used_fallback) *used_fallback = fallback ? 1 : (net_dropped ? 2 : 0);
     if (st != FEM_GPU_OK && st != FEM_GPU_NOT_CONVERGED) return st;
     return true_rel <= opts->rel_tol * 1.0001 ? FEM_GPU_OK : fail(c, FEM_GPU_NOT_CONVERGED, "fcg: not converged");
 }

@@ -132,34 +132,37 @@ __device__ __forceinline__ void stencil_rows(int n, int64_t N, const TS* __restr
     }
 }
 
-// power iteration step (FP64): y = D^-1 A x; dots[0] += y.y
-__global__ void mg_power(int n, const double* __restrict__ S, const double* __restrict__ dinv,
-                         const double* __restrict__ x, double* __restrict__ y, double* dots) {
+// power iteration step: y = D^-1 A x; dots[0] += y.y (in the level's precision)
+template <typename TS, typename TV>
+__global__ void mg_power(int n, const TS* __restrict__ S, const TV* __restrict__ dinv, const TV* __restrict__ x,
+                         TV* __restrict__ y, double* dots) {
     const int64_t N = (int64_t)n * n * n;
     double acc = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-        double s[3];
-        stencil_rows<double, double>(n, N, S, x, i, s);
+        TV s[3];
+        stencil_rows<TS, TV>(n, N, S, x, i, s);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-            const double v = dinv[f * N + i] * s[f];
+            const TV v = dinv[f * N + i] * s[f];
             y[f * N + i] = v;
-            acc = fma(v, v, acc);
+            acc += (double)v * (double)v;
         }
     }
     mg_block_sum_add(acc, dots);
 }
 
-__global__ void mg_sumsq(int64_t m, const double* __restrict__ x, double* dots) {
+template <typename TV>
+__global__ void mg_sumsq(int64_t m, const TV* __restrict__ x, double* dots) {
     double acc = 0.0;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
-        acc = fma(x[t], x[t], acc);
+        acc += (double)x[t] * (double)x[t];
     mg_block_sum_add(acc, dots);
 }
 
-__global__ void mg_scale(int64_t m, double a, const double* __restrict__ y, double* __restrict__ x) {
+template <typename TV>
+__global__ void mg_scale(int64_t m, double a, const TV* __restrict__ y, TV* __restrict__ x) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
-        x[t] = a * y[t];
+        x[t] = (TV)(a * (double)y[t]);
 }
 
 // splitmix64 uniform in [-0.5, 0.5): element t of the stream of `seed`
@@ -544,6 +547,35 @@ void vcycle(fem_mg* g, size_t l, const void* b, void* x) {
     else level_cycle<double>(g, l, (const double*)b, (double*)x);
 }
 
+// lambda_max(D^-1 A) of a level by power iteration from the seeded vector in
+// px (FP64; converted for an FP32 level); px / py are finest-size scratch
+template <typename TS, typename TV>
+double power_lambda(fem_mg* g, const fem_mg::Level& L, const TS* S, const TV* dinv, double* px, double* py, int iters) {
+    const unsigned vb = blocks_for(3 * L.N, kTpb);
+    TV *x = (TV*)px, *y = (TV*)py;
+    if (!std::is_same<TV, double>::value) {
+        mg_convert<double, TV><<<vb, kTpb>>>(3 * L.N, px, y);
+        mg_scale<TV><<<vb, kTpb>>>(3 * L.N, 1.0, y, x);
+    }
+    cudaMemset(g->dots, 0, sizeof(double));
+    mg_sumsq<TV><<<vb, kTpb>>>(3 * L.N, x, g->dots);
+    double xx = 0.0;
+    cudaMemcpy(&xx, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
+    double xn = std::sqrt(xx), lam = 0.0;
+    for (int it = 0; it < iters; ++it) {
+        cudaMemset(g->dots, 0, sizeof(double));
+        mg_power<TS, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, S, dinv, x, y, g->dots);
+        double yy = 0.0;
+        cudaMemcpy(&yy, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
+        const double yn = std::sqrt(yy);
+        lam = yn / xn;
+        if (!(yn > 0.0)) break;
+        mg_scale<TV><<<vb, kTpb>>>(3 * L.N, 1.0 / yn, y, x);
+        xn = 1.0;
+    }
+    return lam;
+}
+
 }  // namespace
 
 bool mg_vcycle(fem_mg* g, const double* r, double* z) {
@@ -569,7 +601,7 @@ fem_gpu_status fem_mg_default_opts(fem_mg_opts* o) {
     o->lo_frac = 0.1;
     o->hi_frac = 1.1;
     o->power_iters = 12;
-    o->fp32_levels = 2;
+    o->fp32_levels = 8;
     return FEM_GPU_OK;
 }
 
@@ -646,22 +678,10 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
             mg_convert<double, float><<<vb, kTpb>>>(3 * L.N, L.dinv, L.dinv32);
         }
         mg_random<<<vb, kTpb>>>(3 * L.N, 0x5EEDULL + l, px);
-        cudaMemset(g->dots, 0, sizeof(double));
-        mg_sumsq<<<vb, kTpb>>>(3 * L.N, px, g->dots);
-        double xx = 0.0;
-        cudaMemcpy(&xx, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
-        double xn = std::sqrt(xx), lam = 0.0;
-        for (int it = 0; it < o.power_iters; ++it) {
-            cudaMemset(g->dots, 0, sizeof(double));
-            mg_power<<<blocks_for(L.N, kTpb), kTpb>>>(L.n, L.S, L.dinv, px, py, g->dots);
-            double yy = 0.0;
-            cudaMemcpy(&yy, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
-            const double yn = std::sqrt(yy);
-            lam = yn / xn;
-            if (!(yn > 0.0)) break;
-            mg_scale<<<vb, kTpb>>>(3 * L.N, 1.0 / yn, py, px);
-            xn = 1.0;
-        }
+        // FP64 levels iterate on the FP64 stencil; FP32 levels on their FP32 copy
+        // (the smoothing interval needs lambda_max to a few digits only)
+        double lam = L.fp32 ? power_lambda<float, float>(g, L, L.S32, L.dinv32, px, py, o.power_iters)
+                            : power_lambda<double, double>(g, L, L.S, L.dinv, px, py, o.power_iters);
         L.lmax = lam;
         if (!(lam > 0.0) || !std::isfinite(lam)) {
             delete g;

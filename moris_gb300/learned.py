@@ -326,37 +326,47 @@ class EnergyStep:
         return y
 
 
-def mg_pcg_residuals(rp, ci, vals, b, mg, rel_tol=1e-8, max_iter=200):
-    """unit-norm residuals (FP32, device) of the iterates of PCG with the V-cycle
-    as preconditioner -- the residuals the correction meets inside that solver"""
+def mg_pcg_residuals(rp, ci, vals, b, mg, rel_tol=1e-8, max_iter=200, cnn=None, factor=2, rho=None):
+    """unit-norm residuals (FP32, device) of the iterates of flexible CG (one
+    previous direction) with M(r) = V r, or V r + P sigma s f(R r / s) when a
+    net is given -- the residuals the correction meets inside that solver"""
     import torch
+    nf = int(round((b.numel() // 3) ** (1.0 / 3.0)))
     x = torch.zeros_like(b)
     r = b.clone()
     z = torch.empty_like(b)
     q = torch.empty_like(b)
-    mg.apply(r, z)
-    p = z.clone()
-    rz = float(r @ z)
     bn = float(torch.linalg.norm(b))
-    out = [(r / bn).float()]
+    out = []
+    p_prev = q_prev = None
+    pq_prev = 1.0
     for _ in range(max_iter):
-        spmv(rp, ci, vals, p, q)
-        a = rz / float(p @ q)
-        x.add_(p, alpha=a)
-        r.add_(q, alpha=-a)
         nr = float(torch.linalg.norm(r))
         if nr <= rel_tol * bn:
             break
         out.append((r / nr).float())
         mg.apply(r, z)
-        rz_new = float(r @ z)
-        p.mul_(rz_new / rz).add_(z)
-        rz = rz_new
+        if cnn is not None:
+            cin, s = restrict(nf, factor, r, rho)
+            if s > 0:
+                prolong_add(nf, factor, cnn.forward(cin, 1), cnn.output_scale * s, z)
+        p = z.clone()
+        if p_prev is not None:
+            p.add_(p_prev, alpha=-float(z @ q_prev) / pq_prev)
+        spmv(rp, ci, vals, p, q)
+        pq = float(p @ q)
+        a = float(p @ r) / pq
+        x.add_(p, alpha=a)
+        r.add_(q, alpha=-a)
+        p_prev, q_prev, pq_prev = p, q.clone(), pq
     return out
 
 
-def mg_field(n, seed, factor):
-    """one SIMP density field: (model, CSR, V-cycle, density, training residuals)"""
+def mg_field(n, seed, factor, cnn=None, closed_loop_iters=20):
+    """one SIMP density field: (model, CSR, V-cycle, density, training
+    residuals).  The residuals are those of V-cycle-preconditioned CG and, when
+    a net is given, also those of the first closed_loop_iters iterations of
+    the solver with the net's correction in the loop (its own feedback)."""
     import torch
     from . import workloads
     from .multigrid import Multigrid
@@ -365,13 +375,16 @@ def mg_field(n, seed, factor):
     rp, ci, vals, b = assembled_system(m)
     mg = Multigrid(m, rp, ci, vals)
     res = mg_pcg_residuals(rp, ci, vals, b, mg)
+    if cnn is not None:
+        res += mg_pcg_residuals(rp, ci, vals, b, mg, max_iter=closed_loop_iters, cnn=cnn, factor=factor, rho=rho_d)
     return m, rp, ci, vals, mg, rho_d, res
 
 
 def train_energy_mg(cnn, n, factor, seeds, epochs=2, batch=4, lr=3e-4, seed=1, log=None):
     """Adam on E_opt, streaming the density fields: every epoch builds each
     field's system and V-cycle, takes the residuals of its V-cycle-preconditioned
-    CG iterates and makes one shuffled pass over them.  Returns per-epoch means
+    CG iterates (from the second epoch on also those of the solver with the
+    current net in the loop) and makes one shuffled pass over them.  Returns per-epoch means
     of E_opt(V r + c) / E_opt(V r) (both negative: above 1 means the correction
     lowers the energy, i.e. helps)."""
     import torch
@@ -380,7 +393,8 @@ def train_energy_mg(cnn, n, factor, seeds, epochs=2, batch=4, lr=3e-4, seed=1, l
     for ep in range(epochs):
         ratios = []
         for fs in seeds:
-            model, rp, ci, vals, mg, rho, res = mg_field(n, fs, factor)
+            # from the second epoch on, the data include the net's own closed loop
+            model, rp, ci, vals, mg, rho, res = mg_field(n, fs, factor, cnn if ep > 0 else None)
             nf = grid_sizes(model)
             st = EnergyStep(rp, ci, vals, mg, rho, nf, factor, cnn)
             z = torch.empty(st.nadof, dtype=torch.float64, device="cuda")

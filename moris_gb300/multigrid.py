@@ -26,7 +26,7 @@ def fcg_config(depth=8, window=200):
 
 class Multigrid:
     def __init__(self, model, rp, ci, vals, coarse_max=5, degree=2, lo_frac=0.1, hi_frac=1.1, power_iters=12,
-                 fp32_levels=2):
+                 fp32_levels=8):
         self.L = lib()
         o = MgOpts(coarse_max, degree, lo_frac, hi_frac, power_iters, fp32_levels)
         h = C.c_void_p()
@@ -77,4 +77,40 @@ def fcg_mg(model, rp, ci, vals, b, x, mg, cnn=None, factor=4, rho_dev=None, rel_
                               C.byref(r), C.byref(fb))
     model._check(st, "fcg_mg")
     return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual, seconds=r.seconds,
-                fallback=bool(fb.value))
+                fallback=fb.value == 1, net_switched_off=fb.value == 2)
+
+
+def main():
+    """python -m moris_gb300.multigrid [--n 128] [--repeat 1]: the SIMP density
+    problem (n^3 hex8, linear B-splines, E = rho^3 with rho in [1e-3, 1]) solved
+    to 1e-8 with FCG and the V-cycle; prints one JSON line per repeat."""
+    import argparse
+    import json
+    import time
+
+    import torch
+
+    from . import learned, workloads
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--fp32-levels", type=int, default=8)
+    a = ap.parse_args()
+    m, mesh, rho = workloads.simp_3d(a.n)
+    rp, ci, vals, b = learned.assembled_system(m)
+    fcg_config(1, 200)
+    for _ in range(a.repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h = Multigrid(m, rp, ci, vals, fp32_levels=a.fp32_levels)
+        torch.cuda.synchronize()
+        ts = time.perf_counter() - t0
+        x = torch.zeros_like(b)
+        r = fcg_mg(m, rp, ci, vals, b, x, h, rel_tol=1e-8, max_iter=20000)
+        r.update(n=a.n, setup_seconds=ts, levels=[h.level_info(lv)[0] for lv in range(h.num_levels)])
+        print(json.dumps(r), flush=True)
+        h.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -938,7 +938,67 @@ fem_gpu_status side_launch_on(fem_gpu_ctx* c, int set, const double* u, double* 
     return r;
 }
 
+// Host-buffer assembly overlaps the copy-back of the CSR values with the
+// element loop: the work runs in chunks (bulk sets split by element index, the
+// other sets whole); after chunk w every CSR row whose basis rank is below
+// final_rank[w] -- the smallest basis rank any later chunk touches -- is final,
+// and its values go to the host on a copy stream while the next chunk computes.
+// On the reference's mesh orderings (x fastest, z slowest) the rows finish in
+// slabs, so nearly all of the transfer hides behind the kernels.
+struct HostPipe {
+    std::vector<int> set;
+    std::vector<int64_t> first, count, final_rank;
+    cudaStream_t copy = nullptr;
+    std::vector<cudaEvent_t> done;  // one per chunk, and the copy stream's end
+};
+
+void host_pipe_release(fem_gpu_ctx* c) {
+    HostPipe* hp = (HostPipe*)c->host_pipe;
+    if (!hp) return;
+    if (hp->copy) cudaStreamSynchronize(hp->copy);
+    for (cudaEvent_t e : hp->done) cudaEventDestroy(e);
+    if (hp->copy) cudaStreamDestroy(hp->copy);
+    delete hp;
+    c->host_pipe = nullptr;
+}
+
+HostPipe* host_pipe(fem_gpu_ctx* c) {
+    if (c->host_pipe) return (HostPipe*)c->host_pipe;
+    HostPipe* hp = new HostPipe();
+    constexpr int64_t kChunk = 32768;  // elements per bulk chunk
+    std::vector<int64_t> minb;
+    for (int k = 0; k < (int)c->sets.size(); ++k) {
+        const SetData& s = c->sets[k];
+        const int64_t step = (!cluster_set(c, k) && s.kind == 0) ? std::max<int64_t>(kChunk, (s.neq + 7) / 8) : s.neq;
+        const int64_t width = s.neq ? (int64_t)s.bases.size() / s.neq : 0;
+        for (int64_t f = 0; f < s.neq; f += step) {
+            const int64_t n = std::min(step, s.neq - f);
+            int64_t mb = c->num_used;
+            for (int64_t i = f * width; i < (f + n) * width; ++i)
+                if (s.bases[i] >= 0) mb = std::min<int64_t>(mb, s.bases[i]);
+            hp->set.push_back(k);
+            hp->first.push_back(f);
+            hp->count.push_back(n);
+            minb.push_back(mb);
+        }
+    }
+    hp->final_rank.assign(minb.size(), c->num_used);
+    for (int64_t w = (int64_t)minb.size() - 2; w >= 0; --w)
+        hp->final_rank[w] = std::min(hp->final_rank[w + 1], minb[w + 1]);
+    cudaError_t e = cudaStreamCreateWithFlags(&hp->copy, cudaStreamNonBlocking);
+    hp->done.assign(minb.size() + 1, nullptr);
+    for (auto& ev : hp->done)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    c->host_pipe = hp;
+    if (e != cudaSuccess) {
+        host_pipe_release(c);
+        return nullptr;
+    }
+    return hp;
+}
+
 void device_release(fem_gpu_ctx* c) {
+    host_pipe_release(c);
     cluster_release(c);
     sensitivity_release(c);
     for (auto& s : c->sets) {
@@ -1211,23 +1271,50 @@ fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* c, const double* u, double* vals, d
         if (sr.dev) cudaMemsetAsync(sr.dev, 0, nad * sizeof(double), sm);
     }
     cudaMemsetAsync(c->d_status.p, 0, sizeof(int), sm);
-    for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
+    auto run = [&](int k, int64_t first, int64_t count) {
         SetData& s = c->sets[k];
         if (cluster_set(c, k))
-            st = cluster_launch_set(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev,
-                                    (double*)sr.dev, nullptr, nullptr, 0);
-        else if (s.kind == 0)
-            st = launch_bulk(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev, (double*)sr.dev,
-                             nullptr, nullptr, 0, nullptr, nullptr);
-        else
-            st = launch_side(c, k, MODE_ASSEMBLE, 0, s.neq, (const double*)su.dev, (double*)sv.dev, (double*)sr.dev,
-                             nullptr, nullptr, 0);
-    }
-    if (st == FEM_GPU_OK && host) {
+            return cluster_launch_set(c, k, MODE_ASSEMBLE, first, count, (const double*)su.dev, (double*)sv.dev,
+                                      (double*)sr.dev, nullptr, nullptr, 0);
+        if (s.kind == 0)
+            return launch_bulk(c, k, MODE_ASSEMBLE, first, count, (const double*)su.dev, (double*)sv.dev,
+                               (double*)sr.dev, nullptr, nullptr, 0, nullptr, nullptr);
+        return launch_side(c, k, MODE_ASSEMBLE, first, count, (const double*)su.dev, (double*)sv.dev, (double*)sr.dev,
+                           nullptr, nullptr, 0);
+    };
+    HostPipe* hp = (host && v) ? host_pipe(c) : nullptr;
+    if (hp) {
+        const int64_t nu = c->num_used;
+        int64_t done_rank = 0;
         cudaError_t e = cudaSuccess;
-        if (v) e = cudaMemcpyAsync(v, sv.dev, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, sm);
-        if (e == cudaSuccess && r) e = cudaMemcpyAsync(r, sr.dev, nad * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        for (size_t w = 0; w < hp->set.size() && st == FEM_GPU_OK && e == cudaSuccess; ++w) {
+            st = run(hp->set[w], hp->first[w], hp->count[w]);
+            const int64_t fin = hp->final_rank[w];
+            if (st != FEM_GPU_OK || fin <= done_rank) continue;
+            e = cudaEventRecord(hp->done[w], sm);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(hp->copy, hp->done[w], 0);
+            for (int f = 0; f < c->dim && e == cudaSuccess; ++f) {
+                const int64_t lo = c->rowptr[f * nu + done_rank], hi = c->rowptr[f * nu + fin];
+                e = cudaMemcpyAsync(v + lo, (double*)sv.dev + lo, (hi - lo) * sizeof(double), cudaMemcpyDeviceToHost,
+                                    hp->copy);
+            }
+            done_rank = fin;
+        }
+        // the residual after the last chunk; the compute stream then waits for
+        // the copy stream so that the staging release and the status read follow
+        if (e == cudaSuccess && st == FEM_GPU_OK && r)
+            e = cudaMemcpyAsync(r, sr.dev, nad * sizeof(double), cudaMemcpyDeviceToHost, sm);
+        if (e == cudaSuccess) e = cudaEventRecord(hp->done.back(), hp->copy);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sm, hp->done.back(), 0);
         if (e != cudaSuccess) st = cuda_fail(c, e, "assemble copy back");
+    } else {
+        for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) st = run(k, 0, c->sets[k].neq);
+        if (st == FEM_GPU_OK && host) {
+            cudaError_t e = cudaSuccess;
+            if (v) e = cudaMemcpyAsync(v, sv.dev, c->nnz * sizeof(double), cudaMemcpyDeviceToHost, sm);
+            if (e == cudaSuccess && r) e = cudaMemcpyAsync(r, sr.dev, nad * sizeof(double), cudaMemcpyDeviceToHost, sm);
+            if (e != cudaSuccess) st = cuda_fail(c, e, "assemble copy back");
+        }
     }
     release(c, su);
     release(c, sv);

@@ -106,6 +106,7 @@ struct fem_gpu_ctx {
     bool stream_set = false;           // caller chose a stream (NULL = legacy default stream)
     fem::DeviceBuf d_rowptr, d_ulen, d_tables, d_scratch, d_status;
     void* batch = nullptr;             // batched-launch state (fem_cluster.cu)
+    void* host_pipe = nullptr;         // chunked assembly with overlapped copy-back (fem_device.cu)
     // IG vertex table (shape sensitivities)
     std::vector<int32_t> vkind, vpar;  // [nv], [nv][8]
     std::vector<double> vx, vval;      // [nv][3], [nv]

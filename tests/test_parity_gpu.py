@@ -230,3 +230,23 @@ def test_nonfinite_input_is_reported(torch):
     with pytest.raises(mg.FemGpuError) as ei:
         m.add_bulk_set(np.arange(4), [1.0, np.nan, 1.0, 1.0], 0.3, mg.RULE_QUAD_2x2, mg.MODEL_PLANE_STRAIN)
     assert ei.value.status == 3
+
+
+def test_host_buffer_assembly_overlaps_the_copy_back(torch):
+    """Host-buffer assembly runs the element loop in chunks and copies every
+    finished row range while the next chunk computes: with more than one chunk
+    (40^3 elements, bulk and side sets) it must equal the device-buffer
+    assembly row for row (only the atomic summation order differs)."""
+    prod, _, _ = problem(3, (40, 40, 40), 1, mg.SHAPE_RECTANGULAR, mg.RULE_HEX_2x2x2, True)
+    prod.finalize()
+    u = uniform01(23, prod.num_adofs) - 0.5
+    rp, _ = prod.graph()
+    vh, rh = prod.assemble_host(u)
+    ud = torch.tensor(u, device="cuda")
+    vd = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rd = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(ud, vd, rd)
+    assert csr_row_rel_err(rp, vh, vd.cpu().numpy()) <= RTOL and rel_err(rh, rd.cpu().numpy()) <= RTOL
+    for _ in range(2):  # the cached chunk plan and copy stream are reused
+        vh2, rh2 = prod.assemble_host(u)
+        assert csr_row_rel_err(rp, vh2, vh) <= RTOL and rel_err(rh2, rh) <= RTOL

@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--c5-cpu-iterations", type=int, default=60,
+                    help="Jacobi-PCG iterations of the C5 CPU baseline sample")
     ap.add_argument("--no-c3", action="store_true", help="skip the XFEM (config 3) record")
     ap.add_argument("--no-c4", action="store_true", help="skip the adjoint-sensitivity (config 4) record")
     ap.add_argument("--no-c5", action="store_true", help="skip the learned-preconditioner (config 5) record")
@@ -425,6 +427,23 @@ def run_c5(stream, args):
                        "Nitsche clamp x=0, traction x=1" % (workloads.BASE_SEED + 5),
            "adofs": m.num_adofs, "nnz": m.nnz, "assembly_seconds": t_asm, "jacobi_pcg": plain,
            "fcg_multigrid": mgr, "wall_time_ratio_jacobi_over_multigrid": plain["seconds"] / mgr["wall_seconds"]}
+    if not args.no_cpu:
+        # CPU Jacobi-PCG on the same CSR (the oracle, all host threads), a bounded
+        # sample of iterations projected to the iteration count of the full solve
+        from oracle.oracle import pcg_mt
+        host = [t.cpu().numpy() for t in (rp, ci, vals, b)]
+        nthreads = os.cpu_count() or 1
+        t = time.perf_counter()
+        _, it, _, _ = pcg_mt(*host, rtol=1e-8, max_iter=args.c5_cpu_iterations, nthreads=nthreads)
+        dt = time.perf_counter() - t
+        per_it = dt / max(it, 1)
+        projected = per_it * plain["iterations"]
+        out["cpu_baseline"] = {"value": projected, "unit": "s to 1e-8 (projected)", "cores": nthreads, "kind": "port",
+                               "sample": "%d Jacobi-PCG iterations of the oracle on the same CSR, %d threads, "
+                                         "%.1f ms each, times the %d iterations of the full solve"
+                                         % (it, nthreads, per_it * 1e3, plain["iterations"])}
+        out["speedup_multigrid_vs_cpu_jacobi_pcg"] = projected / mgr["wall_seconds"]
+        out["speedup_jacobi_pcg_vs_cpu_jacobi_pcg"] = projected / plain["seconds"]
     if os.path.exists(LPC_WEIGHTS):
         cnn, factor, meta = learned.load_cnn(LPC_WEIGHTS)
         meta = json.loads(meta) if meta else {}

@@ -1525,4 +1525,87 @@ int orc_pcg(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, co
     return std::sqrt(rn) / bn <= rtol ? 0 : 2;
 }
 
+// The same Jacobi-PCG with every loop split over nthreads host threads (row
+// blocks; per-thread partial dot products summed in thread order), the CPU
+// counterpart of the reference's AztecOO CG + Jacobi on a node's cores.
+int orc_pcg_mt(int64_t n, const int32_t* rp, const int32_t* ci, const double* v, const double* b, double* x,
+               double rtol, int max_iter, int nthreads, int* iters, double* rel_res) {
+    const int T = std::max(1, nthreads);
+    std::vector<real> r(n), z(n), p(n), q(n), dinv(n, 1.0);
+    std::vector<real> part(3 * T);
+    auto par = [&](auto&& body) {  // body(t, lo, hi) over row blocks
+        std::vector<std::thread> th;
+        for (int t = 0; t < T; ++t) {
+            const int64_t lo = n * t / T, hi = n * (t + 1) / T;
+            th.emplace_back([&, t, lo, hi] { body(t, lo, hi); });
+        }
+        for (auto& h : th) h.join();
+    };
+    auto sum = [&](int k) {
+        real s = 0.0;
+        for (int t = 0; t < T; ++t) s += part[3 * t + k];
+        return s;
+    };
+    par([&](int t, int64_t lo, int64_t hi) {
+        real bb = 0.0, rz = 0.0, rr = 0.0;
+        for (int64_t i = lo; i < hi; ++i) {
+            real s = 0.0, d = 1.0;
+            for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+                s += v[k] * x[ci[k]];
+                if (ci[k] == i) d = v[k];
+            }
+            dinv[i] = 1.0 / d;
+            r[i] = b[i] - s;
+            z[i] = dinv[i] * r[i];
+            p[i] = z[i];
+            bb += b[i] * b[i];
+            rz += r[i] * z[i];
+            rr += r[i] * r[i];
+        }
+        part[3 * t] = bb;
+        part[3 * t + 1] = rz;
+        part[3 * t + 2] = rr;
+    });
+    real bn = std::sqrt(sum(0));
+    if (bn == 0.0) bn = 1.0;
+    real rz = sum(1), rn = sum(2);
+    int it = 0;
+    while (std::sqrt(rn) / bn > rtol && it < max_iter) {
+        par([&](int t, int64_t lo, int64_t hi) {
+            real pq = 0.0;
+            for (int64_t i = lo; i < hi; ++i) {
+                real s = 0.0;
+                for (int32_t k = rp[i]; k < rp[i + 1]; ++k) s += v[k] * p[ci[k]];
+                q[i] = s;
+                pq += p[i] * s;
+            }
+            part[3 * t] = pq;
+        });
+        const real alpha = rz / sum(0);
+        par([&](int t, int64_t lo, int64_t hi) {
+            real rr = 0.0, rz1 = 0.0;
+            for (int64_t i = lo; i < hi; ++i) {
+                x[i] += alpha * p[i];
+                r[i] -= alpha * q[i];
+                z[i] = dinv[i] * r[i];
+                rr += r[i] * r[i];
+                rz1 += r[i] * z[i];
+            }
+            part[3 * t] = rr;
+            part[3 * t + 1] = rz1;
+        });
+        rn = sum(0);
+        const real rz1 = sum(1);
+        const real beta = rz1 / rz;
+        rz = rz1;
+        par([&](int, int64_t lo, int64_t hi) {
+            for (int64_t i = lo; i < hi; ++i) p[i] = z[i] + beta * p[i];
+        });
+        ++it;
+    }
+    *iters = it;
+    *rel_res = std::sqrt(rn) / bn;
+    return std::sqrt(rn) / bn <= rtol ? 0 : 2;
+}
+
 }  // extern "C"

@@ -114,6 +114,9 @@ int orc_assemble(const orc_model* m, const double* u_adof, double* vals, double*
 int orc_pcg(int64_t n, const int32_t* rowptr, const int32_t* colidx, const double* vals,
             const double* b, double* x, double rtol, int max_iter, int jacobi, int* iters,
             double* rel_res);
+/* orc_pcg with its loops split over nthreads host threads */
+int orc_pcg_mt(int64_t n, const int32_t* rowptr, const int32_t* colidx, const double* vals, const double* b,
+               double* x, double rtol, int max_iter, int nthreads, int* iters, double* rel_res);
 
 #ifdef __cplusplus
 }

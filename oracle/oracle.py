@@ -55,6 +55,7 @@ def load():
             "orc_element_pdof_matrices": (_I, [_P, _I, _L, _P, _P, _P, _P]),
             "orc_assemble": (_I, [_P, _P, _P, _P, _I, _L, _I]),
             "orc_pcg": (_I, [_L, _P, _P, _P, _P, _P, _D, _I, _I, _P, _P]),
+            "orc_pcg_mt": (_I, [_L, _P, _P, _P, _P, _P, _D, _I, _I, _P, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -238,4 +239,19 @@ def pcg(rowptr, colidx, vals, b, rtol=1e-10, max_iter=100000, jacobi=True, x0=No
                      _ptr(np.ascontiguousarray(vals, dtype=np.float64)),
                      _ptr(np.ascontiguousarray(b, dtype=np.float64)), _ptr(x), rtol, max_iter,
                      1 if jacobi else 0, C.byref(it), C.byref(rr))
+    return x, it.value, rr.value, rc
+
+
+def pcg_mt(rowptr, colidx, vals, b, rtol=1e-10, max_iter=100000, nthreads=1, x0=None):
+    """Jacobi-PCG with its loops on nthreads host threads; (x, iterations, rel_res, rc)"""
+    lib = load()
+    n = len(b)
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    it = C.c_int()
+    rr = C.c_double()
+    rc = lib.orc_pcg_mt(n, _ptr(np.ascontiguousarray(rowptr, dtype=np.int32)),
+                        _ptr(np.ascontiguousarray(colidx, dtype=np.int32)),
+                        _ptr(np.ascontiguousarray(vals, dtype=np.float64)),
+                        _ptr(np.ascontiguousarray(b, dtype=np.float64)), _ptr(x), rtol, max_iter, nthreads,
+                        C.byref(it), C.byref(rr))
     return x, it.value, rr.value, rc

@@ -146,3 +146,15 @@ def test_multigrid_fcg_beats_jacobi_pcg(torch, record_property):
     finally:
         fcg_config(8, 200)
     record_property("iterations_jacobi", plain["iterations"])
+
+
+def test_oracle_threaded_pcg_matches_serial():
+    """The multithreaded oracle Jacobi-PCG (the CPU baseline of the C5 solve)
+    takes the same iterations as the serial one and reaches the same solution."""
+    from oracle.oracle import pcg, pcg_mt
+    A, b = simp_oracle(8)
+    A = A.tocsr()
+    x1, it1, r1, rc1 = pcg(A.indptr, A.indices, A.data, -b, rtol=1e-10, max_iter=5000)
+    x4, it4, r4, rc4 = pcg_mt(A.indptr, A.indices, A.data, -b, rtol=1e-10, max_iter=5000, nthreads=4)
+    assert rc1 == 0 and rc4 == 0 and abs(it1 - it4) <= 1
+    assert np.linalg.norm(x4 - x1) <= 1e-8 * np.linalg.norm(x1)

@@ -253,6 +253,12 @@ typedef struct fem_xtk_sizes {
 } fem_xtk_sizes;
 fem_gpu_status fem_xtk_decompose(const int32_t* num_elements, const double* lengths, int32_t bspline_order,
                                  const double* node_phi, fem_xtk_model** out);
+/* the same decomposition computed on the GPU (classification, subdivision and
+   cut, first-touch numbering by sorts, enrichment, unzipping, clusters); the
+   model is identical to fem_xtk_decompose's, array for array.  Inputs host
+   arrays; FEM_GPU_UNSUPPORTED for meshes above 2^29 / 3 nodes. */
+fem_gpu_status fem_xtk_decompose_device(const int32_t* num_elements, const double* lengths, int32_t bspline_order,
+                                        const double* node_phi, fem_xtk_model** out);
 fem_gpu_status fem_xtk_get_sizes(const fem_xtk_model* m, fem_xtk_sizes* sizes);
 /* any output pointer may be NULL; sizes as reported by fem_xtk_get_sizes */
 fem_gpu_status fem_xtk_get_ip_mesh(const fem_xtk_model* m, double* node_coords, int32_t* cell_nodes,

@@ -85,6 +85,7 @@ SIGNATURES = {
     "fem_gpu_autotune_batched": (I32, [P, P, P, P]),
     "fem_gpu_set_batched_config": (I32, [P, I32, I32]),
     "fem_xtk_decompose": (I32, [P, P, I32, P, P]),
+    "fem_xtk_decompose_device": (I32, [P, P, I32, P, P]),
     "fem_xtk_get_sizes": (I32, [P, P]),
     "fem_xtk_get_ip_mesh": (I32, [P, P, P, P, P, P, P, P]),
     "fem_xtk_get_bulk": (I32, [P, I32, P, P, P, P, P, P]),

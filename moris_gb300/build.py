@@ -20,7 +20,10 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRCS = ["fem_tables.cpp", "fem_host.cpp", "fem_xtk.cpp"]
 CUDA_SRCS = ["fem_device.cu", "fem_solver.cu", "fem_probe.cu", "fem_learned_pc.cu", "fem_cluster.cu", "fem_sensitivity.cu",
-             "fem_multigrid.cu"]
+             "fem_multigrid.cu", "fem_xtk_device.cu"]
+# the device XFEM decomposition reproduces the host's floating-point results,
+# which are compiled without contraction
+EXTRA_FLAGS = {"fem_xtk_device.cu": ["-fmad=false"]}
 
 
 def _nvcc():
@@ -61,7 +64,7 @@ def build(force=False, verbose=False):
     for s in CUDA_SRCS:
         o = os.path.join(OUT, s + ".o")
         jobs.append([nvcc, GENCODE, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-v",
-                     *inc, "-c", os.path.join(CSRC, s), "-o", o])
+                     *EXTRA_FLAGS.get(s, []), *inc, "-c", os.path.join(CSRC, s), "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -37,19 +37,15 @@
 #include <vector>
 
 #include "fem_internal.hpp"
+#include "fem_xtk.hpp"
 
-namespace {
-
+namespace fem {
 const int kHexSides[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
 const double kHexXi[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                              {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+}  // namespace fem
 
-struct IgVertex {
-    int32_t kind;        // 0 background node, 1 face centre, 2 cell centre, 3 intersection
-    int32_t parents[8];  // background nodes (kinds 0-2) or the two parent IG vertices (kind 3)
-    double x[3];
-    double value;        // level set (kinds 0-2) or edge coordinate t from parents[0] (kind 3)
-};
+namespace {
 
 struct Tet {
     int32_t v[4];     // IG vertex ids
@@ -84,31 +80,6 @@ double signed_det(const double* x0, const double* x1, const double* x2, const do
 }
 
 }  // namespace
-
-struct fem_xtk_model {
-    int p = 1;
-    int64_t ne[3] = {0, 0, 0}, nn[3] = {0, 0, 0}, nbk[3] = {0, 0, 0};
-    // enriched interpolation mesh
-    std::vector<double> coords;
-    std::vector<int32_t> cells;
-    std::vector<int64_t> t_off;
-    std::vector<int32_t> t_bases;
-    std::vector<double> t_w;
-    std::vector<int32_t> cell_bg, cell_phase;
-    int64_t num_enriched_bases = 0;
-    // clusters
-    std::vector<int32_t> uncut[2], cut[2];
-    std::vector<int64_t> ig_off[2];
-    std::vector<double> ig_x[2], ig_xi[2];
-    std::vector<int32_t> ig_v[2];
-    std::vector<int32_t> if_leader, if_follower;
-    std::vector<int64_t> if_off;
-    std::vector<double> if_x, if_xi;
-    std::vector<int32_t> if_v;
-    std::vector<int32_t> gh_leader[2], gh_follower[2];
-    std::vector<double> gh_x[2], gh_xi_l[2], gh_xi_f[2];
-    std::vector<IgVertex> verts;
-};
 
 using namespace fem;
 

@@ -1,6 +1,7 @@
 """XFEM input over the C ABI (fem_xtk_*): decomposition of a uniform level-0
 HEX8 mesh by a nodal level set into TET4 integration cells, Heaviside
-enrichment, interface and ghost facets.  Host-only; returns numpy arrays."""
+enrichment, interface and ghost facets, on the host or on the GPU; returns
+numpy arrays."""
 import ctypes as C
 
 import numpy as np
@@ -9,18 +10,20 @@ from . import FemGpuError, _np_ptr, lib
 from ._lib import XtkSizes
 
 
-def decompose(num_elements, lengths, order, node_phi):
+def decompose(num_elements, lengths, order, node_phi, device=False):
     """node_phi: level set at the (n0+1)(n1+1)(n2+1) grid nodes (i fastest);
-    phase 1 where phi < 0.  Returns a dict of arrays (see fem_xtk_* in
-    include/fem_gpu.h)."""
+    phase 1 where phi < 0.  device=True computes the same decomposition on
+    the GPU (fem_xtk_decompose_device).  Returns a dict of arrays (see fem_xtk_*
+    in include/fem_gpu.h)."""
     L = lib()
     ne = np.ascontiguousarray(num_elements, dtype=np.int32)
     ln = np.ascontiguousarray(lengths, dtype=np.float64)
     phi = np.ascontiguousarray(node_phi, dtype=np.float64)
     h = C.c_void_p()
-    st = L.fem_xtk_decompose(_np_ptr(ne), _np_ptr(ln), order, _np_ptr(phi), C.byref(h))
+    fn = L.fem_xtk_decompose_device if device else L.fem_xtk_decompose
+    st = fn(_np_ptr(ne), _np_ptr(ln), order, _np_ptr(phi), C.byref(h))
     if st:
-        raise FemGpuError(st, "fem_xtk_decompose")
+        raise FemGpuError(st, "fem_xtk_decompose_device" if device else "fem_xtk_decompose")
     try:
         s = XtkSizes()
         L.fem_xtk_get_sizes(h, C.byref(s))

@@ -203,3 +203,31 @@ def test_xfem_quadratic_bsplines_match_oracle():
     v, r = prod.assemble_host(u)
     assert csr_row_rel_err(rp, v, vo) <= RTOL
     assert rel_err(r, ro) <= RTOL
+
+
+def _assert_same(a, b, path="x"):
+    if isinstance(a, dict):
+        assert set(a) == set(b), path
+        for k in a:
+            _assert_same(a[k], b[k], path + "." + str(k))
+    elif isinstance(a, np.ndarray):
+        assert a.shape == b.shape and a.dtype == b.dtype, path
+        assert np.array_equal(a, b), (path, int(np.sum(a != b)))
+    elif hasattr(a, "_fields_"):
+        for name, _ in a._fields_:
+            assert np.array_equal(np.asarray(getattr(a, name)), np.asarray(getattr(b, name))), path + "." + name
+    else:
+        assert a == b, path
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nspheres,rmin,rmax,order", [(10, 5, 0.15, 0.3, 1), (6, 3, 0.25, 0.35, 2),
+                                                         (24, 40, 0.03, 0.12, 1)])
+def test_device_decomposition_equals_host(n, nspheres, rmin, rmax, order):
+    """The GPU decomposition (first-touch numbering by sorts, enrichment and
+    unzipping on the device) returns the host decomposition array for array,
+    bit for bit."""
+    phi = workloads.sphere_field(n, workloads.BASE_SEED + 3, nspheres, rmin, rmax)
+    xh = xtk.decompose((n, n, n), (1.0, 1.0, 1.0), order, phi)
+    xd = xtk.decompose((n, n, n), (1.0, 1.0, 1.0), order, phi, device=True)
+    _assert_same(xh, xd)

@@ -249,8 +249,20 @@ def run_c3(timed, stream, world, args):
     import torch
     import moris_gb300 as mg
     from moris_gb300 import workloads
+    from moris_gb300 import xtk
+    # the decomposition itself, host and device (identical arrays)
+    phi = workloads.sphere_field(NE_C3, workloads.BASE_SEED + 3, 40, 0.03, 0.12)
     t0 = time.perf_counter()
-    m, x, sets = workloads.xfem_spheres(NE_C3, finalize=False)
+    xh = xtk.decompose((NE_C3,) * 3, (1.0,) * 3, 1, phi)
+    t_host = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xd = xtk.decompose((NE_C3,) * 3, (1.0,) * 3, 1, phi, device=True)
+    t_dev = time.perf_counter() - t0
+    same = all(np.array_equal(xh[k][j], xd[k][j]) for k in ("mesh", "interface", "vertices", "cut0", "cut1")
+               for j in xh[k] if isinstance(xh[k][j], np.ndarray))
+    del xh, xd
+    t0 = time.perf_counter()
+    m, x, sets = workloads.xfem_spheres(NE_C3, finalize=False, device=True)
     m.set_stream(stream.cuda_stream)
     m.finalize()
     warps, split, tuned_ms = m.autotune_batched()
@@ -281,7 +293,8 @@ def run_c3(timed, stream, world, args):
            "roofline": {"bound": "fp64", "achieved": fl / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
                         "frac": fl / (ms * 1e-3) / 1e12 / peak, "flops_per_step": fl,
                         "peak_source": "measured in-run (FP64 FMA-chain probe)"},
-           "setup_seconds": setup}
+           "setup_seconds": setup,
+           "decomposition": {"host_seconds": t_host, "device_seconds": t_dev, "identical_arrays": bool(same)}}
     if world == 1 and not args.no_cpu:
         r = cpu_reference_c3(x, sets, min(args.cpu_seconds, 10.0))
         rec["cpu_baseline"] = {"value": r["value"], "unit": "elements/s", "cores": r["cores"], "kind": "port",
@@ -355,7 +368,8 @@ def run_c4(stream, args):
            "pcg_converged": {"state": sol["pcg_u"]["converged"], "adjoint": sol["pcg_lambda"]["converged"]},
            "adjoint_kernel_ms": ms_adj, "vertices_per_s": n_inter / (ms_adj * 1e-3), "chain_ms": ms_chain,
            "fd_check": {"coefficients": int(len(pick)), "h": h, "max_abs_err_over_max_dqdp": worst},
-           "setup_seconds": setup}
+           "setup_seconds": setup,
+           "decomposition": {"host_seconds": t_host, "device_seconds": t_dev, "identical_arrays": bool(same)}}
     if not args.no_cpu:
         # the reference's finite-difference dR/dp (forward FD of IG vertex coordinates),
         # restated on the oracle, timed on a sample of intersection vertices

@@ -132,16 +132,17 @@ def add_xfem_sets(m, sets):
                            alpha=a.get("alpha", 0.0), value=a["value"])
 
 
-def xfem_spheres(n=96, seed=BASE_SEED + 3, nspheres=40, rmin=0.03, rmax=0.12, order=1, finalize=True, **kw):
+def xfem_spheres(n=96, seed=BASE_SEED + 3, nspheres=40, rmin=0.03, rmax=0.12, order=1, finalize=True, device=False,
+                 **kw):
     """Two-phase XFEM workload: n^3 HEX8 background of the unit cube with
     B-splines of `order`, cut by the sphere level set; phase 0 (phi >= 0) E = 1,
     phase 1 (inside the spheres) E = 0.1, nu = 0.3; uncut cells HEX_2x2x2, cut
     clusters TET4 cells with TET_4, Nitsche interface (alpha 100, TRI_7),
-    virtual-work ghost (alpha 0.01, QUAD_2x2).  Returns (model, decomposition,
-    set list)."""
+    virtual-work ghost (alpha 0.01, QUAD_2x2).  device=True decomposes on the
+    GPU (the same arrays).  Returns (model, decomposition, set list)."""
     from . import xtk
     phi = sphere_field(n, seed, nspheres, rmin, rmax)
-    x = xtk.decompose((n, n, n), (1.0, 1.0, 1.0), order, phi)
+    x = xtk.decompose((n, n, n), (1.0, 1.0, 1.0), order, phi, device=device)
     sets = xfem_sets(x, **kw)
     m = FemModel(3, x["mesh"], SHAPE_RECTANGULAR)
     add_xfem_sets(m, sets)

@@ -524,6 +524,23 @@ fem_gpu_status fem_gpu_probe_fp64_tflops(int32_t iters, double* tflops);
 fem_gpu_status fem_gpu_probe_dmma_tflops(int32_t iters, int32_t mixed, double* tflops);
 /* number of kernel launches issued by the context since creation */
 int64_t fem_gpu_launch_count(const fem_gpu_ctx* ctx);
+/* ---- field output (VIS) -----------------------------------------------------
+   Nodal values of an adof field at the interpolation-mesh nodes, out[f][node]
+   = sum over the node's extraction row of w u[f nu + rank] (device buffers;
+   out: dim x num_nodes), the values VIS::Output_Manager::write_field
+   (FEM/VIS/src/cl_VIS_Output_Manager.cpp:679-785) writes at the vertices. */
+fem_gpu_status fem_gpu_nodal_field(fem_gpu_ctx* ctx, const double* u_adof, double* out);
+/* Exodus II file of one element block and nodal fields at one time step (the
+   reference writes through mtk::Writer_Exodus, MTK/src/io/cl_MTK_Writer_Exodus.
+   cpp:112-420, and the SEACAS library; here the netCDF classic 64-bit-offset
+   format is written directly).  Host arrays: coords [num_nodes][dim],
+   cell_nodes [num_cells][nodes_per_cell] 0-based, field_values
+   [num_fields][num_nodes]; elem_type e.g. "HEX8", "QUAD4". */
+fem_gpu_status fem_vis_write_exodus(const char* path, int32_t dim, int64_t num_nodes, const double* coords,
+                                    int64_t num_cells, int32_t nodes_per_cell, const int32_t* cell_nodes,
+                                    const char* elem_type, int32_t num_fields, const char* const* field_names,
+                                    const double* field_values, double time);
+
 /* last error text of the context (never NULL) */
 const char* fem_gpu_last_error(const fem_gpu_ctx* ctx);
 

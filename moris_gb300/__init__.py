@@ -134,6 +134,7 @@ class FemModel:
         self._check(self.L.fem_gpu_create(C.byref(d), C.byref(h)), "create", ctx=False)
         self.h = h
         self.num_sets = 0
+        self.num_nodes = len(coords) // dim
 
     def __del__(self):
         if getattr(self, "h", None):

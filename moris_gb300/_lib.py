@@ -145,6 +145,8 @@ SIGNATURES = {
     "fem_gpu_probe_dmma_tflops": (I32, [I32, I32, P]),
     "fem_gpu_launch_count": (I64, [P]),
     "fem_gpu_last_error": (C.c_char_p, [P]),
+    "fem_gpu_nodal_field": (I32, [P, P, P]),
+    "fem_vis_write_exodus": (I32, [C.c_char_p, I32, I64, P, I64, I32, P, C.c_char_p, I32, P, P, D]),
 }
 
 _lib = None

@@ -708,6 +708,23 @@ bool pick_bulk(int dim, int ngp, int nb, bool rect, BulkVariant* out, int& NBsel
 // ===========================================================================
 using namespace fem;
 
+namespace fem_nodal {
+
+__global__ void nodal_field_kernel(int64_t nn, int dim, int64_t nu, const int64_t* off, const int32_t* rank,
+                                   const double* w, const double* u, double* out) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nn * dim;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int f = (int)(t / nn);
+        const int64_t n = t - f * nn;
+        double s = 0.0;
+        for (int64_t k = off[n]; k < off[n + 1]; ++k)
+            if (rank[k] >= 0) s = fma(w[k], u[f * nu + rank[k]], s);
+        out[t] = s;
+    }
+}
+
+}  // namespace fem_nodal
+
 namespace {
 
 fem_gpu_status check_kernel(fem_gpu_ctx* c, const char* what) {
@@ -1321,6 +1338,40 @@ fem_gpu_status fem_gpu_assemble(fem_gpu_ctx* c, const double* u, double* vals, d
     release(c, sr);
     if (st != FEM_GPU_OK) return st;
     return read_status(c);
+}
+
+// nodal values of an adof field at the interpolation-mesh nodes through the
+// node extraction rows (the values the reference's VIS output evaluates at
+// the vertices, VIS::Output_Manager::write_field, FEM/VIS/src/
+// cl_VIS_Output_Manager.cpp:679-785): out[f][node] = sum_k w_k u[f nu + rank_k]
+fem_gpu_status fem_gpu_nodal_field(fem_gpu_ctx* c, const double* u, double* out) {
+    if (!c || !u || !out) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    const int64_t nn = c->num_nodes, nz = (int64_t)c->t_bases.size();
+    std::vector<int32_t> rk(nz);
+    for (int64_t k = 0; k < nz; ++k) rk[k] = (int32_t)c->basis_rank[c->t_bases[k]];
+    int64_t* doff = nullptr;
+    int32_t* drk = nullptr;
+    double* dw = nullptr;
+    cudaStream_t sm = stream_of(c);
+    cudaError_t e = cudaMallocAsync(&doff, (nn + 1) * sizeof(int64_t), sm);
+    if (e == cudaSuccess) e = cudaMallocAsync(&drk, std::max<int64_t>(nz, 1) * sizeof(int32_t), sm);
+    if (e == cudaSuccess) e = cudaMallocAsync(&dw, std::max<int64_t>(nz, 1) * sizeof(double), sm);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(doff, c->t_off.data(), (nn + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess && nz) e = cudaMemcpyAsync(drk, rk.data(), nz * sizeof(int32_t), cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess && nz) e = cudaMemcpyAsync(dw, c->t_w.data(), nz * sizeof(double), cudaMemcpyHostToDevice, sm);
+    if (e == cudaSuccess) {
+        const int64_t n = nn * c->dim;
+        fem_nodal::nodal_field_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, sm>>>(
+            nn, c->dim, c->num_used, doff, drk, dw, u, out);
+        ++c->launches;
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(doff, sm);
+    cudaFreeAsync(drk, sm);
+    cudaFreeAsync(dw, sm);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+    return e == cudaSuccess ? FEM_GPU_OK : cuda_fail(c, e, "nodal field");
 }
 
 fem_gpu_status fem_gpu_check_status(fem_gpu_ctx* c) {

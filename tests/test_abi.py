@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "fem_gpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"\b(fem_(?:gpu|hmr|cnn|lpc|xtk|gen|mg)_\w+)\s*\(", src)
+    names = re.findall(r"\b(fem_(?:gpu|hmr|cnn|lpc|xtk|gen|mg|vis)_\w+)\s*\(", src)
     return sorted(set(names))
 
 

@@ -491,6 +491,10 @@ fem_gpu_status fem_cnn_train_step(fem_cnn* c, const float* in4, const float* tar
 // interpolation of coarse node values, R = P^T.
 namespace {
 
+unsigned lpc_grid(int64_t work) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 32));
+}
+
 __device__ __forceinline__ float hat(int d, int F) {
     const int a = d < 0 ? -d : d;
     return a >= F ? 0.f : 1.f - (float)a / (float)F;
@@ -729,8 +733,8 @@ fem_gpu_status fem_lpc_restrict(int32_t nf, int32_t factor, const double* r_dev,
     if (!r_dev || !coarse_dev || factor < 1 || nf < 2 || (nf - 1) % factor) return FEM_GPU_BAD_ARG;
     const int nc = (nf - 1) / factor + 1;
     const int64_t Vc = (int64_t)nc * nc * nc;
-    restrict_kernel<<<512, 256>>>(nf, nc, factor, r_dev, coarse_dev, 4, 1.0);
-    if (rho_dev) density_channel_kernel<<<256, 256>>>(nf, nc, factor, rho_dev, coarse_dev);
+    restrict_kernel<<<lpc_grid(Vc * 3), 256>>>(nf, nc, factor, r_dev, coarse_dev, 4, 1.0);
+    if (rho_dev) density_channel_kernel<<<lpc_grid(Vc), 256>>>(nf, nc, factor, rho_dev, coarse_dev);
     // the norm on the device (one double back); the library-wide accumulator
     // makes concurrent calls race, like the rest of the net's entry points
     const double zero = 0.0;
@@ -767,7 +771,8 @@ fem_gpu_status fem_lpc_inject(int32_t nf, int32_t factor, const double* e_dev, d
 // z += scale * P c (c: coarse channels-last [Vc][3])
 fem_gpu_status fem_lpc_prolong_add(int32_t nf, int32_t factor, const float* coarse3, double scale, double* z) {
     if (!coarse3 || !z || factor < 1 || nf < 2 || (nf - 1) % factor) return FEM_GPU_BAD_ARG;
-    prolong_add_kernel<<<512, 256>>>(nf, (nf - 1) / factor + 1, factor, coarse3, scale, z);
+    prolong_add_kernel<<<lpc_grid(3 * (int64_t)nf * nf * nf), 256>>>(nf, (nf - 1) / factor + 1, factor, coarse3, scale,
+                                                                    z);
     return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
 }
 
@@ -775,7 +780,8 @@ fem_gpu_status fem_lpc_prolong_add(int32_t nf, int32_t factor, const float* coar
 fem_gpu_status fem_lpc_prolong_transpose(int32_t nf, int32_t factor, const double* fine, double scale,
                                          float* coarse3) {
     if (!coarse3 || !fine || factor < 1 || nf < 2 || (nf - 1) % factor) return FEM_GPU_BAD_ARG;
-    restrict_kernel<<<512, 256>>>(nf, (nf - 1) / factor + 1, factor, fine, coarse3, 3, scale);
+    const int64_t nc3 = (int64_t)((nf - 1) / factor + 1) * ((nf - 1) / factor + 1) * ((nf - 1) / factor + 1);
+    restrict_kernel<<<lpc_grid(3 * nc3), 256>>>(nf, (nf - 1) / factor + 1, factor, fine, coarse3, 3, scale);
     return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
 }
 
@@ -848,6 +854,7 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
     if (e == cudaSuccess) e = alloc((void**)&Q, (size_t)(M + 1) * n * 8);
     if (cnn && e == cudaSuccess) {
         e = alloc((void**)&cin, cnn->V * 4 * sizeof(float));
+        if (e == cudaSuccess) e = cudaMemset(cin, 0, cnn->V * 4 * sizeof(float));
         if (e == cudaSuccess) e = alloc((void**)&cout, cnn->V * 3 * sizeof(float));
     }
     auto cleanup = [&]() {
@@ -881,13 +888,17 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         }
         if (!net_on) return true;
         double s = 0.0;
-        if (fem_lpc_restrict(nf, factor, r, node_density, cin, &s) != FEM_GPU_OK) return false;
+        // the density channel of cin was written once before the loop
+        if (fem_lpc_restrict(nf, factor, r, nullptr, cin, &s) != FEM_GPU_OK) return false;
         if (s > 0.0) {
             if (fem_cnn_forward(cnn, cin, 1, cout) != FEM_GPU_OK) return false;
-            prolong_add_kernel<<<512, 256>>>(nf, nc, factor, cout, s * cnn->out_scale, z);
+            prolong_add_kernel<<<lpc_grid(3 * (int64_t)nf * nf * nf), 256>>>(nf, nc, factor, cout, s * cnn->out_scale,
+                                                                           z);
         }
         return cudaGetLastError() == cudaSuccess;
     };
+    if (cnn && node_density) density_channel_kernel<<<lpc_grid((int64_t)nc * nc * nc), 256>>>(nf, nc, factor,
+                                                                                                node_density, cin);
     cudaMemset(dots, 0, kMaxM * 8);
     fcg_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb>>>(n, rowptr, colidx, vals, dinv);
     fcg_residual<<<rb, tpb>>>(n, rowptr, colidx, vals, b, x, r, dots);

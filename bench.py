@@ -368,8 +368,7 @@ def run_c4(stream, args):
            "pcg_converged": {"state": sol["pcg_u"]["converged"], "adjoint": sol["pcg_lambda"]["converged"]},
            "adjoint_kernel_ms": ms_adj, "vertices_per_s": n_inter / (ms_adj * 1e-3), "chain_ms": ms_chain,
            "fd_check": {"coefficients": int(len(pick)), "h": h, "max_abs_err_over_max_dqdp": worst},
-           "setup_seconds": setup,
-           "decomposition": {"host_seconds": t_host, "device_seconds": t_dev, "identical_arrays": bool(same)}}
+           "setup_seconds": setup}
     if not args.no_cpu:
         # the reference's finite-difference dR/dp (forward FD of IG vertex coordinates),
         # restated on the oracle, timed on a sample of intersection vertices

@@ -468,8 +468,9 @@ fem_gpu_status fem_gpu_fcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_
    Chebyshev-accelerated point-Jacobi smoothing (the reference smooths with
    SOR) and a dense inverse on the coarsest grid (the reference uses LU).
    For 3D models on a cubic node grid of n^3 nodes (adof f n^3 + node, node =
-   x + n (y + n z)) whose operator is the 27-point nodal stencil of linear
-   B-splines; n - 1 must halve down to <= coarse_max.  Work is issued on the
+   x + n (y + n z)) whose operator is the symmetric 27-point nodal stencil of
+   linear B-splines (FEM_GPU_BAD_ARG otherwise); n - 1 must halve down to
+   <= coarse_max.  Work is issued on the
    legacy default stream. */
 typedef struct fem_mg fem_mg;
 typedef struct fem_mg_opts {

@@ -17,8 +17,9 @@
 //     with the node index fastest, so a warp reads 32 consecutive nodes of one
 //     coefficient; level 0 is scattered from the CSR, level l+1 = P^T S_l P is
 //     formed on the device (one thread per coarse node and component pair,
-//     the 27 x 27 fine offset pairs unrolled so that the 27 coarse taps stay
-//     in registers);
+//     the 27 x 27 fine offset pairs unrolled so that the coarse taps stay in
+//     registers; the 14 taps up to the centre are summed, the other 13 are
+//     mirrored from the neighbours, the Galerkin operator being symmetric);
 //   * smoothing is Chebyshev-accelerated point Jacobi of degree `degree` on
 //     [lo, hi] * lambda_max(D^-1 A) (lambda_max by power iteration): SOR is
 //     sequential, a polynomial in D^-1 A is one stencil sweep per degree.  Pre-
@@ -363,7 +364,8 @@ __global__ void __launch_bounds__(128) mg_rap(int nf, int nc, const double* __re
                                             if (tx >= ntarget(sx)) continue;
                                             const int kc = (target(sx, tx) + 1) + 3 * (target(sy, ty) + 1) +
                                                            9 * (target(sz, tz) + 1);
-                                            acc[kc] += vp;
+                                            // taps above the centre follow by symmetry (mg_rap_mirror)
+                                            if (kc <= 13) acc[kc] += vp;
                                         }
                                     }
                                 }
@@ -372,7 +374,49 @@ __global__ void __launch_bounds__(128) mg_rap(int nf, int nc, const double* __re
             }
         }
 #pragma unroll
-        for (int k = 0; k < 27; ++k) Sc[sidx(k, f, g, Nc, I)] = acc[k];
+        for (int k = 0; k <= 13; ++k) Sc[sidx(k, f, g, Nc, I)] = acc[k];
+    }
+}
+
+// err |= 2 where the level-0 operator is not symmetric (A_ij vs A_ji beyond
+// the rounding of the assembly's atomic sums, relative to the entries and to
+// the diagonals of rows i and j)
+__global__ void mg_check_symmetric(int n, const double* __restrict__ S, int* err) {
+    const int64_t N = (int64_t)n * n * n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 14 * 9 * N;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t I = t % N;
+        const int fg = (int)((t / N) % 9), k = (int)(t / (9 * N));
+        const int f = fg / 3, g = fg % 3;
+        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+        const int X = (int)(I % n), Y = (int)((I / n) % n), Z = (int)(I / ((int64_t)n * n));
+        if (X + dx < 0 || X + dx >= n || Y + dy < 0 || Y + dy >= n || Z + dz < 0 || Z + dz >= n) continue;
+        const int64_t J = I + dx + (int64_t)n * (dy + (int64_t)n * dz);
+        const double a = S[sidx(k, f, g, N, I)], b = S[sidx(26 - k, g, f, N, J)];
+        // entries that cancel to near zero carry the rounding of their terms, which
+        // scale with the diagonal: measure the asymmetry against the diagonals too
+        const double dd = sqrt(fabs(S[sidx(13, f, f, N, I)] * S[sidx(13, g, g, N, J)]));
+        if (!(fabs(a - b) <= 1e-10 * (fabs(a) + fabs(b)) + 1e-12 * dd)) atomicOr(err, 2);
+    }
+}
+
+// the coarse operator is symmetric: tap k > 13 of node I, rows f / columns g,
+// is tap 26 - k of the neighbour J = I + off_k with f and g swapped
+__global__ void mg_rap_mirror(int nc, double* __restrict__ Sc) {
+    const int64_t Nc = (int64_t)nc * nc * nc;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 13 * 9 * Nc;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t I = t % Nc;
+        const int fg = (int)((t / Nc) % 9), k = 14 + (int)(t / (9 * Nc));
+        const int f = fg / 3, g = fg % 3;
+        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+        const int X = (int)(I % nc), Y = (int)((I / nc) % nc), Z = (int)(I / ((int64_t)nc * nc));
+        double v = 0.0;
+        if (X + dx >= 0 && X + dx < nc && Y + dy >= 0 && Y + dy < nc && Z + dz >= 0 && Z + dz < nc) {
+            const int64_t J = I + dx + (int64_t)nc * (dy + (int64_t)nc * dz);
+            v = Sc[sidx(26 - k, g, f, Nc, J)];
+        }
+        Sc[sidx(k, f, g, Nc, I)] = v;
     }
 }
 
@@ -654,13 +698,17 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
     cudaMemset(L0.S, 0, 243 * L0.N * sizeof(double));
     cudaMemset(g->err, 0, sizeof(int));
     mg_csr_to_stencil<<<blocks_for(3 * L0.N, kTpb), kTpb>>>(L0.n, rowptr, colidx, vals, L0.S, g->err);
-    for (size_t l = 0; l + 1 < g->lv.size(); ++l)
+    mg_check_symmetric<<<blocks_for(126 * L0.N, kTpb), kTpb>>>(L0.n, L0.S, g->err);
+    for (size_t l = 0; l + 1 < g->lv.size(); ++l) {
         mg_rap<<<blocks_for(9 * g->lv[l + 1].N, 128), 128>>>(g->lv[l].n, g->lv[l + 1].n, g->lv[l].S, g->lv[l + 1].S);
+        mg_rap_mirror<<<blocks_for(117 * g->lv[l + 1].N, kTpb), kTpb>>>(g->lv[l + 1].n, g->lv[l + 1].S);
+    }
     int herr = 0;
     cudaMemcpy(&herr, g->err, sizeof(int), cudaMemcpyDeviceToHost);
     if (herr) {
         delete g;
-        return fail(c, FEM_GPU_BAD_ARG, "multigrid: operator is not a 27-point nodal stencil on the node grid");
+        return fail(c, FEM_GPU_BAD_ARG, (herr & 1) ? "multigrid: operator is not a 27-point nodal stencil on the node grid"
+                                                   : "multigrid: operator is not symmetric");
     }
     // smoother data: diagonal, FP32 copies, lambda_max(D^-1 A) by power iteration
     // (FP64, in two scratch vectors of the finest size)

@@ -158,3 +158,21 @@ def test_oracle_threaded_pcg_matches_serial():
     x4, it4, r4, rc4 = pcg_mt(A.indptr, A.indices, A.data, -b, rtol=1e-10, max_iter=5000, nthreads=4)
     assert rc1 == 0 and rc4 == 0 and abs(it1 - it4) <= 1
     assert np.linalg.norm(x4 - x1) <= 1e-8 * np.linalg.norm(x1)
+
+
+@pytest.mark.gpu
+def test_unsymmetric_operator_is_rejected(torch):
+    """The hierarchy mirrors half of each Galerkin stencil, so it needs a
+    symmetric operator: one perturbed off-diagonal entry is refused."""
+    from moris_gb300 import FemGpuError
+    from moris_gb300.multigrid import Multigrid
+    m, rp, ci, vals, b, A = device_system(8)
+    bad = vals.clone()
+    row = 5
+    cols = ci[int(rp[row]):int(rp[row + 1])].cpu().numpy()
+    k = int(rp[row]) + int(np.nonzero(cols != row)[0][0])  # an off-diagonal entry of row 5
+    bad[k] *= 1.5
+    with pytest.raises(FemGpuError) as e:
+        Multigrid(m, rp, ci, bad)
+    assert e.value.status == 1
+    Multigrid(m, rp, ci, vals).close()  # the symmetric one is accepted

@@ -395,8 +395,10 @@ __global__ void mg_check_symmetric(int n, const double* __restrict__ S, int* err
         const double a = S[sidx(k, f, g, N, I)], b = S[sidx(26 - k, g, f, N, J)];
         // entries that cancel to near zero carry the rounding of their terms, which
         // scale with the diagonal: measure the asymmetry against the diagonals too
-        const double dd = sqrt(fabs(S[sidx(13, f, f, N, I)] * S[sidx(13, g, g, N, J)]));
-        if (!(fabs(a - b) <= 1e-10 * (fabs(a) + fabs(b)) + 1e-12 * dd)) atomicOr(err, 2);
+        // the threshold in FP32 (a square root on the FP64 pipe costs far more)
+        const float dd = sqrtf(fabsf((float)S[sidx(13, f, f, N, I)]) * fabsf((float)S[sidx(13, g, g, N, J)]));
+        const float tol = 1e-10f * (float)(fabs(a) + fabs(b)) + 1e-12f * dd;
+        if (!((float)fabs(a - b) <= tol)) atomicOr(err, 2);
     }
 }
 

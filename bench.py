@@ -22,6 +22,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -103,7 +104,9 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % gpu_index)
+        # the raw samples (the JSON line carries their summary); BENCH_CLOCKS_DIR keeps them
+        self.path = os.path.join(os.environ.get("BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                                 "clocks_bench_%d.csv" % gpu_index)
 
     def start(self):
         try:

@@ -497,7 +497,7 @@ fem_gpu_status fem_mg_get_stencil(const fem_mg* mg, int32_t level, double* host_
 /* one V-cycle z = V r (device vectors of num_adofs doubles) */
 fem_gpu_status fem_mg_apply(fem_mg* mg, const double* r, double* z);
 /* fem_gpu_fcg with the V-cycle in place of D^-1: M(r) = V r (+ the learned
-   correction P sigma s f(R r / s) when cnn is given); same judge.  A learned
+   correction P sigma s f(R r / s) when cnn is given); same convergence test.  A learned
    correction that stalls the solve (4 iterations without a 10 % residual
    reduction) is switched off and the solve continues with the V-cycle alone
    (*used_fallback = 2); Jacobi-PCG stays the last fallback (*used_fallback = 1). */

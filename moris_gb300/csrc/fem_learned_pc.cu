@@ -980,7 +980,7 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         st = fem_gpu_pcg(c, rowptr, colidx, vals, b, x, &o, &pr, 0);
         fb_iters = pr.iterations;
     }
-    // judge: true residual of the final iterate
+    // convergence test: the true residual of the final iterate
     cudaMemset(dots, 0, kMaxM * 8);
     fcg_residual<<<rb, tpb>>>(n, rowptr, colidx, vals, b, x, r, dots);
     readn(2);

@@ -138,3 +138,6 @@ void sensitivity_release(fem_gpu_ctx* c);
 
 // one multigrid V-cycle z = V r on the legacy default stream (fem_multigrid.cu)
 bool mg_vcycle(fem_mg* g, const double* r, double* z);
+// q = A p with the hierarchy's level-0 FP64 stencil (the operator the CSR
+// holds, without column indices) and dot += p.q
+bool mg_operator(fem_mg* g, const double* p, double* q, double* dot);

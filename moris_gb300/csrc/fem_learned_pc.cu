@@ -937,7 +937,15 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         fcg_orthogonalize<<<vb, tpb>>>(n, z, ps, cf, m, r, p, dots);
         readn(1);
         const double pr = hd[0];
-        fcg_spmv_dot<<<rb, tpb>>>(n, rowptr, colidx, vals, p, q, dots);
+        if (mg) {
+            // the level-0 stencil of the hierarchy is the CSR's operator without indices
+            if (!mg_operator(mg, p, q, dots)) {
+                ok = false;
+                break;
+            }
+        } else {
+            fcg_spmv_dot<<<rb, tpb>>>(n, rowptr, colidx, vals, p, q, dots);
+        }
         readn(1);
         const double pAp = hd[0];
         if (!(pAp > 0.0) || !std::isfinite(pr)) {

@@ -183,6 +183,23 @@ __global__ void mg_convert(int64_t m, const TA* __restrict__ a, TB* __restrict__
         b[t] = (TB)a[t];
 }
 
+// q = A p on an FP64 stencil and dot += p.q (the outer Krylov product)
+__global__ void mg_apply_dot(int n, const double* __restrict__ S, const double* __restrict__ p, double* __restrict__ q,
+                             double* dot) {
+    const int64_t N = (int64_t)n * n * n;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        double s[3];
+        stencil_rows<double, double>(n, N, S, p, i, s);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            q[f * N + i] = s[f];
+            acc = fma(p[f * N + i], s[f], acc);
+        }
+    }
+    mg_block_sum_add(acc, dot);
+}
+
 // Chebyshev start with x = 0: r = b, d = D^-1 b / theta, x = d
 template <typename TV>
 __global__ void mg_cheb_init(int64_t m, const TV* __restrict__ b, const TV* __restrict__ dinv, TV inv_theta,
@@ -623,6 +640,13 @@ double power_lambda(fem_mg* g, const fem_mg::Level& L, const TS* S, const TV* di
 }
 
 }  // namespace
+
+bool mg_operator(fem_mg* g, const double* p, double* q, double* dot) {
+    if (!g) return false;
+    const fem_mg::Level& L = g->lv[0];
+    mg_apply_dot<<<blocks_for(L.N, kTpb), kTpb>>>(L.n, L.S, p, q, dot);
+    return cudaGetLastError() == cudaSuccess;
+}
 
 bool mg_vcycle(fem_mg* g, const double* r, double* z) {
     if (!g) return false;

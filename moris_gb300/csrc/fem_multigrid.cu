@@ -16,10 +16,8 @@
 //     (tap k = (dx+1) + 3 (dy+1) + 9 (dz+1); f, g displacement components)
 //     with the node index fastest, so a warp reads 32 consecutive nodes of one
 //     coefficient; level 0 is scattered from the CSR, level l+1 = P^T S_l P is
-//     formed on the device (one thread per coarse node and component pair,
-//     the 27 x 27 fine offset pairs unrolled so that the coarse taps stay in
-//     registers; the 14 taps up to the centre are summed, the other 13 are
-//     mirrored from the neighbours, the Galerkin operator being symmetric);
+//     formed on the device one axis at a time (P is a Kronecker product of
+//     1D two-scale relations), each pass a thread per node and component pair;
 //   * smoothing is Chebyshev-accelerated point Jacobi of degree `degree` on
 //     [lo, hi] * lambda_max(D^-1 A) (lambda_max by power iteration): SOR is
 //     sequential, a polynomial in D^-1 A is one stencil sweep per degree.  Pre-
@@ -326,74 +324,10 @@ __global__ void mg_prolong(int nf, int nc, const TC* __restrict__ xc, TF* __rest
     }
 }
 
-// Galerkin product Sc = P^T Sf P, one thread per (coarse node, f, g): for fine
-// offsets a (coarse node I -> fine node 2I + a, weight w_a) and stencil taps b
-// (fine node j = 2I + a + b), the fine column j interpolates from the coarse
-// nodes J = I + kc with |a + b - 2 kc| <= 1 per direction (weight 1 for an
-// even sum, 1/2 for each of the two neighbours of an odd one).
+// 1D two-scale targets: fine offset sum s (a + b) reaches the coarse tap s / 2
+// (weight 1) when even, the two taps (s -+ 1) / 2 (weight 1/2 each) when odd
 __device__ __forceinline__ int ntarget(int s) { return (s & 1) ? 2 : 1; }
 __device__ __forceinline__ int target(int s, int t) { return (s & 1) ? ((s - 1) >> 1) + t : (s >> 1); }
-
-__global__ void __launch_bounds__(128) mg_rap(int nf, int nc, const double* __restrict__ Sf, double* __restrict__ Sc) {
-    const int64_t Nc = (int64_t)nc * nc * nc, Nf = (int64_t)nf * nf * nf;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 9 * Nc; t += (int64_t)gridDim.x * blockDim.x) {
-        const int fg = (int)(t / Nc);
-        const int64_t I = t - fg * Nc;
-        const int f = fg / 3, g = fg % 3;
-        const int X = (int)(I % nc), Y = (int)((I / nc) % nc), Z = (int)(I / ((int64_t)nc * nc));
-        double acc[27];
-#pragma unroll
-        for (int k = 0; k < 27; ++k) acc[k] = 0.0;
-#pragma unroll
-        for (int az = -1; az <= 1; ++az) {
-            const int z = 2 * Z + az;
-            if (z < 0 || z >= nf) continue;
-#pragma unroll
-            for (int ay = -1; ay <= 1; ++ay) {
-                const int y = 2 * Y + ay;
-                if (y < 0 || y >= nf) continue;
-#pragma unroll
-                for (int ax = -1; ax <= 1; ++ax) {
-                    const int x = 2 * X + ax;
-                    if (x < 0 || x >= nf) continue;
-                    const double wa = (ax ? 0.5 : 1.0) * (ay ? 0.5 : 1.0) * (az ? 0.5 : 1.0);
-                    const int64_t i = x + (int64_t)nf * (y + (int64_t)nf * z);
-#pragma unroll
-                    for (int bz = -1; bz <= 1; ++bz)
-#pragma unroll
-                        for (int by = -1; by <= 1; ++by)
-#pragma unroll
-                            for (int bx = -1; bx <= 1; ++bx) {
-                                const int kb = (bx + 1) + 3 * (by + 1) + 9 * (bz + 1);
-                                const double v = wa * __ldg(Sf + sidx(kb, f, g, Nf, i));
-                                const int sx = ax + bx, sy = ay + by, sz = az + bz;
-                                const double pw = ((sx & 1) ? 0.5 : 1.0) * ((sy & 1) ? 0.5 : 1.0) *
-                                                  ((sz & 1) ? 0.5 : 1.0);
-                                const double vp = v * pw;
-#pragma unroll
-                                for (int tz = 0; tz < 2; ++tz) {
-                                    if (tz >= ntarget(sz)) continue;
-#pragma unroll
-                                    for (int ty = 0; ty < 2; ++ty) {
-                                        if (ty >= ntarget(sy)) continue;
-#pragma unroll
-                                        for (int tx = 0; tx < 2; ++tx) {
-                                            if (tx >= ntarget(sx)) continue;
-                                            const int kc = (target(sx, tx) + 1) + 3 * (target(sy, ty) + 1) +
-                                                           9 * (target(sz, tz) + 1);
-                                            // taps above the centre follow by symmetry (mg_rap_mirror)
-                                            if (kc <= 13) acc[kc] += vp;
-                                        }
-                                    }
-                                }
-                            }
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k <= 13; ++k) Sc[sidx(k, f, g, Nc, I)] = acc[k];
-    }
-}
 
 // err |= 2 where the level-0 operator is not symmetric (A_ij vs A_ji beyond
 // the rounding of the assembly's atomic sums, relative to the entries and to
@@ -419,23 +353,62 @@ __global__ void mg_check_symmetric(int n, const double* __restrict__ S, int* err
     }
 }
 
-// the coarse operator is symmetric: tap k > 13 of node I, rows f / columns g,
-// is tap 26 - k of the neighbour J = I + off_k with f and g swapped
-__global__ void mg_rap_mirror(int nc, double* __restrict__ Sc) {
-    const int64_t Nc = (int64_t)nc * nc * nc;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 13 * 9 * Nc;
+// One-axis Galerkin coarsening of a 27-point block stencil: P = P_z (x) P_y (x)
+// P_x is separable, so P^T S P is three passes, each coarsening one axis of an
+// (nx, ny, nz) node box with the 1D two-scale relation while the taps along
+// the other two axes pass through.  One thread per output node and component
+// pair; the 3 x 3 (a, b) pairs along the axis times the 9 taps across it are
+// unrolled (117 FMAs for the 27 output taps).
+__host__ __device__ __forceinline__ int tap_of(int AX, int along, int o1, int o2) {
+    int d[3];
+    d[AX] = along;
+    d[(AX + 1) % 3] = o1;
+    d[(AX + 2) % 3] = o2;
+    return (d[0] + 1) + 3 * (d[1] + 1) + 9 * (d[2] + 1);
+}
+
+template <int AX>
+__global__ void __launch_bounds__(128) mg_rap_axis(int3 din, int3 dout, const double* __restrict__ Sin,
+                                                   double* __restrict__ Sout) {
+    const int64_t Nin = (int64_t)din.x * din.y * din.z, Nout = (int64_t)dout.x * dout.y * dout.z;
+    const int nin_ax = AX == 0 ? din.x : AX == 1 ? din.y : din.z;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 9 * Nout;
          t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t I = t % Nc;
-        const int fg = (int)((t / Nc) % 9), k = 14 + (int)(t / (9 * Nc));
+        const int fg = (int)(t / Nout);
+        const int64_t I = t - fg * Nout;
         const int f = fg / 3, g = fg % 3;
-        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-        const int X = (int)(I % nc), Y = (int)((I / nc) % nc), Z = (int)(I / ((int64_t)nc * nc));
-        double v = 0.0;
-        if (X + dx >= 0 && X + dx < nc && Y + dy >= 0 && Y + dy < nc && Z + dz >= 0 && Z + dz < nc) {
-            const int64_t J = I + dx + (int64_t)nc * (dy + (int64_t)nc * dz);
-            v = Sc[sidx(26 - k, g, f, Nc, J)];
+        int c[3] = {(int)(I % dout.x), (int)((I / dout.x) % dout.y), (int)(I / ((int64_t)dout.x * dout.y))};
+        const int C = c[AX];
+        double acc[27];
+#pragma unroll
+        for (int k = 0; k < 27; ++k) acc[k] = 0.0;
+#pragma unroll
+        for (int a = -1; a <= 1; ++a) {
+            const int fc = 2 * C + a;
+            if (fc < 0 || fc >= nin_ax) continue;
+            int ci[3] = {c[0], c[1], c[2]};
+            ci[AX] = fc;
+            const int64_t i = ci[0] + (int64_t)din.x * (ci[1] + (int64_t)din.y * ci[2]);
+            const double wa = a ? 0.5 : 1.0;
+#pragma unroll
+            for (int b = -1; b <= 1; ++b) {
+                const int sm = a + b;
+                const double pw = (sm & 1) ? 0.5 : 1.0;
+#pragma unroll
+                for (int o2 = -1; o2 <= 1; ++o2)
+#pragma unroll
+                    for (int o1 = -1; o1 <= 1; ++o1) {
+                        const double v = wa * pw * __ldg(Sin + sidx(tap_of(AX, b, o1, o2), f, g, Nin, i));
+#pragma unroll
+                        for (int tt = 0; tt < 2; ++tt) {
+                            if (tt >= ntarget(sm)) continue;
+                            acc[tap_of(AX, target(sm, tt), o1, o2)] += v;
+                        }
+                    }
+            }
         }
-        Sc[sidx(k, f, g, Nc, I)] = v;
+#pragma unroll
+        for (int k = 0; k < 27; ++k) Sout[sidx(k, f, g, Nout, I)] = acc[k];
     }
 }
 
@@ -725,9 +698,26 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
     cudaMemset(g->err, 0, sizeof(int));
     mg_csr_to_stencil<<<blocks_for(3 * L0.N, kTpb), kTpb>>>(L0.n, rowptr, colidx, vals, L0.S, g->err);
     mg_check_symmetric<<<blocks_for(126 * L0.N, kTpb), kTpb>>>(L0.n, L0.S, g->err);
-    for (size_t l = 0; l + 1 < g->lv.size(); ++l) {
-        mg_rap<<<blocks_for(9 * g->lv[l + 1].N, 128), 128>>>(g->lv[l].n, g->lv[l + 1].n, g->lv[l].S, g->lv[l + 1].S);
-        mg_rap_mirror<<<blocks_for(117 * g->lv[l + 1].N, kTpb), kTpb>>>(g->lv[l + 1].n, g->lv[l + 1].S);
+    {
+        // Galerkin products axis by axis through two scratch boxes (freed after setup)
+        const int64_t n0 = L0.n, n1 = (n0 - 1) / 2 + 1;
+        double *t1 = nullptr, *t2 = nullptr;
+        if (cudaMalloc(&t1, 243 * n0 * n0 * n1 * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&t2, 243 * n0 * n1 * n1 * sizeof(double)) != cudaSuccess) {
+            cudaFree(t1);
+            delete g;
+            return fail(c, FEM_GPU_OUT_OF_MEMORY, "multigrid Galerkin scratch");
+        }
+        for (size_t l = 0; l + 1 < g->lv.size(); ++l) {
+            const int nf = g->lv[l].n, ncs = g->lv[l + 1].n;
+            const int3 a{nf, nf, nf}, b{nf, nf, ncs}, cc{nf, ncs, ncs}, d{ncs, ncs, ncs};
+            mg_rap_axis<2><<<blocks_for(9 * (int64_t)b.x * b.y * b.z, 128), 128>>>(a, b, g->lv[l].S, t1);
+            mg_rap_axis<1><<<blocks_for(9 * (int64_t)cc.x * cc.y * cc.z, 128), 128>>>(b, cc, t1, t2);
+            mg_rap_axis<0><<<blocks_for(9 * (int64_t)d.x * d.y * d.z, 128), 128>>>(cc, d, t2, g->lv[l + 1].S);
+        }
+        cudaDeviceSynchronize();
+        cudaFree(t1);
+        cudaFree(t2);
     }
     int herr = 0;
     cudaMemcpy(&herr, g->err, sizeof(int), cudaMemcpyDeviceToHost);

@@ -125,7 +125,9 @@ typedef struct fem_gpu_mesh_desc {
    trivial clusters (the integration cell is the interpolation cell);
    otherwise cluster c integrates IG cells [ig_offsets[c], ig_offsets[c+1])
    with ig_coords / ig_param_coords (vertices x dim, node-major) giving the
-   physical and IP-parametric vertex coordinates. */
+   physical and IP-parametric vertex coordinates.
+   A set of any kind may be empty (num_clusters / num_sides == 0, its arrays
+   may then be NULL): it keeps its set index and does no work. */
 typedef struct fem_gpu_bulk_set_desc {
     int32_t iwg_type;             /* FEM_GPU_IWG_STRUC_LINEAR_BULK */
     int32_t ig_cell_type;         /* FEM_GPU_CELL_* */

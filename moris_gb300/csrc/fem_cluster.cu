@@ -1083,6 +1083,7 @@ fem_gpu_status build_batch(fem_gpu_ctx* c, Batch* b) {
     b->nside = 0;
     for (size_t k = 0; k < c->sets.size(); ++k) {
         const SetData& s = c->sets[k];
+        if (s.neq == 0) continue;
         if (s.kind == 1) {
             b->nside++;
             continue;
@@ -1099,6 +1100,7 @@ fem_gpu_status build_batch(fem_gpu_ctx* c, Batch* b) {
         }
         add_items(s, (int)k, 0, s.neq, b->split, items, cost);
     }
+    if (!nb && items.empty() && warp_items.empty()) nb = 8;  // every volume set empty: the launch finds no items
     if (nb != 8 && nb != 27) return fail(c, FEM_GPU_UNSUPPORTED, "batched launch: basis width must be 8 or 27");
     std::vector<Item> ordered = lpt_order(items, cost);
     const int64_t ncta = (int64_t)ordered.size();
@@ -1142,7 +1144,7 @@ fem_gpu_status enqueue_batch(fem_gpu_ctx* c, Batch* b, const double* u, double* 
     a.mode = CM_ASSEMBLE;
     fem_gpu_status r = launch(c, k, a, st);
     for (size_t s = 0; s < c->sets.size() && r == FEM_GPU_OK; ++s)
-        if (c->sets[s].kind == 1) r = side(c, (int)s, u, vals, rhs, st);
+        if (c->sets[s].kind == 1 && c->sets[s].neq > 0) r = side(c, (int)s, u, vals, rhs, st);
     return r;
 }
 
@@ -1244,6 +1246,7 @@ void cluster_release(fem_gpu_ctx* c) {
 // one set through the cluster kernel (fem_gpu_assemble / fem_gpu_element_matrices)
 fem_gpu_status cluster_launch_set(fem_gpu_ctx* c, int set, int mode, int64_t first, int64_t count, const double* u,
                                   double* vals, double* rhs, double* Kout, double* Rout, int nmax) {
+    if (count <= 0) return FEM_GPU_OK;
     const SetData& s = c->sets[set];
     cudaStream_t st = (cudaStream_t)c->stream;
     SetDev d;

@@ -822,6 +822,7 @@ int sm_count() {
 fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int64_t count, const double* u,
                            double* vals, double* rhs, double* Kout, double* Rout, int nmax, const double* x,
                            double* y, int force_variant = -1) {
+    if (count <= 0) return FEM_GPU_OK;
     SetData& s = c->sets[si];
     BulkVariant vars[NUM_VARIANTS];
     int nbsel = 0;
@@ -892,6 +893,7 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
 
 fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int64_t count, const double* u,
                            double* vals, double* rhs, double* Kout, double* Rout, int nmax) {
+    if (count <= 0) return FEM_GPU_OK;
     SetData& s = c->sets[si];
     SetData& ds = s;
     SideArgs a{};
@@ -1059,6 +1061,7 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
         SetData& s = c->sets[k];
         SetData& ds = s;
         const int NPE = c->npe, D = c->dim;
+        if (s.neq == 0) continue;  // an empty set has no device data
         if (cluster_set(c, (int)k)) {
             if ((st = cluster_finalize(c, (int)k)) != FEM_GPU_OK) return st;
             continue;
@@ -1395,6 +1398,7 @@ fem_gpu_status fem_gpu_apply(fem_gpu_ctx* c, const double* x, double* y, uint32_
     if (!(flags & FEM_GPU_ACCUMULATE)) cudaMemsetAsync(sy.dev, 0, nad * sizeof(double), sm);
     for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
         SetData& s = c->sets[k];
+        if (s.neq == 0) continue;
         if (s.kind != 0) {
             st = fail(c, FEM_GPU_UNSUPPORTED, "matrix-free apply covers bulk sets only");
             break;
@@ -1438,7 +1442,7 @@ fem_gpu_status fem_gpu_autotune(fem_gpu_ctx* c, int64_t max_elements) {
     fem_gpu_status st = FEM_GPU_OK;
     for (int k = 0; k < (int)c->sets.size() && st == FEM_GPU_OK; ++k) {
         SetData& s = c->sets[k];
-        if (s.kind != 0 || !s.ig_off.empty()) continue;
+        if (s.kind != 0 || !s.ig_off.empty() || s.neq == 0) continue;
         const int64_t n = max_elements > 0 ? std::min(max_elements, s.neq) : s.neq;
         double best = 1e30;
         int bestv = s.variant;

@@ -317,7 +317,9 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     if (!c || !d) return FEM_GPU_BAD_ARG;
     if (c->host_final) return fail(c, FEM_GPU_BAD_ARG, "sets must be added before finalize");
     if (d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_BULK) return fail(c, FEM_GPU_UNSUPPORTED, "bulk iwg type");
-    if (d->num_clusters <= 0 || !d->cluster_ip_cell || !d->youngs_modulus)
+    // an empty set (no clusters, as on a processor or mesh without cut cells) is
+    // kept so that set indices stay those of the caller, and does no work
+    if (d->num_clusters < 0 || (d->num_clusters > 0 && (!d->cluster_ip_cell || !d->youngs_modulus)))
         return fail(c, FEM_GPU_BAD_ARG, "bulk set arrays");
     const Rule r = gauss_rule(d->integration_rule);
     const int igc = d->ig_cell_type;
@@ -326,7 +328,8 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     if (cell_param_dim(igc) != c->dim) return fail(c, FEM_GPU_BAD_ARG, "integration cell dimension");
     if (c->dim == 3 && d->model_type != FEM_GPU_MODEL_3D) return fail(c, FEM_GPU_BAD_ARG, "3D model type");
     if (c->dim == 2 && d->model_type == FEM_GPU_MODEL_3D) return fail(c, FEM_GPU_BAD_ARG, "2D model type");
-    if (!d->ig_offsets && igc != c->ip_cell) return fail(c, FEM_GPU_BAD_ARG, "trivial clusters need IG == IP cell");
+    if (!d->ig_offsets && igc != c->ip_cell && d->num_clusters > 0)
+        return fail(c, FEM_GPU_BAD_ARG, "trivial clusters need IG == IP cell");
     if (!(d->poisson_ratio > -1.0 && d->poisson_ratio < 0.5)) return fail(c, FEM_GPU_BAD_ARG, "poisson ratio");
     SetData s;
     s.kind = 0;
@@ -338,10 +341,12 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     s.E.assign(d->youngs_modulus, d->youngs_modulus + s.neq);
     for (double e : s.E)
         if (!std::isfinite(e)) return fail(c, FEM_GPU_NONFINITE, "youngs modulus");
-    if (d->ig_offsets) {
-        if (!d->ig_coords || !d->ig_param_coords) return fail(c, FEM_GPU_BAD_ARG, "integration cell arrays");
-        s.ig_off.assign(d->ig_offsets, d->ig_offsets + s.neq + 1);
+    if (d->ig_offsets || igc != c->ip_cell) {
+        if (d->ig_offsets) s.ig_off.assign(d->ig_offsets, d->ig_offsets + s.neq + 1);
+        else s.ig_off.assign(1, 0);
         const int64_t nig = s.ig_off[s.neq];
+        if (nig > 0 && (!d->ig_coords || !d->ig_param_coords))
+            return fail(c, FEM_GPU_BAD_ARG, "integration cell arrays");
         const int64_t per = (int64_t)cell_num_nodes(igc) * c->dim;
         s.ig_coords.assign(d->ig_coords, d->ig_coords + nig * per);
         s.ig_param.assign(d->ig_param_coords, d->ig_param_coords + nig * per);
@@ -378,7 +383,7 @@ fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* c, const fem_gpu_side_set_desc*
         d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE &&
         d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE)
         return fail(c, FEM_GPU_UNSUPPORTED, "side iwg type");
-    if (d->num_sides <= 0 || !d->side_ip_cell || !d->side_ordinal || !d->youngs_modulus)
+    if (d->num_sides < 0 || (d->num_sides > 0 && (!d->side_ip_cell || !d->side_ordinal || !d->youngs_modulus)))
         return fail(c, FEM_GPU_BAD_ARG, "side set arrays");
     const Rule r = gauss_rule(d->integration_rule);
     if (r.n == 0 || r.dim != c->dim - 1) return fail(c, FEM_GPU_BAD_ARG, "side integration rule");
@@ -418,9 +423,10 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
     const bool tri_rule = d->integration_rule == FEM_GPU_RULE_TRI_3 || d->integration_rule == FEM_GPU_RULE_TRI_7;
     if (tri_rule != (d->facet_cell_type == FEM_GPU_CELL_TRI3))
         return fail(c, FEM_GPU_BAD_ARG, "integration rule does not match the facet cell");
-    if (d->num_clusters <= 0 || !d->leader_ip_cell || !d->follower_ip_cell || !d->facet_offsets ||
-        !d->facet_coords || !d->leader_param_coords || !d->follower_param_coords || !d->leader_youngs_modulus ||
-        !d->follower_youngs_modulus)
+    if (d->num_clusters < 0 ||
+        (d->num_clusters > 0 && (!d->leader_ip_cell || !d->follower_ip_cell || !d->facet_offsets ||
+                                 !d->facet_coords || !d->leader_param_coords || !d->follower_param_coords ||
+                                 !d->leader_youngs_modulus || !d->follower_youngs_modulus)))
         return fail(c, FEM_GPU_BAD_ARG, "double-sided set arrays");
     if (!(d->poisson_ratio > -1.0 && d->poisson_ratio < 0.5)) return fail(c, FEM_GPU_BAD_ARG, "poisson ratio");
     if (!std::isfinite(d->alpha)) return fail(c, FEM_GPU_NONFINITE, "alpha");
@@ -434,7 +440,8 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
     for (int64_t i = 0; i < s.neq; ++i)
         if (s.ip_cell[i] < 0 || s.ip_cell[i] >= c->num_cells || s.fcell[i] < 0 || s.fcell[i] >= c->num_cells)
             return fail(c, FEM_GPU_OOB_INDEX, "double-sided cluster cell");
-    s.fc_off.assign(d->facet_offsets, d->facet_offsets + s.neq + 1);
+    if (s.neq) s.fc_off.assign(d->facet_offsets, d->facet_offsets + s.neq + 1);
+    else s.fc_off.assign(1, 0);
     if (s.fc_off[0] != 0) return fail(c, FEM_GPU_BAD_ARG, "facet offsets must start at 0");
     for (int64_t i = 0; i < s.neq; ++i)
         if (s.fc_off[i + 1] <= s.fc_off[i]) return fail(c, FEM_GPU_BAD_ARG, "every cluster needs a facet");
@@ -552,6 +559,9 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
     if (!c) return FEM_GPU_BAD_ARG;
     if (c->host_final) return FEM_GPU_OK;
     if (c->sets.empty()) return fail(c, FEM_GPU_BAD_ARG, "no sets");
+    int64_t total_eq = 0;
+    for (const auto& s : c->sets) total_eq += s.neq;
+    if (total_eq == 0) return fail(c, FEM_GPU_BAD_ARG, "no equation objects in any set");
     const int npe = c->npe, dim = c->dim;
     std::vector<char> cell_used(c->num_cells, 0);
     for (auto& s : c->sets) {

@@ -530,7 +530,7 @@ fem_gpu_status fem_gpu_set_ig_vertices(fem_gpu_ctx* c, int64_t nv, const int32_t
         }
     }
     for (auto& s : c->sets) {
-        if (!(is_cut(s) || is_interface(s))) continue;
+        if (!(is_cut(s) || is_interface(s)) || s.neq == 0) continue;
         if (s.vid.empty()) return fail(c, FEM_GPU_BAD_ARG, "cut / interface set without IG vertex ids");
         for (int32_t v : s.vid)
             if (v < 0 || v >= nv) return fail(c, FEM_GPU_OOB_INDEX, "IG vertex id");
@@ -560,6 +560,7 @@ fem_gpu_status fem_gpu_update_ig_vertices(fem_gpu_ctx* c, const double* t) {
     cudaStream_t st = (cudaStream_t)c->stream;
     cudaError_t e = cudaSuccess;
     for (auto& s : c->sets) {
+        if (s.neq == 0) continue;
         if (is_cut(s)) {
             for (int64_t i = 0; i < s.neq; ++i)
                 for (int64_t g = s.ig_off[i]; g < s.ig_off[i + 1]; ++g)
@@ -589,7 +590,7 @@ fem_gpu_status fem_gpu_update_ig_vertices(fem_gpu_ctx* c, const double* t) {
     fem_gpu_status r = interface_volumes(c);
     if (r != FEM_GPU_OK) return r;
     for (auto& s : c->sets)
-        if (is_interface(s) && e == cudaSuccess) e = refresh(s.d_vol, s.vol, st);
+        if (is_interface(s) && s.neq > 0 && e == cudaSuccess) e = refresh(s.d_vol, s.vol, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return sfail(c, e, "geometry update");
     return FEM_GPU_OK;
@@ -652,7 +653,7 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
     std::vector<std::pair<int32_t, int64_t>> cell_cluster(c->num_cells, {-1, -1});
     for (size_t k = 0; k < c->sets.size(); ++k) {
         SetData& s = c->sets[k];
-        if (!is_cut(s)) continue;
+        if (!is_cut(s) || s.neq == 0) continue;
         if (s.vid.empty()) return fail(c, FEM_GPU_BAD_ARG, "cut set without IG vertex ids");
         if (s.bulk.integration_rule != FEM_GPU_RULE_TET_4 && s.bulk.integration_rule != FEM_GPU_RULE_TET_11)
             return fail(c, FEM_GPU_UNSUPPORTED, "sensitivities of cut clusters need TET4 cells");
@@ -685,7 +686,7 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
     if ((e = upload(dcuts, cuts, st)) != cudaSuccess) return sfail(c, e, "cut table");
     fem_gpu_status r = FEM_GPU_OK;
     for (auto& s : c->sets) {
-        if (!is_interface(s)) continue;
+        if (!is_interface(s) || s.neq == 0) continue;
         if (s.vid.empty() || s.nfv != 3) {
             r = fail(c, FEM_GPU_UNSUPPORTED, "interface sensitivities need TRI3 facets with vertex ids");
             break;

@@ -28,7 +28,24 @@ def distort(mesh, dim, ne, amount, seed):
     return m
 
 
-def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed=1, distortion=0.2, density=False):
+def _add_empty_sets(prod, dim, rule, model):
+    """Sets with no equation objects around the populated ones (product only)."""
+    none_i, none_f = np.zeros(0, np.int32), np.zeros(0)
+    prod.add_bulk_set(none_i, none_f, 0.3, rule, model)
+    prod.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, none_i, none_i, none_f, 0.3,
+                      mg.RULE_BAR_3 if dim == 2 else mg.RULE_QUAD_2x2, model, value=(1.0,) + (0.0,) * (dim - 1))
+    if dim == 3:
+        prod.add_bulk_set(none_i, none_f, 0.3, mg.RULE_TET_4, model, ig_cell=mg.CELL_TET4,
+                          ig_offsets=np.zeros(1, np.int64), ig_coords=none_f, ig_param=none_f)
+        prod.add_double_side_set(mg.IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE, none_i, none_i,
+                                 np.zeros(1, np.int64), none_f, none_f, none_f, none_f, none_f, 0.3, mg.RULE_TRI_3,
+                                 mg.CELL_TRI3, 10.0)
+
+
+def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed=1, distortion=0.2, density=False,
+            empty_sets=False):
+    """Product and oracle models of one mesh.  empty_sets adds, to the product
+    only, sets without equation objects before and after the populated ones."""
     mesh = mg.hmr_uniform_mesh(dim, ne, [1.0] * dim, p)
     if shape == mg.SHAPE_GENERAL:
         mesh = distort(mesh, dim, ne, distortion, seed + 7)
@@ -41,6 +58,8 @@ def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed
     prod = mg.FemModel(dim, mesh, shape)
     orc = OracleModel(dim, ipc, shape, mesh)
     cells = np.arange(nc, dtype=np.int32)
+    if empty_sets:
+        _add_empty_sets(prod, dim, rule, model)
     if density:
         rho = 1e-3 + (1 - 1e-3) * uniform01(seed + 99, len(mesh["coords"]))
         prod.add_bulk_set(cells, E, 0.3, rule, model, node_density=rho, density_exponent=3.0)
@@ -68,6 +87,8 @@ def problem(dim, ne, p, shape=mg.SHAPE_RECTANGULAR, rule=None, sides=False, seed
                           value=trac)
         orc.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, srule, model, right, np.full(len(right), ro), E[right], 0.3, 0.0,
                          trac)
+    if empty_sets:
+        _add_empty_sets(prod, dim, rule, model)
     return prod, orc, mesh
 
 

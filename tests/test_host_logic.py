@@ -122,3 +122,57 @@ def test_bad_inputs_are_rejected():
     with pytest.raises(mg.FemGpuError) as ei:
         m.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, [0], [7], [1.0], 0.3, mg.RULE_BAR_3, mg.MODEL_PLANE_STRAIN)
     assert ei.value.status == 2
+
+
+def test_empty_sets_keep_indices_and_graph():
+    """Sets with no equation objects (a processor without facets on a side set,
+    a mesh with no cut cells) are accepted, keep the caller's set indices and
+    leave the adof numbering and the graph unchanged."""
+    ref, orcm, mesh = build_pair(2, (4, 3), 2)
+    ref.finalize(host_only=True)
+    orcm.finalize()
+    prod = mg.FemModel(2, mesh)
+    nc = len(mesh["cells"])
+    rng = np.random.default_rng(0)
+    E = 10.0 ** rng.uniform(-3, 0, nc)
+    empty_i, empty_f = np.zeros(0, np.int32), np.zeros(0)
+    assert prod.add_bulk_set(empty_i, empty_f, 0.3, mg.RULE_QUAD_2x2, mg.MODEL_PLANE_STRAIN) == 0
+    assert prod.add_bulk_set(np.arange(nc, dtype=np.int32), E, 0.3, mg.RULE_QUAD_2x2, mg.MODEL_PLANE_STRAIN) == 1
+    assert prod.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, empty_i, empty_i, empty_f, 0.3, mg.RULE_BAR_3,
+                             mg.MODEL_PLANE_STRAIN, value=(1.0, 0.0)) == 2
+    prod.finalize(host_only=True)
+    assert prod.num_eq(0) == 0 and prod.num_eq(2) == 0
+    assert prod.num_eq(1) == nc
+    rp_a, ci_a = prod.graph()
+    # the graph depends only on the cells in use: the full-mesh pair's graph
+    rp_b, ci_b = orcm.graph()
+    assert np.array_equal(rp_a, rp_b) and np.array_equal(ci_a, ci_b)
+    for eq in range(nc):
+        assert np.array_equal(prod.element_topology(1, eq), orcm.element_topology(0, eq))
+    with pytest.raises(mg.FemGpuError) as ei:
+        prod.element_topology(0, 0)
+    assert ei.value.status == 2
+
+
+def test_empty_cut_and_interface_sets_accepted():
+    mesh = mg.hmr_uniform_mesh(3, (2, 2, 2), (1.0,) * 3, 1)
+    nc = len(mesh["cells"])
+    m = mg.FemModel(3, mesh)
+    m.add_bulk_set(np.arange(nc, dtype=np.int32), np.ones(nc), 0.3, mg.RULE_HEX_2x2x2, mg.MODEL_3D)
+    # a cut set and an interface set of a mesh the geometry does not cut
+    m.add_bulk_set(np.zeros(0, np.int32), np.zeros(0), 0.3, mg.RULE_TET_4, mg.MODEL_3D, ig_cell=mg.CELL_TET4,
+                   ig_offsets=np.zeros(1, np.int64), ig_coords=np.zeros(0), ig_param=np.zeros(0))
+    m.add_double_side_set(mg.IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE, np.zeros(0, np.int32),
+                          np.zeros(0, np.int32), np.zeros(1, np.int64), np.zeros(0), np.zeros(0), np.zeros(0),
+                          np.zeros(0), np.zeros(0), 0.3, mg.RULE_TRI_3, mg.CELL_TRI3, 10.0)
+    m.finalize(host_only=True)
+    assert [m.num_eq(s) for s in range(3)] == [nc, 0, 0]
+
+
+def test_model_without_equation_objects_is_rejected():
+    mesh = mg.hmr_uniform_mesh(2, (2, 2), (1.0, 1.0), 1)
+    m = mg.FemModel(2, mesh)
+    m.add_bulk_set(np.zeros(0, np.int32), np.zeros(0), 0.3, mg.RULE_QUAD_2x2, mg.MODEL_PLANE_STRAIN)
+    with pytest.raises(mg.FemGpuError) as ei:
+        m.finalize(host_only=True)
+    assert ei.value.status == 1

@@ -232,6 +232,38 @@ def test_nonfinite_input_is_reported(torch):
     assert ei.value.status == 3
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_empty_sets_do_no_work(torch, dim):
+    """Sets without equation objects before and after the populated ones: the
+    per-set, autotuned, element-level and (3D) batched paths give the oracle's
+    system of the populated sets."""
+    ne = (5, 4) if dim == 2 else (3, 3, 2)
+    rule = mg.RULE_QUAD_2x2 if dim == 2 else mg.RULE_HEX_2x2x2
+    prod, orc, _ = problem(dim, ne, 1, mg.SHAPE_RECTANGULAR, rule, True, empty_sets=True)
+    prod.finalize()
+    orc.finalize()
+    bulk = 2 if dim == 2 else 4  # index of the populated bulk set
+    assert all(prod.num_eq(k) == 0 for k in range(bulk)) and prod.num_eq(bulk) == orc.num_eq(0)
+    u = uniform01(5, prod.num_adofs)
+    rp, _ = prod.graph()
+    vo, ro = orc.assemble(u)
+    vh, rh = prod.assemble_host(u)
+    assert csr_row_rel_err(rp, vh, vo) <= RTOL and rel_err(rh, ro) <= RTOL
+    prod.autotune()
+    vh, rh = prod.assemble_host(u)
+    assert csr_row_rel_err(rp, vh, vo) <= RTOL and rel_err(rh, ro) <= RTOL
+    K, R = prod.element_matrices(0, 0, 0, u)
+    assert K.shape[0] == 0 and R.shape[0] == 0
+    if dim == 3:
+        ut = torch.tensor(u, dtype=torch.float64, device="cuda")
+        vals = torch.zeros(prod.nnz, dtype=torch.float64, device="cuda")
+        rhs = torch.zeros(prod.num_adofs, dtype=torch.float64, device="cuda")
+        prod.assemble_batched(ut, vals, rhs)
+        torch.cuda.synchronize()
+        prod.check_status()
+        assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL and rel_err(rhs.cpu().numpy(), ro) <= RTOL
+
+
 def test_host_buffer_assembly_overlaps_the_copy_back(torch):
     """Host-buffer assembly runs the element loop in chunks and copies every
     finished row range while the next chunk computes: with more than one chunk

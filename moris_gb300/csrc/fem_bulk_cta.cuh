@@ -21,9 +21,6 @@
 // way and scatters T^T (K T x) without the K T / T^T K T stages.
 #pragma once
 
-__device__ __forceinline__ bool fem_nonzero(double t) {
-    return (__double_as_longlong(t) << 1) != 0;  // bit test, keeps the FP64 pipe free
-}
 // E0-relative SIMP factor rho(x_q)^beta with rho interpolated from the nodal
 // densities by the IP-cell shape functions at Gauss point q
 __device__ __forceinline__ double fem_density_power(const BulkArgs& p, const double* rho_nodes, int q) {
@@ -32,9 +29,6 @@ __device__ __forceinline__ double fem_density_power(const BulkArgs& p, const dou
     const int npe = p.npe;
     for (int a = 0; a < npe && a < kMaxNodes; ++a) r = fma(__ldg(p.nq + q * npe + a), rho_nodes[a], r);
     return p.beta == 3.0 ? r * r * r : pow(r, p.beta);
-}
-__device__ __forceinline__ bool fem_finite(double t) {
-    return (__double_as_longlong(t) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
 }
 
 // (included inside namespace fem of fem_device.cu)
@@ -94,7 +88,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     uint8_t* TC = sb + L::bTC;
     uint8_t* CP = sb + L::bCP;  // columns of T ordered by nonzero count
     uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x;
     const uint32_t* pairs = p.pairs;
     const bool assemble = mode == MODE_ASSEMBLE, apply = mode == MODE_APPLY;
     const bool want_r = (assemble && p.rhs) || (mode == MODE_ELEMENT && p.Rout);
@@ -226,12 +220,15 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 2: pdof values and (general cells) the Gram matrix ------------
-        if (want_k && tid == NT - 1) {
-            // counting sort of the T columns by nonzero count
-            int pos = 0;
-            for (int c = 0; c <= NPE; ++c)
-                for (int j = 0; j < NB; ++j)
-                    if (TC[j] == c) CP[pos++] = (uint8_t)j;
+        // the T columns ordered by nonzero count (stable): CP[slot] = column
+        for (int j = tid; j < NB; j += NT) {
+            const int cj = j < nb ? TC[j] : 0;
+            int rank = 0;
+            for (int k = 0; k < NB; ++k) {
+                const int ck = k < nb ? TC[k] : 0;
+                rank += (ck < cj) || (ck == cj && k < j);
+            }
+            CP[rank] = (uint8_t)j;
         }
         if (need_u)
             for (int r = tid; r < NPD; r += NT) {
@@ -316,36 +313,30 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 RP[r] = s;
             }
         if (want_k) {
-            // K T for the field blocks (f, g >= f) that the upper triangle of
-            // T^T K T reads; a warp pass covers NPE rows x CPP columns of one
-            // block, columns taken in order of their nonzero count
-            constexpr int CPP = 32 / NPE;
-            constexpr int PASSES = (NB + CPP - 1) / CPP;
-            constexpr int NBLK = D * (D + 1) / 2;
-            const int a = lane % NPE, sub = lane / NPE;
-            for (int w = warp; w < NBLK * PASSES; w += NW) {
-                const int blk = w / PASSES, pass = w - blk * PASSES;
-                int f = 0, bb = blk;
-                while (bb >= D - f) {
-                    bb -= D - f;
-                    ++f;
-                }
-                const int gg = f + bb;
-                const int slot = pass * CPP + sub;
-                if (slot >= NB) continue;
+            // K T for all D x D field blocks, with the columns in count order:
+            // KT[(f,a)][q], q = slot * D + g for column (g, CP[slot]).  Items run
+            // a fastest, then f, g and slot, so the lanes of a warp share one
+            // column (one trip count) and read K along a (by symmetry,
+            // K[(f,a),(g,b)] = K[(g,b),(f,a)]: consecutive words).
+            constexpr int NITEM = NB * D * D * NPE;
+            for (int t = tid; t < NITEM; t += NT) {
+                const int a = t % NPE, rest = t / NPE;
+                const int f = rest % D, rest2 = rest / D;
+                const int gg = rest2 % D, slot = rest2 / D;
                 const int j = CP[slot];
                 const int cnt = j < nb ? TC[j] : 0;
-                const double* Krow = K + (f * NPE + a) * NPD + gg * NPE;
+                const double* Kc = K + f * NPE + a;
                 double s = 0.0;
-                for (int k = 0; k < cnt; ++k) s = fma(Krow[TN[j * NPE + k]], TW[j * NPE + k], s);
-                KT[(f * NPE + a) * NAD + gg * NB + j] = s;
+                for (int k = 0; k < cnt; ++k) s = fma(Kc[(gg * NPE + TN[j * NPE + k]) * NPD], TW[j * NPE + k], s);
+                KT[(f * NPE + a) * NAD + slot * D + gg] = s;
             }
         }
         __syncthreads();
         // ---- phase 5: residual scatter, T^T (K T) upper triangle and scatter --------
         if (need_u)
-            for (int r = tid; r < NAD; r += NT) {
-                const int f = r / NB, i = r - f * NB;
+            for (int pr = tid; pr < NAD; pr += NT) {
+                // rows in count order: the lanes of a warp share trip counts
+                const int slot = pr / D, f = pr - slot * D, i = CP[slot], r = f * NB + i;
                 double s = 0.0;
                 if (i < nb)
                     for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
@@ -358,30 +349,37 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 }
             }
         if (want_k) {
+            // T^T K T over the upper triangle of the count-ordered adofs
+            // (row pr = slot * D + f is adof (f, CP[slot])): with pr <= qc the
+            // row has the sparser T column, so each entry costs the smaller of
+            // the two nonzero counts, and entries of one count are contiguous in
+            // the linear triangle index, so warps run uniform trip counts
             bool bad = false;
-            // rows r and NAD-1-r share one pass: NAD+1 entries of the upper triangle
-            constexpr int NPAIR = (NAD + 1) / 2;
-            for (int pr = warp; pr < NPAIR; pr += NW) {
-                const int r1 = pr, r2 = NAD - 1 - pr;
-                const int n1 = NAD - r1, n2 = (r2 > r1) ? NAD - r2 : 0;
-                for (int t = lane; t < n1 + n2; t += 32) {
-                    const int r = t < n1 ? r1 : r2;
-                    const int c = t < n1 ? r1 + t : r2 + (t - n1);
-                    const int f = r / NB, i = r - f * NB, gg = c / NB, j = c - gg * NB;
-                    if (i >= nb || j >= nb) continue;
-                    const int cnt = TC[i];
-                    double v = 0.0;
-                    for (int k = 0; k < cnt; ++k)
-                        v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + c], v);
-                    bad |= !fem_finite(v);
-                    if (assemble) {
-                        atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
-                        if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
-                    } else {
-                        double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
-                        Ko[r + (int64_t)c * p.nmax] = v;
-                        Ko[c + (int64_t)r * p.nmax] = v;
-                    }
+            constexpr int NTRI = NAD * (NAD + 1) / 2;
+            constexpr int TW1 = 2 * NAD + 1;
+            for (int t = tid; t < NTRI; t += NT) {
+                // row of entry t: off(pr) = pr * NAD - pr (pr - 1) / 2 <= t < off(pr + 1)
+                int pr = (int)((TW1 - sqrtf((float)(TW1 * TW1 - 8 * t))) * 0.5f);
+                pr = pr < 0 ? 0 : (pr > NAD - 1 ? NAD - 1 : pr);
+                while (pr > 0 && pr * NAD - pr * (pr - 1) / 2 > t) --pr;
+                while (pr + 1 < NAD && (pr + 1) * NAD - (pr + 1) * pr / 2 <= t) ++pr;
+                const int qc = pr + (t - (pr * NAD - pr * (pr - 1) / 2));
+                const int sr = pr / D, f = pr - sr * D, sc = qc / D, gg = qc - sc * D;
+                const int i = CP[sr], j = CP[sc];
+                if (i >= nb || j >= nb) continue;
+                const int r = f * NB + i, c = gg * NB + j;
+                const int cnt = TC[i];
+                double v = 0.0;
+                for (int k = 0; k < cnt; ++k)
+                    v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + qc], v);
+                bad |= !fem_finite(v);
+                if (assemble) {
+                    atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
+                    if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
+                } else {
+                    double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
+                    Ko[r + (int64_t)c * p.nmax] = v;
+                    Ko[c + (int64_t)r * p.nmax] = v;
                 }
             }
             if (bad) atomicOr(p.status, 1);

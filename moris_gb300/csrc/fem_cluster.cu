@@ -31,6 +31,7 @@
 #include <cstring>
 #include <vector>
 
+#include "fem_bits.cuh"
 #include "fem_internal.hpp"
 #include "fem_shape.hpp"
 
@@ -254,7 +255,7 @@ __device__ void bulk_item(const ClusterArgs& p, const SetDev& S, const Item& it,
         int cnt = 0;
         for (int a = 0; a < 8; ++a) {
             const double t = T[a * NB + j];
-            if (t != 0.0) {
+            if (fem_nonzero(t)) {
                 TN[j * 8 + cnt] = (uint8_t)a;
                 TW[j * 8 + cnt] = t;
                 ++cnt;
@@ -333,7 +334,7 @@ __device__ void bulk_item(const ClusterArgs& p, const SetDev& S, const Item& it,
         double s = 0.0;
         for (int j = 0; j < nb; ++j) {
             const double t = T[a * NB + j];
-            if (t != 0.0) s = fma(t, UA[f * NB + j], s);
+            if (fem_nonzero(t)) s = fma(t, UA[f * NB + j], s);
         }
         U[r] = s;
     }
@@ -399,7 +400,7 @@ __device__ void bulk_item(const ClusterArgs& p, const SetDev& S, const Item& it,
         if (i >= nb || j >= nb) continue;
         double v = 0.0;
         for (int kk = 0; kk < TC[i]; ++kk) v = fma(TW[i * 8 + kk], KT[(f * 8 + TN[i * 8 + kk]) * NAD + c], v);
-        bad |= !isfinite(v);
+        bad |= !fem_finite(v);
         if (assemble) {
             atomicAdd(p.vals + RB[r] + gg * UL[i] + SL[i * NB + j], v);
             if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + SL[j * NB + i], v);
@@ -504,7 +505,7 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
         int cnt = 0;
         for (int a = 0; a < 8; ++a) {
             const double t = T[(s * 8 + a) * NB + j];
-            if (t != 0.0) {
+            if (fem_nonzero(t)) {
                 TN[jj * 8 + cnt] = (uint8_t)a;
                 TW[jj * 8 + cnt] = t;
                 ++cnt;
@@ -654,7 +655,7 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
         double v = 0.0;
         for (int j = 0; j < nbs[s]; ++j) {
             const double t = T[(s * 8 + a) * NB + j];
-            if (t != 0.0) v = fma(t, UA[(s * 3 + fr) * NB + j], v);
+            if (fem_nonzero(t)) v = fma(t, UA[(s * 3 + fr) * NB + j], v);
         }
         U[r] = v;
     }
@@ -699,7 +700,7 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
         double v = 0.0;
         for (int k = 0; k < TC[coli]; ++k)
             v = fma(TW[coli * 8 + k], KT[(sr * 24 + fr * 8 + TN[coli * 8 + k]) * NAD + c], v);
-        bad |= !isfinite(v);
+        bad |= !fem_finite(v);
         if (assemble) atomicAdd(p.vals + RB[r] + gc * UL[coli] + SL[coli * 2 * NB + colj], v);
         else atomicAdd(p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax + r + (int64_t)c * p.nmax, v);
     }
@@ -760,7 +761,7 @@ __device__ void uncut_warp(const ClusterArgs& p, const SetDev& S, int64_t e, uns
         int cnt = 0;
         for (int a = 0; a < 8; ++a) {
             const double t = T[a * NB + lane];
-            if (t != 0.0) {
+            if (fem_nonzero(t)) {
                 TN[lane * 8 + cnt] = (uint8_t)a;
                 TW[lane * 8 + cnt] = t;
                 ++cnt;
@@ -796,7 +797,7 @@ __device__ void uncut_warp(const ClusterArgs& p, const SetDev& S, int64_t e, uns
         double v = 0.0;
         for (int j = 0; j < nb; ++j) {
             const double t = T[a * NB + j];
-            if (t != 0.0) v = fma(t, UA[f * NB + j], v);
+            if (fem_nonzero(t)) v = fma(t, UA[f * NB + j], v);
         }
         U[lane] = v;
     }
@@ -844,7 +845,7 @@ __device__ void uncut_warp(const ClusterArgs& p, const SetDev& S, int64_t e, uns
         if (i >= nb || j >= nb) continue;
         double v = 0.0;
         for (int kk = 0; kk < TC[i]; ++kk) v = fma(TW[i * 8 + kk], KT[(f * 8 + TN[i * 8 + kk]) * NAD + c], v);
-        bad |= !isfinite(v);
+        bad |= !fem_finite(v);
         if (assemble) {
             atomicAdd(p.vals + RB[r] + gg * UL[i] + SL[i * NB + j], v);
             if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + SL[j * NB + i], v);

@@ -27,6 +27,7 @@
 #include <cstring>
 #include <vector>
 
+#include "fem_bits.cuh"
 #include "fem_internal.hpp"
 #include "fem_shape.hpp"
 
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
             int cnt = 0;
             for (int a = 0; a < NPE; ++a) {
                 const double t = T[a * NB + j];
-                if (t != 0.0) {
+                if (fem_nonzero(t)) {
                     TN[j * NPE + cnt] = (uint8_t)a;
                     TW[j * NPE + cnt] = t;
                     ++cnt;
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
             double s = 0.0;
             for (int j = 0; j < nb; ++j) {
                 const double t = T[a * NB + j];
-                if (t != 0.0) s = fma(t, UA[f * NB + j], s);
+                if (fem_nonzero(t)) s = fma(t, UA[f * NB + j], s);
             }
             U[r] = s;
         }
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
                 if (j >= nb) continue;
                 double v = 0.0;
                 for (int k = 0; k < cnt; ++k) v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + c], v);
-                bad |= !isfinite(v);
+                bad |= !fem_finite(v);
                 if (mode == MODE_ASSEMBLE) {
                     atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
                     if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
@@ -497,7 +498,7 @@ __global__ void side_kernel(SideArgs p) {
             if (p.u)
                 for (int j = 0; j < nb; ++j) {
                     const double t = p.T[(s * NPE + a) * p.maxnb + j];
-                    if (t != 0.0) v = fma(t, p.u[f * p.nu + p.bases[s * p.maxnb + j]], v);
+                    if (fem_nonzero(t)) v = fma(t, p.u[f * p.nu + p.bases[s * p.maxnb + j]], v);
                 }
             U[f * NPE + a] = v;
         }
@@ -649,7 +650,7 @@ __global__ void side_kernel(SideArgs p) {
                         for (int b = 0; b < NPE; ++b) kt = fma(K[(f * NPE + a) * NPD + gg * NPE + b], Ts[b * maxnb + j], kt);
                         v = fma(ta, kt, v);
                     }
-                    bad |= !isfinite(v);
+                    bad |= !fem_finite(v);
                     if (p.mode == MODE_ASSEMBLE)
                         atomicAdd(p.vals + rbase + gg * ul + p.sidx[(s * maxnb + i) * maxnb + j], v);
                     else
@@ -1086,9 +1087,14 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
             if ((e = upload(ds.d_gp, r.pts, sm)) != cudaSuccess) return cuda_fail(c, e, "rule points");
             if ((e = upload(ds.d_gw, r.w, sm)) != cudaSuccess) return cuda_fail(c, e, "rule weights");
             const int npd = D * NPE;
+            // upper-triangle pdof pairs, those of the diagonal field blocks (which
+            // carry the trace term) first, so that warps of the stiffness phase
+            // run one branch
             std::vector<uint32_t> pairs;
-            for (int rr = 0; rr < npd; ++rr)
-                for (int cc = rr; cc < npd; ++cc) pairs.push_back((uint32_t)rr << 16 | (uint32_t)cc);
+            for (int diag = 1; diag >= 0; --diag)
+                for (int rr = 0; rr < npd; ++rr)
+                    for (int cc = rr; cc < npd; ++cc)
+                        if ((rr / NPE == cc / NPE) == (diag == 1)) pairs.push_back((uint32_t)rr << 16 | (uint32_t)cc);
             if ((e = upload(ds.d_pairs, pairs, sm)) != cudaSuccess) return cuda_fail(c, e, "pair table");
             // reference Gram table of the rule (constant-Jacobian cells)
             std::vector<double> g0((size_t)npd * npd, 0.0);

@@ -33,11 +33,39 @@ __device__ __forceinline__ double fem_density_power(const BulkArgs& p, const dou
 
 // (included inside namespace fem of fem_device.cu)
 
+// sum_k w[k] * base[tn[k] * stride] over the nonzeros of one T column; the
+// counts of tensor-product B-spline extraction (1, 2, 4, 8) get fully unrolled
+// bodies, so a warp of one count issues no predicated-off FMAs and all loads
+// of the column up front
+template <int N>
+__device__ __forceinline__ double fem_tdot_n(const double* w, const uint8_t* tn, const double* base, int stride) {
+    double v = 0.0;
+#pragma unroll
+    for (int k = 0; k < N; ++k) v = fma(w[k], base[tn[k] * stride], v);
+    return v;
+}
+__device__ __forceinline__ double fem_tdot(int cnt, const double* w, const uint8_t* tn, const double* base,
+                                           int stride) {
+    switch (cnt) {
+        case 1: return fem_tdot_n<1>(w, tn, base, stride);
+        case 2: return fem_tdot_n<2>(w, tn, base, stride);
+        case 4: return fem_tdot_n<4>(w, tn, base, stride);
+        case 8: return fem_tdot_n<8>(w, tn, base, stride);
+        default: {
+            double v = 0.0;
+            for (int k = 0; k < cnt; ++k) v = fma(w[k], base[tn[k] * stride], v);
+            return v;
+        }
+    }
+}
+
 template <int D, int NPE, int NGP, int NB>
 struct CtaLayout {
     static constexpr int NPD = D * NPE;
     static constexpr int NAD = D * NB;
     static constexpr int NSYM = NPD * (NPD + 1) / 2;
+    static constexpr int NTRI = NAD * (NAD + 1) / 2;       // upper triangle of the element matrix
+    static constexpr int NKT = NB * D * D * NPE;           // K T entries (all field blocks)
     static constexpr int GPR = 2 * NGP * NPD;                      // g and w*g
     static constexpr int R1 = (GPR + NPE * NB > NPD * NAD) ? GPR + NPE * NB : NPD * NAD;
     static constexpr int oX = 0;
@@ -45,7 +73,7 @@ struct CtaLayout {
     static constexpr int oT = oR1 + GPR;                           // inside R1
     static constexpr int oA = oR1 + R1;
     static constexpr int oK = oA + NPD * NPD;
-    static constexpr int oTW = oK + NPD * NPD;
+    static constexpr int oTW = oK + NPD * NPD;                     // [slot][k] T weights in count order
     static constexpr int oU = oTW + NB * NPE;
     static constexpr int oUA = oU + NPD;
     static constexpr int oRP = oUA + NAD;
@@ -53,11 +81,27 @@ struct CtaLayout {
     static constexpr int oCJ = oW + NGP;                           // RECT: detJ/(J_ii J_jj), i<=j
     static constexpr int oRHO = oCJ + 8;                           // nodal densities (SIMP sets)
     static constexpr int ND = oRHO + NPE;
-    static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + NAD, NI = iUL + NB;
-    static constexpr int bTN = 0, bTC = bTN + NB * NPE, bCP = bTC + NB, bS = ((bCP + NB + 1) / 2) * 2;
+    // ints: bases, CSR row starts [f][basis], row lengths, and the CSR row
+    // base of count-ordered adof x for column field g
+    static constexpr int iB = 0, iRB = iB + NB, iUL = iRB + NAD, iRG = iUL + NB, NI = iRG + NAD * D;
+    // bytes: T row lists [slot][k], nonzero counts by basis / by slot, the
+    // count order and its inverse, then the count-ordered scatter slots
+    // [slot][slot] (u16)
+    static constexpr int bTN = 0, bTC = bTN + NB * NPE, bTCP = bTC + NB, bCP = bTCP + NB, bCPI = bCP + NB;
+    static constexpr int bS = ((bCPI + NB + 1) / 2) * 2;
     static constexpr int NBYTE = bS + 2 * NB * NB;
     static constexpr size_t kBytes = ((size_t)ND * 8 + (size_t)NI * 4 + (size_t)NBYTE + 15) / 16 * 16;
+    static_assert(NB <= 32 && D <= 3, "table packing: 5-bit slots, 2-bit fields");
+    static_assert((D - 1) * NPE * NPD + D * NPE <= 1024 && NPD * NAD <= 8192, "K T table packing");
 };
+
+// Item tables of the K T and T^T K T phases (built on the host per basis width,
+// fem_bulk_tables): they replace per-entry index arithmetic by one load.
+//   ktab[t]: slot | kbase << 6 | ktdst << 16, items slot-major so that the
+//            lanes of a warp share one column (one trip count)
+//            kbase = g*NPE*NPD + f*NPE + a, ktdst = (f*NPE + a)*NAD + slot*D + g
+//   tri[t]:  sr | f << 5 | sc << 7 | g << 12 for the upper-triangle entry t
+//            (row x = sr*D + f, column y = sc*D + g, x <= y) in row order
 
 template <int D, int NPE, int NGP, int NB, bool RECT, int NW>
 __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode) {
@@ -84,9 +128,12 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     int32_t* B = si + L::iB;
     int32_t* RB = si + L::iRB;
     int32_t* UL = si + L::iUL;
+    int32_t* RG = si + L::iRG;
     uint8_t* TN = sb + L::bTN;
     uint8_t* TC = sb + L::bTC;
-    uint8_t* CP = sb + L::bCP;  // columns of T ordered by nonzero count
+    uint8_t* TCP = sb + L::bTCP;
+    uint8_t* CP = sb + L::bCP;
+    uint8_t* CPI = sb + L::bCPI;
     uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
     const int tid = threadIdx.x;
     const uint32_t* pairs = p.pairs;
@@ -95,6 +142,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     const bool want_k = (assemble && p.vals) || (mode == MODE_ELEMENT && p.Kout);
     const bool need_u = want_r || apply;
     const double* uin = apply ? p.x : p.u;
+    const bool scatter_k = assemble && p.vals;
+    constexpr int NSR = (NB * NB + NT - 1) / NT;  // scatter slots held per thread
 
     for (int64_t e = blockIdx.x; e < p.ne; e += gridDim.x) {
         const int nb = p.nb[e];
@@ -105,26 +154,30 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         for (int i = tid; i < NB; i += NT) B[i] = p.bases[e * NB + i];
         if (p.rho)
             for (int i = tid; i < NPE; i += NT) RHO[i] = p.rho[e * NPE + i];
-        if (assemble && p.vals)
-            for (int i = tid; i < NB * NB; i += NT) S[i] = p.sidx[e * (NB * NB) + i];
+        // scatter slots [basis][basis] into registers now; they are stored in
+        // count order once the order is known
+        uint16_t sreg[NSR];
+        if (scatter_k) {
+            const uint16_t* sg = p.sidx + e * (NB * NB);
+#pragma unroll
+            for (int m = 0; m < NSR; ++m) {
+                const int k = tid + m * NT;
+                sreg[m] = k < NB * NB ? sg[k] : 0;
+            }
+        }
         __syncthreads();
-        // ---- phase 1: index data, column lists, Gauss-point geometry -----------
+        // ---- phase 1: adof values, T column counts, Gauss-point geometry ---------
         for (int r = tid; r < NAD; r += NT) {
             const int f = r / NB, i = r - f * NB;
             UA[r] = (uin && i < nb) ? uin[f * p.nu + B[i]] : 0.0;
-            if (assemble) RB[r] = i < nb ? p.rowptr[f * p.nu + B[i]] : 0;
+            if (scatter_k) RB[r] = i < nb ? __ldg(p.rowptr + f * p.nu + B[i]) : 0;
         }
+        if (scatter_k)
+            for (int i = tid; i < NB; i += NT) UL[i] = i < nb ? __ldg(p.ulen + B[i]) : 0;
         for (int i = tid; i < NB; i += NT) {
-            if (assemble) UL[i] = i < nb ? p.ulen[B[i]] : 0;
             int cnt = 0;
-            for (int a = 0; a < NPE; ++a) {
-                const double t = T[a * NB + i];
-                if (fem_nonzero(t)) {
-                    TN[i * NPE + cnt] = (uint8_t)a;
-                    TW[i * NPE + cnt] = t;
-                    ++cnt;
-                }
-            }
+            if (i < nb)
+                for (int a = 0; a < NPE; ++a) cnt += fem_nonzero(T[a * NB + i]);
             TC[i] = (uint8_t)cnt;
         }
         if (RECT) {
@@ -219,16 +272,17 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 }
         }
         __syncthreads();
-        // ---- phase 2: pdof values and (general cells) the Gram matrix ------------
-        // the T columns ordered by nonzero count (stable): CP[slot] = column
+        // ---- phase 2: count order, pdof values, (general cells) Gram matrix ----
+        // CP[slot] = basis, stable in basis order; padding bases (count 0) first
         for (int j = tid; j < NB; j += NT) {
-            const int cj = j < nb ? TC[j] : 0;
+            const int cj = TC[j];
             int rank = 0;
             for (int k = 0; k < NB; ++k) {
-                const int ck = k < nb ? TC[k] : 0;
+                const int ck = TC[k];
                 rank += (ck < cj) || (ck == cj && k < j);
             }
             CP[rank] = (uint8_t)j;
+            CPI[j] = (uint8_t)rank;
         }
         if (need_u)
             for (int r = tid; r < NPD; r += NT) {
@@ -250,7 +304,6 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 A[r * NPD + c] = s;
                 A[c * NPD + r] = s;
             }
-            __syncthreads();
         }
         if (!RECT) {
             for (int k = tid; k < NSYM; k += NT) {
@@ -268,9 +321,9 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 A[r * NPD + c] = s;
                 A[c * NPD + r] = s;
             }
-            __syncthreads();
         }
-        // ---- phase 3: isotropic stiffness in pdof space ---------------------------
+        __syncthreads();
+        // ---- phase 3: isotropic stiffness in pdof space, count-ordered data -------
         {
             // with a density field E(x_q) is already inside the Gram sums
             const double escale = p.rho ? 1.0 : E;
@@ -304,6 +357,36 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 K[c * NPD + r] = v;
             }
         }
+        // count-ordered element data: T lists by slot, CSR row bases and the
+        // scatter slots of the count-ordered adofs
+        for (int sl = tid; sl < NB; sl += NT) {
+            const int j = CP[sl];
+            int cnt = 0;
+            for (int a = 0; a < NPE; ++a) {
+                const double t = T[a * NB + j];
+                if (fem_nonzero(t)) {
+                    TN[sl * NPE + cnt] = (uint8_t)a;
+                    TW[sl * NPE + cnt] = t;
+                    ++cnt;
+                }
+            }
+            TCP[sl] = (uint8_t)cnt;
+        }
+        if (scatter_k) {
+            for (int x = tid; x < NAD; x += NT) {
+                const int sl = x / D, f = x - sl * D, i = CP[sl];
+                const int32_t rb = RB[f * NB + i], ul = UL[i];
+                for (int gg = 0; gg < D; ++gg) RG[x * D + gg] = rb + gg * ul;
+            }
+#pragma unroll
+            for (int m = 0; m < NSR; ++m) {
+                const int k = tid + m * NT;
+                if (k < NB * NB) {
+                    const int i = k / NB, j = k - i * NB;
+                    S[CPI[i] * NB + CPI[j]] = sreg[m];
+                }
+            }
+        }
         __syncthreads();
         // ---- phase 4: pdof residual and K T ----------------------------------------
         if (need_u)
@@ -313,33 +396,23 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 RP[r] = s;
             }
         if (want_k) {
-            // K T for all D x D field blocks, with the columns in count order:
-            // KT[(f,a)][q], q = slot * D + g for column (g, CP[slot]).  Items run
-            // a fastest, then f, g and slot, so the lanes of a warp share one
-            // column (one trip count) and read K along a (by symmetry,
-            // K[(f,a),(g,b)] = K[(g,b),(f,a)]: consecutive words).
-            constexpr int NITEM = NB * D * D * NPE;
-            for (int t = tid; t < NITEM; t += NT) {
-                const int a = t % NPE, rest = t / NPE;
-                const int f = rest % D, rest2 = rest / D;
-                const int gg = rest2 % D, slot = rest2 / D;
-                const int j = CP[slot];
-                const int cnt = j < nb ? TC[j] : 0;
-                const double* Kc = K + f * NPE + a;
-                double s = 0.0;
-                for (int k = 0; k < cnt; ++k) s = fma(Kc[(gg * NPE + TN[j * NPE + k]) * NPD], TW[j * NPE + k], s);
-                KT[(f * NPE + a) * NAD + slot * D + gg] = s;
+            // KT[(f,a)][x], x = slot * D + g: K symmetric, K[(f,a),(g,b)] is read
+            // as K[(g,b),(f,a)], consecutive words along a
+            uint32_t nxt = tid < L::NKT ? __ldg(p.ktab + tid) : 0u;
+            for (int t = tid; t < L::NKT; t += NT) {
+                const uint32_t it = nxt;  // next item loaded one iteration ahead
+                if (t + NT < L::NKT) nxt = __ldg(p.ktab + t + NT);
+                const int sl = it & 63, kb = (it >> 6) & 1023, dst = it >> 16;
+                KT[dst] = fem_tdot(TCP[sl], TW + sl * NPE, TN + sl * NPE, K + kb, NPD);
             }
         }
         __syncthreads();
         // ---- phase 5: residual scatter, T^T (K T) upper triangle and scatter --------
         if (need_u)
-            for (int pr = tid; pr < NAD; pr += NT) {
-                // rows in count order: the lanes of a warp share trip counts
-                const int slot = pr / D, f = pr - slot * D, i = CP[slot], r = f * NB + i;
-                double s = 0.0;
-                if (i < nb)
-                    for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
+            for (int x = tid; x < NAD; x += NT) {
+                // count order: the lanes of a warp share trip counts
+                const int sl = x / D, f = x - sl * D, i = CP[sl], r = f * NB + i;
+                const double s = fem_tdot(TCP[sl], TW + sl * NPE, TN + sl * NPE, RP + f * NPE, 1);
                 if (assemble) {
                     if (i < nb) atomicAdd(p.rhs + f * p.nu + B[i], s);
                 } else if (apply) {
@@ -349,34 +422,25 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 }
             }
         if (want_k) {
-            // T^T K T over the upper triangle of the count-ordered adofs
-            // (row pr = slot * D + f is adof (f, CP[slot])): with pr <= qc the
-            // row has the sparser T column, so each entry costs the smaller of
-            // the two nonzero counts, and entries of one count are contiguous in
-            // the linear triangle index, so warps run uniform trip counts
+            // entry (x, y), x <= y, of the count-ordered adofs: the row has the
+            // sparser T column, so the entry costs the smaller nonzero count, and
+            // entries of one count are contiguous in t (uniform warp trip counts)
             bool bad = false;
-            constexpr int NTRI = NAD * (NAD + 1) / 2;
-            constexpr int TW1 = 2 * NAD + 1;
-            for (int t = tid; t < NTRI; t += NT) {
-                // row of entry t: off(pr) = pr * NAD - pr (pr - 1) / 2 <= t < off(pr + 1)
-                int pr = (int)((TW1 - sqrtf((float)(TW1 * TW1 - 8 * t))) * 0.5f);
-                pr = pr < 0 ? 0 : (pr > NAD - 1 ? NAD - 1 : pr);
-                while (pr > 0 && pr * NAD - pr * (pr - 1) / 2 > t) --pr;
-                while (pr + 1 < NAD && (pr + 1) * NAD - (pr + 1) * pr / 2 <= t) ++pr;
-                const int qc = pr + (t - (pr * NAD - pr * (pr - 1) / 2));
-                const int sr = pr / D, f = pr - sr * D, sc = qc / D, gg = qc - sc * D;
-                const int i = CP[sr], j = CP[sc];
-                if (i >= nb || j >= nb) continue;
-                const int r = f * NB + i, c = gg * NB + j;
-                const int cnt = TC[i];
-                double v = 0.0;
-                for (int k = 0; k < cnt; ++k)
-                    v = fma(TW[i * NPE + k], KT[(f * NPE + TN[i * NPE + k]) * NAD + qc], v);
+            uint32_t nxt = tid < L::NTRI ? __ldg(p.tri + tid) : 0u;
+            for (int t = tid; t < L::NTRI; t += NT) {
+                const uint32_t it = nxt;  // next item loaded one iteration ahead
+                if (t + NT < L::NTRI) nxt = __ldg(p.tri + t + NT);
+                const int sr = it & 31, f = (it >> 5) & 3, sc = (it >> 7) & 31, gg = it >> 12;
+                const int cnt = TCP[sr];
+                if (cnt == 0) continue;  // padding (or all-zero) column: nothing to add
+                const int x = sr * D + f, y = sc * D + gg;
+                const double v = fem_tdot(cnt, TW + sr * NPE, TN + sr * NPE, KT + f * NPE * NAD + y, NAD);
                 bad |= !fem_finite(v);
                 if (assemble) {
-                    atomicAdd(p.vals + RB[r] + gg * UL[i] + S[i * NB + j], v);
-                    if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
+                    atomicAdd(p.vals + RG[x * D + gg] + S[sr * NB + sc], v);
+                    if (x != y) atomicAdd(p.vals + RG[y * D + f] + S[sc * NB + sr], v);
                 } else {
+                    const int r = f * NB + CP[sr], c = gg * NB + CP[sc];
                     double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
                     Ko[r + (int64_t)c * p.nmax] = v;
                     Ko[c + (int64_t)r * p.nmax] = v;
@@ -387,4 +451,3 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         __syncthreads();
     }
 }
-

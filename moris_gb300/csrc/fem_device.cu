@@ -80,6 +80,8 @@ struct BulkArgs {
     const double* dn;     // [NGP][D][NPE]
     const double* w;      // [NGP]
     const uint32_t* pairs;// upper-triangle (r << 16 | c) pairs of the pdof Gram matrix
+    const uint32_t* ktab; // K T items of bulk_cta_kernel (fem_bulk_cta.cuh)
+    const uint16_t* tri;  // T^T K T upper-triangle items of bulk_cta_kernel
     const double* g0;     // [NPD][NPD] reference Gram table sum_q w_q dN dN (rectangular cells)
     const double* rho;    // [ne][NPE] nodal densities (nullable: constant E per element)
     const double* nq;     // [NGP][NPE] N of the IP cell at the Gauss points
@@ -853,6 +855,8 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.dn = (const double*)s.d_dn.p;
     a.w = (const double*)s.d_w.p;
     a.pairs = (const uint32_t*)s.d_pairs.p;
+    a.ktab = (const uint32_t*)s.d_ktab.p;
+    a.tri = (const uint16_t*)s.d_tri.p;
     a.g0 = (const double*)s.d_g0.p;
     a.rho = s.rhoe.empty() ? nullptr : (const double*)s.d_rho.p + first * NPE;
     a.nq = (const double*)s.d_nq.p;
@@ -1032,6 +1036,8 @@ void device_release(fem_gpu_ctx* c) {
         dfree(s.d_dn);
         dfree(s.d_w);
         dfree(s.d_pairs);
+        dfree(s.d_ktab);
+        dfree(s.d_tri);
         dfree(s.d_g0);
         dfree(s.d_rho);
         dfree(s.d_nq);
@@ -1112,6 +1118,25 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
                 return fail(c, FEM_GPU_UNSUPPORTED, "no bulk kernel instance for this element");
             ds.nbsel = nbsel ? nbsel : s.maxnb;
             ds.variant = VAR_CTA4;
+            if (nbsel) {
+                // item tables of bulk_cta_kernel, in the packing its loads decode
+                const int NB = nbsel, NAD = D * NB;
+                std::vector<uint32_t> kt;
+                for (int sl = 0; sl < NB; ++sl)
+                    for (int gg = 0; gg < D; ++gg)
+                        for (int f = 0; f < D; ++f)
+                            for (int a = 0; a < NPE; ++a) {
+                                const uint32_t kb = (uint32_t)(gg * NPE * npd + f * NPE + a);
+                                const uint32_t dst = (uint32_t)((f * NPE + a) * NAD + sl * D + gg);
+                                kt.push_back((uint32_t)sl | kb << 6 | dst << 16);
+                            }
+                std::vector<uint16_t> tri;
+                for (int x = 0; x < NAD; ++x)
+                    for (int y = x; y < NAD; ++y)
+                        tri.push_back((uint16_t)((x / D) | (x % D) << 5 | (y / D) << 7 | (y % D) << 12));
+                if ((e = upload(ds.d_ktab, kt, sm)) != cudaSuccess) return cuda_fail(c, e, "K T table");
+                if ((e = upload(ds.d_tri, tri, sm)) != cudaSuccess) return cuda_fail(c, e, "triangle table");
+            }
         } else {
             const Rule r = gauss_rule(s.side.integration_rule);
             ds.ngp = r.n;

@@ -69,6 +69,8 @@ struct SetData {
     DeviceBuf d_nb, d_bases, d_T, d_sidx, d_xe, d_E, d_ord;
     DeviceBuf d_dn, d_w;    // bulk: dN/dxi of the IP cell at the Gauss points, weights
     DeviceBuf d_pairs;      // bulk: upper-triangle index pairs of the pdof Gram matrix
+    DeviceBuf d_ktab;       // bulk: K T item table of the CTA kernels
+    DeviceBuf d_tri;        // bulk: T^T K T upper-triangle item table of the CTA kernels
     DeviceBuf d_g0;         // bulk: reference Gram table sum_q w_q dN/dxi dN/dxi
     DeviceBuf d_gp, d_gw;   // side: facet Gauss points and weights
     DeviceBuf d_igoff, d_igx, d_igxi;            // cut clusters: integration cells

@@ -59,20 +59,24 @@ __device__ __forceinline__ double fem_tdot(int cnt, const double* w, const uint8
     }
 }
 
-template <int D, int NPE, int NGP, int NB>
+template <int D, int NPE, int NGP, int NB, bool RECT>
 struct CtaLayout {
     static constexpr int NPD = D * NPE;
     static constexpr int NAD = D * NB;
     static constexpr int NSYM = NPD * (NPD + 1) / 2;
     static constexpr int NTRI = NAD * (NAD + 1) / 2;       // upper triangle of the element matrix
     static constexpr int NKT = NB * D * D * NPE;           // K T entries (all field blocks)
-    static constexpr int GPR = 2 * NGP * NPD;                      // g and w*g
+    // R1 holds, until phase 3, the Gauss-point gradients g and w*g (general
+    // cells) or the density Gram matrix A (rectangular cells, where g is not
+    // formed), then the staged T; from phase 4 on, K T
+    static constexpr bool A_IN_R1 = RECT && NPD * NPD <= 2 * NGP * NPD;
+    static constexpr int GPR = A_IN_R1 ? NPD * NPD : 2 * NGP * NPD;
     static constexpr int R1 = (GPR + NPE * NB > NPD * NAD) ? GPR + NPE * NB : NPD * NAD;
     static constexpr int oX = 0;
     static constexpr int oR1 = oX + NPE * D;
     static constexpr int oT = oR1 + GPR;                           // inside R1
-    static constexpr int oA = oR1 + R1;
-    static constexpr int oK = oA + NPD * NPD;
+    static constexpr int oA = A_IN_R1 ? oR1 : oR1 + R1;
+    static constexpr int oK = A_IN_R1 ? oR1 + R1 : oA + NPD * NPD;
     static constexpr int oTW = oK + NPD * NPD;                     // [slot][k] T weights in count order
     static constexpr int oU = oTW + NB * NPE;
     static constexpr int oUA = oU + NPD;
@@ -105,7 +109,7 @@ struct CtaLayout {
 
 template <int D, int NPE, int NGP, int NB, bool RECT, int NW>
 __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode) {
-    using L = CtaLayout<D, NPE, NGP, NB>;
+    using L = CtaLayout<D, NPE, NGP, NB, RECT>;
     constexpr int NPD = L::NPD, NAD = L::NAD, NSYM = L::NSYM, NT = 32 * NW;
     extern __shared__ __align__(16) unsigned char smem[];
     double* sd = reinterpret_cast<double*>(smem);
@@ -145,7 +149,12 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     const bool scatter_k = assemble && p.vals;
     constexpr int NSR = (NB * NB + NT - 1) / NT;  // scatter slots held per thread
 
-    for (int64_t e = blockIdx.x; e < p.ne; e += gridDim.x) {
+    // elements are taken in order from a device counter (after each CTA's
+    // first): CTAs cannot drift apart, so the CSR rows being scattered form
+    // one compact front that stays in L2 even when the matrix is many times
+    // larger
+    __shared__ int64_t s_next;
+    for (int64_t e = blockIdx.x; e < p.ne; e = s_next) {
         const int nb = p.nb[e];
         const double E = p.E[e];
         // ---- phase 0: loads --------------------------------------------------
@@ -174,6 +183,27 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         if (scatter_k)
             for (int i = tid; i < NB; i += NT) UL[i] = i < nb ? __ldg(p.ulen + B[i]) : 0;
+        // nonzero lists of the T rows (nodes), for the nodal values: weights in
+        // the K region and basis indices + counts in the scatter-slot region,
+        // both unused until phase 3; built by the last threads of the CTA
+        double* NZW = K;
+        uint8_t* NZJ = reinterpret_cast<uint8_t*>(S);
+        static_assert(NPE * NB <= NPD * NPD && NPE * NB + NPE <= 2 * NB * NB, "node lists fit their regions");
+        if (need_u) {
+            const int a = NT - 1 - tid;
+            if (a >= 0 && a < NPE) {
+                int cnt = 0;
+                for (int j = 0; j < nb; ++j) {
+                    const double t = T[a * NB + j];
+                    if (fem_nonzero(t)) {
+                        NZJ[a * NB + cnt] = (uint8_t)j;
+                        NZW[a * NB + cnt] = t;
+                        ++cnt;
+                    }
+                }
+                NZJ[NPE * NB + a] = (uint8_t)cnt;
+            }
+        }
         for (int i = tid; i < NB; i += NT) {
             int cnt = 0;
             if (i < nb)
@@ -286,12 +316,9 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         if (need_u)
             for (int r = tid; r < NPD; r += NT) {
-                const int f = r / NPE, a = r - f * NPE;
+                const int f = r / NPE, a = r - f * NPE, cnt = NZJ[NPE * NB + a];
                 double s = 0.0;
-                for (int j = 0; j < nb; ++j) {
-                    const double t = T[a * NB + j];
-                    if (fem_nonzero(t)) s = fma(t, UA[f * NB + j], s);
-                }
+                for (int k = 0; k < cnt; ++k) s = fma(NZW[a * NB + k], UA[f * NB + NZJ[a * NB + k]], s);
                 U[r] = s;
             }
         if (RECT && p.rho) {
@@ -408,6 +435,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 5: residual scatter, T^T (K T) upper triangle and scatter --------
+        if (tid == 0) s_next = (int64_t)gridDim.x + (int64_t)atomicAdd(p.queue, 1ull);
         if (need_u)
             for (int x = tid; x < NAD; x += NT) {
                 // count order: the lanes of a warp share trip counts

@@ -98,6 +98,7 @@ struct BulkArgs {
     const double* x;      // apply mode input (adof)
     double* y;            // apply mode output (adof)
     int* status;          // device error flags
+    unsigned long long* queue;  // element counter of the CTA kernels (zeroed per launch)
 };
 
 template <int D, int NPE, int NGP, int NB>
@@ -680,7 +681,7 @@ struct BulkVariant {
 template <int D, int NPE, int NGP, int NB, bool RECT>
 void fill_variants(BulkVariant* v) {
     using LW = BulkLayout<D, NPE, NGP, NB>;
-    using LC = CtaLayout<D, NPE, NGP, NB>;
+    using LC = CtaLayout<D, NPE, NGP, NB, RECT>;
     v[VAR_WARP4] = {(const void*)bulk_kernel<D, NPE, NGP, NB, RECT>, 128, 4, LW::kCtaBytes + 4 * LW::kWarpBytes, true};
     v[VAR_CTA2] = {(const void*)bulk_cta_kernel<D, NPE, NGP, NB, RECT, 2>, 64, 1, LC::kBytes, false};
     v[VAR_CTA4] = {(const void*)bulk_cta_kernel<D, NPE, NGP, NB, RECT, 4>, 128, 1, LC::kBytes, false};
@@ -874,10 +875,17 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.x = x;
     a.y = y;
     a.status = status_ptr(c);
+    // status words 2-3: the element counter of the CTA kernels
+    a.queue = reinterpret_cast<unsigned long long*>(status_ptr(c) + 2);
     cudaError_t e = cudaFuncSetAttribute(V.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)V.smem);
     if (e != cudaSuccess) return cuda_fail(c, e, "bulk smem attribute");
-    // exactly the resident CTAs: the grid-stride loop then sweeps elements in
-    // order as one compact front, so the CSR rows it scatters into stay in L2
+    if (!V.warp_kernel) {
+        e = cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), stream_of(c));
+        if (e != cudaSuccess) return cuda_fail(c, e, "bulk element counter");
+    }
+    // exactly the resident CTAs: they take elements in order (the CTA kernels
+    // from a device counter, the warp kernel by grid stride), one compact
+    // front whose CSR rows stay in L2
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, V.fn, V.threads, V.smem);
     if (e != cudaSuccess) return cuda_fail(c, e, "bulk occupancy");

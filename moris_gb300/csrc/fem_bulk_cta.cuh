@@ -211,16 +211,17 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             TC[i] = (uint8_t)cnt;
         }
         if (RECT) {
-            // constant Jacobian of the brick: diagonal at the first Gauss point;
+            // constant Jacobian of the brick: J_ii = half the edge length along
+            // axis i (node 0 is at xi = (-1,...), nodes 1, 3, 4 are its
+            // neighbours along xi_0, xi_1, xi_2 in the QUAD4 / HEX8 order), which
+            // is the diagonal of sum_a dN_a/dxi x_a at any point of the cell;
             // CJ[i<=j] = detJ / (J_ii J_jj): off-diagonal factors are the
             // remaining J entry (3D) or 1 (2D), diagonal ones one division each
             if (tid < D) {
+                constexpr int kNext[3] = {1, 3, 4};
                 double jd[D];
-                for (int i = 0; i < D; ++i) {
-                    double s = 0.0;
-                    for (int a = 0; a < NPE; ++a) s = fma(__ldg(p.dn + i * NPE + a), X[a * D + i], s);
-                    jd[i] = s;
-                }
+#pragma unroll
+                for (int i = 0; i < D; ++i) jd[i] = 0.5 * (X[kNext[i] * D + i] - X[i]);
                 const double detJ = (D == 3) ? jd[1] * jd[0] * jd[2] : jd[0] * jd[1];
                 // integration points with detJ below -1e-6 are skipped by the
                 // reference element loop (cl_FEM_Element_Bulk.cpp:164)

@@ -189,3 +189,39 @@ def simp_3d(n=128, seed=BASE_SEED + 5, finalize=True, beta=3.0):
     if finalize:
         m.finalize()
     return m, mesh, rho
+
+
+def main():
+    """One batched assembly of the XFEM workload (the case profiled in
+    profiles/): python -m moris_gb300.workloads --xfem 48 [--warps 4 --split 0]"""
+    import argparse
+    import json
+    import time
+
+    import torch
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--xfem", type=int, default=48, help="background cells per edge")
+    ap.add_argument("--warps", type=int, default=4)
+    ap.add_argument("--split", type=int, default=0)
+    ap.add_argument("--repeat", type=int, default=1)
+    a = ap.parse_args()
+    m, x, _ = xfem_spheres(a.xfem, device=True)
+    m.set_batched_config(a.warps, a.split)
+    dev = torch.device("cuda")
+    u = torch.zeros(m.num_adofs, dtype=torch.float64, device=dev)
+    vals = torch.zeros(m.nnz, dtype=torch.float64, device=dev)
+    rhs = torch.zeros(m.num_adofs, dtype=torch.float64, device=dev)
+    times = []
+    for _ in range(a.repeat):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.assemble_batched(u, vals, rhs)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    m.check_status()
+    print(json.dumps({"n": a.xfem, "adofs": m.num_adofs, "nnz": m.nnz, "seconds": times}))
+
+
+if __name__ == "__main__":
+    main()

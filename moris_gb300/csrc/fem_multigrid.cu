@@ -72,25 +72,52 @@ __device__ void mg_block_sum_add(double v, double* out) {
 
 // level-0 stencil from the CSR of the assembled operator (one thread per row);
 // err |= 1 for a column outside the 27-node neighbourhood
-__global__ void mg_csr_to_stencil(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
-                                  const double* __restrict__ v, double* __restrict__ S, int* err) {
-    const int64_t N = (int64_t)n * n * n;
-    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < 3 * N;
-         row += (int64_t)gridDim.x * blockDim.x) {
-        const int f = (int)(row / N);
-        const int64_t i = row - f * N;
-        const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
-        for (int e = rp[row]; e < rp[row + 1]; ++e) {
-            const int64_t col = ci[e];
-            const int g = (int)(col / N);
-            const int64_t j = col - g * N;
-            const int dx = (int)(j % n) - ix, dy = (int)((j / n) % n) - iy, dz = (int)(j / ((int64_t)n * n)) - iz;
-            if (g < 0 || g > 2 || dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
-                atomicOr(err, 1);
-                continue;
+// One CTA per block of kCsRows consecutive rows: their nonzeros are one contiguous
+// range of the CSR, loaded coalesced into shared memory; then kCsPart threads
+// per row take its entries with stride kCsPart.  Consecutive rows are
+// consecutive nodes, so the lanes of a warp that hold the same entry index of
+// neighbouring rows write consecutive words.  A block whose range exceeds the
+// staging space (rows longer than 27 x 3 entries, which are an error anyway)
+// reads from global memory.
+constexpr int kCsRows = 64, kCsPart = 8, kCsCap = kCsRows * 81;
+constexpr size_t kCsSmem = (size_t)kCsCap * (sizeof(double) + sizeof(int32_t));
+__global__ void __launch_bounds__(kCsPart * kCsRows) mg_csr_to_stencil(int n, const int32_t* __restrict__ rp,
+                                                               const int32_t* __restrict__ ci,
+                                                               const double* __restrict__ v,
+                                                               double* __restrict__ S, int* err) {
+    extern __shared__ __align__(16) unsigned char cs_smem[];
+    double* sv = reinterpret_cast<double*>(cs_smem);
+    int32_t* sc = reinterpret_cast<int32_t*>(sv + kCsCap);
+    const int64_t N = (int64_t)n * n * n, rows = 3 * N;
+    for (int64_t r0 = (int64_t)blockIdx.x * kCsRows; r0 < rows; r0 += (int64_t)gridDim.x * kCsRows) {
+        const int64_t r1 = r0 + kCsRows < rows ? r0 + kCsRows : rows;
+        const int64_t e0 = rp[r0], e1 = rp[r1];
+        const bool staged = e1 - e0 <= kCsCap;
+        if (staged)
+            for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+                sv[e - e0] = v[e];
+                sc[e - e0] = ci[e];
             }
-            S[sidx((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1), f, g, N, i)] = v[e];
+        __syncthreads();
+        const int64_t row = r0 + threadIdx.x / kCsPart;
+        if (row < r1) {
+            const int f = (int)(row / N);
+            const int64_t i = row - f * N;
+            const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
+            const int64_t b = rp[row + 1];
+            for (int64_t e = rp[row] + threadIdx.x % kCsPart; e < b; e += kCsPart) {
+                const int64_t col = staged ? sc[e - e0] : ci[e];
+                const int g = (int)(col / N);
+                const int64_t j = col - g * N;
+                const int dx = (int)(j % n) - ix, dy = (int)((j / n) % n) - iy, dz = (int)(j / ((int64_t)n * n)) - iz;
+                if (g < 0 || g > 2 || dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+                    atomicOr(err, 1);
+                    continue;
+                }
+                S[sidx((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1), f, g, N, i)] = staged ? sv[e - e0] : v[e];
+            }
         }
+        __syncthreads();
     }
 }
 
@@ -160,6 +187,16 @@ __global__ void mg_sumsq(int64_t m, const TV* __restrict__ x, double* dots) {
 
 template <typename TV>
 __global__ void mg_scale(int64_t m, double a, const TV* __restrict__ y, TV* __restrict__ x) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
+        x[t] = (TV)(a * (double)y[t]);
+}
+// x = y / sqrt(*yy) (0 when *yy is not positive), the power-iteration
+// normalisation without a host round trip
+template <typename TV>
+__global__ void mg_scale_norm(int64_t m, const double* __restrict__ yy, const TV* __restrict__ y,
+                              TV* __restrict__ x) {
+    const double d = *yy;
+    const double a = d > 0.0 ? 1.0 / sqrt(d) : 0.0;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
         x[t] = (TV)(a * (double)y[t]);
 }
@@ -333,24 +370,38 @@ __device__ __forceinline__ int target(int s, int t) { return (s & 1) ? ((s - 1) 
 // the rounding of the assembly's atomic sums, relative to the entries and to
 // the diagonals of rows i and j)
 __global__ void mg_check_symmetric(int n, const double* __restrict__ S, int* err) {
+    // one thread per node I: every tap k <= 13 and component pair (f, g) of row
+    // I against the mirrored entry (26 - k, g, f) of the neighbour J; threads of
+    // a warp are consecutive nodes, so both operands load coalesced
     const int64_t N = (int64_t)n * n * n;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < 14 * 9 * N;
-         t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t I = t % N;
-        const int fg = (int)((t / N) % 9), k = (int)(t / (9 * N));
-        const int f = fg / 3, g = fg % 3;
-        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+    bool bad = false;
+    for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < N; I += (int64_t)gridDim.x * blockDim.x) {
         const int X = (int)(I % n), Y = (int)((I / n) % n), Z = (int)(I / ((int64_t)n * n));
-        if (X + dx < 0 || X + dx >= n || Y + dy < 0 || Y + dy >= n || Z + dz < 0 || Z + dz >= n) continue;
-        const int64_t J = I + dx + (int64_t)n * (dy + (int64_t)n * dz);
-        const double a = S[sidx(k, f, g, N, I)], b = S[sidx(26 - k, g, f, N, J)];
-        // entries that cancel to near zero carry the rounding of their terms, which
-        // scale with the diagonal: measure the asymmetry against the diagonals too
-        // the threshold in FP32 (a square root on the FP64 pipe costs far more)
-        const float dd = sqrtf(fabsf((float)S[sidx(13, f, f, N, I)]) * fabsf((float)S[sidx(13, g, g, N, J)]));
-        const float tol = 1e-10f * (float)(fabs(a) + fabs(b)) + 1e-12f * dd;
-        if (!((float)fabs(a - b) <= tol)) atomicOr(err, 2);
+        float di[3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) di[f] = fabsf((float)S[sidx(13, f, f, N, I)]);
+        for (int k = 0; k <= 13; ++k) {
+            const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+            if (X + dx < 0 || X + dx >= n || Y + dy < 0 || Y + dy >= n || Z + dz < 0 || Z + dz >= n) continue;
+            const int64_t J = I + dx + (int64_t)n * (dy + (int64_t)n * dz);
+            float dj[3];
+#pragma unroll
+            for (int g = 0; g < 3; ++g) dj[g] = fabsf((float)S[sidx(13, g, g, N, J)]);
+#pragma unroll
+            for (int f = 0; f < 3; ++f)
+#pragma unroll
+                for (int g = 0; g < 3; ++g) {
+                    const double a = S[sidx(k, f, g, N, I)], b = S[sidx(26 - k, g, f, N, J)];
+                    // entries that cancel to near zero carry the rounding of their
+                    // terms, which scales with the diagonals: measure the asymmetry
+                    // against them too (in FP32: a square root on the FP64 pipe
+                    // costs far more)
+                    const float tol = 1e-10f * (float)(fabs(a) + fabs(b)) + 1e-12f * sqrtf(di[f] * dj[g]);
+                    bad |= !((float)fabs(a - b) <= tol);
+                }
+        }
     }
+    if (bad) atomicOr(err, 2);
 }
 
 // One-axis Galerkin coarsening of a 27-point block stencil: P = P_z (x) P_y (x)
@@ -430,21 +481,15 @@ __global__ void mg_dense(int n, const double* __restrict__ S, double* __restrict
 
 // Gauss-Jordan inversion in place, pivot k: stash row k and column k, then
 // update every entry (a[k][k] > 0 for an SPD operator)
-__global__ void mg_gj_stash(int64_t m, const double* __restrict__ A, int64_t k, double* __restrict__ row,
-                            double* __restrict__ col) {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
-        row[t] = A[k * m + t];
-        col[t] = A[t * m + k];
-    }
-}
-__global__ void mg_gj_update(int64_t m, double* __restrict__ A, int64_t k, const double* __restrict__ row,
-                             const double* __restrict__ col) {
-    const double inv = 1.0 / row[k];
+// Gauss-Jordan step k of the in-place inverse, from A to B (two buffers, so the
+// pivot row and column are read from the previous step without a copy)
+__global__ void mg_gj_step(int64_t m, const double* __restrict__ A, double* __restrict__ B, int64_t k) {
+    const double inv = 1.0 / A[k * m + k];
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m * m; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t / m, j = t - i * m;
-        const double rk = (j == k ? 1.0 : row[j]) * inv;
-        if (i == k) A[t] = rk;
-        else A[t] = (j == k ? 0.0 : A[t]) - col[i] * rk;
+        const double rk = (j == k ? 1.0 : A[k * m + j]) * inv;
+        if (i == k) B[t] = rk;
+        else B[t] = (j == k ? 0.0 : A[t]) - A[i * m + k] * rk;
     }
 }
 
@@ -485,6 +530,7 @@ struct fem_mg {
     fem_mg_opts o{};
     double setup_seconds = 0.0;
     double* dots = nullptr;
+    double* pdots = nullptr;  // power-iteration norms (power_iters + 1)
     int* err = nullptr;
     std::vector<void*> bufs;
     ~fem_mg() {
@@ -593,20 +639,22 @@ double power_lambda(fem_mg* g, const fem_mg::Level& L, const TS* S, const TV* di
         mg_convert<double, TV><<<vb, kTpb>>>(3 * L.N, px, y);
         mg_scale<TV><<<vb, kTpb>>>(3 * L.N, 1.0, y, x);
     }
-    cudaMemset(g->dots, 0, sizeof(double));
-    mg_sumsq<TV><<<vb, kTpb>>>(3 * L.N, x, g->dots);
-    double xx = 0.0;
-    cudaMemcpy(&xx, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
-    double xn = std::sqrt(xx), lam = 0.0;
+    // squared norms on the device: pd[0] = |x0|^2, pd[it + 1] = |D^-1 A x_it|^2,
+    // with x_(it+1) normalised there; the host reads them once at the end
+    double* pd = g->pdots;
+    cudaMemset(pd, 0, (iters + 1) * sizeof(double));
+    mg_sumsq<TV><<<vb, kTpb>>>(3 * L.N, x, pd);
     for (int it = 0; it < iters; ++it) {
-        cudaMemset(g->dots, 0, sizeof(double));
-        mg_power<TS, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, S, dinv, x, y, g->dots);
-        double yy = 0.0;
-        cudaMemcpy(&yy, g->dots, sizeof(double), cudaMemcpyDeviceToHost);
-        const double yn = std::sqrt(yy);
+        mg_power<TS, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, S, dinv, x, y, pd + it + 1);
+        mg_scale_norm<TV><<<vb, kTpb>>>(3 * L.N, pd + it + 1, y, x);
+    }
+    std::vector<double> h(iters + 1, 0.0);
+    cudaMemcpy(h.data(), pd, (iters + 1) * sizeof(double), cudaMemcpyDeviceToHost);
+    double xn = std::sqrt(h[0]), lam = 0.0;
+    for (int it = 0; it < iters; ++it) {
+        const double yn = std::sqrt(h[it + 1]);
         lam = yn / xn;
         if (!(yn > 0.0)) break;
-        mg_scale<TV><<<vb, kTpb>>>(3 * L.N, 1.0 / yn, y, x);
         xn = 1.0;
     }
     return lam;
@@ -674,7 +722,8 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
     fem_mg* g = new fem_mg();
     g->o = o;
     g->lv.resize(ns.size());
-    bool ok = g->alloc(&g->dots, 4) && g->alloc(&g->err, 1);
+    bool ok = g->alloc(&g->dots, 4) && g->alloc(&g->pdots, (size_t)std::max(o.power_iters, 1) + 1) &&
+              g->alloc(&g->err, 1);
     for (size_t l = 0; ok && l < ns.size(); ++l) {
         fem_mg::Level& L = g->lv[l];
         L.n = ns[l];
@@ -686,8 +735,8 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
         if (ok && L.fp32) ok = g->alloc(&L.S32, 243 * L.N) && g->alloc(&L.dinv32, 3 * L.N);
     }
     g->m = 3 * g->lv.back().N;
-    double *row = nullptr, *col = nullptr;
-    if (ok) ok = g->alloc(&g->ainv, g->m * g->m) && g->alloc(&row, g->m) && g->alloc(&col, g->m);
+    double* ainv2 = nullptr;
+    if (ok) ok = g->alloc(&g->ainv, g->m * g->m) && g->alloc(&ainv2, g->m * g->m);
     if (!ok) {
         delete g;
         return fail(c, FEM_GPU_OUT_OF_MEMORY, "multigrid hierarchy");
@@ -696,8 +745,10 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
     fem_mg::Level& L0 = g->lv[0];
     cudaMemset(L0.S, 0, 243 * L0.N * sizeof(double));
     cudaMemset(g->err, 0, sizeof(int));
-    mg_csr_to_stencil<<<blocks_for(3 * L0.N, kTpb), kTpb>>>(L0.n, rowptr, colidx, vals, L0.S, g->err);
-    mg_check_symmetric<<<blocks_for(126 * L0.N, kTpb), kTpb>>>(L0.n, L0.S, g->err);
+    cudaFuncSetAttribute(mg_csr_to_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCsSmem);
+    mg_csr_to_stencil<<<blocks_for(3 * L0.N, kCsRows), kCsPart * kCsRows, kCsSmem>>>(L0.n, rowptr, colidx, vals,
+                                                                                    L0.S, g->err);
+    mg_check_symmetric<<<blocks_for(L0.N, kTpb), kTpb>>>(L0.n, L0.S, g->err);
     {
         // Galerkin products axis by axis through two scratch boxes (freed after setup)
         const int64_t n0 = L0.n, n1 = (n0 - 1) / 2 + 1;
@@ -757,8 +808,8 @@ fem_gpu_status fem_mg_create(fem_gpu_ctx* c, const int32_t* rowptr, const int32_
     cudaMemset(g->ainv, 0, g->m * g->m * sizeof(double));
     mg_dense<<<blocks_for(g->m, kTpb), kTpb>>>(LC.n, LC.S, g->ainv);
     for (int64_t k = 0; k < g->m; ++k) {
-        mg_gj_stash<<<blocks_for(g->m, kTpb), kTpb>>>(g->m, g->ainv, k, row, col);
-        mg_gj_update<<<blocks_for(g->m * g->m, kTpb), kTpb>>>(g->m, g->ainv, k, row, col);
+        mg_gj_step<<<blocks_for(g->m * g->m, kTpb), kTpb>>>(g->m, g->ainv, ainv2, k);
+        std::swap(g->ainv, ainv2);
     }
     if (cudaDeviceSynchronize() != cudaSuccess || cudaGetLastError() != cudaSuccess) {
         delete g;

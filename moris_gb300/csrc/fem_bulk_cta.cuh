@@ -1,21 +1,24 @@
 // fem_bulk_cta.cuh -- bulk elasticity with one element per CTA.
 //
-// Same arithmetic as the warp-per-element kernel in fem_device.cu (Gram
-// matrix of the physical gradients, isotropic K from it, sparse T^T K T,
-// CSR scatter), but the phases of one element are spread over NW warps and
-// several CTAs share an SM, so the FP64 pipe sees enough independent warps
-// to cover its latency.  Shared memory per CTA is sized so that 7 CTAs fit
-// on one SM for the hex8 / quadratic B-spline element (the extraction T is
-// staged in the tail of the Gauss-point region and is dead before the K T
-// product overwrites it).
+// The element quantities of the warp-per-element kernel in fem_device.cu (Gram
+// matrix of the physical gradients, isotropic K from it, sparse T^T K T, CSR
+// scatter), with the phases of one element spread over NW warps and several
+// CTAs per SM, so that the FP64 pipe sees enough independent warps to cover its
+// latency.  The T^T K T stage works on the element adofs ordered by the nonzero
+// count of their T column: every upper-triangle entry contracts over the
+// sparser of its two columns, and entries of one count are contiguous, so the
+// warps run uniform trip counts.  Elements come from a device counter, in order.
+// Shared memory per CTA is sized so that 8 CTAs fit on one SM for the hex8 /
+// quadratic B-spline element (the extraction T is staged in a region that the
+// K T product overwrites once T is no longer needed).
 //
 // RECT (axis-aligned brick cells, the reference's CellShape::RECTANGULAR with
 // its diagonal Jacobian): a trilinear map whose Jacobian is diagonal at every
 // Gauss point is affine, so J is constant over the cell and the Gram matrix is
 //   A[(i,a),(j,b)] = detJ / (J_ii J_jj) * G0[(i,a),(j,b)],
 //   G0 = sum_q w_q dN_a/dxi_i dN_b/dxi_j          (per-rule table, p.g0),
-// which replaces 27 FMAs per Gram entry by one multiply.  J is evaluated at
-// the first Gauss point like the reference evaluates it at every point.
+// which replaces 27 FMAs per Gram entry by one multiply.  J_ii is half the
+// edge length of the cell along axis i.
 //
 // MODE_APPLY (matrix-free Jacobian-vector product) forms the pdof K the same
 // way and scatters T^T (K T x) without the K T / T^T K T stages.
@@ -99,8 +102,9 @@ struct CtaLayout {
     static_assert((D - 1) * NPE * NPD + D * NPE <= 1024 && NPD * NAD <= 8192, "K T table packing");
 };
 
-// Item tables of the K T and T^T K T phases (built on the host per basis width,
-// fem_bulk_tables): they replace per-entry index arithmetic by one load.
+// Item tables of the K T and T^T K T phases (built on the host per basis width
+// when a bulk set is uploaded, fem_device.cu): they replace per-entry index
+// arithmetic by one load.
 //   ktab[t]: slot | kbase << 6 | ktdst << 16, items slot-major so that the
 //            lanes of a warp share one column (one trip count)
 //            kbase = g*NPE*NPD + f*NPE + a, ktdst = (f*NPE + a)*NAD + slot*D + g
@@ -150,9 +154,9 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     constexpr int NSR = (NB * NB + NT - 1) / NT;  // scatter slots held per thread
 
     // elements are taken in order from a device counter (after each CTA's
-    // first): CTAs cannot drift apart, so the CSR rows being scattered form
-    // one compact front that stays in L2 even when the matrix is many times
-    // larger
+    // first): CTAs cannot drift apart, so the CSR rows being scattered form one
+    // compact front and most of the scatter stays in L2 even when the matrix is
+    // many times larger than L2
     __shared__ int64_t s_next;
     for (int64_t e = blockIdx.x; e < p.ne; e = s_next) {
         const int nb = p.nb[e];

@@ -189,23 +189,23 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             for (int i = tid; i < NB; i += NT) UL[i] = i < nb ? __ldg(p.ulen + B[i]) : 0;
         // nonzero lists of the T rows (nodes), for the nodal values: weights in
         // the K region and basis indices + counts in the scatter-slot region,
-        // both unused until phase 3; built by the last threads of the CTA
+        // both unused until phase 3; one warp per node, the lanes over the
+        // bases, positions from a ballot (ascending basis order)
         double* NZW = K;
         uint8_t* NZJ = reinterpret_cast<uint8_t*>(S);
         static_assert(NPE * NB <= NPD * NPD && NPE * NB + NPE <= 2 * NB * NB, "node lists fit their regions");
         if (need_u) {
-            const int a = NT - 1 - tid;
-            if (a >= 0 && a < NPE) {
-                int cnt = 0;
-                for (int j = 0; j < nb; ++j) {
-                    const double t = T[a * NB + j];
-                    if (fem_nonzero(t)) {
-                        NZJ[a * NB + cnt] = (uint8_t)j;
-                        NZW[a * NB + cnt] = t;
-                        ++cnt;
-                    }
+            const int lane = tid & 31;
+            for (int a = tid >> 5; a < NPE; a += NW) {
+                const double t = lane < NB ? T[a * NB + lane] : 0.0;
+                const bool nz = lane < nb && fem_nonzero(t);
+                const unsigned m = __ballot_sync(0xffffffffu, nz);
+                if (nz) {
+                    const int pos = __popc(m & ((1u << lane) - 1u));
+                    NZJ[a * NB + pos] = (uint8_t)lane;
+                    NZW[a * NB + pos] = t;
                 }
-                NZJ[NPE * NB + a] = (uint8_t)cnt;
+                if (lane == 0) NZJ[NPE * NB + a] = (uint8_t)__popc(m);
             }
         }
         for (int i = tid; i < NB; i += NT) {
@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             CP[rank] = (uint8_t)j;
             CPI[j] = (uint8_t)rank;
         }
-        if (need_u)
-            for (int r = tid; r < NPD; r += NT) {
+        if (need_u)  // on the last warp (the first one computes the count order)
+            for (int r = tid - (NT - 32); r >= 0 && r < NPD; r += 32) {
                 const int f = r / NPE, a = r - f * NPE, cnt = NZJ[NPE * NB + a];
                 double s = 0.0;
                 for (int k = 0; k < cnt; ++k) s = fma(NZW[a * NB + k], UA[f * NB + NZJ[a * NB + k]], s);
@@ -421,12 +421,20 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 4: pdof residual and K T ----------------------------------------
-        if (need_u)
-            for (int r = tid; r < NPD; r += NT) {
+        if (need_u) {
+            // K U with four lanes per row and a shuffle sum: dot chains a quarter
+            // as long, spread over several warps (4 NPD is a multiple of 32, so a
+            // warp takes part whole)
+            static_assert((4 * NPD) % 32 == 0, "K U lanes fill whole warps");
+            for (int t = tid; t < 4 * NPD; t += NT) {
+                const int r = t >> 2, q = t & 3;
                 double s = 0.0;
-                for (int c = 0; c < NPD; ++c) s = fma(K[r * NPD + c], U[c], s);
-                RP[r] = s;
+                for (int c = q; c < NPD; c += 4) s = fma(K[r * NPD + c], U[c], s);
+                s += __shfl_xor_sync(0xffffffffu, s, 1);
+                s += __shfl_xor_sync(0xffffffffu, s, 2);
+                if (q == 0) RP[r] = s;
             }
+        }
         if (want_k) {
             // KT[(f,a)][x], x = slot * D + g: K symmetric, K[(f,a),(g,b)] is read
             // as K[(g,b),(f,a)], consecutive words along a

@@ -1170,11 +1170,14 @@ fem_gpu_status cluster_finalize(fem_gpu_ctx* c, int set) {
     const int sides = s.kind == 2 ? 2 : 1;
     const Rule r = gauss_rule(s.kind == 2 ? s.dside.integration_rule : s.bulk.integration_rule);
     s.ngp = r.n;
-    std::vector<int32_t> bases((size_t)s.neq * sides * W, -1);
-    std::vector<double> T((size_t)s.neq * sides * 8 * W, 0.0);
+    // repack to the kernel width W (the host arrays are already in that layout
+    // when the set's basis width is W)
+    const bool same = W == s.maxnb;
+    std::vector<int32_t> bases(same ? 0 : (size_t)s.neq * sides * W, -1);
+    std::vector<double> T(same ? 0 : (size_t)s.neq * sides * 8 * W, 0.0);
     const int W2 = sides * W, M2 = sides * s.maxnb;
-    std::vector<uint16_t> sidx((size_t)s.neq * W2 * W2, 0);
-    for (int64_t i = 0; i < s.neq; ++i) {
+    std::vector<uint16_t> sidx(same ? 0 : (size_t)s.neq * W2 * W2, 0);
+    for (int64_t i = 0; i < (same ? 0 : s.neq); ++i) {
         for (int sd = 0; sd < sides; ++sd) {
             for (int j = 0; j < s.maxnb; ++j) bases[(i * sides + sd) * W + j] = s.bases[(i * sides + sd) * s.maxnb + j];
             for (int a = 0; a < 8; ++a)
@@ -1191,9 +1194,9 @@ fem_gpu_status cluster_finalize(fem_gpu_ctx* c, int set) {
     if (e == cudaSuccess) e = upload(s.d_gp, r.pts, st);
     if (e == cudaSuccess) e = upload(s.d_gw, r.w, st);
     if (e == cudaSuccess) e = upload(s.d_nb, s.nb, st);
-    if (e == cudaSuccess) e = upload(s.d_bases, bases, st);
-    if (e == cudaSuccess) e = upload(s.d_T, T, st);
-    if (e == cudaSuccess) e = upload(s.d_sidx, sidx, st);
+    if (e == cudaSuccess) e = upload(s.d_bases, same ? s.bases : bases, st);
+    if (e == cudaSuccess) e = upload(s.d_T, same ? s.T : T, st);
+    if (e == cudaSuccess) e = upload(s.d_sidx, same ? s.sidx : sidx, st);
     if (e == cudaSuccess) e = upload(s.d_xe, s.xe, st);
     if (e == cudaSuccess) e = upload(s.d_E, s.E, st);
     if (s.kind == 0) {
@@ -1210,7 +1213,7 @@ fem_gpu_status cluster_finalize(fem_gpu_ctx* c, int set) {
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cfail(c, e, "cluster set upload");
-    s.bases.swap(bases);
+    if (!same) s.bases.swap(bases);
     s.maxnb = W;
     s.nbsel = W;
     s.T.clear();

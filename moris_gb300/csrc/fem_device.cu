@@ -1157,12 +1157,14 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
             if ((e = upload(ds.d_gw, r.w, sm)) != cudaSuccess) return cuda_fail(c, e, "side gw");
             ds.nbsel = s.maxnb;
         }
-        // repack element data to the kernel's padded basis width
+        // repack element data to the kernel's padded basis width (the host
+        // arrays are already in that layout when the set's width is W)
         const int W = ds.nbsel;
-        std::vector<int32_t> bases((size_t)s.neq * W, -1);
-        std::vector<double> T((size_t)s.neq * NPE * W, 0.0);
-        std::vector<uint16_t> sidx((size_t)s.neq * W * W, 0);
-        for (int64_t i = 0; i < s.neq; ++i) {
+        const bool same = W == s.maxnb;
+        std::vector<int32_t> bases(same ? 0 : (size_t)s.neq * W, -1);
+        std::vector<double> T(same ? 0 : (size_t)s.neq * NPE * W, 0.0);
+        std::vector<uint16_t> sidx(same ? 0 : (size_t)s.neq * W * W, 0);
+        for (int64_t i = 0; i < (same ? 0 : s.neq); ++i) {
             for (int j = 0; j < s.maxnb; ++j) bases[i * W + j] = s.bases[i * s.maxnb + j];
             for (int a = 0; a < NPE; ++a)
                 for (int j = 0; j < s.maxnb; ++j) T[(i * NPE + a) * W + j] = s.T[(i * NPE + a) * s.maxnb + j];
@@ -1171,9 +1173,9 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
                     sidx[(i * W + ii) * W + jj] = s.sidx[(i * s.maxnb + ii) * s.maxnb + jj];
         }
         if ((e = upload(s.d_nb, s.nb, sm)) != cudaSuccess) return cuda_fail(c, e, "nb");
-        if ((e = upload(s.d_bases, bases, sm)) != cudaSuccess) return cuda_fail(c, e, "bases");
-        if ((e = upload(s.d_T, T, sm)) != cudaSuccess) return cuda_fail(c, e, "T");
-        if ((e = upload(s.d_sidx, sidx, sm)) != cudaSuccess) return cuda_fail(c, e, "sidx");
+        if ((e = upload(s.d_bases, same ? s.bases : bases, sm)) != cudaSuccess) return cuda_fail(c, e, "bases");
+        if ((e = upload(s.d_T, same ? s.T : T, sm)) != cudaSuccess) return cuda_fail(c, e, "T");
+        if ((e = upload(s.d_sidx, same ? s.sidx : sidx, sm)) != cudaSuccess) return cuda_fail(c, e, "sidx");
         if ((e = upload(s.d_xe, s.xe, sm)) != cudaSuccess) return cuda_fail(c, e, "xe");
         if ((e = upload(s.d_E, s.E, sm)) != cudaSuccess) return cuda_fail(c, e, "E");
         if (s.kind == 1)

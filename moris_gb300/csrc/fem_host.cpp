@@ -25,9 +25,25 @@ int hw_threads() {
 }
 
 // run f(i) for i in [0, n) on all host threads, in contiguous chunks
+// threads parallel_for uses for n items
+int range_threads(int64_t n) { return (int)std::min<int64_t>(hw_threads(), std::max<int64_t>(1, n / 256)); }
+
+// f(t, begin, end) on nt = range_threads(n) threads, thread t taking the
+// contiguous range [n t / nt, n (t + 1) / nt)
+template <class F>
+void parallel_ranges(int64_t n, int nt, F f) {
+    if (nt <= 1) {
+        f(0, (int64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) th.emplace_back([=]() { f(t, n * t / nt, n * (t + 1) / nt); });
+    for (auto& x : th) x.join();
+}
+
 template <class F>
 void parallel_for(int64_t n, F f) {
-    const int nt = (int)std::min<int64_t>(hw_threads(), std::max<int64_t>(1, n / 256));
+    const int nt = range_threads(n);
     if (nt <= 1) {
         for (int64_t i = 0; i < n; ++i) f(i);
         return;
@@ -39,6 +55,15 @@ void parallel_for(int64_t n, F f) {
             for (int64_t i = b; i < e; ++i) f(i);
         });
     for (auto& x : th) x.join();
+}
+
+// runs the callables on threads of their own: the large per-set arrays are
+// filled concurrently, so their first-touch page faults overlap
+template <class... F>
+void concurrently(F&&... fs) {
+    std::vector<std::thread> th;
+    (th.emplace_back(std::forward<F>(fs)), ...);
+    for (auto& t : th) t.join();
 }
 
 // Cox-de Boor evaluation of one B-spline basis of an element, in element
@@ -498,10 +523,18 @@ fem_gpu_status interface_volumes(fem_gpu_ctx* c) {
     for (auto& s : c->sets)
         need_vol |= s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
     if (need_vol) {
+        // only the cells that interface clusters name need a volume
+        std::vector<char> needed(c->num_cells, 0);
+        for (auto& s : c->sets) {
+            if (s.kind != 2 || s.dside.iwg_type == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST) continue;
+            for (auto v : s.ip_cell) needed[v] = 1;
+            for (auto v : s.fcell) needed[v] = 1;
+        }
         cell_vol.assign(c->num_cells, 0.0);
         for (auto& s : c->sets) {
             if (s.kind != 0) continue;
             for (int64_t i = 0; i < s.neq; ++i) {
+                if (!needed[s.ip_cell[i]]) continue;
                 double v = 0.0;
                 if (s.ig_off.empty()) {
                     v = ip_cell_measure(c, s.ip_cell[i]);
@@ -636,31 +669,38 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
                     partners[fillp[s.fcell[i]]++] = s.ip_cell[i];
                 }
     }
-    // union lists U(b): bases of every equation object that contains b
-    std::vector<std::vector<int32_t>> U(nu);
-    parallel_for(nu, [&](int64_t b) {
-        auto& u = U[b];
-        for (int64_t k = adj_off[b]; k < adj_off[b + 1]; ++k) {
-            const int64_t e = adj[k];
-            u.insert(u.end(), cb.begin() + cb_off[e], cb.begin() + cb_off[e] + cb_len[e]);
-            for (int64_t q = pt_off[e]; q < pt_off[e + 1]; ++q) {
-                const int64_t e2 = partners[q];
-                u.insert(u.end(), cb.begin() + cb_off[e2], cb.begin() + cb_off[e2] + cb_len[e2]);
-            }
-        }
-        std::sort(u.begin(), u.end());
-        u.erase(std::unique(u.begin(), u.end()), u.end());
-    });
+    // union lists U(b): bases of every equation object that contains b.  Each
+    // thread appends the lists of its contiguous basis range to one arena, which
+    // then is a contiguous piece of ucols (no per-basis allocations)
+    const int unt = range_threads(nu);
+    std::vector<std::vector<int32_t>> arena(unt);
     c->ulen.resize(nu);
+    parallel_ranges(nu, unt, [&](int t, int64_t b0, int64_t b1) {
+        std::vector<int32_t>& out = arena[t];
+        std::vector<int32_t> u;
+        for (int64_t b = b0; b < b1; ++b) {
+            u.clear();
+            for (int64_t k = adj_off[b]; k < adj_off[b + 1]; ++k) {
+                const int64_t e = adj[k];
+                u.insert(u.end(), cb.begin() + cb_off[e], cb.begin() + cb_off[e] + cb_len[e]);
+                for (int64_t q = pt_off[e]; q < pt_off[e + 1]; ++q) {
+                    const int64_t e2 = partners[q];
+                    u.insert(u.end(), cb.begin() + cb_off[e2], cb.begin() + cb_off[e2] + cb_len[e2]);
+                }
+            }
+            std::sort(u.begin(), u.end());
+            u.erase(std::unique(u.begin(), u.end()), u.end());
+            c->ulen[b] = (int32_t)u.size();
+            out.insert(out.end(), u.begin(), u.end());
+        }
+    });
     c->uoff.assign(nu + 1, 0);
-    for (int64_t b = 0; b < nu; ++b) {
-        c->ulen[b] = (int32_t)U[b].size();
-        c->uoff[b + 1] = c->uoff[b] + (int64_t)U[b].size();
-    }
+    for (int64_t b = 0; b < nu; ++b) c->uoff[b + 1] = c->uoff[b] + c->ulen[b];
     c->ucols.resize(c->uoff[nu]);
-    parallel_for(nu, [&](int64_t b) { std::copy(U[b].begin(), U[b].end(), c->ucols.begin() + c->uoff[b]); });
-    U.clear();
-    U.shrink_to_fit();
+    parallel_ranges(nu, unt, [&](int t, int64_t b0, int64_t) {
+        std::copy(arena[t].begin(), arena[t].end(), c->ucols.begin() + c->uoff[b0]);
+    });
+    arena.clear();
     const int64_t nad = nu * dim;
     c->rowptr.assign(nad + 1, 0);
     int64_t acc = 0;
@@ -681,11 +721,10 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
             if (2 * maxnb > 255) return fail(c, FEM_GPU_UNSUPPORTED, "more than 255 bases per element");
             s.maxnb = maxnb;
             const int W2 = 2 * maxnb;
-            s.nb.assign(s.neq * 2, 0);
-            s.bases.assign(s.neq * 2 * maxnb, -1);
-            s.T.assign(s.neq * 2 * npe * maxnb, 0.0);
-            s.sidx.assign(s.neq * W2 * W2, 0);
-            s.xe.resize(s.neq * 2 * npe * dim);
+            concurrently([&] { s.nb.assign(s.neq * 2, 0); s.bases.assign(s.neq * 2 * maxnb, -1); },
+                         [&] { s.T.assign(s.neq * 2 * npe * maxnb, 0.0); },
+                         [&] { s.sidx.assign(s.neq * W2 * W2, 0); },
+                         [&] { s.xe.resize(s.neq * 2 * npe * dim); });
 
             std::atomic<bool> bad{false};
             parallel_for(s.neq, [&](int64_t i) {
@@ -729,12 +768,10 @@ fem_gpu_status fem_gpu_finalize_host(fem_gpu_ctx* c) {
         for (int64_t i = 0; i < s.neq; ++i) maxnb = std::max(maxnb, cb_len[s.ip_cell[i]]);
         if (maxnb > 255) return fail(c, FEM_GPU_UNSUPPORTED, "more than 255 bases per element");
         s.maxnb = maxnb;
-        s.nb.resize(s.neq);
-        s.bases.assign(s.neq * maxnb, -1);
-        s.T.assign(s.neq * npe * maxnb, 0.0);
-        s.sidx.assign(s.neq * maxnb * maxnb, 0);
-        s.xe.resize(s.neq * npe * dim);
-        if (!s.node_rho.empty()) s.rhoe.resize(s.neq * npe);
+        concurrently([&] { s.nb.resize(s.neq); s.bases.assign(s.neq * maxnb, -1); },
+                     [&] { s.T.assign(s.neq * npe * maxnb, 0.0); },
+                     [&] { s.sidx.assign(s.neq * maxnb * maxnb, 0); },
+                     [&] { s.xe.resize(s.neq * npe * dim); if (!s.node_rho.empty()) s.rhoe.resize(s.neq * npe); });
         std::atomic<bool> bad{false};
         parallel_for(s.neq, [&](int64_t i) {
             const int64_t e = s.ip_cell[i];

@@ -68,11 +68,14 @@ def sphere_field(n, seed, nspheres=40, rmin=0.03, rmax=0.12):
     cen = u[:3 * nspheres].reshape(nspheres, 3)
     rad = rmin + (rmax - rmin) * u[3 * nspheres:]
     g = np.arange(n + 1) / n
-    z, y, x = np.meshgrid(g, g, g, indexing="ij")
-    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
-    phi = np.full(len(pts), np.inf)
+    # node (ix, iy, iz) at flat index (iz (n+1) + iy) (n+1) + ix; the squared
+    # distance is separable, summed in the order x^2 + y^2, then + z^2
+    phi = np.full((n + 1) ** 3, np.inf)
     for k in range(nspheres):
-        phi = np.minimum(phi, np.linalg.norm(pts - cen[k], axis=1) - rad[k])
+        dx, dy, dz = g - cen[k, 0], g - cen[k, 1], g - cen[k, 2]
+        d2 = (dx * dx)[None, None, :] + (dy * dy)[None, :, None]
+        d2 = d2 + (dz * dz)[:, None, None]
+        np.minimum(phi, (np.sqrt(d2) - rad[k]).ravel(), out=phi)
     return phi
 
 

@@ -479,6 +479,24 @@ def run_c5(stream, args):
     return out
 
 
+def max_over_ranks(v, world, device="cuda"):
+    """The largest value over the ranks (the job's time is its slowest rank's);
+    device is where the collective's tensor lives (cuda for NCCL, cpu for gloo)."""
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, seconds):
+    """Weak scaling: every rank processes the same units; the job's throughput is
+    all of them over the slowest rank's time."""
+    return units_per_rank * world / seconds
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -606,20 +624,12 @@ def main():
         e2e = {"seconds_per_step": dt, "h2d_bytes_per_step": 8 * nad, "d2h_bytes_per_step": 8 * (nnz + nad)}
 
     # max over ranks
-    def maxr(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    ms = maxr(ms)
-    ms_kernel = maxr(ms_kernel)
-    ms_jv = maxr(ms_jv)
+    ms = max_over_ranks(ms, world)
+    ms_kernel = max_over_ranks(ms_kernel, world)
+    ms_jv = max_over_ranks(ms_jv, world)
     if e2e:
-        e2e["seconds_per_step"] = maxr(e2e["seconds_per_step"])
-    total_el = nc * world
-    value = total_el / (ms * 1e-3)
+        e2e["seconds_per_step"] = max_over_ranks(e2e["seconds_per_step"], world)
+    value = job_throughput(nc, world, ms * 1e-3)
     if rank != 0:
         barrier()
         if world > 1:
@@ -658,7 +668,7 @@ def main():
         "setup_seconds": setup_s,
     }
     if e2e:
-        line["e2e"] = {"value": total_el / e2e["seconds_per_step"], "unit": "elements/s",
+        line["e2e"] = {"value": job_throughput(nc, world, e2e["seconds_per_step"]), "unit": "elements/s",
                        "h2d_bytes_per_step": e2e["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]}
     if clocks:
         line["clocks"] = clocks

@@ -49,7 +49,7 @@
 extern "C" {
 #endif
 
-#define FEM_GPU_ABI_VERSION 2
+#define FEM_GPU_ABI_VERSION 3
 
 typedef enum fem_gpu_status {
     FEM_GPU_OK = 0,
@@ -150,6 +150,10 @@ typedef struct fem_gpu_bulk_set_desc {
        ([ig][nodes]; ids into the table of fem_gpu_set_ig_vertices) -- needed
        for the shape sensitivities only */
     const int32_t* ig_vertex_ids;
+    /* the IWG's (and strain-energy IQI's) "Thickness" property: w* is
+       multiplied by it (FEM/INT/src/IWG/cl_FEM_IWG_Isotropic_Struc_Linear_
+       Bulk.cpp:84-85); 0 = no Thickness property (factor 1) */
+    double thickness;
 } fem_gpu_bulk_set_desc;
 
 /* Side set on interpolation-cell facets (trivial side clusters):
@@ -167,6 +171,15 @@ typedef struct fem_gpu_side_set_desc {
     double poisson_ratio;
     double nitsche_alpha;
     double value[3];
+    /* "Thickness" property of the Neumann and Dirichlet IWGs: w* is
+       multiplied by it (..._Neumann.cpp:66-67, ..._Dirichlet.cpp:103-104);
+       0 = no Thickness property (factor 1) */
+    double thickness;
+    /* Dirichlet IWGs: the "Select" property, a spatial_dim x spatial_dim
+       row-major matrix M that projects the prescribed components (rollers:
+       diag(1,0) clamps x only; ..._Dirichlet.cpp:66-81, 107-116); NULL = the
+       identity.  Copied by fem_gpu_add_side_set.  Neumann sets ignore it. */
+    const double* select_matrix;
 } fem_gpu_side_set_desc;
 
 /* Double-sided set: the Nitsche interface (IWG_Isotropic_Struc_Linear_
@@ -347,9 +360,11 @@ fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_
    arguments as fem_gpu_pcg, but the work vectors live in one fixed-size
    device array of the library (systems up to 131072 rows; larger ones are
    rejected with FEM_GPU_BAD_ARG, nothing allocated).  Calls no cudaMalloc /
-   cudaFree.  The first call on a device resolves the array's device address
-   (make that first call before any stream capture).  All calls share the
-   array: calls that overlap on the GPU race. */
+   cudaFree.  fem_gpu_finalize resolves the array's device address on the
+   current device, which loads the module that holds the array; after
+   fem_gpu_finalize_host alone, the first call on a device does it (make that
+   first call before any stream capture).  All calls share the array: calls
+   that overlap on the GPU race. */
 fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* ctx, const int32_t* rowptr, const int32_t* colidx,
                                    const double* vals, const double* b, double* x, const fem_gpu_pcg_opts* opts,
                                    fem_gpu_pcg_report* report, uint32_t flags);
@@ -533,6 +548,16 @@ int64_t fem_gpu_launch_count(const fem_gpu_ctx* ctx);
    out: dim x num_nodes), the values VIS::Output_Manager::write_field
    (FEM/VIS/src/cl_VIS_Output_Manager.cpp:679-785) writes at the vertices. */
 fem_gpu_status fem_gpu_nodal_field(fem_gpu_ctx* ctx, const double* u_adof, double* out);
+/* Stress sigma = D eps(u) of bulk-set equation objects at IP-parametric points:
+   CM_Struc_Linear::flux (FEM/INT/src/CM/cl_FEM_CM_Struc_Linear.cpp:280-302),
+   as the reference's stress IQIs and field output evaluate it.  Point k is
+   equation object eq[k] at xi[k*dim ...] (host arrays); flux[k*ncomp ...] in
+   the model's Voigt order (3D: xx yy zz yz xz xy; plane strain: xx yy zz xy;
+   plane stress: xx yy xy), *ncomp set.  u_adof and flux are device buffers,
+   or host buffers with FEM_GPU_HOST_BUFFERS.  The Thickness property does not
+   scale the stress. */
+fem_gpu_status fem_gpu_element_flux(fem_gpu_ctx* ctx, int32_t set, int64_t count, const int64_t* eq, const double* xi,
+                                    const double* u_adof, double* flux, int32_t* ncomp, uint32_t flags);
 /* Exodus II file of one element block and nodal fields at one time step (the
    reference writes through mtk::Writer_Exodus, MTK/src/io/cl_MTK_Writer_Exodus.
    cpp:112-420, and the SEACAS library; here the netCDF classic 64-bit-offset

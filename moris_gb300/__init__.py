@@ -51,6 +51,18 @@ def _dev_ptr(t):
     return C.c_void_p(t.data_ptr())
 
 
+_default_stream = None
+
+
+def set_default_stream(fn):
+    """Stream for models created from now on: fn() returns a cudaStream_t as an
+    int (torch: ``lambda: torch.cuda.current_stream().cuda_stream``), or fn is
+    None for the library's own stream.  A model whose inputs come from another
+    stream's kernels must run on that stream (or the caller synchronises)."""
+    global _default_stream
+    _default_stream = fn
+
+
 def lib():
     return _lib.load()
 
@@ -135,6 +147,8 @@ class FemModel:
         self.h = h
         self.num_sets = 0
         self.num_nodes = len(coords) // dim
+        if _default_stream is not None:
+            self.set_stream(_default_stream())
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -153,7 +167,7 @@ class FemModel:
         self._check(self.L.fem_gpu_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
 
     def add_bulk_set(self, ip_cells, youngs, poisson, rule, model, ig_cell=None, ig_offsets=None, ig_coords=None,
-                     ig_param=None, node_density=None, density_exponent=3.0, ig_vertex_ids=None):
+                     ig_param=None, node_density=None, density_exponent=3.0, ig_vertex_ids=None, thickness=0.0):
         ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)
         rho = None if node_density is None else np.ascontiguousarray(node_density, dtype=np.float64)
         E = np.ascontiguousarray(youngs, dtype=np.float64)
@@ -164,18 +178,24 @@ class FemModel:
             ig_cell = CELL_QUAD4 if self.dim == 2 else CELL_HEX8
         vid = None if ig_vertex_ids is None else np.ascontiguousarray(ig_vertex_ids, dtype=np.int32)
         d = BulkSetDesc(IWG_STRUC_LINEAR_BULK, ig_cell, rule, model, len(ipc), _np_ptr(ipc), _np_ptr(off),
-                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson, _np_ptr(rho), density_exponent, _np_ptr(vid))
+                        _np_ptr(xc), _np_ptr(xp), _np_ptr(E), poisson, _np_ptr(rho), density_exponent, _np_ptr(vid),
+                        thickness)
         idx = C.c_int32()
         self._check(self.L.fem_gpu_add_bulk_set(self.h, C.byref(d), C.byref(idx)), "add_bulk_set")
         self.num_sets += 1
         return idx.value
 
-    def add_side_set(self, iwg, ip_cells, ordinals, youngs, poisson, rule, model, alpha=0.0, value=(0, 0, 0)):
+    def add_side_set(self, iwg, ip_cells, ordinals, youngs, poisson, rule, model, alpha=0.0, value=(0, 0, 0),
+                     thickness=0.0, select=None):
+        """thickness: the IWG's Thickness property (0 = none); select: the
+        Dirichlet IWG's Select matrix (dim x dim, None = identity)"""
         ipc = np.ascontiguousarray(ip_cells, dtype=np.int32)
         ords = np.ascontiguousarray(ordinals, dtype=np.int32)
         E = np.ascontiguousarray(youngs, dtype=np.float64)
         v = (C.c_double * 3)(*(list(value) + [0.0] * (3 - len(value))))
-        d = SideSetDesc(iwg, rule, model, 0, len(ipc), _np_ptr(ipc), _np_ptr(ords), _np_ptr(E), poisson, alpha, v)
+        sel = None if select is None else np.ascontiguousarray(select, dtype=np.float64).reshape(self.dim, self.dim)
+        d = SideSetDesc(iwg, rule, model, 0, len(ipc), _np_ptr(ipc), _np_ptr(ords), _np_ptr(E), poisson, alpha, v,
+                        thickness, _np_ptr(sel))
         idx = C.c_int32()
         self._check(self.L.fem_gpu_add_side_set(self.h, C.byref(d), C.byref(idx)), "add_side_set")
         self.num_sets += 1
@@ -329,6 +349,26 @@ class FemModel:
         self._check(st, "pcg_noalloc")
         return dict(iterations=r.iterations, converged=bool(r.converged), rel_residual=r.rel_residual,
                     seconds=r.seconds)
+
+    def element_flux(self, s, eq, xi, u):
+        """Voigt stress of bulk set s at IP-parametric points: eq (n,) equation
+        objects, xi (n, dim), u a CUDA tensor of adof values; returns (n, ncomp)"""
+        eqa = np.ascontiguousarray(eq, dtype=np.int64)
+        xia = np.ascontiguousarray(xi, dtype=np.float64).reshape(len(eqa), self.dim)
+        out = np.zeros(len(eqa) * 6)
+        nc = C.c_int32()
+        uu = _dev_ptr(u) if not isinstance(u, np.ndarray) else _np_ptr(np.ascontiguousarray(u, dtype=np.float64))
+        flags = HOST_BUFFERS
+        if not isinstance(u, np.ndarray):
+            # u on the device, the result staged back through a host array
+            import torch
+            o = torch.empty(len(eqa) * 6, dtype=torch.float64, device=u.device)
+            self._check(self.L.fem_gpu_element_flux(self.h, s, len(eqa), _np_ptr(eqa), _np_ptr(xia), uu, _dev_ptr(o),
+                                                    C.byref(nc), 0), "element_flux")
+            return o[:len(eqa) * nc.value].cpu().numpy().reshape(len(eqa), nc.value)
+        self._check(self.L.fem_gpu_element_flux(self.h, s, len(eqa), _np_ptr(eqa), _np_ptr(xia), uu, _np_ptr(out),
+                                                C.byref(nc), flags), "element_flux")
+        return out[:len(eqa) * nc.value].reshape(len(eqa), nc.value)
 
     def autotune(self, max_elements=0):
         self._check(self.L.fem_gpu_autotune(self.h, max_elements), "autotune")

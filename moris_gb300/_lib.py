@@ -10,6 +10,9 @@ import os
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libfem_gpu.so")
 
+# the structures below follow include/fem_gpu.h of this ABI version
+ABI_VERSION = 3
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -27,13 +30,14 @@ class BulkSetDesc(C.Structure):
     _fields_ = [("iwg_type", I32), ("ig_cell_type", I32), ("integration_rule", I32), ("model_type", I32),
                 ("num_clusters", I64), ("cluster_ip_cell", P), ("ig_offsets", P), ("ig_coords", P),
                 ("ig_param_coords", P), ("youngs_modulus", P), ("poisson_ratio", D), ("node_density", P),
-                ("density_exponent", D), ("ig_vertex_ids", P)]
+                ("density_exponent", D), ("ig_vertex_ids", P), ("thickness", D)]
 
 
 class SideSetDesc(C.Structure):
     _fields_ = [("iwg_type", I32), ("integration_rule", I32), ("model_type", I32), ("reserved", I32),
                 ("num_sides", I64), ("side_ip_cell", P), ("side_ordinal", P), ("youngs_modulus", P),
-                ("poisson_ratio", D), ("nitsche_alpha", D), ("value", D * 3)]
+                ("poisson_ratio", D), ("nitsche_alpha", D), ("value", D * 3), ("thickness", D),
+                ("select_matrix", P)]
 
 
 class DoubleSideSetDesc(C.Structure):
@@ -146,6 +150,7 @@ SIGNATURES = {
     "fem_gpu_launch_count": (I64, [P]),
     "fem_gpu_last_error": (C.c_char_p, [P]),
     "fem_gpu_nodal_field": (I32, [P, P, P]),
+    "fem_gpu_element_flux": (I32, [P, I32, I64, P, P, P, P, P, U32]),
     "fem_vis_write_exodus": (I32, [C.c_char_p, I32, I64, P, I64, I32, P, C.c_char_p, I32, P, P, D]),
 }
 
@@ -162,5 +167,8 @@ def load():
             f = getattr(lib, name)
             f.restype = res
             f.argtypes = args
+        if lib.fem_gpu_abi_version() != ABI_VERSION:
+            raise RuntimeError("libfem_gpu.so has ABI version %d, these bindings expect %d; rebuild it"
+                               % (lib.fem_gpu_abi_version(), ABI_VERSION))
         _lib = lib
     return _lib

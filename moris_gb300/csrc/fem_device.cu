@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -437,10 +438,19 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
 
 // ---------------------------------------------------------------------------
 // side sets (Neumann traction, Nitsche Dirichlet) on interpolation-cell
-// facets: one thread per facet (these sets are small: the boundary of the
-// mesh).  Element_Sideset (FEM/INT/src/ELEM/cl_FEM_Element_Sideset.cpp:
-// 261-330), IWG_Isotropic_Struc_Linear_Neumann (:38) and _Dirichlet (:52-240),
+// facets: Element_Sideset (FEM/INT/src/ELEM/cl_FEM_Element_Sideset.cpp:
+// 261-330), IWG_Isotropic_Struc_Linear_Neumann (:38-80) and _Dirichlet
+// (:52-240) with their Thickness (w* times thickness) and Select (a dim x dim
+// projection M of the prescribed components) properties,
 // SP_Dirichlet_Nitsche (gamma = alpha E / h).
+//
+// One CTA per facet (grid-stride over the facets).  Everything of a facet
+// lives in shared memory: the IP-cell coordinates and extraction T, the
+// pdof values, per Gauss point N, dN/dx, w*, the traction operator
+// nDB[f][(g,b)] = lam n_f g_gb + mu (n_g g_fb + delta_fg n.g_b) and its
+// projections, the pdof K and R, and K T.  Threads own Gauss points for the
+// geometry, then pdof entries for K and R, then (entry, column) pairs of
+// K T and T^T (K T), whose results are scattered into the CSR.
 struct SideArgs {
     int64_t ns;
     int iwg, model, ngp, maxnb;
@@ -458,6 +468,8 @@ struct SideArgs {
     int64_t nu;
     double nu_p, alpha;
     double value[3];
+    double thickness;   // w* factor
+    double select[9];   // M, row-major 3 x 3 (the leading dim x dim block is used)
     const double* u;
     double* vals;
     double* rhs;
@@ -469,198 +481,291 @@ struct SideArgs {
     int* status;
 };
 
-template <int D>
-__global__ void side_kernel(SideArgs p) {
-    constexpr int NPE = D == 2 ? 4 : 8, NPD = D * NPE, NS = D == 2 ? 4 : 6;
-    constexpr int NFV = D == 2 ? 2 : 4;
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= p.ns) return;
-    const int nb = p.nb[s];
-    const int ord = p.ord[s];
-    const int quad_f[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
-    const int hex_f[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
-    double X[NPE * D], XI[NPE * D];
-    for (int i = 0; i < NPE * D; ++i) X[i] = p.xe[s * NPE * D + i];
-    for (int a = 0; a < NPE; ++a) {
-        XI[a * D + 0] = ((a & 3) == 1 || (a & 3) == 2) ? 1.0 : -1.0;
-        XI[a * D + 1] = ((a & 3) >= 2) ? 1.0 : -1.0;
-        if (D == 3) XI[a * D + 2] = a >= 4 ? 1.0 : -1.0;
+// shared-memory layout of one facet, in doubles (the basis ids follow as ints)
+struct SideSmem {
+    int X, T, U, R, K, KT, QN, QG, QW, QM, QNRM, QB, QMB, QMTB, QT, QJ, misc, total;
+    __host__ __device__ SideSmem(int D, int maxnb, int ngp) {
+        const int NPE = D == 2 ? 4 : 8, NPD = D * NPE;
+        int o = 0;
+        X = o; o += NPE * D;
+        T = o; o += NPE * maxnb;
+        U = o; o += NPD;
+        R = o; o += NPD;
+        K = o; o += NPD * NPD;
+        KT = o; o += NPD * D * maxnb;
+        QN = o; o += ngp * NPE;
+        QG = o; o += ngp * D * NPE;
+        QW = o; o += ngp;
+        QM = o; o += ngp;
+        QNRM = o; o += ngp * 3;
+        QB = o; o += ngp * D * NPD;
+        QMB = o; o += ngp * D * NPD;
+        QMTB = o; o += ngp * D * NPD;
+        QT = o; o += ngp * D;
+        QJ = o; o += ngp * D;
+        misc = o; o += 4;
+        total = o;
     }
-    int fv[NFV];
-    for (int k = 0; k < NFV; ++k) fv[k] = D == 2 ? quad_f[ord][k] : hex_f[ord][k];
-    const double E = p.E[s];
-    double lam_c, mu_c = 1.0 / (2.0 * (1.0 + p.nu_p));
-    if (p.model == FEM_GPU_MODEL_PLANE_STRESS) lam_c = p.nu_p / (1.0 - p.nu_p * p.nu_p);
-    else lam_c = p.nu_p / ((1.0 + p.nu_p) * (1.0 - 2.0 * p.nu_p));
-    const double lam = E * lam_c, mu = E * mu_c;
-    // pdof values
-    double U[NPD];
-    for (int f = 0; f < D; ++f)
-        for (int a = 0; a < NPE; ++a) {
+    static size_t bytes(int D, int maxnb, int ngp) {
+        return SideSmem(D, maxnb, ngp).total * sizeof(double) + (size_t)maxnb * sizeof(int32_t);
+    }
+};
+
+template <int D>
+__global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
+    constexpr int NPE = D == 2 ? 4 : 8, NPD = D * NPE, NFV = D == 2 ? 2 : 4;
+    extern __shared__ double sm[];
+    const int maxnb = p.maxnb, ngp = p.ngp, tid = threadIdx.x, NT = blockDim.x;
+    const SideSmem L(D, maxnb, ngp);
+    double* X = sm + L.X;
+    double* T = sm + L.T;
+    double* U = sm + L.U;
+    double* R = sm + L.R;
+    double* K = sm + L.K;
+    double* KT = sm + L.KT;
+    double* QN = sm + L.QN;
+    double* QG = sm + L.QG;
+    double* QW = sm + L.QW;
+    double* QM = sm + L.QM;
+    double* QNRM = sm + L.QNRM;
+    double* QB = sm + L.QB;
+    double* QMB = sm + L.QMB;
+    double* QMTB = sm + L.QMTB;
+    double* QT = sm + L.QT;
+    double* QJ = sm + L.QJ;
+    double* misc = sm + L.misc;
+    int32_t* bs = reinterpret_cast<int32_t*>(sm + L.total);
+    const bool neumann = p.iwg == FEM_GPU_IWG_STRUC_LINEAR_NEUMANN;
+    const double beta = p.iwg == FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
+    const double mu_c = 1.0 / (2.0 * (1.0 + p.nu_p));
+    const double lam_c = p.model == FEM_GPU_MODEL_PLANE_STRESS ? p.nu_p / (1.0 - p.nu_p * p.nu_p)
+                                                               : p.nu_p / ((1.0 + p.nu_p) * (1.0 - 2.0 * p.nu_p));
+    // a zero projection adds nothing (the reference skips the IWG)
+    double mnorm = 0.0;
+    for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j) mnorm = fma(p.select[i * 3 + j], p.select[i * 3 + j], mnorm);
+    const bool active = neumann || sqrt(mnorm) >= 2.220446049250313e-16;
+    for (int64_t s = blockIdx.x; s < p.ns; s += gridDim.x) {
+        const int nb = p.nb[s];
+        const int ord = p.ord[s];
+        const double E = p.E[s];
+        const double lam = E * lam_c, mu = E * mu_c;
+        // ---- stage the facet's cell ------------------------------------------------
+        for (int i = tid; i < NPE * D; i += NT) X[i] = p.xe[s * NPE * D + i];
+        for (int i = tid; i < NPE * maxnb; i += NT) T[i] = p.T[s * NPE * maxnb + i];
+        for (int j = tid; j < maxnb; j += NT) bs[j] = p.bases[s * maxnb + j];
+        __syncthreads();
+        // ---- pdof values; per-point geometry -----------------------------------------
+        for (int r = tid; r < NPD; r += NT) {
+            const int f = r / NPE, a = r - f * NPE;
             double v = 0.0;
             if (p.u)
                 for (int j = 0; j < nb; ++j) {
-                    const double t = p.T[(s * NPE + a) * p.maxnb + j];
-                    if (fem_nonzero(t)) v = fma(t, p.u[f * p.nu + p.bases[s * p.maxnb + j]], v);
+                    const double t = T[a * maxnb + j];
+                    if (fem_nonzero(t)) v = fma(t, p.u[f * p.nu + bs[j]], v);
                 }
-            U[f * NPE + a] = v;
+            U[r] = v;
+            R[r] = 0.0;
         }
-    double K[NPD * NPD], R[NPD];
-    for (int i = 0; i < NPD * NPD; ++i) K[i] = 0.0;
-    for (int i = 0; i < NPD; ++i) R[i] = 0.0;
-    // facet geometry per Gauss point
-    auto facet = [&](int q, double* xip, double& detJ, double* nrm) {
-        double Nf[4], dNf[8];
-        const double* xq = p.gp + q * (D - 1);
-        if (D == 2) Shape<4>::eval(xq, Nf, dNf);
-        else Shape<0>::eval(xq, Nf, dNf);
-        double t[2][3] = {{0, 0, 0}, {0, 0, 0}};
-        for (int d = 0; d < D; ++d) xip[d] = 0.0;
-        for (int k = 0; k < NFV; ++k) {
-            for (int d = 0; d < D; ++d) {
-                xip[d] = fma(Nf[k], XI[fv[k] * D + d], xip[d]);
-                for (int m = 0; m < D - 1; ++m) t[m][d] = fma(dNf[m * NFV + k], X[fv[k] * D + d], t[m][d]);
-            }
-        }
-        if (D == 2) {
-            detJ = sqrt(t[0][0] * t[0][0] + t[0][1] * t[0][1]);
-            nrm[0] = t[0][1] / detJ;
-            nrm[1] = -t[0][0] / detJ;
-        } else {
-            const double c0 = t[0][1] * t[1][2] - t[0][2] * t[1][1];
-            const double c1 = t[0][2] * t[1][0] - t[0][0] * t[1][2];
-            const double c2 = t[0][0] * t[1][1] - t[0][1] * t[1][0];
-            detJ = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
-            nrm[0] = c0 / detJ;
-            nrm[1] = c1 / detJ;
-            nrm[2] = c2 / detJ;
-        }
-    };
-    double meas = 0.0;
-    for (int q = 0; q < p.ngp; ++q) {
-        double xip[3], dj, nrm[3];
-        facet(q, xip, dj, nrm);
-        meas += p.gw[q] * dj;
-    }
-    const double h = D == 2 ? meas : sqrt(4.0 * meas / 3.14159265358979323846);
-    const double gamma = p.alpha * E / h;
-    const double beta = p.iwg == FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
-    for (int q = 0; q < p.ngp; ++q) {
-        double xip[3], detJ, nrm[3] = {0, 0, 0};
-        facet(q, xip, detJ, nrm);
-        if (detJ < -1.0e-6) continue;
-        const double ws = p.gw[q] * detJ;
-        double N[NPE], dN[NPE * D];
-        if (D == 2) Shape<0>::eval(xip, N, dN);
-        else Shape<1>::eval(xip, N, dN);
-        if (p.iwg == FEM_GPU_IWG_STRUC_LINEAR_NEUMANN) {
-            for (int f = 0; f < D; ++f)
-                for (int a = 0; a < NPE; ++a) R[f * NPE + a] -= ws * N[a] * p.value[f];
-            continue;
-        }
-        // dN/dx through the interpolation-cell Jacobian (rectangular or general)
-        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-        for (int i = 0; i < D; ++i)
-            for (int j = 0; j < D; ++j)
-                for (int a = 0; a < NPE; ++a) J[i][j] = fma(dN[i * NPE + a], X[a * D + j], J[i][j]);
-        if (D == 2) {
-            const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0], id = 1.0 / det;
-            Ji[0][0] = J[1][1] * id; Ji[0][1] = -J[0][1] * id; Ji[1][0] = -J[1][0] * id; Ji[1][1] = J[0][0] * id;
-        } else {
-            const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
-                               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-            const double id = 1.0 / det;
-            Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
-            Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-            Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-            Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
-            Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-            Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
-            Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
-            Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
-            Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
-        }
-        double g[D][NPE];
-        for (int i = 0; i < D; ++i)
-            for (int a = 0; a < NPE; ++a) {
-                double v = 0.0;
-                for (int k = 0; k < D; ++k) v = fma(Ji[i][k], dN[k * NPE + a], v);
-                g[i][a] = v;
-            }
-        // traction operator (nDB)[f][(g,b)] = lam n_f g_gb + mu (n_g g_fb + delta_fg n.g_b)
-        double nDB[D][NPD];
-        for (int f = 0; f < D; ++f)
-            for (int gg = 0; gg < D; ++gg)
-                for (int b = 0; b < NPE; ++b) {
-                    double ng = 0.0;
-                    for (int k = 0; k < D; ++k) ng += nrm[k] * g[k][b];
-                    nDB[f][gg * NPE + b] = lam * nrm[f] * g[gg][b] + mu * (nrm[gg] * g[f][b] + (f == gg ? ng : 0.0));
+        for (int q = tid; q < ngp; q += NT) {
+            const int quad_f[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+            const int hex_f[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+            double Nf[4], dNf[8];
+            const double* xq = p.gp + q * (D - 1);
+            if (D == 2) Shape<4>::eval(xq, Nf, dNf);
+            else Shape<0>::eval(xq, Nf, dNf);
+            double t[2][3] = {{0, 0, 0}, {0, 0, 0}}, xip[3] = {0, 0, 0};
+            for (int k = 0; k < NFV; ++k) {
+                const int v = D == 2 ? quad_f[ord][k] : hex_f[ord][k];
+                const double xiv[3] = {((v & 3) == 1 || (v & 3) == 2) ? 1.0 : -1.0, ((v & 3) >= 2) ? 1.0 : -1.0,
+                                       v >= 4 ? 1.0 : -1.0};
+                for (int d = 0; d < D; ++d) {
+                    xip[d] = fma(Nf[k], xiv[d], xip[d]);
+                    for (int m = 0; m < D - 1; ++m) t[m][d] = fma(dNf[m * NFV + k], X[v * D + d], t[m][d]);
                 }
-        double trac[D], jump[D];
-        for (int f = 0; f < D; ++f) {
-            double t = 0.0, uu = 0.0;
-            for (int c = 0; c < NPD; ++c) t = fma(nDB[f][c], U[c], t);
-            for (int a = 0; a < NPE; ++a) uu = fma(N[a], U[f * NPE + a], uu);
-            trac[f] = t;
-            jump[f] = uu - p.value[f];
-        }
-        for (int f = 0; f < D; ++f)
-            for (int a = 0; a < NPE; ++a) {
-                const int r = f * NPE + a;
-                double v = -N[a] * trac[f] + gamma * N[a] * jump[f];
-                for (int k = 0; k < D; ++k) v += beta * nDB[k][r] * jump[k];
-                R[r] += ws * v;
             }
-        for (int r = 0; r < NPD; ++r) {
-            const int f = r / NPE, a = r % NPE;
-            for (int c = 0; c < NPD; ++c) {
-                const int gg = c / NPE, b = c % NPE;
-                double v = beta * nDB[gg][r] * N[b] - N[a] * nDB[f][c];
-                if (f == gg) v += gamma * N[a] * N[b];
-                K[r * NPD + c] += ws * v;
+            double detJ, nrm[3] = {0, 0, 0};
+            if (D == 2) {
+                detJ = sqrt(t[0][0] * t[0][0] + t[0][1] * t[0][1]);
+                nrm[0] = t[0][1] / detJ;
+                nrm[1] = -t[0][0] / detJ;
+            } else {
+                const double c0 = t[0][1] * t[1][2] - t[0][2] * t[1][1];
+                const double c1 = t[0][2] * t[1][0] - t[0][0] * t[1][2];
+                const double c2 = t[0][0] * t[1][1] - t[0][1] * t[1][0];
+                detJ = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+                nrm[0] = c0 / detJ;
+                nrm[1] = c1 / detJ;
+                nrm[2] = c2 / detJ;
             }
+            QM[q] = p.gw[q] * detJ;
+            // Gauss points with detJ < -1e-6 are skipped (weight 0)
+            QW[q] = detJ < -1.0e-6 ? 0.0 : p.gw[q] * detJ * p.thickness;
+            for (int d = 0; d < 3; ++d) QNRM[q * 3 + d] = nrm[d];
+            double N[NPE], dN[NPE * D];
+            if (D == 2) Shape<0>::eval(xip, N, dN);
+            else Shape<1>::eval(xip, N, dN);
+            for (int a = 0; a < NPE; ++a) QN[q * NPE + a] = N[a];
+            // dN/dx through the interpolation-cell Jacobian (rectangular or general)
+            double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+            for (int i = 0; i < D; ++i)
+                for (int j = 0; j < D; ++j)
+                    for (int a = 0; a < NPE; ++a) J[i][j] = fma(dN[i * NPE + a], X[a * D + j], J[i][j]);
+            if (D == 2) {
+                const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0], id = 1.0 / det;
+                Ji[0][0] = J[1][1] * id; Ji[0][1] = -J[0][1] * id; Ji[1][0] = -J[1][0] * id; Ji[1][1] = J[0][0] * id;
+            } else {
+                const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                                   J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+                const double id = 1.0 / det;
+                Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
+                Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+                Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+                Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+                Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+                Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
+                Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+                Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
+                Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+            }
+            for (int i = 0; i < D; ++i)
+                for (int a = 0; a < NPE; ++a) {
+                    double v = 0.0;
+                    for (int k = 0; k < D; ++k) v = fma(Ji[i][k], dN[k * NPE + a], v);
+                    QG[(q * D + i) * NPE + a] = v;
+                }
         }
-    }
-    (void)NS;
-    // extraction and scatter
-    const int maxnb = p.maxnb;
-    const int32_t* bs = p.bases + s * maxnb;
-    const double* Ts = p.T + s * NPE * maxnb;
-    for (int f = 0; f < D; ++f)
-        for (int i = 0; i < nb; ++i) {
+        __syncthreads();
+        if (tid == 0) {
+            double meas = 0.0;
+            for (int q = 0; q < ngp; ++q) meas += QM[q];
+            const double h = D == 2 ? meas : sqrt(4.0 * meas / 3.14159265358979323846);
+            misc[0] = p.alpha * E / h;
+        }
+        // ---- traction operator per point -------------------------------------------
+        if (!neumann)
+            for (int k = tid; k < ngp * D * NPD; k += NT) {
+                const int q = k / (D * NPD), rem = k - q * D * NPD, f = rem / NPD, c = rem - f * NPD;
+                const int gg = c / NPE, b = c - gg * NPE;
+                const double* nrm = QNRM + q * 3;
+                const double* g = QG + q * D * NPE;
+                double ng = 0.0;
+                for (int kk = 0; kk < D; ++kk) ng += nrm[kk] * g[kk * NPE + b];
+                QB[k] = lam * nrm[f] * g[gg * NPE + b] + mu * (nrm[gg] * g[f * NPE + b] + (f == gg ? ng : 0.0));
+            }
+        __syncthreads();
+        // projections M nDB and M^T nDB
+        if (!neumann)
+            for (int k = tid; k < ngp * D * NPD; k += NT) {
+                const int q = k / (D * NPD), rem = k - q * D * NPD, f = rem / NPD, c = rem - f * NPD;
+                const double* B = QB + q * D * NPD;
+                double mb = 0.0, mtb = 0.0;
+                for (int kk = 0; kk < D; ++kk) {
+                    mb = fma(p.select[f * 3 + kk], B[kk * NPD + c], mb);
+                    mtb = fma(p.select[kk * 3 + f], B[kk * NPD + c], mtb);
+                }
+                QMB[k] = mb;
+                QMTB[k] = mtb;
+            }
+        // traction and jump per point, projected: M t(u), M (u - g)
+        if (!neumann)
+            for (int q = tid; q < ngp; q += NT) {
+                double trac[3] = {0, 0, 0}, jump[3] = {0, 0, 0};
+                for (int f = 0; f < D; ++f) {
+                    double tt = 0.0, uu = 0.0;
+                    for (int c = 0; c < NPD; ++c) tt = fma(QB[(q * D + f) * NPD + c], U[c], tt);
+                    for (int a = 0; a < NPE; ++a) uu = fma(QN[q * NPE + a], U[f * NPE + a], uu);
+                    trac[f] = tt;
+                    jump[f] = uu - p.value[f];
+                }
+                for (int f = 0; f < D; ++f) {
+                    double mt = 0.0, mj = 0.0;
+                    for (int kk = 0; kk < D; ++kk) {
+                        mt = fma(p.select[f * 3 + kk], trac[kk], mt);
+                        mj = fma(p.select[f * 3 + kk], jump[kk], mj);
+                    }
+                    QT[q * D + f] = mt;
+                    QJ[q * D + f] = mj;
+                }
+            }
+        __syncthreads();
+        // ---- pdof residual and Jacobian --------------------------------------------
+        const double gamma = misc[0];
+        for (int r = tid; r < NPD; r += NT) {
+            const int f = r / NPE, a = r - f * NPE;
+            double v = 0.0;
+            for (int q = 0; q < ngp; ++q) {
+                const double na = QN[q * NPE + a];
+                double t;
+                if (neumann) {
+                    t = -na * p.value[f];
+                } else {
+                    t = na * (gamma * QJ[q * D + f] - QT[q * D + f]);
+                    for (int kk = 0; kk < D; ++kk) t = fma(beta * QB[(q * D + kk) * NPD + r], QJ[q * D + kk], t);
+                }
+                v = fma(QW[q], t, v);
+            }
+            R[r] = active ? v : 0.0;
+        }
+        for (int k = tid; k < NPD * NPD; k += NT) {
+            const int r = k / NPD, c = k - r * NPD;
+            const int f = r / NPE, a = r - f * NPE, gg = c / NPE, b = c - gg * NPE;
+            double v = 0.0;
+            if (!neumann && active)
+                for (int q = 0; q < ngp; ++q) {
+                    const double na = QN[q * NPE + a], nb_ = QN[q * NPE + b];
+                    double t = beta * QMTB[(q * D + gg) * NPD + r] * nb_ - na * QMB[(q * D + f) * NPD + c];
+                    t = fma(gamma * na * p.select[f * 3 + gg], nb_, t);
+                    v = fma(QW[q], t, v);
+                }
+            K[k] = v;
+        }
+        __syncthreads();
+        // ---- extraction: R_a = T^T R, K T, then T^T (K T) and the scatter -----------
+        for (int k = tid; k < D * nb; k += NT) {
+            const int f = k / nb, i = k - f * nb;
             double ra = 0.0;
-            for (int a = 0; a < NPE; ++a) ra = fma(Ts[a * maxnb + i], R[f * NPE + a], ra);
+            for (int a = 0; a < NPE; ++a) ra = fma(T[a * maxnb + i], R[f * NPE + a], ra);
             if (p.mode == MODE_ASSEMBLE) {
                 if (p.rhs) atomicAdd(p.rhs + f * p.nu + bs[i], ra);
             } else if (p.Rout) {
                 p.Rout[(s - p.first) * p.nmax + f * maxnb + i] = ra;
             }
         }
-    if ((p.mode == MODE_ASSEMBLE && !p.vals) || (p.mode == MODE_ELEMENT && !p.Kout)) return;
-    bool bad = false;
-    for (int f = 0; f < D; ++f)
-        for (int i = 0; i < nb; ++i) {
-            const int32_t rbase = p.rowptr[f * p.nu + bs[i]];
-            const int32_t ul = p.ulen[bs[i]];
-            for (int gg = 0; gg < D; ++gg)
-                for (int j = 0; j < nb; ++j) {
-                    double v = 0.0;
-                    for (int a = 0; a < NPE; ++a) {
-                        const double ta = Ts[a * maxnb + i];
-                        if (ta == 0.0) continue;
-                        double kt = 0.0;
-                        for (int b = 0; b < NPE; ++b) kt = fma(K[(f * NPE + a) * NPD + gg * NPE + b], Ts[b * maxnb + j], kt);
-                        v = fma(ta, kt, v);
-                    }
-                    bad |= !fem_finite(v);
-                    if (p.mode == MODE_ASSEMBLE)
-                        atomicAdd(p.vals + rbase + gg * ul + p.sidx[(s * maxnb + i) * maxnb + j], v);
-                    else
-                        p.Kout[(s - p.first) * (int64_t)p.nmax * p.nmax + (f * maxnb + i) + (int64_t)(gg * maxnb + j) * p.nmax] = v;
+        const bool want_k = !((p.mode == MODE_ASSEMBLE && !p.vals) || (p.mode == MODE_ELEMENT && !p.Kout));
+        const int nc = D * nb;
+        if (want_k)
+            for (int k = tid; k < NPD * nc; k += NT) {
+                const int r = k / nc, c = k - r * nc, gg = c / nb, j = c - gg * nb;
+                double v = 0.0;
+                for (int b = 0; b < NPE; ++b) v = fma(K[r * NPD + gg * NPE + b], T[b * maxnb + j], v);
+                KT[r * nc + c] = v;
+            }
+        __syncthreads();
+        if (want_k) {
+            bool bad = false;
+            for (int k = tid; k < nc * nc; k += NT) {
+                const int rr = k / nc, c = k - rr * nc;
+                const int f = rr / nb, i = rr - f * nb, gg = c / nb, j = c - gg * nb;
+                double v = 0.0;
+                for (int a = 0; a < NPE; ++a) {
+                    const double ta = T[a * maxnb + i];
+                    if (fem_nonzero(ta)) v = fma(ta, KT[(f * NPE + a) * nc + c], v);
                 }
+                bad |= !fem_finite(v);
+                if (p.mode == MODE_ASSEMBLE) {
+                    const int32_t rbase = p.rowptr[f * p.nu + bs[i]];
+                    const int32_t ul = p.ulen[bs[i]];
+                    atomicAdd(p.vals + rbase + gg * ul + p.sidx[(s * maxnb + i) * maxnb + j], v);
+                } else {
+                    p.Kout[(s - p.first) * (int64_t)p.nmax * p.nmax + (f * maxnb + i) + (int64_t)(gg * maxnb + j) * p.nmax] = v;
+                }
+            }
+            if (bad) atomicOr(p.status, 1);
         }
-    if (bad) atomicOr(p.status, 1);
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -816,12 +921,6 @@ double lam_coef(int model, double nu) {
     return model == FEM_GPU_MODEL_PLANE_STRESS ? nu / (1.0 - nu * nu) : nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
 }
 
-int sm_count() {
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 1;
-}
 
 fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int64_t count, const double* u,
                            double* vals, double* rhs, double* Kout, double* Rout, int nmax, const double* x,
@@ -931,6 +1030,8 @@ fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.nu_p = s.side.poisson_ratio;
     a.alpha = s.side.nitsche_alpha;
     for (int d = 0; d < 3; ++d) a.value[d] = s.side.value[d];
+    a.thickness = s.side_thickness;
+    for (int k = 0; k < 9; ++k) a.select[k] = s.side_select[k];
     a.u = u;
     a.vals = vals;
     a.rhs = rhs;
@@ -940,10 +1041,16 @@ fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.first = 0;
     a.mode = mode;
     a.status = status_ptr(c);
-    const int threads = 64;
-    const unsigned blocks = (unsigned)((count + threads - 1) / threads);
-    if (D == 2) side_kernel<2><<<blocks, threads, 0, stream_of(c)>>>(a);
-    else side_kernel<3><<<blocks, threads, 0, stream_of(c)>>>(a);
+    const size_t smem = SideSmem::bytes(D, s.maxnb, ds.ngp);
+    const void* fn = D == 2 ? (const void*)side_cta_kernel<2> : (const void*)side_cta_kernel<3>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_fail(c, e, "side kernel shared memory");
+    }
+    const int threads = 128;
+    const unsigned blocks = (unsigned)std::min<int64_t>(count, (int64_t)sm_count() * 8);
+    if (D == 2) side_cta_kernel<2><<<blocks, threads, smem, stream_of(c)>>>(a);
+    else side_cta_kernel<3><<<blocks, threads, smem, stream_of(c)>>>(a);
     c->launches++;
     return check_kernel(c, "side launch");
 }
@@ -951,6 +1058,26 @@ fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
 }  // namespace
 
 namespace fem {
+
+int sm_count() {
+    // multiprocessor count of the current device, read once per device
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev < 64) {
+        const int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    n = n > 0 ? n : 1;
+    if (dev < 64) cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
 
 fem_gpu_status assemble_set(fem_gpu_ctx* c, int set, const double* u, double* vals, double* rhs) {
     SetData& s = c->sets[set];
@@ -1234,7 +1361,12 @@ fem_gpu_status fem_gpu_finalize(fem_gpu_ctx* c) {
     fem_gpu_status st = fem_gpu_finalize_host(c);
     if (st != FEM_GPU_OK) return st;
     if (c->dev_final) return FEM_GPU_OK;
-    return device_finalize(c);
+    st = device_finalize(c);
+    if (st != FEM_GPU_OK) return st;
+    // resolve the allocation-free solver's array on this device now, so that
+    // loading its module (which reserves the array) happens here and not
+    // inside a later fem_gpu_pcg_noalloc call
+    return noalloc_prepare(c);
 }
 
 fem_gpu_status fem_gpu_build_graph(fem_gpu_ctx* c, int32_t* rowptr, int32_t* colidx, uint32_t flags) {
@@ -1411,7 +1543,7 @@ fem_gpu_status fem_gpu_nodal_field(fem_gpu_ctx* c, const double* u, double* out)
     if (e == cudaSuccess && nz) e = cudaMemcpyAsync(dw, c->t_w.data(), nz * sizeof(double), cudaMemcpyHostToDevice, sm);
     if (e == cudaSuccess) {
         const int64_t n = nn * c->dim;
-        fem_nodal::nodal_field_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16), 256, 0, sm>>>(
+        fem_nodal::nodal_field_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 16), 256, 0, sm>>>(
             nn, c->dim, c->num_used, doff, drk, dw, u, out);
         ++c->launches;
         e = cudaGetLastError();
@@ -1421,6 +1553,157 @@ fem_gpu_status fem_gpu_nodal_field(fem_gpu_ctx* c, const double* u, double* out)
     cudaFreeAsync(dw, sm);
     if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
     return e == cudaSuccess ? FEM_GPU_OK : cuda_fail(c, e, "nodal field");
+}
+
+}  // extern "C"
+
+namespace fem_flux {
+
+// stress sigma = D eps(u) of one bulk equation object at an IP-parametric
+// point (CM_Struc_Linear::flux, FEM/INT/src/CM/cl_FEM_CM_Struc_Linear.cpp:
+// 280-302, strain by eval_strain_2d / _3d :349-498, D by CM_Struc_Linear_
+// Isotropic :61-392), one thread per point; the element data of the points
+// are gathered by the host, u_pdof = T u_adof in the kernel
+template <int D>
+__global__ void flux_kernel(int64_t n, int maxnb, int model, double nu_p, const double* xe, const double* T,
+                            const int32_t* bases, const int32_t* nb, const double* E, const double* rho, double beta,
+                            const double* xi, const double* u, int64_t nu, int ncomp, double* out) {
+    constexpr int NPE = D == 2 ? 4 : 8;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        double N[NPE], dN[NPE * D];
+        if (D == 2) Shape<0>::eval(xi + k * D, N, dN);
+        else Shape<1>::eval(xi + k * D, N, dN);
+        const double* X = xe + k * NPE * D;
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j)
+                for (int a = 0; a < NPE; ++a) J[i][j] = fma(dN[i * NPE + a], X[a * D + j], J[i][j]);
+        if (D == 2) {
+            const double id = 1.0 / (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+            Ji[0][0] = J[1][1] * id; Ji[0][1] = -J[0][1] * id; Ji[1][0] = -J[1][0] * id; Ji[1][1] = J[0][0] * id;
+        } else {
+            const double id = 1.0 / (J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                                     J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]));
+            Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
+            Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+            Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+            Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+            Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+            Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
+            Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+            Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
+            Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+        }
+        // grad[f][i] = du_f / dx_i
+        double grad[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int a = 0; a < NPE; ++a) {
+            double g[3] = {0, 0, 0};
+            for (int i = 0; i < D; ++i)
+                for (int kk = 0; kk < D; ++kk) g[i] = fma(Ji[i][kk], dN[kk * NPE + a], g[i]);
+            for (int f = 0; f < D; ++f) {
+                double up = 0.0;
+                for (int j = 0; j < nb[k]; ++j) {
+                    const double t = T[(k * NPE + a) * maxnb + j];
+                    if (fem_nonzero(t)) up = fma(t, u[f * nu + bases[k * maxnb + j]], up);
+                }
+                for (int i = 0; i < D; ++i) grad[f][i] = fma(g[i], up, grad[f][i]);
+            }
+        }
+        double Ek = E[k];
+        if (rho) {
+            double r = 0.0;
+            for (int a = 0; a < NPE; ++a) r = fma(N[a], rho[k * NPE + a], r);
+            Ek *= beta == 3.0 ? r * r * r : pow(r, beta);
+        }
+        const double mu = Ek / (2.0 * (1.0 + nu_p));
+        const double lam = model == FEM_GPU_MODEL_PLANE_STRESS ? Ek * nu_p / (1.0 - nu_p * nu_p)
+                                                               : Ek * nu_p / ((1.0 + nu_p) * (1.0 - 2.0 * nu_p));
+        double* o = out + k * ncomp;
+        if (D == 3) {
+            const double tr = grad[0][0] + grad[1][1] + grad[2][2];
+            for (int i = 0; i < 3; ++i) o[i] = lam * tr + 2.0 * mu * grad[i][i];
+            o[3] = mu * (grad[1][2] + grad[2][1]);
+            o[4] = mu * (grad[0][2] + grad[2][0]);
+            o[5] = mu * (grad[0][1] + grad[1][0]);
+        } else {
+            const double tr = grad[0][0] + grad[1][1];
+            o[0] = lam * tr + 2.0 * mu * grad[0][0];
+            o[1] = lam * tr + 2.0 * mu * grad[1][1];
+            if (model == FEM_GPU_MODEL_PLANE_STRESS) {
+                o[2] = mu * (grad[0][1] + grad[1][0]);
+            } else {
+                o[2] = lam * tr;
+                o[3] = mu * (grad[0][1] + grad[1][0]);
+            }
+        }
+    }
+}
+
+}  // namespace fem_flux
+
+extern "C" {
+
+fem_gpu_status fem_gpu_element_flux(fem_gpu_ctx* c, int32_t set, int64_t count, const int64_t* eq, const double* xi,
+                                    const double* u, double* flux, int32_t* ncomp, uint32_t flags) {
+    if (!c || count < 0 || (count > 0 && (!eq || !xi || !u || !flux))) return FEM_GPU_BAD_ARG;
+    if (!c->dev_final) return FEM_GPU_NOT_FINALIZED;
+    if (set < 0 || set >= (int32_t)c->sets.size() || c->sets[set].kind != 0)
+        return fail(c, FEM_GPU_BAD_ARG, "element_flux: not a bulk set");
+    const SetData& s = c->sets[set];
+    const int D = c->dim, NPE = c->npe, model = s.bulk.model_type;
+    const int nc = D == 3 ? 6 : (model == FEM_GPU_MODEL_PLANE_STRESS ? 3 : 4);
+    if (ncomp) *ncomp = nc;
+    if (count == 0) return FEM_GPU_OK;
+    const int maxnb = s.maxnb;
+    std::vector<double> xe((size_t)count * NPE * D), T((size_t)count * NPE * maxnb), E(count), rho;
+    std::vector<int32_t> bs((size_t)count * maxnb), nbv(count);
+    if (!s.rhoe.empty()) rho.resize((size_t)count * NPE);
+    for (int64_t k = 0; k < count; ++k) {
+        const int64_t e = eq[k];
+        if (e < 0 || e >= s.neq) return fail(c, FEM_GPU_OOB_INDEX, "element_flux: equation object index");
+        std::copy_n(s.xe.data() + e * NPE * D, NPE * D, xe.data() + k * NPE * D);
+        std::copy_n(s.T.data() + e * NPE * maxnb, NPE * maxnb, T.data() + k * NPE * maxnb);
+        std::copy_n(s.bases.data() + e * maxnb, maxnb, bs.data() + k * maxnb);
+        nbv[k] = s.nb[e];
+        // the stiffness modulus carries the Thickness property; the stress does not
+        E[k] = s.E[e] / s.bulk_thickness;
+        if (!rho.empty()) std::copy_n(s.rhoe.data() + e * NPE, NPE, rho.data() + k * NPE);
+    }
+    const bool host = flags & FEM_GPU_HOST_BUFFERS;
+    const int64_t nad = c->num_used * c->dim;
+    cudaStream_t sm = stream_of(c);
+    Staged su, so, sxi, sxe, sT, sE, sb, snb, sr;
+    fem_gpu_status st;
+    if ((st = stage_in(c, u, nad * sizeof(double), host, su)) != FEM_GPU_OK) return st;
+    if ((st = stage_out_alloc(c, flux, (size_t)count * nc * sizeof(double), host, so)) != FEM_GPU_OK) return st;
+    if ((st = stage_in(c, xi, (size_t)count * D * sizeof(double), true, sxi)) != FEM_GPU_OK) return st;
+    if ((st = stage_in(c, xe.data(), xe.size() * sizeof(double), true, sxe)) != FEM_GPU_OK) return st;
+    if ((st = stage_in(c, T.data(), T.size() * sizeof(double), true, sT)) != FEM_GPU_OK) return st;
+    if ((st = stage_in(c, E.data(), E.size() * sizeof(double), true, sE)) != FEM_GPU_OK) return st;
+    if ((st = stage_in(c, bs.data(), bs.size() * sizeof(int32_t), true, sb)) != FEM_GPU_OK) return st;
+    if ((st = stage_in(c, nbv.data(), nbv.size() * sizeof(int32_t), true, snb)) != FEM_GPU_OK) return st;
+    if (!rho.empty() && (st = stage_in(c, rho.data(), rho.size() * sizeof(double), true, sr)) != FEM_GPU_OK)
+        return st;
+    const unsigned blocks = (unsigned)std::min<int64_t>((count + 127) / 128, (int64_t)sm_count() * 8);
+    const double beta = s.bulk.density_exponent;
+    if (D == 2)
+        fem_flux::flux_kernel<2><<<blocks, 128, 0, sm>>>(count, maxnb, model, s.bulk.poisson_ratio, (double*)sxe.dev,
+                                                         (double*)sT.dev, (int32_t*)sb.dev, (int32_t*)snb.dev,
+                                                         (double*)sE.dev, (double*)sr.dev, beta, (double*)sxi.dev,
+                                                         (double*)su.dev, c->num_used, nc, (double*)so.dev);
+    else
+        fem_flux::flux_kernel<3><<<blocks, 128, 0, sm>>>(count, maxnb, model, s.bulk.poisson_ratio, (double*)sxe.dev,
+                                                         (double*)sT.dev, (int32_t*)sb.dev, (int32_t*)snb.dev,
+                                                         (double*)sE.dev, (double*)sr.dev, beta, (double*)sxi.dev,
+                                                         (double*)su.dev, c->num_used, nc, (double*)so.dev);
+    ++c->launches;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && host)
+        e = cudaMemcpyAsync(flux, so.dev, (size_t)count * nc * sizeof(double), cudaMemcpyDeviceToHost, sm);
+    for (Staged* p : {&su, &so, &sxi, &sxe, &sT, &sE, &sb, &snb, &sr}) release(c, *p);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sm);
+    return e == cudaSuccess ? FEM_GPU_OK : cuda_fail(c, e, "element flux");
 }
 
 fem_gpu_status fem_gpu_check_status(fem_gpu_ctx* c) {

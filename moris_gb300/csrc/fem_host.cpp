@@ -366,6 +366,14 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     s.E.assign(d->youngs_modulus, d->youngs_modulus + s.neq);
     for (double e : s.E)
         if (!std::isfinite(e)) return fail(c, FEM_GPU_NONFINITE, "youngs modulus");
+    // the Thickness property multiplies w* of every term of this linear
+    // elastic set (stiffness, residual, strain energy, their derivatives), which
+    // is the same as multiplying E
+    if (d->thickness < 0.0 || !std::isfinite(d->thickness)) return fail(c, FEM_GPU_BAD_ARG, "bulk set thickness");
+    if (d->thickness > 0.0) {
+        s.bulk_thickness = d->thickness;
+        for (double& e : s.E) e *= d->thickness;
+    }
     if (d->ig_offsets || igc != c->ip_cell) {
         if (d->ig_offsets) s.ig_off.assign(d->ig_offsets, d->ig_offsets + s.neq + 1);
         else s.ig_off.assign(1, 0);
@@ -415,6 +423,20 @@ fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* c, const fem_gpu_side_set_desc*
     SetData s;
     s.kind = 1;
     s.side = *d;
+    if (d->thickness < 0.0 || !std::isfinite(d->thickness)) return fail(c, FEM_GPU_BAD_ARG, "side set thickness");
+    s.side_thickness = d->thickness > 0.0 ? d->thickness : 1.0;
+    if (d->select_matrix) {
+        if (d->iwg_type == FEM_GPU_IWG_STRUC_LINEAR_NEUMANN)
+            return fail(c, FEM_GPU_BAD_ARG, "a Select matrix applies to Dirichlet sets only");
+        for (int k = 0; k < 9; ++k) s.side_select[k] = 0.0;
+        for (int i = 0; i < c->dim; ++i)
+            for (int j = 0; j < c->dim; ++j) {
+                const double v = d->select_matrix[i * c->dim + j];
+                if (!std::isfinite(v)) return fail(c, FEM_GPU_NONFINITE, "select matrix");
+                s.side_select[i * 3 + j] = v;
+            }
+    }
+    s.side.select_matrix = nullptr;
     s.neq = d->num_sides;
     s.ip_cell.assign(d->side_ip_cell, d->side_ip_cell + s.neq);
     s.ordinal.assign(d->side_ordinal, d->side_ordinal + s.neq);

@@ -35,6 +35,9 @@ struct SetData {
     int kind = 0;  // 0 bulk, 1 side, 2 double-sided (interface / ghost)
     fem_gpu_bulk_set_desc bulk{};
     fem_gpu_side_set_desc side{};
+    double bulk_thickness = 1.0;   // bulk sets: Thickness property (folded into E)
+    double side_thickness = 1.0;   // side sets: w* factor (Thickness property)
+    double side_select[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // side sets: Select matrix M (3 x 3 row-major)
     fem_gpu_double_side_set_desc dside{};
     int64_t neq = 0;
     std::vector<int32_t> ip_cell;
@@ -119,6 +122,8 @@ struct fem_gpu_ctx {
 
 namespace fem {
 fem_gpu_status fail(fem_gpu_ctx* c, fem_gpu_status s, const std::string& msg);
+// multiprocessor count of the current device (cached per device; grid sizing)
+int sm_count();
 // device side (fem_device.cu)
 fem_gpu_status device_finalize(fem_gpu_ctx* c);
 void device_release(fem_gpu_ctx* c);
@@ -134,6 +139,9 @@ double ip_cell_measure(const fem_gpu_ctx* c, int64_t cell);
 fem_gpu_status interface_volumes(fem_gpu_ctx* c);
 // one set's assembly through its kernel (fem_device.cu); vals / rhs may be NULL
 fem_gpu_status assemble_set(fem_gpu_ctx* c, int set, const double* u, double* vals, double* rhs);
+// device address of fem_gpu_pcg_noalloc's fixed array on the current device,
+// resolved once per device (fem_solver.cu); loads that file's module
+fem_gpu_status noalloc_prepare(fem_gpu_ctx* c);
 // device memory of the sensitivity path (fem_sensitivity.cu)
 void sensitivity_release(fem_gpu_ctx* c);
 }  // namespace fem

@@ -492,7 +492,7 @@ fem_gpu_status fem_cnn_train_step(fem_cnn* c, const float* in4, const float* tar
 namespace {
 
 unsigned lpc_grid(int64_t work) {
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 32));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, (int64_t)sm_count() * 32));
 }
 
 __device__ __forceinline__ float hat(int d, int F) {
@@ -789,7 +789,7 @@ fem_gpu_status fem_lpc_prolong_transpose(int32_t nf, int32_t factor, const doubl
 fem_gpu_status fem_gpu_spmv(int64_t n, const int32_t* rowptr, const int32_t* colidx, const double* vals,
                             const double* x, double* y) {
     if (n < 1 || !rowptr || !colidx || !vals || !x || !y) return FEM_GPU_BAD_ARG;
-    const unsigned blocks = (unsigned)std::min<int64_t>((n * fem::kLanesPerRow + 255) / 256, 152 * 16);
+    const unsigned blocks = (unsigned)std::min<int64_t>((n * fem::kLanesPerRow + 255) / 256, (int64_t)sm_count() * 16);
     csr_spmv_kernel<<<blocks, 256>>>(n, rowptr, colidx, vals, x, y);
     return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
 }
@@ -866,8 +866,8 @@ static fem_gpu_status fcg_run(fem_gpu_ctx* c, const int32_t* rowptr, const int32
         return fail(c, FEM_GPU_OUT_OF_MEMORY, "fcg workspace");
     }
     const int tpb = 256;
-    const unsigned rb = (unsigned)std::min<int64_t>((n * fem::kLanesPerRow + tpb - 1) / tpb, 152 * 16);
-    const unsigned vb = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    const unsigned rb = (unsigned)std::min<int64_t>((n * fem::kLanesPerRow + tpb - 1) / tpb, (int64_t)sm_count() * 16);
+    const unsigned vb = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, (int64_t)sm_count() * 16);
     double hd[kMaxM];
     auto readn = [&](int k) {
         cudaMemcpy(hd, dots, k * sizeof(double), cudaMemcpyDeviceToHost);

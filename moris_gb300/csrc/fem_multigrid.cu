@@ -506,7 +506,7 @@ __global__ void mg_gemv(int64_t m, const double* __restrict__ A, const double* _
 }
 
 unsigned blocks_for(int64_t work, int tpb) {
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + tpb - 1) / tpb, 152 * 32));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((work + tpb - 1) / tpb, (int64_t)fem::sm_count() * 32));
 }
 
 }  // namespace

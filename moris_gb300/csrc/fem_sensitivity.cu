@@ -615,7 +615,7 @@ fem_gpu_status fem_gpu_strain_energy(fem_gpu_ctx* c, const double* u, double* dq
         e = cudaMallocAsync(&d, sizeof(double), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(double), st);
         if (e == cudaSuccess) {
-            dot_kernel<<<152 * 4, 256, 0, st>>>(nad, u, dqdu, d);
+            dot_kernel<<<(unsigned)sm_count() * 4, 256, 0, st>>>(nad, u, dqdu, d);
             e = cudaMemcpyAsync(q, d, sizeof(double), cudaMemcpyDeviceToHost, st);
         }
         if (d) cudaFreeAsync(d, st);

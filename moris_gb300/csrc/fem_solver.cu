@@ -220,8 +220,8 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
     cudaMemsetAsync(st, 0, sizeof(CgState), sm);
     const int tpb = 256;
     const unsigned row_blocks = (unsigned)((n * fem::kLanesPerRow + tpb - 1) / tpb);
-    const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, 152 * 16);
-    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, (int64_t)sm_count() * 16);
+    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, (int64_t)sm_count() * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
                                                                 opts->preconditioner == 1);
     k_init<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, b, x, r, z, p, dinv, st);
@@ -288,7 +288,11 @@ extern "C" fem_gpu_status fem_gpu_pcg(fem_gpu_ctx* c, const int32_t* rowptr, con
 // and the five work vectors r, z, p, q and 1/diag(A), so systems up to
 // kNoAllocMaxRows rows are accepted; larger ones are rejected with
 // FEM_GPU_BAD_ARG.  Every GPU that loads the library keeps this array
-// (about 5.2 MB) until the process exits.
+// (about 5.2 MB) until the process exits.  The array comes with this file's
+// module, which CUDA loads lazily: fem_gpu_finalize resolves the array's
+// address on the current device (noalloc_prepare), so the module is loaded
+// there; after fem_gpu_finalize_host alone the first fem_gpu_pcg_noalloc call
+// on a device does it.
 namespace {
 
 constexpr int64_t kNoAllocMaxRows = 131072;
@@ -322,6 +326,26 @@ fem_gpu_status noalloc_scratch(fem_gpu_ctx* c, double** out) {
 
 }  // namespace
 
+namespace fem {
+fem_gpu_status noalloc_prepare(fem_gpu_ctx* c) {
+    double* p = nullptr;
+    fem_gpu_status st = noalloc_scratch(c, &p);
+    if (st != FEM_GPU_OK) return st;
+    // with lazy loading a kernel's code is loaded at its first launch; reading
+    // the attributes of the solver's kernels loads them now
+    const void* kernels[] = {(const void*)k_diag_inv, (const void*)k_init,     (const void*)k_set_thresh,
+                             (const void*)k_spmv_pq,  (const void*)k_update_xr, (const void*)k_update_p,
+                             (const void*)k_advance};
+    for (const void* k : kernels) {
+        cudaFuncAttributes a;
+        const cudaError_t e = cudaFuncGetAttributes(&a, k);
+        if (e != cudaSuccess)
+            return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg_noalloc: kernel load: ") + cudaGetErrorString(e));
+    }
+    return FEM_GPU_OK;
+}
+}  // namespace fem
+
 extern "C" fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* c, const int32_t* rowptr, const int32_t* colidx,
                                               const double* vals, const double* b, double* x,
                                               const fem_gpu_pcg_opts* opts, fem_gpu_pcg_report* rep,
@@ -352,7 +376,7 @@ extern "C" fem_gpu_status fem_gpu_pcg_noalloc(fem_gpu_ctx* c, const int32_t* row
     if (e != cudaSuccess) return fail(c, FEM_GPU_CUDA_ERROR, std::string("pcg_noalloc: ") + cudaGetErrorString(e));
     const int tpb = 256;
     const unsigned row_blocks = (unsigned)((n * fem::kLanesPerRow + tpb - 1) / tpb);
-    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, (int64_t)sm_count() * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv,
                                                                 opts->preconditioner == 1);
     k_init<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, b, x, r, z, p, dinv, cs);
@@ -417,8 +441,8 @@ extern "C" fem_gpu_status fem_gpu_pcg_snapshots(fem_gpu_ctx* c, const int32_t* r
     cudaMemsetAsync(st, 0, sizeof(CgState), sm);
     const int tpb = 256;
     const unsigned row_blocks = (unsigned)((n * fem::kLanesPerRow + tpb - 1) / tpb);
-    const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, 152 * 16);
-    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 152 * 16);
+    const unsigned spmv_blocks = (unsigned)std::min<int64_t>(row_blocks, (int64_t)sm_count() * 16);
+    const unsigned vec_blocks = (unsigned)std::min<int64_t>((n + tpb - 1) / tpb, (int64_t)sm_count() * 16);
     k_diag_inv<<<(unsigned)((n + tpb - 1) / tpb), tpb, 0, sm>>>(n, rowptr, colidx, vals, dinv, opts->preconditioner == 1);
     k_init<<<row_blocks, tpb, 0, sm>>>(n, rowptr, colidx, vals, b, x, r, z, p, dinv, st);
     k_set_thresh<<<1, 1, 0, sm>>>(st, opts->rel_tol);

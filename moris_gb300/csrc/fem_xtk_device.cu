@@ -122,7 +122,7 @@ bool select_indices(const uint8_t* flags, int64_t n, DevVec<int32_t>& out, int64
     DevVec<int32_t> idx;
     DevVec<int32_t> cnt;
     if (!idx.alloc(n) || !out.alloc(n) || !cnt.alloc(1)) return false;
-    k_iota<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 64)), 256>>>(idx.p, n);
+    k_iota<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)fem::sm_count() * 64)), 256>>>(idx.p, n);
     if (!cub_run([&](void* t, size_t& b) {
             return cub::DeviceSelect::Flagged(t, b, idx.p, flags, out.p, cnt.p, (int)n);
         }))
@@ -134,7 +134,7 @@ bool select_indices(const uint8_t* flags, int64_t n, DevVec<int32_t>& out, int64
 }
 
 unsigned grid(int64_t n, int tpb = 256) {
-    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + tpb - 1) / tpb, 152 * 64));
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + tpb - 1) / tpb, (int64_t)fem::sm_count() * 64));
 }
 #define GRID_STRIDE(i, n) for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (n); \
                                i += (int64_t)gridDim.x * blockDim.x)

@@ -457,6 +457,7 @@ struct BulkSet {
     real nu;
     std::vector<real> node_rho;  // optional nodal density field
     real beta = 3.0;
+    real thickness = 1.0;        // Thickness property (multiplies w*)
 };
 /* double-sided cluster set (interface / ghost): facets with vertex coords
    and their parametric coords in the leader and follower IP cells */
@@ -474,6 +475,9 @@ struct SideSet {
     std::vector<real> E;
     real nu, alpha;
     real value[3];
+    real thickness = 1.0;        // Thickness property (multiplies w*)
+    bool has_select = false;     // Select property of the Dirichlet IWG (dim x dim)
+    real select[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 }  // namespace
@@ -692,6 +696,31 @@ int orc_model_set_density(orc_model* m, int set, const double* node_rho, double 
     if (set < 0 || set >= (int)m->bulk.size()) return 1;
     m->bulk[set].node_rho.assign(node_rho, node_rho + m->num_nodes);
     m->bulk[set].beta = beta;
+    return 0;
+}
+
+/* the Thickness property of a bulk set (IWG_Isotropic_Struc_Linear_Bulk,
+   FEM/INT/src/IWG/cl_FEM_IWG_Isotropic_Struc_Linear_Bulk.cpp:84-85: w* is
+   multiplied by it) */
+int orc_model_set_bulk_thickness(orc_model* m, int set, double thickness) {
+    if (set < 0 || set >= (int)m->bulk.size() || !(thickness > 0.0)) return 1;
+    m->bulk[set].thickness = thickness;
+    return 0;
+}
+
+/* Thickness and Select properties of the k-th side set: w* times the
+   thickness (..._Neumann.cpp:66-67, ..._Dirichlet.cpp:103-104); the selection
+   matrix M projects the Dirichlet terms (..._Dirichlet.cpp:66-81, 107-116),
+   NULL = the identity */
+int orc_model_set_side_options(orc_model* m, int side_set, double thickness, const double* select) {
+    if (side_set < 0 || side_set >= (int)m->side.size() || !(thickness > 0.0)) return 1;
+    SideSet& s = m->side[side_set];
+    s.thickness = thickness;
+    s.has_select = select != nullptr;
+    for (int k = 0; k < 9; ++k) s.select[k] = 0.0;
+    if (select)
+        for (int i = 0; i < m->dim; ++i)
+            for (int j = 0; j < m->dim; ++j) s.select[i * 3 + j] = select[i * m->dim + j];
     return 0;
 }
 
@@ -987,7 +1016,7 @@ void bulk_pdof(const orc_model* m, const BulkSet& s, int64_t eq, const Mat& upd,
             Mat Jig = mul(dNig, Xig);
             const real detJ = det_bulk(Jig, s.ig_cell, ig_rect);
             if (detJ < -1.0e-6) continue;
-            const real wstar = rt.w[q] * detJ;
+            const real wstar = rt.w[q] * detJ * s.thickness;
             Mat xip = mul(Nig, XIig);  // 1 x d
             Mat Nrow, dNdx;
             ip_eval(m, Xip, xip.a.data(), Nrow, dNdx);
@@ -1083,7 +1112,7 @@ void side_pdof(const orc_model* m, const SideSet& s, int64_t eq, const Mat& upd,
             nrm[2] = c2 / detJ;
         }
         if (detJ < -1.0e-6) continue;
-        const real wstar = rt.w[q] * detJ;
+        const real wstar = rt.w[q] * detJ * s.thickness;
         Mat xip = mul(Ns, XIs);
         Mat Nrow, dNdx;
         ip_eval(m, Xip, xip.a.data(), Nrow, dNdx);
@@ -1095,6 +1124,15 @@ void side_pdof(const orc_model* m, const SideSet& s, int64_t eq, const Mat& upd,
             add_scaled(R, -wstar, mul(Nt, t));
             continue;
         }
+        // selection matrix M (identity without a Select property)
+        Mat M(d, d, 0.0);
+        real mnorm = 0.0;
+        for (int i = 0; i < d; ++i)
+            for (int j = 0; j < d; ++j) {
+                M(i, j) = s.has_select ? s.select[i * 3 + j] : (i == j ? 1.0 : 0.0);
+                mnorm += M(i, j) * M(i, j);
+            }
+        if (std::sqrt(mnorm) < 1e-16) continue;  // a zero projection adds nothing
         Mat B = test_strain(s.model, dNdx);
         Mat Fn = flat_normal(nrm, d, nstress);
         Mat nDB = mul(Fn, mul(D, B));  // d x nd (testTraction == dTractiondDOF)
@@ -1102,15 +1140,17 @@ void side_pdof(const orc_model* m, const SideSet& s, int64_t eq, const Mat& upd,
         Mat jump = mul(N, uvec);
         for (int k = 0; k < d; ++k) jump(k, 0) -= s.value[k];
         Mat nDBt = trans(nDB);
-        Mat r = mul(Nt, trac);
+        Mat Mjump = mul(M, jump);
+        Mat r = mul(Nt, mul(M, trac));
         for (auto& v : r.a) v = -v;
-        add_scaled(r, beta, mul(nDBt, jump));
-        add_scaled(r, gamma, mul(Nt, jump));
+        add_scaled(r, beta, mul(nDBt, Mjump));
+        add_scaled(r, gamma, mul(Nt, Mjump));
         add_scaled(R, wstar, r);
-        Mat k = mul(nDBt, N);
+        Mat MN = mul(M, N);
+        Mat k = mul(nDBt, MN);
         for (auto& v : k.a) v *= beta;
-        add_scaled(k, gamma, mul(Nt, N));
-        add_scaled(k, -1.0, mul(Nt, nDB));
+        add_scaled(k, gamma, mul(Nt, MN));
+        add_scaled(k, -1.0, mul(Nt, mul(M, nDB)));
         add_scaled(K, wstar, k);
     }
     (void)nstress;
@@ -1397,6 +1437,37 @@ int orc_element_matrices(const orc_model* m, int set, int64_t eq, const double* 
     element_adof(m, set, eq, u_adof, Ka, Ra);
     std::memcpy(K, Ka.a.data(), Ka.a.size() * sizeof(real));
     std::memcpy(R, Ra.a.data(), Ra.a.size() * sizeof(real));
+    return 0;
+}
+
+/* stress of a bulk equation object at an IP-parametric point:
+   CM_Struc_Linear::flux = D eps(u) (FEM/INT/src/CM/cl_FEM_CM_Struc_Linear.cpp:
+   280-302) with u_pdof = T u_adof; Voigt order of the model (3D: xx yy zz yz
+   xz xy; plane strain: xx yy zz xy; plane stress: xx yy xy) */
+int orc_element_flux(const orc_model* m, int set, int64_t eq, const double* xi, const double* u_adof,
+                     double* flux, int32_t* ncomp) {
+    if (!m->finalized || set < 0 || set >= (int)m->bulk.size()) return 1;
+    const BulkSet& s = m->bulk[set];
+    if (eq < 0 || eq >= (int64_t)s.ip_cell.size()) return 1;
+    const int cell = s.ip_cell[eq];
+    const int d = m->dim, npe = cell_nodes(m->ip_cell);
+    Mat T = element_T(m, cell);
+    std::vector<int32_t> ids = element_ids(m, cell);
+    Mat ua((int)ids.size(), 1);
+    for (size_t k = 0; k < ids.size(); ++k) ua(k, 0) = u_adof[ids[k]];
+    Mat up = mul(T, ua);
+    Mat Nrow, dNdx;
+    ip_eval(m, ip_coords(m, cell), xi, Nrow, dNdx);
+    real E = s.E[eq];
+    if (!s.node_rho.empty()) {
+        real rho = 0.0;
+        for (int a = 0; a < npe; ++a) rho += Nrow(0, a) * s.node_rho[m->cells[(int64_t)cell * npe + a]];
+        E *= std::pow(rho, s.beta);
+    }
+    Mat D = constitutive(s.model, d, E, s.nu);
+    Mat sig = mul(D, mul(test_strain(s.model, dNdx), up));
+    for (int i = 0; i < sig.r; ++i) flux[i] = sig(i, 0);
+    *ncomp = sig.r;
     return 0;
 }
 

@@ -83,6 +83,11 @@ int orc_model_add_side_set(orc_model* m, int iwg, int rule, int model_type, int6
                            const double* value);
 /* double-sided set (interface / ghost); sets are indexed bulk sets first,
    then side sets, then double-sided sets */
+/* Thickness property of bulk set `set` (w* times thickness) */
+int orc_model_set_bulk_thickness(orc_model* m, int set, double thickness);
+/* Thickness and Select properties of the side_set-th side set; select is a
+   dim x dim row-major matrix or NULL (identity) */
+int orc_model_set_side_options(orc_model* m, int side_set, double thickness, const double* select);
 int orc_model_add_double_side_set(orc_model* m, int iwg, int facet_cell, int rule, int model_type,
                                   int64_t num_clusters, const int32_t* leader, const int32_t* follower,
                                   const int64_t* facet_offsets, const double* facet_coords,
@@ -103,6 +108,10 @@ int orc_element_topology(const orc_model* m, int set, int64_t eq, int32_t* ids, 
 int orc_element_matrices(const orc_model* m, int set, int64_t eq, const double* u_adof,
                          double* K_colmajor, double* R);
 /* pdof-space (before T^T K T) element matrices, for unit checks */
+/* Voigt stress of bulk set `set`, equation object eq, at IP-parametric point
+   xi; ncomp = number of components */
+int orc_element_flux(const orc_model* m, int set, int64_t eq, const double* xi, const double* u_adof,
+                     double* flux, int32_t* ncomp);
 int orc_element_pdof_matrices(const orc_model* m, int set, int64_t eq, const double* u_pdof,
                               double* K_colmajor, double* R, int32_t* npdof);
 /* full assembly; eq_stride > 1 assembles every eq_stride-th element only

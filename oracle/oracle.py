@@ -42,6 +42,9 @@ def load():
             "orc_model_set_density": (_I, [_P, _I, _P, _D]),
             "orc_model_add_double_side_set": (_I, [_P, _I, _I, _I, _I, _L, _P, _P, _P, _P, _P, _P, _P, _P, _D,
                                                    _D]),
+            "orc_model_set_bulk_thickness": (_I, [_P, _I, _D]),
+            "orc_model_set_side_options": (_I, [_P, _I, _D, _P]),
+            "orc_element_flux": (_I, [_P, _I, _L, _P, _P, _P, _P]),
             "orc_model_finalize": (_I, [_P]),
             "orc_model_update_ig": (_I, [_P, _I, _L, _P, _P]),
             "orc_model_update_facets": (_I, [_P, _I, _L, _P, _P, _P]),
@@ -175,6 +178,23 @@ class OracleModel:
         r = self.lib.orc_model_add_side_set(self.h, iwg, rule, model, len(ipc), _ptr(ipc), _ptr(ords),
                                             _ptr(E), nu, alpha, _ptr(v))
         assert r == 0
+
+    def set_bulk_thickness(self, bulk_set, thickness):
+        assert self.lib.orc_model_set_bulk_thickness(self.h, bulk_set, thickness) == 0
+
+    def set_side_options(self, side_set, thickness=1.0, select=None):
+        """Thickness and Select properties of the side_set-th side set"""
+        sel = None if select is None else np.ascontiguousarray(select, dtype=np.float64).ravel()
+        assert self.lib.orc_model_set_side_options(self.h, side_set, thickness, _ptr(sel)) == 0
+
+    def element_flux(self, s, eq, xi, u_adof):
+        """Voigt stress of a bulk equation object at IP-parametric point xi"""
+        out = np.zeros(6)
+        n = C.c_int32()
+        x = np.ascontiguousarray(xi, dtype=np.float64)
+        u = np.ascontiguousarray(u_adof, dtype=np.float64)
+        assert self.lib.orc_element_flux(self.h, s, eq, _ptr(x), _ptr(u), _ptr(out), C.byref(n)) == 0
+        return out[:n.value].copy()
 
     def finalize(self):
         assert self.lib.orc_model_finalize(self.h) == 0

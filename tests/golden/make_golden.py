@@ -1,8 +1,9 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run once in a container that has the reference mounted:
+Run once where the reference source tree is available, with its root as the
+argument:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference source tree>
 
 It copies the reference's own shape-function and quadrature fixture files
 (``projects/FEM/INT/test/data``: raw ``uint rows, uint cols`` + column-major
@@ -10,7 +11,13 @@ doubles, read by ``LINALG/src/fn_load_matrix_from_binary_file.hpp``) and
 extracts the deterministic linear-element inputs of the elasticity IWG unit
 tests (``FEM/INT/test/FEM_Test_Proxy/cl_FEM_Inputs_for_Elasticity_UT.cpp``,
 ``fill_xhat_Elast`` / ``fill_uhat_Elast``, interpolation order 1) into
-``elasticity_inputs.json``.  Nothing at test time reads the reference.
+``elasticity_inputs.json``.  It also extracts the 2 x 2 QUAD4 mesh of the
+reference's plane-strain example (``projects/EXA/structure/linear/Plane_Strain/
+4elements.e``, Exodus II in netCDF classic format, read with scipy's netCDF
+reader) into ``plane_strain_4elements.json``: node coordinates, 0-based cell
+connectivity and the side sets as (cell, side ordinal) pairs, where the
+ordinal is the Exodus side number minus one (side k joins local nodes k and
+k+1).  Nothing at test time reads the reference.
 """
 import json
 import os
@@ -48,6 +55,25 @@ def _case_block(text, func, dim, order):
     return [[float(x) for x in r.split(",") if x.strip()] for r in rows]
 
 
+def plane_strain_mesh(ref):
+    from scipy.io import netcdf_file
+    path = os.path.join(ref, "projects", "EXA", "structure", "linear", "Plane_Strain", "4elements.e")
+    f = netcdf_file(path, "r", mmap=False)
+    v = f.variables
+
+    def names(key):
+        return [b"".join(r).decode().strip("\x00") for r in v[key][:]]
+
+    coords = [[float(x), float(y)] for x, y in zip(v["coordx"][:], v["coordy"][:])]
+    cells = (v["connect1"][:] - 1).tolist()
+    sides = {}
+    for k, name in enumerate(names("ss_names")):
+        sides[name] = {"cells": (v["elem_ss%d" % (k + 1)][:] - 1).tolist(),
+                       "ordinals": (v["side_ss%d" % (k + 1)][:] - 1).tolist()}
+    return {"source": "projects/EXA/structure/linear/Plane_Strain/4elements.e", "coords": coords, "cells": cells,
+            "block": names("eb_names")[0], "side_sets": sides}
+
+
 def main(ref):
     here = os.path.dirname(os.path.abspath(__file__))
     data = os.path.join(ref, "projects", "FEM", "INT", "test", "data")
@@ -61,7 +87,11 @@ def main(ref):
         out["uhat_%dd" % dim] = _case_block(src, "uhat_Elast", dim, 1)
     with open(os.path.join(here, "elasticity_inputs.json"), "w") as f:
         json.dump(out, f, indent=1)
+    with open(os.path.join(here, "plane_strain_4elements.json"), "w") as f:
+        json.dump(plane_strain_mesh(ref), f, indent=1)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference source tree>")
+    main(sys.argv[1])

@@ -30,7 +30,7 @@ def test_binding_covers_header():
 
 def test_library_answers_without_gpu():
     lib = mg.lib()
-    assert lib.fem_gpu_abi_version() == 2
+    assert lib.fem_gpu_abi_version() == 3
     assert lib.fem_gpu_status_string(0) == b"ok"
     assert lib.fem_gpu_device_count() >= 0
 

@@ -282,3 +282,69 @@ def test_host_buffer_assembly_overlaps_the_copy_back(torch):
     for _ in range(2):  # the cached chunk plan and copy stream are reused
         vh2, rh2 = prod.assemble_host(u)
         assert csr_row_rel_err(rp, vh2, vh) <= RTOL and rel_err(rh2, rh) <= RTOL
+
+
+SELECT_CASES = [
+    # dim, ne, p, shape, rule, iwg
+    (2, (5, 4), 2, mg.SHAPE_GENERAL, mg.RULE_QUAD_2x2, mg.IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE),
+    (3, (3, 2, 3), 2, mg.SHAPE_GENERAL, mg.RULE_HEX_3x3x3, mg.IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE),
+    (3, (3, 3, 2), 1, mg.SHAPE_RECTANGULAR, mg.RULE_HEX_2x2x2, mg.IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE),
+]
+
+
+@pytest.mark.parametrize("case", SELECT_CASES, ids=lambda c: "d%d-p%d-iwg%d" % (c[0], c[2], c[5]))
+def test_select_and_thickness_properties_match_oracle(torch, case):
+    """Dirichlet sets with a general (non-diagonal) Select matrix and every set
+    with a Thickness property (..._Dirichlet.cpp:66-116, ..._Neumann.cpp:66-67,
+    ..._Bulk.cpp:84-85): element operators, CSR values and residual."""
+    from oracle import OracleModel
+    from tests.common import distort
+    dim, ne, p, shape, rule, iwg = case
+    mesh = mg.hmr_uniform_mesh(dim, ne, [1.0] * dim, p)
+    if shape == mg.SHAPE_GENERAL:
+        mesh = distort(mesh, dim, ne, 0.2, 8)
+    nc = len(mesh["cells"])
+    E = 10.0 ** (-3.0 * uniform01(2, nc))
+    model = mg.MODEL_3D if dim == 3 else mg.MODEL_PLANE_STRAIN
+    ipc = mg.CELL_QUAD4 if dim == 2 else mg.CELL_HEX8
+    srule = mg.RULE_BAR_3 if dim == 2 else mg.RULE_QUAD_2x2
+    M = np.random.default_rng(4).uniform(-1.0, 1.0, (dim, dim))
+    t_bulk, t_dir, t_neu = 0.37, 0.6, 1.7
+    cells = np.arange(nc, dtype=np.int32)
+    left = cells[cells % ne[0] == 0]
+    right = cells[cells % ne[0] == ne[0] - 1]
+    prod = mg.FemModel(dim, mesh, shape)
+    orc = OracleModel(dim, ipc, shape, mesh)
+    prod.add_bulk_set(cells, E, 0.3, rule, model, thickness=t_bulk)
+    orc.add_bulk_set(ipc, rule, model, cells, E, 0.3)
+    orc.set_bulk_thickness(0, t_bulk)
+    g = tuple(0.01 * (k + 1) for k in range(dim))
+    prod.add_side_set(iwg, left, np.full(len(left), 3), E[left], 0.3, srule, model, alpha=50.0, value=g,
+                      thickness=t_dir, select=M)
+    orc.add_side_set(iwg, srule, model, left, np.full(len(left), 3), E[left], 0.3, 50.0, g)
+    orc.set_side_options(0, t_dir, M)
+    trac = (1e-3,) + (2e-3,) * (dim - 1)
+    prod.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, right, np.full(len(right), 1), E[right], 0.3, srule, model,
+                      value=trac, thickness=t_neu)
+    orc.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, srule, model, right, np.full(len(right), 1), E[right], 0.3, 0.0,
+                     trac)
+    orc.set_side_options(1, t_neu, None)
+    prod.finalize()
+    orc.finalize()
+    u = uniform01(12, prod.num_adofs) - 0.5
+    for s in range(3):
+        n_eq = orc.num_eq(s)
+        K, R = prod.element_matrices(s, 0, n_eq, u)
+        for eq in range(n_eq):
+            Ko, Ro = orc.element_matrices(s, eq, u)
+            n = len(Ro)
+            assert rel_err(K[eq, :n, :n], Ko) <= RTOL, (s, eq)
+            assert rel_err(R[eq, :n], Ro) <= RTOL, (s, eq)
+    rp, _ = prod.graph()
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(torch.tensor(u, device="cuda"), vals, rhs)
+    torch.cuda.synchronize()
+    vo, ro = orc.assemble(u)
+    assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL
+    assert rel_err(rhs.cpu().numpy(), ro) <= RTOL

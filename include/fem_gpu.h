@@ -69,17 +69,22 @@ typedef enum fem_gpu_status {
 /* cell topologies (mtk::Geometry_Type + interpolation order 1) */
 enum { FEM_GPU_CELL_QUAD4 = 0, FEM_GPU_CELL_HEX8 = 1, FEM_GPU_CELL_TRI3 = 2, FEM_GPU_CELL_TET4 = 3,
        FEM_GPU_CELL_LINE2 = 4 };
-/* Gauss rules (mtk::Integration_Order) */
+/* Gauss rules (mtk::Integration_Order).  FEM_GPU_RULE_AUTO in a set
+   descriptor picks the reference's automatic rule of that set
+   (fem_gpu_auto_integration_rule with the interpolation cells' linear order). */
 enum {
+    FEM_GPU_RULE_AUTO = -1,
     FEM_GPU_RULE_BAR_1 = 0, FEM_GPU_RULE_BAR_3 = 1, FEM_GPU_RULE_QUAD_2x2 = 2, FEM_GPU_RULE_HEX_2x2x2 = 3,
     FEM_GPU_RULE_HEX_3x3x3 = 4, FEM_GPU_RULE_TRI_7 = 5, FEM_GPU_RULE_TET_4 = 6, FEM_GPU_RULE_TET_11 = 7,
     FEM_GPU_RULE_TRI_3 = 8
 };
+/* set kinds of fem_gpu_auto_integration_rule (fem::Element_Type) */
+enum { FEM_GPU_SET_BULK = 0, FEM_GPU_SET_SIDESET = 1, FEM_GPU_SET_DOUBLE_SIDESET = 2 };
 /* fem::Model_Type of CM_Struc_Linear_Isotropic */
 enum { FEM_GPU_MODEL_PLANE_STRAIN = 0, FEM_GPU_MODEL_PLANE_STRESS = 1, FEM_GPU_MODEL_3D = 2 };
 /* mtk::CellShape of the interpolation cells */
 enum { FEM_GPU_SHAPE_RECTANGULAR = 0, FEM_GPU_SHAPE_GENERAL = 1 };
-/* fem::IWG_Type subset (FEM/INT/src/IWG/cl_FEM_IWG_Factory.cpp:191-224) */
+/* fem::IWG_Type subset (FEM/INT/src/IWG/cl_FEM_IWG_Factory.cpp:191-224, 463) */
 enum {
     FEM_GPU_IWG_STRUC_LINEAR_BULK = 0,
     FEM_GPU_IWG_STRUC_LINEAR_NEUMANN = 1,
@@ -87,7 +92,8 @@ enum {
     FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE = 3,
     FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE = 4,
     FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE = 5,
-    FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST = 6
+    FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST = 6,   /* with SP_Ghost_Virtual_Work */
+    FEM_GPU_IWG_GHOST_NORMAL_FIELD = 7       /* with SP_Ghost_Displacement */
 };
 /* flags */
 enum {
@@ -187,7 +193,11 @@ typedef struct fem_gpu_side_set_desc {
    51-386, with SP_Nitsche_Interface, SP/cl_FEM_SP_Nitsche_Interface.cpp:51-97)
    or the face-oriented virtual-work ghost penalty (IWG_Isotropic_Struc_Linear_
    Virtual_Work_Ghost, ..._Virtual_Work_Ghost.cpp:50-244, with
-   SP_Ghost_Virtual_Work, SP/cl_FEM_SP_Ghost_Virtual_Work.cpp:30-38) over the
+   SP_Ghost_Virtual_Work, SP/cl_FEM_SP_Ghost_Virtual_Work.cpp:30-38) or the
+   normal-derivative ghost penalty (IWG_Ghost_Normal_Field, FEM/INT/src/IWG/
+   cl_FEM_IWG_Ghost_Normal_Field.cpp:36-233, order 1, with
+   SP_Ghost_Displacement, SP/cl_FEM_SP_Ghost_Displacement.cpp:51-63: gamma =
+   alpha h E, E = leader_youngs_modulus as its Material property) over the
    facets of one leader / follower pair of IP cells (mtk::Double_Side_Cluster,
    Element_Double_Sideset, FEM/INT/src/ELEM/cl_FEM_Element_Double_Sideset.cpp:
    142-347).  Each equation object is one cluster: a list of facets given by
@@ -198,7 +208,7 @@ typedef struct fem_gpu_side_set_desc {
    measures of the bulk clusters on the leader / follower IP cells; the ghost
    element size is the side length measure of the cluster's facets. */
 typedef struct fem_gpu_double_side_set_desc {
-    int32_t iwg_type;             /* INTERFACE_SYMMETRIC / _UNSYMMETRIC_NITSCHE or VW_GHOST */
+    int32_t iwg_type;             /* INTERFACE_SYMMETRIC / _UNSYMMETRIC_NITSCHE, VW_GHOST or GHOST_NORMAL_FIELD */
     int32_t facet_cell_type;      /* FEM_GPU_CELL_TRI3 or FEM_GPU_CELL_QUAD4 (3D only) */
     int32_t integration_rule;     /* TRI_3 / TRI_7 for triangles, QUAD_2x2 for quads */
     int32_t model_type;           /* FEM_GPU_MODEL_3D */
@@ -231,6 +241,15 @@ typedef struct fem_gpu_pcg_report {
 
 /* ---- library ------------------------------------------------------------ */
 int32_t fem_gpu_abi_version(void);
+/* The reference's automatic integration rule, Set::get_auto_integration_order
+   (FEM/INT/src/CORE/cl_FEM_Set.cpp:2983-3185): by set kind (FEM_GPU_SET_*),
+   the geometry of the integration cells (bulk: QUAD4, HEX8, TRI3, TET4;
+   sides: LINE2 or QUAD4 facets; double-sided: TRI3 or QUAD4 facets) and the
+   interpolation order of the interpolation cells (1 linear, 2 quadratic,
+   3 cubic).  FEM_GPU_UNSUPPORTED when the reference's choice is not one of
+   this library's rules (e.g. TET_35 for quadratic tetrahedra). */
+fem_gpu_status fem_gpu_auto_integration_rule(int32_t set_kind, int32_t cell_type, int32_t interpolation_order,
+                                             int32_t* rule);
 const char* fem_gpu_status_string(fem_gpu_status s);
 /* number of CUDA devices (0 without a GPU; never fails) */
 int32_t fem_gpu_device_count(void);

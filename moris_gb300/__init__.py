@@ -16,6 +16,8 @@ from ._lib import BulkSetDesc, DoubleSideSetDesc, MeshDesc, PcgOpts, PcgReport, 
 CELL_QUAD4, CELL_HEX8, CELL_TRI3, CELL_TET4, CELL_LINE2 = 0, 1, 2, 3, 4
 RULE_BAR_1, RULE_BAR_3, RULE_QUAD_2x2, RULE_HEX_2x2x2, RULE_HEX_3x3x3 = 0, 1, 2, 3, 4
 RULE_TRI_7, RULE_TET_4, RULE_TET_11, RULE_TRI_3 = 5, 6, 7, 8
+RULE_AUTO = -1
+SET_BULK, SET_SIDESET, SET_DOUBLE_SIDESET = 0, 1, 2
 MODEL_PLANE_STRAIN, MODEL_PLANE_STRESS, MODEL_3D = 0, 1, 2
 SHAPE_RECTANGULAR, SHAPE_GENERAL = 0, 1
 IWG_STRUC_LINEAR_BULK = 0
@@ -25,6 +27,7 @@ IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE = 3
 IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE = 4
 IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE = 5
 IWG_STRUC_LINEAR_VW_GHOST = 6
+IWG_GHOST_NORMAL_FIELD = 7
 HOST_BUFFERS, NO_JACOBIAN, NO_RESIDUAL, ACCUMULATE, ASYNC = 1, 2, 4, 8, 16
 
 
@@ -84,6 +87,15 @@ def bspline_tmatrix(num_coefs, lengths, order, points):
     if st:
         raise FemGpuError(st, "fem_gen_bspline_tmatrix")
     return cols, vals
+
+
+def auto_integration_rule(set_kind, cell, interpolation_order=1):
+    """The reference's automatic integration rule (Set::get_auto_integration_order)."""
+    r = C.c_int32()
+    st = lib().fem_gpu_auto_integration_rule(set_kind, cell, interpolation_order, C.byref(r))
+    if st:
+        raise FemGpuError(st, "fem_gpu_auto_integration_rule")
+    return r.value
 
 
 def probe_fp64_tflops(iters=20000):

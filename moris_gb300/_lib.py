@@ -72,6 +72,7 @@ class MgOpts(C.Structure):
 # check against include/fem_gpu.h
 SIGNATURES = {
     "fem_gpu_abi_version": (I32, []),
+    "fem_gpu_auto_integration_rule": (I32, [I32, I32, I32, P]),
     "fem_gpu_status_string": (C.c_char_p, [I32]),
     "fem_gpu_device_count": (I32, []),
     "fem_hmr_uniform_mesh": (I32, [I32, P, P, I32, P]),

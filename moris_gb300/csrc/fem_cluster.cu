@@ -467,7 +467,9 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
     uint8_t* TC = sb + Lo::bTC; // [2][NB]
     uint16_t* SL = reinterpret_cast<uint16_t*>(sb + Lo::bS);  // [2NB][2NB]
     const bool assemble = p.mode == CM_ASSEMBLE;
-    const bool ghost = S.iwg == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
+    // ghost penalties: virtual work (traction jump) or normal field (jump of du/dn)
+    const bool normal_field = S.iwg == FEM_GPU_IWG_GHOST_NORMAL_FIELD;
+    const bool ghost = S.iwg == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST || normal_field;
     const double beta = S.iwg == FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
     const int nbs[2] = {S.nb[2 * e], S.nb[2 * e + 1]};
     const double Es[2] = {S.E[e], S.EF[e]};
@@ -576,6 +578,26 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
                 const int kb = j % 24, i = (j / 24) % 3, pre = j / 72;  // pre = (s*8 + a)*2 + s'
                 KT[j] = fma(n[i], P[pre * 24 + kb], KT[j]);
             }
+        } else if (normal_field) {
+            // Normal-field ghost: per point the normal derivatives DN[s][a] = n . g_s[:, a]
+            // of both sides, then K[(s,f,a),(s',f,b)] += +-sum_q w* DN[s][a] DN[s'][b]
+            // (the same for every component f; gamma at the end)
+            for (int idx = tid; idx < ngp * 16; idx += TH) {
+                const int q = idx >> 4, sd_ = (idx >> 3) & 1, a = idx & 7;
+                const double* g = GG + (q * 2 + sd_) * 24;
+                GS[idx] = n[0] * g[a] + n[1] * g[8 + a] + n[2] * g[16 + a];
+            }
+            __syncthreads();
+            for (int j = 0; j < PER; ++j) {
+                const int idx = tid + j * TH;
+                const int r = idx / 48, c = idx % 48;
+                const int sr = r / 24, rr = r % 24, sc = c / 24, cc = c % 24;
+                if (rr / 8 != cc / 8) continue;
+                double v = 0.0;
+                for (int q = 0; q < ngp; ++q)
+                    v = fma(WQ[q] * GS[q * 16 + sr * 8 + rr % 8], GS[q * 16 + sc * 8 + cc % 8], v);
+                K[idx] = fma(sr == sc ? 1.0 : -1.0, v, K[idx]);
+            }
         } else {
             // Ghost: per point w* (n-projected strain) and the traction operators of
             // both sides, then K += sum_q sum_h GS_q[h]^T TR_q[h] (alpha h_G at the end)
@@ -645,8 +667,10 @@ __device__ void double_item(const ClusterArgs& p, const SetDev& S, const Item& i
             K[idx] = fma(sg, Q[((sr * 8 + rr % 8) * 2 + sc) * 8 + cc % 8], K[idx]);
         }
     } else {
-        // SP_Ghost_Virtual_Work: alpha h^(2(p-1)+1), p = 1, h = sqrt(4 A / pi)
-        const double gamma = S.alpha * sqrt(4.0 * SC[3] / 3.14159265358979323846);
+        // SP_Ghost_Virtual_Work: alpha h^(2(p-1)+1), p = 1, h = sqrt(4 A / pi);
+        // SP_Ghost_Displacement: the same times the leader's modulus
+        const double h = sqrt(4.0 * SC[3] / 3.14159265358979323846);
+        const double gamma = normal_field ? S.alpha * h * Es[0] : S.alpha * h;
         for (int j = 0; j < PER; ++j) K[tid + j * TH] *= gamma;
     }
     // pdof values of both sides

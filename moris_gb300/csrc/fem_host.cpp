@@ -103,6 +103,46 @@ extern "C" {
 
 int32_t fem_gpu_abi_version(void) { return FEM_GPU_ABI_VERSION; }
 
+// Set::get_auto_integration_order (FEM/INT/src/CORE/cl_FEM_Set.cpp:2983-3185):
+// rule tables per (set kind, integration geometry, interpolation order); -1
+// where the reference's choice is not a rule of this library
+fem_gpu_status fem_gpu_auto_integration_rule(int32_t set_kind, int32_t cell, int32_t order, int32_t* rule) {
+    if (!rule || order < 1 || order > 3) return FEM_GPU_BAD_ARG;
+    const int o = order - 1;
+    // entries: linear, quadratic, cubic
+    static const int bulk_line[3] = {FEM_GPU_RULE_BAR_3, -1, -1};           // BAR_3, BAR_4, BAR_5
+    static const int bulk_quad[3] = {FEM_GPU_RULE_QUAD_2x2, -1, -1};        // QUAD_2x2, QUAD_3x3, QUAD_5x5
+    static const int bulk_hex[3] = {FEM_GPU_RULE_HEX_2x2x2, FEM_GPU_RULE_HEX_3x3x3, -1};  // ..., HEX_4x4x4
+    static const int bulk_tri[3] = {FEM_GPU_RULE_TRI_7, -1, -1};            // TRI_7, TRI_12, TRI_25
+    static const int bulk_tet[3] = {FEM_GPU_RULE_TET_11, -1, -1};           // TET_11, TET_35, TET_56
+    static const int side_line[3] = {FEM_GPU_RULE_BAR_3, -1, -1};           // BAR_3, BAR_4, BAR_5
+    static const int side_quad[3] = {FEM_GPU_RULE_QUAD_2x2, -1, -1};        // QUAD_2x2, QUAD_4x4, QUAD_5x5
+    static const int side_tri[3] = {FEM_GPU_RULE_TRI_7, -1, -1};            // TRI_7, TRI_12, TRI_25
+    const int* t = nullptr;
+    if (set_kind == FEM_GPU_SET_BULK) {
+        switch (cell) {
+            case FEM_GPU_CELL_LINE2: t = bulk_line; break;
+            case FEM_GPU_CELL_QUAD4: t = bulk_quad; break;
+            case FEM_GPU_CELL_HEX8: t = bulk_hex; break;
+            case FEM_GPU_CELL_TRI3: t = bulk_tri; break;
+            case FEM_GPU_CELL_TET4: t = bulk_tet; break;
+            default: return FEM_GPU_BAD_ARG;
+        }
+    } else if (set_kind == FEM_GPU_SET_SIDESET || set_kind == FEM_GPU_SET_DOUBLE_SIDESET) {
+        switch (cell) {
+            case FEM_GPU_CELL_LINE2: t = side_line; break;
+            case FEM_GPU_CELL_QUAD4: t = side_quad; break;
+            case FEM_GPU_CELL_TRI3: t = side_tri; break;
+            default: return FEM_GPU_BAD_ARG;
+        }
+    } else {
+        return FEM_GPU_BAD_ARG;
+    }
+    if (t[o] < 0) return FEM_GPU_UNSUPPORTED;
+    *rule = t[o];
+    return FEM_GPU_OK;
+}
+
 const char* fem_gpu_status_string(fem_gpu_status s) {
     switch (s) {
         case FEM_GPU_OK: return "ok";
@@ -346,8 +386,11 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     // kept so that set indices stay those of the caller, and does no work
     if (d->num_clusters < 0 || (d->num_clusters > 0 && (!d->cluster_ip_cell || !d->youngs_modulus)))
         return fail(c, FEM_GPU_BAD_ARG, "bulk set arrays");
-    const Rule r = gauss_rule(d->integration_rule);
     const int igc = d->ig_cell_type;
+    int rule = d->integration_rule;
+    if (rule == FEM_GPU_RULE_AUTO && fem_gpu_auto_integration_rule(FEM_GPU_SET_BULK, igc, 1, &rule) != FEM_GPU_OK)
+        return fail(c, FEM_GPU_BAD_ARG, "no automatic integration rule for this integration cell");
+    const Rule r = gauss_rule(rule);
     if (r.n == 0 || cell_num_nodes(igc) == 0 || r.dim != cell_param_dim(igc))
         return fail(c, FEM_GPU_BAD_ARG, "integration rule does not match the integration cell");
     if (cell_param_dim(igc) != c->dim) return fail(c, FEM_GPU_BAD_ARG, "integration cell dimension");
@@ -359,6 +402,7 @@ fem_gpu_status fem_gpu_add_bulk_set(fem_gpu_ctx* c, const fem_gpu_bulk_set_desc*
     SetData s;
     s.kind = 0;
     s.bulk = *d;
+    s.bulk.integration_rule = rule;
     s.neq = d->num_clusters;
     s.ip_cell.assign(d->cluster_ip_cell, d->cluster_ip_cell + s.neq);
     for (auto v : s.ip_cell)
@@ -418,11 +462,16 @@ fem_gpu_status fem_gpu_add_side_set(fem_gpu_ctx* c, const fem_gpu_side_set_desc*
         return fail(c, FEM_GPU_UNSUPPORTED, "side iwg type");
     if (d->num_sides < 0 || (d->num_sides > 0 && (!d->side_ip_cell || !d->side_ordinal || !d->youngs_modulus)))
         return fail(c, FEM_GPU_BAD_ARG, "side set arrays");
-    const Rule r = gauss_rule(d->integration_rule);
+    int rule = d->integration_rule;
+    if (rule == FEM_GPU_RULE_AUTO)
+        fem_gpu_auto_integration_rule(FEM_GPU_SET_SIDESET, c->dim == 2 ? FEM_GPU_CELL_LINE2 : FEM_GPU_CELL_QUAD4, 1,
+                                      &rule);
+    const Rule r = gauss_rule(rule);
     if (r.n == 0 || r.dim != c->dim - 1) return fail(c, FEM_GPU_BAD_ARG, "side integration rule");
     SetData s;
     s.kind = 1;
     s.side = *d;
+    s.side.integration_rule = rule;
     if (d->thickness < 0.0 || !std::isfinite(d->thickness)) return fail(c, FEM_GPU_BAD_ARG, "side set thickness");
     s.side_thickness = d->thickness > 0.0 ? d->thickness : 1.0;
     if (d->select_matrix) {
@@ -459,15 +508,18 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
     if (c->host_final) return fail(c, FEM_GPU_BAD_ARG, "sets must be added before finalize");
     if (d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE &&
         d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE &&
-        d->iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST)
+        !is_ghost_iwg(d->iwg_type))
         return fail(c, FEM_GPU_UNSUPPORTED, "double-sided iwg type");
     if (c->dim != 3 || c->ip_cell != FEM_GPU_CELL_HEX8 || d->model_type != FEM_GPU_MODEL_3D)
         return fail(c, FEM_GPU_UNSUPPORTED, "double-sided sets need a 3D HEX8 model");
     if (d->facet_cell_type != FEM_GPU_CELL_TRI3 && d->facet_cell_type != FEM_GPU_CELL_QUAD4)
         return fail(c, FEM_GPU_BAD_ARG, "facet cell type");
-    const Rule r = gauss_rule(d->integration_rule);
+    int rule = d->integration_rule;
+    if (rule == FEM_GPU_RULE_AUTO)
+        fem_gpu_auto_integration_rule(FEM_GPU_SET_DOUBLE_SIDESET, d->facet_cell_type, 1, &rule);
+    const Rule r = gauss_rule(rule);
     if (r.n == 0 || r.dim != 2 || r.n > 9) return fail(c, FEM_GPU_BAD_ARG, "facet integration rule");
-    const bool tri_rule = d->integration_rule == FEM_GPU_RULE_TRI_3 || d->integration_rule == FEM_GPU_RULE_TRI_7;
+    const bool tri_rule = rule == FEM_GPU_RULE_TRI_3 || rule == FEM_GPU_RULE_TRI_7;
     if (tri_rule != (d->facet_cell_type == FEM_GPU_CELL_TRI3))
         return fail(c, FEM_GPU_BAD_ARG, "integration rule does not match the facet cell");
     if (d->num_clusters < 0 ||
@@ -480,6 +532,7 @@ fem_gpu_status fem_gpu_add_double_side_set(fem_gpu_ctx* c, const fem_gpu_double_
     SetData s;
     s.kind = 2;
     s.dside = *d;
+    s.dside.integration_rule = rule;
     s.neq = d->num_clusters;
     s.nfv = cell_num_nodes(d->facet_cell_type);
     s.ip_cell.assign(d->leader_ip_cell, d->leader_ip_cell + s.neq);
@@ -543,12 +596,12 @@ fem_gpu_status interface_volumes(fem_gpu_ctx* c) {
     std::vector<double> cell_vol;
     bool need_vol = false;
     for (auto& s : c->sets)
-        need_vol |= s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
+        need_vol |= s.kind == 2 && !is_ghost_iwg(s.dside.iwg_type);
     if (need_vol) {
         // only the cells that interface clusters name need a volume
         std::vector<char> needed(c->num_cells, 0);
         for (auto& s : c->sets) {
-            if (s.kind != 2 || s.dside.iwg_type == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST) continue;
+            if (s.kind != 2 || is_ghost_iwg(s.dside.iwg_type)) continue;
             for (auto v : s.ip_cell) needed[v] = 1;
             for (auto v : s.fcell) needed[v] = 1;
         }
@@ -582,7 +635,7 @@ fem_gpu_status interface_volumes(fem_gpu_ctx* c) {
         }
     }
     for (auto& s : c->sets) {
-        if (s.kind != 2 || s.dside.iwg_type == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST) continue;
+        if (s.kind != 2 || is_ghost_iwg(s.dside.iwg_type)) continue;
         s.vol.resize(s.neq * 2);
         for (int64_t i = 0; i < s.neq; ++i) {
             s.vol[i * 2] = cell_vol[s.ip_cell[i]];

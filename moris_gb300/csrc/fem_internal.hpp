@@ -121,6 +121,10 @@ struct fem_gpu_ctx {
 };
 
 namespace fem {
+// double-sided IWG families: the Nitsche interface (needs cluster volumes) or a ghost penalty
+inline bool is_ghost_iwg(int iwg) {
+    return iwg == FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST || iwg == FEM_GPU_IWG_GHOST_NORMAL_FIELD;
+}
 fem_gpu_status fail(fem_gpu_ctx* c, fem_gpu_status s, const std::string& msg);
 // multiprocessor count of the current device (cached per device; grid sizing)
 int sm_count();

@@ -490,7 +490,7 @@ double lam_of(int model, double nu) {
 
 bool is_cut(const SetData& s) { return s.kind == 0 && !s.ig_off.empty(); }
 bool is_interface(const SetData& s) {
-    return s.kind == 2 && s.dside.iwg_type != FEM_GPU_IWG_STRUC_LINEAR_VW_GHOST;
+    return s.kind == 2 && !is_ghost_iwg(s.dside.iwg_type);
 }
 
 }  // namespace

@@ -86,10 +86,13 @@ XFEM_GHOST_ALPHA = 0.01
 
 
 def xfem_sets(x, E=XFEM_E, nu=XFEM_NU, tet_rule=RULE_TET_4, tri_rule=RULE_TRI_7, hex_rule=RULE_HEX_2x2x2,
-              alpha_if=XFEM_NITSCHE_ALPHA, alpha_gh=XFEM_GHOST_ALPHA):
+              alpha_if=XFEM_NITSCHE_ALPHA, alpha_gh=XFEM_GHOST_ALPHA, ghost_iwg=IWG_STRUC_LINEAR_VW_GHOST,
+              ghost_rule=None):
     """Set list of a decomposed XFEM mesh (phase-wise elasticity, Nitsche
-    interface, virtual-work ghost), in the order bulk sets, then double-sided
-    sets: [(kind, args)], kind 'bulk' or 'double'.  Empty sets are left out."""
+    interface, ghost penalty: virtual work by default, or the normal-field
+    ghost with ghost_iwg = IWG_GHOST_NORMAL_FIELD), in the order bulk sets,
+    then double-sided sets: [(kind, args)], kind 'bulk' or 'double'.  Empty
+    sets are left out."""
     sets = []
     for p in (0, 1):
         c = x["uncut%d" % p]
@@ -113,10 +116,11 @@ def xfem_sets(x, E=XFEM_E, nu=XFEM_NU, tet_rule=RULE_TET_4, tri_rule=RULE_TRI_7,
         g = x["ghost%d" % p]
         n = len(g["leader"])
         if n:
-            sets.append(("double", dict(iwg=IWG_STRUC_LINEAR_VW_GHOST, leader=g["leader"], follower=g["follower"],
+            sets.append(("double", dict(iwg=ghost_iwg, leader=g["leader"], follower=g["follower"],
                                         offsets=g["offsets"], coords=g["coords"], leader_param=g["leader_param"],
                                         follower_param=g["follower_param"], EL=np.full(n, E[p]), EF=np.full(n, E[p]),
-                                        nu=nu, rule=RULE_QUAD_2x2, facet_cell=CELL_QUAD4, alpha=alpha_gh)))
+                                        nu=nu, rule=RULE_QUAD_2x2 if ghost_rule is None else ghost_rule,
+                                        facet_cell=CELL_QUAD4, alpha=alpha_gh)))
     return sets
 
 

@@ -535,6 +535,27 @@ static real bspline_shape(int p, int basis, real xi) {
 
 extern "C" {
 
+/* Set::get_auto_integration_order (FEM/INT/src/CORE/cl_FEM_Set.cpp:2983-3185)
+   for linear interpolation cells: the reference picks the rule from the set
+   type and the integration cell's geometry.  kind 0 bulk, 1 side set,
+   2 double side set; -1 if none.                                           */
+int orc_auto_rule(int kind, int cell) {
+    if (kind == 0) {
+        if (cell == ORC_CELL_LINE2) return ORC_RULE_BAR_3;
+        if (cell == ORC_CELL_QUAD4) return ORC_RULE_QUAD_2x2;
+        if (cell == ORC_CELL_HEX8) return ORC_RULE_HEX_2x2x2;
+        if (cell == ORC_CELL_TRI3) return ORC_RULE_TRI_7;
+        if (cell == ORC_CELL_TET4) return ORC_RULE_TET_11;
+        return -1;
+    }
+    if (kind == 1 || kind == 2) {
+        if (cell == ORC_CELL_LINE2) return ORC_RULE_BAR_3;
+        if (cell == ORC_CELL_QUAD4) return ORC_RULE_QUAD_2x2;
+        if (cell == ORC_CELL_TRI3) return ORC_RULE_TRI_7;
+    }
+    return -1;
+}
+
 int orc_rule_size(int rule, int* dim, int* npts) {
     RuleTab t = make_rule(rule);
     if (t.n == 0) return 1;
@@ -673,6 +694,7 @@ void orc_model_free(orc_model* m) { delete m; }
 int orc_model_add_bulk_set(orc_model* m, int ig_cell, int rule, int model, int64_t nc, const int32_t* ipc,
                            const int64_t* ig_off, const double* ig_coords, const double* ig_param,
                            const double* E, double nu) {
+    if (rule < 0) rule = orc_auto_rule(0, ig_cell);
     if (m->finalized) return 1;
     BulkSet s;
     s.ig_cell = ig_cell;
@@ -726,6 +748,7 @@ int orc_model_set_side_options(orc_model* m, int side_set, double thickness, con
 
 int orc_model_add_side_set(orc_model* m, int iwg, int rule, int model, int64_t ns, const int32_t* ipc,
                            const int32_t* ord, const double* E, double nu, double alpha, const double* value) {
+    if (rule < 0) rule = orc_auto_rule(1, m->dim == 2 ? ORC_CELL_LINE2 : ORC_CELL_QUAD4);
     if (m->finalized) return 1;
     SideSet s;
     s.iwg = iwg;
@@ -745,6 +768,7 @@ int orc_model_add_double_side_set(orc_model* m, int iwg, int facet_cell, int rul
                                   const int32_t* leader, const int32_t* follower, const int64_t* fc_off,
                                   const double* fc_x, const double* fc_xl, const double* fc_xf, const double* EL,
                                   const double* EF, double nu, double alpha) {
+    if (rule < 0) rule = orc_auto_rule(2, facet_cell);
     if (m->finalized) return 1;
     DoubleSet s;
     s.iwg = iwg;
@@ -1247,7 +1271,15 @@ Mat ghost_flat_normal_3d(const real* n) {
      50-244) with SP_Ghost_Virtual_Work::eval_SP (SP/cl_FEM_SP_Ghost_Virtual_
      Work.cpp:30-38): gamma = alpha h^(2(p-1)+1), p = 1, h the side length
      measure sqrt(4 A / pi) (Cluster::compute_cluster_cell_length_measure,
-     FEM/INT/src/ELEM/cl_FEM_Cluster.cpp:858-920).
+     FEM/INT/src/ELEM/cl_FEM_Cluster.cpp:858-920);
+   - IWG_Ghost_Normal_Field (FEM/INT/src/IWG/cl_FEM_IWG_Ghost_Normal_Field.cpp:
+     36-233) with SP_Ghost_Displacement::eval_SP (SP/cl_FEM_SP_Ghost_
+     Displacement.cpp:51-63): the penalty on the jump of the normal
+     derivative of every displacement component, order 1 (linear IP cells):
+       R_L += w gamma (dN_L/dn)_f [[du_f/dn]],  R_F -= w gamma (dN_F/dn)_f [[du_f/dn]],
+       K_ST = +-w gamma (dN_S/dn) (dN_T/dn)^T per component (+ for S = T),
+     gamma = alpha h^(2(1 - 1) + 1) E_L, E_L the leader's Material property,
+     h the same side length measure.
    Output K (48 x 48) and R (48) in [leader pdofs | follower pdofs], each
    type-major.                                                                */
 void double_pdof(const orc_model* m, const DoubleSet& s, int64_t eq, const Mat& updL, const Mat& updF, Mat& K,
@@ -1275,11 +1307,13 @@ void double_pdof(const orc_model* m, const DoubleSet& s, int64_t eq, const Mat& 
             facet_point(s, f, &rt.pts[(size_t)q * rt.dim], dj, n, Nf);
             area += rt.w[q] * dj;
         }
-    const bool ghost = s.iwg == ORC_IWG_STRUC_LINEAR_VW_GHOST;
+    const bool normal_field = s.iwg == ORC_IWG_GHOST_NORMAL_FIELD;
+    const bool ghost = s.iwg == ORC_IWG_STRUC_LINEAR_VW_GHOST || normal_field;
     real gamma, wl = 0.0, wf = 0.0;
     if (ghost) {
         const real h = std::pow(4.0 * area / M_PI, 1.0 / 2.0);
         gamma = s.alpha * std::pow(h, 2.0 * (1.0 - 1.0) + 1.0);
+        if (normal_field) gamma *= s.EL[eq];
     } else {
         const real VL = cell_cluster_volume(m, cl), VF = cell_cluster_volume(m, cf);
         const real deno = VL / s.EL[eq] + VF / s.EF[eq];
@@ -1311,6 +1345,30 @@ void double_pdof(const orc_model* m, const DoubleSet& s, int64_t eq, const Mat& 
             Mat Fn = flat_normal(n, d, 6);
             Mat tL = mul(Fn, mul(DL, BL)), tF = mul(Fn, mul(DF, BF));  // traction operators
             Mat tLt = trans(tL), tFt = trans(tF), NLt = trans(NL), NFt = trans(NF);
+            if (normal_field) {
+                // block-diagonal normal derivatives of the two sides
+                Mat gL(nd, d, 0.0), gF(nd, d, 0.0);
+                for (int fld = 0; fld < d; ++fld)
+                    for (int a = 0; a < npe; ++a) {
+                        real vl = 0.0, vf = 0.0;
+                        for (int k = 0; k < d; ++k) {
+                            vl += n[k] * dL(k, a);
+                            vf += n[k] * dF(k, a);
+                        }
+                        gL(fld * npe + a, fld) = vl;
+                        gF(fld * npe + a, fld) = vf;
+                    }
+                Mat jump = mul(trans(gL), uL);
+                add_scaled(jump, -1.0, mul(trans(gF), uF));
+                Mat gLt = trans(gL), gFt = trans(gF);
+                add_scaled(RL, w * gamma, mul(gL, jump));
+                add_scaled(RF, -w * gamma, mul(gF, jump));
+                add_scaled(KLL, w * gamma, mul(gL, gLt));
+                add_scaled(KFL, -w * gamma, mul(gF, gLt));
+                add_scaled(KLF, -w * gamma, mul(gL, gFt));
+                add_scaled(KFF, w * gamma, mul(gF, gFt));
+                continue;
+            }
             if (ghost) {
                 Mat FnM = ghost_flat_normal_3d(n);
                 Mat gL = trans(mul(FnM, BL)), gF = trans(mul(FnM, BF));  // B^T FnM^T

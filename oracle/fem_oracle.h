@@ -36,10 +36,14 @@ enum {
     ORC_IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE = 3,
     ORC_IWG_STRUC_LINEAR_INTERFACE_SYMMETRIC_NITSCHE = 4,
     ORC_IWG_STRUC_LINEAR_INTERFACE_UNSYMMETRIC_NITSCHE = 5,
-    ORC_IWG_STRUC_LINEAR_VW_GHOST = 6
+    ORC_IWG_STRUC_LINEAR_VW_GHOST = 6,
+    ORC_IWG_GHOST_NORMAL_FIELD = 7
 };
 
 /* ---- reference-element tables ---------------------------------------- */
+/* the reference's automatic integration rule of a set (kind 0 bulk, 1 side,
+   2 double side) with integration cells `cell`, linear interpolation cells */
+int orc_auto_rule(int kind, int cell);
 int orc_rule_size(int rule, int* dim, int* npts);
 /* points are stored one column per point (dim x npts, column-major) */
 int orc_rule(int rule, double* pts, double* weights);

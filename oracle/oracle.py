@@ -25,6 +25,7 @@ def load():
         path = _build.build()
         lib = C.CDLL(path)
         sig = {
+            "orc_auto_rule": (_I, [_I, _I]),
             "orc_rule_size": (_I, [_I, _P, _P]),
             "orc_rule": (_I, [_I, _P, _P]),
             "orc_cell_num_nodes": (_I, [_I]),
@@ -73,6 +74,10 @@ class OracleLib:
 
     def __init__(self):
         self.lib = load()
+
+    def auto_rule(self, kind, cell):
+        """the reference's automatic integration rule (kind 0 bulk, 1 side, 2 double)"""
+        return self.lib.orc_auto_rule(kind, cell)
 
     def rule(self, rule):
         dim, n = C.c_int(), C.c_int()

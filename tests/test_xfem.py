@@ -14,10 +14,16 @@ from common import RTOL, csr_row_rel_err, rel_err
 N_SMALL = 10
 
 
-def small_xfem(n=N_SMALL, seed=workloads.BASE_SEED + 3, nspheres=5, rmin=0.15, rmax=0.3, order=1):
+def small_xfem(n=N_SMALL, seed=workloads.BASE_SEED + 3, nspheres=5, rmin=0.15, rmax=0.3, order=1, **set_options):
     phi = workloads.sphere_field(n, seed, nspheres, rmin, rmax)
     x = xtk.decompose((n, n, n), (1.0, 1.0, 1.0), order, phi)
-    return x, workloads.xfem_sets(x)
+    return x, workloads.xfem_sets(x, **set_options)
+
+
+# the reference's automatic rules everywhere, and the normal-field ghost with
+# SP_Ghost_Displacement in place of the virtual-work ghost
+AUTO_NF = dict(tet_rule=mg.RULE_AUTO, tri_rule=mg.RULE_AUTO, hex_rule=mg.RULE_AUTO, ghost_rule=mg.RULE_AUTO,
+               ghost_iwg=mg.IWG_GHOST_NORMAL_FIELD)
 
 
 def oracle_of(x, sets):
@@ -124,8 +130,83 @@ def test_oracle_double_sided_jacobian_is_residual_derivative():
             assert np.max(np.abs(fd - col)) <= 1e-6 * max(1.0, np.max(np.abs(K)))
 
 
+def test_automatic_rules_match_the_oracle_table():
+    """Set::get_auto_integration_order (FEM/INT/src/CORE/cl_FEM_Set.cpp:2983-3185)
+    for linear interpolation cells: the library's table against the oracle's"""
+    from oracle import OracleLib
+    ol = OracleLib()
+    cells = (mg.CELL_LINE2, mg.CELL_QUAD4, mg.CELL_HEX8, mg.CELL_TRI3, mg.CELL_TET4)
+    for kind in (mg.SET_BULK, mg.SET_SIDESET, mg.SET_DOUBLE_SIDESET):
+        for cell in cells:
+            want = ol.auto_rule(kind, cell)
+            if want < 0:
+                with pytest.raises(mg.FemGpuError):
+                    mg.auto_integration_rule(kind, cell)
+            else:
+                assert mg.auto_integration_rule(kind, cell) == want, (kind, cell)
+    # the reference's named choices
+    assert mg.auto_integration_rule(mg.SET_BULK, mg.CELL_HEX8) == mg.RULE_HEX_2x2x2
+    assert mg.auto_integration_rule(mg.SET_BULK, mg.CELL_TET4) == mg.RULE_TET_11
+    assert mg.auto_integration_rule(mg.SET_DOUBLE_SIDESET, mg.CELL_TRI3) == mg.RULE_TRI_7
+    assert mg.auto_integration_rule(mg.SET_BULK, mg.CELL_HEX8, 2) == mg.RULE_HEX_3x3x3
+    with pytest.raises(mg.FemGpuError):  # TET_35 is not one of the library's rules
+        mg.auto_integration_rule(mg.SET_BULK, mg.CELL_TET4, 2)
+
+
+def test_oracle_normal_field_ghost_is_symmetric_and_consistent():
+    """IWG_Ghost_Normal_Field restated: K is the derivative of R, symmetric and
+    positive semi-definite (it is a penalty on the jump of du/dn)."""
+    x, sets = small_xfem(**AUTO_NF)
+    orc = oracle_of(x, sets)
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal(orc.num_adofs) * 1e-2
+    ghosts = [s for s, (k, a) in enumerate(sets) if k == "double" and a["iwg"] == mg.IWG_GHOST_NORMAL_FIELD]
+    assert ghosts
+    for s in ghosts:
+        for e in (0, orc.num_eq(s) - 1):
+            ids = orc.element_topology(s, e)
+            K, R = orc.element_matrices(s, e, u)
+            assert np.max(np.abs(K - K.T)) <= 1e-14 * np.max(np.abs(K))
+            assert np.min(np.linalg.eigvalsh(0.5 * (K + K.T))) >= -1e-12 * np.max(np.abs(K))
+            # R = K u_e (linear in u)
+            assert np.max(np.abs(R - K @ u[ids])) <= 1e-12 * np.max(np.abs(R))
+
+
 # ---------------------------------------------------------------------------
 # GPU parity
+
+@pytest.mark.gpu
+def test_xfem_automatic_rules_and_normal_field_ghost_match_oracle():
+    import torch
+    x, sets = small_xfem(**AUTO_NF)
+    prod = product_of(x, sets)
+    orc = oracle_of(x, sets)
+    rng = np.random.default_rng(6)
+    u = rng.standard_normal(prod.num_adofs)
+    for s in range(len(sets)):
+        ne = prod.num_eq(s)
+        K, R = prod.element_matrices(s, 0, ne, u)
+        for e in range(0, ne, max(1, ne // 40)):
+            Ko, Ro = orc.element_matrices(s, e, u)
+            idx = compact_index(prod, s, e)
+            assert rel_err(K[e][np.ix_(idx, idx)], Ko) <= RTOL, (s, e)
+            assert rel_err(R[e][idx], Ro) <= RTOL, (s, e)
+    vo, ro = orc.assemble(u)
+    rp, _ = prod.graph()
+    ud = torch.tensor(u, device="cuda")
+    vd = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rd = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble_batched(ud, vd, rd)
+    torch.cuda.synchronize()
+    assert csr_row_rel_err(rp, vd.cpu().numpy(), vo) <= RTOL
+    assert rel_err(rd.cpu().numpy(), ro) <= RTOL
+    # AUTO resolves to the reference's named rules: the same system as spelling them out
+    explicit = dict(tet_rule=mg.RULE_TET_11, tri_rule=mg.RULE_TRI_7, hex_rule=mg.RULE_HEX_2x2x2,
+                    ghost_rule=mg.RULE_QUAD_2x2, ghost_iwg=mg.IWG_GHOST_NORMAL_FIELD)
+    prod2 = product_of(x, workloads.xfem_sets(x, **explicit))
+    v2, r2 = prod2.assemble_host(u)
+    assert csr_row_rel_err(rp, v2, vo) <= RTOL and rel_err(r2, ro) <= RTOL
+
 
 @pytest.mark.gpu
 def test_xfem_element_matrices_match_oracle():

@@ -264,6 +264,48 @@ fem_gpu_status fem_hmr_mesh_arrays(const fem_hmr_mesh* m, double* node_coords, i
                                    int64_t* t_offsets, int32_t* t_bases, double* t_weights);
 fem_gpu_status fem_hmr_mesh_free(fem_hmr_mesh* m);
 
+/* ---- refined (hierarchical) HMR meshes ----------------------------------------
+   A graded tensor-product B-spline hierarchy with HMR's rules: ne domain
+   elements per direction and max(staircase_buffer, order) padding elements
+   around them (Parameters::get_padding_size, HMR/src/cl_HMR_Parameters.cpp:
+   418-423); refinement as Background_Mesh_Base::perform_refinement
+   (cl_HMR_Background_Mesh_Base.cpp:648-737: padding test of the queued domain
+   elements within `padding_refinement` -- HMR's ceil(max polynomial / 2) --
+   and the staircase buffer); basis states as BSpline_Mesh::
+   determine_basis_state (cl_HMR_BSpline_Mesh.hpp:738-807); element T matrices
+   as T_Matrix_Base::calculate_t_matrix, truncated or not (cl_HMR_T_Matrix_
+   Base.cpp:41-248).  Element and basis indices are domain-relative (padding
+   elements have negative indices); a level-l basis m has the support elements
+   m - order .. m per direction. */
+typedef struct fem_hmr_refined fem_hmr_refined;
+fem_gpu_status fem_hmr_refined_create(int32_t spatial_dim, const int32_t* num_elements, const double* lengths,
+                                      int32_t bspline_order, int32_t staircase_buffer, int32_t padding_refinement,
+                                      fem_hmr_refined** out);
+fem_gpu_status fem_hmr_refined_free(fem_hmr_refined* m);
+/* one perform_refinement of the given active domain elements (levels[count],
+   ijk[count][dim]) with the buffers above */
+fem_gpu_status fem_hmr_refined_refine(fem_hmr_refined* m, int64_t count, const int32_t* levels, const int32_t* ijk);
+/* the active domain elements in HMR's order (coarsest elements x fastest,
+   each followed by its active descendants, children x fastest); NULL arrays =
+   count only */
+fem_gpu_status fem_hmr_refined_active_elements(const fem_hmr_refined* m, int64_t* count, int32_t* levels,
+                                               int32_t* ijk);
+/* the T matrix of one element: T[(order+1)^dim][ndof] row-major, rows in the
+   element-local basis order of HMR's B-spline elements (HMR/src/cl_HMR_BSpline_
+   Element_*.hpp), columns the active (truncated) bases that support the
+   element, in calculate_t_matrix's order, with their level and ijk.  All
+   output pointers NULL = size query (*ndof); capacity = columns of T. */
+fem_gpu_status fem_hmr_refined_element_t_matrix(const fem_hmr_refined* m, int32_t level, const int32_t* ijk,
+                                                int32_t truncate, int32_t capacity, int32_t* ndof, double* T,
+                                                int32_t* dof_level, int32_t* dof_ijk);
+/* The Lagrange mesh of the active domain elements (QUAD4 / HEX8 cells in the
+   order of fem_hmr_refined_active_elements, nodes numbered by first visit)
+   with the extraction row of every node over the active bases (ids ordered by
+   level, then z, y, x): T_Matrix_Base::evaluate (cl_HMR_T_Matrix_Base.cpp:
+   306-457).  Read it with fem_hmr_mesh_sizes / fem_hmr_mesh_arrays; it feeds
+   fem_gpu_create like the uniform mesh (cells are axis-aligned bricks). */
+fem_gpu_status fem_hmr_refined_mesh(const fem_hmr_refined* m, int32_t truncate, fem_hmr_mesh** out);
+
 /* ---- XFEM decomposition of a uniform level-0 HEX8 mesh (host only) -------
    Input of the cut-cell path, standing in for the reference's XTK
    (XTK/src/cl_XTK_Model.cpp:690 decompose; 24-tet regular subdivision,

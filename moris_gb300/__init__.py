@@ -139,6 +139,86 @@ def hmr_uniform_mesh(dim, num_elements, lengths, bspline_order):
                 t_bases=t_b, t_w=t_w)
 
 
+def _mesh_dict(L, h, dim):
+    nn, nc, nb, nz = (C.c_int64() for _ in range(4))
+    L.fem_hmr_mesh_sizes(h, C.byref(nn), C.byref(nc), C.byref(nb), C.byref(nz))
+    npe = 4 if dim == 2 else 8
+    coords = np.zeros(nn.value * dim)
+    cells = np.zeros(nc.value * npe, dtype=np.int32)
+    t_off = np.zeros(nn.value + 1, dtype=np.int64)
+    t_b = np.zeros(nz.value, dtype=np.int32)
+    t_w = np.zeros(nz.value)
+    L.fem_hmr_mesh_arrays(h, _np_ptr(coords), _np_ptr(cells), _np_ptr(t_off), _np_ptr(t_b), _np_ptr(t_w))
+    L.fem_hmr_mesh_free(h)
+    return dict(coords=coords.reshape(-1, dim), cells=cells.reshape(-1, npe), num_bases=nb.value, t_off=t_off,
+                t_bases=t_b, t_w=t_w)
+
+
+class RefinedHmr:
+    """A refined (hierarchical) HMR B-spline mesh (fem_hmr_refined_*):
+    refine active domain elements level by level, query element T matrices,
+    and produce the Lagrange mesh with node extraction rows for FemModel."""
+
+    def __init__(self, dim, num_elements, lengths, order, staircase_buffer=None, padding_refinement=None):
+        self.L = lib()
+        self.dim, self.order = dim, order
+        buf = order if staircase_buffer is None else staircase_buffer
+        pr = (order + 1) // 2 if padding_refinement is None else padding_refinement
+        ne = np.ascontiguousarray(num_elements, dtype=np.int32)
+        ln = np.ascontiguousarray(lengths, dtype=np.float64)
+        h = C.c_void_p()
+        st = self.L.fem_hmr_refined_create(dim, _np_ptr(ne), _np_ptr(ln), order, buf, pr, C.byref(h))
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.fem_hmr_refined_free(self.h)
+            self.h = None
+
+    def refine(self, elements):
+        """elements: [(level, ijk)] of active domain elements (domain-relative ijk)"""
+        lv = np.ascontiguousarray([l for l, _ in elements], dtype=np.int32)
+        ijk = np.ascontiguousarray([list(e) for _, e in elements], dtype=np.int32).ravel()
+        st = self.L.fem_hmr_refined_refine(self.h, len(lv), _np_ptr(lv), _np_ptr(ijk))
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_refine")
+
+    def active_elements(self):
+        n = C.c_int64()
+        self.L.fem_hmr_refined_active_elements(self.h, C.byref(n), None, None)
+        lv = np.zeros(n.value, dtype=np.int32)
+        ijk = np.zeros(n.value * self.dim, dtype=np.int32)
+        self.L.fem_hmr_refined_active_elements(self.h, C.byref(n), _np_ptr(lv), _np_ptr(ijk))
+        return lv, ijk.reshape(-1, self.dim)
+
+    def element_t_matrix(self, level, ijk, truncate):
+        """(T [(order+1)^dim, ndof], dof levels [ndof], dof ijk [ndof, dim])"""
+        e = np.ascontiguousarray(ijk, dtype=np.int32)
+        nd = C.c_int32()
+        st = self.L.fem_hmr_refined_element_t_matrix(self.h, level, _np_ptr(e), int(truncate), 0, C.byref(nd), None,
+                                                    None, None)
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_element_t_matrix")
+        n, B = nd.value, (self.order + 1) ** self.dim
+        T = np.zeros(B * max(n, 1))
+        dl = np.zeros(max(n, 1), dtype=np.int32)
+        di = np.zeros(max(n, 1) * self.dim, dtype=np.int32)
+        st = self.L.fem_hmr_refined_element_t_matrix(self.h, level, _np_ptr(e), int(truncate), n, C.byref(nd),
+                                                    _np_ptr(T), _np_ptr(dl), _np_ptr(di))
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_element_t_matrix")
+        return T[:B * n].reshape(B, n), dl[:n], di[:n * self.dim].reshape(n, self.dim)
+
+    def mesh(self, truncate=True):
+        h = C.c_void_p()
+        st = self.L.fem_hmr_refined_mesh(self.h, int(truncate), C.byref(h))
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_mesh")
+        return _mesh_dict(self.L, h, self.dim)
+
+
 class FemModel:
     """A context of libfem_gpu: one interpolation mesh, its sets, the CSR graph."""
 

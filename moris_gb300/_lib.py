@@ -72,6 +72,12 @@ class MgOpts(C.Structure):
 # check against include/fem_gpu.h
 SIGNATURES = {
     "fem_gpu_abi_version": (I32, []),
+    "fem_hmr_refined_create": (I32, [I32, P, P, I32, I32, I32, P]),
+    "fem_hmr_refined_free": (I32, [P]),
+    "fem_hmr_refined_refine": (I32, [P, I64, P, P]),
+    "fem_hmr_refined_active_elements": (I32, [P, P, P, P]),
+    "fem_hmr_refined_element_t_matrix": (I32, [P, I32, P, I32, I32, P, P, P, P]),
+    "fem_hmr_refined_mesh": (I32, [P, I32, P]),
     "fem_gpu_auto_integration_rule": (I32, [I32, I32, I32, P]),
     "fem_gpu_status_string": (C.c_char_p, [I32]),
     "fem_gpu_device_count": (I32, []),

@@ -87,16 +87,6 @@ double bspline_value(int p, int j, double xi) {
 }  // namespace
 }  // namespace fem
 
-struct fem_hmr_mesh {
-    int dim = 0;
-    int64_t num_bases = 0;
-    std::vector<double> coords;
-    std::vector<int32_t> cells;
-    std::vector<int64_t> t_off;
-    std::vector<int32_t> t_bases;
-    std::vector<double> t_w;
-};
-
 using namespace fem;
 
 extern "C" {

@@ -87,6 +87,18 @@ struct SetData {
 
 }  // namespace fem
 
+// Lagrange interpolation mesh with the extraction rows of its nodes
+// (fem_hmr_uniform_mesh, fem_hmr_refined_mesh)
+struct fem_hmr_mesh {
+    int dim = 0;
+    int64_t num_bases = 0;
+    std::vector<double> coords;
+    std::vector<int32_t> cells;
+    std::vector<int64_t> t_off;
+    std::vector<int32_t> t_bases;
+    std::vector<double> t_w;
+};
+
 struct fem_gpu_ctx {
     int dim = 0, ip_cell = 0, shape = 0, npe = 0;
     int64_t num_nodes = 0, num_cells = 0, num_bases = 0;

@@ -17,7 +17,9 @@ reference's plane-strain example (``projects/EXA/structure/linear/Plane_Strain/
 reader) into ``plane_strain_4elements.json``: node coordinates, 0-based cell
 connectivity and the side sets as (cell, side ordinal) pairs, where the
 ordinal is the Exodus side number minus one (side k joins local nodes k and
-k+1).  Nothing at test time reads the reference.
+k+1).  And it copies HMR's T-matrix fixture (``projects/HMR/test/data/
+T-Matrix_test_values.hdf5``, read by ``tests/hdf5_min.py``).  Nothing at test
+time reads the reference.
 """
 import json
 import os
@@ -79,6 +81,9 @@ def main(ref):
     data = os.path.join(ref, "projects", "FEM", "INT", "test", "data")
     for b in BINS:
         shutil.copyfile(os.path.join(data, b), os.path.join(here, b))
+    # HMR's T-matrix fixture (HDF5, read by tests/hdf5_min.py)
+    shutil.copyfile(os.path.join(ref, "projects", "HMR", "test", "data", "T-Matrix_test_values.hdf5"),
+                    os.path.join(here, "T-Matrix_test_values.hdf5"))
     src = open(os.path.join(ref, "projects", "FEM", "INT", "test", "FEM_Test_Proxy",
                             "cl_FEM_Inputs_for_Elasticity_UT.cpp")).read()
     out = {}

@@ -452,14 +452,14 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         if (need_u)
             for (int x = tid; x < NAD; x += NT) {
                 // count order: the lanes of a warp share trip counts
-                const int sl = x / D, f = x - sl * D, i = CP[sl], r = f * NB + i;
+                const int sl = x / D, f = x - sl * D, i = CP[sl];
                 const double s = fem_tdot(TCP[sl], TW + sl * NPE, TN + sl * NPE, RP + f * NPE, 1);
                 if (assemble) {
                     if (i < nb) atomicAdd(p.rhs + f * p.nu + B[i], s);
                 } else if (apply) {
                     if (i < nb) atomicAdd(p.y + f * p.nu + B[i], s);
-                } else {
-                    p.Rout[(e - p.first) * p.nmax + r] = s;
+                } else if (i < p.kw) {
+                    p.Rout[(e - p.first) * p.nmax + f * p.kw + i] = s;
                 }
             }
         if (want_k) {
@@ -481,7 +481,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                     atomicAdd(p.vals + RG[x * D + gg] + S[sr * NB + sc], v);
                     if (x != y) atomicAdd(p.vals + RG[y * D + f] + S[sc * NB + sr], v);
                 } else {
-                    const int r = f * NB + CP[sr], c = gg * NB + CP[sc];
+                    // rows and columns in the set's padding width (Kout's layout)
+                    const int r = f * p.kw + CP[sr], c = gg * p.kw + CP[sc];
                     double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
                     Ko[r + (int64_t)c * p.nmax] = v;
                     Ko[c + (int64_t)r * p.nmax] = v;

@@ -96,6 +96,7 @@ struct BulkArgs {
     double* Kout;         // element matrices [count][nmax][nmax] col-major (nullable)
     double* Rout;         // element residuals [count][nmax]
     int nmax;
+    int kw;               // basis stride of Kout / Rout rows (the set's padding width, <= NB)
     const double* x;      // apply mode input (adof)
     double* y;            // apply mode output (adof)
     int* status;          // device error flags
@@ -379,8 +380,8 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
                     for (int k = 0; k < TC[i]; ++k) s = fma(TW[i * NPE + k], RP[f * NPE + TN[i * NPE + k]], s);
                 if (mode == MODE_ASSEMBLE) {
                     if (i < nb) atomicAdd(p.rhs + f * p.nu + B[i], s);
-                } else {
-                    p.Rout[(e - p.first) * p.nmax + r] = s;
+                } else if (i < p.kw) {
+                    p.Rout[(e - p.first) * p.nmax + f * p.kw + i] = s;
                 }
             }
         }
@@ -424,8 +425,9 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
                     if (c != r) atomicAdd(p.vals + RB[c] + f * UL[j] + S[j * NB + i], v);
                 } else {
                     double* Ko = p.Kout + (e - p.first) * (int64_t)p.nmax * p.nmax;
-                    Ko[r + (int64_t)c * p.nmax] = v;
-                    Ko[c + (int64_t)r * p.nmax] = v;
+                    const int ro = f * p.kw + i, co = gg * p.kw + j;
+                    Ko[ro + (int64_t)co * p.nmax] = v;
+                    Ko[co + (int64_t)ro * p.nmax] = v;
                 }
             }
         }
@@ -971,6 +973,7 @@ fem_gpu_status launch_bulk(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.Kout = Kout;
     a.Rout = Rout;
     a.nmax = nmax;
+    a.kw = s.maxnb;
     a.x = x;
     a.y = y;
     a.status = status_ptr(c);

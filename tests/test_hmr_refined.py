@@ -148,12 +148,16 @@ def test_assembly_on_refined_mesh_matches_oracle(torch, case):
     assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
     u = np.random.default_rng(5).uniform(-1.0, 1.0, prod.num_adofs)
     K, R = prod.element_matrices(0, 0, nc, u)
+    width = prod.max_element_adofs(0) // d  # the padded layout: row f * width + i
     for eq in range(nc):
         ids = orc.element_topology(0, eq)
         assert np.array_equal(prod.element_topology(0, eq), ids)
         Ko, Ro = orc.element_matrices(0, eq, u)
-        n = len(ids)
-        assert rel_err(K[eq, :n, :n], Ko) <= RTOL and rel_err(R[eq, :n], Ro) <= RTOL
+        nb = len(ids) // d
+        idx = np.array([f * width + i for f in range(d) for i in range(nb)])
+        assert rel_err(K[eq][np.ix_(idx, idx)], Ko) <= RTOL and rel_err(R[eq][idx], Ro) <= RTOL
+        pad = np.setdiff1d(np.arange(d * width), idx)
+        assert not K[eq][pad].any() and not K[eq][:, pad].any() and not R[eq][pad].any()
     vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
     rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
     prod.assemble(torch.tensor(u, device="cuda"), vals, rhs)

@@ -31,7 +31,9 @@ inline void check(fem_gpu_status s, fem_gpu_ctx* c, const char* what) {
 
 class Gpu_Solver_Interface {
   public:
-    explicit Gpu_Solver_Interface(const fem_gpu_mesh_desc& mesh) { check(fem_gpu_create(&mesh, &ctx_), nullptr, "fem_gpu_create"); }
+    explicit Gpu_Solver_Interface(const fem_gpu_mesh_desc& mesh) : dim_(mesh.spatial_dim) {
+        check(fem_gpu_create(&mesh, &ctx_), nullptr, "fem_gpu_create");
+    }
     ~Gpu_Solver_Interface() { fem_gpu_destroy(ctx_); }
     Gpu_Solver_Interface(const Gpu_Solver_Interface&) = delete;
     Gpu_Solver_Interface& operator=(const Gpu_Solver_Interface&) = delete;
@@ -44,6 +46,11 @@ class Gpu_Solver_Interface {
     int add_side_set(const fem_gpu_side_set_desc& d) {
         int32_t i = -1;
         check(fem_gpu_add_side_set(ctx_, &d, &i), ctx_, "add_side_set");
+        return i;
+    }
+    int add_double_side_set(const fem_gpu_double_side_set_desc& d) {
+        int32_t i = -1;
+        check(fem_gpu_add_double_side_set(ctx_, &d, &i), ctx_, "add_double_side_set");
         return i;
     }
     void finalize() {
@@ -64,7 +71,8 @@ class Gpu_Solver_Interface {
         check(fem_gpu_get_element_topology(ctx_, set, eq, ids.data(), &n), ctx_, "element_topology");
         ids.resize(n);
     }
-    // element operator (column-major, nmax x nmax, zero padded) and residual
+    // element operator (column-major, nmax x nmax, zero padded: row f * width +
+    // i, width = nmax / dim, for bulk and side sets) and residual
     void get_equation_object_operator_and_rhs(int set, long eq, const double* u_adof_host, std::vector<double>& K,
                                               std::vector<double>& R) {
         int32_t nmax = 0;
@@ -85,12 +93,14 @@ class Gpu_Solver_Interface {
               "assemble");
     }
 
+    int spatial_dim() const { return dim_; }
     int64_t num_adofs() const { return num_adofs_; }
     int64_t nnz() const { return nnz_; }
     fem_gpu_ctx* handle() { return ctx_; }
 
   private:
     fem_gpu_ctx* ctx_ = nullptr;
+    int dim_ = 0;
     int64_t num_adofs_ = 0, nnz_ = 0;
     int32_t num_sets_ = 0;
 };

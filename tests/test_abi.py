@@ -50,3 +50,23 @@ def test_cpp_layer_compiles():
         r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), f],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_moris_adapter_links_against_the_library():
+    """The integration program (tests/cpp/solver_interface_main.cpp: a
+    Solver_Interface subclass over include/fem_gpu_moris_adapter.hpp, with the
+    reference's signatures for Matrix, Dist_Matrix and Dist_Vector) compiles
+    and links against libfem_gpu.so."""
+    import shutil
+    import subprocess
+    import tempfile
+    import pytest
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    with tempfile.TemporaryDirectory() as d:
+        r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"),
+                            "-I", os.path.join(ROOT, "tests", "cpp"),
+                            os.path.join(ROOT, "tests", "cpp", "solver_interface_main.cpp"),
+                            "-L", os.path.join(ROOT, "moris_gb300", "_build"), "-lfem_gpu",
+                            "-o", os.path.join(d, "si")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr

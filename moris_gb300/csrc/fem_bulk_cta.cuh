@@ -328,13 +328,32 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             }
         if (RECT && p.rho) {
             // density-weighted reference Gram matrix of this element
-            for (int k = tid; k < NSYM; k += NT) {
-                const uint32_t pc = __ldg(pairs + k);
-                const int r = pc >> 16, c = pc & 0xffff;
-                double s = 0.0;
-                for (int q = 0; q < NGP; ++q) s = fma(WS[q] * __ldg(p.dn + q * NPD + r), __ldg(p.dn + q * NPD + c), s);
-                A[r * NPD + c] = s;
-                A[c * NPD + r] = s;
+            if (!L::A_IN_R1) {
+                // the weighted gradients w_q E(x_q) dN_r(x_q) once per point, in the
+                // region of the general-cell gradients (unused by bricks): one FMA
+                // per Gram term instead of a multiply and an FMA
+                double* WDN = g;
+                for (int i = tid; i < NGP * NPD; i += NT) WDN[i] = WS[i / NPD] * __ldg(p.dn + i);
+                __syncthreads();
+                for (int k = tid; k < NSYM; k += NT) {
+                    const uint32_t pc = __ldg(pairs + k);
+                    const int r = pc >> 16, c = pc & 0xffff;
+                    double s = 0.0;
+#pragma unroll 4
+                    for (int q = 0; q < NGP; ++q) s = fma(WDN[q * NPD + r], __ldg(p.dn + q * NPD + c), s);
+                    A[r * NPD + c] = s;
+                    A[c * NPD + r] = s;
+                }
+            } else {
+                for (int k = tid; k < NSYM; k += NT) {
+                    const uint32_t pc = __ldg(pairs + k);
+                    const int r = pc >> 16, c = pc & 0xffff;
+                    double s = 0.0;
+                    for (int q = 0; q < NGP; ++q)
+                        s = fma(WS[q] * __ldg(p.dn + q * NPD + r), __ldg(p.dn + q * NPD + c), s);
+                    A[r * NPD + c] = s;
+                    A[c * NPD + r] = s;
+                }
             }
         }
         if (!RECT) {

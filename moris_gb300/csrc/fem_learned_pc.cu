@@ -11,19 +11,26 @@
 //         positively homogeneous and the scaling by s is exact).
 // Weights are kept as FP32 masters and used as BF16; activations are BF16,
 // accumulation FP32.  Forward and data-gradient convolutions are implicit
-// GEMMs on the tensor cores (mma.sync m16n8k16 bf16): M = 16 voxels per warp,
-// N = output channels, K = 27 taps x input channels.  The weight gradient is
+// GEMMs on the 5th-generation tensor cores (tcgen05.mma with TMEM
+// accumulators and TMA-fed operand tiles, fem_conv_umma.cuh): M = 128 voxels,
+// N = output channels, K = 27 taps x input channels.  The warp-level
+// mma.sync m16n8k16 kernel below stays as the reference of the tensor-core
+// path in the tests (FEM_CNN_CONV_KERNEL selects it).  The weight gradient is
 // an FP32 reduction over voxels.  Training (Adam) runs on the GPU; the
 // flexible CG that uses the net is fem_gpu_fcg.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include <mutex>
+
+#include "fem_conv_umma.cuh"
 #include "fem_internal.hpp"
 #include "fem_spmv.cuh"
 
@@ -249,6 +256,8 @@ struct fem_cnn {
     int64_t step = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ready = nullptr;  // joins the net's stream to the legacy default stream
+    int* d_status = nullptr;  // bounded waits of the tensor-core convolution (bit 2)
+    int conv_kernel = 0;      // 0 tcgen05 (default), 1 mma.sync
     bool dirty = true;        // bf16 copies need refresh
     double out_scale = 1.0;   // the correction applied by fem_gpu_fcg is out_scale * f
 };
@@ -262,25 +271,85 @@ fem_gpu_status cnn_pack(fem_cnn* c) {
     return cudaGetLastError() == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
 }
 
-void conv(fem_cnn* c, int nb, const __nv_bfloat16* in, int cin, int cout, const __nv_bfloat16* w, int sign, int relu,
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on the driver library)
+EncodeTiled encode_tiled() {
+    static EncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(f);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// the channels-last tensor (C, x, y, z, sample) of one activation buffer and
+// the box of one 8-channel chunk of a tile's halo block
+bool conv_tensor_map(CUtensorMap* map, const __nv_bfloat16* in, int nb, int n, int C) {
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t e = 2;  // bytes per BF16
+    const cuuint64_t dims[5] = {(cuuint64_t)C, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)nb};
+    const cuuint64_t strides[4] = {C * e, (cuuint64_t)n * C * e, (cuuint64_t)n * n * C * e,
+                                   (cuuint64_t)n * n * n * C * e};
+    const cuuint32_t box[5] = {8, fem_umma::kHx, fem_umma::kHy, 3, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16*>(in), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool conv(fem_cnn* c, int nb, const __nv_bfloat16* in, int cin, int cout, const __nv_bfloat16* w, int sign, int relu,
           const __nv_bfloat16* mask, __nv_bfloat16* out_bf, float* out_f) {
-    ConvArgs a{nb, c->n, cin, cout, in, w, sign, relu, mask, out_bf, out_f};
-    const int64_t tiles = ((int64_t)nb * c->V + 15) / 16;
-    const int threads = 128;
-    const unsigned blocks = (unsigned)((tiles * 32 + threads - 1) / threads);
-    conv_mma_kernel<<<blocks, threads, 0, c->stream>>>(a);
+    if (c->conv_kernel == 1) {
+        ConvArgs a{nb, c->n, cin, cout, in, w, sign, relu, mask, out_bf, out_f};
+        const int64_t tiles = ((int64_t)nb * c->V + 15) / 16;
+        const int threads = 128;
+        const unsigned blocks = (unsigned)((tiles * 32 + threads - 1) / threads);
+        conv_mma_kernel<<<blocks, threads, 0, c->stream>>>(a);
+        return cudaGetLastError() == cudaSuccess;
+    }
+    CUtensorMap map;
+    if (!conv_tensor_map(&map, in, nb, c->n, cin)) return false;
+    fem_umma::UmmaConvArgs a{nb, c->n, cin, cout, sign, relu, w, mask, out_bf, out_f, c->d_status};
+    const size_t smem = fem_umma::smem_bytes(cin, cout);
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(fem_umma::conv_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)fem_umma::smem_bytes(32, 32));
+    });
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fem_umma::conv_umma_kernel, fem_umma::kThreads, smem);
+    const int n = c->n;
+    const int64_t tiles = (int64_t)nb * n * ((n + fem_umma::kTy - 1) / fem_umma::kTy) *
+                          ((n + fem_umma::kTx - 1) / fem_umma::kTx);
+    const int64_t grid = std::min<int64_t>(tiles, (int64_t)fem::sm_count() * std::max(per_sm, 1));
+    fem_umma::conv_umma_kernel<<<(unsigned)grid, fem_umma::kThreads, smem, c->stream>>>(map, a);
+    return cudaGetLastError() == cudaSuccess;
 }
 
 // forward of nb samples already packed in act[0]
-void cnn_forward(fem_cnn* c, int nb) {
+bool cnn_forward(fem_cnn* c, int nb) {
+    bool ok = true;
     for (int l = 0; l < kLayers; ++l) {
         const bool last = l == kLayers - 1;
-        conv(c, nb, c->act[l], pad16(kCin[l]), pad16(kCout[l]), c->wf[l], +1, last ? 0 : 1, nullptr,
-             last ? nullptr : c->act[l + 1], last ? c->y : nullptr);
+        ok &= conv(c, nb, c->act[l], pad16(kCin[l]), pad16(kCout[l]), c->wf[l], +1, last ? 0 : 1, nullptr,
+                   last ? nullptr : c->act[l + 1], last ? c->y : nullptr);
     }
+    return ok;
 }
 
-void cnn_backward(fem_cnn* c, int nb) {
+bool cnn_backward(fem_cnn* c, int nb) {
+    bool ok = true;
     // grad[kLayers] holds dL/dy (bf16, 16 channels)
     cudaMemsetAsync(c->gw, 0, sizeof(float) * c->off[kLayers], c->stream);
     const int64_t total = (int64_t)nb * c->V;
@@ -290,9 +359,25 @@ void cnn_backward(fem_cnn* c, int nb) {
         conv_wgrad_kernel<<<grid, 256, 0, c->stream>>>(nb, c->n, pad16(kCin[l]), pad16(kCout[l]), kCin[l], kCout[l],
                                                        c->act[l], c->grad[l + 1], c->gw + c->off[l], vpb);
         if (l > 0)  // data gradient, masked by the ReLU of layer l-1's output
-            conv(c, nb, c->grad[l + 1], pad16(kCout[l]), pad16(kCin[l]), c->wt[l], -1, 0, c->act[l], c->grad[l],
-                 nullptr);
+            ok &= conv(c, nb, c->grad[l + 1], pad16(kCout[l]), pad16(kCin[l]), c->wt[l], -1, 0, c->act[l],
+                       c->grad[l], nullptr);
     }
+    return ok;
+}
+
+// the end of a net call: a launch that failed, a CUDA error, or a bounded
+// wait of the tensor-core convolution that expired (status bit 2)
+fem_gpu_status cnn_finish(fem_cnn* c, cudaError_t e, bool launched) {
+    if (!launched) return FEM_GPU_CUDA_ERROR;
+    int st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return FEM_GPU_CUDA_ERROR;
+    if (st) {
+        cudaMemset(c->d_status, 0, sizeof(int));
+        return FEM_GPU_TIMEOUT;
+    }
+    return FEM_GPU_OK;
 }
 
 // the net runs on its own stream; its inputs are produced on the legacy default
@@ -361,6 +446,13 @@ fem_gpu_status fem_cnn_create(int32_t n, int32_t batch_max, uint64_t seed, fem_c
     }
     if (e == cudaSuccess) e = cudaMalloc(&c->y, vox * kPad * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&c->loss, sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(int));
+    {
+        // FEM_CNN_CONV_KERNEL=mma selects the warp-level mma.sync convolution
+        const char* k = std::getenv("FEM_CNN_CONV_KERNEL");
+        c->conv_kernel = (k && std::string(k) == "mma") ? 1 : 0;
+    }
     if (e == cudaSuccess) e = cudaMemcpy(c->wm, c->host_master.data(), nw * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(c->am, 0, nw * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(c->av, 0, nw * sizeof(float));
@@ -390,6 +482,7 @@ fem_gpu_status fem_cnn_destroy(fem_cnn* c) {
     }
     cudaFree(c->y);
     cudaFree(c->loss);
+    cudaFree(c->d_status);
     if (c->ready) cudaEventDestroy(c->ready);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -430,11 +523,10 @@ fem_gpu_status fem_cnn_forward(fem_cnn* c, const float* in4, int32_t nb, float* 
     const int64_t vox = (int64_t)nb * c->V;
     after_default_stream(c);
     pack_input_kernel<<<256, 256, 0, c->stream>>>(vox, in4, c->act[0]);
-    cnn_forward(c, nb);
+    const bool ok = cnn_forward(c, nb);
     cudaError_t e = cudaMemcpy2DAsync(y3, 3 * sizeof(float), c->y, kPad * sizeof(float), 3 * sizeof(float), vox,
                                       cudaMemcpyDeviceToDevice, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
+    return cnn_finish(c, e, ok);
 }
 
 // loss = sum (y - target)^2 / (nb*V*3) and its weight gradient (no update);
@@ -446,17 +538,16 @@ fem_gpu_status fem_cnn_loss_grad(fem_cnn* c, const float* in4, const float* targ
     const int64_t vox = (int64_t)nb * c->V;
     after_default_stream(c);
     pack_input_kernel<<<256, 256, 0, c->stream>>>(vox, in4, c->act[0]);
-    cnn_forward(c, nb);
+    bool ok = cnn_forward(c, nb);
     cudaMemsetAsync(c->loss, 0, sizeof(double), c->stream);
     const float scale = 1.f / (float)(vox * 3);
     loss_kernel<<<512, 256, 0, c->stream>>>(vox, kPad, c->y, target3, c->grad[kLayers], scale, c->loss);
-    cnn_backward(c, nb);
+    ok &= cnn_backward(c, nb);
     cudaError_t e = cudaSuccess;
     if (loss) e = cudaMemcpyAsync(loss, c->loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess && grad)
         e = cudaMemcpyAsync(grad, c->gw, c->off[kLayers] * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
+    return cnn_finish(c, e, ok);
 }
 
 // one Adam step on a batch
@@ -467,11 +558,11 @@ fem_gpu_status fem_cnn_train_step(fem_cnn* c, const float* in4, const float* tar
     const int64_t vox = (int64_t)nb * c->V;
     after_default_stream(c);
     pack_input_kernel<<<256, 256, 0, c->stream>>>(vox, in4, c->act[0]);
-    cnn_forward(c, nb);
+    bool ok = cnn_forward(c, nb);
     cudaMemsetAsync(c->loss, 0, sizeof(double), c->stream);
     const float scale = 1.f / (float)(vox * 3);
     loss_kernel<<<512, 256, 0, c->stream>>>(vox, kPad, c->y, target3, c->grad[kLayers], scale, c->loss);
-    cnn_backward(c, nb);
+    ok &= cnn_backward(c, nb);
     c->step++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - std::pow(b1, (float)c->step), c2 = 1.f - std::pow(b2, (float)c->step);
@@ -479,8 +570,7 @@ fem_gpu_status fem_cnn_train_step(fem_cnn* c, const float* in4, const float* tar
     cnn_pack(c);
     cudaError_t e = cudaSuccess;
     if (loss) e = cudaMemcpyAsync(loss, c->loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    return e == cudaSuccess ? FEM_GPU_OK : FEM_GPU_CUDA_ERROR;
+    return cnn_finish(c, e, ok);
 }
 
 }  // extern "C"

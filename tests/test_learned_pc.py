@@ -92,6 +92,36 @@ def test_gpu_forward_is_exact_on_exactly_representable_data(torch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("n", [17, 33])
+def test_tensor_core_convolution_matches_warp_mma(torch, monkeypatch, n):
+    """The tcgen05 convolution (TMA halo blocks, TMEM accumulators) against
+    the warp-level mma.sync kernel on grids of several 8 x 16 tiles with
+    partial edge tiles and two samples: forward output and weight gradient
+    (both read BF16 operands and accumulate in FP32, in different orders)."""
+    from moris_gb300.learned import Cnn
+    nb = 2
+    x, t = _inputs(nb, n, 21)
+    w = _weights(22)
+    xd = torch.tensor(x.ravel(), device="cuda")
+    td = torch.tensor(t.ravel(), device="cuda")
+    monkeypatch.delenv("FEM_CNN_CONV_KERNEL", raising=False)
+    a = Cnn(n, batch_max=nb)
+    monkeypatch.setenv("FEM_CNN_CONV_KERNEL", "mma")
+    b = Cnn(n, batch_max=nb)
+    monkeypatch.delenv("FEM_CNN_CONV_KERNEL")
+    outs = []
+    for cnn in (a, b):
+        cnn.set_weights(w)
+        y = cnn.forward(xd, nb).cpu().numpy()
+        loss, g = cnn.loss_grad(xd, td, nb)
+        outs.append((y, loss, g))
+    (ya, la, ga), (yb, lb, gb) = outs
+    assert np.linalg.norm(ya - yb) <= 5e-3 * np.linalg.norm(yb)
+    assert abs(la - lb) <= 5e-3 * lb
+    assert np.linalg.norm(ga - gb) <= 2e-2 * np.linalg.norm(gb)
+
+
+@pytest.mark.gpu
 def test_training_reduces_loss(torch):
     from moris_gb300.learned import Cnn, train
     n = 6

@@ -559,6 +559,7 @@ def run_c5(timed, stream, args):
                                          % (it, nthreads, per_it * 1e3, plain["iterations"])}
         out["speedup_multigrid_vs_cpu_jacobi_pcg"] = projected / mgr["wall_seconds"]
         out["speedup_jacobi_pcg_vs_cpu_jacobi_pcg"] = projected / plain["seconds"]
+    out["learned_conv"] = conv_record()
     if os.path.exists(LPC_WEIGHTS):
         cnn, factor, meta = learned.load_cnn(LPC_WEIGHTS)
         meta = json.loads(meta) if meta else {}
@@ -576,6 +577,46 @@ def run_c5(timed, stream, args):
     else:
         out["fcg_learned"] = {"unavailable": "no trained weights (python -m moris_gb300.train_lpc)"}
     return out
+
+
+def bf16_peak():
+    """the measured dense bf16 burst peak of this GPU type (TFLOP/s) and its source"""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "of measured (cuBLAS bf16 burst)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "of fallback (1.9 PFLOP/s bf16 burst)"
+
+
+def conv_record(n=65, batches=(1, 8), reps=20):
+    """Tensor-core roofline of the learned correction's convolutions on the
+    n^3 coarse grid of the SIMP solve (65^3 for 128^3 elements): device time
+    per call (CUDA events on the net's stream) of each 3x3x3 layer, forward
+    and data gradient, and TFLOP/s of the algorithmic work 2*27*cin*cout per
+    voxel (real channels, real voxels) against the measured dense bf16 peak
+    (burst: each call is timed alone)."""
+    from moris_gb300 import learned
+    layers = [(4, 32), (32, 32), (32, 32), (32, 3)]
+    names = ["fwd%d %d->%d" % (l, a, b) for l, (a, b) in enumerate(layers)] + \
+            ["dgrad%d %d->%d" % (l, b, a) for l, (a, b) in enumerate(layers) if l > 0]
+    work = [layers[l] for l in range(4)] + [layers[l] for l in range(1, 4)]
+    peak, note = bf16_peak()
+    rec = {"kernel": "conv_umma_pipe_kernel (tcgen05.mma kind::f16 M=128 N=3*cout (x taps folded into N), bf16 "
+                     "operands, f32 TMEM accumulators, TMA halo blocks 16x10x3 voxels x 8 channels)", "grid": "%d^3" % n, "peak_bf16_tflops": peak,
+           "peak_note": note, "batches": {}}
+    cnn = learned.Cnn(n, batch_max=max(batches), seed=3)
+    for nb in batches:
+        ms = cnn.profile(nb, reps)
+        rows = []
+        for name, (a, b), t in zip(names, work, ms):
+            fl = 2.0 * 27 * a * b * n ** 3 * nb
+            rows.append({"layer": name, "ms": float(t), "tflops": fl / (t * 1e-3) / 1e12,
+                         "frac": fl / (t * 1e-3) / 1e12 / peak})
+        tot_fl = sum(2.0 * 27 * a * b * n ** 3 * nb for a, b in work)
+        rec["batches"][str(nb)] = {"layers": rows, "total_ms": float(ms.sum()),
+                                   "total_tflops": tot_fl / (ms.sum() * 1e-3) / 1e12}
+    del cnn
+    return rec
 
 
 _FP64_PEAK = []

@@ -509,6 +509,14 @@ fem_gpu_status fem_cnn_loss_grad(fem_cnn* cnn, const float* in4, const float* ta
                                  float* grad);
 fem_gpu_status fem_cnn_train_step(fem_cnn* cnn, const float* in4, const float* target3, int32_t samples, float lr,
                                   double* loss);
+
+/* device time (ms per call, CUDA events on the net's stream, reps calls each)
+   of the forward convolution of every layer, ms[0..3], and of the data
+   gradients of layers 1..3, ms[4..6], on `samples` samples; the activation
+   buffers hold whatever the last call left (their contents do not change the
+   time).  No counterpart in the reference: it measures this library's own
+   convolution kernels. */
+fem_gpu_status fem_cnn_profile(fem_cnn* cnn, int32_t samples, int32_t reps, double* ms);
 /* coarse input for a fine residual (node grid nf^3, coarsening factor F):
    channels 0..2 = R r / ||R r||, channel 3 = log10(restricted density) / 3;
    ||R r|| is reduced on the device into a library-wide accumulator, so calls

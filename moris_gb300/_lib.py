@@ -133,6 +133,7 @@ SIGNATURES = {
     "fem_cnn_get_output_scale": (D, [P]),
     "fem_cnn_loss_grad": (I32, [P, P, P, I32, P, P]),
     "fem_cnn_train_step": (I32, [P, P, P, I32, C.c_float, P]),
+    "fem_cnn_profile": (I32, [P, I32, I32, P]),
     "fem_lpc_restrict": (I32, [I32, I32, P, P, P, P]),
     "fem_lpc_inject": (I32, [I32, I32, P, D, P]),
     "fem_lpc_prolong_add": (I32, [I32, I32, P, D, P]),

@@ -293,19 +293,44 @@ EncodeTiled encode_tiled() {
 }
 
 // the channels-last tensor (C, x, y, z, sample) of one activation buffer and
-// the box of one 8-channel chunk of a tile's halo block
+// the box of a tile's halo block, all C channels of 16 x 10 x 3 voxels; one
+// voxel's channels are one 64-byte (C = 32) or 32-byte (C = 16) row, written
+// with the matching TMA swizzle (the tensor cores read the same pattern)
 bool conv_tensor_map(CUtensorMap* map, const __nv_bfloat16* in, int nb, int n, int C) {
     EncodeTiled enc = encode_tiled();
-    if (!enc) return false;
+    if (!enc || (C != 16 && C != 32)) return false;
     const cuuint64_t e = 2;  // bytes per BF16
     const cuuint64_t dims[5] = {(cuuint64_t)C, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)n, (cuuint64_t)nb};
     const cuuint64_t strides[4] = {C * e, (cuuint64_t)n * C * e, (cuuint64_t)n * n * C * e,
                                    (cuuint64_t)n * n * n * C * e};
-    const cuuint32_t box[5] = {8, fem_umma::kHx, fem_umma::kHy, 3, 1};
+    const cuuint32_t box[5] = {(cuuint32_t)C, fem_umma::kHx, fem_umma::kHy, 3, 1};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16*>(in), dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, C == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// one pipeline instance per (input chunks, output channels); one CTA per SM
+// (the weights and a four-block halo ring fill shared memory), persistent
+// over the tiles
+template <int NCHK, int COUT>
+bool launch_umma_inst(const CUtensorMap& map, const fem_umma::UmmaConvArgs& a, cudaStream_t st) {
+    auto kern = fem_umma::conv_umma_pipe_kernel<NCHK, COUT>;
+    const size_t smem = fem_umma::pipe_smem_bytes(8 * NCHK, COUT);
+    static std::once_flag attr;
+    std::call_once(attr, [&] { cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
+    const int64_t grid = std::min<int64_t>(fem_umma::num_tiles(a.nb, a.n), (int64_t)fem::sm_count());
+    kern<<<(unsigned)grid, fem_umma::kPipeThreads, smem, st>>>(map, a);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+bool launch_umma(const CUtensorMap& map, const fem_umma::UmmaConvArgs& a, cudaStream_t st) {
+    if ((a.cin != 16 && a.cin != 32) || (a.cout != 16 && a.cout != 32) || (a.sign != 1 && a.sign != -1) ||
+        fem_umma::num_tiles(a.nb, a.n) >= (1ll << 31))
+        return false;
+    if (a.cin == 16) return a.cout == 16 ? launch_umma_inst<2, 16>(map, a, st) : launch_umma_inst<2, 32>(map, a, st);
+    return a.cout == 16 ? launch_umma_inst<4, 16>(map, a, st) : launch_umma_inst<4, 32>(map, a, st);
 }
 
 bool conv(fem_cnn* c, int nb, const __nv_bfloat16* in, int cin, int cout, const __nv_bfloat16* w, int sign, int relu,
@@ -321,20 +346,7 @@ bool conv(fem_cnn* c, int nb, const __nv_bfloat16* in, int cin, int cout, const 
     CUtensorMap map;
     if (!conv_tensor_map(&map, in, nb, c->n, cin)) return false;
     fem_umma::UmmaConvArgs a{nb, c->n, cin, cout, sign, relu, w, mask, out_bf, out_f, c->d_status};
-    const size_t smem = fem_umma::smem_bytes(cin, cout);
-    static std::once_flag attr;
-    std::call_once(attr, [] {
-        cudaFuncSetAttribute(fem_umma::conv_umma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)fem_umma::smem_bytes(32, 32));
-    });
-    int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fem_umma::conv_umma_kernel, fem_umma::kThreads, smem);
-    const int n = c->n;
-    const int64_t tiles = (int64_t)nb * n * ((n + fem_umma::kTy - 1) / fem_umma::kTy) *
-                          ((n + fem_umma::kTx - 1) / fem_umma::kTx);
-    const int64_t grid = std::min<int64_t>(tiles, (int64_t)fem::sm_count() * std::max(per_sm, 1));
-    fem_umma::conv_umma_kernel<<<(unsigned)grid, fem_umma::kThreads, smem, c->stream>>>(map, a);
-    return cudaGetLastError() == cudaSuccess;
+    return launch_umma(map, a, c->stream);
 }
 
 // forward of nb samples already packed in act[0]
@@ -571,6 +583,44 @@ fem_gpu_status fem_cnn_train_step(fem_cnn* c, const float* in4, const float* tar
     cudaError_t e = cudaSuccess;
     if (loss) e = cudaMemcpyAsync(loss, c->loss, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     return cnn_finish(c, e, ok);
+}
+
+// device time of each forward convolution (ms per call, averaged over reps
+// calls, CUDA events on the net's stream) on the current contents of the
+// activation buffers; ms[kLayers + l - 1] gets the data gradient of layer l
+// (l = 1..3)
+fem_gpu_status fem_cnn_profile(fem_cnn* c, int32_t nb, int32_t reps, double* ms) {
+    if (!c || !ms || nb < 1 || nb > c->nb_max || reps < 1) return FEM_GPU_BAD_ARG;
+    if (c->dirty) cnn_pack(c);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return FEM_GPU_CUDA_ERROR;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return FEM_GPU_CUDA_ERROR;
+    }
+    bool ok = cnn_forward(c, nb);  // warm-up
+    for (int l = 0; l < 2 * kLayers - 1; ++l) {
+        const bool fwd = l < kLayers;
+        const int L = fwd ? l : l - kLayers + 1;
+        const bool last = L == kLayers - 1;
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < reps; ++r) {
+            if (fwd)
+                ok &= conv(c, nb, c->act[L], pad16(kCin[L]), pad16(kCout[L]), c->wf[L], +1, last ? 0 : 1, nullptr,
+                           last ? nullptr : c->act[L + 1], last ? c->y : nullptr);
+            else
+                ok &= conv(c, nb, c->grad[L + 1], pad16(kCout[L]), pad16(kCin[L]), c->wt[L], -1, 0, c->act[L],
+                           c->grad[L], nullptr);
+        }
+        cudaEventRecord(e1, c->stream);
+        cudaEventSynchronize(e1);
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        ms[l] = t / reps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return cnn_finish(c, cudaGetLastError(), ok);
 }
 
 }  // extern "C"

@@ -92,7 +92,7 @@ def test_gpu_forward_is_exact_on_exactly_representable_data(torch):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n", [17, 33])
+@pytest.mark.parametrize("n", [17, 33, 65])
 def test_tensor_core_convolution_matches_warp_mma(torch, monkeypatch, n):
     """The tcgen05 convolution (TMA halo blocks, TMEM accumulators) against
     the warp-level mma.sync kernel on grids of several 8 x 16 tiles with
@@ -119,6 +119,15 @@ def test_tensor_core_convolution_matches_warp_mma(torch, monkeypatch, n):
     assert np.linalg.norm(ya - yb) <= 5e-3 * np.linalg.norm(yb)
     assert abs(la - lb) <= 5e-3 * lb
     assert np.linalg.norm(ga - gb) <= 2e-2 * np.linalg.norm(gb)
+
+
+@pytest.mark.gpu
+def test_convolution_profile_times_every_layer(torch):
+    """fem_cnn_profile: a positive device time for each of the four forward
+    convolutions and the three data gradients."""
+    from moris_gb300.learned import Cnn
+    ms = Cnn(17, batch_max=2, seed=4).profile(2, reps=2)
+    assert ms.shape == (7,) and np.all(np.isfinite(ms)) and np.all(ms > 0)
 
 
 @pytest.mark.gpu

@@ -447,12 +447,116 @@ __global__ void __launch_bounds__(256) bulk_kernel(BulkArgs p, int mode, int war
 // SP_Dirichlet_Nitsche (gamma = alpha E / h).
 //
 // One CTA per facet (grid-stride over the facets).  Everything of a facet
-// lives in shared memory: the IP-cell coordinates and extraction T, the
-// pdof values, per Gauss point N, dN/dx, w*, the traction operator
-// nDB[f][(g,b)] = lam n_f g_gb + mu (n_g g_fb + delta_fg n.g_b) and its
-// projections, the pdof K and R, and K T.  Threads own Gauss points for the
-// geometry, then pdof entries for K and R, then (entry, column) pairs of
-// K T and T^T (K T), whose results are scattered into the CSR.
+// lives in shared memory: the IP-cell coordinates and extraction T (with the
+// nonzeros of every T column as a list), the pdof values, per Gauss point N,
+// dN/dx, w*, the traction operator nDB[f][(g,b)] = lam n_f g_gb + mu (n_g g_fb
+// + delta_fg n.g_b) and its projections (w* and beta folded in), the facet
+// Gram matrix sum_q w* N_a N_b, the pdof K and R, and K T.  Threads own Gauss
+// points for the geometry, then pdof entries for K and R, then (entry, column)
+// pairs of K T and T^T (K T), which contract over the nonzeros of one T column
+// only, and whose results are scattered into the CSR.  FP64 is the bound on
+// this GPU, so the stages that add nothing are skipped: a Neumann set (or a
+// zero Select matrix) has K = 0, and pdof pairs of two nodes off the facet
+// (N_a = N_b = 0 at every point) have K = 0.
+// per (facet ordinal, Gauss point): the facet's own shape derivatives
+// [(D-1) x NFV], the cell's N [NPE] and dN/dxi [D x NPE] at the point
+__host__ __device__ constexpr int side_ref_len(int D) {
+    return D == 2 ? 1 * 2 + 4 + 2 * 4 : 2 * 4 + 8 + 3 * 8;
+}
+// facet vertices of each ordinal (QUAD4 edges, HEX8 faces: the MTK node order)
+__host__ __device__ inline int side_face_vertex(int D, int ord, int k) {
+    const int quad_f[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+    const int hex_f[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
+    return D == 2 ? quad_f[ord][k] : hex_f[ord][k];
+}
+
+// per facet: for every Gauss point w* (w detJ times the thickness, 0 where
+// detJ < -1e-6), w detJ, the unit normal (3) and the inverse cell Jacobian
+// (3 x 3), then 1/h of SP_Dirichlet_Nitsche (h = the facet measure in 2-D,
+// sqrt(4 A / pi) in 3-D)
+constexpr int kSideGeoPerPoint = 14;
+__host__ __device__ constexpr int side_geo_len(int ngp) { return ngp * kSideGeoPerPoint + 2; }
+
+// The facet geometry depends on the mesh alone, so it is computed once when
+// the set is uploaded, one thread per (facet, Gauss point) -- the per-point
+// divisions and square roots would otherwise occupy the FP64 pipe on a few
+// lanes of every assembly.
+template <int D>
+__global__ void side_geometry_kernel(int64_t ns, int ngp, const double* xe, const int32_t* ordv, const double* gw,
+                                     const double* sref, int rect, double thickness, double* out) {
+    constexpr int NPE = D == 2 ? 4 : 8, NFV = D == 2 ? 2 : 4, REF = side_ref_len(D);
+    const int SG = side_geo_len(ngp);
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ns * ngp; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = k / ngp;
+        const int q = (int)(k - s * ngp), ord = ordv[s];
+        const double* X = xe + s * NPE * D;
+        const double* dNf = sref + (ord * ngp + q) * REF;
+        const double* dN = dNf + (D - 1) * NFV + NPE;
+        double t[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        for (int kk = 0; kk < NFV; ++kk) {
+            const int v = side_face_vertex(D, ord, kk);
+            for (int d = 0; d < D; ++d)
+                for (int m = 0; m < D - 1; ++m) t[m][d] = fma(dNf[m * NFV + kk], X[v * D + d], t[m][d]);
+        }
+        double detJ, nrm[3] = {0, 0, 0};
+        if (D == 2) {
+            detJ = sqrt(t[0][0] * t[0][0] + t[0][1] * t[0][1]);
+            nrm[0] = t[0][1] / detJ;
+            nrm[1] = -t[0][0] / detJ;
+        } else {
+            const double c0 = t[0][1] * t[1][2] - t[0][2] * t[1][1];
+            const double c1 = t[0][2] * t[1][0] - t[0][0] * t[1][2];
+            const double c2 = t[0][0] * t[1][1] - t[0][1] * t[1][0];
+            detJ = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
+            nrm[0] = c0 / detJ;
+            nrm[1] = c1 / detJ;
+            nrm[2] = c2 / detJ;
+        }
+        double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, Ji[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j)
+                if (!rect || i == j)
+                    for (int a = 0; a < NPE; ++a) J[i * 3 + j] = fma(dN[i * NPE + a], X[a * D + j], J[i * 3 + j]);
+        if (rect) {
+            for (int i = 0; i < D; ++i) Ji[i * 3 + i] = 1.0 / J[i * 3 + i];
+        } else if (D == 2) {
+            const double det = J[0] * J[4] - J[1] * J[3], id = 1.0 / det;
+            Ji[0] = J[4] * id; Ji[1] = -J[1] * id; Ji[3] = -J[3] * id; Ji[4] = J[0] * id;
+        } else {
+            const double det = J[0] * (J[4] * J[8] - J[7] * J[5]) - J[1] * (J[3] * J[8] - J[5] * J[6]) +
+                               J[2] * (J[3] * J[7] - J[4] * J[6]);
+            const double id = 1.0 / det;
+            Ji[0] = (J[4] * J[8] - J[7] * J[5]) * id;
+            Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id;
+            Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+            Ji[3] = (J[5] * J[6] - J[3] * J[8]) * id;
+            Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id;
+            Ji[5] = (J[3] * J[2] - J[0] * J[5]) * id;
+            Ji[6] = (J[3] * J[7] - J[6] * J[4]) * id;
+            Ji[7] = (J[6] * J[1] - J[0] * J[7]) * id;
+            Ji[8] = (J[0] * J[4] - J[3] * J[1]) * id;
+        }
+        double* o = out + s * SG + q * kSideGeoPerPoint;
+        o[0] = detJ < -1.0e-6 ? 0.0 : gw[q] * detJ * thickness;
+        o[1] = gw[q] * detJ;
+        for (int d = 0; d < 3; ++d) o[2 + d] = nrm[d];
+        for (int m = 0; m < 9; ++m) o[5 + m] = Ji[m];
+    }
+}
+
+// 1/h per facet from the measures of its points
+template <int D>
+__global__ void side_h_kernel(int64_t ns, int ngp, double* out) {
+    const int SG = side_geo_len(ngp);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += (int64_t)gridDim.x * blockDim.x) {
+        double meas = 0.0;
+        for (int q = 0; q < ngp; ++q) meas += out[s * SG + q * kSideGeoPerPoint + 1];
+        const double h = D == 2 ? meas : sqrt(4.0 * meas / 3.14159265358979323846);
+        out[s * SG + ngp * kSideGeoPerPoint] = 1.0 / h;
+        out[s * SG + ngp * kSideGeoPerPoint + 1] = 0.0;
+    }
+}
+
 struct SideArgs {
     int64_t ns;
     int iwg, model, ngp, maxnb;
@@ -467,6 +571,10 @@ struct SideArgs {
     const int32_t* ulen;
     const double* gp;   // [ngp] facet Gauss points (dim-1 coords each)
     const double* gw;   // [ngp]
+    const double* sref; // [ordinal][ngp][side_ref_len(D)]: facet dN, cell N, cell dN/dxi
+    const double* sgeo; // [facet][side_geo_len(ngp)]: per point w*, measure, normal, J^-1; 1/h
+    int rect;           // axis-aligned brick cells: diagonal, constant Jacobian
+    int select_identity; // M = I (no Select property): the projections are copies
     int64_t nu;
     double nu_p, alpha;
     double value[3];
@@ -485,12 +593,14 @@ struct SideArgs {
 
 // shared-memory layout of one facet, in doubles (the basis ids follow as ints)
 struct SideSmem {
-    int X, T, U, R, K, KT, QN, QG, QW, QM, QNRM, QB, QMB, QMTB, QT, QJ, misc, total;
+    int X, T, TW, NG, U, R, K, KT, QN, QG, QW, QNRM, QB, QMB, QMTB, QT, QJ, QJI, QTU, QJU, misc, total;
     __host__ __device__ SideSmem(int D, int maxnb, int ngp) {
         const int NPE = D == 2 ? 4 : 8, NPD = D * NPE;
         int o = 0;
         X = o; o += NPE * D;
         T = o; o += NPE * maxnb;
+        TW = o; o += NPE * maxnb;
+        NG = o; o += NPE * NPE;
         U = o; o += NPD;
         R = o; o += NPD;
         K = o; o += NPD * NPD;
@@ -498,29 +608,37 @@ struct SideSmem {
         QN = o; o += ngp * NPE;
         QG = o; o += ngp * D * NPE;
         QW = o; o += ngp;
-        QM = o; o += ngp;
         QNRM = o; o += ngp * 3;
         QB = o; o += ngp * D * NPD;
         QMB = o; o += ngp * D * NPD;
         QMTB = o; o += ngp * D * NPD;
         QT = o; o += ngp * D;
         QJ = o; o += ngp * D;
+        QJI = o; o += ngp * 9;
+        QTU = o; o += ngp * D;
+        QJU = o; o += ngp * D;
         misc = o; o += 4;
         total = o;
     }
+    // doubles, then the basis ids (int32), the T column lists (uint8 node
+    // index per nonzero), their counts (uint8) and the cell nodes with those
+    // on the facet first (uint8)
     static size_t bytes(int D, int maxnb, int ngp) {
-        return SideSmem(D, maxnb, ngp).total * sizeof(double) + (size_t)maxnb * sizeof(int32_t);
+        const int NPE = D == 2 ? 4 : 8;
+        return SideSmem(D, maxnb, ngp).total * sizeof(double) + (size_t)maxnb * (sizeof(int32_t) + NPE + 1) + NPE;
     }
 };
 
 template <int D>
-__global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
+__global__ void __launch_bounds__(128, 8) side_cta_kernel(SideArgs p) {
     constexpr int NPE = D == 2 ? 4 : 8, NPD = D * NPE, NFV = D == 2 ? 2 : 4;
     extern __shared__ double sm[];
     const int maxnb = p.maxnb, ngp = p.ngp, tid = threadIdx.x, NT = blockDim.x;
     const SideSmem L(D, maxnb, ngp);
     double* X = sm + L.X;
     double* T = sm + L.T;
+    double* TW = sm + L.TW;
+    double* NG = sm + L.NG;
     double* U = sm + L.U;
     double* R = sm + L.R;
     double* K = sm + L.K;
@@ -528,15 +646,20 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
     double* QN = sm + L.QN;
     double* QG = sm + L.QG;
     double* QW = sm + L.QW;
-    double* QM = sm + L.QM;
     double* QNRM = sm + L.QNRM;
     double* QB = sm + L.QB;
     double* QMB = sm + L.QMB;
     double* QMTB = sm + L.QMTB;
     double* QT = sm + L.QT;
     double* QJ = sm + L.QJ;
+    double* QJI = sm + L.QJI;
+    double* QTU = sm + L.QTU;
+    double* QJU = sm + L.QJU;
     double* misc = sm + L.misc;
     int32_t* bs = reinterpret_cast<int32_t*>(sm + L.total);
+    uint8_t* TN = reinterpret_cast<uint8_t*>(bs + maxnb);  // [maxnb][NPE]
+    uint8_t* TC = TN + maxnb * NPE;                          // [maxnb]
+    uint8_t* FP = TC + maxnb;                                // [NPE]: facet nodes first
     const bool neumann = p.iwg == FEM_GPU_IWG_STRUC_LINEAR_NEUMANN;
     const double beta = p.iwg == FEM_GPU_IWG_STRUC_LINEAR_DIRICHLET_SYMMETRIC_NITSCHE ? -1.0 : 1.0;
     const double mu_c = 1.0 / (2.0 * (1.0 + p.nu_p));
@@ -547,6 +670,9 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
     for (int i = 0; i < D; ++i)
         for (int j = 0; j < D; ++j) mnorm = fma(p.select[i * 3 + j], p.select[i * 3 + j], mnorm);
     const bool active = neumann || sqrt(mnorm) >= 2.220446049250313e-16;
+    // K = 0 for a Neumann set and for a zero projection: the assembly skips the
+    // K, K T and T^T K T stages (element outputs still write the zeros)
+    const bool k_zero = neumann || !active;
     for (int64_t s = blockIdx.x; s < p.ns; s += gridDim.x) {
         const int nb = p.nb[s];
         const int ord = p.ord[s];
@@ -557,6 +683,20 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
         for (int i = tid; i < NPE * maxnb; i += NT) T[i] = p.T[s * NPE * maxnb + i];
         for (int j = tid; j < maxnb; j += NT) bs[j] = p.bases[s * maxnb + j];
         __syncthreads();
+        // the nonzeros of every T column, in node order (the products they skip
+        // are exact zeros)
+        for (int j = tid; j < maxnb; j += NT) {
+            int cnt = 0;
+            for (int a = 0; a < NPE; ++a) {
+                const double t = T[a * maxnb + j];
+                if (fem_nonzero(t)) {
+                    TN[j * NPE + cnt] = (uint8_t)a;
+                    TW[j * NPE + cnt] = t;
+                    ++cnt;
+                }
+            }
+            TC[j] = (uint8_t)cnt;
+        }
         // ---- pdof values; per-point geometry -----------------------------------------
         for (int r = tid; r < NPD; r += NT) {
             const int f = r / NPE, a = r - f * NPE;
@@ -569,82 +709,33 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
             U[r] = v;
             R[r] = 0.0;
         }
-        for (int q = tid; q < ngp; q += NT) {
-            const int quad_f[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
-            const int hex_f[6][4] = {{1, 5, 4, 0}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {0, 3, 2, 1}, {4, 5, 6, 7}};
-            double Nf[4], dNf[8];
-            const double* xq = p.gp + q * (D - 1);
-            if (D == 2) Shape<4>::eval(xq, Nf, dNf);
-            else Shape<0>::eval(xq, Nf, dNf);
-            double t[2][3] = {{0, 0, 0}, {0, 0, 0}}, xip[3] = {0, 0, 0};
-            for (int k = 0; k < NFV; ++k) {
-                const int v = D == 2 ? quad_f[ord][k] : hex_f[ord][k];
-                const double xiv[3] = {((v & 3) == 1 || (v & 3) == 2) ? 1.0 : -1.0, ((v & 3) >= 2) ? 1.0 : -1.0,
-                                       v >= 4 ? 1.0 : -1.0};
-                for (int d = 0; d < D; ++d) {
-                    xip[d] = fma(Nf[k], xiv[d], xip[d]);
-                    for (int m = 0; m < D - 1; ++m) t[m][d] = fma(dNf[m * NFV + k], X[v * D + d], t[m][d]);
-                }
-            }
-            double detJ, nrm[3] = {0, 0, 0};
-            if (D == 2) {
-                detJ = sqrt(t[0][0] * t[0][0] + t[0][1] * t[0][1]);
-                nrm[0] = t[0][1] / detJ;
-                nrm[1] = -t[0][0] / detJ;
-            } else {
-                const double c0 = t[0][1] * t[1][2] - t[0][2] * t[1][1];
-                const double c1 = t[0][2] * t[1][0] - t[0][0] * t[1][2];
-                const double c2 = t[0][0] * t[1][1] - t[0][1] * t[1][0];
-                detJ = sqrt(c0 * c0 + c1 * c1 + c2 * c2);
-                nrm[0] = c0 / detJ;
-                nrm[1] = c1 / detJ;
-                nrm[2] = c2 / detJ;
-            }
-            QM[q] = p.gw[q] * detJ;
-            // Gauss points with detJ < -1e-6 are skipped (weight 0)
-            QW[q] = detJ < -1.0e-6 ? 0.0 : p.gw[q] * detJ * p.thickness;
-            for (int d = 0; d < 3; ++d) QNRM[q * 3 + d] = nrm[d];
-            double N[NPE], dN[NPE * D];
-            if (D == 2) Shape<0>::eval(xip, N, dN);
-            else Shape<1>::eval(xip, N, dN);
-            for (int a = 0; a < NPE; ++a) QN[q * NPE + a] = N[a];
-            // dN/dx through the interpolation-cell Jacobian (rectangular or general)
-            double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-            for (int i = 0; i < D; ++i)
-                for (int j = 0; j < D; ++j)
-                    for (int a = 0; a < NPE; ++a) J[i][j] = fma(dN[i * NPE + a], X[a * D + j], J[i][j]);
-            if (D == 2) {
-                const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0], id = 1.0 / det;
-                Ji[0][0] = J[1][1] * id; Ji[0][1] = -J[0][1] * id; Ji[1][0] = -J[1][0] * id; Ji[1][1] = J[0][0] * id;
-            } else {
-                const double det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
-                                   J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-                const double id = 1.0 / det;
-                Ji[0][0] = (J[1][1] * J[2][2] - J[2][1] * J[1][2]) * id;
-                Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
-                Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-                Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
-                Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-                Ji[1][2] = (J[1][0] * J[0][2] - J[0][0] * J[1][2]) * id;
-                Ji[2][0] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
-                Ji[2][1] = (J[2][0] * J[0][1] - J[0][0] * J[2][1]) * id;
-                Ji[2][2] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
-            }
-            for (int i = 0; i < D; ++i)
-                for (int a = 0; a < NPE; ++a) {
-                    double v = 0.0;
-                    for (int k = 0; k < D; ++k) v = fma(Ji[i][k], dN[k * NPE + a], v);
-                    QG[(q * D + i) * NPE + a] = v;
-                }
+        // per point: w*, the normal and J^-1 (computed once per mesh), N from
+        // the reference table
+        constexpr int REF = side_ref_len(D);
+        const double* geo = p.sgeo + s * side_geo_len(ngp);
+        for (int k = tid; k < ngp * kSideGeoPerPoint; k += NT) {
+            const int q = k / kSideGeoPerPoint, m = k - q * kSideGeoPerPoint;
+            const double v = geo[k];
+            if (m == 0) QW[q] = v;
+            else if (m >= 2 && m < 5) QNRM[q * 3 + m - 2] = v;
+            else if (m >= 5) QJI[q * 9 + m - 5] = v;
+        }
+        for (int k = tid; k < ngp * NPE; k += NT) {
+            const int q = k / NPE, a = k - q * NPE;
+            QN[k] = p.sref[(ord * ngp + q) * REF + (D - 1) * NFV + a];
+        }
+        if (tid == 0) misc[0] = p.alpha * E * geo[ngp * kSideGeoPerPoint];
+        __syncthreads();
+        // dN/dx = J^-1 dN/dxi (lanes over point, component and node)
+        for (int k = tid; k < ngp * D * NPE; k += NT) {
+            const int q = k / (D * NPE), i = (k / NPE) % D, a = k % NPE;
+            const double* dN = p.sref + (ord * ngp + q) * REF + (D - 1) * NFV + NPE;
+            const double* Ji = QJI + q * 9;
+            double v = 0.0;
+            for (int kk = 0; kk < D; ++kk) v = fma(Ji[i * 3 + kk], dN[kk * NPE + a], v);
+            QG[k] = v;
         }
         __syncthreads();
-        if (tid == 0) {
-            double meas = 0.0;
-            for (int q = 0; q < ngp; ++q) meas += QM[q];
-            const double h = D == 2 ? meas : sqrt(4.0 * meas / 3.14159265358979323846);
-            misc[0] = p.alpha * E / h;
-        }
         // ---- traction operator per point -------------------------------------------
         if (!neumann)
             for (int k = tid; k < ngp * D * NPD; k += NT) {
@@ -654,11 +745,17 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
                 const double* g = QG + q * D * NPE;
                 double ng = 0.0;
                 for (int kk = 0; kk < D; ++kk) ng += nrm[kk] * g[kk * NPE + b];
-                QB[k] = lam * nrm[f] * g[gg * NPE + b] + mu * (nrm[gg] * g[f * NPE + b] + (f == gg ? ng : 0.0));
+                const double qb = lam * nrm[f] * g[gg * NPE + b] + mu * (nrm[gg] * g[f * NPE + b] + (f == gg ? ng : 0.0));
+                QB[k] = qb;
+                if (p.select_identity) {
+                    // M nDB = M^T nDB = nDB: the projections below, without the zero terms
+                    QMB[k] = QW[q] * qb;
+                    QMTB[k] = beta * QW[q] * qb;
+                }
             }
         __syncthreads();
         // projections M nDB and M^T nDB
-        if (!neumann)
+        if (!neumann && !p.select_identity)
             for (int k = tid; k < ngp * D * NPD; k += NT) {
                 const int q = k / (D * NPD), rem = k - q * D * NPD, f = rem / NPD, c = rem - f * NPD;
                 const double* B = QB + q * D * NPD;
@@ -667,29 +764,54 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
                     mb = fma(p.select[f * 3 + kk], B[kk * NPD + c], mb);
                     mtb = fma(p.select[kk * 3 + f], B[kk * NPD + c], mtb);
                 }
-                QMB[k] = mb;
-                QMTB[k] = mtb;
+                // w* folded in, and beta into M^T nDB (both only feed K)
+                QMB[k] = QW[q] * mb;
+                QMTB[k] = beta * QW[q] * mtb;
             }
-        // traction and jump per point, projected: M t(u), M (u - g)
+        // facet Gram matrix sum_q w* N_a N_b (the gamma term of K)
+        if (!k_zero)
+            for (int k = tid; k < NPE * NPE; k += NT) {
+                const int a = k / NPE, b = k - a * NPE;
+                double g = 0.0;
+                for (int q = 0; q < ngp; ++q) g = fma(QW[q] * QN[q * NPE + a], QN[q * NPE + b], g);
+                NG[k] = g;
+            }
+        // traction and jump per point and component, then projected: M t(u), M (u - g)
         if (!neumann)
-            for (int q = tid; q < ngp; q += NT) {
-                double trac[3] = {0, 0, 0}, jump[3] = {0, 0, 0};
-                for (int f = 0; f < D; ++f) {
-                    double tt = 0.0, uu = 0.0;
-                    for (int c = 0; c < NPD; ++c) tt = fma(QB[(q * D + f) * NPD + c], U[c], tt);
-                    for (int a = 0; a < NPE; ++a) uu = fma(QN[q * NPE + a], U[f * NPE + a], uu);
-                    trac[f] = tt;
-                    jump[f] = uu - p.value[f];
+            for (int k = tid; k < ngp * D; k += NT) {
+                const int q = k / D, f = k - q * D;
+                double tt = 0.0, uu = 0.0;
+                for (int c = 0; c < NPD; ++c) tt = fma(QB[(q * D + f) * NPD + c], U[c], tt);
+                for (int a = 0; a < NPE; ++a) uu = fma(QN[q * NPE + a], U[f * NPE + a], uu);
+                QTU[k] = tt;
+                QJU[k] = uu - p.value[f];
+                if (p.select_identity) {
+                    QT[k] = tt;
+                    QJ[k] = uu - p.value[f];
                 }
-                for (int f = 0; f < D; ++f) {
-                    double mt = 0.0, mj = 0.0;
-                    for (int kk = 0; kk < D; ++kk) {
-                        mt = fma(p.select[f * 3 + kk], trac[kk], mt);
-                        mj = fma(p.select[f * 3 + kk], jump[kk], mj);
-                    }
-                    QT[q * D + f] = mt;
-                    QJ[q * D + f] = mj;
+            }
+        __syncthreads();
+        // the cell nodes on the facet (N_a nonzero at some point: a nonzero
+        // diagonal Gram entry) first, then the others
+        if (!k_zero && tid == 0) {
+            int nf = 0;
+            for (int a = 0; a < NPE; ++a)
+                if (fem_nonzero(NG[a * NPE + a])) FP[nf++] = (uint8_t)a;
+            int o = nf;
+            for (int a = 0; a < NPE; ++a)
+                if (!fem_nonzero(NG[a * NPE + a])) FP[o++] = (uint8_t)a;
+            misc[1] = nf;
+        }
+        if (!neumann && !p.select_identity)
+            for (int k = tid; k < ngp * D; k += NT) {
+                const int q = k / D, f = k - q * D;
+                double mt = 0.0, mj = 0.0;
+                for (int kk = 0; kk < D; ++kk) {
+                    mt = fma(p.select[f * 3 + kk], QTU[q * D + kk], mt);
+                    mj = fma(p.select[f * 3 + kk], QJU[q * D + kk], mj);
                 }
+                QT[k] = mt;
+                QJ[k] = mj;
             }
         __syncthreads();
         // ---- pdof residual and Jacobian --------------------------------------------
@@ -710,38 +832,62 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
             }
             R[r] = active ? v : 0.0;
         }
-        for (int k = tid; k < NPD * NPD; k += NT) {
-            const int r = k / NPD, c = k - r * NPD;
-            const int f = r / NPE, a = r - f * NPE, gg = c / NPE, b = c - gg * NPE;
-            double v = 0.0;
-            if (!neumann && active)
-                for (int q = 0; q < ngp; ++q) {
-                    const double na = QN[q * NPE + a], nb_ = QN[q * NPE + b];
-                    double t = beta * QMTB[(q * D + gg) * NPD + r] * nb_ - na * QMB[(q * D + f) * NPD + c];
-                    t = fma(gamma * na * p.select[f * 3 + gg], nb_, t);
-                    v = fma(QW[q], t, v);
+        // K[(f,a),(g,b)] = sum_q w*[beta (M^T nDB)_(g,(f,a)) N_b - N_a (M nDB)_(f,(g,b))]
+        //                 + gamma M_fg sum_q w* N_a N_b
+        // (w* and beta are inside QMTB / QMB).  N_b = 0 at every point for a
+        // node b off the facet, so its terms are exact zeros: the entries are
+        // taken block by block -- both nodes on the facet (every term), row
+        // node on (the N_a terms), column node on (the N_b terms), both off
+        // (K = 0) -- which keeps the work of a warp uniform
+        if (!k_zero) {
+            const int nf = (int)misc[1], no = NPE - nf;
+            const int non = D * nf, noff = D * no;
+            // block (row class, column class): 0 on-on, 1 on-off, 2 off-on, 3 off-off
+            for (int blk = 0; blk < 4; ++blk) {
+                const bool ron = blk < 2, con = (blk & 1) == 0;
+                const int nr = ron ? non : noff, nc_ = con ? non : noff, nrn = ron ? nf : no, ncn = con ? nf : no;
+                for (int k = tid; k < nr * nc_; k += NT) {
+                    const int ri = k / nc_, ci = k - ri * nc_;
+                    const int f = ri / nrn, a = FP[(ron ? 0 : nf) + ri % nrn];
+                    const int gg = ci / ncn, b = FP[(con ? 0 : nf) + ci % ncn];
+                    const int r = f * NPE + a, c = gg * NPE + b;
+                    double v = 0.0;
+                    if (ron && con) {
+                        for (int q = 0; q < ngp; ++q) {
+                            v = fma(QMTB[(q * D + gg) * NPD + r], QN[q * NPE + b], v);
+                            v = fma(-QN[q * NPE + a], QMB[(q * D + f) * NPD + c], v);
+                        }
+                        v = fma(gamma * p.select[f * 3 + gg], NG[a * NPE + b], v);
+                    } else if (con) {
+                        for (int q = 0; q < ngp; ++q) v = fma(QMTB[(q * D + gg) * NPD + r], QN[q * NPE + b], v);
+                    } else if (ron) {
+                        for (int q = 0; q < ngp; ++q) v = fma(-QN[q * NPE + a], QMB[(q * D + f) * NPD + c], v);
+                    }
+                    K[r * NPD + c] = v;
                 }
-            K[k] = v;
+            }
         }
+        else if (p.mode != MODE_ASSEMBLE)
+            for (int k = tid; k < NPD * NPD; k += NT) K[k] = 0.0;
         __syncthreads();
         // ---- extraction: R_a = T^T R, K T, then T^T (K T) and the scatter -----------
         for (int k = tid; k < D * nb; k += NT) {
             const int f = k / nb, i = k - f * nb;
             double ra = 0.0;
-            for (int a = 0; a < NPE; ++a) ra = fma(T[a * maxnb + i], R[f * NPE + a], ra);
+            for (int m = 0; m < TC[i]; ++m) ra = fma(TW[i * NPE + m], R[f * NPE + TN[i * NPE + m]], ra);
             if (p.mode == MODE_ASSEMBLE) {
                 if (p.rhs) atomicAdd(p.rhs + f * p.nu + bs[i], ra);
             } else if (p.Rout) {
                 p.Rout[(s - p.first) * p.nmax + f * maxnb + i] = ra;
             }
         }
-        const bool want_k = !((p.mode == MODE_ASSEMBLE && !p.vals) || (p.mode == MODE_ELEMENT && !p.Kout));
+        const bool want_k = !((p.mode == MODE_ASSEMBLE && (!p.vals || k_zero)) || (p.mode == MODE_ELEMENT && !p.Kout));
         const int nc = D * nb;
         if (want_k)
             for (int k = tid; k < NPD * nc; k += NT) {
                 const int r = k / nc, c = k - r * nc, gg = c / nb, j = c - gg * nb;
                 double v = 0.0;
-                for (int b = 0; b < NPE; ++b) v = fma(K[r * NPD + gg * NPE + b], T[b * maxnb + j], v);
+                for (int m = 0; m < TC[j]; ++m) v = fma(K[r * NPD + gg * NPE + TN[j * NPE + m]], TW[j * NPE + m], v);
                 KT[r * nc + c] = v;
             }
         __syncthreads();
@@ -751,10 +897,7 @@ __global__ void __launch_bounds__(128) side_cta_kernel(SideArgs p) {
                 const int rr = k / nc, c = k - rr * nc;
                 const int f = rr / nb, i = rr - f * nb, gg = c / nb, j = c - gg * nb;
                 double v = 0.0;
-                for (int a = 0; a < NPE; ++a) {
-                    const double ta = T[a * maxnb + i];
-                    if (fem_nonzero(ta)) v = fma(ta, KT[(f * NPE + a) * nc + c], v);
-                }
+                for (int m = 0; m < TC[i]; ++m) v = fma(TW[i * NPE + m], KT[(f * NPE + TN[i * NPE + m]) * nc + c], v);
                 bad |= !fem_finite(v);
                 if (p.mode == MODE_ASSEMBLE) {
                     const int32_t rbase = p.rowptr[f * p.nu + bs[i]];
@@ -1029,6 +1172,13 @@ fem_gpu_status launch_side(fem_gpu_ctx* c, int si, int mode, int64_t first, int6
     a.ulen = (const int32_t*)c->d_ulen.p;
     a.gp = (const double*)ds.d_gp.p;
     a.gw = (const double*)ds.d_gw.p;
+    a.sref = (const double*)ds.d_sref.p;
+    a.sgeo = (const double*)ds.d_sgeo.p + first * side_geo_len(ds.ngp);
+    a.rect = c->shape == FEM_GPU_SHAPE_RECTANGULAR;
+    a.select_identity = 1;
+    for (int i = 0; i < D; ++i)
+        for (int j = 0; j < D; ++j)
+            if (s.side_select[i * 3 + j] != (i == j ? 1.0 : 0.0)) a.select_identity = 0;
     a.nu = c->num_used;
     a.nu_p = s.side.poisson_ratio;
     a.alpha = s.side.nitsche_alpha;
@@ -1186,6 +1336,8 @@ void device_release(fem_gpu_ctx* c) {
         dfree(s.d_nq);
         dfree(s.d_gp);
         dfree(s.d_gw);
+        dfree(s.d_sref);
+        dfree(s.d_sgeo);
     }
     dfree(c->d_rowptr);
     dfree(c->d_ulen);
@@ -1285,6 +1437,31 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
             ds.ngp = r.n;
             if ((e = upload(ds.d_gp, r.pts, sm)) != cudaSuccess) return cuda_fail(c, e, "side gp");
             if ((e = upload(ds.d_gw, r.w, sm)) != cudaSuccess) return cuda_fail(c, e, "side gw");
+            // the geometry-independent shape values of every facet ordinal and
+            // point: the facet's own derivatives, the cell's N and dN/dxi at the
+            // point's image in the cell
+            {
+                const int D = c->dim, NFV = D == 2 ? 2 : 4, nord = D == 2 ? 4 : 6, REF = side_ref_len(D);
+                std::vector<double> ref((size_t)nord * r.n * REF, 0.0);
+                for (int o = 0; o < nord; ++o)
+                    for (int q = 0; q < r.n; ++q) {
+                        double* out = ref.data() + ((size_t)o * r.n + q) * REF;
+                        double Nf[4], dNf[8], xip[3] = {0, 0, 0};
+                        const double* xq = r.pts.data() + q * (D - 1);
+                        if (D == 2) Shape<4>::eval(xq, Nf, dNf);
+                        else Shape<0>::eval(xq, Nf, dNf);
+                        for (int k = 0; k < NFV; ++k) {
+                            const int v = side_face_vertex(D, o, k);
+                            const double xiv[3] = {((v & 3) == 1 || (v & 3) == 2) ? 1.0 : -1.0,
+                                                   ((v & 3) >= 2) ? 1.0 : -1.0, v >= 4 ? 1.0 : -1.0};
+                            for (int d = 0; d < D; ++d) xip[d] = std::fma(Nf[k], xiv[d], xip[d]);
+                        }
+                        for (int k = 0; k < (D - 1) * NFV; ++k) out[k] = dNf[k];
+                        if (D == 2) Shape<0>::eval(xip, out + (D - 1) * NFV, out + (D - 1) * NFV + 4);
+                        else Shape<1>::eval(xip, out + (D - 1) * NFV, out + (D - 1) * NFV + 8);
+                    }
+                if ((e = upload(ds.d_sref, ref, sm)) != cudaSuccess) return cuda_fail(c, e, "side reference table");
+            }
             ds.nbsel = s.maxnb;
         }
         // repack element data to the kernel's padded basis width (the host
@@ -1308,8 +1485,31 @@ fem_gpu_status device_finalize(fem_gpu_ctx* c) {
         if ((e = upload(s.d_sidx, same ? s.sidx : sidx, sm)) != cudaSuccess) return cuda_fail(c, e, "sidx");
         if ((e = upload(s.d_xe, s.xe, sm)) != cudaSuccess) return cuda_fail(c, e, "xe");
         if ((e = upload(s.d_E, s.E, sm)) != cudaSuccess) return cuda_fail(c, e, "E");
-        if (s.kind == 1)
+        if (s.kind == 1) {
             if ((e = upload(s.d_ord, s.ordinal, sm)) != cudaSuccess) return cuda_fail(c, e, "ordinals");
+            // the facet geometry, once
+            const int64_t ns = s.neq;
+            const std::vector<double> zeros((size_t)std::max<int64_t>(ns, 1) * side_geo_len(s.ngp), 0.0);
+            if ((e = upload(s.d_sgeo, zeros, sm)) != cudaSuccess) return cuda_fail(c, e, "side geometry");
+            if (ns > 0) {
+                const int rect = c->shape == FEM_GPU_SHAPE_RECTANGULAR;
+                const unsigned g1 = (unsigned)std::min<int64_t>((ns * s.ngp + 255) / 256, (int64_t)sm_count() * 8);
+                const unsigned g2 = (unsigned)std::min<int64_t>((ns + 255) / 256, (int64_t)sm_count() * 8);
+                double* out = (double*)s.d_sgeo.p;
+                if (c->dim == 2) {
+                    side_geometry_kernel<2><<<g1, 256, 0, sm>>>(ns, s.ngp, (const double*)s.d_xe.p,
+                                                                (const int32_t*)s.d_ord.p, (const double*)s.d_gw.p,
+                                                                (const double*)s.d_sref.p, rect, s.side_thickness, out);
+                    side_h_kernel<2><<<g2, 256, 0, sm>>>(ns, s.ngp, out);
+                } else {
+                    side_geometry_kernel<3><<<g1, 256, 0, sm>>>(ns, s.ngp, (const double*)s.d_xe.p,
+                                                                (const int32_t*)s.d_ord.p, (const double*)s.d_gw.p,
+                                                                (const double*)s.d_sref.p, rect, s.side_thickness, out);
+                    side_h_kernel<3><<<g2, 256, 0, sm>>>(ns, s.ngp, out);
+                }
+                if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "side geometry kernel");
+            }
+        }
         if (s.kind == 1) s.maxnb = W;
     }
     // the side kernel and host topology read maxnb-padded arrays: keep the

@@ -76,6 +76,8 @@ struct SetData {
     DeviceBuf d_tri;        // bulk: T^T K T upper-triangle item table of the CTA kernels
     DeviceBuf d_g0;         // bulk: reference Gram table sum_q w_q dN/dxi dN/dxi
     DeviceBuf d_gp, d_gw;   // side: facet Gauss points and weights
+    DeviceBuf d_sref;       // side: facet / cell shape values per ordinal and point
+    DeviceBuf d_sgeo;       // side: per facet and point w*, normal, J^-1; 1/h (built once)
     DeviceBuf d_igoff, d_igx, d_igxi;            // cut clusters: integration cells
     DeviceBuf d_fcoff, d_fcx, d_fcxl, d_fcxf;    // double-sided: facets
     DeviceBuf d_EF, d_vol;

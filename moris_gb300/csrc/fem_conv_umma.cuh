@@ -32,12 +32,13 @@
 //
 // Each CTA is a warp-specialised persistent pipeline over its tiles: one lane
 // of warp 0 streams the halo blocks through a ring of shared-memory stages
-// with TMA, one lane of warp 1 issues every tile's tcgen05.mma chain
-// (descriptors as compile-time offsets) into one of four TMEM accumulators,
-// and warps 2..5 read their lane quadrant back with tcgen05.ld, add the
-// shifted x neighbours, apply ReLU / the ReLU mask of the data gradient, convert to BF16
-// and / or FP32 and store -- so the copies, the MMAs and the epilogue of
-// consecutive tiles overlap.  Every mbarrier wait is bounded: on expiry the
+// with TMA, one lane each of warps 1 and 6 issues the tcgen05.mma chains of
+// the even and odd tiles (descriptors as compile-time offsets) into four TMEM
+// accumulators (all 512 columns: one CTA per SM), and warps 2..5 read their
+// lane quadrant back with tcgen05.ld, add the shifted x neighbours, apply
+// ReLU / the ReLU mask of the data gradient, convert to BF16 and / or FP32
+// and store -- so the copies, the MMAs and the epilogue of consecutive tiles
+// overlap.  Every mbarrier wait is bounded: on expiry the
 // kernel records the failure in the status word, the other roles stop at
 // their next wait, the copies and MMAs in flight are waited for (bounded) and
 // the TMEM is freed.
@@ -225,9 +226,12 @@ constexpr int kPipeThreads = 224;  // + warp 6: a second MMA lane (odd tiles)
 
 __host__ __device__ constexpr size_t pipe_smem_bytes(int cin, int cout) {
     // weights, the halo ring, kStages + 2 kAcc mbarriers, TMEM address and
-    // abort word; 1 KB alignment slack and 2 KB of tail room
-    return ((size_t)27 * cin * cout * 2 + 1023) / 1024 * 1024 + (size_t)kStages * kHaloRows * cin * 2 +
-           ((kStages + 2 * kAcc) * 8 + 16) + 1024 + 2048;
+    // abort word; 1 KB alignment slack and 2 KB of tail room; at least 120 KB,
+    // so that a second CTA never shares the SM (each takes all 512 TMEM
+    // columns, and a second allocation would wait for the first CTA to end)
+    const size_t need = ((size_t)27 * cin * cout * 2 + 1023) / 1024 * 1024 + (size_t)kStages * kHaloRows * cin * 2 +
+                        ((kStages + 2 * kAcc) * 8 + 16) + 1024 + 2048;
+    return need > 120 * 1024 ? need : 120 * 1024;
 }
 
 // Warp-specialised persistent pipeline.  Warp 0 (one lane) streams the halo

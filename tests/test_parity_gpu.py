@@ -348,3 +348,48 @@ def test_select_and_thickness_properties_match_oracle(torch, case):
     vo, ro = orc.assemble(u)
     assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL
     assert rel_err(rhs.cpu().numpy(), ro) <= RTOL
+
+
+def test_zero_select_adds_nothing(torch):
+    """A Dirichlet set whose Select matrix is zero contributes nothing: the
+    reference skips the IWG when the projection's norm is below machine
+    epsilon (..._Dirichlet.cpp:86, 161).  Its element operators and residuals are
+    zero, and the assembled system is the oracle's (brick cells, linear
+    B-splines, with a Neumann set beside it)."""
+    from oracle import OracleModel
+    dim, ne, p = 3, (3, 2, 2), 1
+    mesh = mg.hmr_uniform_mesh(dim, ne, [1.0] * dim, p)
+    nc = len(mesh["cells"])
+    E = 10.0 ** (-3.0 * uniform01(5, nc))
+    cells = np.arange(nc, dtype=np.int32)
+    left = cells[cells % ne[0] == 0]
+    right = cells[cells % ne[0] == ne[0] - 1]
+    prod = mg.FemModel(dim, mesh, mg.SHAPE_RECTANGULAR)
+    orc = OracleModel(dim, mg.CELL_HEX8, mg.SHAPE_RECTANGULAR, mesh)
+    prod.add_bulk_set(cells, E, 0.3, mg.RULE_HEX_2x2x2, mg.MODEL_3D)
+    orc.add_bulk_set(mg.CELL_HEX8, mg.RULE_HEX_2x2x2, mg.MODEL_3D, cells, E, 0.3)
+    zero = np.zeros((dim, dim))
+    iwg = mg.IWG_STRUC_LINEAR_DIRICHLET_UNSYMMETRIC_NITSCHE
+    prod.add_side_set(iwg, left, np.full(len(left), 3), E[left], 0.3, mg.RULE_QUAD_2x2, mg.MODEL_3D, alpha=50.0,
+                      value=(0.01, 0.02, 0.03), select=zero)
+    orc.add_side_set(iwg, mg.RULE_QUAD_2x2, mg.MODEL_3D, left, np.full(len(left), 3), E[left], 0.3, 50.0,
+                     (0.01, 0.02, 0.03))
+    orc.set_side_options(0, 1.0, zero)
+    trac = (1e-3, 2e-3, 3e-3)
+    prod.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, right, np.full(len(right), 1), E[right], 0.3, mg.RULE_QUAD_2x2,
+                      mg.MODEL_3D, value=trac)
+    orc.add_side_set(mg.IWG_STRUC_LINEAR_NEUMANN, mg.RULE_QUAD_2x2, mg.MODEL_3D, right, np.full(len(right), 1),
+                     E[right], 0.3, 0.0, trac)
+    prod.finalize()
+    orc.finalize()
+    u = uniform01(13, prod.num_adofs) - 0.5
+    K, R = prod.element_matrices(1, 0, orc.num_eq(1), u)
+    assert not np.any(K) and not np.any(R)
+    rp, _ = prod.graph()
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(torch.tensor(u, device="cuda"), vals, rhs)
+    torch.cuda.synchronize()
+    vo, ro = orc.assemble(u)
+    assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL
+    assert rel_err(rhs.cpu().numpy(), ro) <= RTOL

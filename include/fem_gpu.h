@@ -305,6 +305,22 @@ fem_gpu_status fem_hmr_refined_element_t_matrix(const fem_hmr_refined* m, int32_
    306-457).  Read it with fem_hmr_mesh_sizes / fem_hmr_mesh_arrays; it feeds
    fem_gpu_create like the uniform mesh (cells are axis-aligned bricks). */
 fem_gpu_status fem_hmr_refined_mesh(const fem_hmr_refined* m, int32_t truncate, fem_hmr_mesh** out);
+/* The same mesh with the element T matrices and the node rows evaluated on
+   the GPU (one thread per element / per node; the refined elements of every
+   level as sorted keys on the device).  The numbers equal the host's bit for
+   bit: the T entries are exact dyadic fractions, and the node rows use the
+   host's operations in its order. */
+fem_gpu_status fem_hmr_refined_mesh_device(const fem_hmr_refined* m, int32_t truncate, fem_hmr_mesh** out);
+/* T matrices of `count` elements (levels[count], domain-relative
+   ijk[count][dim]) on the GPU: ndof[count]; T[count][(order+1)^dim][capacity]
+   row-major, dof_level[count][capacity], dof_ijk[count][capacity][dim] as
+   fem_hmr_refined_element_t_matrix gives them; all three NULL = size query
+   (ndof only).  FEM_GPU_BAD_ARG when an element has more than `capacity`
+   columns (ndof still set). */
+fem_gpu_status fem_hmr_refined_element_t_matrices_device(const fem_hmr_refined* m, int32_t truncate, int64_t count,
+                                                         const int32_t* levels, const int32_t* ijk, int32_t capacity,
+                                                         int32_t* ndof, double* T, int32_t* dof_level,
+                                                         int32_t* dof_ijk);
 
 /* ---- XFEM decomposition of a uniform level-0 HEX8 mesh (host only) -------
    Input of the cut-cell path, standing in for the reference's XTK

@@ -211,12 +211,39 @@ class RefinedHmr:
             raise FemGpuError(st, "fem_hmr_refined_element_t_matrix")
         return T[:B * n].reshape(B, n), dl[:n], di[:n * self.dim].reshape(n, self.dim)
 
-    def mesh(self, truncate=True):
+    def mesh(self, truncate=True, device=False):
+        """The Lagrange mesh of the active elements with its node rows; with
+        device=True the element T matrices and node rows are evaluated on the GPU."""
         h = C.c_void_p()
-        st = self.L.fem_hmr_refined_mesh(self.h, int(truncate), C.byref(h))
+        fn = self.L.fem_hmr_refined_mesh_device if device else self.L.fem_hmr_refined_mesh
+        st = fn(self.h, int(truncate), C.byref(h))
         if st:
-            raise FemGpuError(st, "fem_hmr_refined_mesh")
+            raise FemGpuError(st, "fem_hmr_refined_mesh" + ("_device" if device else ""))
         return _mesh_dict(self.L, h, self.dim)
+
+    def element_t_matrices_device(self, levels, ijk, truncate):
+        """T matrices of several elements computed on the GPU: a list of
+        (T [(order+1)^dim, ndof], dof levels [ndof], dof ijk [ndof, dim])"""
+        lv = np.ascontiguousarray(levels, dtype=np.int32)
+        e = np.ascontiguousarray(ijk, dtype=np.int32).reshape(len(lv), self.dim)
+        n = len(lv)
+        nd = np.zeros(max(n, 1), dtype=np.int32)
+        st = self.L.fem_hmr_refined_element_t_matrices_device(self.h, int(truncate), n, _np_ptr(lv), _np_ptr(e), 0,
+                                                              _np_ptr(nd), None, None, None)
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_element_t_matrices_device")
+        cap, B = max(int(nd[:n].max()) if n else 1, 1), (self.order + 1) ** self.dim
+        T = np.zeros(n * B * cap)
+        dl = np.zeros(n * cap, dtype=np.int32)
+        di = np.zeros(n * cap * self.dim, dtype=np.int32)
+        st = self.L.fem_hmr_refined_element_t_matrices_device(self.h, int(truncate), n, _np_ptr(lv), _np_ptr(e), cap,
+                                                              _np_ptr(nd), _np_ptr(T), _np_ptr(dl), _np_ptr(di))
+        if st:
+            raise FemGpuError(st, "fem_hmr_refined_element_t_matrices_device")
+        T = T.reshape(n, B, cap)
+        dl = dl.reshape(n, cap)
+        di = di.reshape(n, cap, self.dim)
+        return [(T[i, :, :nd[i]], dl[i, :nd[i]], di[i, :nd[i]]) for i in range(n)]
 
 
 class FemModel:

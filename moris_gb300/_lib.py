@@ -78,6 +78,8 @@ SIGNATURES = {
     "fem_hmr_refined_active_elements": (I32, [P, P, P, P]),
     "fem_hmr_refined_element_t_matrix": (I32, [P, I32, P, I32, I32, P, P, P, P]),
     "fem_hmr_refined_mesh": (I32, [P, I32, P]),
+    "fem_hmr_refined_mesh_device": (I32, [P, I32, P]),
+    "fem_hmr_refined_element_t_matrices_device": (I32, [P, I32, I64, P, P, I32, P, P, P, P]),
     "fem_gpu_auto_integration_rule": (I32, [I32, I32, I32, P]),
     "fem_gpu_status_string": (C.c_char_p, [I32]),
     "fem_gpu_device_count": (I32, []),

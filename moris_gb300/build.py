@@ -20,7 +20,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 HOST_SRCS = ["fem_tables.cpp", "fem_host.cpp", "fem_hmr.cpp", "fem_xtk.cpp", "fem_vis.cpp"]
 CUDA_SRCS = ["fem_device.cu", "fem_solver.cu", "fem_probe.cu", "fem_learned_pc.cu", "fem_cluster.cu", "fem_sensitivity.cu",
-             "fem_multigrid.cu", "fem_xtk_device.cu"]
+             "fem_multigrid.cu", "fem_xtk_device.cu", "fem_hmr_device.cu"]
 # the device XFEM decomposition reproduces the host's floating-point results,
 # which are compiled without contraction
 EXTRA_FLAGS = {"fem_xtk_device.cu": ["-fmad=false"]}

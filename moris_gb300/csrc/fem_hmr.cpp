@@ -371,6 +371,64 @@ void leaves(const fem_hmr_refined* h, std::vector<std::pair<int, Idx>>& out) {
     }
 }
 
+// the hierarchy in the device's form (sorted keys per refined level)
+fem::HmrDevice device_form(const fem_hmr_refined* h) {
+    fem::HmrDevice d;
+    d.dim = h->dim;
+    d.p = h->p;
+    d.pad = h->pad;
+    d.nloc = h->nloc;
+    d.levels = max_level(h);
+    for (int k = 0; k < 3; ++k) d.ne[k] = h->ne[k];
+    for (int b = 0; b < h->nloc; ++b)
+        for (int k = 0; k < 3; ++k) d.local[b][k] = (int)h->local[b].v[k];
+    d.koff.push_back(0);
+    for (int l = 0; l < d.levels; ++l) {
+        std::vector<uint64_t> ks(h->refined[l].begin(), h->refined[l].end());
+        std::sort(ks.begin(), ks.end());
+        d.keys.insert(d.keys.end(), ks.begin(), ks.end());
+        d.koff.push_back((int64_t)d.keys.size());
+    }
+    return d;
+}
+
+// element T matrices of a list of elements on the GPU: per element its
+// columns (column-major by dof) and dofs
+fem_gpu_status element_t_device(const fem_hmr_refined* h, const std::vector<std::pair<int, Idx>>& els,
+                                bool truncate, std::vector<std::vector<double>>& Ts,
+                                std::vector<std::vector<Dof>>& Ds) {
+    const int64_t n = (int64_t)els.size();
+    const fem::HmrDevice d = device_form(h);
+    std::vector<int32_t> lv(n), nd(n);
+    std::vector<int64_t> ix((size_t)n * 3), toff(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        lv[i] = els[i].first;
+        for (int k = 0; k < 3; ++k) ix[i * 3 + k] = els[i].second.v[k];
+    }
+    fem_gpu_status st = fem::hmr_element_t_device(d, truncate, n, lv.data(), ix.data(), nd.data(), nullptr,
+                                                  nullptr, nullptr);
+    if (st != FEM_GPU_OK) return st;
+    for (int64_t i = 0; i < n; ++i) toff[i + 1] = toff[i] + (int64_t)nd[i] * h->nloc;
+    std::vector<double> T((size_t)std::max<int64_t>(toff[n], 1));
+    std::vector<int64_t> dofs((size_t)std::max<int64_t>(toff[n] / h->nloc, 1) * 4);
+    st = fem::hmr_element_t_device(d, truncate, n, lv.data(), ix.data(), nd.data(), toff.data(), T.data(),
+                                   dofs.data());
+    if (st != FEM_GPU_OK) return st;
+    Ts.assign(n, {});
+    Ds.assign(n, {});
+    for (int64_t i = 0; i < n; ++i) {
+        Ts[i].assign(T.begin() + toff[i], T.begin() + toff[i + 1]);
+        const int64_t d0 = toff[i] / h->nloc;
+        for (int j = 0; j < nd[i]; ++j) {
+            Dof df;
+            df.level = (int)dofs[(d0 + j) * 4];
+            for (int k = 0; k < 3; ++k) df.m.v[k] = dofs[(d0 + j) * 4 + 1 + k];
+            Ds[i].push_back(df);
+        }
+    }
+    return FEM_GPU_OK;
+}
+
 fem_gpu_status check_ijk(const fem_hmr_refined* h, int level, const int32_t* ijk, Idx& e) {
     if (level < 0 || level >= kMaxLevel || !ijk) return FEM_GPU_BAD_ARG;
     for (int k = 0; k < h->dim; ++k) e.v[k] = (int64_t)ijk[k] + ((int64_t)h->pad << level);
@@ -477,15 +535,24 @@ fem_gpu_status fem_hmr_refined_element_t_matrix(const fem_hmr_refined* h, int32_
     return FEM_GPU_OK;
 }
 
-fem_gpu_status fem_hmr_refined_mesh(const fem_hmr_refined* h, int32_t truncate, fem_hmr_mesh** out) {
+// The Lagrange mesh of the active elements with the node rows, the element T
+// matrices and node rows computed on the host or on the GPU (the same
+// numbers: see fem_hmr_device.cu)
+static fem_gpu_status build_mesh(const fem_hmr_refined* h, bool truncate, bool device, fem_hmr_mesh** out) {
     if (!h || !out) return FEM_GPU_BAD_ARG;
     *out = nullptr;
-    const int D = h->dim, L = max_level(h), npe = D == 2 ? 4 : 8;
+    const int D = h->dim, L = max_level(h), npe = D == 2 ? 4 : 8, B = h->nloc;
     std::vector<std::pair<int, Idx>> lv;
     leaves(h, lv);
     // element T matrices and the active bases they use, numbered by (level, ijk x fastest)
     std::vector<std::vector<double>> Ts(lv.size());
     std::vector<std::vector<Dof>> Ds(lv.size());
+    if (device) {
+        const fem_gpu_status st = element_t_device(h, lv, truncate, Ts, Ds);
+        if (st != FEM_GPU_OK) return st;
+    } else {
+        for (size_t i = 0; i < lv.size(); ++i) element_t(h, lv[i].first, lv[i].second, truncate, Ts[i], Ds[i]);
+    }
     std::vector<std::pair<uint64_t, Dof>> used;
     std::unordered_set<uint64_t> seen;
     auto dof_key = [&](const Dof& d) {
@@ -493,11 +560,9 @@ fem_gpu_status fem_hmr_refined_mesh(const fem_hmr_refined* h, int32_t truncate, 
         for (int k = D - 1; k >= 0; --k) key = (key << kIdxBits) | (uint64_t)d.m.v[k];
         return key;  // level, then z, y, x
     };
-    for (size_t i = 0; i < lv.size(); ++i) {
-        element_t(h, lv[i].first, lv[i].second, truncate != 0, Ts[i], Ds[i]);
+    for (size_t i = 0; i < lv.size(); ++i)
         for (auto& d : Ds[i])
             if (seen.insert(dof_key(d)).second) used.push_back({dof_key(d), d});
-    }
     std::sort(used.begin(), used.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
     std::unordered_map<uint64_t, int32_t> bid;
     for (size_t i = 0; i < used.size(); ++i) bid[used[i].first] = (int32_t)i;
@@ -505,53 +570,138 @@ fem_gpu_status fem_hmr_refined_mesh(const fem_hmr_refined* h, int32_t truncate, 
     m->dim = D;
     m->num_bases = (int64_t)used.size();
     m->t_off.push_back(0);
+    // nodes by first visit; the first visit evaluates the node's row
     std::unordered_map<uint64_t, int32_t> node;
+    std::vector<int64_t> first_elem;
     const int corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
     for (size_t i = 0; i < lv.size(); ++i) {
         const int l = lv[i].first;
         const Idx& e = lv[i].second;
-        const int B = h->nloc, nd = (int)Ds[i].size();
         for (int a = 0; a < npe; ++a) {
             Idx key;
             for (int k = 0; k < D; ++k) key.v[k] = (e.v[k] + corner[a][k]) << (L - l);
             auto it = node.find(pack(key));
             if (it == node.end()) {
                 const int32_t id = (int32_t)(m->coords.size() / D);
-                node[pack(key)] = id;
-                double x[3];
+                it = node.emplace(pack(key), id).first;
                 for (int k = 0; k < D; ++k) {
                     const double hL = h->len[k] / h->ne[k] / std::pow(2.0, L);
-                    x[k] = (double)(key.v[k] - ((int64_t)h->pad << L)) * hL;
-                    m->coords.push_back(x[k]);
+                    m->coords.push_back((double)(key.v[k] - ((int64_t)h->pad << L)) * hL);
                 }
-                // the element's local B-splines at the node, times its T
-                std::vector<double> lag(B);
-                for (int b = 0; b < B; ++b) {
-                    const Idx mb = h->local_basis(e, b);
-                    double v = 1.0;
-                    for (int k = 0; k < D; ++k) {
-                        const double hl = h->len[k] / h->ne[k] / std::pow(2.0, l);
-                        const double t = (x[k] + h->pad * h->len[k] / h->ne[k]) / hl - (double)(mb.v[k] - h->p);
-                        v *= cardinal(h->p, t);
-                    }
-                    lag[b] = v;
-                }
-                for (int j = 0; j < nd; ++j) {
-                    double s = 0.0;
-                    for (int b = 0; b < B; ++b) s += lag[b] * Ts[i][(size_t)j * B + b];
-                    if (std::abs(s) > 1e-12) {
-                        m->t_bases.push_back(bid[dof_key(Ds[i][j])]);
-                        m->t_w.push_back(s);
-                    }
-                }
-                m->t_off.push_back((int64_t)m->t_bases.size());
-                it = node.find(pack(key));
+                first_elem.push_back((int64_t)i);
             }
             m->cells.push_back(it->second);
         }
     }
+    const int64_t nn = (int64_t)first_elem.size();
+    // the rows: the element's local B-splines at the node, times its T
+    std::vector<int64_t> roff(nn + 1, 0);
+    for (int64_t k = 0; k < nn; ++k) roff[k + 1] = roff[k] + (int64_t)Ds[first_elem[k]].size();
+    std::vector<double> rows((size_t)std::max<int64_t>(roff[nn], 1));
+    if (device) {
+        std::vector<int32_t> lvl(lv.size()), nd(lv.size());
+        std::vector<int64_t> ix(lv.size() * 3), toff(lv.size() + 1, 0);
+        for (size_t i = 0; i < lv.size(); ++i) {
+            lvl[i] = lv[i].first;
+            nd[i] = (int32_t)Ds[i].size();
+            for (int k = 0; k < 3; ++k) ix[i * 3 + k] = lv[i].second.v[k];
+            toff[i + 1] = toff[i] + (int64_t)Ts[i].size();
+        }
+        std::vector<double> Tflat((size_t)std::max<int64_t>(toff[lv.size()], 1));
+        for (size_t i = 0; i < lv.size(); ++i) std::copy(Ts[i].begin(), Ts[i].end(), Tflat.begin() + toff[i]);
+        const fem::HmrDevice d = device_form(h);
+        const fem_gpu_status st =
+            fem::hmr_node_rows_device(d, h->len, nn, first_elem.data(), m->coords.data(), lvl.data(), ix.data(),
+                                      nd.data(), toff.data(), Tflat.data(), roff.data(), rows.data());
+        if (st != FEM_GPU_OK) {
+            delete m;
+            return st;
+        }
+    } else {
+        for (int64_t k = 0; k < nn; ++k) {
+            const size_t i = (size_t)first_elem[k];
+            const int l = lv[i].first;
+            const Idx& e = lv[i].second;
+            const double* x = m->coords.data() + k * D;
+            std::vector<double> lag(B);
+            for (int b = 0; b < B; ++b) {
+                const Idx mb = h->local_basis(e, b);
+                double v = 1.0;
+                for (int kk = 0; kk < D; ++kk) {
+                    const double hl = h->len[kk] / h->ne[kk] / std::pow(2.0, l);
+                    const double t = (x[kk] + h->pad * h->len[kk] / h->ne[kk]) / hl - (double)(mb.v[kk] - h->p);
+                    v *= cardinal(h->p, t);
+                }
+                lag[b] = v;
+            }
+            const int nd = (int)Ds[i].size();
+            for (int j = 0; j < nd; ++j) {
+                double s = 0.0;
+                for (int b = 0; b < B; ++b) s += lag[b] * Ts[i][(size_t)j * B + b];
+                rows[roff[k] + j] = s;
+            }
+        }
+    }
+    for (int64_t k = 0; k < nn; ++k) {
+        const auto& Di = Ds[first_elem[k]];
+        for (size_t j = 0; j < Di.size(); ++j) {
+            const double s = rows[roff[k] + j];
+            if (std::abs(s) > 1e-12) {
+                m->t_bases.push_back(bid[dof_key(Di[j])]);
+                m->t_w.push_back(s);
+            }
+        }
+        m->t_off.push_back((int64_t)m->t_bases.size());
+    }
     *out = m;
     return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_hmr_refined_mesh(const fem_hmr_refined* h, int32_t truncate, fem_hmr_mesh** out) {
+    return build_mesh(h, truncate != 0, false, out);
+}
+
+fem_gpu_status fem_hmr_refined_mesh_device(const fem_hmr_refined* h, int32_t truncate, fem_hmr_mesh** out) {
+    return build_mesh(h, truncate != 0, true, out);
+}
+
+fem_gpu_status fem_hmr_refined_element_t_matrices_device(const fem_hmr_refined* h, int32_t truncate, int64_t count,
+                                                         const int32_t* levels, const int32_t* ijk,
+                                                         int32_t capacity, int32_t* ndof, double* T,
+                                                         int32_t* dof_level, int32_t* dof_ijk) {
+    if (!h || count < 0 || (count > 0 && (!levels || !ijk || !ndof))) return FEM_GPU_BAD_ARG;
+    std::vector<std::pair<int, Idx>> els;
+    for (int64_t i = 0; i < count; ++i) {
+        Idx e;
+        const fem_gpu_status st = check_ijk(h, levels[i], ijk + i * h->dim, e);
+        if (st != FEM_GPU_OK) return st;
+        els.push_back({levels[i], e});
+    }
+    std::vector<std::vector<double>> Ts;
+    std::vector<std::vector<Dof>> Ds;
+    const fem_gpu_status st = element_t_device(h, els, truncate != 0, Ts, Ds);
+    if (st != FEM_GPU_OK) return st;
+    const int B = h->nloc;
+    bool fits = true;
+    for (int64_t i = 0; i < count; ++i) {
+        const int nd = (int)Ds[i].size();
+        ndof[i] = nd;
+        if (nd > capacity) {
+            fits = false;
+            continue;
+        }
+        for (int j = 0; j < nd; ++j) {
+            if (T)
+                for (int b = 0; b < B; ++b) T[((size_t)i * B + b) * capacity + j] = Ts[i][(size_t)j * B + b];
+            if (dof_level) dof_level[i * capacity + j] = Ds[i][j].level;
+            if (dof_ijk)
+                for (int k = 0; k < h->dim; ++k)
+                    dof_ijk[(i * capacity + j) * h->dim + k] =
+                        (int32_t)(Ds[i][j].m.v[k] - ((int64_t)h->pad << Ds[i][j].level));
+        }
+    }
+    if (!T && !dof_level && !dof_ijk) return FEM_GPU_OK;  // size query
+    return fits ? FEM_GPU_OK : FEM_GPU_BAD_ARG;
 }
 
 }  // extern "C"

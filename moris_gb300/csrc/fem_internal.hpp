@@ -162,6 +162,33 @@ fem_gpu_status assemble_set(fem_gpu_ctx* c, int set, const double* u, double* va
 fem_gpu_status noalloc_prepare(fem_gpu_ctx* c);
 // device memory of the sensitivity path (fem_sensitivity.cu)
 void sensitivity_release(fem_gpu_ctx* c);
+
+// Refined HMR meshes on the GPU (fem_hmr_device.cu): the hierarchy as the
+// device sees it -- the refined elements of every level as sorted packed keys
+// (HMR "mesh" coordinates counted from the first padding element, 20 bits per
+// direction), the element-local basis offsets and the sizes.
+constexpr int kHmrMaxLocal = 64;
+struct HmrDevice {
+    int dim = 0, p = 0, pad = 0, nloc = 0, levels = 0;  // levels: refined levels + 1
+    int64_t ne[3] = {1, 1, 1};
+    int local[kHmrMaxLocal][3] = {};
+    std::vector<uint64_t> keys;  // level-major, sorted within a level
+    std::vector<int64_t> koff;   // [levels + 1]
+};
+// element T matrices of `count` elements (level, mesh coordinates) computed
+// on the GPU: pass 1 fills ndof; with T != nullptr pass 2 writes, per element
+// i, T[toff[i] .. + nloc * ndof[i]) (column-major by dof, as the host's
+// element_t) and dofs[dof_off[i] .. + ndof[i]] as (level, m0, m1, m2)
+fem_gpu_status hmr_element_t_device(const HmrDevice& h, bool truncate, int64_t count, const int32_t* level,
+                                    const int64_t* idx, int32_t* ndof, const int64_t* toff, double* T,
+                                    int64_t* dofs);
+// node rows on the GPU: for every first visit (element elem[k], node
+// coordinates x[k*dim ..]), the element's local B-splines at the node times
+// its T: rows[roff[k] .. + ndof[elem[k]]) (same operations and order as the
+// host's evaluation)
+fem_gpu_status hmr_node_rows_device(const HmrDevice& h, const double* len, int64_t nfirst, const int64_t* elem,
+                                    const double* x, const int32_t* level, const int64_t* idx, const int32_t* ndof,
+                                    const int64_t* toff, const double* T, const int64_t* roff, double* rows);
 }  // namespace fem
 
 // one multigrid V-cycle z = V r on the legacy default stream (fem_multigrid.cu)

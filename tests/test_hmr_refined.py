@@ -217,3 +217,42 @@ def test_plane_strain_example_on_a_graded_mesh(torch):
     xi = [(-1.0, -1.0), (1.0, -1.0), (1.0, 1.0), (-1.0, 1.0)][a]
     sig = m.element_flux(0, [cell], [xi], torch.tensor(u, device="cuda"))[0]
     assert np.max(np.abs(sig[:3] - np.array([0.0, -1.0, -0.3]))) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# T matrices and node rows evaluated on the GPU
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", LABELS, ids=_label)
+def test_device_t_matrices_reproduce_the_reference(torch, case):
+    """The GPU's element T matrix of the fixture element equals the reference's
+    values exactly, with the host's columns (levels and ijk)."""
+    d, p, t = case
+    h = mg.RefinedHmr(d, (1,) * d, (2.0,) * d, p, staircase_buffer=p, padding_refinement=1)
+    h.refine([(0, (0,) * d)])
+    h.refine([(1, (0,) * d)])
+    [(T, dl, di)] = h.element_t_matrices_device([2], [(0,) * d], bool(t))
+    assert np.array_equal(T, FIXTURE[_label(case)])
+    _, hl, hi = h.element_t_matrix(2, (0,) * d, bool(t))
+    assert np.array_equal(dl, hl) and np.array_equal(di, hi)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", GRADED, ids=lambda c: "d%d-p%d-%s" % (c[0], c[2], "x".join(map(str, c[1]))))
+@pytest.mark.parametrize("truncate", [True, False], ids=["truncated", "plain"])
+def test_device_evaluation_equals_host(torch, case, truncate):
+    """Graded meshes (levels 0-3, 2-D and 3-D, orders 1-3): the T matrix of
+    every active element and the whole node-row mesh computed on the GPU are
+    the host's, bit for bit."""
+    d, ne, p = case
+    h = _graded(mg.RefinedHmr, d, ne, p)
+    lv, ijk = h.active_elements()
+    dev = h.element_t_matrices_device(lv, ijk, truncate)
+    for (l, e), (T, dl, di) in zip(zip(lv, ijk), dev):
+        Th, hl, hi = h.element_t_matrix(int(l), e, truncate)
+        assert np.array_equal(T, Th) and np.array_equal(dl, hl) and np.array_equal(di, hi), (l, e)
+    a, b = h.mesh(truncate, device=True), h.mesh(truncate)
+    assert a["num_bases"] == b["num_bases"]
+    for k in ("coords", "cells", "t_off", "t_bases", "t_w"):
+        assert np.array_equal(a[k], b[k]), k

@@ -158,18 +158,26 @@ __device__ __forceinline__ void stencil_rows(int n, int64_t N, const TS* __restr
     }
 }
 
-// power iteration step: y = D^-1 A x; dots[0] += y.y (in the level's precision)
+// power iteration step: y = D^-1 A (a x), a = 1 / sqrt(*xx) (1 without xx: x
+// is the previous step's y, normalised here instead of in a pass of its own);
+// dots[0] += y.y (in the level's precision)
 template <typename TS, typename TV>
 __global__ void mg_power(int n, const TS* __restrict__ S, const TV* __restrict__ dinv, const TV* __restrict__ x,
-                         TV* __restrict__ y, double* dots) {
+                         const double* __restrict__ xx, TV* __restrict__ y, double* dots) {
     const int64_t N = (int64_t)n * n * n;
+    double a = 1.0;
+    if (xx) {
+        const double d = *xx;
+        a = d > 0.0 ? 1.0 / sqrt(d) : 0.0;
+    }
+    const TV at = (TV)a;
     double acc = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
         TV s[3];
         stencil_rows<TS, TV>(n, N, S, x, i, s);
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
-            const TV v = dinv[f * N + i] * s[f];
+            const TV v = dinv[f * N + i] * s[f] * at;
             y[f * N + i] = v;
             acc += (double)v * (double)v;
         }
@@ -190,17 +198,6 @@ __global__ void mg_scale(int64_t m, double a, const TV* __restrict__ y, TV* __re
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
         x[t] = (TV)(a * (double)y[t]);
 }
-// x = y / sqrt(*yy) (0 when *yy is not positive), the power-iteration
-// normalisation without a host round trip
-template <typename TV>
-__global__ void mg_scale_norm(int64_t m, const double* __restrict__ yy, const TV* __restrict__ y,
-                              TV* __restrict__ x) {
-    const double d = *yy;
-    const double a = d > 0.0 ? 1.0 / sqrt(d) : 0.0;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x)
-        x[t] = (TV)(a * (double)y[t]);
-}
-
 // splitmix64 uniform in [-0.5, 0.5): element t of the stream of `seed`
 __global__ void mg_random(int64_t m, uint64_t seed, double* __restrict__ x) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (int64_t)gridDim.x * blockDim.x) {
@@ -639,14 +636,15 @@ double power_lambda(fem_mg* g, const fem_mg::Level& L, const TS* S, const TV* di
         mg_convert<double, TV><<<vb, kTpb>>>(3 * L.N, px, y);
         mg_scale<TV><<<vb, kTpb>>>(3 * L.N, 1.0, y, x);
     }
-    // squared norms on the device: pd[0] = |x0|^2, pd[it + 1] = |D^-1 A x_it|^2,
-    // with x_(it+1) normalised there; the host reads them once at the end
+    // squared norms on the device: pd[0] = |x0|^2, pd[it + 1] = |y_it|^2 with
+    // y_it = D^-1 A x_it and x_(it+1) = y_it / |y_it|, the normalisation done by
+    // the next step as it reads y_it; the host reads the norms once at the end
     double* pd = g->pdots;
     cudaMemset(pd, 0, (iters + 1) * sizeof(double));
     mg_sumsq<TV><<<vb, kTpb>>>(3 * L.N, x, pd);
     for (int it = 0; it < iters; ++it) {
-        mg_power<TS, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, S, dinv, x, y, pd + it + 1);
-        mg_scale_norm<TV><<<vb, kTpb>>>(3 * L.N, pd + it + 1, y, x);
+        mg_power<TS, TV><<<blocks_for(L.N, kTpb), kTpb>>>(L.n, S, dinv, x, it ? pd + it : nullptr, y, pd + it + 1);
+        std::swap(x, y);
     }
     std::vector<double> h(iters + 1, 0.0);
     cudaMemcpy(h.data(), pd, (iters + 1) * sizeof(double), cudaMemcpyDeviceToHost);

@@ -79,6 +79,7 @@ struct SetData {
     DeviceBuf d_sref;       // side: facet / cell shape values per ordinal and point
     DeviceBuf d_sgeo;       // side: per facet and point w*, normal, J^-1; 1/h (built once)
     DeviceBuf d_igoff, d_igx, d_igxi;            // cut clusters: integration cells
+    DeviceBuf d_adjul;      // cut clusters: pdof values of u and lambda per cluster, cluster of each cell (sensitivities)
     DeviceBuf d_fcoff, d_fcx, d_fcxl, d_fcxf;    // double-sided: facets
     DeviceBuf d_EF, d_vol;
     int ngp = 0;            // Gauss points of the set's rule

@@ -207,20 +207,35 @@ __device__ Dual<M> tet_volume(const Dual<M> X[4][3]) {
     return (1.0 / 6.0) * det;
 }
 
-// cut clusters: one CTA per cluster, one thread per integration cell
-__global__ void adjoint_tets(AdjArgs A, CutSetDev S) {
-    __shared__ double U[24], L[24], X[24];
+// Cut clusters: F = sum_q w detJ (1/2 sigma(u):eps(u) - sigma(u):eps(lambda))
+// over every integration cell in forward-mode dual arithmetic with one slot
+// per tet vertex, dF/dt added to G of the moving vertices.  One thread per
+// integration cell of the whole set: the cells of a cluster (1 to about 100)
+// rarely fill whole warps, and on this GPU
+// an FP64 warp instruction costs the pipe the same however few of its lanes
+// are active.  The cluster's pdof values u and lambda are gathered once per
+// cluster first (adjoint_cluster_values), which also writes every cell's
+// cluster index.
+__global__ void adjoint_cluster_values(AdjArgs A, CutSetDev S, double* UL /*[neq][48]*/, int32_t* cell_cluster) {
     const int64_t e = blockIdx.x;
     if (e >= S.neq) return;
-    const int tid = threadIdx.x;
-    for (int i = tid; i < 24; i += blockDim.x) X[i] = S.xe[e * 24 + i];
+    for (int64_t g = S.ig_off[e] + threadIdx.x; g < S.ig_off[e + 1]; g += blockDim.x) cell_cluster[g] = (int32_t)e;
     const int nb = S.nb[e];
-    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.u, A.nu, U, tid, blockDim.x);
-    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.lam, A.nu, L, tid, blockDim.x);
-    __syncthreads();
-    const double jd[3] = {0.5 * (X[18] - X[0]), 0.5 * (X[19] - X[1]), 0.5 * (X[20] - X[2])};
-    const double lam = S.E[e] * S.lam_c, mu = S.E[e] * S.mu_c;
-    for (int64_t g = S.ig_off[e] + tid; g < S.ig_off[e + 1]; g += blockDim.x) {
+    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.u, A.nu, UL + e * 48, threadIdx.x, blockDim.x);
+    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.lam, A.nu, UL + e * 48 + 24, threadIdx.x,
+                blockDim.x);
+}
+
+__global__ void adjoint_tets_flat(AdjArgs A, CutSetDev S, const double* __restrict__ UL,
+                                  const int32_t* __restrict__ cell_cluster, int64_t ncells) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ncells;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = cell_cluster[g];
+        const double* X = S.xe + e * 24;
+        const double* U = UL + e * 48;
+        const double* L = U + 24;
+        const double jd[3] = {0.5 * (X[18] - X[0]), 0.5 * (X[19] - X[1]), 0.5 * (X[20] - X[2])};
+        const double lam = S.E[e] * S.lam_c, mu = S.E[e] * S.mu_c;
         Dual<4> Xv[4][3], xi[4][3];
         bool mv[4];
         int32_t vids[4];
@@ -276,142 +291,182 @@ struct IfSetDev {
     const int32_t* link;   // [neq][4]: leader (set, eq), follower (set, eq) among the cut sets
 };
 
-// interface clusters: one CTA per cluster; threads over facets, then over the
-// leader / follower integration cells (cluster volumes of the SP)
-__global__ void adjoint_interface(AdjArgs A, IfSetDev S, const CutSetDev* cuts) {
-    __shared__ double U[48], L[48], X[48];
-    __shared__ double sums[4];  // A, B, C, area
+// The interface sum, flattened like the cut cells (a cluster has a few
+// facets).  The facet integrals are formed once, in dual arithmetic:
+//   iface_cluster_values   per cluster: pdof values of u and lambda of both
+//                          sides, each facet's cluster index;
+//   iface_facets           one thread per facet: the values A, B, C, |G| into
+//                          the cluster sums, the derivatives kept per facet;
+//   iface_apply            one thread per facet: dF/dt with the now known
+//                          cluster sums (w_L, w_F, gamma);
+//   iface_volumes          one thread per (cluster, side, cell of the linked
+//                          cut cluster): dF/dV through w_L, w_F and gamma.
+constexpr int kIfParts = 12;  // dA, dB, dC, d|G| for the three vertices
+
+__global__ void iface_cluster_values(AdjArgs A, IfSetDev S, double* UL /*[neq][96]*/, int32_t* facet_cluster) {
     const int64_t e = blockIdx.x;
     if (e >= S.neq) return;
-    const int tid = threadIdx.x;
-    for (int i = tid; i < 48; i += blockDim.x) X[i] = S.xe[e * 48 + i];
+    for (int64_t f = S.fc_off[e] + threadIdx.x; f < S.fc_off[e + 1]; f += blockDim.x) facet_cluster[f] = (int32_t)e;
     for (int s = 0; s < 2; ++s) {
         const int nb = S.nb[2 * e + s];
-        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.u, A.nu, U + 24 * s, tid,
-                    blockDim.x);
-        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.lam, A.nu, L + 24 * s, tid,
-                    blockDim.x);
+        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.u, A.nu,
+                    UL + e * 96 + 24 * s, threadIdx.x, blockDim.x);
+        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.lam, A.nu,
+                    UL + e * 96 + 48 + 24 * s, threadIdx.x, blockDim.x);
     }
-    if (tid < 4) sums[tid] = 0.0;
-    __syncthreads();
-    const double Es[2] = {S.E[e], S.EF[e]};
-    const double beta = S.beta_sym ? -1.0 : 1.0;
-    const double vl = S.vol[2 * e] / Es[0], vf = S.vol[2 * e + 1] / Es[1], Ssum = vl + vf;
-    const double wl = vl / Ssum, wf = vf / Ssum;
-    // pass 1: facet integrals (values) for the cluster sums
-    // pass 2: their derivatives, scaled by the now known weights
-    const int64_t f0 = S.fc_off[e], f1 = S.fc_off[e + 1];
-    for (int pass = 0; pass < 2; ++pass) {
-        for (int64_t f = f0 + tid; f < f1; f += blockDim.x) {
-            Dual<3> Xv[3][3];
-            bool mv[3];
-            int32_t vids[3];
-            for (int k = 0; k < 3; ++k) {
-                vids[k] = S.vid[f * 3 + k];
-                vertex_dual<3>(A, vids[k], k, Xv[k], mv[k]);
-            }
-            // facet detJ |(x0-x2) x (x1-x2)| / 2 and the unit normal
-            Dual<3> a[3], b[3], cr[3];
-            for (int d = 0; d < 3; ++d) {
-                a[d] = Xv[0][d] - Xv[2][d];
-                b[d] = Xv[1][d] - Xv[2][d];
-            }
-            cr[0] = a[1] * b[2] - a[2] * b[1];
-            cr[1] = a[2] * b[0] - a[0] * b[2];
-            cr[2] = a[0] * b[1] - a[1] * b[0];
-            const Dual<3> nn = dsqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-            if (!(nn.v > 0.0)) continue;
-            const Dual<3> inv = dinv(nn);
-            const Dual<3> n[3] = {cr[0] * inv, cr[1] * inv, cr[2] * inv};
-            const Dual<3> detJ = 0.5 * nn;
-            Dual<3> xi[2][3][3];  // [side][vertex][d]
+}
+
+__global__ void iface_facets(AdjArgs A, IfSetDev S, const double* __restrict__ UL,
+                             const int32_t* __restrict__ facet_cluster, int64_t nfacets, double* sums /*[neq][4]*/,
+                             double* parts /*[nf][kIfParts]*/) {
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nfacets;
+         f += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = facet_cluster[f];
+        const double* X = S.xe + e * 48;
+        const double* U = UL + e * 96;
+        const double* L = U + 48;
+        const double Es[2] = {S.E[e], S.EF[e]};
+        const double beta = S.beta_sym ? -1.0 : 1.0;
+        double* P = parts + f * kIfParts;
+        Dual<3> Xv[3][3];
+        bool mv[3];
+        for (int k = 0; k < 3; ++k) vertex_dual<3>(A, S.vid[f * 3 + k], k, Xv[k], mv[k]);
+        // facet detJ |(x0-x2) x (x1-x2)| / 2 and the unit normal
+        Dual<3> a[3], b[3], cr[3];
+        for (int d = 0; d < 3; ++d) {
+            a[d] = Xv[0][d] - Xv[2][d];
+            b[d] = Xv[1][d] - Xv[2][d];
+        }
+        cr[0] = a[1] * b[2] - a[2] * b[1];
+        cr[1] = a[2] * b[0] - a[0] * b[2];
+        cr[2] = a[0] * b[1] - a[1] * b[0];
+        const Dual<3> nn = dsqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        if (!(nn.v > 0.0)) {
+            for (int k = 0; k < kIfParts; ++k) P[k] = 0.0;
+            continue;
+        }
+        const Dual<3> inv = dinv(nn);
+        const Dual<3> n[3] = {cr[0] * inv, cr[1] * inv, cr[2] * inv};
+        const Dual<3> detJ = 0.5 * nn;
+        Dual<3> xi[2][3][3];  // [side][vertex][d]
+        for (int s = 0; s < 2; ++s) {
+            const double* Xs = X + 24 * s;
+            for (int k = 0; k < 3; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    const double jd = 0.5 * (Xs[18 + d] - Xs[d]);
+                    xi[s][k][d] = (-1.0 - Xs[d] / jd) + (1.0 / jd) * Xv[k][d];
+                }
+        }
+        Dual<3> fa(0.0), fb(0.0), fc(0.0), fr(0.0);
+        for (int q = 0; q < S.ngp; ++q) {
+            const double z0 = S.gp[q * 2], z1 = S.gp[q * 2 + 1];
+            const double Nf[3] = {z0, z1, 1.0 - z0 - z1};
+            Dual<3> uv[2][3], Gu[2][3][3], lv[2][3], Gl[2][3][3];
             for (int s = 0; s < 2; ++s) {
                 const double* Xs = X + 24 * s;
-                for (int k = 0; k < 3; ++k)
-                    for (int d = 0; d < 3; ++d) {
-                        const double jd = 0.5 * (Xs[18 + d] - Xs[d]);
-                        xi[s][k][d] = (-1.0 - Xs[d] / jd) + (1.0 / jd) * Xv[k][d];
-                    }
+                const double jd[3] = {0.5 * (Xs[18] - Xs[0]), 0.5 * (Xs[19] - Xs[1]), 0.5 * (Xs[20] - Xs[2])};
+                Dual<3> xq[3];
+                for (int d = 0; d < 3; ++d) {
+                    xq[d] = Dual<3>(0.0);
+                    for (int k = 0; k < 3; ++k) axpy(Nf[k], xi[s][k][d], xq[d]);
+                }
+                hex_field<3>(xq, jd, U + 24 * s, uv[s], Gu[s]);
+                hex_field<3>(xq, jd, L + 24 * s, lv[s], Gl[s]);
             }
-            Dual<3> fa(0.0), fb(0.0), fc(0.0), fr(0.0);
-            for (int q = 0; q < S.ngp; ++q) {
-                const double z0 = S.gp[q * 2], z1 = S.gp[q * 2 + 1];
-                const double Nf[3] = {z0, z1, 1.0 - z0 - z1};
-                Dual<3> uv[2][3], Gu[2][3][3], lv[2][3], Gl[2][3][3];
-                for (int s = 0; s < 2; ++s) {
-                    const double* Xs = X + 24 * s;
-                    const double jd[3] = {0.5 * (Xs[18] - Xs[0]), 0.5 * (Xs[19] - Xs[1]), 0.5 * (Xs[20] - Xs[2])};
-                    Dual<3> xq[3];
-                    for (int d = 0; d < 3; ++d) {
-                        xq[d] = Dual<3>(0.0);
-                        for (int k = 0; k < 3; ++k) axpy(Nf[k], xi[s][k][d], xq[d]);
-                    }
-                    hex_field<3>(xq, jd, U + 24 * s, uv[s], Gu[s]);
-                    hex_field<3>(xq, jd, L + 24 * s, lv[s], Gl[s]);
-                }
-                // tractions t_s(.) = sigma_s(.) n
-                Dual<3> tu[2][3], tl[2][3];
-                for (int s = 0; s < 2; ++s) {
-                    Dual<3> Su[3][3], Sl[3][3];
-                    stress<3>(Gu[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Su);
-                    stress<3>(Gl[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Sl);
-                    for (int i = 0; i < 3; ++i) {
-                        tu[s][i] = Su[i][0] * n[0] + Su[i][1] * n[1] + Su[i][2] * n[2];
-                        tl[s][i] = Sl[i][0] * n[0] + Sl[i][1] * n[1] + Sl[i][2] * n[2];
-                    }
-                }
-                Dual<3> qa(0.0), qb(0.0), qc(0.0);
+            // tractions t_s(.) = sigma_s(.) n
+            Dual<3> tu[2][3], tl[2][3];
+            for (int s = 0; s < 2; ++s) {
+                Dual<3> Su[3][3], Sl[3][3];
+                stress<3>(Gu[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Su);
+                stress<3>(Gl[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Sl);
                 for (int i = 0; i < 3; ++i) {
-                    const Dual<3> ju = uv[0][i] - uv[1][i], jl = lv[0][i] - lv[1][i];
-                    qa = qa + beta * (tl[0][i] * ju) - jl * tu[0][i];
-                    qb = qb + beta * (tl[1][i] * ju) - jl * tu[1][i];
-                    qc = qc + jl * ju;
+                    tu[s][i] = Su[i][0] * n[0] + Su[i][1] * n[1] + Su[i][2] * n[2];
+                    tl[s][i] = Sl[i][0] * n[0] + Sl[i][1] * n[1] + Sl[i][2] * n[2];
                 }
-                const Dual<3> ws = S.gw[q] * detJ;
-                fa = fa + ws * qa;
-                fb = fb + ws * qb;
-                fc = fc + ws * qc;
-                fr = fr + ws;
             }
-            if (pass == 0) {
-                atomicAdd(&sums[0], fa.v);
-                atomicAdd(&sums[1], fb.v);
-                atomicAdd(&sums[2], fc.v);
-                atomicAdd(&sums[3], fr.v);
-            } else {
-                // F = -(wL A + wF B + gamma C), gamma = 2 alpha |G| / S
-                const double gamma = 2.0 * S.alpha * sums[3] / Ssum;
-                const double dg_darea = 2.0 * S.alpha / Ssum;
-                for (int k = 0; k < 3; ++k)
-                    if (mv[k])
-                        atomicAdd(A.G + vids[k],
-                                  -(wl * fa.d[k] + wf * fb.d[k] + gamma * fc.d[k] + sums[2] * dg_darea * fr.d[k]));
+            Dual<3> qa(0.0), qb(0.0), qc(0.0);
+            for (int i = 0; i < 3; ++i) {
+                const Dual<3> ju = uv[0][i] - uv[1][i], jl = lv[0][i] - lv[1][i];
+                qa = qa + beta * (tl[0][i] * ju) - jl * tu[0][i];
+                qb = qb + beta * (tl[1][i] * ju) - jl * tu[1][i];
+                qc = qc + jl * ju;
             }
+            const Dual<3> ws = S.gw[q] * detJ;
+            fa = fa + ws * qa;
+            fb = fb + ws * qb;
+            fc = fc + ws * qc;
+            fr = fr + ws;
         }
-        __syncthreads();
+        atomicAdd(sums + e * 4 + 0, fa.v);
+        atomicAdd(sums + e * 4 + 1, fb.v);
+        atomicAdd(sums + e * 4 + 2, fc.v);
+        atomicAdd(sums + e * 4 + 3, fr.v);
+        for (int k = 0; k < 3; ++k) {
+            // a vertex that does not move has no derivative slot
+            P[k] = mv[k] ? fa.d[k] : 0.0;
+            P[3 + k] = mv[k] ? fb.d[k] : 0.0;
+            P[6 + k] = mv[k] ? fc.d[k] : 0.0;
+            P[9 + k] = mv[k] ? fr.d[k] : 0.0;
+        }
     }
-    // cluster volumes: dF/dV through w_L, w_F and gamma
-    const double gamma = 2.0 * S.alpha * sums[3] / Ssum;
-    const double dwl_dvl = vf / (Ssum * Ssum), dwl_dvf = -vl / (Ssum * Ssum);
-    const double dg_dv = -gamma / Ssum;
-    for (int side = 0; side < 2; ++side) {
-        const CutSetDev& C = cuts[S.link[e * 4 + side * 2]];
-        const int64_t ce = S.link[e * 4 + side * 2 + 1];
-        const double dwl = side == 0 ? dwl_dvl : dwl_dvf;
-        // dF/dvol = -((A - B) dwL/dv + C dgamma/dv) / E_side
-        const double coef = -((sums[0] - sums[1]) * dwl + sums[2] * dg_dv) / Es[side];
-        for (int64_t g = C.ig_off[ce] + tid; g < C.ig_off[ce + 1]; g += blockDim.x) {
-            Dual<4> Xv[4][3];
-            bool mv[4];
-            int32_t vids[4];
-            for (int k = 0; k < 4; ++k) {
-                vids[k] = C.vid[g * 4 + k];
-                vertex_dual<4>(A, vids[k], k, Xv[k], mv[k]);
-            }
-            const Dual<4> vol = tet_volume<4>(Xv);
-            for (int k = 0; k < 4; ++k)
-                if (mv[k]) atomicAdd(A.G + vids[k], coef * vol.d[k]);
+}
+
+// the cluster's Nitsche weights and gamma from its sums and volumes
+__device__ __forceinline__ void iface_weights(const IfSetDev& S, int64_t e, double& wl, double& wf, double& Ssum) {
+    const double vl = S.vol[2 * e] / S.E[e], vf = S.vol[2 * e + 1] / S.EF[e];
+    Ssum = vl + vf;
+    wl = vl / Ssum;
+    wf = vf / Ssum;
+}
+
+__global__ void iface_apply(AdjArgs A, IfSetDev S, const int32_t* __restrict__ facet_cluster, int64_t nfacets,
+                            const double* __restrict__ sums, const double* __restrict__ parts) {
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nfacets;
+         f += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = facet_cluster[f];
+        double wl, wf, Ssum;
+        iface_weights(S, e, wl, wf, Ssum);
+        // F = -(wL A + wF B + gamma C), gamma = 2 alpha |G| / S
+        const double gamma = 2.0 * S.alpha * sums[e * 4 + 3] / Ssum;
+        const double dg_darea = 2.0 * S.alpha / Ssum;
+        const double* P = parts + f * kIfParts;
+        for (int k = 0; k < 3; ++k) {
+            const double g = -(wl * P[k] + wf * P[3 + k] + gamma * P[6 + k] + sums[e * 4 + 2] * dg_darea * P[9 + k]);
+            if (P[k] != 0.0 || P[3 + k] != 0.0 || P[6 + k] != 0.0 || P[9 + k] != 0.0)
+                atomicAdd(A.G + S.vid[f * 3 + k], g);
         }
+    }
+}
+
+// items: (interface cluster e, side) per cell of the linked cut cluster
+__global__ void iface_volumes(AdjArgs A, IfSetDev S, const CutSetDev* cuts, int64_t nitems,
+                              const int64_t* __restrict__ item_e, const int64_t* __restrict__ item_cell,
+                              const double* __restrict__ sums) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nitems;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t es = item_e[t], e = es >> 1;
+        const int side = (int)(es & 1);
+        const CutSetDev& C = cuts[S.link[e * 4 + side * 2]];
+        const int64_t g = item_cell[t];
+        double wl, wf, Ssum;
+        iface_weights(S, e, wl, wf, Ssum);
+        const double vl = S.vol[2 * e] / S.E[e], vf = S.vol[2 * e + 1] / S.EF[e];
+        const double gamma = 2.0 * S.alpha * sums[e * 4 + 3] / Ssum;
+        const double dwl = side == 0 ? vf / (Ssum * Ssum) : -vl / (Ssum * Ssum);
+        const double dg_dv = -gamma / Ssum;
+        const double Es = side == 0 ? S.E[e] : S.EF[e];
+        // dF/dvol = -((A - B) dwL/dv + C dgamma/dv) / E_side
+        const double coef = -((sums[e * 4 + 0] - sums[e * 4 + 1]) * dwl + sums[e * 4 + 2] * dg_dv) / Es;
+        Dual<4> Xv[4][3];
+        bool mv[4];
+        int32_t vids[4];
+        for (int k = 0; k < 4; ++k) {
+            vids[k] = C.vid[g * 4 + k];
+            vertex_dual<4>(A, vids[k], k, Xv[k], mv[k]);
+        }
+        const Dual<4> vol = tet_volume<4>(Xv);
+        for (int k = 0; k < 4; ++k)
+            if (mv[k]) atomicAdd(A.G + vids[k], coef * vol.d[k]);
     }
 }
 
@@ -502,6 +557,7 @@ void sensitivity_release(fem_gpu_ctx* c) {
     for (auto& s : c->sets) {
         dfree(s.d_vid);
         dfree(s.d_link);
+        dfree(s.d_adjul);
     }
 }
 
@@ -649,7 +705,7 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
     A.nu = c->num_used;
     // cut sets
     std::vector<CutSetDev> cuts;
-    std::vector<int> cut_index(c->sets.size(), -1);
+    std::vector<int> cut_index(c->sets.size(), -1), cut_set;  // set -> cut index, cut index -> set
     std::vector<std::pair<int32_t, int64_t>> cell_cluster(c->num_cells, {-1, -1});
     for (size_t k = 0; k < c->sets.size(); ++k) {
         SetData& s = c->sets[k];
@@ -674,12 +730,30 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         d.gw = (const double*)s.d_gw.p;
         d.ngp = s.ngp;
         cut_index[k] = (int)cuts.size();
+        cut_set.push_back((int)k);
         for (int64_t i = 0; i < s.neq; ++i) cell_cluster[s.ip_cell[i]] = {(int32_t)cuts.size(), i};
         cuts.push_back(d);
     }
-    for (const CutSetDev& d : cuts) {
-        adjoint_tets<<<(unsigned)std::max<int64_t>(d.neq, 1), 64, 0, st>>>(A, d);
-        c->launches++;
+    for (size_t k = 0, ci = 0; k < c->sets.size(); ++k) {
+        if (cut_index[k] < 0) continue;
+        SetData& s = c->sets[k];
+        const CutSetDev& d = cuts[ci++];
+        const int64_t ncells = s.ig_off.empty() ? 0 : s.ig_off.back();
+        // per-cluster pdof values of u and lambda, then one thread per cell
+        // [neq][48] doubles, then [ncells] cluster indices
+        const size_t need = (size_t)d.neq * 48 * sizeof(double) + (size_t)std::max<int64_t>(ncells, 1) * sizeof(int32_t);
+        if (!s.d_adjul.p || s.d_adjul.bytes < need) {
+            dfree(s.d_adjul);
+            if ((e = cudaMalloc(&s.d_adjul.p, need)) != cudaSuccess) return sfail(c, e, "adjoint cluster values");
+            s.d_adjul.bytes = need;
+        }
+        double* UL = (double*)s.d_adjul.p;
+        int32_t* cc = reinterpret_cast<int32_t*>(UL + (size_t)d.neq * 48);
+        adjoint_cluster_values<<<(unsigned)std::max<int64_t>(d.neq, 1), 64, 0, st>>>(A, d, UL, cc);
+        const unsigned grid =
+            (unsigned)std::max<int64_t>(1, std::min<int64_t>((ncells + 63) / 64, (int64_t)sm_count() * 16));
+        adjoint_tets_flat<<<grid, 64, 0, st>>>(A, d, UL, cc, ncells);
+        c->launches += 2;
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return sfail(c, e, "adjoint tets");
     DeviceBuf dcuts;
@@ -728,8 +802,55 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         d.ngp = s.ngp;
         d.vol = (const double*)s.d_vol.p;
         d.link = (const int32_t*)s.d_link.p;
-        adjoint_interface<<<(unsigned)std::max<int64_t>(s.neq, 1), 64, 0, st>>>(A, d, (const CutSetDev*)dcuts.p);
-        c->launches++;
+        // scratch: per cluster U, L (96) and sums (4); per facet the cluster
+        // index and the derivative parts; the volume items
+        const int64_t nf = s.fc_off.empty() ? 0 : s.fc_off.back();
+        std::vector<int64_t> item_e, item_cell;
+        for (int64_t i = 0; i < s.neq; ++i)
+            for (int side = 0; side < 2; ++side) {
+                const int cs = s.link[i * 4 + side * 2];
+                const int64_t ce = s.link[i * 4 + side * 2 + 1];
+                const std::vector<int64_t>& io = c->sets[cut_set[cs]].ig_off;
+                for (int64_t g = io[ce]; g < io[ce + 1]; ++g) {
+                    item_e.push_back(i * 2 + side);
+                    item_cell.push_back(g);
+                }
+            }
+        const int64_t ni = (int64_t)item_e.size();
+        const size_t need = (size_t)s.neq * 100 * sizeof(double) + (size_t)std::max<int64_t>(nf, 1) * kIfParts * sizeof(double) +
+                            (size_t)std::max<int64_t>(nf, 1) * sizeof(int32_t);
+        if (!s.d_adjul.p || s.d_adjul.bytes < need) {
+            dfree(s.d_adjul);
+            if ((e = cudaMalloc(&s.d_adjul.p, need)) != cudaSuccess) {
+                r = sfail(c, e, "interface scratch");
+                break;
+            }
+            s.d_adjul.bytes = need;
+        }
+        double* UL = (double*)s.d_adjul.p;
+        double* sums = UL + (size_t)s.neq * 96;
+        double* parts = sums + (size_t)s.neq * 4;
+        int32_t* fcl = reinterpret_cast<int32_t*>(parts + (size_t)std::max<int64_t>(nf, 1) * kIfParts);
+        DeviceBuf ditem_e, ditem_c;
+        if ((e = upload(ditem_e, item_e, st)) != cudaSuccess || (e = upload(ditem_c, item_cell, st)) != cudaSuccess) {
+            dfree(ditem_e);
+            dfree(ditem_c);
+            r = sfail(c, e, "interface volume items");
+            break;
+        }
+        cudaMemsetAsync(sums, 0, (size_t)s.neq * 4 * sizeof(double), st);
+        const auto grid_of = [](int64_t n) {
+            return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 63) / 64, (int64_t)sm_count() * 16));
+        };
+        iface_cluster_values<<<(unsigned)std::max<int64_t>(s.neq, 1), 64, 0, st>>>(A, d, UL, fcl);
+        iface_facets<<<grid_of(nf), 64, 0, st>>>(A, d, UL, fcl, nf, sums, parts);
+        iface_apply<<<grid_of(nf), 64, 0, st>>>(A, d, fcl, nf, sums, parts);
+        iface_volumes<<<grid_of(ni), 64, 0, st>>>(A, d, (const CutSetDev*)dcuts.p, ni, (const int64_t*)ditem_e.p,
+                                                  (const int64_t*)ditem_c.p, sums);
+        c->launches += 4;
+        cudaStreamSynchronize(st);
+        dfree(ditem_e);
+        dfree(ditem_c);
         if ((e = cudaGetLastError()) != cudaSuccess) {
             r = sfail(c, e, "adjoint interface");
             break;

@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
                 vox_next = voxel(i + 1, live_next);
                 fetch_mask(vox_next, live_next, mk_next);
             }
-            // lane 0 polls, the warp follows its verdict (tcgen05.ld needs all lanes)
+            // lane 0 polls, the warp follows its result (tcgen05.ld needs all lanes)
             int ok = 0;
             if (lane == 0) ok = mbar_wait_or_abort(acc_full(a), (uint32_t)(i / kAcc) & 1u, abort);
             if (!__shfl_sync(0xffffffffu, ok, 0)) {

@@ -416,7 +416,7 @@ def run_c4(stream, args):
     torch.cuda.synchronize()
     ms_adj = e0.elapsed_time(e1) / reps
     t1 = time.perf_counter()
-    m.gen_dqdp(G, c["cols"], c["vals"], len(c["p"]), dqdp)
+    m.gen_dqdp(G, None, None, len(c["p"]), dqdp)  # the field stored at build
     ms_chain = (time.perf_counter() - t1) * 1e3
     dq = dqdp.cpu().numpy()
     # central FD (h = 1e-6) of Q - lambda^T R at fixed u, lambda on 50 random active coefficients

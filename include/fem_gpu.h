@@ -491,9 +491,19 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* ctx, const double* u, const dou
    mean of their background nodes, phi at a background node = sum_j
    tmat[node][k] p_(cols[node][k]) (width entries per node, e.g. the cubic
    B-spline field of fem_gen_bspline_tmatrix).  G, dqdp: device; cols, tmat:
-   host [num_background_nodes][width]; dqdp overwritten. */
+   host [num_background_nodes][width] (validated and stored as by
+   fem_gpu_set_level_set_field), or both NULL for the stored field, whose
+   sizes must then match; dqdp overwritten. */
 fem_gpu_status fem_gen_dqdp(fem_gpu_ctx* ctx, const double* G, int64_t num_background_nodes, int32_t width,
                             const int32_t* cols, const double* tmat, int64_t num_coefs, double* dqdp);
+/* the design variables' level-set field, validated (every id in
+   [0, num_coefs)) and kept on the device for the whole optimisation, so that
+   each fem_gen_dqdp call moves no table (the reference's design-variable
+   interface keeps the field's coefficient map the same way,
+   FEM/MSI/src/cl_MSI_Design_Variable_Interface.hpp:35-240).  cols, tmat: host
+   [num_background_nodes][width]. */
+fem_gpu_status fem_gpu_set_level_set_field(fem_gpu_ctx* ctx, int64_t num_background_nodes, int32_t width,
+                                           const int32_t* cols, const double* tmat, int64_t num_coefs);
 /* tensor-product B-spline field of `order` on a uniform grid of
    num_coefs[d] = n_d + order coefficients over [0, lengths[d]] (HMR
    numbering, i fastest; BSpline_Field::get_dfield_dadvs,

@@ -369,7 +369,26 @@ class FemModel:
     def drdp_adjoint(self, u, lam, G):
         self._check(self.L.fem_gpu_drdp_adjoint(self.h, _dev_ptr(u), _dev_ptr(lam), _dev_ptr(G)), "drdp_adjoint")
 
+    def set_level_set_field(self, cols, tmat, num_coefs):
+        """Stores the level-set field on the device (fem_gpu_set_level_set_field)."""
+        cols = np.ascontiguousarray(cols, dtype=np.int32)
+        tmat = np.ascontiguousarray(tmat, dtype=np.float64)
+        if cols.shape != tmat.shape or cols.ndim != 2:
+            raise ValueError("cols and tmat: [nodes][width] of one shape")
+        self._check(self.L.fem_gpu_set_level_set_field(self.h, cols.shape[0], cols.shape[1], _np_ptr(cols),
+                                                       _np_ptr(tmat), num_coefs), "set_level_set_field")
+        self._ls_shape = cols.shape
+
     def gen_dqdp(self, G, cols, tmat, num_coefs, dqdp):
+        """dQ/dp through the level-set field; cols = tmat = None uses the field
+        stored by set_level_set_field."""
+        if cols is None and tmat is None:
+            nbn, width = getattr(self, "_ls_shape", (0, 0))
+            if nbn == 0:
+                raise ValueError("no stored level-set field")
+            self._check(self.L.fem_gen_dqdp(self.h, _dev_ptr(G), nbn, width, None, None, num_coefs,
+                                            _dev_ptr(dqdp)), "gen_dqdp")
+            return
         cols = np.ascontiguousarray(cols, dtype=np.int32)
         tmat = np.ascontiguousarray(tmat, dtype=np.float64)
         self._check(self.L.fem_gen_dqdp(self.h, _dev_ptr(G), cols.shape[0], cols.shape[1], _np_ptr(cols),

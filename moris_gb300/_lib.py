@@ -111,6 +111,7 @@ SIGNATURES = {
     "fem_gpu_strain_energy": (I32, [P, P, P, P]),
     "fem_gpu_drdp_adjoint": (I32, [P, P, P, P]),
     "fem_gen_dqdp": (I32, [P, P, I64, I32, P, P, I64, P]),
+    "fem_gpu_set_level_set_field": (I32, [P, I64, I32, P, P, I64]),
     "fem_gen_bspline_tmatrix": (I32, [P, P, I32, I64, P, P, P]),
     "fem_gpu_finalize": (I32, [P]),
     "fem_gpu_finalize_host": (I32, [P]),

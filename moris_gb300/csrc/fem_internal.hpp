@@ -80,6 +80,8 @@ struct SetData {
     DeviceBuf d_sgeo;       // side: per facet and point w*, normal, J^-1; 1/h (built once)
     DeviceBuf d_igoff, d_igx, d_igxi;            // cut clusters: integration cells
     DeviceBuf d_adjul;      // cut clusters: pdof values of u and lambda per cluster, cluster of each cell (sensitivities)
+    DeviceBuf d_items;      // interface clusters: volume items (e * 2 + side, cell) of the sensitivities
+    int64_t nitems = 0;
     DeviceBuf d_fcoff, d_fcx, d_fcxl, d_fcxf;    // double-sided: facets
     DeviceBuf d_EF, d_vol;
     int ngp = 0;            // Gauss points of the set's rule
@@ -131,6 +133,15 @@ struct fem_gpu_ctx {
     std::vector<int32_t> vkind, vpar;  // [nv], [nv][8]
     std::vector<double> vx, vval;      // [nv][3], [nv]
     fem::DeviceBuf d_vkind, d_vpar, d_vx;
+    fem::DeviceBuf d_adjcuts;          // cut-set table of the sensitivity kernels
+    bool adj_topo = false;             // vertex kinds / parents, vertex ids, links and items are on the device
+    bool adj_coords = false;           // vertex coordinates are on the device
+    fem::DeviceBuf d_vval;             // vertex values (phi at background parents)
+    bool ls_phi = false;               // d_vval holds the current table's values
+    fem::DeviceBuf d_lscols, d_lst;    // level-set field: coefficient ids and weights [nodes][width]
+    int64_t ls_nbn = 0, ls_ncoef = 0;  // field sizes (0 nodes: none)
+    int32_t ls_width = 0;
+    int64_t ls_checked_nbn = -1;       // vertex parents checked against this many background nodes
     int64_t launches = 0;
     std::string err;
 };

@@ -554,11 +554,20 @@ void sensitivity_release(fem_gpu_ctx* c) {
     dfree(c->d_vkind);
     dfree(c->d_vpar);
     dfree(c->d_vx);
+    dfree(c->d_adjcuts);
+    dfree(c->d_vval);
+    dfree(c->d_lscols);
+    dfree(c->d_lst);
+    c->ls_nbn = 0;
+    c->ls_phi = false;
     for (auto& s : c->sets) {
         dfree(s.d_vid);
         dfree(s.d_link);
         dfree(s.d_adjul);
+        dfree(s.d_items);
+        s.nitems = 0;
     }
+    c->adj_topo = c->adj_coords = false;
 }
 
 }  // namespace fem
@@ -574,6 +583,8 @@ fem_gpu_status fem_gpu_set_ig_vertices(fem_gpu_ctx* c, int64_t nv, const int32_t
     c->vpar.assign(parents, parents + nv * 8);
     c->vx.assign(coords, coords + nv * 3);
     c->vval.assign(value, value + nv);
+    c->adj_topo = c->adj_coords = c->ls_phi = false;
+    c->ls_checked_nbn = -1;
     for (int64_t v = 0; v < nv; ++v) {
         const int k = c->vkind[v];
         if (k < 0 || k > 3) return fail(c, FEM_GPU_BAD_ARG, "IG vertex kind");
@@ -607,6 +618,7 @@ fem_gpu_status fem_gpu_update_ig_vertices(fem_gpu_ctx* c, const double* t) {
         for (int d = 0; d < 3; ++d) c->vx[v * 3 + d] = c->vx[p0 * 3 + d] + t[v] * (c->vx[p1 * 3 + d] - c->vx[p0 * 3 + d]);
         c->vval[v] = t[v];
     }
+    c->adj_coords = false;
     const int npe = c->npe;
     auto param = [&](int64_t cell, const double* x, double* xi) {
         const double* X0 = &c->coords[(int64_t)c->cells[cell * npe + 0] * 3];
@@ -690,11 +702,20 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         return fail(c, FEM_GPU_UNSUPPORTED, "shape sensitivities need 3D rectangular cells");
     cudaStream_t st = (cudaStream_t)c->stream;
     const int64_t nv = (int64_t)c->vkind.size();
-    cudaError_t e = refresh(c->d_vkind, c->vkind, st);
-    if (e == cudaSuccess) e = refresh(c->d_vpar, c->vpar, st);
-    if (e == cudaSuccess) e = refresh(c->d_vx, c->vx, st);
+    // the vertex table, vertex ids, interface links and volume items depend on
+    // the topology only and go to the device once per vertex table; the
+    // coordinates once per geometry update
+    const bool topo = !c->adj_topo;
+    c->adj_topo = false;
+    cudaError_t e = cudaSuccess;
+    if (topo) {
+        e = refresh(c->d_vkind, c->vkind, st);
+        if (e == cudaSuccess) e = refresh(c->d_vpar, c->vpar, st);
+    }
+    if (e == cudaSuccess && !c->adj_coords) e = refresh(c->d_vx, c->vx, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(G, 0, nv * sizeof(double), st);
     if (e != cudaSuccess) return sfail(c, e, "adjoint vertex table");
+    c->adj_coords = true;
     AdjArgs A{};
     A.vkind = (const int32_t*)c->d_vkind.p;
     A.vpar = (const int32_t*)c->d_vpar.p;
@@ -706,14 +727,14 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
     // cut sets
     std::vector<CutSetDev> cuts;
     std::vector<int> cut_index(c->sets.size(), -1), cut_set;  // set -> cut index, cut index -> set
-    std::vector<std::pair<int32_t, int64_t>> cell_cluster(c->num_cells, {-1, -1});
+    std::vector<std::pair<int32_t, int64_t>> cell_cluster(topo ? c->num_cells : 0, {-1, -1});
     for (size_t k = 0; k < c->sets.size(); ++k) {
         SetData& s = c->sets[k];
         if (!is_cut(s) || s.neq == 0) continue;
         if (s.vid.empty()) return fail(c, FEM_GPU_BAD_ARG, "cut set without IG vertex ids");
         if (s.bulk.integration_rule != FEM_GPU_RULE_TET_4 && s.bulk.integration_rule != FEM_GPU_RULE_TET_11)
             return fail(c, FEM_GPU_UNSUPPORTED, "sensitivities of cut clusters need TET4 cells");
-        if ((e = refresh(s.d_vid, s.vid, st)) != cudaSuccess) return sfail(c, e, "vertex ids");
+        if (topo && (e = refresh(s.d_vid, s.vid, st)) != cudaSuccess) return sfail(c, e, "vertex ids");
         CutSetDev d{};
         d.neq = s.neq;
         d.xe = (const double*)s.d_xe.p;
@@ -731,7 +752,8 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         d.ngp = s.ngp;
         cut_index[k] = (int)cuts.size();
         cut_set.push_back((int)k);
-        for (int64_t i = 0; i < s.neq; ++i) cell_cluster[s.ip_cell[i]] = {(int32_t)cuts.size(), i};
+        if (topo)
+            for (int64_t i = 0; i < s.neq; ++i) cell_cluster[s.ip_cell[i]] = {(int32_t)cuts.size(), i};
         cuts.push_back(d);
     }
     for (size_t k = 0, ci = 0; k < c->sets.size(); ++k) {
@@ -756,8 +778,7 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         c->launches += 2;
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return sfail(c, e, "adjoint tets");
-    DeviceBuf dcuts;
-    if ((e = upload(dcuts, cuts, st)) != cudaSuccess) return sfail(c, e, "cut table");
+    if ((e = refresh(c->d_adjcuts, cuts, st)) != cudaSuccess) return sfail(c, e, "cut table");
     fem_gpu_status r = FEM_GPU_OK;
     for (auto& s : c->sets) {
         if (!is_interface(s) || s.neq == 0) continue;
@@ -765,22 +786,36 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
             r = fail(c, FEM_GPU_UNSUPPORTED, "interface sensitivities need TRI3 facets with vertex ids");
             break;
         }
-        s.link.assign(s.neq * 4, 0);
-        for (int64_t i = 0; i < s.neq; ++i) {
-            const auto L = cell_cluster[s.ip_cell[i]], F = cell_cluster[s.fcell[i]];
-            if (L.first < 0 || F.first < 0) {
-                r = fail(c, FEM_GPU_BAD_ARG, "interface cluster without cut clusters on its cells");
+        if (topo) {
+            s.link.assign(s.neq * 4, 0);
+            for (int64_t i = 0; i < s.neq; ++i) {
+                const auto L = cell_cluster[s.ip_cell[i]], F = cell_cluster[s.fcell[i]];
+                if (L.first < 0 || F.first < 0) {
+                    r = fail(c, FEM_GPU_BAD_ARG, "interface cluster without cut clusters on its cells");
+                    break;
+                }
+                s.link[i * 4 + 0] = L.first;
+                s.link[i * 4 + 1] = (int32_t)L.second;
+                s.link[i * 4 + 2] = F.first;
+                s.link[i * 4 + 3] = (int32_t)F.second;
+            }
+            if (r != FEM_GPU_OK) break;
+            // volume items: (e * 2 + side) in the first half, the integration cell in the second
+            std::vector<int64_t> items;
+            for (int pass = 0; pass < 2; ++pass)
+                for (int64_t i = 0; i < s.neq; ++i)
+                    for (int side = 0; side < 2; ++side) {
+                        const int cs = s.link[i * 4 + side * 2];
+                        const int64_t ce = s.link[i * 4 + side * 2 + 1];
+                        const std::vector<int64_t>& io = c->sets[cut_set[cs]].ig_off;
+                        for (int64_t g = io[ce]; g < io[ce + 1]; ++g) items.push_back(pass == 0 ? i * 2 + side : g);
+                    }
+            s.nitems = (int64_t)items.size() / 2;
+            if ((e = refresh(s.d_link, s.link, st)) != cudaSuccess || (e = refresh(s.d_vid, s.vid, st)) != cudaSuccess ||
+                (e = upload(s.d_items, items, st)) != cudaSuccess) {
+                r = sfail(c, e, "interface links");
                 break;
             }
-            s.link[i * 4 + 0] = L.first;
-            s.link[i * 4 + 1] = (int32_t)L.second;
-            s.link[i * 4 + 2] = F.first;
-            s.link[i * 4 + 3] = (int32_t)F.second;
-        }
-        if (r != FEM_GPU_OK) break;
-        if ((e = refresh(s.d_link, s.link, st)) != cudaSuccess || (e = refresh(s.d_vid, s.vid, st)) != cudaSuccess) {
-            r = sfail(c, e, "interface links");
-            break;
         }
         IfSetDev d{};
         d.neq = s.neq;
@@ -805,18 +840,8 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         // scratch: per cluster U, L (96) and sums (4); per facet the cluster
         // index and the derivative parts; the volume items
         const int64_t nf = s.fc_off.empty() ? 0 : s.fc_off.back();
-        std::vector<int64_t> item_e, item_cell;
-        for (int64_t i = 0; i < s.neq; ++i)
-            for (int side = 0; side < 2; ++side) {
-                const int cs = s.link[i * 4 + side * 2];
-                const int64_t ce = s.link[i * 4 + side * 2 + 1];
-                const std::vector<int64_t>& io = c->sets[cut_set[cs]].ig_off;
-                for (int64_t g = io[ce]; g < io[ce + 1]; ++g) {
-                    item_e.push_back(i * 2 + side);
-                    item_cell.push_back(g);
-                }
-            }
-        const int64_t ni = (int64_t)item_e.size();
+        const int64_t ni = s.nitems;
+        const int64_t* item_e = (const int64_t*)s.d_items.p;
         const size_t need = (size_t)s.neq * 100 * sizeof(double) + (size_t)std::max<int64_t>(nf, 1) * kIfParts * sizeof(double) +
                             (size_t)std::max<int64_t>(nf, 1) * sizeof(int32_t);
         if (!s.d_adjul.p || s.d_adjul.bytes < need) {
@@ -831,13 +856,6 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         double* sums = UL + (size_t)s.neq * 96;
         double* parts = sums + (size_t)s.neq * 4;
         int32_t* fcl = reinterpret_cast<int32_t*>(parts + (size_t)std::max<int64_t>(nf, 1) * kIfParts);
-        DeviceBuf ditem_e, ditem_c;
-        if ((e = upload(ditem_e, item_e, st)) != cudaSuccess || (e = upload(ditem_c, item_cell, st)) != cudaSuccess) {
-            dfree(ditem_e);
-            dfree(ditem_c);
-            r = sfail(c, e, "interface volume items");
-            break;
-        }
         cudaMemsetAsync(sums, 0, (size_t)s.neq * 4 * sizeof(double), st);
         const auto grid_of = [](int64_t n) {
             return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 63) / 64, (int64_t)sm_count() * 16));
@@ -845,57 +863,87 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         iface_cluster_values<<<(unsigned)std::max<int64_t>(s.neq, 1), 64, 0, st>>>(A, d, UL, fcl);
         iface_facets<<<grid_of(nf), 64, 0, st>>>(A, d, UL, fcl, nf, sums, parts);
         iface_apply<<<grid_of(nf), 64, 0, st>>>(A, d, fcl, nf, sums, parts);
-        iface_volumes<<<grid_of(ni), 64, 0, st>>>(A, d, (const CutSetDev*)dcuts.p, ni, (const int64_t*)ditem_e.p,
-                                                  (const int64_t*)ditem_c.p, sums);
+        iface_volumes<<<grid_of(ni), 64, 0, st>>>(A, d, (const CutSetDev*)c->d_adjcuts.p, ni, item_e, item_e + ni,
+                                                  sums);
         c->launches += 4;
-        cudaStreamSynchronize(st);
-        dfree(ditem_e);
-        dfree(ditem_c);
         if ((e = cudaGetLastError()) != cudaSuccess) {
             r = sfail(c, e, "adjoint interface");
             break;
         }
     }
-    cudaStreamSynchronize(st);
-    dfree(dcuts);
-    (void)cut_index;
-    return r;
+    if (r != FEM_GPU_OK) return r;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return sfail(c, e, "adjoint");
+    c->adj_topo = true;
+    return FEM_GPU_OK;
+}
+
+fem_gpu_status fem_gpu_set_level_set_field(fem_gpu_ctx* c, int64_t nbn, int32_t width, const int32_t* cols,
+                                           const double* tmat, int64_t ncoef) {
+    if (!c || !cols || !tmat || width <= 0 || nbn <= 0 || ncoef <= 0) return FEM_GPU_BAD_ARG;
+    const int64_t n = nbn * width;
+    for (int64_t k = 0; k < n; ++k)
+        if (cols[k] < 0 || cols[k] >= ncoef) return fail(c, FEM_GPU_OOB_INDEX, "level-set coefficient id");
+    c->ls_nbn = 0;
+    cudaStream_t st = (cudaStream_t)c->stream;
+    cudaError_t e = cudaSuccess;
+    if (!c->d_lscols.p || c->d_lscols.bytes < (size_t)n * sizeof(int32_t)) {
+        dfree(c->d_lscols);
+        if ((e = cudaMalloc(&c->d_lscols.p, (size_t)n * sizeof(int32_t))) == cudaSuccess)
+            c->d_lscols.bytes = (size_t)n * sizeof(int32_t);
+    }
+    if (e == cudaSuccess && (!c->d_lst.p || c->d_lst.bytes < (size_t)n * sizeof(double))) {
+        dfree(c->d_lst);
+        if ((e = cudaMalloc(&c->d_lst.p, (size_t)n * sizeof(double))) == cudaSuccess)
+            c->d_lst.bytes = (size_t)n * sizeof(double);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_lscols.p, cols, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_lst.p, tmat, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return sfail(c, e, "level-set field");
+    c->ls_nbn = nbn;
+    c->ls_width = width;
+    c->ls_ncoef = ncoef;
+    return FEM_GPU_OK;
 }
 
 fem_gpu_status fem_gen_dqdp(fem_gpu_ctx* c, const double* G, int64_t nbn, int32_t width, const int32_t* cols,
                             const double* tmat, int64_t ncoef, double* dqdp) {
-    if (!c || !G || !cols || !tmat || !dqdp || width <= 0 || nbn <= 0 || ncoef <= 0) return FEM_GPU_BAD_ARG;
+    if (!c || !G || !dqdp || width <= 0 || nbn <= 0 || ncoef <= 0 || (!cols) != (!tmat)) return FEM_GPU_BAD_ARG;
     if (c->vkind.empty()) return fail(c, FEM_GPU_BAD_ARG, "no IG vertex table");
+    if (cols) {
+        const fem_gpu_status r = fem_gpu_set_level_set_field(c, nbn, width, cols, tmat, ncoef);
+        if (r != FEM_GPU_OK) return r;
+    } else if (c->ls_nbn != nbn || c->ls_width != width || c->ls_ncoef != ncoef) {
+        return fail(c, FEM_GPU_BAD_ARG, "no level-set field of these sizes (fem_gpu_set_level_set_field)");
+    }
     const int64_t nv = (int64_t)c->vkind.size();
-    for (int64_t k = 0; k < nbn * width; ++k)
-        if (cols[k] < 0 || cols[k] >= ncoef) return fail(c, FEM_GPU_OOB_INDEX, "level-set coefficient id");
-    for (int64_t v = 0; v < nv; ++v)
-        if (c->vkind[v] != 3)
-            for (int m = 0; m < 8; ++m)
-                if (c->vpar[v * 8 + m] >= nbn) return fail(c, FEM_GPU_OOB_INDEX, "background node of an IG vertex");
+    // background parents of the vertex table against this field (once per table and field size)
+    if (c->ls_checked_nbn != nbn) {
+        for (int64_t v = 0; v < nv; ++v)
+            if (c->vkind[v] != 3)
+                for (int m = 0; m < 8; ++m)
+                    if (c->vpar[v * 8 + m] >= nbn) return fail(c, FEM_GPU_OOB_INDEX, "background node of an IG vertex");
+        c->ls_checked_nbn = nbn;
+    }
     cudaStream_t st = (cudaStream_t)c->stream;
-    // level set at the parents: vval holds phi for kinds 0-2
-    std::vector<int32_t> vc(cols, cols + nbn * width);
-    std::vector<double> vt(tmat, tmat + nbn * width);
-    DeviceBuf dphi, dcols, dt;
-    cudaError_t e = upload(dphi, c->vval, st);
-    if (e == cudaSuccess) e = upload(dcols, vc, st);
-    if (e == cudaSuccess) e = upload(dt, vt, st);
-    if (e == cudaSuccess) e = refresh(c->d_vkind, c->vkind, st);
-    if (e == cudaSuccess) e = refresh(c->d_vpar, c->vpar, st);
+    // level set at the parents: vval holds phi for kinds 0-2 (set with the
+    // vertex table; geometry updates change the kind-3 entries only)
+    cudaError_t e = cudaSuccess;
+    if (!c->ls_phi) e = refresh(c->d_vval, c->vval, st);
+    if (e == cudaSuccess && !c->adj_topo) e = refresh(c->d_vkind, c->vkind, st);
+    if (e == cudaSuccess && !c->adj_topo) e = refresh(c->d_vpar, c->vpar, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(dqdp, 0, ncoef * sizeof(double), st);
     if (e == cudaSuccess) {
+        c->ls_phi = true;
         dqdp_chain<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(nv, (const int32_t*)c->d_vkind.p,
-                                                                 (const int32_t*)c->d_vpar.p, (const double*)dphi.p,
-                                                                 G, width, (const int32_t*)dcols.p,
-                                                                 (const double*)dt.p, dqdp);
+                                                                 (const int32_t*)c->d_vpar.p, (const double*)c->d_vval.p,
+                                                                 G, width, (const int32_t*)c->d_lscols.p,
+                                                                 (const double*)c->d_lst.p, dqdp);
         c->launches++;
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    dfree(dphi);
-    dfree(dcols);
-    dfree(dt);
     if (e != cudaSuccess) return sfail(c, e, "dq/dp chain");
     return FEM_GPU_OK;
 }

@@ -122,6 +122,7 @@ def build(n=64, ncoef=32, order=2, p=None, finalize=True, stream=None):
     m.set_ig_vertices(v["kind"], v["parents"], v["coords"], v["value"])
     if finalize:
         m.finalize()
+        m.set_level_set_field(cols, vals, len(p))
     return dict(model=m, x=x, sets=sets, p=p, cols=cols, vals=vals, phi=phi, n=n, ncoef=ncoef)
 
 
@@ -192,5 +193,5 @@ def sensitivities(c, u, lam):
     G = torch.empty(nv, dtype=torch.float64, device="cuda")
     m.drdp_adjoint(u, lam, G)
     dqdp = torch.empty(len(c["p"]), dtype=torch.float64, device="cuda")
-    m.gen_dqdp(G, c["cols"], c["vals"], len(c["p"]), dqdp)
+    m.gen_dqdp(G, None, None, len(c["p"]), dqdp)
     return G, dqdp

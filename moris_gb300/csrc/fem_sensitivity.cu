@@ -101,30 +101,58 @@ __device__ __forceinline__ void axpy(double s, const Dual<M>& b, Dual<M>& a) {
     for (int i = 0; i < M; ++i) a.d[i] = fma(s, b.d[i], a.d[i]);
 }
 
-// gradients of a field (nodal values f[fld*8 + a]) at an IP point of a rectangular HEX8
-// cell: grad[fld][i] = sum_a f dN_a/dxi_i / jd_i; val[fld] = sum_a f N_a
-template <int M>
-__device__ void hex_field(const Dual<M>* xi, const double* jd, const double* f, Dual<M> val[3], Dual<M> grad[3][3]) {
-    for (int fl = 0; fl < 3; ++fl) {
-        val[fl] = Dual<M>(0.0);
-        for (int i = 0; i < 3; ++i) grad[fl][i] = Dual<M>(0.0);
-    }
+// A trilinear field of a rectangular HEX8 cell (nodal values f_a, shape
+// functions N_a = (1 + s_x xi)(1 + s_y eta)(1 + s_z zeta) / 8) written as a
+// polynomial in the physical offsets (x, y, z) from the cell centre:
+//   f = k0 + k1 x + k2 y + k3 z + k4 xy + k5 yz + k6 xz + k7 xyz,
+// k_m = (1/8) sum_a f_a prod_{d in m} s_d(a) / prod_{d in m} jd_d  (jd the half
+// edge lengths).  Its gradient needs only the pair products:
+//   df/dx = k1 + k4 y + k6 z + k7 yz,  df/dy = k2 + k4 x + k5 z + k7 xz,
+//   df/dz = k3 + k6 x + k5 y + k7 xy.
+// Monomial m -> the set of coordinates it contains (bit d for coordinate d).
+__device__ __forceinline__ int monomial_mask(int m) {
+    return m < 4 ? (m == 0 ? 0 : 1 << (m - 1)) : (m == 4 ? 3 : m == 5 ? 6 : m == 6 ? 5 : 7);
+}
+// coefficient r = comp * 8 + m of the field with nodal values f[comp * 8 + a]
+// on the cell X[8][3] (node 0 and node 6 opposite corners)
+__device__ double monomial_coefficient(const double* f, const double* X, int r) {
+    const int fl = r >> 3, mask = monomial_mask(r & 7);
+    double c = 0.0;
     for (int a = 0; a < 8; ++a) {
-        const double sx = ((a & 3) == 1 || (a & 3) == 2) ? 1.0 : -1.0;
-        const double sy = ((a & 3) >= 2) ? 1.0 : -1.0;
-        const double sz = a >= 4 ? 1.0 : -1.0;
-        const Dual<M> fx = 1.0 + sx * xi[0], fy = 1.0 + sy * xi[1], fz = 1.0 + sz * xi[2];
-        const Dual<M> fyz = fy * fz, fxz = fx * fz, fxy = fx * fy;
-        const Dual<M> N = 0.125 * (fx * fyz);
-        const double c0 = 0.125 * sx / jd[0], c1 = 0.125 * sy / jd[1], c2 = 0.125 * sz / jd[2];
-        for (int fl = 0; fl < 3; ++fl) {
-            const double fv = f[fl * 8 + a];
-            if (fv == 0.0) continue;
-            axpy(fv, N, val[fl]);
-            axpy(fv * c0, fyz, grad[fl][0]);
-            axpy(fv * c1, fxz, grad[fl][1]);
-            axpy(fv * c2, fxy, grad[fl][2]);
-        }
+        const int sx = ((a & 3) == 1 || (a & 3) == 2) ? 1 : -1;
+        const int sy = ((a & 3) >= 2) ? 1 : -1;
+        const int sz = a >= 4 ? 1 : -1;
+        const int sg = ((mask & 1) ? sx : 1) * ((mask & 2) ? sy : 1) * ((mask & 4) ? sz : 1);
+        c += sg > 0 ? f[fl * 8 + a] : -f[fl * 8 + a];
+    }
+    double den = 8.0;
+    for (int d = 0; d < 3; ++d)
+        if (mask & (1 << d)) den *= 0.5 * (X[18 + d] - X[d]);
+    return c / den;
+}
+
+// a0 + a1 p + a2 q + a3 r (constant coefficients)
+template <int M>
+__device__ __forceinline__ Dual<M> lin3(double a0, double a1, const Dual<M>& p, double a2, const Dual<M>& q, double a3,
+                                        const Dual<M>& r) {
+    Dual<M> o;
+    o.v = fma(a3, r.v, fma(a2, q.v, fma(a1, p.v, a0)));
+    for (int i = 0; i < M; ++i) o.d[i] = fma(a3, r.d[i], fma(a2, q.d[i], a1 * p.d[i]));
+    return o;
+}
+
+// gradient grad[comp][d] (and with VAL the value) of a field in monomial form
+// k[comp * 8 + m] at the offsets x[3]; pr = {xy, yz, xz}
+template <int M, bool VAL>
+__device__ __forceinline__ void mono_field(const double* __restrict__ k, const Dual<M> x[3], const Dual<M> pr[3],
+                                           Dual<M> val[3], Dual<M> grad[3][3]) {
+    for (int fl = 0; fl < 3; ++fl) {
+        const double* c = k + fl * 8;
+        grad[fl][0] = lin3(c[1], c[4], x[1], c[6], x[2], c[7], pr[1]);
+        grad[fl][1] = lin3(c[2], c[4], x[0], c[5], x[2], c[7], pr[2]);
+        grad[fl][2] = lin3(c[3], c[6], x[0], c[5], x[1], c[7], pr[0]);
+        // k0 + k2 y + k3 z + k5 yz + x df/dx
+        if (VAL) val[fl] = lin3(c[0], c[2], x[1], c[3], x[2], c[5], pr[1]) + x[0] * grad[fl][0];
     }
 }
 
@@ -219,11 +247,14 @@ __device__ Dual<M> tet_volume(const Dual<M> X[4][3]) {
 __global__ void adjoint_cluster_values(AdjArgs A, CutSetDev S, double* UL /*[neq][48]*/, int32_t* cell_cluster) {
     const int64_t e = blockIdx.x;
     if (e >= S.neq) return;
+    __shared__ double nod[48];
     for (int64_t g = S.ig_off[e] + threadIdx.x; g < S.ig_off[e + 1]; g += blockDim.x) cell_cluster[g] = (int32_t)e;
     const int nb = S.nb[e];
-    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.u, A.nu, UL + e * 48, threadIdx.x, blockDim.x);
-    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.lam, A.nu, UL + e * 48 + 24, threadIdx.x,
-                blockDim.x);
+    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.u, A.nu, nod, threadIdx.x, blockDim.x);
+    pdof_values(S.T + e * 8 * S.W, S.bases + e * S.W, nb, S.W, A.lam, A.nu, nod + 24, threadIdx.x, blockDim.x);
+    __syncthreads();
+    for (int r = threadIdx.x; r < 48; r += blockDim.x)
+        UL[e * 48 + r] = monomial_coefficient(nod + (r / 24) * 24, S.xe + e * 24, r % 24);
 }
 
 __global__ void adjoint_tets_flat(AdjArgs A, CutSetDev S, const double* __restrict__ UL,
@@ -234,15 +265,15 @@ __global__ void adjoint_tets_flat(AdjArgs A, CutSetDev S, const double* __restri
         const double* X = S.xe + e * 24;
         const double* U = UL + e * 48;
         const double* L = U + 24;
-        const double jd[3] = {0.5 * (X[18] - X[0]), 0.5 * (X[19] - X[1]), 0.5 * (X[20] - X[2])};
+        const double xc[3] = {0.5 * (X[18] + X[0]), 0.5 * (X[19] + X[1]), 0.5 * (X[20] + X[2])};
         const double lam = S.E[e] * S.lam_c, mu = S.E[e] * S.mu_c;
-        Dual<4> Xv[4][3], xi[4][3];
+        Dual<4> Xv[4][3], xo[4][3];  // vertices, their offsets from the cell centre
         bool mv[4];
         int32_t vids[4];
         for (int k = 0; k < 4; ++k) {
             vids[k] = S.vid[g * 4 + k];
             vertex_dual<4>(A, vids[k], k, Xv[k], mv[k]);
-            for (int d = 0; d < 3; ++d) xi[k][d] = (-1.0 - X[d] / jd[d]) + (1.0 / jd[d]) * Xv[k][d];
+            for (int d = 0; d < 3; ++d) xo[k][d] = (-xc[d]) + Xv[k][d];
         }
         if (!(mv[0] || mv[1] || mv[2] || mv[3])) continue;
         const Dual<4> detJ = tet_volume<4>(Xv);
@@ -253,11 +284,12 @@ __global__ void adjoint_tets_flat(AdjArgs A, CutSetDev S, const double* __restri
             Dual<4> xq[3];
             for (int d = 0; d < 3; ++d) {
                 xq[d] = Dual<4>(0.0);
-                for (int k = 0; k < 4; ++k) axpy(Nt[k], xi[k][d], xq[d]);
+                for (int k = 0; k < 4; ++k) axpy(Nt[k], xo[k][d], xq[d]);
             }
-            Dual<4> uv[3], Gu[3][3], lv[3], Gl[3][3], Su[3][3];
-            hex_field<4>(xq, jd, U, uv, Gu);
-            hex_field<4>(xq, jd, L, lv, Gl);
+            const Dual<4> pr[3] = {xq[0] * xq[1], xq[1] * xq[2], xq[0] * xq[2]};
+            Dual<4> Gu[3][3], Gl[3][3], Su[3][3];
+            mono_field<4, false>(U, xq, pr, nullptr, Gu);
+            mono_field<4, false>(L, xq, pr, nullptr, Gl);
             stress<4>(Gu, lam, mu, Su);
             Dual<4> phi(0.0);
             for (int i = 0; i < 3; ++i)
@@ -306,14 +338,19 @@ constexpr int kIfParts = 12;  // dA, dB, dC, d|G| for the three vertices
 __global__ void iface_cluster_values(AdjArgs A, IfSetDev S, double* UL /*[neq][96]*/, int32_t* facet_cluster) {
     const int64_t e = blockIdx.x;
     if (e >= S.neq) return;
+    __shared__ double nod[96];
     for (int64_t f = S.fc_off[e] + threadIdx.x; f < S.fc_off[e + 1]; f += blockDim.x) facet_cluster[f] = (int32_t)e;
     for (int s = 0; s < 2; ++s) {
         const int nb = S.nb[2 * e + s];
-        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.u, A.nu,
-                    UL + e * 96 + 24 * s, threadIdx.x, blockDim.x);
+        pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.u, A.nu, nod + 24 * s,
+                    threadIdx.x, blockDim.x);
         pdof_values(S.T + (e * 2 + s) * 8 * S.W, S.bases + (e * 2 + s) * S.W, nb, S.W, A.lam, A.nu,
-                    UL + e * 96 + 48 + 24 * s, threadIdx.x, blockDim.x);
+                    nod + 48 + 24 * s, threadIdx.x, blockDim.x);
     }
+    __syncthreads();
+    // [u side 0, u side 1, lambda side 0, lambda side 1], each on its side's cell
+    for (int r = threadIdx.x; r < 96; r += blockDim.x)
+        UL[e * 96 + r] = monomial_coefficient(nod + (r / 24) * 24, S.xe + e * 48 + 24 * ((r / 24) & 1), r % 24);
 }
 
 __global__ void iface_facets(AdjArgs A, IfSetDev S, const double* __restrict__ UL,
@@ -348,40 +385,30 @@ __global__ void iface_facets(AdjArgs A, IfSetDev S, const double* __restrict__ U
         const Dual<3> inv = dinv(nn);
         const Dual<3> n[3] = {cr[0] * inv, cr[1] * inv, cr[2] * inv};
         const Dual<3> detJ = 0.5 * nn;
-        Dual<3> xi[2][3][3];  // [side][vertex][d]
-        for (int s = 0; s < 2; ++s) {
-            const double* Xs = X + 24 * s;
-            for (int k = 0; k < 3; ++k)
-                for (int d = 0; d < 3; ++d) {
-                    const double jd = 0.5 * (Xs[18 + d] - Xs[d]);
-                    xi[s][k][d] = (-1.0 - Xs[d] / jd) + (1.0 / jd) * Xv[k][d];
-                }
-        }
+        double xc[2][3];  // the sides' cell centres
+        for (int s = 0; s < 2; ++s)
+            for (int d = 0; d < 3; ++d) xc[s][d] = 0.5 * (X[24 * s + 18 + d] + X[24 * s + d]);
         Dual<3> fa(0.0), fb(0.0), fc(0.0), fr(0.0);
         for (int q = 0; q < S.ngp; ++q) {
             const double z0 = S.gp[q * 2], z1 = S.gp[q * 2 + 1];
             const double Nf[3] = {z0, z1, 1.0 - z0 - z1};
-            Dual<3> uv[2][3], Gu[2][3][3], lv[2][3], Gl[2][3][3];
-            for (int s = 0; s < 2; ++s) {
-                const double* Xs = X + 24 * s;
-                const double jd[3] = {0.5 * (Xs[18] - Xs[0]), 0.5 * (Xs[19] - Xs[1]), 0.5 * (Xs[20] - Xs[2])};
-                Dual<3> xq[3];
-                for (int d = 0; d < 3; ++d) {
-                    xq[d] = Dual<3>(0.0);
-                    for (int k = 0; k < 3; ++k) axpy(Nf[k], xi[s][k][d], xq[d]);
-                }
-                hex_field<3>(xq, jd, U + 24 * s, uv[s], Gu[s]);
-                hex_field<3>(xq, jd, L + 24 * s, lv[s], Gl[s]);
+            // per side: values and tractions t_s(.) = sigma_s(.) n, each
+            // gradient turned into its traction at once
+            Dual<3> uv[2][3], lv[2][3], tu[2][3], tl[2][3], xp[3];
+            for (int d = 0; d < 3; ++d) {
+                xp[d] = Dual<3>(0.0);
+                for (int k = 0; k < 3; ++k) axpy(Nf[k], Xv[k][d], xp[d]);
             }
-            // tractions t_s(.) = sigma_s(.) n
-            Dual<3> tu[2][3], tl[2][3];
             for (int s = 0; s < 2; ++s) {
-                Dual<3> Su[3][3], Sl[3][3];
-                stress<3>(Gu[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Su);
-                stress<3>(Gl[s], Es[s] * S.lam_c, Es[s] * S.mu_c, Sl);
-                for (int i = 0; i < 3; ++i) {
-                    tu[s][i] = Su[i][0] * n[0] + Su[i][1] * n[1] + Su[i][2] * n[2];
-                    tl[s][i] = Sl[i][0] * n[0] + Sl[i][1] * n[1] + Sl[i][2] * n[2];
+                Dual<3> xq[3];
+                for (int d = 0; d < 3; ++d) xq[d] = (-xc[s][d]) + xp[d];
+                const Dual<3> pr[3] = {xq[0] * xq[1], xq[1] * xq[2], xq[0] * xq[2]};
+                for (int fld = 0; fld < 2; ++fld) {
+                    Dual<3> Gf[3][3], Sf[3][3];
+                    mono_field<3, true>((fld ? L : U) + 24 * s, xq, pr, fld ? lv[s] : uv[s], Gf);
+                    stress<3>(Gf, Es[s] * S.lam_c, Es[s] * S.mu_c, Sf);
+                    Dual<3>* t = fld ? tl[s] : tu[s];
+                    for (int i2 = 0; i2 < 3; ++i2) t[i2] = Sf[i2][0] * n[0] + Sf[i2][1] * n[1] + Sf[i2][2] * n[2];
                 }
             }
             Dual<3> qa(0.0), qb(0.0), qc(0.0);

@@ -74,9 +74,10 @@ __device__ void mg_block_sum_add(double v, double* out) {
 // err |= 1 for a column outside the 27-node neighbourhood
 // One CTA per block of kCsRows consecutive rows: their nonzeros are one contiguous
 // range of the CSR, loaded coalesced into shared memory; then kCsPart threads
-// per row take its entries with stride kCsPart.  Consecutive rows are
-// consecutive nodes, so the lanes of a warp that hold the same entry index of
-// neighbouring rows write consecutive words.  A block whose range exceeds the
+// per row take its entries with stride kCsPart, the lanes of a warp on 32
+// consecutive rows with the same part.  Consecutive rows are consecutive
+// nodes, and interior rows have the same column pattern, so a warp's lanes
+// write entry p of 32 neighbouring nodes: consecutive words of one tap.  A block whose range exceeds the
 // staging space (rows longer than 27 x 3 entries, which are an error anyway)
 // reads from global memory.
 constexpr int kCsRows = 64, kCsPart = 8, kCsCap = kCsRows * 81;
@@ -99,18 +100,28 @@ __global__ void __launch_bounds__(kCsPart * kCsRows) mg_csr_to_stencil(int n, co
                 sc[e - e0] = ci[e];
             }
         __syncthreads();
-        const int64_t row = r0 + threadIdx.x / kCsPart;
+        const int64_t row = r0 + threadIdx.x % kCsRows;
         if (row < r1) {
             const int f = (int)(row / N);
             const int64_t i = row - f * N;
             const int ix = (int)(i % n), iy = (int)((i / n) % n), iz = (int)(i / ((int64_t)n * n));
             const int64_t b = rp[row + 1];
-            for (int64_t e = rp[row] + threadIdx.x % kCsPart; e < b; e += kCsPart) {
+            const int64_t n2 = (int64_t)n * n;
+            for (int64_t e = rp[row] + threadIdx.x / kCsRows; e < b; e += kCsPart) {
                 const int64_t col = staged ? sc[e - e0] : ci[e];
-                const int g = (int)(col / N);
-                const int64_t j = col - g * N;
-                const int dx = (int)(j % n) - ix, dy = (int)((j / n) % n) - iy, dz = (int)(j / ((int64_t)n * n)) - iz;
-                if (g < 0 || g > 2 || dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) {
+                // component and node offset d = j - i without divisions: d =
+                // dx + n dy + n^2 dz with |dx|, |dy|, |dz| <= 1 is split by
+                // sign tests (n >= 3); any other column leaves |dx| > 1 or a
+                // neighbour outside the grid and is flagged
+                const int g = (int)(col >= N) + (int)(col >= 2 * N);
+                int64_t d = col - g * N - i;
+                const int dz = (int)(d > n2 / 2) - (int)(d < -(n2 / 2));
+                d -= dz * n2;
+                const int dy = (int)(d > n / 2) - (int)(d < -(n / 2));
+                d -= (int64_t)dy * n;
+                const int dx = (int)(d < -2 ? -2 : d > 2 ? 2 : d);
+                if (col < 0 || col >= 3 * N || dx < -1 || dx > 1 || ix + dx < 0 || ix + dx >= n || iy + dy < 0 ||
+                    iy + dy >= n || iz + dz < 0 || iz + dz >= n) {
                     atomicOr(err, 1);
                     continue;
                 }

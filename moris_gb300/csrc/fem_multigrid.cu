@@ -380,32 +380,47 @@ __device__ __forceinline__ int target(int s, int t) { return (s & 1) ? ((s - 1) 
 __global__ void mg_check_symmetric(int n, const double* __restrict__ S, int* err) {
     // one thread per node I: every tap k <= 13 and component pair (f, g) of row
     // I against the mirrored entry (26 - k, g, f) of the neighbour J; threads of
-    // a warp are consecutive nodes, so both operands load coalesced
+    // a warp are consecutive nodes, so both operands load coalesced.  An
+    // element adds the same value to both entries in one scatter, so they are
+    // usually equal to the bit: an integer comparison (finite values only)
+    // settles a pair, and the tolerance test on the FP64 pipe runs only when a
+    // lane of the warp needs it.  The loop bound is uniform per warp, so every
+    // vote sees all 32 lanes (blockDim a multiple of 32).
     const int64_t N = (int64_t)n * n * n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     bool bad = false;
-    for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < N; I += (int64_t)gridDim.x * blockDim.x) {
-        const int X = (int)(I % n), Y = (int)((I / n) % n), Z = (int)(I / ((int64_t)n * n));
-        float di[3];
-#pragma unroll
-        for (int f = 0; f < 3; ++f) di[f] = fabsf((float)S[sidx(13, f, f, N, I)]);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < N; base += stride) {
+        const int64_t I = base + (threadIdx.x & 31);
+        const bool live = I < N;
+        const int X = live ? (int)(I % n) : 0, Y = live ? (int)((I / n) % n) : 0,
+                  Z = live ? (int)(I / ((int64_t)n * n)) : 0;
         for (int k = 0; k <= 13; ++k) {
             const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-            if (X + dx < 0 || X + dx >= n || Y + dy < 0 || Y + dy >= n || Z + dz < 0 || Z + dz >= n) continue;
+            const bool inside = live && X + dx >= 0 && X + dx < n && Y + dy >= 0 && Y + dy < n && Z + dz >= 0 &&
+                                Z + dz < n;
             const int64_t J = I + dx + (int64_t)n * (dy + (int64_t)n * dz);
-            float dj[3];
-#pragma unroll
-            for (int g = 0; g < 3; ++g) dj[g] = fabsf((float)S[sidx(13, g, g, N, J)]);
 #pragma unroll
             for (int f = 0; f < 3; ++f)
 #pragma unroll
                 for (int g = 0; g < 3; ++g) {
-                    const double a = S[sidx(k, f, g, N, I)], b = S[sidx(26 - k, g, f, N, J)];
-                    // entries that cancel to near zero carry the rounding of their
-                    // terms, which scales with the diagonals: measure the asymmetry
-                    // against them too (in FP32: a square root on the FP64 pipe
-                    // costs far more)
-                    const float tol = 1e-10f * (float)(fabs(a) + fabs(b)) + 1e-12f * sqrtf(di[f] * dj[g]);
-                    bad |= !((float)fabs(a - b) <= tol);
+                    double a = 0.0, b = 0.0;
+                    if (inside) {
+                        a = S[sidx(k, f, g, N, I)];
+                        b = S[sidx(26 - k, g, f, N, J)];
+                    }
+                    const long long ab = __double_as_longlong(a);
+                    const bool same = ab == __double_as_longlong(b) && ((ab >> 52) & 0x7ff) != 0x7ff;
+                    if (__all_sync(0xffffffffu, same)) continue;
+                    if (!same) {
+                        // entries that cancel to near zero carry the rounding of
+                        // their terms, which scales with the diagonals: measure the
+                        // asymmetry against them too (in FP32: a square root on the
+                        // FP64 pipe costs far more)
+                        const float di = fabsf((float)S[sidx(13, f, f, N, I)]);
+                        const float dj = fabsf((float)S[sidx(13, g, g, N, J)]);
+                        const float tol = 1e-10f * (float)(fabs(a) + fabs(b)) + 1e-12f * sqrtf(di * dj);
+                        bad |= !((float)fabs(a - b) <= tol);
+                    }
                 }
         }
     }

@@ -275,14 +275,15 @@ def c3_flops(st):
     """FP64 operations of the cluster kernel's formulation per step (counted
     from the kernel code, FMA = 2):
       uncut cell      5,050 (Gram from the rule table, isotropic K, R = K u, K T, T^T K T)
-      cut point         800 (IG->IP map, detJ, J^-1 dN: 200; 300 Gram FMAs)
-      cut cluster     4,750 (epilogue as for an uncut cell)
+      cut point         120 (IG->IP map, detJ, w*, monomials, 28 moment FMAs)
+      cut cluster    16,750 (Gram from the moments: 300 entries x 20 FMAs; epilogue
+                             as for an uncut cell)
       interface facet 22,100 (7 points x 460 geometry, facet moments P and Q,
                               normal-weighted cluster moments A1)
       interface clus. 47,000 (K from A1 and Q, R = K u, K T, T^T K T on 48 x 48)
       ghost cluster   86,000 (4 points geometry, n.D.B operators, 4 x 3 rank-1
                               updates of the 48 x 48 block, epilogue)"""
-    return (5050 * st["uncut_cells"] + 800 * st["cut_points"] + 4750 * st["cut_clusters"] +
+    return (5050 * st["uncut_cells"] + 120 * st["cut_points"] + 16750 * st["cut_clusters"] +
             22100 * st["interface_facets"] + 47000 * st["interface_clusters"] + 86000 * st["ghost_faces"])
 
 

@@ -169,41 +169,71 @@ __device__ __forceinline__ void ip_gradients(const double* X, const double* xi, 
         }
 }
 
+// one integration point of a cut cluster: its IP-parametric position xi and
+// w* = w detJ_IG (0 for points the reference skips)
+__device__ void cut_point(const SetDev& S, int64_t e, int q, double* xi, double& ws) {
+    const int k = q / S.ngp, qq = q - k * S.ngp;
+    const int64_t gi = S.ig_off[e] + k;
+    const double* xh = S.ig_xi + gi * 12;
+    const double* xx = S.ig_x + gi * 12;
+    double Nt[4], dNt[12];
+    Shape<3>::eval(S.gp + qq * 3, Nt, dNt);
+    for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+        for (int a = 0; a < 4; ++a) s = fma(Nt[a], xh[a * 3 + d], s);
+        xi[d] = s;
+    }
+    // TET4 Jacobian rows x0-x2, x1-x2, x3-x2; detJ / 6
+    double a0[3], a1[3], a3[3];
+    for (int d = 0; d < 3; ++d) {
+        a0[d] = xx[0 * 3 + d] - xx[2 * 3 + d];
+        a1[d] = xx[1 * 3 + d] - xx[2 * 3 + d];
+        a3[d] = xx[3 * 3 + d] - xx[2 * 3 + d];
+    }
+    const double detJ = (a0[0] * (a1[1] * a3[2] - a3[1] * a1[2]) - a0[1] * (a1[0] * a3[2] - a1[2] * a3[0]) +
+                         a0[2] * (a1[0] * a3[1] - a1[1] * a3[0])) /
+                        6.0;
+    // points with detJ below -1e-6 are skipped (cl_FEM_Element_Bulk.cpp:164)
+    ws = detJ < -1.0e-6 ? 0.0 : S.gw[qq] * detJ;
+}
+
 // one bulk integration point: gradients and w* (0 for points the reference skips)
 __device__ void bulk_point(const SetDev& S, int64_t e, int q, const double* X, double* g, double& ws) {
-    double xi[3], w, detJ, N[8];
+    double xi[3], N[8], dj;
     if (!S.cut) {
         for (int d = 0; d < 3; ++d) xi[d] = S.gp[q * 3 + d];
-        w = S.gw[q];
+        double detJ;
         ip_gradients(X, xi, S.rect, N, g, detJ);
-    } else {
-        const int k = q / S.ngp, qq = q - k * S.ngp;
-        const int64_t gi = S.ig_off[e] + k;
-        const double* xh = S.ig_xi + gi * 12;
-        const double* xx = S.ig_x + gi * 12;
-        double Nt[4], dNt[12];
-        Shape<3>::eval(S.gp + qq * 3, Nt, dNt);
-        for (int d = 0; d < 3; ++d) {
-            double s = 0.0;
-            for (int a = 0; a < 4; ++a) s = fma(Nt[a], xh[a * 3 + d], s);
-            xi[d] = s;
-        }
-        // TET4 Jacobian rows x0-x2, x1-x2, x3-x2; detJ / 6
-        double a0[3], a1[3], a3[3];
-        for (int d = 0; d < 3; ++d) {
-            a0[d] = xx[0 * 3 + d] - xx[2 * 3 + d];
-            a1[d] = xx[1 * 3 + d] - xx[2 * 3 + d];
-            a3[d] = xx[3 * 3 + d] - xx[2 * 3 + d];
-        }
-        detJ = (a0[0] * (a1[1] * a3[2] - a3[1] * a1[2]) - a0[1] * (a1[0] * a3[2] - a1[2] * a3[0]) +
-                a0[2] * (a1[0] * a3[1] - a1[1] * a3[0])) /
-               6.0;
-        w = S.gw[qq];
-        double dj;
-        ip_gradients(X, xi, S.rect, N, g, dj);
+        ws = detJ < -1.0e-6 ? 0.0 : S.gw[q] * detJ;
+        return;
     }
-    // points with detJ below -1e-6 are skipped (cl_FEM_Element_Bulk.cpp:164)
-    ws = detJ < -1.0e-6 ? 0.0 : w * detJ;
+    cut_point(S, e, q, xi, ws);
+    ip_gradients(X, xi, S.rect, N, g, dj);
+}
+
+// Gram matrix of a rectangular IP cell from the moments of its points.  On a
+// brick dN_a/dx_i = (1 / jd_i) dN_a/dxi_i, and dN_a/dxi_i is a combination of
+// four of the seven monomials m = (1, xi, eta, zeta, xi eta, eta zeta, xi zeta):
+//   dN_a/dxi   = s_x / 8 (1 + s_y eta + s_z zeta + s_y s_z eta zeta)
+//   dN_a/deta  = s_y / 8 (1 + s_x xi  + s_z zeta + s_x s_z xi zeta)
+//   dN_a/dzeta = s_z / 8 (1 + s_x xi  + s_y eta  + s_x s_y xi eta)
+// so A[(i,a),(j,b)] = sum_q w*_q g_ia g_jb is a signed sum of 16 entries of the
+// moment matrix M = sum_q w*_q m m^T, formed at 28 products per point instead
+// of 300.
+__device__ __forceinline__ void grad_monomials(int i, int a, int mono[4], double sgn[4]) {
+    const double s[3] = {((a & 3) == 1 || (a & 3) == 2) ? 1.0 : -1.0, ((a & 3) >= 2) ? 1.0 : -1.0,
+                         a >= 4 ? 1.0 : -1.0};
+    // the two other coordinates of direction i and their product monomial
+    const int o1 = i == 0 ? 1 : 0, o2 = i == 2 ? 1 : 2;
+    const int prod = i == 0 ? 5 : i == 1 ? 6 : 4;
+    mono[0] = 0;
+    mono[1] = 1 + o1;
+    mono[2] = 1 + o2;
+    mono[3] = prod;
+    sgn[0] = s[i];
+    sgn[1] = s[i] * s[o1];
+    sgn[2] = s[i] * s[o2];
+    sgn[3] = s[i] * s[o1] * s[o2];
 }
 
 template <int NB, int W>
@@ -299,6 +329,71 @@ __device__ void bulk_item(const ClusterArgs& p, const SetDev& S, const Item& it,
             const double cj = i1 == i2 ? cd[i1] : jd[3 - i1 - i2];
             acc[j] = skip ? 0.0 : cj * S.g0[pr[j] * 24 + pc[j]];
         }
+    } else if (S.cut && S.rect) {
+        // moments M = sum_q w* m m^T of the item's points (28 entries, lane l
+        // < 28 of every warp owns entry l over the warp's share of the points)
+        double* MM = G;   // [kChunk][8] monomials of the chunk's points
+        double* WM = WG;  // [kChunk][8] w* times them
+        const int lane = tid & 31, warp = tid >> 5;
+        int ma = 0, mb = 0;
+        {
+            int rem = lane < 28 ? lane : 0;
+            while (rem >= 7 - ma) {
+                rem -= 7 - ma;
+                ++ma;
+            }
+            mb = ma + rem;
+        }
+        double macc = 0.0;
+        for (int q0 = it.q0; q0 < it.q1; q0 += kChunk) {
+            const int nq = min(kChunk, it.q1 - q0);
+            if (tid < kChunk) {
+                double xi[3] = {0.0, 0.0, 0.0}, ws = 0.0;
+                if (tid < nq) cut_point(S, e, q0 + tid, xi, ws);
+                const double m[7] = {1.0, xi[0], xi[1], xi[2], xi[0] * xi[1], xi[1] * xi[2], xi[0] * xi[2]};
+                for (int k = 0; k < 7; ++k) {
+                    MM[tid * 8 + k] = m[k];
+                    WM[tid * 8 + k] = ws * m[k];
+                }
+            }
+            __syncthreads();
+            if (lane < 28)
+                for (int t = warp; t < nq; t += W) macc = fma(WM[t * 8 + ma], MM[t * 8 + mb], macc);
+            __syncthreads();
+        }
+        // warp partial sums, then M (7 x 7) in the KT region (free until K T)
+        double* part = KT + 64;
+        if (lane < 28) part[warp * 28 + lane] = macc;
+        __syncthreads();
+        double* Mm = KT;
+        if (tid < 28) {
+            double v = 0.0;
+            for (int w2 = 0; w2 < W; ++w2) v += part[w2 * 28 + tid];
+            Mm[ma * 7 + mb] = v;
+            Mm[mb * 7 + ma] = v;
+        }
+        __syncthreads();
+        const double ij[3] = {1.0 / (0.5 * (X[6 * 3 + 0] - X[0])), 1.0 / (0.5 * (X[6 * 3 + 1] - X[1])),
+                              1.0 / (0.5 * (X[6 * 3 + 2] - X[2]))};
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            if (tid + j * TH >= kNSYM) continue;
+            const int i1 = pr[j] / 8, a = pr[j] - i1 * 8, i2 = pc[j] / 8, b = pc[j] - i2 * 8;
+            int mu[4], mv[4];
+            double su[4], sv[4];
+            grad_monomials(i1, a, mu, su);
+            grad_monomials(i2, b, mv, sv);
+            double v = 0.0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                double t = 0.0;
+#pragma unroll
+                for (int w2 = 0; w2 < 4; ++w2) t = fma(sv[w2], Mm[mu[u] * 7 + mv[w2]], t);
+                v = fma(su[u], t, v);
+            }
+            acc[j] = v * (ij[i1] * ij[i2] * (1.0 / 64.0));
+        }
+        __syncthreads();
     } else
     for (int q0 = it.q0; q0 < it.q1; q0 += kChunk) {
         const int nq = min(kChunk, it.q1 - q0);

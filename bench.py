@@ -97,7 +97,10 @@ def flops_per_element(order=2, ngp=27, rect=True, density=False):
     rect=True is the constant-Jacobian (brick) path: the Gram matrix is a
     scaled per-rule table; rect=False the per-Gauss-point path.  density=True
     is the SIMP path: E(x_q) = E0 rho(x_q)^beta per Gauss point, so the Gram
-    matrix is summed per element over the points with those weights."""
+    matrix is summed per element over the points with those weights.
+    Quadratic extraction is the tensor product of (1/2, 1/2, 0) / (0, 1/2, 1/2):
+    K T is formed as (K/8) P summed axis by axis, 19 additions per row of K and
+    column field (8 node values -> 27 bases)."""
     tc1, nzrow = {1: ([1, 1], 1), 2: ([1, 2, 1], 8)}[order]
     tc = [a * b * c for c in tc1 for b in tc1 for a in tc1]
     NGP, NPD, NB, D = ngp, 24, len(tc), 3
@@ -112,7 +115,10 @@ def flops_per_element(order=2, ngp=27, rect=True, density=False):
         kiso = nsym * 3 + 3 * 36 * 4
     upd = NPD * nzrow * 2                                     # u_pdof = T u_adof
     resid = NPD * NPD * 2 + D * sum(tc) * 2                   # R_p = K u, R_a = T^T R_p
-    kt = (D * (D + 1) // 2) * 8 * sum(tc) * 2                 # K T on the field blocks g >= f
+    if order == 2:
+        kt = NPD * D * 19                                     # K T summed axis by axis (y, x, z stages)
+    else:
+        kt = (D * (D + 1) // 2) * 8 * sum(tc) * 2             # K T over the T column nonzeros
     ka = 0                                                    # upper triangle of T^T (K T)
     nad = D * NB
     for r in range(nad):

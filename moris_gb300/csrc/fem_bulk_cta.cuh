@@ -22,6 +22,16 @@
 //
 // MODE_APPLY (matrix-free Jacobian-vector product) forms the pdof K the same
 // way and scatters T^T (K T x) without the K T / T^T K T stages.
+//
+// Uniform quadratic B-splines (3D HEX8, 27 bases): at the cell corners every
+// basis is the tensor product of the 1D values (1/2, 1/2, 0) / (0, 1/2, 1/2),
+// so T = 1/8 P with P the 0/1 pattern of nodes (x left/right) x (y) x (z).
+// When an element's T is exactly that (checked per element: every nonzero
+// 1/8, each column a tensor-product node set, all 27 present), K is formed
+// as K/8 (exact: a power of two) and K T = (K/8) P is summed axis by axis:
+// 8 node values -> 27 bases in three 2 -> 3 stages of additions (about 6 per
+// output group instead of the column-count FMAs); other elements take the
+// general path.
 #pragma once
 
 // E0-relative SIMP factor rho(x_q)^beta with rho interpolated from the nodal
@@ -96,7 +106,10 @@ struct CtaLayout {
     // [slot][slot] (u16)
     static constexpr int bTN = 0, bTC = bTN + NB * NPE, bTCP = bTC + NB, bCP = bTCP + NB, bCPI = bCP + NB;
     static constexpr int bS = ((bCPI + NB + 1) / 2) * 2;
-    static constexpr int NBYTE = bS + 2 * NB * NB;
+    static constexpr int bNJ = bS + 2 * NB * NB;  // tensor-product elements: slot of natural basis code
+    static constexpr int NBYTE = bNJ + NB;
+    // uniform quadratic B-spline elements (sum-factorised K T)
+    static constexpr bool kTQ2 = D == 3 && NPE == 8 && NB == 27;
     static constexpr size_t kBytes = ((size_t)ND * 8 + (size_t)NI * 4 + (size_t)NBYTE + 15) / 16 * 16;
     static_assert(NB <= 32 && D <= 3, "table packing: 5-bit slots, 2-bit fields");
     static_assert((D - 1) * NPE * NPD + D * NPE <= 1024 && NPD * NAD <= 8192, "K T table packing");
@@ -143,6 +156,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     uint8_t* CP = sb + L::bCP;
     uint8_t* CPI = sb + L::bCPI;
     uint16_t* S = reinterpret_cast<uint16_t*>(sb + L::bS);
+    uint8_t* NJ = sb + L::bNJ;
     const int tid = threadIdx.x;
     const uint32_t* pairs = p.pairs;
     const bool assemble = mode == MODE_ASSEMBLE, apply = mode == MODE_APPLY;
@@ -158,6 +172,7 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
     // compact front and most of the scatter stays in L2 even when the matrix is
     // many times larger than L2
     __shared__ int64_t s_next;
+    __shared__ int s_tq2;
     for (int64_t e = blockIdx.x; e < p.ne; e = s_next) {
         const int nb = p.nb[e];
         const double E = p.E[e];
@@ -319,6 +334,41 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             CP[rank] = (uint8_t)j;
             CPI[j] = (uint8_t)rank;
         }
+        if (L::kTQ2 && want_k && (tid >> 5) == 1) {
+            // tensor-product check of T (second warp): lane j finds the nodes of
+            // column j, their codes along x, y, z (0: left node only, 1: both,
+            // 2: right only) and checks the set and the weights
+            const int j = tid & 31;
+            bool ok = true;
+            unsigned code = 0u;
+            if (j < NB) {
+                unsigned mask = 0u;
+                for (int a = 0; a < NPE; ++a) {
+                    const long long tb = __double_as_longlong(T[a * NB + j]);
+                    if (tb != 0ll) {
+                        mask |= 1u << a;
+                        ok &= tb == 0x3FC0000000000000ll;  // 0.125
+                    }
+                }
+                // HEX8 nodes: x left {0,3,4,7}, right {1,2,5,6}; y left {0,1,4,5},
+                // right {2,3,6,7}; z left {0..3}, right {4..7}
+                const unsigned L3[3] = {0x99u, 0x33u, 0x0Fu}, R3[3] = {0x66u, 0xCCu, 0xF0u};
+                unsigned expect = 0xFFu;
+                int nat = 0, mul = 1;
+                for (int d = 0; d < 3; ++d) {
+                    const int c = (mask & L3[d]) ? ((mask & R3[d]) ? 1 : 0) : 2;
+                    expect &= c == 0 ? L3[d] : c == 2 ? R3[d] : 0xFFu;
+                    nat += c * mul;
+                    mul *= 3;
+                }
+                ok &= j < nb && mask != 0u && mask == expect;
+                code = 1u << nat;
+                if (ok) NJ[nat] = (uint8_t)j;
+            }
+            const unsigned all = __reduce_or_sync(0xffffffffu, code);
+            const bool allok = __all_sync(0xffffffffu, ok);
+            if (j == 0) s_tq2 = allok && all == (1u << 27) - 1u;
+        }
         if (need_u)  // on the last warp (the first one computes the count order)
             for (int r = tid - (NT - 32); r >= 0 && r < NPD; r += 32) {
                 const int f = r / NPE, a = r - f * NPE, cnt = NZJ[NPE * NB + a];
@@ -375,9 +425,11 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         }
         __syncthreads();
         // ---- phase 3: isotropic stiffness in pdof space, count-ordered data -------
+        const bool tq2 = L::kTQ2 && NW >= 2 && want_k && s_tq2;  // the check runs on the second warp
         {
-            // with a density field E(x_q) is already inside the Gram sums
-            const double escale = p.rho ? 1.0 : E;
+            // with a density field E(x_q) is already inside the Gram sums;
+            // tensor-product elements form K / 8 (K T = (K / 8) P)
+            const double escale = (p.rho ? 1.0 : E) * (tq2 ? 0.125 : 1.0);
             const double lam = escale * p.lam_c, mu = escale * p.mu_c;
             const double* G = p.rho ? A : p.g0;
             for (int k = tid; k < NSYM; k += NT) {
@@ -423,6 +475,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
             }
             TCP[sl] = (uint8_t)cnt;
         }
+        // natural basis code -> count-ordered slot (in place)
+        if (tq2 && tid < 27) NJ[tid] = CPI[NJ[tid]];
         if (scatter_k) {
             for (int x = tid; x < NAD; x += NT) {
                 const int sl = x / D, f = x - sl * D, i = CP[sl];
@@ -451,10 +505,37 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 for (int c = q; c < NPD; c += 4) s = fma(K[r * NPD + c], U[c], s);
                 s += __shfl_xor_sync(0xffffffffu, s, 1);
                 s += __shfl_xor_sync(0xffffffffu, s, 2);
-                if (q == 0) RP[r] = s;
+                if (q == 0) RP[r] = tq2 ? 8.0 * s : s;  // K / 8 on tensor-product elements (exact)
             }
         }
-        if (want_k) {
+        if (want_k && tq2) {
+            // KT[(f,a)][slot(j) D + g] = sum over the nodes b of basis j of
+            // (K/8)[(f,a),(g,b)]; thread (row r = (f,a), g, jy): the y stage for
+            // its jy, then x and z, nine outputs.  K is read as K[(g,b),(f,a)]
+            // (symmetric): the lanes take consecutive rows, consecutive words.
+            for (int t = tid; t < NPD * 9; t += NT) {
+                const int r = t % NPD, gj = t / NPD, gg = gj / 3, jy = gj - 3 * gg;
+                double w[2][2];  // [bx][bz]: the y stage
+#pragma unroll
+                for (int bz = 0; bz < 2; ++bz)
+#pragma unroll
+                    for (int bx = 0; bx < 2; ++bx) {
+                        // HEX8 node of (bx, by, bz): (0,0) 0, (1,0) 1, (1,1) 2, (0,1) 3 in a layer
+                        const int b0 = 4 * bz + (bx ? 1 : 0), b1 = 4 * bz + (bx ? 2 : 3);
+                        const double v0 = K[(gg * NPE + b0) * NPD + r], v1 = K[(gg * NPE + b1) * NPD + r];
+                        w[bx][bz] = jy == 0 ? v0 : jy == 2 ? v1 : v0 + v1;
+                    }
+#pragma unroll
+                for (int jx = 0; jx < 3; ++jx) {
+                    const double u0 = jx == 0 ? w[0][0] : jx == 2 ? w[1][0] : w[0][0] + w[1][0];
+                    const double u1 = jx == 0 ? w[0][1] : jx == 2 ? w[1][1] : w[0][1] + w[1][1];
+                    const int nat = jx + 3 * jy;
+                    KT[r * NAD + NJ[nat] * D + gg] = u0;
+                    KT[r * NAD + NJ[nat + 9] * D + gg] = u0 + u1;
+                    KT[r * NAD + NJ[nat + 18] * D + gg] = u1;
+                }
+            }
+        } else if (want_k) {
             // KT[(f,a)][x], x = slot * D + g: K symmetric, K[(f,a),(g,b)] is read
             // as K[(g,b),(f,a)], consecutive words along a
             uint32_t nxt = tid < L::NKT ? __ldg(p.ktab + tid) : 0u;

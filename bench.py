@@ -99,8 +99,10 @@ def flops_per_element(order=2, ngp=27, rect=True, density=False):
     is the SIMP path: E(x_q) = E0 rho(x_q)^beta per Gauss point, so the Gram
     matrix is summed per element over the points with those weights.
     Quadratic extraction is the tensor product of (1/2, 1/2, 0) / (0, 1/2, 1/2):
-    K T is formed as (K/8) P summed axis by axis, 19 additions per row of K and
-    column field (8 node values -> 27 bases)."""
+    K is formed as K/64, K T / 8 as (K/64) P summed axis by axis (19 additions
+    per row of K and column field, 8 node values -> 27 bases), and each entry
+    of T^T K T = P^T (K/64) P as a plain sum over the sparser column's nodes
+    (count - 1 additions)."""
     tc1, nzrow = {1: ([1, 1], 1), 2: ([1, 2, 1], 8)}[order]
     tc = [a * b * c for c in tc1 for b in tc1 for a in tc1]
     NGP, NPD, NB, D = ngp, 24, len(tc), 3
@@ -121,8 +123,14 @@ def flops_per_element(order=2, ngp=27, rect=True, density=False):
         kt = (D * (D + 1) // 2) * 8 * sum(tc) * 2             # K T over the T column nonzeros
     ka = 0                                                    # upper triangle of T^T (K T)
     nad = D * NB
-    for r in range(nad):
-        ka += tc[r % NB] * (nad - r) * 2
+    if order == 2:
+        # count-ordered adofs: the row holds the sparser column, count - 1 additions
+        srt = sorted(tc)
+        for x in range(nad):
+            ka += (srt[x // D] - 1) * (nad - x)
+    else:
+        for r in range(nad):
+            ka += tc[r % NB] * (nad - r) * 2
     return geo + gram + kiso + upd + resid + kt + ka
 
 

@@ -28,10 +28,11 @@
 // so T = 1/8 P with P the 0/1 pattern of nodes (x left/right) x (y) x (z).
 // When an element's T is exactly that (checked per element: every nonzero
 // 1/8, each column a tensor-product node set, all 27 present), K is formed
-// as K/8 (exact: a power of two) and K T = (K/8) P is summed axis by axis:
-// 8 node values -> 27 bases in three 2 -> 3 stages of additions (about 6 per
-// output group instead of the column-count FMAs); other elements take the
-// general path.
+// as K/64 (exact: a power of two), K T / 8 = (K/64) P is summed axis by axis
+// (8 node values -> 27 bases in three 2 -> 3 stages of additions) and
+// T^T K T = P^T ((K/64) P) is a plain sum over each column's nodes: count - 1
+// additions per entry instead of count FMAs.  Other elements take the general
+// path.
 #pragma once
 
 // E0-relative SIMP factor rho(x_q)^beta with rho interpolated from the nodal
@@ -56,6 +57,28 @@ __device__ __forceinline__ double fem_tdot_n(const double* w, const uint8_t* tn,
 #pragma unroll
     for (int k = 0; k < N; ++k) v = fma(w[k], base[tn[k] * stride], v);
     return v;
+}
+// sum of base[tn[k] * stride] over one column's nonzeros (columns whose
+// weights are all equal, the weight folded elsewhere): count - 1 additions
+template <int N>
+__device__ __forceinline__ double fem_tsum_n(const uint8_t* tn, const double* base, int stride) {
+    double v = base[tn[0] * stride];
+#pragma unroll
+    for (int k = 1; k < N; ++k) v += base[tn[k] * stride];
+    return v;
+}
+__device__ __forceinline__ double fem_tsum(int cnt, const uint8_t* tn, const double* base, int stride) {
+    switch (cnt) {
+        case 1: return fem_tsum_n<1>(tn, base, stride);
+        case 2: return fem_tsum_n<2>(tn, base, stride);
+        case 4: return fem_tsum_n<4>(tn, base, stride);
+        case 8: return fem_tsum_n<8>(tn, base, stride);
+        default: {
+            double v = 0.0;
+            for (int k = 0; k < cnt; ++k) v += base[tn[k] * stride];
+            return v;
+        }
+    }
 }
 __device__ __forceinline__ double fem_tdot(int cnt, const double* w, const uint8_t* tn, const double* base,
                                            int stride) {
@@ -428,8 +451,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
         const bool tq2 = L::kTQ2 && NW >= 2 && want_k && s_tq2;  // the check runs on the second warp
         {
             // with a density field E(x_q) is already inside the Gram sums;
-            // tensor-product elements form K / 8 (K T = (K / 8) P)
-            const double escale = (p.rho ? 1.0 : E) * (tq2 ? 0.125 : 1.0);
+            // tensor-product elements form K / 64 (T^T K T = P^T (K / 64) P)
+            const double escale = (p.rho ? 1.0 : E) * (tq2 ? 1.0 / 64.0 : 1.0);
             const double lam = escale * p.lam_c, mu = escale * p.mu_c;
             const double* G = p.rho ? A : p.g0;
             for (int k = tid; k < NSYM; k += NT) {
@@ -505,12 +528,12 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 for (int c = q; c < NPD; c += 4) s = fma(K[r * NPD + c], U[c], s);
                 s += __shfl_xor_sync(0xffffffffu, s, 1);
                 s += __shfl_xor_sync(0xffffffffu, s, 2);
-                if (q == 0) RP[r] = tq2 ? 8.0 * s : s;  // K / 8 on tensor-product elements (exact)
+                if (q == 0) RP[r] = tq2 ? 64.0 * s : s;  // K / 64 on tensor-product elements (exact)
             }
         }
         if (want_k && tq2) {
             // KT[(f,a)][slot(j) D + g] = sum over the nodes b of basis j of
-            // (K/8)[(f,a),(g,b)]; thread (row r = (f,a), g, jy): the y stage for
+            // (K/64)[(f,a),(g,b)]; thread (row r = (f,a), g, jy): the y stage for
             // its jy, then x and z, nine outputs.  K is read as K[(g,b),(f,a)]
             // (symmetric): the lanes take consecutive rows, consecutive words.
             for (int t = tid; t < NPD * 9; t += NT) {
@@ -575,7 +598,8 @@ __global__ void __launch_bounds__(32 * NW) bulk_cta_kernel(BulkArgs p, int mode)
                 const int cnt = TCP[sr];
                 if (cnt == 0) continue;  // padding (or all-zero) column: nothing to add
                 const int x = sr * D + f, y = sc * D + gg;
-                const double v = fem_tdot(cnt, TW + sr * NPE, TN + sr * NPE, KT + f * NPE * NAD + y, NAD);
+                const double v = tq2 ? fem_tsum(cnt, TN + sr * NPE, KT + f * NPE * NAD + y, NAD)
+                                     : fem_tdot(cnt, TW + sr * NPE, TN + sr * NPE, KT + f * NPE * NAD + y, NAD);
                 bad |= !fem_finite(v);
                 if (assemble) {
                     atomicAdd(p.vals + RG[x * D + gg] + S[sr * NB + sc], v);

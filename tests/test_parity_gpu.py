@@ -393,3 +393,49 @@ def test_zero_select_adds_nothing(torch):
     vo, ro = orc.assemble(u)
     assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL
     assert rel_err(rhs.cpu().numpy(), ro) <= RTOL
+
+
+def test_tensor_and_general_extraction_paths_match_oracle(torch):
+    """Uniform quadratic elements take the bulk kernel's tensor-product path
+    (T = P/8, checked per element); an element with a node whose extraction
+    weights differ, by 1e-3 or by one unit in the last place, takes the
+    column-list path.  Both kinds in one launch: element matrices, CSR values
+    and residual against the oracle with the same extraction."""
+    from oracle import OracleModel
+    dim, ne = 3, (4, 3, 3)
+    mesh = mg.hmr_uniform_mesh(dim, ne, [1.0] * dim, 2)
+    tw, off = mesh["t_w"].copy(), mesh["t_off"]
+    for n in range(0, len(off) - 1, 7):
+        tw[off[n]:off[n + 1]] *= 1.0 + 1e-3 * (1 + n % 5)
+    tw[off[3]] = np.nextafter(tw[off[3]], 1.0)
+    mesh = dict(mesh, t_w=tw)
+    nc = len(mesh["cells"])
+    touched = {n for n in range(0, len(off) - 1, 7)} | {3}
+    tensor_cells = [c for c in range(nc) if not touched & set(mesh["cells"][c].tolist())]
+    assert 0 < len(tensor_cells) < nc  # both paths present
+    E = 10.0 ** (-3.0 * uniform01(3, nc))
+    cells = np.arange(nc, dtype=np.int32)
+    prod = mg.FemModel(dim, mesh, mg.SHAPE_RECTANGULAR)
+    orc = OracleModel(dim, mg.CELL_HEX8, mg.SHAPE_RECTANGULAR, mesh)
+    prod.add_bulk_set(cells, E, 0.3, mg.RULE_HEX_3x3x3, mg.MODEL_3D)
+    orc.add_bulk_set(mg.CELL_HEX8, mg.RULE_HEX_3x3x3, mg.MODEL_3D, cells, E, 0.3)
+    prod.finalize()
+    orc.finalize()
+    rp, ci = prod.graph()
+    rpo, cio = orc.graph()
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    u = uniform01(6, prod.num_adofs) - 0.5
+    K, R = prod.element_matrices(0, 0, nc, u)
+    for eq in range(nc):
+        Ko, Ro = orc.element_matrices(0, eq, u)
+        n = len(Ro)
+        assert rel_err(K[eq, :n, :n], Ko) <= RTOL, eq
+        assert rel_err(R[eq, :n], Ro) <= RTOL, eq
+    vo, ro = orc.assemble(u, nthreads=4)
+    ut = torch.tensor(u, device="cuda")
+    vals = torch.empty(prod.nnz, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(prod.num_adofs, dtype=torch.float64, device="cuda")
+    prod.assemble(ut, vals, rhs)
+    torch.cuda.synchronize()
+    assert csr_row_rel_err(rp, vals.cpu().numpy(), vo) <= RTOL
+    assert rel_err(rhs.cpu().numpy(), ro) <= RTOL

@@ -81,6 +81,8 @@ struct SetData {
     DeviceBuf d_igoff, d_igx, d_igxi;            // cut clusters: integration cells
     DeviceBuf d_adjul;      // cut clusters: pdof values of u and lambda per cluster, cluster of each cell (sensitivities)
     DeviceBuf d_items;      // interface clusters: volume items (e * 2 + side, cell) of the sensitivities
+    DeviceBuf d_tperm;      // cut clusters: integration cells grouped by their number of moving vertices
+    int64_t tperm_off[5] = {0, 0, 0, 0, 0};  // group of cells with m moving vertices: [off[m-1], off[m]), m = 1..4
     int64_t nitems = 0;
     DeviceBuf d_fcoff, d_fcx, d_fcxl, d_fcxf;    // double-sided: facets
     DeviceBuf d_EF, d_vol;

@@ -217,7 +217,10 @@ __device__ void vertex_dual(const AdjArgs& A, int32_t v, int slot, Dual<M> x[3],
         x[d] = Dual<M>(A.vx[(int64_t)v * 3 + d]);
         if (moving) {
             const int32_t p0 = A.vpar[(int64_t)v * 8], p1 = A.vpar[(int64_t)v * 8 + 1];
-            x[d].d[slot] = A.vx[(int64_t)p1 * 3 + d] - A.vx[(int64_t)p0 * 3 + d];
+            const double dx = A.vx[(int64_t)p1 * 3 + d] - A.vx[(int64_t)p0 * 3 + d];
+            // slot chosen at run time: a select per slot keeps the dual in registers
+#pragma unroll
+            for (int i = 0; i < M; ++i) x[d].d[i] = i == slot ? dx : x[d].d[i];
         }
     }
 }
@@ -257,41 +260,48 @@ __global__ void adjoint_cluster_values(AdjArgs A, CutSetDev S, double* UL /*[neq
         UL[e * 48 + r] = monomial_coefficient(nod + (r / 24) * 24, S.xe + e * 24, r % 24);
 }
 
+// Cells with exactly M moving vertices (listed in `cells`): the moving
+// vertices take derivative slots 0..M-1 in vertex order; cells without a
+// moving vertex contribute nothing and are not listed.
+template <int M>
 __global__ void adjoint_tets_flat(AdjArgs A, CutSetDev S, const double* __restrict__ UL,
-                                  const int32_t* __restrict__ cell_cluster, int64_t ncells) {
-    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ncells;
-         g += (int64_t)gridDim.x * blockDim.x) {
+                                  const int32_t* __restrict__ cell_cluster, const int32_t* __restrict__ cells,
+                                  int64_t ncells) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncells;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = cells[i];
         const int64_t e = cell_cluster[g];
         const double* X = S.xe + e * 24;
         const double* U = UL + e * 48;
         const double* L = U + 24;
         const double xc[3] = {0.5 * (X[18] + X[0]), 0.5 * (X[19] + X[1]), 0.5 * (X[20] + X[2])};
         const double lam = S.E[e] * S.lam_c, mu = S.E[e] * S.mu_c;
-        Dual<4> Xv[4][3], xo[4][3];  // vertices, their offsets from the cell centre
+        Dual<M> Xv[4][3], xo[4][3];  // vertices, their offsets from the cell centre
         bool mv[4];
         int32_t vids[4];
+        int slot[4], next = 0;
         for (int k = 0; k < 4; ++k) {
             vids[k] = S.vid[g * 4 + k];
-            vertex_dual<4>(A, vids[k], k, Xv[k], mv[k]);
+            slot[k] = A.vkind[vids[k]] == 3 ? next++ : -1;
+            vertex_dual<M>(A, vids[k], slot[k], Xv[k], mv[k]);
             for (int d = 0; d < 3; ++d) xo[k][d] = (-xc[d]) + Xv[k][d];
         }
-        if (!(mv[0] || mv[1] || mv[2] || mv[3])) continue;
-        const Dual<4> detJ = tet_volume<4>(Xv);
-        Dual<4> F(0.0);
+        const Dual<M> detJ = tet_volume<M>(Xv);
+        Dual<M> F(0.0);
         for (int q = 0; q < S.ngp; ++q) {
             const double z0 = S.gp[q * 3], z1 = S.gp[q * 3 + 1], z2 = S.gp[q * 3 + 2];
             const double Nt[4] = {z0, z1, 1.0 - z0 - z1 - z2, z2};
-            Dual<4> xq[3];
+            Dual<M> xq[3];
             for (int d = 0; d < 3; ++d) {
-                xq[d] = Dual<4>(0.0);
+                xq[d] = Dual<M>(0.0);
                 for (int k = 0; k < 4; ++k) axpy(Nt[k], xo[k][d], xq[d]);
             }
-            const Dual<4> pr[3] = {xq[0] * xq[1], xq[1] * xq[2], xq[0] * xq[2]};
-            Dual<4> Gu[3][3], Gl[3][3], Su[3][3];
-            mono_field<4, false>(U, xq, pr, nullptr, Gu);
-            mono_field<4, false>(L, xq, pr, nullptr, Gl);
-            stress<4>(Gu, lam, mu, Su);
-            Dual<4> phi(0.0);
+            const Dual<M> pr[3] = {xq[0] * xq[1], xq[1] * xq[2], xq[0] * xq[2]};
+            Dual<M> Gu[3][3], Gl[3][3], Su[3][3];
+            mono_field<M, false>(U, xq, pr, nullptr, Gu);
+            mono_field<M, false>(L, xq, pr, nullptr, Gl);
+            stress<M>(Gu, lam, mu, Su);
+            Dual<M> phi(0.0);
             for (int i = 0; i < 3; ++i)
                 for (int j = 0; j < 3; ++j) phi = phi + Su[i][j] * (0.5 * Gu[i][j] + (-1.0) * Gl[i][j]);
             // skipped points (detJ < -1e-6) contribute nothing (cl_FEM_Element_Bulk.cpp:164)
@@ -299,7 +309,12 @@ __global__ void adjoint_tets_flat(AdjArgs A, CutSetDev S, const double* __restri
             axpy(S.gw[q], detJ * phi, F);
         }
         for (int k = 0; k < 4; ++k)
-            if (mv[k]) atomicAdd(A.G + vids[k], F.d[k]);
+            if (mv[k]) {
+                double dk = 0.0;
+#pragma unroll
+                for (int i2 = 0; i2 < M; ++i2) dk = i2 == slot[k] ? F.d[i2] : dk;
+                atomicAdd(A.G + vids[k], dk);
+            }
     }
 }
 
@@ -592,7 +607,9 @@ void sensitivity_release(fem_gpu_ctx* c) {
         dfree(s.d_link);
         dfree(s.d_adjul);
         dfree(s.d_items);
+        dfree(s.d_tperm);
         s.nitems = 0;
+        for (int64_t& o : s.tperm_off) o = 0;
     }
     c->adj_topo = c->adj_coords = false;
 }
@@ -798,11 +815,41 @@ fem_gpu_status fem_gpu_drdp_adjoint(fem_gpu_ctx* c, const double* u, const doubl
         }
         double* UL = (double*)s.d_adjul.p;
         int32_t* cc = reinterpret_cast<int32_t*>(UL + (size_t)d.neq * 48);
+        if (topo) {
+            // integration cells grouped by their number of moving (intersection)
+            // vertices, 1 to 4; cells without one are left out
+            std::vector<int32_t> cnt(ncells);
+            int64_t grp[5] = {0, 0, 0, 0, 0};
+            for (int64_t g = 0; g < ncells; ++g) {
+                int m = 0;
+                for (int k = 0; k < 4; ++k) m += c->vkind[s.vid[g * 4 + k]] == 3;
+                cnt[g] = m;
+                ++grp[m];
+            }
+            s.tperm_off[0] = 0;
+            for (int m = 1; m <= 4; ++m) s.tperm_off[m] = s.tperm_off[m - 1] + grp[m];
+            std::vector<int32_t> perm(std::max<int64_t>(s.tperm_off[4], 1));
+            int64_t pos[5] = {0, s.tperm_off[0], s.tperm_off[1], s.tperm_off[2], s.tperm_off[3]};
+            for (int64_t g = 0; g < ncells; ++g)
+                if (cnt[g] > 0) perm[pos[cnt[g]]++] = (int32_t)g;
+            if ((e = upload(s.d_tperm, perm, st)) != cudaSuccess) return sfail(c, e, "moving-vertex groups");
+        }
         adjoint_cluster_values<<<(unsigned)std::max<int64_t>(d.neq, 1), 64, 0, st>>>(A, d, UL, cc);
-        const unsigned grid =
-            (unsigned)std::max<int64_t>(1, std::min<int64_t>((ncells + 63) / 64, (int64_t)sm_count() * 16));
-        adjoint_tets_flat<<<grid, 64, 0, st>>>(A, d, UL, cc, ncells);
-        c->launches += 2;
+        c->launches++;
+        const int32_t* perm = (const int32_t*)s.d_tperm.p;
+        for (int m = 1; m <= 4; ++m) {
+            const int64_t a0 = s.tperm_off[m - 1], n = s.tperm_off[m] - a0;
+            if (n <= 0) continue;
+            const unsigned grid =
+                (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 63) / 64, (int64_t)sm_count() * 16));
+            switch (m) {
+                case 1: adjoint_tets_flat<1><<<grid, 64, 0, st>>>(A, d, UL, cc, perm + a0, n); break;
+                case 2: adjoint_tets_flat<2><<<grid, 64, 0, st>>>(A, d, UL, cc, perm + a0, n); break;
+                case 3: adjoint_tets_flat<3><<<grid, 64, 0, st>>>(A, d, UL, cc, perm + a0, n); break;
+                default: adjoint_tets_flat<4><<<grid, 64, 0, st>>>(A, d, UL, cc, perm + a0, n); break;
+            }
+            c->launches++;
+        }
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return sfail(c, e, "adjoint tets");
     if ((e = refresh(c->d_adjcuts, cuts, st)) != cudaSuccess) return sfail(c, e, "cut table");

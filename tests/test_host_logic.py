@@ -176,3 +176,30 @@ def test_model_without_equation_objects_is_rejected():
     with pytest.raises(mg.FemGpuError) as ei:
         m.finalize(host_only=True)
     assert ei.value.status == 1
+
+
+def test_level_set_field_is_validated_on_the_host():
+    """fem_gpu_set_level_set_field checks every coefficient id before it
+    touches the device, and fem_gen_dqdp refuses a table given by half or a
+    stored field of other sizes (the device pointers below are never read)."""
+    import ctypes
+    mesh = mg.hmr_uniform_mesh(3, (2, 2, 2), [1.0] * 3, 1)
+    m = mg.FemModel(3, mesh)
+    nodes, width, ncoef = len(mesh["coords"]), 8, 64
+    cols = (np.arange(nodes * width, dtype=np.int32) % ncoef).reshape(nodes, width)
+    vals = np.full((nodes, width), 0.125)
+    for bad in (ncoef, -1):
+        c2 = cols.copy()
+        c2[5, 3] = bad
+        with pytest.raises(mg.FemGpuError) as ei:
+            m.set_level_set_field(c2, vals, ncoef)
+        assert ei.value.args[0].startswith("fem_gpu status 2 ")  # FEM_GPU_OOB_INDEX
+    with pytest.raises(ValueError):
+        m.set_level_set_field(cols[:, :4], vals, ncoef)
+    with pytest.raises(ValueError):
+        m.gen_dqdp(None, None, None, ncoef, None)  # no field stored
+    lib = mg.lib()
+    dev = ctypes.c_void_p(256)
+    tw = vals.ctypes.data_as(ctypes.c_void_p)
+    assert lib.fem_gen_dqdp(m.h, dev, nodes, width, None, tw, ncoef, dev) == 1  # FEM_GPU_BAD_ARG
+    assert lib.fem_gen_dqdp(m.h, dev, nodes, width, None, None, ncoef, dev) == 1  # no vertex table, no field

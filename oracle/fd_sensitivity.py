@@ -66,13 +66,13 @@ def _cluster_index(sets, x):
     return cut_sets, iface
 
 
-def reference_fd_dfdt(orc, sets, x, u, lam, vertices, rel=1e-6, tol=1e-12):
-    """dF/dt_v for the given intersection vertices by the reference's FD scheme on
-    the oracle's cluster residuals (F = Q - lambda^T R; Q the bulk strain energy)."""
+def fd_index(sets, x):
+    """Lookups of the FD loop, built once (like the model): the cut sets and the
+    interface set, the clusters of every background cell, the background cells
+    whose clusters hold each IG vertex, and each background cell's bounds."""
     cut_sets, iface = _cluster_index(sets, x)
-    V = x["vertices"]
-    # background cell -> (cut set position, eq) per phase; interface eq per background cell
     bg = x["cell_background"]
+    # background cell -> (cut set position, eq) per phase; interface eq per background cell
     cut_of_cell = {}
     for pos, (si, a) in enumerate(cut_sets):
         for e, cell in enumerate(a["ip_cells"]):
@@ -81,6 +81,43 @@ def reference_fd_dfdt(orc, sets, x, u, lam, vertices, rel=1e-6, tol=1e-12):
     if iface is not None:
         for e, cell in enumerate(iface[1]["leader"]):
             if_of_cell[int(bg[cell])] = e
+    # (vertex, background cell) pairs of every integration cell and interface facet
+    pv, pc = [], []
+    for pos, (si, a) in enumerate(cut_sets):
+        offs = np.asarray(a["ig_offsets"])
+        e_of_row = np.repeat(np.arange(len(offs) - 1), np.diff(offs))
+        cell_of_row = bg[np.asarray(a["ip_cells"])[e_of_row]]
+        ids = np.asarray(a["ig_vertex_ids"]).reshape(len(e_of_row), -1)
+        pv.append(ids.ravel())
+        pc.append(np.repeat(cell_of_row, ids.shape[1]))
+    if iface is not None:
+        a = iface[1]
+        offs = np.asarray(a["offsets"])
+        e_of_row = np.repeat(np.arange(len(offs) - 1), np.diff(offs))
+        cell_of_row = bg[np.asarray(a["leader"])[e_of_row]]
+        ids = np.asarray(a["facet_vertex_ids"]).reshape(len(e_of_row), -1)
+        pv.append(ids.ravel())
+        pc.append(np.repeat(cell_of_row, ids.shape[1]))
+    pairs = np.unique(np.stack([np.concatenate(pv), np.concatenate(pc)], axis=1), axis=0) if pv else \
+        np.zeros((0, 2), dtype=np.int64)
+    nv = len(x["vertices"]["kind"])
+    vstart = np.searchsorted(pairs[:, 0], np.arange(nv + 1))
+    # bounds of a background cell: the first IP cell on it
+    cells_u, first = np.unique(bg, return_index=True)
+    X = x["mesh"]["coords"][x["mesh"]["cells"][first]]
+    bounds = {int(c): (X[k].min(axis=0), X[k].max(axis=0)) for k, c in enumerate(cells_u)}
+    return dict(cut_sets=cut_sets, iface=iface, cut_of_cell=cut_of_cell, if_of_cell=if_of_cell,
+                pair_cells=pairs[:, 1], vstart=vstart, bounds=bounds)
+
+
+def reference_fd_dfdt(orc, sets, x, u, lam, vertices, rel=1e-6, tol=1e-12, index=None):
+    """dF/dt_v for the given intersection vertices by the reference's FD scheme on
+    the oracle's cluster residuals (F = Q - lambda^T R; Q the bulk strain energy).
+    `index`: the lookups of fd_index (built here when not given)."""
+    ix = fd_index(sets, x) if index is None else index
+    cut_sets, iface = ix["cut_sets"], ix["iface"]
+    cut_of_cell, if_of_cell = ix["cut_of_cell"], ix["if_of_cell"]
+    V = x["vertices"]
 
     def cut_arrays(pos, e):
         si, a = cut_sets[pos]
@@ -104,32 +141,17 @@ def reference_fd_dfdt(orc, sets, x, u, lam, vertices, rel=1e-6, tol=1e-12):
             return -float(lam[ids] @ R)
         return float((0.5 * u[ids] - lam[ids]) @ R)
 
-    def cell_bounds(cell):
-        X = x["mesh"]["coords"][x["mesh"]["cells"][cell]]
-        return X.min(axis=0), X.max(axis=0)
-
     out = np.zeros(len(vertices))
     for iv, v in enumerate(vertices):
         p0, p1 = V["parents"][v, 0], V["parents"][v, 1]
         dxdt = V["coords"][p1] - V["coords"][p0]
         xv = V["coords"][v]
         # background cells whose clusters contain v
-        cells = set()
-        for pos, (si, a) in enumerate(cut_sets):
-            hit = np.nonzero(np.any(a["ig_vertex_ids"] == v, axis=1))[0]
-            offs = a["ig_offsets"]
-            for g in hit:
-                e = int(np.searchsorted(offs, g, side="right") - 1)
-                cells.add(int(bg[a["ip_cells"][e]]))
-        if iface is not None:
-            hit = np.nonzero(np.any(iface[1]["facet_vertex_ids"] == v, axis=1))[0]
-            offs = iface[1]["offsets"]
-            for f in hit:
-                e = int(np.searchsorted(offs, f, side="right") - 1)
-                cells.add(int(bg[iface[1]["leader"][e]]))
+        cells = ix["pair_cells"][ix["vstart"][v]:ix["vstart"][v + 1]]
         g = np.zeros(3)
         for cell in cells:
-            lo, hi = cell_bounds(np.nonzero(bg == cell)[0][0])
+            cell = int(cell)
+            lo, hi = ix["bounds"][cell]
             members = cut_of_cell.get(cell, [])
             ie = if_of_cell.get(cell)
             base = {}

@@ -31,6 +31,37 @@ def test_edge_coordinates_reproduce_the_decomposition():
     assert np.max(np.abs(t[k] - c["x"]["vertices"]["value"][k])) < 1e-14
 
 
+def test_fd_index_finds_every_cluster_of_a_vertex():
+    """The FD loop's prebuilt lookups (fd_index) against a scan of every
+    integration cell and interface facet: for each IG vertex the background
+    cells of the clusters that hold it, and each cell's bounds."""
+    from oracle.fd_sensitivity import _cluster_index, fd_index
+    c = S.build(n=8, ncoef=12, finalize=False)
+    x, sets = c["x"], c["sets"]
+    ix = fd_index(sets, x)
+    bg = x["cell_background"]
+    cut_sets, iface = _cluster_index(sets, x)
+    want = {}
+    for _, a in cut_sets:
+        offs = a["ig_offsets"]
+        for e in range(len(offs) - 1):
+            for v in np.asarray(a["ig_vertex_ids"])[offs[e]:offs[e + 1]].ravel():
+                want.setdefault(int(v), set()).add(int(bg[a["ip_cells"][e]]))
+    if iface is not None:
+        a = iface[1]
+        offs = a["offsets"]
+        for e in range(len(offs) - 1):
+            for v in np.asarray(a["facet_vertex_ids"])[offs[e]:offs[e + 1]].ravel():
+                want.setdefault(int(v), set()).add(int(bg[a["leader"][e]]))
+    nv = len(x["vertices"]["kind"])
+    for v in range(nv):
+        got = set(int(cc) for cc in ix["pair_cells"][ix["vstart"][v]:ix["vstart"][v + 1]])
+        assert got == want.get(v, set()), v
+    for cell, (lo, hi) in ix["bounds"].items():
+        X = x["mesh"]["coords"][x["mesh"]["cells"][np.nonzero(bg == cell)[0][0]]]
+        assert np.array_equal(lo, X.min(axis=0)) and np.array_equal(hi, X.max(axis=0))
+
+
 def oracle_of(c):
     return oracle_model(c["x"], c["sets"])
 
